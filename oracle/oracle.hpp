@@ -1,0 +1,178 @@
+// Typhon CPU oracle — TEST INFRASTRUCTURE ONLY.
+//
+// A literal C++ restatement of the Fortran routines of Typhon (Haider-BA/typhon)
+// on the unstructured finite-volume residual-and-update path.  It exists to
+// check the GPU library: only tests/, __graft_entry__.smoke() and the CPU leg
+// of bench.py may build, load or run it, and never as the thing measured or
+// shipped.  Every function cites the Fortran file:line it restates; the loop
+// and summation orders follow the Fortran so that results can be compared
+// bit for bit where the GPU path runs in its exact mode.
+//
+// Parity pin: the oracle reproduces the golden monitor files of Typhon's own
+// non-regression suite (NRG/TIME/RUNGEKUTTA/*/RHOERR.tmon,
+// NRG/MESH/CON/PER2D-TRANS/RHODEV.tmon) to their printed precision; see
+// tests/test_oracle_golden.py.
+//
+// Indices are 0-based here.  Ghost cells are numbered after the interior
+// cells, in the order Typhon assigns them (init_connect_grid.f90).
+#pragma once
+#include <cmath>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace ory {
+
+struct V3 {
+  double x = 0, y = 0, z = 0;
+};
+inline V3 v3(double a, double b, double c) { V3 v; v.x = a; v.y = b; v.z = c; return v; }
+inline V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 operator-(V3 a) { return v3(-a.x, -a.y, -a.z); }
+inline V3 operator*(double s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+inline V3 operator/(V3 a, double s) { return v3(a.x / s, a.y / s, a.z / s); }
+// v3d_scalar_product (CFDTOOLS/Math/VEC3D.f90:555-561)
+inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// v3d_sqrnorme (VEC3D.f90:529-535)
+inline double sqrabs(V3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+// v3d_norme (VEC3D.f90:503-509)
+inline double vabs(V3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+// v3d_vectorial_product (VEC3D.f90:583-591)
+inline V3 cross(V3 a, V3 b) {
+  return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+// Element type codes of CFDTOOLS/Mesh/ELEMVTEX.f90:17-37.
+enum ElemType {
+  ELEM_BAR2 = 2, ELEM_TRI3 = 13, ELEM_QUAD4 = 24, ELEM_TETRA4 = 101,
+  ELEM_PYRA5 = 121, ELEM_PENTA6 = 131, ELEM_HEXA8 = 141
+};
+int elem_dim(int type);
+int elem_nvtex(int type);
+
+struct ElemSection {
+  int type = 0;
+  std::vector<int> ielem;  // element numbers (1-based, as stored in the file)
+  std::vector<int> vtex;   // nelem * nv vertex numbers (1-based)
+  int nv() const { return elem_nvtex(type); }
+  int nelem() const { return (int)ielem.size(); }
+};
+
+struct Mark {
+  std::string family;
+  std::vector<int> tags;  // element numbers of boundary face elements
+};
+
+// Content of a Typhon .tym mesh (TYFMT_MESH.f90 reader) or of a generator.
+struct RawMesh {
+  std::vector<V3> vtex;
+  std::vector<ElemSection> sections;  // cell and face element sections in file order
+  std::vector<Mark> marks;
+};
+
+bool read_tym(const std::string& path, RawMesh& out, std::string& err);
+
+// Boundary families and how the solver treats them.
+enum BcKind { BC_PERIODIC = 1, BC_SYMMETRY = 2, BC_WALL = 3 };
+struct BcDef {
+  std::string family;   // family name as in the mesh marks
+  int kind = 0;
+  // periodic: partner family and the translation from this family to the partner
+  std::string partner;
+  V3 translation;
+  // wall: wall velocity
+  V3 wall_velocity;
+};
+
+struct Boco {
+  std::string family;
+  std::vector<int> iface;  // mesh faces of the family (0-based), in mark order
+  int kind = 0;
+  int def = -1;            // index into the BcDef list
+  double rlink = 0;        // +1 for FAMILY1 side, -1 for FAMILY2 side
+  std::vector<int> partner_face;  // periodic: partner face of each face
+  V3 wall_velocity;
+};
+
+// Preprocessed mesh in Typhon's numbering (st_ustmesh).
+struct UMesh {
+  int dim = 2;        // geometric dimension (2: COORD=2D, 3: 3D)
+  int ncell_int = 0, ncell = 0, nface_int = 0, nface = 0, nface_lim = 0;
+  std::vector<int> fc1, fc2;        // face -> cells (fc2 is a ghost index for boundary faces)
+  std::vector<std::vector<int>> facevtex;
+  std::vector<V3> fnormal, fcentre;
+  std::vector<double> fsurf;
+  std::vector<V3> ccentre;          // ncell (ghosts included once connections are set)
+  std::vector<double> cvol;
+  std::vector<std::vector<int>> colors;  // coo_colorgroup: faces of each colour, ascending
+  std::vector<Boco> bocos;
+};
+
+// create_face_connect + calc_ustmesh + grid_postproc + init_connect_grid.
+bool build_umesh(const RawMesh& raw, int geo_dim, const std::vector<BcDef>& bcs, UMesh& m,
+                 std::string& err);
+
+// ---------------------------------------------------------------------------
+// Solver
+enum Scheme { SCH_HLLC = 1, SCH_RUSANOV = 2, SCH_ROE = 3, SCH_HLLCK = 4 };
+enum HighRes { HRES_NONE = 0, HRES_MUSCL = 1, HRES_MUSCLFAST = 2, HRES_MUSCLUNS = 3 };
+enum Limiter { LIM_NONE = 0, LIM_MINMOD = 1, LIM_ALBADA = 2, LIM_VLEER = 3, LIM_SBEE = 4,
+               LIM_KIM3 = 5, LIM_LIM03 = 6 };
+enum PostLim { POSTLIM_NONE = 0, POSTLIM_BARTH = 1, POSTLIM_SUPERBARTH = 2 };
+enum GradMeth { GRAD_NONE = 0, GRAD_LSQ = 1, GRAD_LSQW = 2 };
+enum RkMethod { RK2 = 1, RK2SSP = 2, RK3SSP = 3, RK4 = 4, LSRK25BB = 5, LSRK26BB = 6,
+                LSRK12BS = 7, LSRK13BS = 8 };
+
+struct SpatParams {
+  int scheme = SCH_HLLC;
+  int highres = HRES_NONE;
+  int limiter = LIM_ALBADA;
+  int postlim = POSTLIM_NONE;
+  int gradmeth = GRAD_NONE;
+  double gamma = 1.4;
+  double roe_entropy_fix = 0.1;  // Harten fix width (fraction of local sound speed), Roe only
+};
+
+struct RkTable {
+  int nstage = 0;
+  std::vector<double> coef;  // nstage x nstage, row-major: coef[(i-1)*n + (j-1)] = coef(i,j)
+  double c(int i, int j) const { return coef[(i - 1) * nstage + (j - 1)]; }
+};
+RkTable rk_table(int method);
+
+// Field layout: [var][cell], var 0=rho, 1=p or rhoE, 2..4 = vector components.
+struct Solver {
+  const UMesh* m = nullptr;
+  SpatParams sp;
+  RkTable rk;
+  double cfl = 1.0;
+  std::vector<double> cons, prim;      // 5*ncell
+  std::vector<double> grad;            // 15*ncell: grad rho (3), grad p (3), du_i/dx_j (9, row i)
+  std::vector<double> cell_l, cell_r;  // 5*nface
+  std::vector<double> flux;            // 5*nface
+  std::vector<double> residu;          // 5*ncell
+  std::vector<double> dtloc;           // ncell
+  std::vector<double> gradcond;        // 9*ncell_int, Cholesky factors (column-major 3x3)
+  bool gradcond_ok = false;
+  std::vector<double> limratio;        // 3*ncell: Barth ratios of the last stage (rho, p, vector)
+  double cur_res = 0;
+
+  void init(const UMesh* mesh, const SpatParams& p, int rk_method, double cfl_);
+  void varprim();
+  void varcons();
+  void boco_cell_state();
+  void boco_cell_grad();
+  void boco_face_state();
+  void precalc_grad_lsq();
+  void calc_gradient();
+  void hres_states();
+  void postlimit_barth(double klim);
+  void face_fluxes();
+  void flux_to_res();
+  void calc_rhs();               // one residual evaluation at dtloc
+  double timestep();             // stab_cond: global min dt over interior cells
+  void rk_step(double dt);       // treelevel_rungekutta + update_field
+};
+
+}  // namespace ory

@@ -1,0 +1,271 @@
+// Typhon CPU oracle — C entry points for the tests (ctypes).  TEST INFRASTRUCTURE ONLY.
+//
+// Also holds the drivers of Typhon's own non-regression cases whose meshes are readable
+// here (.tym): the cycle loop of SOURCE/MAIN/integration.f90:59-142 and
+// SOURCE/MAIN/integration_cyclezone.f90:80-170 (unsteady, global time step), and the
+// volume-average probes of CFDTOOLS/Mesh/PROBECALC.f90:66-90 written by
+// SOURCE/MAIN/write_monitors_cycle.f90:40-67 after calc_varprim.
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "oracle.hpp"
+
+using namespace ory;
+
+namespace {
+struct MeshHandle {
+  RawMesh raw;
+  UMesh m;
+};
+void set_err(char* buf, int len, const std::string& s) {
+  if (buf && len > 0) {
+    std::strncpy(buf, s.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
+  }
+}
+std::vector<BcDef> make_bcs(int nbc, const char* const* fam, const int* kind, const char* const* partner,
+                            const double* trans, const double* wallvel) {
+  std::vector<BcDef> bcs(nbc);
+  for (int i = 0; i < nbc; ++i) {
+    bcs[i].family = fam[i];
+    bcs[i].kind = kind[i];
+    if (partner && partner[i]) bcs[i].partner = partner[i];
+    if (trans) bcs[i].translation = v3(trans[3 * i], trans[3 * i + 1], trans[3 * i + 2]);
+    if (wallvel) bcs[i].wall_velocity = v3(wallvel[3 * i], wallvel[3 * i + 1], wallvel[3 * i + 2]);
+  }
+  return bcs;
+}
+}  // namespace
+
+extern "C" {
+
+// ---- raw meshes ----
+void* ory_raw_new() { return new MeshHandle(); }
+void ory_raw_free(void* h) { delete (MeshHandle*)h; }
+int ory_raw_read_tym(void* h, const char* path, char* err, int errlen) {
+  std::string e;
+  if (!read_tym(path, ((MeshHandle*)h)->raw, e)) { set_err(err, errlen, e); return -1; }
+  return 0;
+}
+void ory_raw_set_vtex(void* h, int n, const double* xyz) {
+  auto& r = ((MeshHandle*)h)->raw;
+  r.vtex.resize(n);
+  for (int i = 0; i < n; ++i) r.vtex[i] = v3(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+}
+void ory_raw_add_section(void* h, int type, int nelem, const int* ielem, const int* vtex) {
+  ElemSection s;
+  s.type = type;
+  s.ielem.assign(ielem, ielem + nelem);
+  s.vtex.assign(vtex, vtex + (size_t)nelem * elem_nvtex(type));
+  ((MeshHandle*)h)->raw.sections.push_back(std::move(s));
+}
+void ory_raw_add_mark(void* h, const char* name, int ntag, const int* tags) {
+  Mark mk;
+  mk.family = name;
+  mk.tags.assign(tags, tags + ntag);
+  ((MeshHandle*)h)->raw.marks.push_back(std::move(mk));
+}
+int ory_raw_counts(void* h, int* out) {  // nvtex, nsections, nmarks
+  auto& r = ((MeshHandle*)h)->raw;
+  out[0] = (int)r.vtex.size();
+  out[1] = (int)r.sections.size();
+  out[2] = (int)r.marks.size();
+  return 0;
+}
+
+// ---- preprocessing ----
+int ory_mesh_build(void* h, int geo_dim, int nbc, const char* const* fam, const int* kind,
+                   const char* const* partner, const double* trans, const double* wallvel, char* err,
+                   int errlen) {
+  auto* mh = (MeshHandle*)h;
+  std::string e;
+  if (!build_umesh(mh->raw, geo_dim, make_bcs(nbc, fam, kind, partner, trans, wallvel), mh->m, e)) {
+    set_err(err, errlen, e);
+    return -1;
+  }
+  return 0;
+}
+// sizes: ncell_int, ncell, nface_int, nface, ncolors, dim, nboco
+void ory_mesh_sizes(void* h, int* out) {
+  auto& m = ((MeshHandle*)h)->m;
+  out[0] = m.ncell_int; out[1] = m.ncell; out[2] = m.nface_int; out[3] = m.nface;
+  out[4] = (int)m.colors.size(); out[5] = m.dim; out[6] = (int)m.bocos.size();
+}
+// Export Typhon's preprocessed arrays (0-based).  face_color: colour of each face;
+// face_partner: periodic partner face (-1 otherwise); face_bckind: 0 interior, else BcKind.
+void ory_mesh_export(void* h, int* fc1, int* fc2, double* fnormal, double* fcentre, double* fsurf,
+                     double* ccentre, double* cvol, int* face_color, int* face_partner, int* face_bckind,
+                     double* face_wallvel) {
+  auto& m = ((MeshHandle*)h)->m;
+  for (int f = 0; f < m.nface; ++f) {
+    fc1[f] = m.fc1[f]; fc2[f] = m.fc2[f];
+    fnormal[3 * f] = m.fnormal[f].x; fnormal[3 * f + 1] = m.fnormal[f].y; fnormal[3 * f + 2] = m.fnormal[f].z;
+    fcentre[3 * f] = m.fcentre[f].x; fcentre[3 * f + 1] = m.fcentre[f].y; fcentre[3 * f + 2] = m.fcentre[f].z;
+    fsurf[f] = m.fsurf[f];
+    face_partner[f] = -1;
+    face_bckind[f] = 0;
+    face_wallvel[3 * f] = face_wallvel[3 * f + 1] = face_wallvel[3 * f + 2] = 0.0;
+  }
+  for (int c = 0; c < m.ncell; ++c) {
+    ccentre[3 * c] = m.ccentre[c].x; ccentre[3 * c + 1] = m.ccentre[c].y; ccentre[3 * c + 2] = m.ccentre[c].z;
+    cvol[c] = m.cvol[c];
+  }
+  for (size_t ic = 0; ic < m.colors.size(); ++ic)
+    for (int f : m.colors[ic]) face_color[f] = (int)ic;
+  for (auto& b : m.bocos)
+    for (size_t k = 0; k < b.iface.size(); ++k) {
+      int f = b.iface[k];
+      face_bckind[f] = b.kind;
+      if (b.kind == BC_PERIODIC) face_partner[f] = b.partner_face[k];
+      face_wallvel[3 * f] = b.wall_velocity.x;
+      face_wallvel[3 * f + 1] = b.wall_velocity.y;
+      face_wallvel[3 * f + 2] = b.wall_velocity.z;
+    }
+}
+void ory_mesh_facevtex(void* h, int maxv, int* out) {  // nface x maxv, 1-based vertices, 0 pad
+  auto& m = ((MeshHandle*)h)->m;
+  for (int f = 0; f < m.nface; ++f)
+    for (int k = 0; k < maxv; ++k) out[f * maxv + k] = k < (int)m.facevtex[f].size() ? m.facevtex[f][k] : 0;
+}
+
+// ---- solver ----
+// iparams: scheme, highres, limiter, postlim, gradmeth, rk_method
+// dparams: gamma, cfl, roe_entropy_fix
+void* ory_solver_new(void* mesh, const int* ip, const double* dp) {
+  auto* s = new Solver();
+  SpatParams sp;
+  sp.scheme = ip[0]; sp.highres = ip[1]; sp.limiter = ip[2]; sp.postlim = ip[3]; sp.gradmeth = ip[4];
+  sp.gamma = dp[0];
+  sp.roe_entropy_fix = dp[2];
+  s->init(&((MeshHandle*)mesh)->m, sp, ip[5], dp[1]);
+  return s;
+}
+void ory_solver_free(void* s) { delete (Solver*)s; }
+void ory_solver_set_cons(void* s, const double* c) {
+  auto* S = (Solver*)s;
+  std::memcpy(S->cons.data(), c, S->cons.size() * sizeof(double));
+}
+void ory_solver_set_prim(void* s, const double* p) {
+  auto* S = (Solver*)s;
+  std::memcpy(S->prim.data(), p, S->prim.size() * sizeof(double));
+  S->varcons();
+}
+// which: 0 cons, 1 prim, 2 grad, 3 residu, 4 flux, 5 cell_l, 6 cell_r, 7 dtloc, 8 limratio
+int ory_solver_get(void* s, int which, double* out) {
+  auto* S = (Solver*)s;
+  const std::vector<double>* v = nullptr;
+  switch (which) {
+    case 0: v = &S->cons; break;
+    case 1: v = &S->prim; break;
+    case 2: v = &S->grad; break;
+    case 3: v = &S->residu; break;
+    case 4: v = &S->flux; break;
+    case 5: v = &S->cell_l; break;
+    case 6: v = &S->cell_r; break;
+    case 7: v = &S->dtloc; break;
+    case 8: v = &S->limratio; break;
+    default: return -1;
+  }
+  std::memcpy(out, v->data(), v->size() * sizeof(double));
+  return (int)v->size();
+}
+double ory_solver_timestep(void* s) { return ((Solver*)s)->timestep(); }
+// one residual evaluation with a uniform dtloc = dt (calc_rhs)
+void ory_solver_rhs(void* s, double dt) {
+  auto* S = (Solver*)s;
+  std::fill(S->dtloc.begin(), S->dtloc.end(), dt);
+  S->calc_rhs();
+}
+void ory_solver_rk_step(void* s, double dt) { ((Solver*)s)->rk_step(dt); }
+// n explicit steps with the global stability time step; dts receives each dt (may be null)
+int ory_solver_run_steps(void* s, int n, double* dts) {
+  auto* S = (Solver*)s;
+  for (int i = 0; i < n; ++i) {
+    double dt = S->timestep();
+    if (!(dt > 0.0)) return -1;
+    if (dts) dts[i] = dt;
+    S->rk_step(dt);
+  }
+  return 0;
+}
+
+// ---- Typhon non-regression cases with .tym meshes ----
+// case 1: NRG/TIME/RUNGEKUTTA/<method>  (HLLC, MUSCL-FAST, van Albada, periodic),
+//         probe RHOERR = vol-avg (rho - rho_exact(x - 50 t, y))^2
+// case 2: NRG/MESH/CON/PER2D-TRANS     (Rusanov, first order, periodic),
+//         probe RHODEV = vol-avg (rho - 1.25)^2
+// Writes ncycle probe values into out; returns the number of time steps taken, < 0 on error.
+int ory_run_nrg(int which, void* mesh, int rk_method, double cfl, int ncycle, double duration, double* out) {
+  auto& m = ((MeshHandle*)mesh)->m;
+  Solver S;
+  SpatParams sp;
+  if (which == 1) {
+    sp.scheme = SCH_HLLC; sp.highres = HRES_MUSCLFAST; sp.limiter = LIM_ALBADA; sp.gradmeth = GRAD_LSQ;
+  } else if (which == 2) {
+    sp.scheme = SCH_RUSANOV; sp.highres = HRES_NONE; sp.gradmeth = GRAD_NONE;
+  } else {
+    return -1;
+  }
+  S.init(&m, sp, rk_method, cfl);
+  const double pi = 3.14159265358979323846;
+  const int nc = m.ncell;
+  for (int c = 0; c < nc; ++c) {  // BLOCK:INIT at cell centres, ghosts included (init_ns_ust.f90)
+    double x = m.ccentre[c].x, y = m.ccentre[c].y;
+    double rho, vx;
+    if (which == 1) {
+      double s = std::sin(2 * pi * x) * std::sin(2 * pi * y);
+      rho = 1 + (s * s) / 2;
+      vx = 50.;
+    } else {
+      rho = 1. + 9 * x * (x - 1) * y * (y - 1);
+      vx = 10.;
+    }
+    S.prim[c] = rho;
+    S.prim[nc + c] = 100000 / 14.;
+    S.prim[2 * nc + c] = vx;
+    S.prim[3 * nc + c] = 0.;
+    S.prim[4 * nc + c] = 0.;
+  }
+  S.varcons();
+  const double dtbase = duration / ncycle;
+  double curtps = 0.0;
+  int nsteps = 0;
+  for (int icycle = 1; icycle <= ncycle; ++icycle) {
+    double cycle_time = 0.0;
+    bool end_cycle = false;
+    while (!end_cycle) {
+      double dtmax = dtbase - cycle_time;
+      double dt = S.timestep();
+      if (!(dt > 0.0)) return -2;
+      dt = std::min(dt, dtmax);
+      if (dt >= dtbase - cycle_time) { end_cycle = true; dt = dtbase - cycle_time; }
+      S.rk_step(dt);
+      cycle_time = cycle_time + dt;
+      ++nsteps;
+    }
+    curtps = curtps + dtbase;
+    S.varprim();
+    double num = 0.0, vol = 0.0;
+    for (int c = 0; c < m.ncell_int; ++c) {
+      double q;
+      if (which == 1) {
+        double x = m.ccentre[c].x, y = m.ccentre[c].y;
+        double s = std::sin(2 * pi * (x - 50 * curtps)) * std::sin(2 * pi * y);
+        double e = S.prim[c] - (1 + (s * s) / 2);
+        q = e * e;
+      } else {
+        double e = S.prim[c] - 1.25;
+        q = e * e;
+      }
+      num += q * m.cvol[c];
+      vol += m.cvol[c];
+    }
+    out[icycle - 1] = num / vol;
+  }
+  return nsteps;
+}
+
+}  // extern "C"

@@ -1,0 +1,714 @@
+// Typhon CPU oracle — explicit Euler path.  TEST INFRASTRUCTURE ONLY (see oracle.hpp).
+//
+// Each routine restates one Typhon routine in its loop and summation order:
+//   varprim          SOURCE/EQNS/calc_varprim_ns.f90:37-57
+//   varcons          SOURCE/EQNS/calc_varcons_ns.f90:30-48
+//   boco_*           SOURCE/MGRID/calcboco_gen.f90:40-88, calcboco_connect_per_match.f90:45-84,
+//                    SOURCE/MGRID/calcboco_ust_sym.f90 (symmetry), calcboco_ust.f90
+//   precalc_grad_lsq SOURCE/MGRID/precalc_grad_lsq.f90:43-159, SOURCE/MATH/MATRIX.f90:42-70
+//   calc_gradient    SOURCE/MGRID/calc_gradient.f90:67-196, MATRIX.f90:79-111
+//   hres_states      SOURCE/MAIN/calc_hres_states.f90:55-119, SOURCE/EQNS/hres_ns_muscl*.f90,
+//                    SOURCE/EQNS/tvdgrad{str,fst,uns}_{scal,vect}.f90, SOURCE/MGRID/LIMITER.f90
+//   postlimit_barth  SOURCE/MGRID/postlimit_barth.f90:42-223
+//   face_fluxes      SOURCE/EQNS/calc_flux_hllc.f90:61-171, calc_roe_states.f90:35-53,
+//                    calc_flux_rusanov.f90:57-83; Roe: new (no Typhon implementation)
+//   flux_to_res      SOURCE/MAIN/flux_to_res.f90:47-144
+//   timestep         SOURCE/EQNS/calc_ns_timestep.f90:52-103, SOURCE/ZONE/calc_zonetimestep.f90:54-126
+//   rk_step          SOURCE/MAIN/treelevel_rungekutta.f90:48-113, SOURCE/ZONE/update_field.f90:33-71,
+//                    SOURCE/PARAM/MENU_NUM.f90:368-449
+#include <algorithm>
+#include <cmath>
+#include <limits>
+
+#include "oracle.hpp"
+
+namespace ory {
+
+RkTable rk_table(int method) {
+  RkTable t;
+  auto set = [&](int n, std::initializer_list<std::initializer_list<double>> rows) {
+    t.nstage = n;
+    t.coef.assign((size_t)n * n, 0.0);
+    int i = 0;
+    for (auto& r : rows) {
+      int j = 0;
+      for (double v : r) t.coef[(size_t)i * n + j++] = v;
+      ++i;
+    }
+  };
+  switch (method) {
+    case RK2: set(2, {{.5}, {0., 1.}}); break;
+    case RK2SSP: set(2, {{1.}, {.5, .5}}); break;
+    case RK3SSP: set(3, {{1.}, {.25, .25}, {1. / 6., 1. / 6., 4. / 6.}}); break;
+    case RK4: set(4, {{.5}, {0., .5}, {0., 0., 1.}, {1. / 6., 2. / 6., 2. / 6., 1. / 6.}}); break;
+    case LSRK25BB:
+      set(5, {{0.1815754863270908}, {0., 0.238260222208392}, {0., 0., 0.330500707328},
+              {0., 0., 0., 0.5}, {0., 0., 0., 0., 1.}});
+      break;
+    case LSRK26BB:
+      set(6, {{0.11797990162882}, {0., 0.18464696649448}, {0., 0., 0.24662360430959},
+              {0., 0., 0., 0.33183954253762}, {0., 0., 0., 0., 0.5}, {0., 0., 0., 0., 0., 1.}});
+      break;
+    case LSRK12BS: set(2, {{1.}, {0., 1.}}); break;
+    case LSRK13BS: set(3, {{.15}, {0., .4}, {0., 0., 1.}}); break;
+    default: break;
+  }
+  return t;
+}
+
+void Solver::init(const UMesh* mesh, const SpatParams& p, int rk_method, double cfl_) {
+  m = mesh;
+  sp = p;
+  rk = rk_table(rk_method);
+  cfl = cfl_;
+  const size_t nc = m->ncell, nf = m->nface;
+  cons.assign(5 * nc, 0.0);
+  prim.assign(5 * nc, 0.0);
+  grad.assign(15 * nc, 0.0);
+  cell_l.assign(5 * nf, 0.0);
+  cell_r.assign(5 * nf, 0.0);
+  flux.assign(5 * nf, 0.0);
+  residu.assign(5 * nc, 0.0);
+  dtloc.assign(nc, 0.0);
+  limratio.assign(3 * nc, 1.0);
+  gradcond_ok = false;
+}
+
+// calc_varprim_ns.f90:43-54, over all cells (ghosts too)
+void Solver::varprim() {
+  const int nc = m->ncell;
+  const double g1 = sp.gamma - 1.0;
+  for (int i = 0; i < nc; ++i) {
+    double rho = cons[i];
+    V3 vel = v3(cons[2 * nc + i], cons[3 * nc + i], cons[4 * nc + i]) / rho;
+    double ec = 0.5 * rho * sqrabs(vel);
+    prim[i] = rho;
+    prim[nc + i] = g1 * (cons[nc + i] - ec);
+    prim[2 * nc + i] = vel.x;
+    prim[3 * nc + i] = vel.y;
+    prim[4 * nc + i] = vel.z;
+  }
+}
+
+// calc_varcons_ns.f90:37-46
+void Solver::varcons() {
+  const int nc = m->ncell;
+  const double ig1 = 1.0 / (sp.gamma - 1.0);
+  for (int i = 0; i < nc; ++i) {
+    double rho = prim[i];
+    V3 vel = v3(prim[2 * nc + i], prim[3 * nc + i], prim[4 * nc + i]);
+    cons[i] = rho;
+    cons[nc + i] = ig1 * prim[nc + i] + 0.5 * rho * sqrabs(vel);
+    cons[2 * nc + i] = rho * vel.x;
+    cons[3 * nc + i] = rho * vel.y;
+    cons[4 * nc + i] = rho * vel.z;
+  }
+}
+
+// calcboco_gen(bccon_cell_state): periodic copy (calcboco_connect_per_match.f90:56-78) and
+// physical ghost states (calcboco_ust.f90 -> calcboco_ust_sym / wall)
+void Solver::boco_cell_state() {
+  const int nc = m->ncell;
+  for (auto& b : m->bocos) {
+    for (size_t k = 0; k < b.iface.size(); ++k) {
+      int f = b.iface[k];
+      int g = m->fc2[f];
+      if (b.kind == BC_PERIODIC) {
+        int s = m->fc1[b.partner_face[k]];
+        for (int v = 0; v < 5; ++v) prim[v * nc + g] = prim[v * nc + s];
+      } else if (b.kind == BC_SYMMETRY) {
+        // calcboco_ust_sym: mirror the velocity across the face plane
+        int i = m->fc1[f];
+        V3 fn = m->fnormal[f];
+        V3 u = v3(prim[2 * nc + i], prim[3 * nc + i], prim[4 * nc + i]);
+        V3 ug = u - (2.0 * dot(u, fn)) * fn;
+        prim[g] = prim[i];
+        prim[nc + g] = prim[nc + i];
+        prim[2 * nc + g] = ug.x;
+        prim[3 * nc + g] = ug.y;
+        prim[4 * nc + g] = ug.z;
+      } else if (b.kind == BC_WALL) {
+        int i = m->fc1[f];
+        V3 u = v3(prim[2 * nc + i], prim[3 * nc + i], prim[4 * nc + i]);
+        V3 ug = 2.0 * b.wall_velocity - u;
+        prim[g] = prim[i];
+        prim[nc + g] = prim[nc + i];
+        prim[2 * nc + g] = ug.x;
+        prim[3 * nc + g] = ug.y;
+        prim[4 * nc + g] = ug.z;
+      }
+    }
+  }
+}
+
+// calcboco_gen(bccon_cell_grad): connections only (calcboco_gen.f90:78-84)
+void Solver::boco_cell_grad() {
+  const int nc = m->ncell;
+  for (auto& b : m->bocos) {
+    if (b.kind != BC_PERIODIC) continue;
+    for (size_t k = 0; k < b.iface.size(); ++k) {
+      int g = m->fc2[b.iface[k]];
+      int s = m->fc1[b.partner_face[k]];
+      for (int v = 0; v < 15; ++v) grad[v * nc + g] = grad[v * nc + s];
+    }
+  }
+}
+
+// calcboco_gen(bccon_face_state): cell_r(face) = cell_l(partner face)
+void Solver::boco_face_state() {
+  const int nf = m->nface;
+  for (auto& b : m->bocos) {
+    if (b.kind != BC_PERIODIC) continue;
+    for (size_t k = 0; k < b.iface.size(); ++k) {
+      int f = b.iface[k], fp = b.partner_face[k];
+      for (int v = 0; v < 5; ++v) cell_r[v * nf + f] = cell_l[v * nf + fp];
+    }
+  }
+}
+
+// MATRIX.f90:42-70 (cholesky_decomp), a column-major 3x3: a(i,j) = a[(j-1)*3 + (i-1)]
+static void cholesky_decomp(double* a) {
+  auto A = [&](int i, int j) -> double& { return a[(j - 1) * 3 + (i - 1)]; };
+  for (int i = 1; i <= 3; ++i)
+    for (int j = i; j <= 3; ++j) {
+      double sum = A(i, j);
+      for (int k = i - 1; k >= 1; --k) sum = sum - A(i, k) * A(j, k);
+      if (i == j) A(i, i) = std::sqrt(sum);
+      else A(j, i) = sum / A(i, i);
+    }
+}
+// MATRIX.f90:79-111 (cholesky_solve), b(3, p) column-major
+static void cholesky_solve(const double* a, double* b, int p) {
+  auto A = [&](int i, int j) { return a[(j - 1) * 3 + (i - 1)]; };
+  auto B = [&](int i, int k) -> double& { return b[(k - 1) * 3 + (i - 1)]; };
+  for (int i = 1; i <= 3; ++i) {
+    for (int j = 1; j <= i - 1; ++j)
+      for (int k = 1; k <= p; ++k) B(i, k) = B(i, k) - A(i, j) * B(j, k);
+    for (int k = 1; k <= p; ++k) B(i, k) = B(i, k) / A(i, i);
+  }
+  for (int i = 3; i >= 1; --i) {
+    for (int j = i + 1; j <= 3; ++j)
+      for (int k = 1; k <= p; ++k) B(i, k) = B(i, k) - A(j, i) * B(j, k);
+    for (int k = 1; k <= p; ++k) B(i, k) = B(i, k) / A(i, i);
+  }
+}
+
+// precalc_grad_lsq.f90:43-159
+void Solver::precalc_grad_lsq() {
+  const int nci = m->ncell_int, nf = m->nface, nfi = m->nface_int;
+  gradcond.assign(9 * (size_t)nci, 0.0);
+  std::vector<V3> dcg(nf);
+  for (int f = 0; f < nf; ++f) {
+    dcg[f] = m->ccentre[m->fc2[f]] - m->ccentre[m->fc1[f]];
+    if (sp.gradmeth == GRAD_LSQW) dcg[f] = dcg[f] / sqrabs(dcg[f]);
+  }
+  auto add = [&](int c, const V3& d) {
+    double im[9];
+    im[0] = d.x * d.x; im[4] = d.y * d.y; im[8] = d.z * d.z;
+    im[3] = d.x * d.y; im[1] = im[3];
+    im[6] = d.x * d.z; im[2] = im[6];
+    im[7] = d.y * d.z; im[5] = im[7];
+    for (int k = 0; k < 9; ++k) gradcond[9 * (size_t)c + k] = gradcond[9 * (size_t)c + k] + im[k];
+  };
+  for (int f = 0; f < nfi; ++f) { add(m->fc1[f], dcg[f]); add(m->fc2[f], dcg[f]); }
+  for (int f = nfi; f < nf; ++f) add(m->fc1[f], dcg[f]);
+  if (m->dim == 2)
+    for (int c = 0; c < nci; ++c) gradcond[9 * (size_t)c + 8] = gradcond[9 * (size_t)c + 8] + 1.0;
+  for (int c = 0; c < nci; ++c) cholesky_decomp(&gradcond[9 * (size_t)c]);
+  gradcond_ok = true;
+}
+
+// calc_gradient.f90:67-196 (5 components: rho, p, u, v, w)
+void Solver::calc_gradient() {
+  if (!gradcond_ok) precalc_grad_lsq();
+  const int nc = m->ncell, nci = m->ncell_int, nf = m->nface, nfi = m->nface_int;
+  std::vector<V3> dcg(nf);
+  for (int f = 0; f < nf; ++f) {
+    V3 d = m->ccentre[m->fc2[f]] - m->ccentre[m->fc1[f]];
+    if (sp.gradmeth == GRAD_LSQW) {
+      double s = sqrabs(d);
+      d = d / (s * s);
+    }
+    dcg[f] = d;
+  }
+  // rhs(1:3, ic*dim + dec), dim = 5: per cell a column-major 3x5 block
+  std::vector<double> rhs(15 * (size_t)nci, 0.0);
+  for (auto& col : m->colors)
+    for (int f : col) {
+      int i1 = m->fc1[f], i2 = m->fc2[f];
+      for (int v = 0; v < 5; ++v) {
+        double dsca = prim[v * nc + i2] - prim[v * nc + i1];
+        double* r1 = &rhs[15 * (size_t)i1 + 3 * v];
+        r1[0] = r1[0] + dsca * dcg[f].x;
+        r1[1] = r1[1] + dsca * dcg[f].y;
+        r1[2] = r1[2] + dsca * dcg[f].z;
+        if (f < nfi) {
+          double* r2 = &rhs[15 * (size_t)i2 + 3 * v];
+          r2[0] = r2[0] + dsca * dcg[f].x;
+          r2[1] = r2[1] + dsca * dcg[f].y;
+          r2[2] = r2[2] + dsca * dcg[f].z;
+        }
+      }
+    }
+  for (int c = 0; c < nci; ++c) cholesky_solve(&gradcond[9 * (size_t)c], &rhs[15 * (size_t)c], 5);
+  // grad%tabvect(is) for rho, p; grad%tabtens(1)%mat(i, 1:3) = rhs(1:3, nscal + i)
+  for (int c = 0; c < nci; ++c)
+    for (int v = 0; v < 5; ++v)
+      for (int k = 0; k < 3; ++k) grad[(3 * v + k) * (size_t)nc + c] = rhs[15 * (size_t)c + 3 * v + k];
+}
+
+// ---------------------------------------------------------------------------
+// Limiters (LIMITER.f90).  Scalars go through the array forms (*_t), vector components
+// through the scalar forms (called by *_vt), as in tvdgrad*_{scal,vect}.
+static double sgn1(double x) { return std::signbit(x) ? -1.0 : 1.0; }
+static double lim_scalar_form(int lim, double x1, double x2) {
+  switch (lim) {
+    case LIM_MINMOD: {  // LIMITER.f90:72-82
+      double s = 0.5 * (sgn1(x1) + sgn1(x2));
+      return s * std::min(std::fabs(x1), std::fabs(x2));
+    }
+    case LIM_ALBADA: {  // LIMITER.f90:122-133
+      double s = x1 * x2;
+      if (s <= 0.0) return 0.0;
+      return s * (x1 + x2) / (x1 * x1 + x2 * x2);
+    }
+    case LIM_VLEER: {
+      double s = x1 * x2;
+      if (s <= 0.0) return 0.0;
+      return 2.0 * s / (x1 + x2);
+    }
+    case LIM_SBEE: {
+      double r = 0.0;
+      if (x1 > 0.0 && x2 > 0.0) r = std::max(std::min(2.0 * x1, x2), std::min(2.0 * x2, x1));
+      if (x1 < 0.0 && x2 < 0.0) r = std::min(std::max(2.0 * x1, x2), std::max(2.0 * x2, x1));
+      return r;
+    }
+    case LIM_KIM3: {
+      double r = 0.0;
+      if (x1 > 0.0 && x2 > 0.0) { r = (2.0 * x1 + x2) / 3.0; r = std::min(std::min(2.0 * x1, 2.0 * x2), r); }
+      if (x1 < 0.0 && x2 < 0.0) { r = (2.0 * x1 + x2) / 3.0; r = std::max(std::max(2.0 * x1, 2.0 * x2), r); }
+      return r;
+    }
+    case LIM_LIM03: {
+      double eta = (x1 * x1 + x2 * x2) / 0.01 / 0.01;
+      double r = 0.0;
+      if (eta < 1.0) r = (2.0 * x2 + x1) / 3.0;
+      else if (x1 > 0.0 && x2 > 0.0) { r = (2.0 * x2 + x1) / 3.0; r = std::min(std::min(1.6 * x2, 2.0 * x1), r); }
+      else if (x1 < 0.0 && x2 < 0.0) { r = (2.0 * x2 + x1) / 3.0; r = std::max(std::max(1.6 * x2, 2.0 * x1), r); }
+      else if (x1 < 0.0 && x2 > 0.0) { r = (2.0 * x2 + x1) / 3.0; r = std::max(0.0, std::min(-0.5 * x1, r)); }
+      else if (x1 > 0.0 && x2 < 0.0) { r = (2.0 * x2 + x1) / 3.0; r = std::min(0.0, std::max(-0.5 * x1, r)); }
+      return r;
+    }
+  }
+  return 0.0;
+}
+static double lim_array_form(int lim, double x1, double x2) {
+  switch (lim) {
+    case LIM_MINMOD:  // LIMITER.f90:85-92
+      if (x1 > 0.0 && x2 > 0.0) return std::min(x1, x2);
+      if (x1 < 0.0 && x2 < 0.0) return std::max(x1, x2);
+      return 0.0;
+    case LIM_ALBADA:  // LIMITER.f90:136-144
+      if ((x1 > 0.0 && x2 > 0.0) || (x1 < 0.0 && x2 < 0.0))
+        return x1 * x2 * (x1 + x2) / (x1 * x1 + x2 * x2);
+      return 0.0;
+    case LIM_VLEER:
+      if ((x1 > 0.0 && x2 > 0.0) || (x1 < 0.0 && x2 < 0.0)) return 2.0 * x1 * x2 / (x1 + x2);
+      return 0.0;
+    default:
+      return lim_scalar_form(lim, x1, x2);
+  }
+}
+// limiter applied to the MUSCL slopes: fast/str use lim(2g - LR, LR), uns uses lim(g, LR);
+// kim3 swaps its arguments (tvdgrad*.f90)
+static double apply_lim(int lim, bool uns, bool arrayform, double g, double LR) {
+  double a = uns ? g : 2.0 * g - LR, b = LR;
+  if (lim == LIM_KIM3) std::swap(a, b);
+  return arrayform ? lim_array_form(lim, a, b) : lim_scalar_form(lim, a, b);
+}
+
+void Solver::hres_states() {
+  const int nc = m->ncell, nf = m->nface;
+  for (int f = 0; f < nf; ++f) {
+    const int icl = m->fc1[f], icr = m->fc2[f];
+    if (sp.highres == HRES_NONE) {  // distrib_field.f90
+      for (int v = 0; v < 5; ++v) {
+        cell_l[v * nf + f] = prim[v * nc + icl];
+        cell_r[v * nf + f] = prim[v * nc + icr];
+      }
+      continue;
+    }
+    const V3 CL = m->ccentre[icl], CR = m->ccentre[icr], F = m->fcentre[f];
+    V3 uLR = CR - CL;
+    double dLR;
+    double kLF = 0, kRF = 0;
+    V3 LF, RF;
+    if (sp.highres == HRES_MUSCLFAST) {  // hres_ns_musclfast.f90:40-50
+      kLF = vabs(F - CL);
+      kRF = -vabs(F - CR);
+      dLR = kLF - kRF;
+      uLR = uLR / dLR;
+    } else {  // hres_ns_muscl.f90 / hres_ns_muscluns.f90:40-50
+      LF = F - CL;
+      RF = F - CR;
+      dLR = vabs(uLR);
+      uLR = uLR / dLR;
+    }
+    const bool uns = sp.highres == HRES_MUSCLUNS;
+    double dL[5], dR[5];
+    // scalars (rho, p)
+    for (int s = 0; s < 2; ++s) {
+      double LRsca = (prim[s * nc + icr] - prim[s * nc + icl]) / dLR;
+      for (int side = 0; side < 2; ++side) {
+        int c = side == 0 ? icl : icr;
+        V3 vg = v3(grad[(3 * s) * (size_t)nc + c], grad[(3 * s + 1) * (size_t)nc + c],
+                   grad[(3 * s + 2) * (size_t)nc + c]);
+        double out;
+        if (sp.highres == HRES_MUSCLFAST) {  // tvdgradfst_scal.f90:35-57
+          double sg;
+          if (sp.limiter == LIM_NONE) sg = LRsca;
+          else sg = apply_lim(sp.limiter, false, true, dot(vg, uLR), LRsca);
+          out = sg * (side == 0 ? kLF : kRF);
+        } else {  // tvdgradstr_scal.f90 / tvdgraduns_scal.f90:35-57
+          double sg = dot(vg, uLR);
+          if (sp.limiter == LIM_NONE) sg = LRsca - sg;
+          else sg = apply_lim(sp.limiter, uns, true, sg, LRsca) - sg;
+          vg = vg + sg * uLR;
+          out = dot(vg, side == 0 ? LF : RF);
+        }
+        (side == 0 ? dL : dR)[s] = out;
+      }
+    }
+    // velocity (tensor gradient)
+    {
+      V3 qL = v3(prim[2 * nc + icl], prim[3 * nc + icl], prim[4 * nc + icl]);
+      V3 qR = v3(prim[2 * nc + icr], prim[3 * nc + icr], prim[4 * nc + icr]);
+      V3 LRvec = (qR - qL) / dLR;
+      for (int side = 0; side < 2; ++side) {
+        int c = side == 0 ? icl : icr;
+        double T[3][3];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) T[i][j] = grad[(6 + 3 * i + j) * (size_t)nc + c];
+        auto matvec = [&](const V3& v) {
+          // matmul(t%mat, tab(v)) (TENSOR3.f90:255-262)
+          return v3(T[0][0] * v.x + T[0][1] * v.y + T[0][2] * v.z,
+                    T[1][0] * v.x + T[1][1] * v.y + T[1][2] * v.z,
+                    T[2][0] * v.x + T[2][1] * v.y + T[2][2] * v.z);
+        };
+        V3 vc = matvec(uLR);
+        double lrv[3] = {LRvec.x, LRvec.y, LRvec.z};
+        double vcc[3] = {vc.x, vc.y, vc.z};
+        double out[3];
+        if (sp.highres == HRES_MUSCLFAST) {  // tvdgradfst_vect.f90:35-58
+          double k = side == 0 ? kLF : kRF;
+          for (int i = 0; i < 3; ++i) {
+            double s = sp.limiter == LIM_NONE ? lrv[i] : apply_lim(sp.limiter, false, false, vcc[i], lrv[i]);
+            out[i] = k * s;
+          }
+        } else {  // tvdgradstr_vect.f90 / tvdgraduns_vect.f90:36-58
+          double s[3];
+          for (int i = 0; i < 3; ++i) {
+            if (sp.limiter == LIM_NONE) s[i] = lrv[i] - vcc[i];
+            else s[i] = apply_lim(sp.limiter, uns, false, vcc[i], lrv[i]) - vcc[i];
+          }
+          // tgrad = tgrad + (s .tens. uLR)  (TENSOR3.f90:283-292)
+          double u[3] = {uLR.x, uLR.y, uLR.z};
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) T[i][j] = T[i][j] + s[i] * u[j];
+          V3 d = matvec(side == 0 ? LF : RF);
+          out[0] = d.x; out[1] = d.y; out[2] = d.z;
+        }
+        for (int i = 0; i < 3; ++i) (side == 0 ? dL : dR)[2 + i] = out[i];
+      }
+    }
+    for (int v = 0; v < 5; ++v) {
+      cell_l[v * nf + f] = prim[v * nc + icl] + dL[v];
+      cell_r[v * nf + f] = prim[v * nc + icr] + dR[v];
+    }
+  }
+}
+
+// postlimit_barth.f90:42-223.  A face whose reconstructed increment is exactly zero imposes
+// no constraint (the Fortran divides by it; its MAX/MIN of a NaN is compiler-dependent).
+void Solver::postlimit_barth(double klim) {
+  const int nc = m->ncell, nf = m->nface;
+  std::vector<double> ratio(nc);
+  auto constrain = [&](int c, double num, double den) {
+    if (den == 0.0) return;
+    double l = num / den;
+    l = std::max(klim * l, 0.0);
+    ratio[c] = std::min(ratio[c], l);
+  };
+  for (int s = 0; s < 2; ++s) {
+    std::fill(ratio.begin(), ratio.end(), 1.0);
+    for (int f = 0; f < nf; ++f) {
+      int icl = m->fc1[f], icr = m->fc2[f];
+      double LR = prim[s * nc + icr] - prim[s * nc + icl];
+      constrain(icl, LR, cell_l[s * nf + f] - prim[s * nc + icl]);
+      constrain(icr, -LR, cell_r[s * nf + f] - prim[s * nc + icr]);
+    }
+    for (int f = 0; f < nf; ++f) {
+      int icl = m->fc1[f], icr = m->fc2[f];
+      cell_l[s * nf + f] = prim[s * nc + icl] + ratio[icl] * (cell_l[s * nf + f] - prim[s * nc + icl]);
+      cell_r[s * nf + f] = prim[s * nc + icr] + ratio[icr] * (cell_r[s * nf + f] - prim[s * nc + icr]);
+    }
+    for (int c = 0; c < nc; ++c) limratio[s * nc + c] = ratio[c];
+  }
+  std::fill(ratio.begin(), ratio.end(), 1.0);
+  for (int f = 0; f < nf; ++f) {
+    int icl = m->fc1[f], icr = m->fc2[f];
+    for (int k = 0; k < 3; ++k) {
+      double LR = prim[(2 + k) * nc + icr] - prim[(2 + k) * nc + icl];
+      constrain(icl, LR, cell_l[(2 + k) * nf + f] - prim[(2 + k) * nc + icl]);
+    }
+    for (int k = 0; k < 3; ++k) {
+      double LR = prim[(2 + k) * nc + icr] - prim[(2 + k) * nc + icl];
+      constrain(icr, -LR, cell_r[(2 + k) * nf + f] - prim[(2 + k) * nc + icr]);
+    }
+  }
+  for (int f = 0; f < nf; ++f) {
+    int icl = m->fc1[f], icr = m->fc2[f];
+    for (int k = 0; k < 3; ++k) {
+      int v = 2 + k;
+      cell_l[v * nf + f] = prim[v * nc + icl] + ratio[icl] * (cell_l[v * nf + f] - prim[v * nc + icl]);
+      cell_r[v * nf + f] = prim[v * nc + icr] + ratio[icr] * (cell_r[v * nf + f] - prim[v * nc + icr]);
+    }
+  }
+  for (int c = 0; c < nc; ++c) limratio[2 * nc + c] = ratio[c];
+}
+
+// ---------------------------------------------------------------------------
+// Face fluxes per unit area, written into flux (5 x nface)
+namespace {
+struct State { double rho, p; V3 u; };
+inline State face_state(const std::vector<double>& q, int nf, int f) {
+  State s;
+  s.rho = q[f]; s.p = q[nf + f];
+  s.u = v3(q[2 * nf + f], q[3 * nf + f], q[4 * nf + f]);
+  return s;
+}
+}  // namespace
+
+// Roe flux-difference splitting (Roe 1981) with Harten's entropy fix on the acoustic waves.
+// Typhon parses SCHEME=ROE but has no implementation (calc_flux_inviscid.f90:48-79): this
+// is new code written from the published method, with the Roe averages of
+// calc_roe_states.f90:35-53.  Fluxes per unit area along the unit normal n.
+static void roe_flux(double g, const State& L, const State& R, V3 n, double delta_frac, double* F) {
+  const double ig1 = 1.0 / (g - 1.0);
+  const double gig1 = g / (g - 1.0);
+  // Roe averages (calc_roe_states.f90)
+  double t1 = std::sqrt(R.rho / L.rho);
+  double rroe = L.rho * t1;
+  double kl = 1.0 / (1.0 + t1), kr = t1 * kl;
+  V3 uroe = kl * L.u + kr * R.u;
+  double hl = gig1 * L.p / L.rho + 0.5 * sqrabs(L.u);
+  double hr = gig1 * R.p / R.rho + 0.5 * sqrabs(R.u);
+  double hroe = kl * hl + kr * hr;
+  double q2 = sqrabs(uroe);
+  double a2 = (g - 1.0) * (hroe - 0.5 * q2);
+  double a = std::sqrt(a2);
+  double vn = dot(uroe, n);
+  double vnl = dot(L.u, n), vnr = dot(R.u, n);
+  double rel = ig1 * L.p + 0.5 * L.rho * sqrabs(L.u);
+  double rer = ig1 * R.p + 0.5 * R.rho * sqrabs(R.u);
+  // jumps
+  double drho = R.rho - L.rho, dp = R.p - L.p, dvn = vnr - vnl;
+  V3 du = R.u - L.u;
+  // wave strengths
+  double al1 = (dp - rroe * a * dvn) / (2.0 * a2);
+  double al5 = (dp + rroe * a * dvn) / (2.0 * a2);
+  double al2 = drho - dp / a2;  // entropy wave
+  V3 dut = du - dvn * n;        // shear waves (tangential velocity jump)
+  // eigenvalues with Harten's fix on the acoustic ones
+  double l1 = std::fabs(vn - a), l5 = std::fabs(vn + a), l2 = std::fabs(vn);
+  double delta = delta_frac * a;
+  if (l1 < delta) l1 = (l1 * l1 + delta * delta) / (2.0 * delta);
+  if (l5 < delta) l5 = (l5 * l5 + delta * delta) / (2.0 * delta);
+  // dissipation |A| dQ, components (mass, energy, momentum)
+  double d_mass = l1 * al1 + l2 * al2 + l5 * al5;
+  V3 d_mom = l1 * al1 * (uroe - a * n) + l2 * al2 * uroe + l5 * al5 * (uroe + a * n) +
+             (l2 * rroe) * dut;
+  double d_ener = l1 * al1 * (hroe - a * vn) + l2 * al2 * (0.5 * q2) + l5 * al5 * (hroe + a * vn) +
+                  (l2 * rroe) * (dot(uroe, du) - vn * dvn);
+  // central part
+  double fl_mass = vnl * L.rho, fr_mass = vnr * R.rho;
+  double fl_ener = vnl * (rel + L.p), fr_ener = vnr * (rer + R.p);
+  V3 fl_mom = (vnl * L.rho) * L.u + L.p * n, fr_mom = (vnr * R.rho) * R.u + R.p * n;
+  F[0] = 0.5 * (fl_mass + fr_mass - d_mass);
+  F[1] = 0.5 * (fl_ener + fr_ener - d_ener);
+  V3 fm = 0.5 * (fl_mom + fr_mom - d_mom);
+  F[2] = fm.x; F[3] = fm.y; F[4] = fm.z;
+}
+
+void Solver::face_fluxes() {
+  const int nf = m->nface;
+  const double g = sp.gamma;
+  const double ig1 = 1.0 / (g - 1.0);
+  for (int f = 0; f < nf; ++f) {
+    State L = face_state(cell_l, nf, f), R = face_state(cell_r, nf, f);
+    V3 fn = m->fnormal[f];
+    double F[5];
+    if (sp.scheme == SCH_HLLC) {  // calc_flux_hllc.f90:86-171, beta = 1
+      // calc_roe_states.f90:35-53
+      const double gig1 = g / (g - 1.0);
+      double t1 = std::sqrt(R.rho / L.rho);
+      double roe_rho = L.rho * t1;
+      double kl = 1.0 / (1.0 + t1);
+      double kr = t1 * kl;
+      V3 roe_u = kl * L.u + kr * R.u;
+      double h1 = gig1 * L.p / L.rho + 0.5 * sqrabs(L.u);
+      double h2 = gig1 * R.p / R.rho + 0.5 * sqrabs(R.u);
+      h1 = kl * h1 + kr * h2;
+      double roe_p = (h1 - 0.5 * sqrabs(roe_u)) * roe_rho / gig1;
+      double vnl = dot(L.u, fn), vnr = dot(R.u, fn);
+      double al = std::sqrt(g * L.p / L.rho), ar = std::sqrt(g * R.p / R.rho);
+      double vm = dot(roe_u, fn);
+      double am = std::sqrt(g * roe_p / roe_rho);
+      double rel = ig1 * L.p + 0.5 * L.rho * sqrabs(L.u);
+      double rer = ig1 * R.p + 0.5 * R.rho * sqrabs(R.u);
+      const double beta = 1.0;
+      double sl = std::min(vnl - beta * al, vm - am);
+      double sr = std::max(vnr + beta * ar, vm + am);
+      if (sl >= 0.0) {
+        F[0] = vnl * L.rho;
+        F[1] = vnl * (rel + L.p);
+        V3 mo = (vnl * L.rho) * L.u + L.p * fn;
+        F[2] = mo.x; F[3] = mo.y; F[4] = mo.z;
+      } else if (sr <= 0.0) {
+        F[0] = vnr * R.rho;
+        F[1] = vnr * (rer + R.p);
+        V3 mo = (vnr * R.rho) * R.u + R.p * fn;
+        F[2] = mo.x; F[3] = mo.y; F[4] = mo.z;
+      } else {
+        double rqL = L.rho * (sl - vnl);
+        double rqR = R.rho * (sr - vnr);
+        double Sst = (rqR * vnr - rqL * vnl - R.p + L.p) / (rqR - rqL);
+        double iks, rst, pst, rest;
+        V3 rvst;
+        if (Sst >= 0.0) {
+          iks = 1.0 / (sl - Sst);
+          rst = rqL * iks;
+          pst = L.p - rqL * (vnl - Sst);
+          rvst = iks * ((rqL * L.u) + (pst - L.p) * fn);
+          rest = iks * (rel * (sl - vnl) - L.p * vnl + pst * Sst);
+        } else {
+          iks = 1.0 / (sr - Sst);
+          rst = rqR * iks;
+          pst = R.p - rqR * (vnr - Sst);
+          rvst = iks * ((rqR * R.u) + (pst - R.p) * fn);
+          rest = iks * (rer * (sr - vnr) - R.p * vnr + pst * Sst);
+        }
+        F[0] = Sst * rst;
+        F[1] = Sst * (rest + pst);
+        V3 mo = (Sst * rvst) + (pst * fn);
+        F[2] = mo.x; F[3] = mo.y; F[4] = mo.z;
+      }
+    } else if (sp.scheme == SCH_RUSANOV) {  // calc_flux_rusanov.f90:57-83
+      double vnl = dot(L.u, fn), vnr = dot(R.u, fn);
+      double al = std::sqrt(g * L.p / L.rho), ar = std::sqrt(g * R.p / R.rho);
+      double ray = std::max(std::fabs(vnl) + al, std::fabs(vnr) + ar);
+      double rel = ig1 * L.p + 0.5 * L.rho * sqrabs(L.u);
+      double rer = ig1 * R.p + 0.5 * R.rho * sqrabs(R.u);
+      F[0] = 0.5 * ((vnl + ray) * L.rho + (vnr - ray) * R.rho);
+      F[1] = 0.5 * ((vnl + ray) * rel + (vnr - ray) * rer + vnl * L.p + vnr * R.p);
+      V3 mo = 0.5 * ((((vnl + ray) * L.rho) * L.u + ((vnr - ray) * R.rho) * R.u) + (L.p + R.p) * fn);
+      F[2] = mo.x; F[3] = mo.y; F[4] = mo.z;
+    } else {
+      roe_flux(g, L, R, fn, sp.roe_entropy_fix, F);
+    }
+    for (int v = 0; v < 5; ++v) flux[v * nf + f] = F[v];
+  }
+}
+
+// flux_to_res.f90:47-144: F *= S, colour-ordered scatter, R *= dtloc/V (interior cells)
+void Solver::flux_to_res() {
+  const int nc = m->ncell, nci = m->ncell_int, nf = m->nface;
+  for (int v = 0; v < 5; ++v)
+    for (int f = 0; f < nf; ++f) flux[v * nf + f] = m->fsurf[f] * flux[v * nf + f];
+  std::fill(residu.begin(), residu.end(), 0.0);
+  for (auto& col : m->colors)
+    for (int f : col) {
+      int i1 = m->fc1[f], i2 = m->fc2[f];
+      for (int v = 0; v < 5; ++v) {
+        residu[v * nc + i1] = residu[v * nc + i1] - flux[v * nf + f];
+        residu[v * nc + i2] = residu[v * nc + i2] + flux[v * nf + f];
+      }
+    }
+  for (int c = 0; c < nci; ++c) {
+    double coef = dtloc[c] / m->cvol[c];
+    for (int v = 0; v < 5; ++v) residu[v * nc + c] = coef * residu[v * nc + c];
+  }
+}
+
+// calc_rhs.f90 explicit part: prim, ghost states, gradient, face states, fluxes, residual
+void Solver::calc_rhs() {
+  varprim();
+  if (sp.gradmeth != GRAD_NONE) {
+    boco_cell_state();
+    calc_gradient();
+    boco_cell_grad();
+  }
+  hres_states();
+  if (sp.postlim == POSTLIM_BARTH) postlimit_barth(0.5);
+  if (sp.postlim == POSTLIM_SUPERBARTH) postlimit_barth(1.0);
+  boco_face_state();
+  face_fluxes();
+  flux_to_res();
+}
+
+// calc_ns_timestep.f90:52-103 + calc_zonetimestep.f90 min over interior cells
+double Solver::timestep() {
+  const int nc = m->ncell, nci = m->ncell_int;
+  const double gg1 = sp.gamma * (sp.gamma - 1.0);
+  std::vector<double> sumS(nci, 0.0);
+  for (auto& col : m->colors)
+    for (int f : col) {
+      int i1 = m->fc1[f], i2 = m->fc2[f];
+      sumS[i1] = sumS[i1] + m->fsurf[f];
+      if (i2 < nci) sumS[i2] = sumS[i2] + m->fsurf[f];
+    }
+  double dt = std::numeric_limits<double>::max();
+  for (int c = 0; c < nci; ++c) {
+    double d = cfl * 2.0 * m->cvol[c] / sumS[c];
+    double irho = 1.0 / cons[c];
+    double rv2 = cons[2 * nc + c] * cons[2 * nc + c] + cons[3 * nc + c] * cons[3 * nc + c] +
+                 cons[4 * nc + c] * cons[4 * nc + c];
+    double a2 = (cons[nc + c] - 0.5 * rv2 * irho) * gg1 * irho;
+    if (!(a2 > 0.0)) return -1.0;  // negative or NaN internal energy
+    d = d / (std::sqrt(rv2) * irho + std::sqrt(a2));
+    dtloc[c] = d;
+    dt = std::min(dt, d);
+  }
+  return dt;
+}
+
+// treelevel_rungekutta.f90:48-113 then update_field.f90:38 (U += residu) with a global dt
+void Solver::rk_step(double dt) {
+  const int nc = m->ncell;
+  const int n = rk.nstage;
+  std::fill(dtloc.begin(), dtloc.end(), dt);
+  std::vector<double> u0 = cons;
+  std::vector<std::vector<double>> rhs(n);
+  for (int i = 1; i <= n; ++i) {
+    if (i >= 2) {
+      cons = u0;
+      for (int s = 1; s <= i - 1; ++s) {
+        double c = rk.c(i - 1, s);
+        for (size_t k = 0; k < cons.size(); ++k) cons[k] = cons[k] + c * rhs[s - 1][k];
+      }
+    }
+    calc_rhs();
+    rhs[i - 1] = residu;
+  }
+  // residu = coef(n,1)*rhs1 + sum coef(n,s)*rhs_s   (scale then xeqxpay)
+  for (size_t k = 0; k < residu.size(); ++k) residu[k] = rk.c(n, 1) * rhs[0][k];
+  for (int s = 2; s <= n; ++s) {
+    double c = rk.c(n, s);
+    for (size_t k = 0; k < residu.size(); ++k) residu[k] = residu[k] + c * rhs[s - 1][k];
+  }
+  cons = u0;
+  for (size_t k = 0; k < cons.size(); ++k) cons[k] = cons[k] + residu[k];
+  (void)nc;
+}
+
+}  // namespace ory

@@ -1,0 +1,201 @@
+"""ctypes binding of the CPU oracle (oracle/build/liboracle.so) for the tests.
+
+The oracle is the checker: tests compare the GPU library against it, never the
+other way round.  ``load()`` builds it with make on first use.
+"""
+import ctypes as C
+import pathlib
+import subprocess
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+LIB = ROOT / "oracle" / "build" / "liboracle.so"
+
+# enums of oracle/oracle.hpp
+BC_PERIODIC, BC_SYMMETRY, BC_WALL = 1, 2, 3
+SCH_HLLC, SCH_RUSANOV, SCH_ROE = 1, 2, 3
+HRES_NONE, HRES_MUSCL, HRES_MUSCLFAST, HRES_MUSCLUNS = 0, 1, 2, 3
+LIM_NONE, LIM_MINMOD, LIM_ALBADA, LIM_VLEER, LIM_SBEE, LIM_KIM3, LIM_LIM03 = range(7)
+POSTLIM_NONE, POSTLIM_BARTH, POSTLIM_SUPERBARTH = 0, 1, 2
+GRAD_NONE, GRAD_LSQ, GRAD_LSQW = 0, 1, 2
+RK = {"RK2": 1, "RK2-SSP": 2, "RK3-SSP": 3, "RK4": 4, "RK25BB": 5, "RK26BB": 6, "RK12BS": 7, "RK13BS": 8}
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB))
+        vp = C.c_void_p
+        lib.ory_raw_new.restype = vp
+        lib.ory_raw_free.argtypes = [vp]
+        lib.ory_raw_read_tym.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int]
+        lib.ory_raw_set_vtex.argtypes = [vp, C.c_int, vp]
+        lib.ory_raw_add_section.argtypes = [vp, C.c_int, C.c_int, vp, vp]
+        lib.ory_raw_add_mark.argtypes = [vp, C.c_char_p, C.c_int, vp]
+        lib.ory_mesh_build.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, vp, C.c_char_p, C.c_int]
+        lib.ory_mesh_sizes.argtypes = [vp, vp]
+        lib.ory_mesh_export.argtypes = [vp] + [vp] * 11
+        lib.ory_mesh_facevtex.argtypes = [vp, C.c_int, vp]
+        lib.ory_solver_new.restype = vp
+        lib.ory_solver_new.argtypes = [vp, vp, vp]
+        lib.ory_solver_free.argtypes = [vp]
+        lib.ory_solver_set_cons.argtypes = [vp, vp]
+        lib.ory_solver_set_prim.argtypes = [vp, vp]
+        lib.ory_solver_get.argtypes = [vp, C.c_int, vp]
+        lib.ory_solver_timestep.argtypes = [vp]
+        lib.ory_solver_timestep.restype = C.c_double
+        lib.ory_solver_rhs.argtypes = [vp, C.c_double]
+        lib.ory_solver_rk_step.argtypes = [vp, C.c_double]
+        lib.ory_solver_run_steps.argtypes = [vp, C.c_int, vp]
+        lib.ory_run_nrg.argtypes = [C.c_int, vp, C.c_int, C.c_double, C.c_int, C.c_double, vp]
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Mesh:
+    """Raw mesh + Typhon preprocessing inside the oracle."""
+
+    def __init__(self):
+        self.lib = load()
+        self.h = C.c_void_p(self.lib.ory_raw_new())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.ory_raw_free(self.h)
+            self.h = None
+
+    @classmethod
+    def from_tym(cls, path):
+        m = cls()
+        err = C.create_string_buffer(256)
+        if m.lib.ory_raw_read_tym(m.h, str(path).encode(), err, 256) != 0:
+            raise RuntimeError(err.value.decode())
+        return m
+
+    @classmethod
+    def from_raw(cls, raw):
+        """raw: typhon_gb300.umesh.RawMesh-like object (vtex, sections, marks)."""
+        m = cls()
+        vt = np.ascontiguousarray(raw.vtex, dtype=np.float64)
+        m.lib.ory_raw_set_vtex(m.h, vt.shape[0], _p(vt))
+        for typ, ielem, conn in raw.sections:
+            ie = np.ascontiguousarray(ielem, dtype=np.int32)
+            cv = np.ascontiguousarray(conn, dtype=np.int32)
+            m.lib.ory_raw_add_section(m.h, int(typ), ie.shape[0], _p(ie), _p(cv))
+        for name, tags in raw.marks:
+            t = np.ascontiguousarray(tags, dtype=np.int32)
+            m.lib.ory_raw_add_mark(m.h, name.encode(), t.shape[0], _p(t))
+        return m
+
+    def build(self, dim, bcs):
+        """bcs: list of (family, kind, partner, translation(3), wall_velocity(3))."""
+        n = len(bcs)
+        fam = (C.c_char_p * n)(*[b[0].encode() for b in bcs])
+        kind = np.array([b[1] for b in bcs], dtype=np.int32)
+        par = (C.c_char_p * n)(*[(b[2] or "").encode() for b in bcs])
+        tr = np.array([b[3] for b in bcs], dtype=np.float64).reshape(-1)
+        wv = np.array([b[4] if len(b) > 4 else (0, 0, 0) for b in bcs], dtype=np.float64).reshape(-1)
+        err = C.create_string_buffer(256)
+        rc = self.lib.ory_mesh_build(self.h, dim, n, C.cast(fam, C.c_void_p), _p(kind),
+                                     C.cast(par, C.c_void_p), _p(tr), _p(wv), err, 256)
+        if rc != 0:
+            raise RuntimeError(err.value.decode())
+        s = np.zeros(7, dtype=np.int32)
+        self.lib.ory_mesh_sizes(self.h, _p(s))
+        (self.ncell_int, self.ncell, self.nface_int, self.nface, self.ncolors, self.dim,
+         self.nboco) = map(int, s)
+        return self
+
+    def export(self):
+        nf, nc = self.nface, self.ncell
+        d = dict(
+            fc1=np.zeros(nf, np.int32), fc2=np.zeros(nf, np.int32),
+            fnormal=np.zeros((nf, 3)), fcentre=np.zeros((nf, 3)), fsurf=np.zeros(nf),
+            ccentre=np.zeros((nc, 3)), cvol=np.zeros(nc),
+            face_color=np.zeros(nf, np.int32), face_partner=np.zeros(nf, np.int32),
+            face_bckind=np.zeros(nf, np.int32), face_wallvel=np.zeros((nf, 3)))
+        self.lib.ory_mesh_export(self.h, *[_p(d[k]) for k in (
+            "fc1", "fc2", "fnormal", "fcentre", "fsurf", "ccentre", "cvol", "face_color",
+            "face_partner", "face_bckind", "face_wallvel")])
+        d.update(ncell_int=self.ncell_int, ncell=self.ncell, nface_int=self.nface_int,
+                 nface=self.nface, dim=self.dim)
+        return d
+
+
+class Solver:
+    def __init__(self, mesh, scheme=SCH_HLLC, highres=HRES_NONE, limiter=LIM_ALBADA,
+                 postlim=POSTLIM_NONE, gradmeth=GRAD_NONE, rk="RK4", gamma=1.4, cfl=1.0,
+                 entropy_fix=0.1):
+        self.lib = load()
+        self.mesh = mesh
+        ip = np.array([scheme, highres, limiter, postlim, gradmeth, RK[rk]], np.int32)
+        dp = np.array([gamma, cfl, entropy_fix], np.float64)
+        self.h = C.c_void_p(self.lib.ory_solver_new(mesh.h, _p(ip), _p(dp)))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.ory_solver_free(self.h)
+            self.h = None
+
+    def set_cons(self, cons):
+        c = np.ascontiguousarray(cons, dtype=np.float64)
+        assert c.size == 5 * self.mesh.ncell
+        self.lib.ory_solver_set_cons(self.h, _p(c))
+
+    def set_prim(self, prim):
+        c = np.ascontiguousarray(prim, dtype=np.float64)
+        assert c.size == 5 * self.mesh.ncell
+        self.lib.ory_solver_set_prim(self.h, _p(c))
+
+    _SIZES = {0: "c5", 1: "c5", 2: "c15", 3: "c5", 4: "f5", 5: "f5", 6: "f5", 7: "c1", 8: "c3"}
+
+    def get(self, which):
+        code = {"cons": 0, "prim": 1, "grad": 2, "residu": 3, "flux": 4, "cell_l": 5,
+                "cell_r": 6, "dtloc": 7, "limratio": 8}[which]
+        kind = self._SIZES[code]
+        n = self.mesh.ncell if kind[0] == "c" else self.mesh.nface
+        k = int(kind[1:])
+        out = np.zeros(k * n)
+        self.lib.ory_solver_get(self.h, code, _p(out))
+        return out.reshape(k, n)
+
+    def timestep(self):
+        return self.lib.ory_solver_timestep(self.h)
+
+    def rhs(self, dt):
+        self.lib.ory_solver_rhs(self.h, dt)
+
+    def rk_step(self, dt):
+        self.lib.ory_solver_rk_step(self.h, dt)
+
+    def run_steps(self, n):
+        dts = np.zeros(n)
+        rc = self.lib.ory_solver_run_steps(self.h, n, _p(dts))
+        if rc != 0:
+            raise RuntimeError("oracle step failed (negative energy or NaN)")
+        return dts
+
+
+def run_nrg(which, mesh, rk, cfl, ncycle=100, duration=0.1):
+    lib = load()
+    out = np.zeros(ncycle)
+    ns = lib.ory_run_nrg(which, mesh.h, RK[rk], cfl, ncycle, duration, _p(out))
+    if ns < 0:
+        raise RuntimeError(f"oracle NRG case failed ({ns})")
+    return out, ns
+
+
+PERIODIC_UNIT_SQUARE = [("IMIN", BC_PERIODIC, "IMAX", (1.0, 0.0, 0.0)),
+                        ("JMIN", BC_PERIODIC, "JMAX", (0.0, 1.0, 0.0))]
