@@ -1,0 +1,313 @@
+"""Benchmark: FP64 cell-updates/s of the explicit residual-and-update path on one GB300.
+
+Workload (default): the 3D Euler Taylor-Green vortex on the periodic [0,2 pi]^3 box, 64^3
+hexahedra split into 5 tetrahedra = 1,310,720 cells (2,646,016 faces), nodes jittered by
++-5% of h (seed 1234); least-squares gradients, MUSCL-UNS with the Barth post-limiter, Roe
+flux, SSP-RK3 at CFL 0.8, global stability time step computed on the device each step.
+A "step" is one full SSP-RK3 step (3 residual evaluations) of every cell; one
+cell-update = one cell advanced by one step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload tgv3d|vortex2d] [--n 64] [--mode fast|exact]
+
+--impl reference times the CPU restatement of Typhon's solver (oracle/, OpenMP on all
+host cores) on the same configuration: Typhon itself is Fortran and cannot be built here.
+N > 1 runs independent replicas (the path is not sharded), one per GPU.
+Prints one JSON line (rank 0).
+"""
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-updates/s FP64"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="tgv3d", choices=["tgv3d", "vortex2d"])
+    ap.add_argument("--n", type=int, default=None, help="cells per direction (default: the workload's)")
+    ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--cpu-sample-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def kernel_bytes(md, nslot_avg):
+    """Compulsory (algorithmic) DRAM bytes per launch of each kernel: every array element
+    the kernel needs is counted once (cells and faces of the whole mesh).  FP64 = 8 B,
+    index = 4 B.  nci interior cells, nf faces, ng ghost cells, f = faces per cell."""
+    nci, nf, ng = md.ncell_int, md.nface, md.ncell - md.ncell_int
+    nc = md.ncell
+    cf = 4 * nslot_avg * nci                                # gather list entries
+    return {
+        "ghost_prim": ng * (8 + 40 + 40),                   # gsrc/gface, read prim, write prim
+        "grad": cf + nf * (8 + 48) + nc * 40 + nci * 120,    # list, fc1/fc2 + weights, prim, write grad
+        "ghost_grad": ng * (8 + 120 + 120),
+        "face_states": nf * (8 + 24 + 8 + 24 + 24 + 80) + nc * (40 + 120),  # fc, uLR, dLR, LF, RF, write cl/cr
+        "barth": cf + nf * (8 + 80) + nc * 40 + nci * 24,    # list, fc, cl/cr, prim, write ratio
+        "face_flux_lim": nf * (8 + 4 + 4 + 80 + 24 + 8 + 40) + nc * (40 + 24),
+        "face_flux": nf * (8 + 4 + 4 + 24 + 8 + 40 + 64) + nc * (40 + 120),
+        "rk_update": cf + nf * 40 + nci * (8 + 40 + 40 + 40 + 40 + 40 + 40),  # vol, flux, u0, acc r/w, cur, prim
+        "gather": cf + nf * 40 + nci * (8 + 40),
+        "timestep": nci * (8 + 8 + 40),
+        "prim": nci * 80,
+    }
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import typhon_gb300 as ty
+    from typhon_gb300 import _capi, cases
+    from typhon_gb300 import build as tybuild
+
+    tybuild.build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = cases.WORKLOADS[args.workload]
+    n = args.n or w["n"]
+    t0 = time.time()
+    md = cases.make_mesh(args.workload, n)
+    t_mesh = time.time() - t0
+    prim = cases.initial_prim(args.workload, md.cell_centre)
+    g = ty.Grid(md, device=local)
+    g.set_spat(w["scheme"], w["highres"], w["limiter"], w["postlim"], mode=args.mode)
+    g.set_prim(prim)
+    stream = torch.cuda.Stream(device=local)
+    _capi.check(g.lib.ty_set_stream(g.h, stream.cuda_stream), "ty_set_stream")
+    nci = md.ncell_int
+    info = g.info()
+    nslot_avg = (2 * md.nface_int + (md.nface - md.nface_int)) / nci
+    # warmup
+    g.run_steps(w["rk"], w["cfl"], args.warmup)
+    torch.cuda.synchronize(local)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    _capi.check(g.lib.ty_profile_enable(g.h, 1), "ty_profile_enable")
+    barrier()
+    torch.cuda.synchronize(local)
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            g.run_steps(w["rk"], w["cfl"], args.steps)
+            e1.record(stream)
+        torch.cuda.synchronize(local)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    nk = len(_capi.KERNEL_NAMES)
+    kms = np.zeros(nk)
+    kl = np.zeros(nk, np.int32)
+    _capi.check(g.lib.ty_profile_read(g.h, nk, kms.ctypes.data, kl.ctypes.data), "ty_profile_read")
+    _capi.check(g.lib.ty_profile_enable(g.h, 0), "ty_profile_enable")
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = nci * args.steps * world / (ms * 1e-3)
+    # per-kernel roofline
+    peak, peak_kind = measured_peaks()
+    kb = kernel_bytes(md, nslot_avg)
+    per = {}
+    for i, name in enumerate(_capi.KERNEL_NAMES):
+        if kl[i] > 0:
+            avg_ms = kms[i] / kl[i]
+            per[name] = {"launches": int(kl[i]), "total_ms": round(float(kms[i]), 4),
+                         "avg_ms": round(float(avg_ms), 5), "share": round(float(kms[i] / kms.sum()), 4),
+                         "achieved_gbs": round(kb[name] / (avg_ms * 1e-3) / 1e9, 1)}
+    dom = max(per, key=lambda k: per[k]["total_ms"])
+    ach = per[dom]["achieved_gbs"]
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": int(kb[dom])}
+    # end to end through the public API with host buffers, per step: H2D state, one step, D2H state
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    cons_host = g.get_cons()
+    torch.cuda.synchronize(local)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        g.set_cons(cons_host)
+        g.run_steps(w["rk"], w["cfl"], 1)
+        cons_host = g.get_cons()
+    torch.cuda.synchronize(local)
+    t_e2e = time.perf_counter() - t0
+    barrier()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = {"value": nci * e2e_steps * world / t_e2e, "unit": "cell-updates/s",
+           "h2d_bytes_per_step": 40 * nci, "d2h_bytes_per_step": 40 * nci, "steps": e2e_steps}
+    clocks = clk.summary()
+    out = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload} {'64^3x5 tets' if args.workload == 'tgv3d' else '64x64x2 tris'}"
+                   if n == w["n"] else f"{args.workload} n={n}", "cells": nci, "faces": md.nface,
+                   "scheme": w["scheme"], "highres": w["highres"], "limiter": w["limiter"],
+                   "postlim": w["postlim"], "rk": w["rk"], "cfl": w["cfl"], "mode": args.mode,
+                   "parallelism": f"replicas{world}",
+                   "l2": "working set larger than L2 (no flush needed)"},
+        "e2e": e2e, "roofline": roofline, "kernels": per,
+        "gpu_launches": int(kl.sum()), "clocks": clocks, "mesh_build_s": round(t_mesh, 2),
+    }
+    g.close()
+    return out
+
+
+def cpu_sample(args, n_steps):
+    """The CPU restatement (oracle, OpenMP) on the same mesh and setup: n_steps steps."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_py as op
+    from typhon_gb300 import cases
+    w = cases.WORKLOADS[args.workload]
+    n = args.n or w["n"]
+    raw = cases.make_raw(args.workload, n)
+    from typhon_gb300 import umesh
+    om = op.Mesh.from_raw(raw).build(w["dim"], umesh.periodic_box_bcs((w["length"],) * w["dim"]))
+    sch = {"HLLC": op.SCH_HLLC, "RUSANOV": op.SCH_RUSANOV, "ROE": op.SCH_ROE}[w["scheme"]]
+    hres = {"NONE": op.HRES_NONE, "MUSCL": op.HRES_MUSCL, "MUSCL-FAST": op.HRES_MUSCLFAST,
+            "MUSCL-UNS": op.HRES_MUSCLUNS}[w["highres"]]
+    lim = {"NONE": op.LIM_NONE, "ALBADA": op.LIM_ALBADA}[w["limiter"]]
+    post = {"NONE": op.POSTLIM_NONE, "BARTH": op.POSTLIM_BARTH}[w["postlim"]]
+    s = op.Solver(om, sch, hres, lim, post, op.GRAD_LSQ, rk=w["rk"], cfl=w["cfl"])
+    d = om.export()
+    s.set_prim(cases.initial_prim(args.workload, d["ccentre"]))
+    s.run_steps(1)  # warm (first-touch, LSQ factors)
+    t0 = time.perf_counter()
+    s.run_steps(n_steps)
+    dt = time.perf_counter() - t0
+    cores = os.cpu_count()
+    return {"value": om.ncell_int * n_steps / dt, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+            "sample": f"{n_steps} {w['rk']} step(s) of the full {om.ncell_int}-cell mesh, OpenMP on {cores} "
+                      f"threads ({dt:.1f} s)"}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+        steps = max(1, min(args.steps, 3))
+        cb = cpu_sample(args, steps)
+        out = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": cb["unit"], "n_gpus": world,
+               "steps": steps, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64", "data": "synthetic",
+               "config": {"workload": args.workload, "note": "CPU restatement of Typhon's solver (oracle), "
+                          "Typhon is Fortran and no Fortran compiler is available"},
+               "cpu_baseline": cb,
+               "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+    out = run_ours(args, rank, world, local)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+            out["cpu_baseline"] = cpu_sample(args, args.cpu_sample_steps)
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

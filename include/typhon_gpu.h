@@ -1,0 +1,197 @@
+/*
+ * typhon_gpu.h — C ABI of the GB300 (sm_103a) finite-volume residual-and-update library.
+ *
+ * Drop-in for the explicit hot path of Typhon (Fortran 90 CFD solver, Haider-BA/typhon):
+ * the zone residual, the Runge-Kutta stage and the time step.  Every entry point is
+ * extern "C", takes plain pointers and sizes, and returns an int status (TY_OK = 0,
+ * negative = TY_ERR_*).  Fortran binds it with ISO_C_BINDING, Python with ctypes.
+ *
+ * Conventions
+ *   - A ty_mesh handle owns all device memory; state stays resident on the GPU between
+ *     calls.  One CUDA stream per handle; calls on one handle are not re-entrant, calls on
+ *     different handles are independent.
+ *   - Index arrays are int32.  Arrays "in Typhon layout" are: facecell column-major
+ *     fils(nface,2), 1-based; scalars as separate contiguous arrays; vectors as
+ *     array-of-structs (x,y,z) per element, as st_genericfield stores them
+ *     (CFDTOOLS/Mesh/Field/BASEFIELD.f90:30-54).
+ *   - Conserved variables: rho, rho*E, rho*u (vector); primitive: rho, p, u (vector).
+ *   - Errors that Typhon turns into error_stop (negative internal energy, NaN time step)
+ *     are returned as status codes; the handle stays usable.
+ */
+#ifndef TYPHON_GPU_H
+#define TYPHON_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define TY_OK 0
+#define TY_ERR_ARG -1          /* bad argument (null pointer, size, enum value) */
+#define TY_ERR_CUDA -2         /* CUDA runtime error (message in ty_last_error) */
+#define TY_ERR_NOMEM -3        /* device allocation failed */
+#define TY_ERR_MESH -4         /* inconsistent mesh description */
+#define TY_ERR_NEGENERGY -5    /* negative or NaN internal energy in the time step */
+#define TY_ERR_NANDT -6        /* NaN time step */
+#define TY_ERR_STATE -7        /* call out of order (no state uploaded, no parameters set) */
+#define TY_ERR_UNSUPPORTED -8  /* option not available */
+#define TY_ERR_LSQ -9          /* least-squares matrix not positive definite */
+
+/* ---- option enums (values match the oracle and the Python binding) ---- */
+enum ty_scheme { TY_SCH_HLLC = 1, TY_SCH_RUSANOV = 2, TY_SCH_ROE = 3 };
+enum ty_highres { TY_HRES_NONE = 0, TY_HRES_MUSCL = 1, TY_HRES_MUSCLFAST = 2, TY_HRES_MUSCLUNS = 3 };
+enum ty_limiter {
+  TY_LIM_NONE = 0, TY_LIM_MINMOD = 1, TY_LIM_ALBADA = 2, TY_LIM_VLEER = 3,
+  TY_LIM_SUPERBEE = 4, TY_LIM_KIM3 = 5, TY_LIM_LIM03 = 6
+};
+enum ty_postlim { TY_POSTLIM_NONE = 0, TY_POSTLIM_BARTH = 1, TY_POSTLIM_SUPERBARTH = 2 };
+enum ty_gradmeth { TY_GRAD_NONE = 0, TY_GRAD_LSQ = 1, TY_GRAD_LSQW = 2 };
+enum ty_rk {
+  TY_RK2 = 1, TY_RK2SSP = 2, TY_RK3SSP = 3, TY_RK4 = 4, TY_LSRK25BB = 5, TY_LSRK26BB = 6,
+  TY_LSRK12BS = 7, TY_LSRK13BS = 8
+};
+enum ty_bc { TY_BC_INTERIOR = 0, TY_BC_PERIODIC = 1, TY_BC_SYMMETRY = 2, TY_BC_WALL = 3 };
+/* Arithmetic mode of the kernels.
+ *   TY_MODE_EXACT: every FP64 operation in the order Typhon evaluates it, each rounded
+ *                  separately (no fused multiply-add); results match the CPU restatement
+ *                  bit for bit.
+ *   TY_MODE_FAST:  algebraically rearranged (precomputed reciprocals and reconstruction
+ *                  weights, fused multiply-add); agrees with EXACT to ~1e-13 relative. */
+enum ty_mode { TY_MODE_EXACT = 0, TY_MODE_FAST = 1 };
+
+/* Preprocessed mesh in Typhon's numbering (st_ustmesh after grid_preproc and
+ * init_connect_grid): interior faces first, boundary faces last, one ghost cell per
+ * boundary face numbered after the interior cells.
+ * Replaces the umesh argument of integration_grid (SOURCE/MAIN/integration_grid.f90:8). */
+typedef struct ty_mesh_desc {
+  int32_t dim;              /* 2 (COORD=2D) or 3 */
+  int32_t ncell_int;        /* interior cells */
+  int32_t ncell;            /* interior + ghost cells */
+  int32_t nface_int;        /* interior faces (first in the face list) */
+  int32_t nface;            /* all faces */
+  const int32_t* facecell;  /* [2*nface] fils(nface,2), 1-based, column-major */
+  const double* face_normal;   /* [3*nface] unit normal from cell 1 to cell 2, AoS */
+  const double* face_surface;  /* [nface] */
+  const double* face_centre;   /* [3*nface] AoS */
+  const double* cell_centre;   /* [3*ncell] AoS, ghost cells included */
+  const double* cell_volume;   /* [ncell] */
+  const int32_t* face_color;   /* [nface] colour group of each face (coo_colorgroup,
+                                  0-based); fixes the summation order of the residual */
+  const int32_t* face_bc;      /* [nface] ty_bc kind of each face (0 for interior faces) */
+  const int32_t* face_partner; /* [nface] periodic partner face, 1-based, 0 if none */
+  const double* face_wallvel;  /* [3*nface] wall velocity of wall faces, or NULL */
+} ty_mesh_desc;
+
+typedef struct ty_mesh ty_mesh;
+
+typedef struct ty_spat_params {
+  int32_t scheme;     /* ty_scheme   (SPAT_PARAM:SCHEME) */
+  int32_t highres;    /* ty_highres  (SPAT_PARAM:HIGHRES) */
+  int32_t limiter;    /* ty_limiter  (SPAT_PARAM:LIMITER) */
+  int32_t postlim;    /* ty_postlim  (SPAT_PARAM:POST-LIMITER) */
+  int32_t gradmeth;   /* ty_gradmeth (SPAT_PARAM:GRADMETH) */
+  int32_t mode;       /* ty_mode */
+  double gamma;       /* ratio of specific heats (AIR: 1.4) */
+  double entropy_fix; /* Roe only: Harten fix width as a fraction of the sound speed */
+} ty_spat_params;
+
+/* Version string of the library. */
+const char* ty_version(void);
+/* Text of a status code. */
+const char* ty_error_string(int status);
+/* Detail of the last error on this thread (CUDA message, failing index, ...). */
+const char* ty_last_error(void);
+
+/* Create the device-side mesh: copies the description to HBM and derives the cell->face
+ * gather lists (in colour order), the least-squares factors (precalc_grad_lsq.f90:43-159)
+ * and the per-face reconstruction geometry.  device: CUDA ordinal.
+ * Replaces Typhon's grid set-up consumed by calc_rhs (SOURCE/MAIN/calc_rhs.f90:10). */
+int ty_mesh_create(const ty_mesh_desc* desc, int device, ty_mesh** out);
+int ty_mesh_destroy(ty_mesh* mesh);
+/* Sizes of a device mesh: ncell_int, ncell, nface_int, nface, max faces per cell. */
+int ty_mesh_info(const ty_mesh* mesh, int32_t* out5);
+
+/* Spatial scheme (def_spat.f90:58-313 equivalents). */
+int ty_set_params(ty_mesh* mesh, const ty_spat_params* params);
+
+/* Conserved state in Typhon layout (field%etatcons): rho[ncell_int], rhoE[ncell_int],
+ * rhou[3*ncell_int] (AoS).  Host pointers; the copy is synchronous. */
+int ty_state_upload(ty_mesh* mesh, const double* rho, const double* rhoE, const double* rhou);
+int ty_state_download(ty_mesh* mesh, double* rho, double* rhoE, double* rhou);
+/* Same, SoA device pointers [5][ncell_int] (rho, rhoE, rhou, rhov, rhow) on the handle's
+ * device; stream-ordered on the handle's stream. */
+int ty_state_upload_device(ty_mesh* mesh, const double* cons_soa);
+int ty_state_download_device(ty_mesh* mesh, double* cons_soa);
+/* Primitive variables of the current state [5][ncell_int] (rho, p, u, v, w), host. */
+int ty_prim_download(ty_mesh* mesh, double* prim_soa);
+
+/* Global stability time step (calc_ns_timestep.f90:52-103 + min of
+ * calc_zonetimestep.f90:95): dt = min_c 2 CFL V_c / sum_f S_f / (|u|+a). */
+int ty_timestep(ty_mesh* mesh, double cfl, double* dt_out);
+
+/* One zone residual with a uniform time step dt (calc_rhs explicit part:
+ * calc_varprim, boundary states, gradients, high-order face states, fluxes and
+ * flux_to_res): R = dt/V * sum(+-F S).  Replaces integration_grid
+ * (SOURCE/MAIN/integration_grid.f90:8-121).  R_out: host [5][ncell_int] SoA or NULL. */
+int ty_residual(ty_mesh* mesh, double dt, double* R_out);
+
+/* One explicit Runge-Kutta step of size dt (treelevel_rungekutta.f90:8-113 followed by
+ * update_field.f90:38), state updated in place on the device. */
+int ty_rk_step(ty_mesh* mesh, int32_t rk_method, double dt);
+
+/* nsteps explicit steps, each with the global stability time step at CFL cfl, computed on
+ * the device (no host synchronisation between steps).  dt_last: the last step's dt (host)
+ * or NULL. */
+int ty_rk_steps(ty_mesh* mesh, int32_t rk_method, double cfl, int32_t nsteps, double* dt_last);
+
+/* Debug/parity access to intermediate fields of the last residual evaluation (host):
+ * which = 0 prim [5][ncell], 1 grad [15][ncell], 2 face flux*S [5][nface],
+ *         3 limiter ratios [3][ncell] (Barth post-limiter). */
+int ty_debug_get(ty_mesh* mesh, int32_t which, double* out);
+
+/* Wait for the handle's stream. */
+int ty_synchronize(ty_mesh* mesh);
+
+/* Run the handle's work on the caller's CUDA stream (a cudaStream_t of the handle's
+ * device, e.g. a PyTorch stream), or on the handle's own stream again when stream is NULL.
+ * Waits for work already queued on the previous stream. */
+int ty_set_stream(ty_mesh* mesh, void* stream);
+
+/* Per-kernel CUDA-event timing of every launch issued while enabled (enabling clears the
+ * record).  ty_profile_read returns, per kernel id (0 prim, 1 ghost_prim, 2 grad,
+ * 3 ghost_grad, 4 face_states, 5 barth, 6 face_flux, 7 face_flux_lim, 8 rk_update,
+ * 9 gather, 10 timestep), the summed milliseconds and the number of launches. */
+int ty_profile_enable(ty_mesh* mesh, int32_t on);
+int ty_profile_read(ty_mesh* mesh, int32_t n, double* ms, int32_t* launches);
+
+/* ---------------------------------------------------------------------------------
+ * Host mesh preprocessing (no GPU): builds the ty_mesh_desc arrays from an element mesh
+ * the way Typhon's grid_preproc and init_connect_grid do (face creation and order,
+ * geometry, colouring, ghost cells, periodic matching).  Counterpart of
+ * create_face_connect (CFDTOOLS/Mesh/MESHCONNECT.f90:34), calc_meshgeom
+ * (CFDTOOLS/Mesh/MESHGEOM.f90:421) and coo_colorgroup (CFDTOOLS/Base/COLOR.f90:33). */
+typedef struct ty_umesh ty_umesh;
+int ty_umesh_new(ty_umesh** out);
+int ty_umesh_free(ty_umesh* um);
+/* nodes: [3*nvtex]; element sections (cells of the highest dimension and boundary face
+ * elements) with their element numbers and 1-based vertex lists, as in a .tym file. */
+int ty_umesh_set_nodes(ty_umesh* um, int32_t nvtex, const double* xyz);
+int ty_umesh_add_section(ty_umesh* um, int32_t elemtype, int32_t nelem, const int32_t* ielem,
+                         const int32_t* vtex);
+int ty_umesh_add_mark(ty_umesh* um, const char* family, int32_t ntag, const int32_t* tags);
+/* Boundary definitions, then preprocessing.  kind: ty_bc; periodic families give their
+ * partner family and the translation from this family to the partner. */
+int ty_umesh_add_bc(ty_umesh* um, const char* family, int32_t kind, const char* partner,
+                    const double* translation3, const double* wallvel3);
+int ty_umesh_build(ty_umesh* um, int32_t dim);
+/* Pointers into the built description (valid until ty_umesh_free). */
+int ty_umesh_desc(const ty_umesh* um, ty_mesh_desc* out);
+/* Face -> vertex lists of the built mesh: [nface*4] 1-based, 0 padded. */
+int ty_umesh_facevtex(const ty_umesh* um, int32_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TYPHON_GPU_H */

@@ -78,6 +78,7 @@ void Solver::init(const UMesh* mesh, const SpatParams& p, int rk_method, double 
 void Solver::varprim() {
   const int nc = m->ncell;
   const double g1 = sp.gamma - 1.0;
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nc; ++i) {
     double rho = cons[i];
     V3 vel = v3(cons[2 * nc + i], cons[3 * nc + i], cons[4 * nc + i]) / rho;
@@ -94,6 +95,7 @@ void Solver::varprim() {
 void Solver::varcons() {
   const int nc = m->ncell;
   const double ig1 = 1.0 / (sp.gamma - 1.0);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nc; ++i) {
     double rho = prim[i];
     V3 vel = v3(prim[2 * nc + i], prim[3 * nc + i], prim[4 * nc + i]);
@@ -223,6 +225,7 @@ void Solver::calc_gradient() {
   if (!gradcond_ok) precalc_grad_lsq();
   const int nc = m->ncell, nci = m->ncell_int, nf = m->nface, nfi = m->nface_int;
   std::vector<V3> dcg(nf);
+#pragma omp parallel for schedule(static)
   for (int f = 0; f < nf; ++f) {
     V3 d = m->ccentre[m->fc2[f]] - m->ccentre[m->fc1[f]];
     if (sp.gradmeth == GRAD_LSQW) {
@@ -233,8 +236,10 @@ void Solver::calc_gradient() {
   }
   // rhs(1:3, ic*dim + dec), dim = 5: per cell a column-major 3x5 block
   std::vector<double> rhs(15 * (size_t)nci, 0.0);
-  for (auto& col : m->colors)
-    for (int f : col) {
+  for (auto& col : m->colors)  // faces of one colour touch distinct cells
+#pragma omp parallel for schedule(static)
+    for (size_t q = 0; q < col.size(); ++q) {
+      const int f = col[q];
       int i1 = m->fc1[f], i2 = m->fc2[f];
       for (int v = 0; v < 5; ++v) {
         double dsca = prim[v * nc + i2] - prim[v * nc + i1];
@@ -250,8 +255,10 @@ void Solver::calc_gradient() {
         }
       }
     }
+#pragma omp parallel for schedule(static)
   for (int c = 0; c < nci; ++c) cholesky_solve(&gradcond[9 * (size_t)c], &rhs[15 * (size_t)c], 5);
   // grad%tabvect(is) for rho, p; grad%tabtens(1)%mat(i, 1:3) = rhs(1:3, nscal + i)
+#pragma omp parallel for schedule(static)
   for (int c = 0; c < nci; ++c)
     for (int v = 0; v < 5; ++v)
       for (int k = 0; k < 3; ++k) grad[(3 * v + k) * (size_t)nc + c] = rhs[15 * (size_t)c + 3 * v + k];
@@ -329,6 +336,7 @@ static double apply_lim(int lim, bool uns, bool arrayform, double g, double LR) 
 
 void Solver::hres_states() {
   const int nc = m->ncell, nf = m->nface;
+#pragma omp parallel for schedule(static)
   for (int f = 0; f < nf; ++f) {
     const int icl = m->fc1[f], icr = m->fc2[f];
     if (sp.highres == HRES_NONE) {  // distrib_field.f90
@@ -441,12 +449,16 @@ void Solver::postlimit_barth(double klim) {
   };
   for (int s = 0; s < 2; ++s) {
     std::fill(ratio.begin(), ratio.end(), 1.0);
-    for (int f = 0; f < nf; ++f) {
+    for (auto& col : m->colors)  // min is order-independent; a colour's faces touch distinct cells
+#pragma omp parallel for schedule(static)
+    for (size_t q = 0; q < col.size(); ++q) {
+      const int f = col[q];
       int icl = m->fc1[f], icr = m->fc2[f];
       double LR = prim[s * nc + icr] - prim[s * nc + icl];
       constrain(icl, LR, cell_l[s * nf + f] - prim[s * nc + icl]);
       constrain(icr, -LR, cell_r[s * nf + f] - prim[s * nc + icr]);
     }
+#pragma omp parallel for schedule(static)
     for (int f = 0; f < nf; ++f) {
       int icl = m->fc1[f], icr = m->fc2[f];
       cell_l[s * nf + f] = prim[s * nc + icl] + ratio[icl] * (cell_l[s * nf + f] - prim[s * nc + icl]);
@@ -455,7 +467,10 @@ void Solver::postlimit_barth(double klim) {
     for (int c = 0; c < nc; ++c) limratio[s * nc + c] = ratio[c];
   }
   std::fill(ratio.begin(), ratio.end(), 1.0);
-  for (int f = 0; f < nf; ++f) {
+  for (auto& col : m->colors)
+#pragma omp parallel for schedule(static)
+  for (size_t q = 0; q < col.size(); ++q) {
+    const int f = col[q];
     int icl = m->fc1[f], icr = m->fc2[f];
     for (int k = 0; k < 3; ++k) {
       double LR = prim[(2 + k) * nc + icr] - prim[(2 + k) * nc + icl];
@@ -466,6 +481,7 @@ void Solver::postlimit_barth(double klim) {
       constrain(icr, -LR, cell_r[(2 + k) * nf + f] - prim[(2 + k) * nc + icr]);
     }
   }
+#pragma omp parallel for schedule(static)
   for (int f = 0; f < nf; ++f) {
     int icl = m->fc1[f], icr = m->fc2[f];
     for (int k = 0; k < 3; ++k) {
@@ -544,6 +560,7 @@ void Solver::face_fluxes() {
   const int nf = m->nface;
   const double g = sp.gamma;
   const double ig1 = 1.0 / (g - 1.0);
+#pragma omp parallel for schedule(static)
   for (int f = 0; f < nf; ++f) {
     State L = face_state(cell_l, nf, f), R = face_state(cell_r, nf, f);
     V3 fn = m->fnormal[f];
@@ -623,17 +640,21 @@ void Solver::face_fluxes() {
 // flux_to_res.f90:47-144: F *= S, colour-ordered scatter, R *= dtloc/V (interior cells)
 void Solver::flux_to_res() {
   const int nc = m->ncell, nci = m->ncell_int, nf = m->nface;
-  for (int v = 0; v < 5; ++v)
-    for (int f = 0; f < nf; ++f) flux[v * nf + f] = m->fsurf[f] * flux[v * nf + f];
+#pragma omp parallel for schedule(static)
+  for (int f = 0; f < nf; ++f)
+    for (int v = 0; v < 5; ++v) flux[v * nf + f] = m->fsurf[f] * flux[v * nf + f];
   std::fill(residu.begin(), residu.end(), 0.0);
-  for (auto& col : m->colors)
-    for (int f : col) {
+  for (auto& col : m->colors)  // faces of one colour touch distinct cells
+#pragma omp parallel for schedule(static)
+    for (size_t q = 0; q < col.size(); ++q) {
+      const int f = col[q];
       int i1 = m->fc1[f], i2 = m->fc2[f];
       for (int v = 0; v < 5; ++v) {
         residu[v * nc + i1] = residu[v * nc + i1] - flux[v * nf + f];
         residu[v * nc + i2] = residu[v * nc + i2] + flux[v * nf + f];
       }
     }
+#pragma omp parallel for schedule(static)
   for (int c = 0; c < nci; ++c) {
     double coef = dtloc[c] / m->cvol[c];
     for (int v = 0; v < 5; ++v) residu[v * nc + c] = coef * residu[v * nc + c];
@@ -662,24 +683,28 @@ double Solver::timestep() {
   const double gg1 = sp.gamma * (sp.gamma - 1.0);
   std::vector<double> sumS(nci, 0.0);
   for (auto& col : m->colors)
-    for (int f : col) {
+#pragma omp parallel for schedule(static)
+    for (size_t q = 0; q < col.size(); ++q) {
+      const int f = col[q];
       int i1 = m->fc1[f], i2 = m->fc2[f];
       sumS[i1] = sumS[i1] + m->fsurf[f];
       if (i2 < nci) sumS[i2] = sumS[i2] + m->fsurf[f];
     }
   double dt = std::numeric_limits<double>::max();
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(min : dt) reduction(max : bad)
   for (int c = 0; c < nci; ++c) {
     double d = cfl * 2.0 * m->cvol[c] / sumS[c];
     double irho = 1.0 / cons[c];
     double rv2 = cons[2 * nc + c] * cons[2 * nc + c] + cons[3 * nc + c] * cons[3 * nc + c] +
                  cons[4 * nc + c] * cons[4 * nc + c];
     double a2 = (cons[nc + c] - 0.5 * rv2 * irho) * gg1 * irho;
-    if (!(a2 > 0.0)) return -1.0;  // negative or NaN internal energy
+    if (!(a2 > 0.0)) { bad = 1; continue; }  // negative or NaN internal energy
     d = d / (std::sqrt(rv2) * irho + std::sqrt(a2));
     dtloc[c] = d;
     dt = std::min(dt, d);
   }
-  return dt;
+  return bad ? -1.0 : dt;
 }
 
 // treelevel_rungekutta.f90:48-113 then update_field.f90:38 (U += residu) with a global dt
@@ -694,20 +719,26 @@ void Solver::rk_step(double dt) {
       cons = u0;
       for (int s = 1; s <= i - 1; ++s) {
         double c = rk.c(i - 1, s);
-        for (size_t k = 0; k < cons.size(); ++k) cons[k] = cons[k] + c * rhs[s - 1][k];
+        const size_t nk = cons.size();
+#pragma omp parallel for schedule(static)
+        for (size_t k = 0; k < nk; ++k) cons[k] = cons[k] + c * rhs[s - 1][k];
       }
     }
     calc_rhs();
     rhs[i - 1] = residu;
   }
   // residu = coef(n,1)*rhs1 + sum coef(n,s)*rhs_s   (scale then xeqxpay)
-  for (size_t k = 0; k < residu.size(); ++k) residu[k] = rk.c(n, 1) * rhs[0][k];
+  const size_t nk = residu.size();
+#pragma omp parallel for schedule(static)
+  for (size_t k = 0; k < nk; ++k) residu[k] = rk.c(n, 1) * rhs[0][k];
   for (int s = 2; s <= n; ++s) {
     double c = rk.c(n, s);
-    for (size_t k = 0; k < residu.size(); ++k) residu[k] = residu[k] + c * rhs[s - 1][k];
+#pragma omp parallel for schedule(static)
+    for (size_t k = 0; k < nk; ++k) residu[k] = residu[k] + c * rhs[s - 1][k];
   }
   cons = u0;
-  for (size_t k = 0; k < cons.size(); ++k) cons[k] = cons[k] + residu[k];
+#pragma omp parallel for schedule(static)
+  for (size_t k = 0; k < nk; ++k) cons[k] = cons[k] + residu[k];
   (void)nc;
 }
 

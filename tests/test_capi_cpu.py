@@ -1,0 +1,126 @@
+"""CPU checks of the C ABI library: it loads, exports every declared entry point, its
+native mesh preprocessing reproduces Typhon's (the oracle's) arrays bit for bit, the
+.tym reader/writer round-trips, and argument errors come back as status codes."""
+import ctypes as C
+import pathlib
+import re
+
+import numpy as np
+import pytest
+
+import oracle_py as op
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def ty():
+    from typhon_gb300 import build
+    build.build()
+    import typhon_gb300
+    return typhon_gb300
+
+
+def declared_entry_points():
+    text = (ROOT / "include" / "typhon_gpu.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(ty_\w+)\s*\(", text, re.M)))
+
+
+def test_exports_every_declared_symbol(ty):
+    from typhon_gb300 import _capi
+    lib = _capi.lib()
+    names = declared_entry_points()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(_capi.exported_names())
+    assert lib.ty_version().decode().startswith("typhon_gb300")
+
+
+def test_argument_errors_without_gpu(ty):
+    from typhon_gb300 import _capi
+    lib = _capi.lib()
+    h = C.c_void_p()
+    assert lib.ty_mesh_create(None, 0, C.byref(h)) == -1
+    assert lib.ty_set_params(None, None) == -1
+    assert lib.ty_error_string(-5).decode() == "negative or NaN internal energy"
+    d = _capi.MeshDesc()
+    d.dim = 4
+    assert lib.ty_mesh_create(C.byref(d), 0, C.byref(h)) == -1
+
+
+def _same(md, d):
+    return {
+        "fc1": np.array_equal(md.fc1, d["fc1"]), "fc2": np.array_equal(md.fc2, d["fc2"]),
+        "normal": np.array_equal(md.face_normal, d["fnormal"]),
+        "fcentre": np.array_equal(md.face_centre, d["fcentre"]),
+        "surface": np.array_equal(md.face_surface, d["fsurf"]),
+        "centre": np.array_equal(md.cell_centre, d["ccentre"]),
+        "volume": np.array_equal(md.cell_volume, d["cvol"]),
+        "colour": np.array_equal(md.face_color, d["face_color"]),
+        "partner": np.array_equal(md.face_partner - 1, d["face_partner"]),
+        "bc": np.array_equal(md.face_bc, d["face_bckind"]),
+    }
+
+
+def test_preprocess_quad20_matches_oracle(ty, golden_dir):
+    raw = ty.read_tym(golden_dir / "quad20x20.tym")
+    md = ty.preprocess(raw, 2, ty.periodic_box_bcs((1.0, 1.0)))
+    d = op.Mesh.from_tym(golden_dir / "quad20x20.tym").build(2, op.PERIODIC_UNIT_SQUARE).export()
+    assert all(_same(md, d).values()), _same(md, d)
+
+
+def test_preprocess_symmetry_quad20x10_matches_oracle(ty, golden_dir):
+    bcs = [(f, op.BC_SYMMETRY, "", (0, 0, 0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX")]
+    raw = ty.read_tym(golden_dir / "quad20x10.tym")
+    md = ty.preprocess(raw, 2, bcs)
+    d = op.Mesh.from_tym(golden_dir / "quad20x10.tym").build(2, bcs).export()
+    assert all(_same(md, d).values()), _same(md, d)
+
+
+@pytest.mark.parametrize("n", [8, 64])
+def test_preprocess_vortex_mesh_matches_oracle(ty, n):
+    raw = ty.gen_grid2d(n, n, 10.0, 10.0, "tri", jitter=0.1, seed=1234)
+    md = ty.preprocess(raw, 2, ty.periodic_box_bcs((10.0, 10.0)))
+    d = op.Mesh.from_raw(raw).build(2, ty.periodic_box_bcs((10.0, 10.0))).export()
+    assert all(_same(md, d).values()), _same(md, d)
+    if n == 64:  # the configuration's sizes: 8192 triangles, 12416 faces, 256 periodic faces
+        assert (md.ncell_int, md.nface, md.nface - md.nface_int) == (8192, 12416, 256)
+
+
+@pytest.mark.parametrize("n", [4, 6])
+def test_preprocess_tet_box_matches_oracle(ty, n):
+    L = 2 * np.pi
+    raw = ty.gen_tet_box(n, L, jitter=0.05, seed=1234)
+    md = ty.preprocess(raw, 3, ty.periodic_box_bcs((L, L, L)))
+    d = op.Mesh.from_raw(raw).build(3, ty.periodic_box_bcs((L, L, L))).export()
+    assert all(_same(md, d).values()), _same(md, d)
+    assert md.ncell_int == 5 * n ** 3
+    assert abs(md.cell_volume[:md.ncell_int].sum() - L ** 3) < 1e-9 * L ** 3
+
+
+def test_tym_roundtrip(ty, tmp_path):
+    raw = ty.gen_grid2d(6, 5, 3.0, 2.0, "quad")
+    p = tmp_path / "m.tym"
+    ty.write_tym(p, raw)
+    back = ty.read_tym(p)
+    assert np.array_equal(back.vtex, raw.vtex)
+    for a, b in zip(back.sections, raw.sections):
+        assert a[0] == b[0] and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+    assert [m[0] for m in back.marks] == [m[0] for m in raw.marks]
+    # the oracle's independent reader agrees
+    m = op.Mesh.from_tym(p).build(2, [("IMIN", op.BC_PERIODIC, "IMAX", (3.0, 0, 0)),
+                                      ("JMIN", op.BC_PERIODIC, "JMAX", (0, 2.0, 0))])
+    assert m.ncell_int == 30
+
+
+def test_golden_mesh_reader_agrees(ty, golden_dir):
+    for name in ("quad20x20.tym", "quad10x10.tym", "tri5x10.tym", "mxlay2x20quad-h50.tym"):
+        raw = ty.read_tym(golden_dir / name)
+        assert raw.ncell > 0 and raw.vtex.shape[1] == 3
+
+
+def test_bad_mesh_is_rejected(ty):
+    raw = ty.gen_grid2d(4, 4, 1.0, 1.0, "quad")
+    with pytest.raises(ty.TyphonError):
+        ty.preprocess(raw, 2, [("IMIN", 1, "IMAX", (1.0, 0, 0))])   # JMIN/JMAX undefined

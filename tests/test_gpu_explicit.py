@@ -1,0 +1,244 @@
+"""GPU parity of the explicit path (through the C ABI) against the CPU oracle.
+
+Exact mode (TY_MODE_EXACT) must reproduce the oracle bit for bit: gradients, face fluxes,
+residuals and Runge-Kutta states.  Fast mode must stay within 1e-12 relative L2 per
+conserved variable (the tolerance of the FP64 explicit path).  The Typhon golden monitor
+files are replayed through the GPU as well.
+"""
+import numpy as np
+import pytest
+
+import oracle_py as op
+
+pytestmark = pytest.mark.gpu
+
+FAST_RTOL = 1e-12   # relative L2 per conserved variable, fast mode vs oracle
+
+OSCH = {"HLLC": op.SCH_HLLC, "RUSANOV": op.SCH_RUSANOV, "ROE": op.SCH_ROE}
+OHRES = {"NONE": op.HRES_NONE, "MUSCL": op.HRES_MUSCL, "MUSCL-FAST": op.HRES_MUSCLFAST,
+         "MUSCL-UNS": op.HRES_MUSCLUNS}
+OLIM = {"NONE": op.LIM_NONE, "MINMOD": op.LIM_MINMOD, "ALBADA": op.LIM_ALBADA, "VAN_LEER": op.LIM_VLEER,
+        "SUPERBEE": op.LIM_SBEE, "KIM3": op.LIM_KIM3, "LIM03": op.LIM_LIM03}
+OPOST = {"NONE": op.POSTLIM_NONE, "BARTH": op.POSTLIM_BARTH, "SUPERBARTH": op.POSTLIM_SUPERBARTH}
+
+
+@pytest.fixture(scope="module")
+def ty():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from typhon_gb300 import build
+    build.build()
+    import typhon_gb300
+    return typhon_gb300
+
+
+def make_case(ty, kind, n):
+    from typhon_gb300 import cases
+    if kind == "vortex":
+        raw = ty.gen_grid2d(n, n, 10.0, 10.0, "tri", jitter=0.1, seed=1234)
+        bcs = ty.periodic_box_bcs((10.0, 10.0))
+        md = ty.preprocess(raw, 2, bcs)
+        prim = cases.isentropic_vortex(md.cell_centre)
+        dim = 2
+    elif kind == "tgv":
+        L = 2 * np.pi
+        raw = ty.gen_tet_box(n, L, jitter=0.05, seed=1234)
+        bcs = ty.periodic_box_bcs((L, L, L))
+        md = ty.preprocess(raw, 3, bcs)
+        prim = cases.taylor_green(md.cell_centre)
+        dim = 3
+    else:
+        raise ValueError(kind)
+    om = op.Mesh.from_raw(raw).build(dim, bcs)
+    return md, om, prim
+
+
+def pair(ty, md, om, prim, scheme, highres, limiter, postlim="NONE", mode="exact", rk="RK4", cfl=0.8):
+    gm = "NONE" if highres == "NONE" else "LSQ"
+    g = ty.Grid(md)
+    g.set_spat(scheme, highres, limiter, postlim, gradmeth=gm, mode=mode)
+    g.set_prim(prim)
+    s = op.Solver(om, OSCH[scheme], OHRES[highres], OLIM[limiter], OPOST[postlim],
+                  op.GRAD_NONE if gm == "NONE" else op.GRAD_LSQ, rk=rk, cfl=cfl)
+    s.set_prim(prim)
+    return g, s
+
+
+def relerr(a, b):
+    return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+
+
+COMBOS = [
+    ("HLLC", "MUSCL-FAST", "ALBADA", "NONE"),
+    ("HLLC", "MUSCL", "ALBADA", "NONE"),
+    ("HLLC", "MUSCL-UNS", "MINMOD", "NONE"),
+    ("RUSANOV", "NONE", "NONE", "NONE"),
+    ("HLLC", "NONE", "NONE", "NONE"),
+    ("ROE", "MUSCL-UNS", "NONE", "BARTH"),
+    ("ROE", "MUSCL-FAST", "VAN_LEER", "NONE"),
+    ("HLLC", "MUSCL", "SUPERBEE", "SUPERBARTH"),
+    ("RUSANOV", "MUSCL-FAST", "KIM3", "NONE"),
+    ("HLLC", "MUSCL-FAST", "LIM03", "NONE"),
+]
+
+
+@pytest.mark.parametrize("kind,n", [("vortex", 12), ("tgv", 4)])
+@pytest.mark.parametrize("combo", COMBOS, ids=["-".join(c) for c in COMBOS])
+def test_exact_residual_bitwise(ty, kind, n, combo):
+    md, om, prim = make_case(ty, kind, n)
+    g, s = pair(ty, md, om, prim, *combo)
+    dt = s.timestep()
+    assert g.calc_zonetimestep(0.8) == dt
+    R = g.integration_grid(dt)
+    s.rhs(dt)
+    nci = md.ncell_int
+    if combo[1] != "NONE":
+        gg, sg = g.debug("grad"), s.get("grad")
+        assert np.array_equal(gg[:, :nci], sg[:, :nci]), "gradient"
+    assert np.array_equal(g.debug("flux"), s.get("flux")), "face flux"
+    assert np.array_equal(R, s.get("residu")[:, :nci]), "residual"
+
+
+@pytest.mark.parametrize("rk", ["RK2", "RK2-SSP", "RK3-SSP", "RK4", "RK25BB", "RK26BB", "RK12BS", "RK13BS"])
+def test_exact_rk_steps_bitwise(ty, rk):
+    md, om, prim = make_case(ty, "vortex", 16)
+    g, s = pair(ty, md, om, prim, "HLLC", "MUSCL-FAST", "ALBADA", rk=rk)
+    for _ in range(3):
+        dt = s.timestep()
+        assert g.calc_zonetimestep(0.8) == dt
+        g.treelevel_rungekutta(rk, dt)
+        s.rk_step(dt)
+    assert np.array_equal(g.get_cons(), s.get("cons")[:, :md.ncell_int])
+
+
+def test_exact_tgv_barth_roe_steps_bitwise(ty):
+    md, om, prim = make_case(ty, "tgv", 6)
+    g, s = pair(ty, md, om, prim, "ROE", "MUSCL-UNS", "NONE", "BARTH", rk="RK3-SSP")
+    for _ in range(3):
+        dt = s.timestep()
+        g.treelevel_rungekutta("RK3-SSP", dt)
+        s.rk_step(dt)
+    assert np.array_equal(g.get_cons(), s.get("cons")[:, :md.ncell_int])
+
+
+def test_device_timestep_loop_matches_host_loop(ty):
+    md, om, prim = make_case(ty, "vortex", 16)
+    g1, s = pair(ty, md, om, prim, "HLLC", "MUSCL-FAST", "ALBADA")
+    g2 = ty.Grid(md)
+    g2.set_spat("HLLC", "MUSCL-FAST", "ALBADA", mode="exact")
+    g2.set_prim(prim)
+    for _ in range(4):
+        g1.treelevel_rungekutta("RK4", g1.calc_zonetimestep(0.8))
+    dt_last = g2.run_steps("RK4", 0.8, 4)
+    dts = s.run_steps(4)
+    assert dt_last == dts[-1]
+    assert np.array_equal(g1.get_cons(), g2.get_cons())
+    assert np.array_equal(g2.get_cons(), s.get("cons")[:, :md.ncell_int])
+
+
+def test_fast_mode_vortex_full_size(ty):
+    """The 2D vortex configuration at its full size (8192 triangles): 20 RK4 steps."""
+    md, om, prim = make_case(ty, "vortex", 64)
+    g, s = pair(ty, md, om, prim, "HLLC", "MUSCL", "ALBADA", mode="fast")
+    g.run_steps("RK4", 0.8, 20)
+    s.run_steps(20)
+    rel = relerr(g.get_cons(), s.get("cons")[:, :md.ncell_int])
+    assert np.all(rel <= FAST_RTOL), rel
+
+
+def test_fast_mode_tgv_small(ty):
+    md, om, prim = make_case(ty, "tgv", 8)
+    g, s = pair(ty, md, om, prim, "ROE", "MUSCL-UNS", "NONE", "BARTH", mode="fast", rk="RK3-SSP")
+    g.run_steps("RK3-SSP", 0.8, 5)
+    s.run_steps(5)
+    rel = relerr(g.get_cons(), s.get("cons")[:, :md.ncell_int])
+    assert np.all(rel <= FAST_RTOL), rel
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+def test_runs_are_deterministic(ty, mode):
+    md, om, prim = make_case(ty, "tgv", 6)
+    outs = []
+    for _ in range(2):
+        g = ty.Grid(md)
+        g.set_spat("ROE", "MUSCL-UNS", "NONE", "BARTH", mode=mode)
+        g.set_prim(prim)
+        g.run_steps("RK3-SSP", 0.8, 3)
+        outs.append(g.get_cons())
+        g.close()
+    assert np.array_equal(outs[0], outs[1])
+
+
+def _print_ulp(v):
+    return 10.0 ** (np.floor(np.log10(np.abs(v))) - 7)
+
+
+@pytest.mark.parametrize("case,method,cfl", [("RK4", "RK4", 2.0), ("RK3-SSP", "RK3-SSP", 1.5),
+                                             ("RK25BB", "RK25BB", 2.5)])
+def test_nrg_rungekutta_replayed_on_gpu(ty, golden_dir, case, method, cfl):
+    """NRG/TIME/RUNGEKUTTA/<case>: the Typhon golden RHOERR monitor, computed from the GPU
+    state (exact mode) after each of the 100 cycles."""
+    raw = ty.read_tym(golden_dir / "quad20x20.tym")
+    md = ty.preprocess(raw, 2, ty.periodic_box_bcs((1.0, 1.0)))
+    c = md.cell_centre
+    s_ = np.sin(2 * np.pi * c[:, 0]) * np.sin(2 * np.pi * c[:, 1])
+    prim = np.stack([1 + (s_ * s_) / 2, np.full(len(c), 100000 / 14.), np.full(len(c), 50.),
+                     np.zeros(len(c)), np.zeros(len(c))])
+    g = ty.Grid(md)
+    g.set_spat("HLLC", "MUSCL-FAST", "ALBADA", mode="exact")
+    g.set_prim(prim)
+    nci = md.ncell_int
+    vol = md.cell_volume[:nci]
+    x, y = c[:nci, 0], c[:nci, 1]
+    out = []
+    t = 0.0
+    for _ in range(100):
+        g.integration_cyclezone(method, cfl, 0.1 / 100)
+        t = t + 0.1 / 100
+        rho = g.get_prim()[0]
+        e = np.sin(2 * np.pi * (x - 50 * t)) * np.sin(2 * np.pi * y)
+        out.append(np.sum((rho - (1 + e * e / 2)) ** 2 * vol) / np.sum(vol))
+    gold = np.loadtxt(golden_dir / f"{case}__RHOERR.tmon")[:, 2]
+    err = np.abs(np.array(out) - gold) / _print_ulp(gold)
+    assert err.max() <= 0.5 + 1e-3, err.max()
+
+
+def test_nrg_per2d_trans_replayed_on_gpu(ty, golden_dir):
+    raw = ty.read_tym(golden_dir / "quad20x20.tym")
+    md = ty.preprocess(raw, 2, ty.periodic_box_bcs((1.0, 1.0)))
+    c = md.cell_centre
+    x, y = c[:, 0], c[:, 1]
+    prim = np.stack([1. + 9 * x * (x - 1) * y * (y - 1), np.full(len(c), 100000 / 14.), np.full(len(c), 10.),
+                     np.zeros(len(c)), np.zeros(len(c))])
+    g = ty.Grid(md)
+    g.set_spat("RUSANOV", "NONE", mode="exact")
+    g.set_prim(prim)
+    vol = md.cell_volume[:md.ncell_int]
+    out = []
+    for _ in range(100):
+        g.integration_cyclezone("RK3-SSP", 1.0, 0.001)
+        rho = g.get_prim()[0]
+        out.append(np.sum((rho - 1.25) ** 2 * vol) / np.sum(vol))
+    gold = np.loadtxt(golden_dir / "PER2D-TRANS__RHODEV.tmon")[:, 2]
+    err = np.abs(np.array(out) - gold) / _print_ulp(gold)
+    assert err.max() <= 0.5 + 1e-3, err.max()
+
+
+def test_negative_energy_is_reported_and_handle_survives(ty):
+    md, om, prim = make_case(ty, "vortex", 8)
+    g = ty.Grid(md)
+    g.set_spat("HLLC", "MUSCL-FAST", "ALBADA", mode="fast")
+    bad = prim.copy()
+    bad[1, 5] = -1.0
+    g.set_prim(bad)
+    with pytest.raises(ty.TyphonError) as e:
+        g.calc_zonetimestep(0.8)
+    assert e.value.status == -5
+    g.set_prim(prim)
+    assert g.calc_zonetimestep(0.8) > 0
+
+
+def test_smoke_entry():
+    import __graft_entry__ as ge
+    ge.smoke()

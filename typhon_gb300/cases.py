@@ -1,0 +1,70 @@
+"""Synthetic workloads: meshes and initial conditions of the benchmark configurations.
+
+  vortex2d   2D Euler isentropic vortex (strength 5, M_inf = 0.5, gamma = 1.4) on the
+             periodic [0,10]^2 box, 64x64 quads split into 8192 triangles, interior nodes
+             jittered by +-10% of h (seed 1234); HLLC + MUSCL + van Albada, RK4, CFL 0.8.
+  tgv3d      3D Euler Taylor-Green vortex (M = 0.1, gamma = 1.4) on the periodic
+             [0,2 pi]^3 box, 64^3 hexahedra split into 5 tetrahedra (1,310,720 cells),
+             interior nodes jittered by +-5% of h (seed 1234); least-squares gradients,
+             MUSCL-UNS with the Barth post-limiter, Roe flux, SSP-RK3.
+Both are nondimensional (rho_inf = 1).  The initial states are evaluated at cell centres.
+"""
+import numpy as np
+
+from . import umesh
+
+
+def isentropic_vortex(xy, xc=5.0, yc=5.0, beta=5.0, mach=0.5, gamma=1.4):
+    """Primitive state (rho, p, u, v, w) of the isentropic vortex of strength beta advected at
+    Mach `mach` along x (free stream rho = p = 1)."""
+    x, y = xy[:, 0] - xc, xy[:, 1] - yc
+    r2 = x * x + y * y
+    e = np.exp(0.5 * (1.0 - r2))
+    uinf = mach * np.sqrt(gamma)
+    du = -beta / (2 * np.pi) * y * e
+    dv = beta / (2 * np.pi) * x * e
+    T = 1.0 - (gamma - 1.0) * beta * beta / (8.0 * gamma * np.pi * np.pi) * e * e
+    rho = T ** (1.0 / (gamma - 1.0))
+    p = rho * T
+    return np.stack([rho, p, uinf + du, dv, np.zeros_like(x)])
+
+
+def taylor_green(xyz, mach=0.1, gamma=1.4):
+    """Primitive state of the Taylor-Green vortex (V0 = rho0 = 1, p0 = 1/(gamma M^2),
+    isothermal density rho = p / p0)."""
+    x, y, z = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+    p0 = 1.0 / (gamma * mach * mach)
+    u = np.sin(x) * np.cos(y) * np.cos(z)
+    v = -np.cos(x) * np.sin(y) * np.cos(z)
+    p = p0 + (np.cos(2 * x) + np.cos(2 * y)) * (np.cos(2 * z) + 2.0) / 16.0
+    rho = p / p0
+    return np.stack([rho, p, u, v, np.zeros_like(x)])
+
+
+WORKLOADS = {
+    "vortex2d": dict(dim=2, n=64, length=10.0, jitter=0.10, seed=1234, scheme="HLLC", highres="MUSCL",
+                     limiter="ALBADA", postlim="NONE", rk="RK4", cfl=0.8, steps=200),
+    "tgv3d": dict(dim=3, n=64, length=2 * np.pi, jitter=0.05, seed=1234, scheme="ROE", highres="MUSCL-UNS",
+                  limiter="NONE", postlim="BARTH", rk="RK3-SSP", cfl=0.8, steps=500),
+}
+
+
+def make_raw(name, n=None):
+    w = WORKLOADS[name]
+    n = n or w["n"]
+    if w["dim"] == 2:
+        return umesh.gen_grid2d(n, n, w["length"], w["length"], "tri", jitter=w["jitter"], seed=w["seed"])
+    return umesh.gen_tet_box(n, w["length"], jitter=w["jitter"], seed=w["seed"])
+
+
+def make_mesh(name, n=None):
+    """Preprocessed mesh of a workload (native preprocessing)."""
+    w = WORKLOADS[name]
+    raw = make_raw(name, n)
+    return umesh.preprocess(raw, w["dim"], umesh.periodic_box_bcs((w["length"],) * w["dim"]))
+
+
+def initial_prim(name, centres):
+    if name == "vortex2d":
+        return isentropic_vortex(centres)
+    return taylor_green(centres)

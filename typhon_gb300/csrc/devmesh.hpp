@@ -1,0 +1,143 @@
+// Device-resident mesh and state of one ty_mesh handle (plain struct of device pointers,
+// passed by value to the kernels).  Layout: structure-of-arrays, one contiguous FP64
+// array per component, cells padded to a multiple of 32 so that every component starts
+// 256-byte aligned.
+//
+//   cells  0 .. nci-1        interior cells (Typhon's numbering)
+//          nci .. nc-1       ghost cells, one per boundary face
+//   faces  0 .. nfi-1        interior faces, nfi .. nf-1 boundary faces
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace tyk {
+
+constexpr int kMaxSlot = 8;    // faces per cell held in the gather list (hexahedra need 6)
+constexpr int kMaxStage = 6;   // Runge-Kutta stages
+
+struct DevMesh {
+  int dim = 0, nci = 0, nc = 0, nfi = 0, nf = 0, ng = 0, nslot = 0;
+  int ldc = 0;  // leading dimension of cell arrays (>= nc, multiple of 32)
+  int ldf = 0;  // leading dimension of face arrays (>= nf, multiple of 32)
+  // connectivity
+  const int* fc1 = nullptr;    // [nf] cell on the normal's tail
+  const int* fc2 = nullptr;    // [nf] cell on the normal's head (ghost for boundary faces)
+  const int* fbc = nullptr;    // [nf] ty_bc kind
+  const int* part = nullptr;   // [nf] periodic partner face or -1
+  const int* cf = nullptr;     // [nslot][nci] (face << 1 | side), side 1 = cell is fc2; -1 pad;
+                               // slots in Typhon's colour order (summation order)
+  const int* gsrc = nullptr;   // [ng] interior cell that feeds each ghost
+  const int* gface = nullptr;  // [ng] boundary face of each ghost
+  // geometry
+  const double* fn = nullptr;     // [3][ldf] unit normal
+  const double* fs = nullptr;     // [ldf] surface
+  const double* fwall = nullptr;  // [3][ldf] wall velocity
+  const double* cvol = nullptr;   // [ldc]
+  const double* sumS = nullptr;   // [nci] sum of face surfaces, colour order (time step)
+  const double* dcg = nullptr;    // [3][ldf] centre(fc2) - centre(fc1) (LSQ, weighted for W-LSQ)
+  const double* lsq = nullptr;    // [6][nci] Cholesky factor L11 L21 L31 L22 L32 L33
+  const double* lsqw = nullptr;   // [6][ldf] fast mode: per face, A^-1 d for fc1 (0..2), fc2 (3..5)
+  const double* uLR = nullptr;    // [3][ldf] MUSCL direction (unit for MUSCL/-UNS, 1/dLR-scaled for FAST)
+  const double* dLR = nullptr;    // [ldf]
+  const double* kLF = nullptr;    // [ldf] MUSCL-FAST |F - C_L|
+  const double* kRF = nullptr;    // [ldf] MUSCL-FAST -|F - C_R|
+  const double* LF = nullptr;     // [3][ldf] MUSCL/-UNS F - C_L
+  const double* RF = nullptr;     // [3][ldf] MUSCL/-UNS F - C_R
+  const double* recw = nullptr;   // [8][ldf] fast MUSCL-UNS/MUSCL, no limiter: per side w (3), k (1)
+};
+
+struct DevState {
+  double* u0 = nullptr;    // [5][ldc] state at the start of the step (the solution between steps)
+  double* cur = nullptr;   // [5][ldc] state of the current stage
+  double* acc = nullptr;   // [5][ldc] Runge-Kutta combination sum coef(n,s) rhs_s
+  double* pk[kMaxStage + 1] = {};  // [5][ldc] partial sums of later stage states
+  double* prim = nullptr;  // [5][ldc] rho, p, u, v, w (ghosts included)
+  double* grad = nullptr;  // [15][ldc] grad rho, grad p, du_i/dx_j (row i)
+  double* cl = nullptr;    // [5][ldf] face states (post-limiter path)
+  double* cr = nullptr;    // [5][ldf]
+  double* ratio = nullptr; // [3][ldc] post-limiter ratios (rho, p, velocity)
+  double* flux = nullptr;  // [5][ldf] face flux times surface
+  double* res = nullptr;   // [5][ldc] residual of ty_residual
+  unsigned long long* dtbits = nullptr;  // [4] minimum time step slots (bit pattern of a positive double)
+  int* err = nullptr;      // [4] error word, first bad cell, ...
+};
+
+struct SpatOpts {
+  int scheme, highres, limiter, postlim, gradmeth, mode;
+  double gamma, entropy_fix;
+};
+
+// One Runge-Kutta update applied at the end of a stage: partial sum of the state of stage
+// `target`, P_target <- (u0 or P_target) + c * R.  The partial sum of the next stage is the
+// next stage state (written to cur); later ones are kept in pk[target].
+struct RkOp {
+  int target;   // stage index (2..nstage) whose state the term belongs to
+  int from_u0;  // 1: first term, start from u0; 0: accumulate into pk[target]
+  int is_next;  // 1: target is the next stage (result goes to cur)
+  double c;
+};
+struct RkStagePlan {
+  int nops = 0;
+  RkOp ops[kMaxStage];
+  int acc_init = 0;   // 1: acc = c_acc * R; 0: acc = acc + c_acc * R
+  double c_acc = 0;
+  int final_stage = 0;  // 1: u0 <- u0 + acc
+  int has_acc = 1;
+};
+
+// Kernel identifiers for the per-kernel timing of ty_profile_read.
+enum KernelId {
+  K_PRIM = 0, K_GHOST_PRIM, K_GRAD, K_GHOST_GRAD, K_FACE_STATES, K_BARTH, K_FACE_FLUX, K_FACE_FLUX_LIM,
+  K_RK_UPDATE, K_GATHER, K_TIMESTEP, K_NUM
+};
+
+// Optional CUDA-event timing of every launch (host side only).
+struct Prof {
+  bool on = false;
+  struct Rec { int id; cudaEvent_t a, b; };
+  std::vector<Rec> rec;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  cudaEvent_t get() {
+    if (used == pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      pool.push_back(e);
+    }
+    return pool[used++];
+  }
+  template <class F>
+  void launch(int id, cudaStream_t st, F&& f) {
+    if (!on) { f(); return; }
+    cudaEvent_t a = get(), b = get();
+    cudaEventRecord(a, st);
+    f();
+    cudaEventRecord(b, st);
+    rec.push_back(Rec{id, a, b});
+  }
+  void reset() { rec.clear(); used = 0; }
+  ~Prof() { for (auto e : pool) cudaEventDestroy(e); }
+};
+
+// Launch sequences implemented once per arithmetic mode (kernels_exact.cu, kernels_fast.cu).
+#define TY_DECLARE_MODE(NS)                                                                        \
+  namespace NS {                                                                                   \
+  cudaError_t prim_from(const DevMesh& m, const DevState& s, const SpatOpts& o, const double* cons,   \
+                        cudaStream_t st, Prof* pr);                                                 \
+  cudaError_t residual_faces(const DevMesh& m, const DevState& s, const SpatOpts& o,               \
+                             cudaStream_t st, Prof* pr);                                           \
+  cudaError_t residual_gather(const DevMesh& m, const DevState& s, double dt,                      \
+                              const unsigned long long* dtbits, cudaStream_t st, Prof* pr);        \
+  cudaError_t rk_update(const DevMesh& m, const DevState& s, const SpatOpts& o,                    \
+                        const RkStagePlan& plan, double dt, const unsigned long long* dtbits,      \
+                        unsigned long long* dtbits_next, double cfl, cudaStream_t st, Prof* pr);   \
+  cudaError_t timestep(const DevMesh& m, const DevState& s, const SpatOpts& o, const double* cons, \
+                       double cfl, unsigned long long* dtbits, cudaStream_t st, Prof* pr);         \
+  }
+
+TY_DECLARE_MODE(kexact)
+TY_DECLARE_MODE(kfast)
+
+}  // namespace tyk

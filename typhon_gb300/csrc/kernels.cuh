@@ -1,0 +1,757 @@
+// Kernels of the explicit residual-and-update path, compiled once per arithmetic mode.
+//
+// Included by kernels_exact.cu (TY_KNS = kexact, TY_FAST = 0, compiled with -fmad=false:
+// every FP64 operation separately rounded, in Typhon's order) and kernels_fast.cu
+// (TY_KNS = kfast, TY_FAST = 1, fused multiply-add and precomputed weights).
+//
+// Typhon routines restated (file:line of the Fortran reference):
+//   k_prim          SOURCE/EQNS/calc_varprim_ns.f90:43-54
+//   k_ghost_prim    SOURCE/MGRID/calcboco_connect_per_match.f90:56-78 (periodic copy),
+//                   SOURCE/MGRID/calcboco_ust_sym.f90 (symmetry mirror)
+//   k_grad          SOURCE/MGRID/calc_gradient.f90:67-196 + SOURCE/MATH/MATRIX.f90:79-111
+//   k_ghost_grad    SOURCE/MGRID/calcboco_gen.f90:78-84 (connections only)
+//   recon           SOURCE/EQNS/hres_ns_musclfast.f90, hres_ns_muscl.f90, hres_ns_muscluns.f90,
+//                   tvdgrad{fst,str,uns}_{scal,vect}.f90, SOURCE/MGRID/LIMITER.f90
+//   k_barth         SOURCE/MGRID/postlimit_barth.f90:42-223
+//   flux_*          SOURCE/EQNS/calc_flux_hllc.f90:61-171, calc_roe_states.f90:35-53,
+//                   calc_flux_rusanov.f90:57-83; Roe: new (Roe 1981 + Harten fix)
+//   k_gather        SOURCE/MAIN/flux_to_res.f90:47-144 (colour-ordered sums, as a gather)
+//   k_rk_update     SOURCE/MAIN/treelevel_rungekutta.f90:60-113, SOURCE/ZONE/update_field.f90:38
+//   k_timestep      SOURCE/EQNS/calc_ns_timestep.f90:52-103
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/typhon_gpu.h"
+#include "devmesh.hpp"
+
+#ifndef TY_KNS
+#error "define TY_KNS and TY_FAST before including kernels.cuh"
+#endif
+
+namespace tyk {
+namespace TY_KNS {
+
+constexpr bool kFast = TY_FAST;
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ double d3(const double* a, int ld, int i, int k) { return a[k * (size_t)ld + i]; }
+
+// ---------------------------------------------------------------------------
+// Limiters (LIMITER.f90).  Scalars (rho, p) pass through the array forms, vector
+// components through the scalar forms, as tvdgrad*_scal / tvdgrad*_vect call them.
+__device__ __forceinline__ double sgn1(double x) { return signbit(x) ? -1.0 : 1.0; }
+
+__device__ double lim_scalar_form(int lim, double x1, double x2) {
+  switch (lim) {
+    case TY_LIM_MINMOD: {
+      double s = 0.5 * (sgn1(x1) + sgn1(x2));
+      return s * fmin(fabs(x1), fabs(x2));
+    }
+    case TY_LIM_ALBADA: {
+      double s = x1 * x2;
+      if (s <= 0.0) return 0.0;
+      return s * (x1 + x2) / (x1 * x1 + x2 * x2);
+    }
+    case TY_LIM_VLEER: {
+      double s = x1 * x2;
+      if (s <= 0.0) return 0.0;
+      return 2.0 * s / (x1 + x2);
+    }
+    case TY_LIM_SUPERBEE: {
+      double r = 0.0;
+      if (x1 > 0.0 && x2 > 0.0) r = fmax(fmin(2.0 * x1, x2), fmin(2.0 * x2, x1));
+      if (x1 < 0.0 && x2 < 0.0) r = fmin(fmax(2.0 * x1, x2), fmax(2.0 * x2, x1));
+      return r;
+    }
+    case TY_LIM_KIM3: {
+      double r = 0.0;
+      if (x1 > 0.0 && x2 > 0.0) { r = (2.0 * x1 + x2) / 3.0; r = fmin(fmin(2.0 * x1, 2.0 * x2), r); }
+      if (x1 < 0.0 && x2 < 0.0) { r = (2.0 * x1 + x2) / 3.0; r = fmax(fmax(2.0 * x1, 2.0 * x2), r); }
+      return r;
+    }
+    case TY_LIM_LIM03: {
+      double eta = (x1 * x1 + x2 * x2) / 0.01 / 0.01;
+      double r = 0.0;
+      if (eta < 1.0) r = (2.0 * x2 + x1) / 3.0;
+      else if (x1 > 0.0 && x2 > 0.0) { r = (2.0 * x2 + x1) / 3.0; r = fmin(fmin(1.6 * x2, 2.0 * x1), r); }
+      else if (x1 < 0.0 && x2 < 0.0) { r = (2.0 * x2 + x1) / 3.0; r = fmax(fmax(1.6 * x2, 2.0 * x1), r); }
+      else if (x1 < 0.0 && x2 > 0.0) { r = (2.0 * x2 + x1) / 3.0; r = fmax(0.0, fmin(-0.5 * x1, r)); }
+      else if (x1 > 0.0 && x2 < 0.0) { r = (2.0 * x2 + x1) / 3.0; r = fmin(0.0, fmax(-0.5 * x1, r)); }
+      return r;
+    }
+  }
+  return 0.0;
+}
+__device__ double lim_array_form(int lim, double x1, double x2) {
+  switch (lim) {
+    case TY_LIM_MINMOD:
+      if (x1 > 0.0 && x2 > 0.0) return fmin(x1, x2);
+      if (x1 < 0.0 && x2 < 0.0) return fmax(x1, x2);
+      return 0.0;
+    case TY_LIM_ALBADA:
+      if ((x1 > 0.0 && x2 > 0.0) || (x1 < 0.0 && x2 < 0.0)) return x1 * x2 * (x1 + x2) / (x1 * x1 + x2 * x2);
+      return 0.0;
+    case TY_LIM_VLEER:
+      if ((x1 > 0.0 && x2 > 0.0) || (x1 < 0.0 && x2 < 0.0)) return 2.0 * x1 * x2 / (x1 + x2);
+      return 0.0;
+    default:
+      return lim_scalar_form(lim, x1, x2);
+  }
+}
+// slope limiter of the MUSCL variants: lim(2g - LR, LR) for FAST/str, lim(g, LR) for UNS;
+// KIM3 takes its arguments swapped
+__device__ __forceinline__ double apply_lim(int lim, bool uns, bool arrayform, double g, double LR) {
+  double a = uns ? g : 2.0 * g - LR, b = LR;
+  if (lim == TY_LIM_KIM3) { double t = a; a = b; b = t; }
+  return arrayform ? lim_array_form(lim, a, b) : lim_scalar_form(lim, a, b);
+}
+
+// ---------------------------------------------------------------------------
+// cons -> prim (calc_varprim_ns.f90:43-54)
+__device__ __forceinline__ void cons_to_prim(double gamma, const double c[5], double q[5]) {
+  const double g1 = gamma - 1.0;
+  double rho = c[0];
+  double vx = c[2] / rho, vy = c[3] / rho, vz = c[4] / rho;
+  double ec = 0.5 * rho * (vx * vx + vy * vy + vz * vz);
+  q[0] = rho;
+  q[1] = g1 * (c[1] - ec);
+  q[2] = vx; q[3] = vy; q[4] = vz;
+}
+
+__global__ void k_prim(DevMesh m, const double* __restrict__ cons, double* __restrict__ prim, double gamma) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  double u[5], q[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) u[v] = cons[v * (size_t)m.ldc + c];
+  cons_to_prim(gamma, u, q);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) prim[v * (size_t)m.ldc + c] = q[v];
+}
+
+// ghost states: periodic copy, symmetry mirror (velocity reflected across the face)
+__global__ void k_ghost_prim(DevMesh m, double* __restrict__ prim) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m.ng) return;
+  const int g = m.nci + k, src = m.gsrc[k], f = m.gface[k];
+  const size_t ld = m.ldc;
+  const int kind = m.fbc[f];
+  prim[g] = prim[src];
+  prim[ld + g] = prim[ld + src];
+  double vx = prim[2 * ld + src], vy = prim[3 * ld + src], vz = prim[4 * ld + src];
+  if (kind == TY_BC_SYMMETRY) {
+    double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
+    double wx = vx - 0.0, wy = vy - 0.0, wz = vz - 0.0;
+    double dn = 2.0 * (wx * nx + wy * ny + wz * nz);
+    vx = vx - dn * nx; vy = vy - dn * ny; vz = vz - dn * nz;
+  }
+  prim[2 * ld + g] = vx;
+  prim[3 * ld + g] = vy;
+  prim[4 * ld + g] = vz;
+}
+
+// ---------------------------------------------------------------------------
+// least-squares gradient: b_c = sum_f (q(fc2) - q(fc1)) d_f over the cell's faces in colour
+// order, then the Cholesky solve (exact) or, in fast mode, the precomputed A^-1 d weights.
+__global__ void __launch_bounds__(kBlock) k_grad(DevMesh m, DevState s) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t ld = m.ldc;
+  double b[15];
+#pragma unroll
+  for (int k = 0; k < 15; ++k) b[k] = 0.0;
+  const double* __restrict__ prim = s.prim;
+  for (int sl = 0; sl < m.nslot; ++sl) {
+    int e = m.cf[sl * (size_t)m.nci + c];
+    if (e < 0) break;
+    int f = e >> 1;
+    int i1 = m.fc1[f], i2 = m.fc2[f];
+    if constexpr (kFast) {
+      const int side = e & 1;
+      const double wx = d3(m.lsqw, m.ldf, f, 3 * side), wy = d3(m.lsqw, m.ldf, f, 3 * side + 1),
+                   wz = d3(m.lsqw, m.ldf, f, 3 * side + 2);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double dsca = prim[v * ld + i2] - prim[v * ld + i1];
+        b[3 * v] = fma(dsca, wx, b[3 * v]);
+        b[3 * v + 1] = fma(dsca, wy, b[3 * v + 1]);
+        b[3 * v + 2] = fma(dsca, wz, b[3 * v + 2]);
+      }
+    } else {
+      const double dx = d3(m.dcg, m.ldf, f, 0), dy = d3(m.dcg, m.ldf, f, 1), dz = d3(m.dcg, m.ldf, f, 2);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double dsca = prim[v * ld + i2] - prim[v * ld + i1];
+        b[3 * v] = b[3 * v] + dsca * dx;
+        b[3 * v + 1] = b[3 * v + 1] + dsca * dy;
+        b[3 * v + 2] = b[3 * v + 2] + dsca * dz;
+      }
+    }
+  }
+  if constexpr (!kFast) {
+    const double L11 = m.lsq[c], L21 = m.lsq[m.nci + c], L31 = m.lsq[2 * (size_t)m.nci + c];
+    const double L22 = m.lsq[3 * (size_t)m.nci + c], L32 = m.lsq[4 * (size_t)m.nci + c];
+    const double L33 = m.lsq[5 * (size_t)m.nci + c];
+    // cholesky_solve (MATRIX.f90:79-111), column per variable
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      double x1 = b[3 * v], x2 = b[3 * v + 1], x3 = b[3 * v + 2];
+      x1 = x1 / L11;
+      x2 = x2 - L21 * x1;
+      x2 = x2 / L22;
+      x3 = x3 - L31 * x1;
+      x3 = x3 - L32 * x2;
+      x3 = x3 / L33;
+      x3 = x3 / L33;
+      x2 = x2 - L32 * x3;
+      x2 = x2 / L22;
+      x1 = x1 - L21 * x2;
+      x1 = x1 - L31 * x3;
+      x1 = x1 / L11;
+      b[3 * v] = x1; b[3 * v + 1] = x2; b[3 * v + 2] = x3;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 15; ++k) s.grad[k * ld + c] = b[k];
+}
+
+__global__ void k_ghost_grad(DevMesh m, double* __restrict__ grad) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m.ng) return;
+  const int f = m.gface[k];
+  if (m.fbc[f] != TY_BC_PERIODIC) return;
+  const int g = m.nci + k, src = m.gsrc[k];
+  const size_t ld = m.ldc;
+#pragma unroll
+  for (int v = 0; v < 15; ++v) grad[v * ld + g] = grad[v * ld + src];
+}
+
+// ---------------------------------------------------------------------------
+// High-order face state on one side of face f (side 0: cell fc1 "L", side 1: cell fc2 "R").
+__device__ void recon(const DevMesh& m, const DevState& s, const SpatOpts& o, int f, int side, double q[5]) {
+  const size_t ld = m.ldc;
+  const int icl = m.fc1[f], icr = m.fc2[f];
+  const int c = side ? icr : icl;
+  const double* __restrict__ prim = s.prim;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) q[v] = prim[v * ld + c];
+  if (o.highres == TY_HRES_NONE) return;
+  const double* __restrict__ gr = s.grad;
+  const double ux = d3(m.uLR, m.ldf, f, 0), uy = d3(m.uLR, m.ldf, f, 1), uz = d3(m.uLR, m.ldf, f, 2);
+  const double dLR = m.dLR[f];
+  if (o.highres == TY_HRES_MUSCLFAST) {
+    const double k = side ? m.kRF[f] : m.kLF[f];
+    // scalars (tvdgradfst_scal.f90:35-57)
+#pragma unroll
+    for (int sv = 0; sv < 2; ++sv) {
+      double LR = (prim[sv * ld + icr] - prim[sv * ld + icl]) / dLR;
+      double sg;
+      if (o.limiter == TY_LIM_NONE) {
+        sg = LR;
+      } else {
+        double g = gr[(3 * sv) * ld + c] * ux + gr[(3 * sv + 1) * ld + c] * uy + gr[(3 * sv + 2) * ld + c] * uz;
+        sg = apply_lim(o.limiter, false, true, g, LR);
+      }
+      q[sv] = q[sv] + sg * k;
+    }
+    // velocity (tvdgradfst_vect.f90:36-58)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      double LR = (prim[(2 + i) * ld + icr] - prim[(2 + i) * ld + icl]) / dLR;
+      double sg;
+      if (o.limiter == TY_LIM_NONE) {
+        sg = LR;
+      } else {
+        double g = gr[(6 + 3 * i) * ld + c] * ux + gr[(7 + 3 * i) * ld + c] * uy + gr[(8 + 3 * i) * ld + c] * uz;
+        sg = apply_lim(o.limiter, false, false, g, LR);
+      }
+      q[2 + i] = q[2 + i] + k * sg;
+    }
+    return;
+  }
+  // MUSCL / MUSCL-UNS (tvdgradstr_*.f90, tvdgraduns_*.f90)
+  const bool uns = o.highres == TY_HRES_MUSCLUNS;
+  const double* CF = side ? m.RF : m.LF;
+  const double cx = d3(CF, m.ldf, f, 0), cy = d3(CF, m.ldf, f, 1), cz = d3(CF, m.ldf, f, 2);
+#pragma unroll
+  for (int sv = 0; sv < 2; ++sv) {
+    double LR = (prim[sv * ld + icr] - prim[sv * ld + icl]) / dLR;
+    double gx = gr[(3 * sv) * ld + c], gy = gr[(3 * sv + 1) * ld + c], gz = gr[(3 * sv + 2) * ld + c];
+    double g = gx * ux + gy * uy + gz * uz;
+    double sg = o.limiter == TY_LIM_NONE ? LR - g : apply_lim(o.limiter, uns, true, g, LR) - g;
+    gx = gx + sg * ux; gy = gy + sg * uy; gz = gz + sg * uz;
+    q[sv] = q[sv] + (gx * cx + gy * cy + gz * cz);
+  }
+  double T[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) T[k] = gr[(6 + k) * ld + c];
+  double sgv[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    double LR = (prim[(2 + i) * ld + icr] - prim[(2 + i) * ld + icl]) / dLR;
+    double g = T[3 * i] * ux + T[3 * i + 1] * uy + T[3 * i + 2] * uz;
+    sgv[i] = o.limiter == TY_LIM_NONE ? LR - g : apply_lim(o.limiter, uns, false, g, LR) - g;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    double t0 = T[3 * i] + sgv[i] * ux, t1 = T[3 * i + 1] + sgv[i] * uy, t2 = T[3 * i + 2] + sgv[i] * uz;
+    q[2 + i] = q[2 + i] + (t0 * cx + t1 * cy + t2 * cz);
+  }
+}
+
+// velocity mirrored across the face plane (calcboco_ust_sym.f90, face-state mode)
+__device__ __forceinline__ void mirror(const DevMesh& m, int f, double q[5]) {
+  double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
+  double wx = q[2] - 0.0, wy = q[3] - 0.0, wz = q[4] - 0.0;
+  double dn = 2.0 * (wx * nx + wy * ny + wz * nz);
+  q[2] = q[2] - dn * nx; q[3] = q[3] - dn * ny; q[4] = q[4] - dn * nz;
+}
+
+// ---------------------------------------------------------------------------
+// Riemann fluxes per unit area, F = (mass, energy, momentum x, y, z)
+__device__ void flux_hllc(double g, const double* L, const double* R, double nx, double ny, double nz, double* F) {
+  const double ig1 = 1.0 / (g - 1.0);
+  const double gig1 = g / (g - 1.0);
+  // calc_roe_states.f90:37-53
+  double t1 = sqrt(R[0] / L[0]);
+  double roe_rho = L[0] * t1;
+  double kl = 1.0 / (1.0 + t1);
+  double kr = t1 * kl;
+  double rux = kl * L[2] + kr * R[2], ruy = kl * L[3] + kr * R[3], ruz = kl * L[4] + kr * R[4];
+  double sqL = L[2] * L[2] + L[3] * L[3] + L[4] * L[4];
+  double sqR = R[2] * R[2] + R[3] * R[3] + R[4] * R[4];
+  double h1 = gig1 * L[1] / L[0] + 0.5 * sqL;
+  double h2 = gig1 * R[1] / R[0] + 0.5 * sqR;
+  h1 = kl * h1 + kr * h2;
+  double roe_p = (h1 - 0.5 * (rux * rux + ruy * ruy + ruz * ruz)) * roe_rho / gig1;
+  // calc_flux_hllc.f90:86-171 (beta = 1)
+  double vnl = L[2] * nx + L[3] * ny + L[4] * nz;
+  double vnr = R[2] * nx + R[3] * ny + R[4] * nz;
+  double al = sqrt(g * L[1] / L[0]);
+  double ar = sqrt(g * R[1] / R[0]);
+  double vm = rux * nx + ruy * ny + ruz * nz;
+  double am = sqrt(g * roe_p / roe_rho);
+  double rel = ig1 * L[1] + 0.5 * L[0] * sqL;
+  double rer = ig1 * R[1] + 0.5 * R[0] * sqR;
+  const double beta = 1.0;
+  double sl = fmin(vnl - beta * al, vm - am);
+  double sr = fmax(vnr + beta * ar, vm + am);
+  if (sl >= 0.0) {
+    F[0] = vnl * L[0];
+    F[1] = vnl * (rel + L[1]);
+    double m0 = vnl * L[0];
+    F[2] = m0 * L[2] + L[1] * nx; F[3] = m0 * L[3] + L[1] * ny; F[4] = m0 * L[4] + L[1] * nz;
+  } else if (sr <= 0.0) {
+    F[0] = vnr * R[0];
+    F[1] = vnr * (rer + R[1]);
+    double m0 = vnr * R[0];
+    F[2] = m0 * R[2] + R[1] * nx; F[3] = m0 * R[3] + R[1] * ny; F[4] = m0 * R[4] + R[1] * nz;
+  } else {
+    double rqL = L[0] * (sl - vnl);
+    double rqR = R[0] * (sr - vnr);
+    double Sst = (rqR * vnr - rqL * vnl - R[1] + L[1]) / (rqR - rqL);
+    double iks, rst, pst, rest, rvx, rvy, rvz;
+    if (Sst >= 0.0) {
+      iks = 1.0 / (sl - Sst);
+      rst = rqL * iks;
+      pst = L[1] - rqL * (vnl - Sst);
+      double dp = pst - L[1];
+      rvx = iks * ((rqL * L[2]) + dp * nx); rvy = iks * ((rqL * L[3]) + dp * ny); rvz = iks * ((rqL * L[4]) + dp * nz);
+      rest = iks * (rel * (sl - vnl) - L[1] * vnl + pst * Sst);
+    } else {
+      iks = 1.0 / (sr - Sst);
+      rst = rqR * iks;
+      pst = R[1] - rqR * (vnr - Sst);
+      double dp = pst - R[1];
+      rvx = iks * ((rqR * R[2]) + dp * nx); rvy = iks * ((rqR * R[3]) + dp * ny); rvz = iks * ((rqR * R[4]) + dp * nz);
+      rest = iks * (rer * (sr - vnr) - R[1] * vnr + pst * Sst);
+    }
+    F[0] = Sst * rst;
+    F[1] = Sst * (rest + pst);
+    F[2] = (Sst * rvx) + (pst * nx); F[3] = (Sst * rvy) + (pst * ny); F[4] = (Sst * rvz) + (pst * nz);
+  }
+}
+
+__device__ void flux_rusanov(double g, const double* L, const double* R, double nx, double ny, double nz, double* F) {
+  const double ig1 = 1.0 / (g - 1.0);
+  double vnl = L[2] * nx + L[3] * ny + L[4] * nz;
+  double vnr = R[2] * nx + R[3] * ny + R[4] * nz;
+  double al = sqrt(g * L[1] / L[0]);
+  double ar = sqrt(g * R[1] / R[0]);
+  double ray = fmax(fabs(vnl) + al, fabs(vnr) + ar);
+  double rel = ig1 * L[1] + 0.5 * L[0] * (L[2] * L[2] + L[3] * L[3] + L[4] * L[4]);
+  double rer = ig1 * R[1] + 0.5 * R[0] * (R[2] * R[2] + R[3] * R[3] + R[4] * R[4]);
+  F[0] = 0.5 * ((vnl + ray) * L[0] + (vnr - ray) * R[0]);
+  F[1] = 0.5 * ((vnl + ray) * rel + (vnr - ray) * rer + vnl * L[1] + vnr * R[1]);
+  double a = (vnl + ray) * L[0], b = (vnr - ray) * R[0], pp = L[1] + R[1];
+  F[2] = 0.5 * ((a * L[2] + b * R[2]) + pp * nx);
+  F[3] = 0.5 * ((a * L[3] + b * R[3]) + pp * ny);
+  F[4] = 0.5 * ((a * L[4] + b * R[4]) + pp * nz);
+}
+
+// Roe flux-difference splitting with Harten's entropy fix (new: Typhon has no Roe flux)
+__device__ void flux_roe(double g, double eps, const double* L, const double* R, double nx, double ny, double nz,
+                         double* F) {
+  const double ig1 = 1.0 / (g - 1.0);
+  const double gig1 = g / (g - 1.0);
+  double t1 = sqrt(R[0] / L[0]);
+  double rroe = L[0] * t1;
+  double kl = 1.0 / (1.0 + t1), kr = t1 * kl;
+  double ux = kl * L[2] + kr * R[2], uy = kl * L[3] + kr * R[3], uz = kl * L[4] + kr * R[4];
+  double sqL = L[2] * L[2] + L[3] * L[3] + L[4] * L[4];
+  double sqR = R[2] * R[2] + R[3] * R[3] + R[4] * R[4];
+  double hl = gig1 * L[1] / L[0] + 0.5 * sqL;
+  double hr = gig1 * R[1] / R[0] + 0.5 * sqR;
+  double hroe = kl * hl + kr * hr;
+  double q2 = ux * ux + uy * uy + uz * uz;
+  double a2 = (g - 1.0) * (hroe - 0.5 * q2);
+  double a = sqrt(a2);
+  double vn = ux * nx + uy * ny + uz * nz;
+  double vnl = L[2] * nx + L[3] * ny + L[4] * nz;
+  double vnr = R[2] * nx + R[3] * ny + R[4] * nz;
+  double rel = ig1 * L[1] + 0.5 * L[0] * sqL;
+  double rer = ig1 * R[1] + 0.5 * R[0] * sqR;
+  double drho = R[0] - L[0], dp = R[1] - L[1], dvn = vnr - vnl;
+  double dux = R[2] - L[2], duy = R[3] - L[3], duz = R[4] - L[4];
+  double al1 = (dp - rroe * a * dvn) / (2.0 * a2);
+  double al5 = (dp + rroe * a * dvn) / (2.0 * a2);
+  double al2 = drho - dp / a2;
+  double dutx = dux - dvn * nx, duty = duy - dvn * ny, dutz = duz - dvn * nz;
+  double l1 = fabs(vn - a), l5 = fabs(vn + a), l2 = fabs(vn);
+  double delta = eps * a;
+  if (l1 < delta) l1 = (l1 * l1 + delta * delta) / (2.0 * delta);
+  if (l5 < delta) l5 = (l5 * l5 + delta * delta) / (2.0 * delta);
+  double w1 = l1 * al1, w2 = l2 * al2, w5 = l5 * al5, ws = l2 * rroe;
+  double d_mass = w1 + w2 + w5;
+  double dmx = w1 * (ux - a * nx) + w2 * ux + w5 * (ux + a * nx) + ws * dutx;
+  double dmy = w1 * (uy - a * ny) + w2 * uy + w5 * (uy + a * ny) + ws * duty;
+  double dmz = w1 * (uz - a * nz) + w2 * uz + w5 * (uz + a * nz) + ws * dutz;
+  double d_ener = w1 * (hroe - a * vn) + w2 * (0.5 * q2) + w5 * (hroe + a * vn) +
+                  ws * ((ux * dux + uy * duy + uz * duz) - vn * dvn);
+  double ml = vnl * L[0], mr = vnr * R[0];
+  F[0] = 0.5 * (ml + mr - d_mass);
+  F[1] = 0.5 * (vnl * (rel + L[1]) + vnr * (rer + R[1]) - d_ener);
+  F[2] = 0.5 * ((ml * L[2] + L[1] * nx) + (mr * R[2] + R[1] * nx) - dmx);
+  F[3] = 0.5 * ((ml * L[3] + L[1] * ny) + (mr * R[3] + R[1] * ny) - dmy);
+  F[4] = 0.5 * ((ml * L[4] + L[1] * nz) + (mr * R[4] + R[1] * nz) - dmz);
+}
+
+__device__ __forceinline__ void face_flux(const DevMesh& m, const SpatOpts& o, int f, const double* QL,
+                                          const double* QR, double* __restrict__ flux) {
+  const double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
+  double F[5];
+  if (o.scheme == TY_SCH_HLLC) flux_hllc(o.gamma, QL, QR, nx, ny, nz, F);
+  else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
+  else flux_roe(o.gamma, o.entropy_fix, QL, QR, nx, ny, nz, F);
+  const double S = m.fs[f];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) flux[v * (size_t)m.ldf + f] = S * F[v];
+}
+
+// fused face states + flux (no post-limiter)
+__global__ void __launch_bounds__(kBlock) k_face_flux(DevMesh m, DevState s, SpatOpts o) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  double QL[5], QR[5];
+  recon(m, s, o, f, 0, QL);
+  const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
+  if (kind == TY_BC_PERIODIC) {
+    recon(m, s, o, m.part[f], 0, QR);  // cell_r(face) = cell_l(partner face)
+  } else if (kind == TY_BC_SYMMETRY) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) QR[v] = QL[v];
+    mirror(m, f, QR);
+  } else {
+    recon(m, s, o, f, 1, QR);
+  }
+  face_flux(m, o, f, QL, QR, s.flux);
+}
+
+// post-limiter path, 1: unlimited face states
+__global__ void __launch_bounds__(kBlock) k_face_states(DevMesh m, DevState s, SpatOpts o) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  double Q[5];
+  recon(m, s, o, f, 0, Q);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) s.cl[v * (size_t)m.ldf + f] = Q[v];
+  recon(m, s, o, f, 1, Q);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) s.cr[v * (size_t)m.ldf + f] = Q[v];
+}
+
+// post-limiter path, 2: Barth-type ratio of each interior cell (postlimit_barth.f90:60-80,
+// 140-170).  A face whose increment is exactly zero imposes no constraint.
+__global__ void __launch_bounds__(kBlock) k_barth(DevMesh m, DevState s, double klim) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t ld = m.ldc, lf = m.ldf;
+  double r[3] = {1.0, 1.0, 1.0};
+  double qc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) qc[v] = s.prim[v * ld + c];
+  for (int sl = 0; sl < m.nslot; ++sl) {
+    int e = m.cf[sl * (size_t)m.nci + c];
+    if (e < 0) break;
+    int f = e >> 1, side = e & 1;
+    int nb = side ? m.fc1[f] : m.fc2[f];
+    const double* qf = side ? s.cr : s.cl;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      double LR = s.prim[v * ld + nb] - qc[v];  // = +-(q(fc2) - q(fc1)) seen from c
+      double den = qf[v * lf + f] - qc[v];
+      if (den != 0.0) {
+        double l = fmax(klim * (LR / den), 0.0);
+        int k = v < 2 ? v : 2;
+        r[k] = fmin(r[k], l);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) s.ratio[k * ld + c] = r[k];
+}
+
+// post-limiter path, 3: limited states + flux
+__global__ void __launch_bounds__(kBlock) k_face_flux_lim(DevMesh m, DevState s, SpatOpts o) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const size_t ld = m.ldc, lf = m.ldf;
+  double QL[5], QR[5];
+  auto limited = [&](int face, int side, double* Q) {
+    int c = side ? m.fc2[face] : m.fc1[face];
+    const double* qf = side ? s.cr : s.cl;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      double qc = s.prim[v * ld + c];
+      double rr = s.ratio[(v < 2 ? v : 2) * ld + c];
+      Q[v] = qc + rr * (qf[v * lf + face] - qc);
+    }
+  };
+  limited(f, 0, QL);
+  const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
+  if (kind == TY_BC_PERIODIC) {
+    limited(m.part[f], 0, QR);
+  } else if (kind == TY_BC_SYMMETRY) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) QR[v] = QL[v];
+    mirror(m, f, QR);
+  } else {
+    limited(f, 1, QR);
+  }
+  face_flux(m, o, f, QL, QR, s.flux);
+}
+
+// ---------------------------------------------------------------------------
+// residual R_c = dt/V_c * sum(+-F S), in the colour order of flux_to_res
+__device__ __forceinline__ void gather_residual(const DevMesh& m, const DevState& s, int c, double R[5]) {
+#pragma unroll
+  for (int v = 0; v < 5; ++v) R[v] = 0.0;
+  const double* __restrict__ F = s.flux;
+  const size_t lf = m.ldf;
+  for (int sl = 0; sl < m.nslot; ++sl) {
+    int e = m.cf[sl * (size_t)m.nci + c];
+    if (e < 0) break;
+    int f = e >> 1;
+    if (e & 1) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) R[v] = R[v] + F[v * lf + f];
+    } else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) R[v] = R[v] - F[v * lf + f];
+    }
+  }
+}
+
+__device__ __forceinline__ double load_dt(double dt, const unsigned long long* dtbits) {
+  return dtbits ? __longlong_as_double((long long)*dtbits) : dt;
+}
+
+__global__ void __launch_bounds__(kBlock) k_gather(DevMesh m, DevState s, double dt, const unsigned long long* dtbits) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  double R[5];
+  gather_residual(m, s, c, R);
+  const double coef = load_dt(dt, dtbits) / m.cvol[c];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) s.res[v * (size_t)m.ldc + c] = coef * R[v];
+}
+
+// per-cell stability time step; returns false for negative or NaN internal energy
+__device__ __forceinline__ bool cell_dt(const DevMesh& m, double gamma, double cfl, int c, const double u[5], double& dt) {
+  const double gg1 = gamma * (gamma - 1.0);
+  double d = cfl * 2.0 * m.cvol[c] / m.sumS[c];
+  double irho = 1.0 / u[0];
+  double rv2 = u[2] * u[2] + u[3] * u[3] + u[4] * u[4];
+  double a2 = (u[1] - 0.5 * rv2 * irho) * gg1 * irho;
+  if (!(a2 > 0.0)) return false;
+  dt = d / (sqrt(rv2) * irho + sqrt(a2));
+  return true;
+}
+
+// block minimum of positive doubles through their bit patterns (order-independent, exact)
+__device__ __forceinline__ void block_min_dt(double dt, unsigned long long* dtbits) {
+  __shared__ unsigned long long smin[kBlock / 32];
+  unsigned long long b = (unsigned long long)__double_as_longlong(dt);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long t = __shfl_down_sync(0xffffffffu, b, o);
+    b = t < b ? t : b;
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) smin[w] = b;
+  __syncthreads();
+  if (w == 0) {
+    b = lane < (int)(blockDim.x >> 5) ? smin[lane] : ~0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long t = __shfl_down_sync(0xffffffffu, b, o);
+      b = t < b ? t : b;
+    }
+    if (lane == 0) atomicMin(dtbits, b);
+  }
+}
+
+__device__ __forceinline__ void flag_error(int* err, int code, int cell) {
+  if (atomicCAS(err, 0, code) == 0) err[1] = cell;
+}
+
+__global__ void __launch_bounds__(kBlock) k_timestep(DevMesh m, const double* __restrict__ cons, double gamma,
+                                                      double cfl, unsigned long long* dtbits, int* err) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  double dt = __longlong_as_double(0x7fefffffffffffffll);  // largest finite double
+  if (c < m.nci) {
+    double u[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) u[v] = cons[v * (size_t)m.ldc + c];
+    double d;
+    if (cell_dt(m, gamma, cfl, c, u, d)) {
+      dt = d;
+      if (!(d > 0.0)) flag_error(err, TY_ERR_NANDT, c);
+    } else {
+      flag_error(err, TY_ERR_NEGENERGY, c);
+    }
+  }
+  block_min_dt(dt, dtbits);
+}
+
+// Runge-Kutta update at the end of a stage.  Applies the plan's partial sums, the final
+// combination, and derives the primitive variables of the new state (and its time step
+// after the last stage when dtbits_next is given).
+__global__ void __launch_bounds__(kBlock) k_rk_update(DevMesh m, DevState s, RkStagePlan plan, double gamma, double dt,
+                                                       const unsigned long long* dtbits, unsigned long long* dtbits_next,
+                                                       double cfl) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = c < m.nci;
+  double dtc = __longlong_as_double(0x7fefffffffffffffll);
+  if (active) {
+    const size_t ld = m.ldc;
+    double R[5];
+    gather_residual(m, s, c, R);
+    const double coef = load_dt(dt, dtbits) / m.cvol[c];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) R[v] = coef * R[v];
+    double u0[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) u0[v] = s.u0[v * ld + c];
+    double next[5];
+    bool have_next = false;
+    for (int k = 0; k < plan.nops; ++k) {
+      const RkOp op = plan.ops[k];
+      double* part = s.pk[op.target];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double base = op.from_u0 ? u0[v] : part[v * ld + c];
+        double val = base + op.c * R[v];
+        if (op.is_next) next[v] = val;
+        else part[v * ld + c] = val;
+      }
+      if (op.is_next) have_next = true;
+    }
+    if (plan.has_acc) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        double a = plan.acc_init ? plan.c_acc * R[v] : s.acc[v * ld + c] + plan.c_acc * R[v];
+        if (plan.final_stage) next[v] = u0[v] + a;
+        else s.acc[v * ld + c] = a;
+      }
+      if (plan.final_stage) have_next = true;
+    }
+    if (have_next) {
+      double* dst = plan.final_stage ? s.u0 : s.cur;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) dst[v * ld + c] = next[v];
+      double q[5];
+      cons_to_prim(gamma, next, q);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) s.prim[v * ld + c] = q[v];
+      if (dtbits_next) {
+        double d;
+        if (cell_dt(m, gamma, cfl, c, next, d)) {
+          dtc = d;
+          if (!(d > 0.0)) flag_error(s.err, TY_ERR_NANDT, c);
+        } else {
+          flag_error(s.err, TY_ERR_NEGENERGY, c);
+        }
+      }
+    }
+  }
+  if (dtbits_next) block_min_dt(dtc, dtbits_next);
+}
+
+// ---------------------------------------------------------------------------
+// launch sequences
+inline unsigned nblk(int n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+
+cudaError_t prim_from(const DevMesh& m, const DevState& s, const SpatOpts& o, const double* cons,
+                      cudaStream_t st, Prof* pr) {
+  if (m.nci > 0)
+    pr->launch(K_PRIM, st, [&] { k_prim<<<nblk(m.nci), kBlock, 0, st>>>(m, cons, s.prim, o.gamma); });
+  return cudaGetLastError();
+}
+
+// everything between the primitive variables of a stage state and the face fluxes
+cudaError_t residual_faces(const DevMesh& m, const DevState& s, const SpatOpts& o, cudaStream_t st, Prof* pr) {
+  if (m.ng > 0)
+    pr->launch(K_GHOST_PRIM, st, [&] { k_ghost_prim<<<nblk(m.ng), kBlock, 0, st>>>(m, s.prim); });
+  if (o.gradmeth != TY_GRAD_NONE) {
+    pr->launch(K_GRAD, st, [&] { k_grad<<<nblk(m.nci), kBlock, 0, st>>>(m, s); });
+    if (m.ng > 0)
+      pr->launch(K_GHOST_GRAD, st, [&] { k_ghost_grad<<<nblk(m.ng), kBlock, 0, st>>>(m, s.grad); });
+  }
+  if (o.postlim != TY_POSTLIM_NONE) {
+    pr->launch(K_FACE_STATES, st, [&] { k_face_states<<<nblk(m.nf), kBlock, 0, st>>>(m, s, o); });
+    const double klim = o.postlim == TY_POSTLIM_BARTH ? 0.5 : 1.0;
+    pr->launch(K_BARTH, st, [&] { k_barth<<<nblk(m.nci), kBlock, 0, st>>>(m, s, klim); });
+    pr->launch(K_FACE_FLUX_LIM, st, [&] { k_face_flux_lim<<<nblk(m.nf), kBlock, 0, st>>>(m, s, o); });
+  } else {
+    pr->launch(K_FACE_FLUX, st, [&] { k_face_flux<<<nblk(m.nf), kBlock, 0, st>>>(m, s, o); });
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t residual_gather(const DevMesh& m, const DevState& s, double dt, const unsigned long long* dtbits,
+                            cudaStream_t st, Prof* pr) {
+  pr->launch(K_GATHER, st, [&] { k_gather<<<nblk(m.nci), kBlock, 0, st>>>(m, s, dt, dtbits); });
+  return cudaGetLastError();
+}
+
+cudaError_t rk_update(const DevMesh& m, const DevState& s, const SpatOpts& o, const RkStagePlan& plan, double dt,
+                      const unsigned long long* dtbits, unsigned long long* dtbits_next, double cfl,
+                      cudaStream_t st, Prof* pr) {
+  pr->launch(K_RK_UPDATE, st, [&] {
+    k_rk_update<<<nblk(m.nci), kBlock, 0, st>>>(m, s, plan, o.gamma, dt, dtbits, dtbits_next, cfl);
+  });
+  return cudaGetLastError();
+}
+
+cudaError_t timestep(const DevMesh& m, const DevState& s, const SpatOpts& o, const double* cons, double cfl,
+                     unsigned long long* dtbits, cudaStream_t st, Prof* pr) {
+  pr->launch(K_TIMESTEP, st, [&] {
+    k_timestep<<<nblk(m.nci), kBlock, 0, st>>>(m, cons, o.gamma, cfl, dtbits, s.err);
+  });
+  return cudaGetLastError();
+}
+
+}  // namespace TY_KNS
+}  // namespace tyk

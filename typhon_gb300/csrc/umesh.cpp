@@ -1,0 +1,513 @@
+// Host mesh preprocessing of the typhon_gb300 library (no GPU).
+//
+// Builds the ty_mesh_desc arrays of include/typhon_gpu.h from an element mesh the way
+// Typhon prepares a grid, so that face numbering, orientation, colours, ghost cells and
+// every geometric value come out as Typhon computes them:
+//   faces of each element, created cell by cell   CFDTOOLS/Mesh/create_facevtex.f90:60-210
+//   interior faces first, boundary faces reversed  CFDTOOLS/Mesh/MESHCONNECT.f90:538-598
+//   boundary marks matched to faces                CFDTOOLS/Mesh/seek_bcface_face.f90
+//   face/cell geometry                             CFDTOOLS/Mesh/MESHGEOM.f90:37-330
+//   greedy first-fit face colouring                CFDTOOLS/Base/COLOR.f90:55-81
+//   ghost cells, periodic partners                 SOURCE/ZONE/init_connect_grid.f90:60-246,
+//                                                  SOURCE/ZONE/init_ustboco_ghostcell.f90:44-80
+// Data structures differ from Typhon's (hash maps instead of vertex->face scans, a spatial
+// hash for periodic matching) so that meshes of millions of cells preprocess in seconds.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/typhon_gpu.h"
+#include "internal.hpp"
+
+namespace {
+
+struct V3 { double x, y, z; };
+inline V3 mk(double a, double b, double c) { return V3{a, b, c}; }
+inline V3 add(V3 a, V3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 sub(V3 a, V3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 scl(double s, V3 a) { return mk(s * a.x, s * a.y, s * a.z); }
+inline V3 dvd(V3 a, double s) { return mk(a.x / s, a.y / s, a.z / s); }
+inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline double norm(V3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+inline V3 cross(V3 a, V3 b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+
+int elem_nv(int t) {
+  switch (t) {
+    case 2: return 2;     // BAR2
+    case 13: return 3;    // TRI3
+    case 24: return 4;    // QUAD4
+    case 101: return 4;   // TETRA4
+    case 131: return 6;   // PENTA6
+    case 141: return 8;   // HEXA8
+  }
+  return 0;
+}
+int elem_dim(int t) {
+  switch (t) {
+    case 2: return 1;
+    case 13: case 24: return 2;
+    case 101: case 131: case 141: return 3;
+  }
+  return 0;
+}
+
+struct Section { int type; std::vector<int> ielem, vtex; };
+struct Mark { std::string family; std::vector<int> tags; };
+struct BcIn { std::string family, partner; int kind; V3 trans, wallvel; };
+
+std::string upper(std::string s) {
+  for (auto& c : s) c = (char)toupper((unsigned char)c);
+  return s;
+}
+
+// Faces are identified by their sorted vertex list (up to 4 vertices).
+struct FaceKey {
+  std::array<int, 4> v;
+  bool operator==(const FaceKey& o) const { return v == o.v; }
+};
+struct FaceKeyHash {
+  size_t operator()(const FaceKey& k) const {
+    uint64_t h = 1469598103934665603ull;
+    for (int x : k.v) { h ^= (uint64_t)(uint32_t)x; h *= 1099511628211ull; }
+    return (size_t)h;
+  }
+};
+FaceKey key_of(const int* f, int n) {
+  FaceKey k;
+  k.v = {0, 0, 0, 0};
+  for (int i = 0; i < n; ++i) k.v[i] = f[i];
+  std::sort(k.v.begin(), k.v.begin() + n);
+  return k;
+}
+
+}  // namespace
+
+struct ty_umesh {
+  std::vector<V3> nodes;
+  std::vector<Section> sections;
+  std::vector<Mark> marks;
+  std::vector<BcIn> bcs;
+  bool built = false;
+  int dim = 0, ncell_int = 0, ncell = 0, nface_int = 0, nface = 0;
+  std::vector<int32_t> facecell;          // [2*nface], 1-based, column-major
+  std::vector<int32_t> facevtex;          // [4*nface], 1-based, 0 padded
+  std::vector<double> fnormal, fcentre, fsurf, ccentre, cvol, fwallvel;
+  std::vector<int32_t> fcolor, fbc, fpartner;
+};
+
+extern "C" {
+
+int ty_umesh_new(ty_umesh** out) {
+  if (!out) return TY_ERR_ARG;
+  *out = new ty_umesh();
+  return TY_OK;
+}
+int ty_umesh_free(ty_umesh* um) {
+  delete um;
+  return TY_OK;
+}
+int ty_umesh_set_nodes(ty_umesh* um, int32_t n, const double* xyz) {
+  if (!um || n < 0 || (n && !xyz)) return TY_ERR_ARG;
+  um->nodes.resize(n);
+  for (int i = 0; i < n; ++i) um->nodes[i] = mk(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+  return TY_OK;
+}
+int ty_umesh_add_section(ty_umesh* um, int32_t type, int32_t nelem, const int32_t* ielem,
+                         const int32_t* vtex) {
+  if (!um || nelem < 0 || elem_nv(type) == 0 || (nelem && (!ielem || !vtex))) return TY_ERR_ARG;
+  Section s;
+  s.type = type;
+  s.ielem.assign(ielem, ielem + nelem);
+  s.vtex.assign(vtex, vtex + (size_t)nelem * elem_nv(type));
+  um->sections.push_back(std::move(s));
+  return TY_OK;
+}
+int ty_umesh_add_mark(ty_umesh* um, const char* family, int32_t ntag, const int32_t* tags) {
+  if (!um || !family || ntag < 0 || (ntag && !tags)) return TY_ERR_ARG;
+  Mark m;
+  m.family = family;
+  m.tags.assign(tags, tags + ntag);
+  um->marks.push_back(std::move(m));
+  return TY_OK;
+}
+int ty_umesh_add_bc(ty_umesh* um, const char* family, int32_t kind, const char* partner,
+                    const double* t3, const double* w3) {
+  if (!um || !family || kind < TY_BC_PERIODIC || kind > TY_BC_WALL) return TY_ERR_ARG;
+  BcIn b;
+  b.family = upper(family);
+  b.partner = partner ? upper(partner) : "";
+  b.kind = kind;
+  b.trans = t3 ? mk(t3[0], t3[1], t3[2]) : mk(0, 0, 0);
+  b.wallvel = w3 ? mk(w3[0], w3[1], w3[2]) : mk(0, 0, 0);
+  um->bcs.push_back(b);
+  return TY_OK;
+}
+
+int ty_umesh_build(ty_umesh* um, int32_t dim) {
+  if (!um || (dim != 2 && dim != 3)) return TY_ERR_ARG;
+  auto fail = [&](const char* msg) { tyi::set_error(msg); return TY_ERR_MESH; };
+  um->dim = dim;
+  const int nvtex = (int)um->nodes.size();
+  int maxdim = 0;
+  for (auto& s : um->sections) maxdim = std::max(maxdim, elem_dim(s.type));
+  int ncell_int = 0;
+  for (auto& s : um->sections)
+    if (elem_dim(s.type) == maxdim) ncell_int += (int)s.ielem.size();
+
+  // ---- faces in creation order ----
+  std::vector<int> fv;        // 4 per face, creation order
+  std::vector<int> fnv;       // vertex count per face
+  std::vector<int> c1, c2;    // 1-based cells, 0 = none
+  std::unordered_map<FaceKey, int, FaceKeyHash> lookup;
+  lookup.reserve((size_t)ncell_int * 3);
+  static const int tri[3][2] = {{1, 2}, {2, 3}, {3, 1}};
+  static const int quad[4][2] = {{1, 2}, {2, 3}, {3, 4}, {4, 1}};
+  static const int tet[4][3] = {{1, 3, 2}, {1, 2, 4}, {2, 3, 4}, {3, 1, 4}};
+  static const int hexa[6][4] = {{1, 2, 3, 4}, {1, 2, 6, 5}, {5, 6, 7, 8},
+                                 {4, 3, 7, 8}, {1, 4, 8, 5}, {2, 3, 7, 6}};
+  for (auto& s : um->sections) {
+    if (elem_dim(s.type) != maxdim) continue;
+    const int nv = elem_nv(s.type);
+    for (size_t ic = 0; ic < s.ielem.size(); ++ic) {
+      const int icell = s.ielem[ic];
+      const int* e = &s.vtex[ic * nv];
+      auto create = [&](const int* loc, int n) -> bool {
+        int f[4] = {0, 0, 0, 0};
+        for (int k = 0; k < n; ++k) {
+          f[k] = e[loc[k] - 1];
+          if (f[k] < 1 || f[k] > nvtex) return false;
+        }
+        FaceKey key = key_of(f, n);
+        auto it = lookup.find(key);
+        if (it == lookup.end()) {
+          int id = (int)c1.size();
+          lookup.emplace(key, id);
+          for (int k = 0; k < 4; ++k) fv.push_back(f[k]);
+          fnv.push_back(n);
+          c1.push_back(icell);
+          c2.push_back(0);
+        } else {
+          if (c2[it->second] != 0) return false;
+          c2[it->second] = icell;
+        }
+        return true;
+      };
+      bool ok = true;
+      switch (s.type) {
+        case 13: for (int k = 0; k < 3 && ok; ++k) ok = create(tri[k], 2); break;
+        case 24: for (int k = 0; k < 4 && ok; ++k) ok = create(quad[k], 2); break;
+        case 101: for (int k = 0; k < 4 && ok; ++k) ok = create(tet[k], 3); break;
+        case 131: {
+          static const int t1[3] = {1, 2, 3}, t2[3] = {4, 5, 6};
+          static const int q1[4] = {1, 3, 6, 4}, q2[4] = {1, 2, 5, 4}, q3[4] = {2, 3, 6, 5};
+          ok = create(t1, 3) && create(t2, 3) && create(q1, 4) && create(q2, 4) && create(q3, 4);
+          break;
+        }
+        case 141: for (int k = 0; k < 6 && ok; ++k) ok = create(hexa[k], 4); break;
+        default: return fail("unsupported element type");
+      }
+      if (!ok) return fail("bad connectivity (vertex out of range or 3 cells on a face)");
+    }
+  }
+  const int nface = (int)c1.size();
+
+  // ---- reorder: interior faces first in creation order, boundary faces reversed ----
+  std::vector<int> newidx(nface);
+  int nfi = 0, nfl = 0;
+  for (int f = 0; f < nface; ++f) {
+    if (c2[f] == 0) { ++nfl; newidx[f] = nface - nfl; }
+    else newidx[f] = nfi++;
+  }
+  std::vector<int> F1(nface), F2(nface), FV(4 * (size_t)nface), FN(nface);
+  for (int f = 0; f < nface; ++f) {
+    int n = newidx[f];
+    F1[n] = c1[f]; F2[n] = c2[f]; FN[n] = fnv[f];
+    for (int k = 0; k < 4; ++k) FV[4 * (size_t)n + k] = fv[4 * (size_t)f + k];
+  }
+  for (auto& kv : lookup) kv.second = newidx[kv.second];
+
+  // ---- boundary marks -> boundary faces (mark order) ----
+  struct Boco { std::string family; std::vector<int> iface; int kind = 0; int def = -1; double rlink = 0;
+                std::vector<int> partner; };
+  std::vector<Boco> bocos;
+  {
+    std::unordered_map<int, std::pair<int, int>> face_elem;  // element number -> (section, index)
+    for (size_t si = 0; si < um->sections.size(); ++si) {
+      auto& s = um->sections[si];
+      if (elem_dim(s.type) != maxdim - 1) continue;
+      for (size_t i = 0; i < s.ielem.size(); ++i) face_elem.emplace(s.ielem[i], std::make_pair((int)si, (int)i));
+    }
+    for (auto& mkr : um->marks) {
+      Boco b;
+      b.family = upper(mkr.family);
+      for (int tag : mkr.tags) {
+        auto it = face_elem.find(tag);
+        if (it == face_elem.end()) continue;
+        auto& s = um->sections[it->second.first];
+        int nv = elem_nv(s.type);
+        auto fk = lookup.find(key_of(&s.vtex[(size_t)it->second.second * nv], nv));
+        if (fk != lookup.end() && fk->second >= nfi) b.iface.push_back(fk->second);
+      }
+      if (!b.iface.empty()) bocos.push_back(std::move(b));
+    }
+    size_t nb = 0;
+    for (auto& b : bocos) nb += b.iface.size();
+    if ((int)nb != nfl) return fail("tagged faces do not match the boundary faces");
+  }
+  const int ncell = ncell_int + nfl;
+
+  // ---- geometry (operation order of MESHGEOM.f90) ----
+  std::vector<V3> fn(nface), fc(nface), cc(ncell, mk(0, 0, 0));
+  std::vector<double> fs(nface), cv(ncell, 0.0);
+  auto X = [&](int iv) { return um->nodes[iv - 1]; };
+  for (int f = 0; f < nface; ++f) {
+    const int* v = &FV[4 * (size_t)f];
+    if (dim == 2) {
+      if (FN[f] != 2) return fail("2D meshes need 2-vertex faces");
+      V3 nrm = cross(mk(0., 0., 1.), sub(X(v[1]), X(v[0])));
+      double s = norm(nrm);
+      fn[f] = dvd(nrm, s);
+      fs[f] = s;
+      fc[f] = scl(0.5, add(X(v[0]), X(v[1])));
+    } else if (FN[f] == 3) {
+      V3 a = X(v[0]), b = X(v[1]), c = X(v[2]);
+      V3 nrm = scl(0.5, cross(sub(b, a), sub(c, a)));
+      double s = norm(nrm);
+      fn[f] = dvd(nrm, s);
+      fs[f] = s;
+      fc[f] = dvd(add(add(a, b), c), 3.0);
+    } else if (FN[f] == 4) {
+      V3 a = X(v[0]), b = X(v[1]), c = X(v[2]), d = X(v[3]);
+      V3 nrm = scl(0.5, cross(sub(b, a), sub(c, a)));
+      double s1 = norm(nrm);
+      V3 cg1 = dvd(add(add(a, b), c), 3.0);
+      V3 pt = scl(0.5, cross(sub(c, a), sub(d, a)));
+      double s2 = norm(pt);
+      V3 cg2 = dvd(add(add(a, c), d), 3.0);
+      nrm = add(nrm, pt);
+      double s = norm(nrm);
+      fn[f] = dvd(nrm, s);
+      fs[f] = s;
+      fc[f] = dvd(add(scl(s1, cg1), scl(s2, cg2)), s1 + s2);
+    } else {
+      return fail("faces with 3 or 4 vertices expected in 3D");
+    }
+  }
+  {
+    std::vector<V3> mid(ncell_int, mk(0, 0, 0));
+    std::vector<int> nb(ncell_int, 0);
+    for (int f = 0; f < nface; ++f) {
+      int a = F1[f] - 1;
+      mid[a] = add(mid[a], fc[f]);
+      nb[a]++;
+      if (F2[f] > 0 && F2[f] <= ncell_int) {
+        int b = F2[f] - 1;
+        mid[b] = add(mid[b], fc[f]);
+        nb[b]++;
+      }
+    }
+    for (int c = 0; c < ncell_int; ++c) mid[c] = dvd(mid[c], (double)nb[c]);
+    const double kcg = dim == 2 ? 1.0 / 3.0 : 1.0 / 4.0;
+    const double kvol = dim == 2 ? 1.0 / 2.0 : 1.0 / 3.0;
+    auto elem = [&](V3 vK, int f, V3& cg, double& vol) {
+      V3 vKH = sub(fc[f], vK);
+      double h = std::fabs(dot(vKH, fn[f]));
+      cg = sub(fc[f], scl(kcg, vKH));
+      vol = kvol * h * fs[f];
+    };
+    for (int f = 0; f < nface; ++f) {
+      V3 cg; double vol;
+      int a = F1[f] - 1;
+      elem(mid[a], f, cg, vol);
+      cc[a] = add(cc[a], scl(vol, cg));
+      cv[a] = cv[a] + vol;
+      if (F2[f] > 0 && F2[f] <= ncell_int) {
+        int b = F2[f] - 1;
+        elem(mid[b], f, cg, vol);
+        cc[b] = add(cc[b], scl(vol, cg));
+        cv[b] = cv[b] + vol;
+      }
+    }
+    for (int c = 0; c < ncell_int; ++c) {
+      if (!(cv[c] > 0.0)) return fail("degenerate cell (zero volume)");
+      cc[c] = dvd(cc[c], cv[c]);
+    }
+  }
+  for (int f = 0; f < nface; ++f)
+    if (F2[f] != 0 && F1[f] > F2[f]) std::swap(F1[f], F2[f]);
+  for (int f = 0; f < nface; ++f) {
+    V3 v12 = F2[f] != 0 ? sub(cc[F2[f] - 1], cc[F1[f] - 1]) : sub(fc[f], cc[F1[f] - 1]);
+    if (dot(v12, fn[f]) < 0.0) fn[f] = mk(-fn[f].x, -fn[f].y, -fn[f].z);
+  }
+
+  // ---- greedy colouring: the first colour free at both cells (boundary: one cell) ----
+  std::vector<int> color(nface);
+  {
+    std::vector<std::vector<int>> vcol(ncell);
+    int ncolor = 0;
+    for (int f = 0; f < nface; ++f) {
+      int a = F1[f] - 1;
+      int b = (F2[f] == 0 || F2[f] > ncell) ? a : F2[f] - 1;
+      int chosen = -1;
+      for (int ic = 0; ic < ncolor && chosen < 0; ++ic) {
+        bool used = std::find(vcol[a].begin(), vcol[a].end(), ic) != vcol[a].end() ||
+                    std::find(vcol[b].begin(), vcol[b].end(), ic) != vcol[b].end();
+        if (!used) chosen = ic;
+      }
+      if (chosen < 0) chosen = ncolor++;
+      color[f] = chosen;
+      vcol[a].push_back(chosen);
+      vcol[b].push_back(chosen);
+    }
+  }
+
+  // ---- ghost cells: physical boundaries first, then periodic connections ----
+  std::vector<int> fbc(nface, TY_BC_INTERIOR), fpart(nface, 0);
+  std::vector<double> fwall(3 * (size_t)nface, 0.0);
+  int nlim = 0;
+  for (auto& b : bocos) {
+    for (size_t i = 0; i < um->bcs.size(); ++i)
+      if (um->bcs[i].kind != TY_BC_PERIODIC && um->bcs[i].family == b.family) { b.def = (int)i; break; }
+    if (b.def >= 0) {
+      const BcIn& d = um->bcs[b.def];
+      b.kind = d.kind;
+      for (int f : b.iface) {
+        ++nlim;
+        int a = F1[f] - 1, g = ncell_int + nlim - 1;
+        F2[f] = g + 1;
+        fbc[f] = d.kind;
+        fwall[3 * (size_t)f] = d.wallvel.x; fwall[3 * (size_t)f + 1] = d.wallvel.y; fwall[3 * (size_t)f + 2] = d.wallvel.z;
+        cv[g] = cv[a];
+        if (d.kind == TY_BC_SYMMETRY) {
+          V3 n = fn[f], gc = cc[a];
+          cc[g] = add(gc, scl(2.0 * dot(sub(fc[f], gc), n), n));
+        } else {
+          cc[g] = sub(scl(2.0, fc[f]), cc[a]);
+        }
+      }
+      continue;
+    }
+    for (size_t i = 0; i < um->bcs.size(); ++i) {
+      if (um->bcs[i].kind != TY_BC_PERIODIC) continue;
+      if (um->bcs[i].family == b.family) { b.def = (int)i; b.rlink = 1.0; break; }
+      if (um->bcs[i].partner == b.family) { b.def = (int)i; b.rlink = -1.0; break; }
+    }
+    if (b.def < 0) return fail("a boundary family has no definition");
+    b.kind = TY_BC_PERIODIC;
+  }
+  for (auto& b : bocos) {
+    if (b.kind != TY_BC_PERIODIC) continue;
+    const BcIn& d = um->bcs[b.def];
+    Boco* b2 = nullptr;
+    for (auto& o : bocos)
+      if (o.kind == TY_BC_PERIODIC && o.def == b.def && o.rlink * b.rlink < 0) {
+        if (b2) return fail("too many matching periodic families");
+        b2 = &o;
+      }
+    if (!b2 || b2->iface.size() != b.iface.size()) return fail("no matching periodic family");
+    // nearest partner face centre to each translated face centre (spatial hash, ties to the
+    // lowest index as in matching_index)
+    const size_t nf = b.iface.size();
+    double h = std::numeric_limits<double>::max();
+    for (int f : b2->iface) h = std::min(h, std::sqrt(fs[f]));
+    if (!(h > 0.0)) h = 1.0;
+    auto cell_of = [&](V3 p) {
+      return std::array<long long, 3>{(long long)std::floor(p.x / h), (long long)std::floor(p.y / h),
+                                      (long long)std::floor(p.z / h)};
+    };
+    struct AH { size_t operator()(const std::array<long long, 3>& a) const {
+      return (size_t)(a[0] * 73856093LL ^ a[1] * 19349663LL ^ a[2] * 83492791LL); } };
+    std::unordered_map<std::array<long long, 3>, std::vector<int>, AH> grid;
+    for (size_t k = 0; k < nf; ++k) grid[cell_of(fc[b2->iface[k]])].push_back((int)k);
+    b.partner.resize(nf);
+    for (size_t k = 0; k < nf; ++k) {
+      V3 p = fc[b.iface[k]];
+      p = add(p, scl(b.rlink, d.trans));
+      auto c0 = cell_of(p);
+      double best = std::numeric_limits<double>::max();
+      int ib = -1;
+      for (long long dx = -1; dx <= 1; ++dx)
+        for (long long dy = -1; dy <= 1; ++dy)
+          for (long long dz = -1; dz <= 1; ++dz) {
+            auto it = grid.find({c0[0] + dx, c0[1] + dy, c0[2] + dz});
+            if (it == grid.end()) continue;
+            for (int j : it->second) {
+              double dist = norm(sub(p, fc[b2->iface[j]]));
+              if (dist < best || (dist == best && j < ib)) { best = dist; ib = j; }
+            }
+          }
+      if (ib < 0 || !(best <= 1e-6 * h)) return fail("periodic faces do not match");
+      b.partner[k] = b2->iface[ib];
+    }
+    for (int f : b.iface) {
+      ++nlim;
+      F2[f] = ncell_int + nlim;
+    }
+    for (size_t k = 0; k < nf; ++k) {
+      int f = b.iface[k], fp = b.partner[k];
+      int g = F2[f] - 1, icper = F1[fp] - 1;
+      V3 dfc = sub(cc[icper], fc[fp]);
+      cv[g] = cv[icper];
+      cc[g] = add(fc[f], dfc);
+      fbc[f] = TY_BC_PERIODIC;
+      fpart[f] = fp + 1;
+    }
+  }
+  for (int f = 0; f < nface; ++f)
+    if (F2[f] == 0) return fail("boundary face without ghost cell");
+
+  // ---- export ----
+  um->ncell_int = ncell_int; um->ncell = ncell; um->nface_int = nfi; um->nface = nface;
+  um->facecell.resize(2 * (size_t)nface);
+  for (int f = 0; f < nface; ++f) { um->facecell[f] = F1[f]; um->facecell[nface + f] = F2[f]; }
+  um->facevtex.assign(FV.begin(), FV.end());
+  for (int f = 0; f < nface; ++f)
+    for (int k = FN[f]; k < 4; ++k) um->facevtex[4 * (size_t)f + k] = 0;
+  um->fnormal.resize(3 * (size_t)nface); um->fcentre.resize(3 * (size_t)nface); um->fsurf = fs;
+  for (int f = 0; f < nface; ++f) {
+    um->fnormal[3 * (size_t)f] = fn[f].x; um->fnormal[3 * (size_t)f + 1] = fn[f].y; um->fnormal[3 * (size_t)f + 2] = fn[f].z;
+    um->fcentre[3 * (size_t)f] = fc[f].x; um->fcentre[3 * (size_t)f + 1] = fc[f].y; um->fcentre[3 * (size_t)f + 2] = fc[f].z;
+  }
+  um->ccentre.resize(3 * (size_t)ncell);
+  for (int c = 0; c < ncell; ++c) {
+    um->ccentre[3 * (size_t)c] = cc[c].x; um->ccentre[3 * (size_t)c + 1] = cc[c].y; um->ccentre[3 * (size_t)c + 2] = cc[c].z;
+  }
+  um->cvol = cv;
+  um->fcolor = color;
+  um->fbc = fbc;
+  um->fpartner = fpart;
+  um->fwallvel = fwall;
+  um->built = true;
+  return TY_OK;
+}
+
+int ty_umesh_desc(const ty_umesh* um, ty_mesh_desc* d) {
+  if (!um || !d || !um->built) return TY_ERR_STATE;
+  d->dim = um->dim;
+  d->ncell_int = um->ncell_int; d->ncell = um->ncell;
+  d->nface_int = um->nface_int; d->nface = um->nface;
+  d->facecell = um->facecell.data();
+  d->face_normal = um->fnormal.data();
+  d->face_surface = um->fsurf.data();
+  d->face_centre = um->fcentre.data();
+  d->cell_centre = um->ccentre.data();
+  d->cell_volume = um->cvol.data();
+  d->face_color = um->fcolor.data();
+  d->face_bc = um->fbc.data();
+  d->face_partner = um->fpartner.data();
+  d->face_wallvel = um->fwallvel.data();
+  return TY_OK;
+}
+
+int ty_umesh_facevtex(const ty_umesh* um, int32_t* out) {
+  if (!um || !out || !um->built) return TY_ERR_STATE;
+  std::memcpy(out, um->facevtex.data(), um->facevtex.size() * sizeof(int32_t));
+  return TY_OK;
+}
+
+}  // extern "C"

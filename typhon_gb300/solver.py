@@ -1,0 +1,165 @@
+"""Host-side mirror of Typhon's zone-integration interface on top of the C ABI.
+
+``Grid`` plays the role of Typhon's st_grid for one zone on one GPU: it owns the device
+mesh (ty_mesh) and its resident state, and exposes the calls that Typhon's drivers make,
+under the same names and with the same meaning:
+
+  calc_zonetimestep      SOURCE/ZONE/calc_zonetimestep.f90:10 (global stability dt)
+  integration_grid       SOURCE/MAIN/integration_grid.f90:8 (zone residual dt/V sum F S)
+  treelevel_rungekutta   SOURCE/MAIN/treelevel_rungekutta.f90:8 + update_field.f90:9
+  integration_cyclezone  SOURCE/MAIN/integration_cyclezone.f90:11 (unsteady cycle loop)
+
+Errors that Typhon turns into error_stop are raised as TyphonError with the library's
+status code.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from .umesh import MeshDesc
+
+# option names as in Typhon's SPAT_PARAM / TIME_PARAM blocks (SOURCE/PARAM/def_spat.f90,
+# def_time.f90) -> C ABI enum values
+SCHEME = {"HLLC": 1, "RUSANOV": 2, "ROE": 3}
+HIGHRES = {"NONE": 0, "MUSCL": 1, "MUSCL-FAST": 2, "MUSCL-UNS": 3}
+LIMITER = {"NONE": 0, "MINMOD": 1, "ALBADA": 2, "VAN_ALBADA": 2, "VAN_LEER": 3, "VANLEER": 3, "SUPERBEE": 4,
+           "KIM3": 5, "LIM03": 6}
+POSTLIM = {"NONE": 0, "BARTH": 1, "SUPERBARTH": 2}
+GRADMETH = {"NONE": 0, "LSQ": 1, "W-LSQ": 2}
+RK_METHOD = {"RK2": 1, "RK2-SSP": 2, "RK3-SSP": 3, "RK4": 4, "RK25BB": 5, "RK26BB": 6, "RK12BS": 7, "RK13BS": 8}
+MODE = {"exact": 0, "fast": 1}
+
+
+def prim_to_cons(prim, gamma=1.4):
+    """calc_varcons_ns (SOURCE/EQNS/calc_varcons_ns.f90:37-46), same operation order."""
+    rho, p, u, v, w = prim
+    ig1 = 1.0 / (gamma - 1.0)
+    cons = np.empty_like(prim)
+    cons[0] = rho
+    cons[1] = ig1 * p + 0.5 * rho * (u * u + v * v + w * w)
+    cons[2], cons[3], cons[4] = rho * u, rho * v, rho * w
+    return cons
+
+
+class Grid:
+    """One zone grid resident on one GPU."""
+
+    def __init__(self, mesh: MeshDesc, device=0):
+        self.mesh = mesh
+        self.lib = _capi.lib()
+        self._desc = mesh.to_c()
+        h = C.c_void_p()
+        _capi.check(self.lib.ty_mesh_create(C.byref(self._desc), int(device), C.byref(h)), "ty_mesh_create")
+        self.h = h
+        self.nci = mesh.ncell_int
+        self.gamma = 1.4
+        self.time = 0.0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ty_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def info(self):
+        out = np.zeros(5, np.int32)
+        _capi.check(self.lib.ty_mesh_info(self.h, out.ctypes.data), "ty_mesh_info")
+        return dict(zip(("ncell_int", "ncell", "nface_int", "nface", "max_faces_per_cell"), map(int, out)))
+
+    # -- def_spat --------------------------------------------------------------------------
+    def set_spat(self, scheme="HLLC", highres="NONE", limiter="ALBADA", postlim="NONE", gradmeth=None,
+                 mode="exact", gamma=1.4, entropy_fix=0.1):
+        """SPAT_PARAM: SCHEME, HIGHRES, LIMITER, POST-LIMITER, GRADMETH (LSQ by default with
+        MUSCL, none for first order, as get_gradientmethod in SOURCE/PARAM/MENU_NUM.f90)."""
+        if gradmeth is None:
+            gradmeth = "NONE" if highres == "NONE" else "LSQ"
+        p = _capi.SpatParams(SCHEME[scheme], HIGHRES[highres], LIMITER[limiter], POSTLIM[postlim],
+                             GRADMETH[gradmeth], MODE[mode], float(gamma), float(entropy_fix))
+        _capi.check(self.lib.ty_set_params(self.h, C.byref(p)), "ty_set_params")
+        self.gamma = gamma
+
+    # -- state -----------------------------------------------------------------------------
+    def set_cons(self, cons):
+        """Conserved state [5][ncell_int] (rho, rhoE, rhou, rhov, rhow), host array."""
+        cons = np.ascontiguousarray(cons, np.float64).reshape(5, -1)[:, :self.nci]
+        rho = np.ascontiguousarray(cons[0])
+        rhoE = np.ascontiguousarray(cons[1])
+        rhou = np.ascontiguousarray(cons[2:5].T)
+        _capi.check(self.lib.ty_state_upload(self.h, rho.ctypes.data, rhoE.ctypes.data, rhou.ctypes.data),
+                    "ty_state_upload")
+
+    def set_prim(self, prim):
+        self.set_cons(prim_to_cons(np.asarray(prim, np.float64).reshape(5, -1)[:, :self.nci], self.gamma))
+
+    def get_cons(self):
+        rho = np.zeros(self.nci)
+        rhoE = np.zeros(self.nci)
+        rhou = np.zeros((self.nci, 3))
+        _capi.check(self.lib.ty_state_download(self.h, rho.ctypes.data, rhoE.ctypes.data, rhou.ctypes.data),
+                    "ty_state_download")
+        return np.vstack([rho, rhoE, rhou.T])
+
+    def get_prim(self):
+        out = np.zeros((5, self.nci))
+        _capi.check(self.lib.ty_prim_download(self.h, out.ctypes.data), "ty_prim_download")
+        return out
+
+    def set_cons_device(self, ptr):
+        _capi.check(self.lib.ty_state_upload_device(self.h, C.c_void_p(ptr)), "ty_state_upload_device")
+
+    def get_cons_device(self, ptr):
+        _capi.check(self.lib.ty_state_download_device(self.h, C.c_void_p(ptr)), "ty_state_download_device")
+
+    # -- Typhon calls ------------------------------------------------------------------------
+    def calc_zonetimestep(self, cfl):
+        dt = C.c_double()
+        _capi.check(self.lib.ty_timestep(self.h, float(cfl), C.byref(dt)), "ty_timestep")
+        return dt.value
+
+    def integration_grid(self, dt, out=True):
+        R = np.zeros((5, self.nci)) if out else None
+        _capi.check(self.lib.ty_residual(self.h, float(dt), R.ctypes.data if out else None), "ty_residual")
+        return R
+
+    def treelevel_rungekutta(self, method, dt):
+        _capi.check(self.lib.ty_rk_step(self.h, RK_METHOD[method], float(dt)), "ty_rk_step")
+        self.time += dt
+
+    def run_steps(self, method, cfl, nsteps):
+        """nsteps steps with the global stability time step, all on the device."""
+        dt = C.c_double()
+        _capi.check(self.lib.ty_rk_steps(self.h, RK_METHOD[method], float(cfl), int(nsteps), C.byref(dt)),
+                    "ty_rk_steps")
+        return dt.value
+
+    def integration_cyclezone(self, method, cfl, cycle_dt):
+        """Integrate one unsteady cycle of length cycle_dt: global stability dt, the last step
+        cut to end the cycle exactly (integration_cyclezone.f90:80-170)."""
+        cycle_time = 0.0
+        nstep = 0
+        while True:
+            dtmax = cycle_dt - cycle_time
+            dt = min(self.calc_zonetimestep(cfl), dtmax)
+            end = dt >= cycle_dt - cycle_time
+            if end:
+                dt = cycle_dt - cycle_time
+            self.treelevel_rungekutta(method, dt)
+            cycle_time = cycle_time + dt
+            nstep += 1
+            if end:
+                return nstep
+
+    def debug(self, which):
+        m = self.mesh
+        shapes = {"prim": (0, 5, m.ncell), "grad": (1, 15, m.ncell), "flux": (2, 5, m.nface),
+                  "ratio": (3, 3, m.ncell)}
+        code, rows, n = shapes[which]
+        out = np.zeros((rows, n))
+        _capi.check(self.lib.ty_debug_get(self.h, code, out.ctypes.data), "ty_debug_get")
+        return out
+
+    def synchronize(self):
+        _capi.check(self.lib.ty_synchronize(self.h), "ty_synchronize")

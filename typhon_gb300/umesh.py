@@ -1,0 +1,382 @@
+"""Element meshes: Typhon's .tym (XBIN) format, synthetic generators, and preprocessing.
+
+``RawMesh`` holds what a .tym file holds (nodes, element sections, boundary marks).
+``preprocess`` runs the library's native preprocessing (ty_umesh_*, the equivalent of
+Typhon's grid_preproc + init_connect_grid) and returns a ``MeshDesc`` with the arrays that
+``ty_mesh_create`` takes.
+
+Formats and conventions restated from the reference:
+  XBIN stream header and data sections   CFDTOOLS/FileFormat/internal/XBIN_IO.f90:70-135,
+                                         XBIN_DATA.f90:139-215
+  TYPHON mesh sections                   CFDTOOLS/FileFormat/internal/TYFMT_MESH.f90,
+                                         TYPHON_FMT.f90:95-170
+  structured 2D generators (quad, tri)   CFDTOOLS/FileFormat/ty2dmesh.f90:612-744
+"""
+import ctypes as C
+import struct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi
+
+# element types (CFDTOOLS/Mesh/ELEMVTEX.f90:17-37)
+ELEM_BAR2, ELEM_TRI3, ELEM_QUAD4, ELEM_TETRA4, ELEM_PENTA6, ELEM_HEXA8 = 2, 13, 24, 101, 131, 141
+NVTEX = {ELEM_BAR2: 2, ELEM_TRI3: 3, ELEM_QUAD4: 4, ELEM_TETRA4: 4, ELEM_PENTA6: 6, ELEM_HEXA8: 8}
+DIM = {ELEM_BAR2: 1, ELEM_TRI3: 2, ELEM_QUAD4: 2, ELEM_TETRA4: 3, ELEM_PENTA6: 3, ELEM_HEXA8: 3}
+
+BC_PERIODIC, BC_SYMMETRY, BC_WALL = 1, 2, 3
+
+
+@dataclass
+class RawMesh:
+    vtex: np.ndarray                                   # (nvtex, 3) float64
+    sections: list = field(default_factory=list)       # [(elemtype, ielem int32[n], conn int32[n, nv])]
+    marks: list = field(default_factory=list)          # [(family, tags int32[])]
+
+    @property
+    def ncell(self):
+        dmax = max(DIM[t] for t, _, _ in self.sections)
+        return sum(len(ie) for t, ie, _ in self.sections if DIM[t] == dmax)
+
+
+# ---------------------------------------------------------------------------
+# XBIN / TYPHON format
+_XBIN_HEADER = b"XBIN"
+
+
+def _section_head(f, datatype, name, usertype, params=(), string=b""):
+    f.write(struct.pack("<h", datatype))
+    f.write(name.encode().ljust(32)[:32])
+    f.write(struct.pack("<hhhhh", 0, usertype, 4, 8, len(params)))
+    if params:
+        f.write(np.asarray(params, dtype="<i4").tobytes())
+    f.write(struct.pack("<h", len(string)))
+    f.write(string)
+
+
+def write_tym(path, raw: RawMesh):
+    """Write a TYPHON mesh file (XBIN version 2, TYPHON format version 3)."""
+    cells = [s for s in raw.sections if DIM[s[0]] == max(DIM[t] for t, _, _ in raw.sections)]
+    faces = [s for s in raw.sections if s not in cells]
+    with open(path, "wb") as f:
+        f.write(_XBIN_HEADER + bytes([0, 2]) + bytes([4, 3, 2, 1]))
+        _section_head(f, 1, "FILE_HEADER", 1, (3, 10, 1, 0, 11))
+        f.write(b"END")
+        ncell = sum(len(s[1]) for s in cells)
+        nface = sum(len(s[1]) for s in faces)
+        _section_head(f, 1, "USTMESH", 10, (0, ncell, nface, len(raw.vtex), len(cells), len(faces), 0,
+                                             len(raw.marks)))
+        f.write(b"END")
+        for typ, ielem, conn in cells:
+            _section_head(f, 15, "CELLS", 12, (typ,))
+            f.write(struct.pack("<ii", len(ielem), NVTEX[typ]))
+            f.write(np.asarray(ielem, "<i4").tobytes())
+            f.write(np.asarray(conn, "<i4").tobytes())
+            f.write(b"END")
+        _section_head(f, 20, "NODES", 11)
+        f.write(struct.pack("<iii", 1, len(raw.vtex), 3))
+        f.write(np.asarray(raw.vtex, "<f8").tobytes())
+        f.write(b"END")
+        for typ, ielem, conn in faces:
+            _section_head(f, 15, "FACES", 15, (typ,))
+            f.write(struct.pack("<ii", len(ielem), NVTEX[typ]))
+            f.write(np.asarray(ielem, "<i4").tobytes())
+            f.write(np.asarray(conn, "<i4").tobytes())
+            f.write(b"END")
+        for name, tags in raw.marks:
+            _section_head(f, 10, name, 20)
+            f.write(struct.pack("<iii", 1, len(tags), 0))
+            f.write(np.asarray(tags, "<i4").tobytes())
+            f.write(b"END")
+
+
+class _Reader:
+    def __init__(self, data):
+        self.d = data
+        self.p = 0
+
+    def take(self, n):
+        if self.p + n > len(self.d):
+            raise ValueError("truncated XBIN file")
+        b = self.d[self.p:self.p + n]
+        self.p += n
+        return b
+
+    def i16(self):
+        return struct.unpack("<h", self.take(2))[0]
+
+    def i32(self, n=1):
+        v = np.frombuffer(self.take(4 * n), "<i4")
+        return int(v[0]) if n == 1 else v.copy()
+
+    def head(self, version):
+        h = dict(datatype=self.i16(), name=self.take(32).decode().rstrip(" \0"))
+        h["groupindex"], h["usertype"], h["intsize"], h["realsize"] = (self.i16() for _ in range(4))
+        n = self.i16()
+        h["param"] = [int(x) for x in np.atleast_1d(self.i32(n))] if n > 0 else []
+        h["string"] = ""
+        if version >= 2:
+            sl = self.i16()
+            h["string"] = self.take(sl).decode() if sl > 0 else ""
+        if h["intsize"] != 4 or h["realsize"] != 8:
+            raise ValueError("unexpected integer/real size in XBIN section " + h["name"])
+        if h["datatype"] in (10, 20):
+            h["firstindex"], h["nelem"], h["dim"] = self.i32(), self.i32(), self.i32()
+        elif h["datatype"] in (15, 25):
+            h["nelem"], h["dim"] = self.i32(), self.i32()
+        return h
+
+    def end(self):
+        if self.take(3) != b"END":
+            raise ValueError("bad end of XBIN data section")
+
+
+def read_tym(path) -> RawMesh:
+    """Read a TYPHON mesh file (little-endian XBIN, mesh_full)."""
+    with open(path, "rb") as f:
+        r = _Reader(f.read())
+    if r.take(4) != _XBIN_HEADER:
+        raise ValueError("not a XBIN file")
+    v = r.take(2)
+    version = v[0] * 256 + v[1]
+    if r.take(4) != bytes([4, 3, 2, 1]):
+        raise ValueError("only little-endian XBIN files are supported")
+    h = r.head(version)
+    r.end()
+    ty_version = h["param"][0]
+    mh = r.head(version)
+    r.end()
+    p = mh["param"]
+    if ty_version == 1:
+        ncellsec, nfacesec, nmark = p[4], p[5], p[6]
+    else:
+        ncellsec, nfacesec, nmark = p[4], p[5], p[7]
+    if mh["string"]:
+        raise ValueError("shared meshes are not supported")
+
+    def elems(usertype):
+        eh = r.head(version)
+        if eh["usertype"] != usertype:
+            raise ValueError("unexpected section " + eh["name"])
+        typ, n, nv = eh["param"][0], eh["nelem"], eh["dim"]
+        if eh["datatype"] == 15:
+            ielem = r.i32(n) if n > 1 else np.array([r.i32()], np.int32)
+        else:
+            ielem = np.arange(eh["firstindex"], eh["firstindex"] + n, dtype=np.int32)
+        conn = np.frombuffer(r.take(4 * n * nv), "<i4").reshape(n, nv).copy()
+        r.end()
+        return typ, np.asarray(ielem, np.int32), conn
+
+    raw = RawMesh(vtex=np.zeros((0, 3)))
+    for _ in range(ncellsec):
+        raw.sections.append(elems(12))
+    nh = r.head(version)
+    raw.vtex = np.frombuffer(r.take(8 * nh["nelem"] * nh["dim"]), "<f8").reshape(nh["nelem"], nh["dim"]).copy()
+    r.end()
+    for _ in range(nfacesec):
+        raw.sections.append(elems(15))
+    for _ in range(nmark):
+        mh2 = r.head(version)
+        tags = np.frombuffer(r.take(4 * mh2["nelem"]), "<i4").copy()
+        r.end()
+        raw.marks.append((mh2["name"], tags))
+    return raw
+
+
+# ---------------------------------------------------------------------------
+# Generators
+def gen_grid2d(ni, nj, lx, ly, kind="tri", jitter=0.0, seed=1234):
+    """Structured 2D grid on [0,lx]x[0,ly] in the numbering of ty2dmesh (ty2dmesh.f90:612-744).
+
+    kind: "quad" (QUAD4) or "tri" (each quad split into (a,c,b) and (b,c,d)).  jitter moves
+    every interior node by U(-jitter*h, +jitter*h) in x and y (numpy default_rng(seed));
+    boundary nodes stay on the box so that periodic faces match.  Marks: IMIN, IMAX, JMIN,
+    JMAX (BAR2 face elements numbered 1..2(ni+nj)).
+    """
+    i = np.arange(ni + 1)[:, None]
+    j = np.arange(nj + 1)[None, :]
+    hx, hy = lx / ni, ly / nj
+    x = np.broadcast_to(i * hx, (ni + 1, nj + 1)).astype(np.float64).copy()
+    y = np.broadcast_to(j * hy, (ni + 1, nj + 1)).astype(np.float64).copy()
+    if jitter > 0:
+        rng = np.random.default_rng(seed)
+        dx = rng.uniform(-jitter * hx, jitter * hx, size=(ni + 1, nj + 1))
+        dy = rng.uniform(-jitter * hy, jitter * hy, size=(ni + 1, nj + 1))
+        inner = np.zeros((ni + 1, nj + 1), bool)
+        inner[1:-1, 1:-1] = True
+        x[inner] += dx[inner]
+        y[inner] += dy[inner]
+    vtex = np.stack([x.reshape(-1), y.reshape(-1), np.zeros((ni + 1) * (nj + 1))], axis=1)
+    I, J = np.meshgrid(np.arange(1, ni + 1), np.arange(1, nj + 1), indexing="ij")
+    I, J = I.reshape(-1), J.reshape(-1)
+    iva = (I - 1) * (nj + 1) + J
+    ivb, ivc, ivd = iva + 1, iva + (nj + 1), iva + 1 + (nj + 1)
+    if kind == "quad":
+        conn = np.stack([iva, ivc, ivd, ivb], axis=1).astype(np.int32)
+        sec = (ELEM_QUAD4, np.arange(1, ni * nj + 1, dtype=np.int32), conn)
+    else:
+        conn = np.empty((2 * ni * nj, 3), np.int32)
+        conn[0::2] = np.stack([iva, ivc, ivb], axis=1)
+        conn[1::2] = np.stack([ivb, ivc, ivd], axis=1)
+        sec = (ELEM_TRI3, np.arange(1, 2 * ni * nj + 1, dtype=np.int32), conn)
+    jj = np.arange(1, nj + 1)
+    ii = np.arange(1, ni + 1)
+    bar_imin = np.stack([jj, jj + 1], 1)
+    base = ni * (nj + 1)
+    bar_imax = np.stack([base + jj, base + jj + 1], 1)
+    bar_jmin = np.stack([(ii - 1) * (nj + 1) + 1, ii * (nj + 1) + 1], 1)
+    bar_jmax = np.stack([ii * (nj + 1), (ii + 1) * (nj + 1)], 1)
+    bars = np.concatenate([bar_imin, bar_imax, bar_jmin, bar_jmax]).astype(np.int32)
+    nb = len(bars)
+    fsec = (ELEM_BAR2, np.arange(1, nb + 1, dtype=np.int32), bars)
+    marks = [("IMIN", np.arange(1, nj + 1, dtype=np.int32)),
+             ("IMAX", np.arange(nj + 1, 2 * nj + 1, dtype=np.int32)),
+             ("JMIN", np.arange(2 * nj + 1, 2 * nj + ni + 1, dtype=np.int32)),
+             ("JMAX", np.arange(2 * nj + ni + 1, 2 * (nj + ni) + 1, dtype=np.int32))]
+    return RawMesh(vtex=vtex, sections=[sec, fsec], marks=marks)
+
+
+def gen_tet_box(n, length, jitter=0.0, seed=1234):
+    """n^3 hexahedra on [0,length]^3, each split into 5 tetrahedra with alternating parity
+    (conforming, also across periodic boundaries for even n); interior nodes jittered by
+    U(-jitter*h, +jitter*h) per coordinate (numpy default_rng(seed)).  Boundary triangles
+    are marked IMIN/IMAX (x), JMIN/JMAX (y), KMIN/KMAX (z)."""
+    h = length / n
+    g = np.arange(n + 1) * h
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    vt = np.stack([X, Y, Z], axis=-1).reshape(-1, 3).astype(np.float64)
+    if jitter > 0:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-jitter * h, jitter * h, size=vt.shape)
+        idx = np.arange(n + 1)
+        inner = ((idx[:, None, None] > 0) & (idx[:, None, None] < n) &
+                 (idx[None, :, None] > 0) & (idx[None, :, None] < n) &
+                 (idx[None, None, :] > 0) & (idx[None, None, :] < n)).reshape(-1)
+        vt[inner] += d[inner]
+
+    def vid(i, j, k):
+        return (i * (n + 1) + j) * (n + 1) + k + 1
+
+    I, J, K = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    I, J, K = I.reshape(-1), J.reshape(-1), K.reshape(-1)
+    v = [vid(I, J, K), vid(I + 1, J, K), vid(I + 1, J + 1, K), vid(I, J + 1, K),
+         vid(I, J, K + 1), vid(I + 1, J, K + 1), vid(I + 1, J + 1, K + 1), vid(I, J + 1, K + 1)]
+    v = np.stack(v, axis=1)
+    even = ((I + J + K) % 2 == 0)[:, None]
+    tets_even = [(1, 3, 4, 6), (0, 1, 3, 4), (2, 3, 1, 6), (5, 4, 6, 1), (7, 6, 4, 3)]
+    tets_odd = [(0, 2, 5, 7), (1, 0, 2, 5), (3, 2, 0, 7), (4, 5, 7, 0), (6, 7, 5, 2)]
+    conn = np.empty((len(I), 5, 4), np.int32)
+    for t in range(5):
+        conn[:, t, :] = np.where(even, v[:, list(tets_even[t])], v[:, list(tets_odd[t])])
+    conn = conn.reshape(-1, 4)
+    # boundary triangles: faces seen once
+    fl = np.concatenate([conn[:, [0, 2, 1]], conn[:, [0, 1, 3]], conn[:, [1, 2, 3]], conn[:, [2, 0, 3]]])
+    key = np.sort(fl, axis=1)
+    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    bnd = fl[cnt[inv.reshape(-1)] == 1]
+    cen = vt[bnd - 1].mean(axis=1)
+    tol = 1e-9 * length
+    names = [("IMIN", 0, 0.0), ("IMAX", 0, length), ("JMIN", 1, 0.0), ("JMAX", 1, length),
+             ("KMIN", 2, 0.0), ("KMAX", 2, length)]
+    faces, marks, nextid = [], [], 1
+    for name, ax, val in names:
+        sel = bnd[np.abs(cen[:, ax] - val) < tol]
+        ids = np.arange(nextid, nextid + len(sel), dtype=np.int32)
+        nextid += len(sel)
+        faces.append(sel)
+        marks.append((name, ids))
+    fconn = np.concatenate(faces).astype(np.int32)
+    secs = [(ELEM_TETRA4, np.arange(1, len(conn) + 1, dtype=np.int32), conn),
+            (ELEM_TRI3, np.arange(1, len(fconn) + 1, dtype=np.int32), fconn)]
+    return RawMesh(vtex=vt, sections=secs, marks=marks)
+
+
+# ---------------------------------------------------------------------------
+def periodic_box_bcs(lengths):
+    """Periodic connections IMIN<->IMAX, JMIN<->JMAX (and KMIN<->KMAX in 3D)."""
+    out = [("IMIN", BC_PERIODIC, "IMAX", (lengths[0], 0.0, 0.0)),
+           ("JMIN", BC_PERIODIC, "JMAX", (0.0, lengths[1], 0.0))]
+    if len(lengths) > 2:
+        out.append(("KMIN", BC_PERIODIC, "KMAX", (0.0, 0.0, lengths[2])))
+    return out
+
+
+class MeshDesc:
+    """Preprocessed mesh (numpy copies of the ty_mesh_desc arrays, 0-based where noted)."""
+
+    def __init__(self, d, facevtex):
+        nf, nc = d.nface, d.ncell
+
+        def arr(ptr, n, dt):
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(dt)), shape=(n,)).copy()
+
+        self.dim, self.ncell_int, self.ncell = d.dim, d.ncell_int, d.ncell
+        self.nface_int, self.nface = d.nface_int, d.nface
+        self.facecell = arr(d.facecell, 2 * nf, C.c_int32)          # 1-based, fils(nf,2)
+        self.face_normal = arr(d.face_normal, 3 * nf, C.c_double).reshape(nf, 3)
+        self.face_surface = arr(d.face_surface, nf, C.c_double)
+        self.face_centre = arr(d.face_centre, 3 * nf, C.c_double).reshape(nf, 3)
+        self.cell_centre = arr(d.cell_centre, 3 * nc, C.c_double).reshape(nc, 3)
+        self.cell_volume = arr(d.cell_volume, nc, C.c_double)
+        self.face_color = arr(d.face_color, nf, C.c_int32)
+        self.face_bc = arr(d.face_bc, nf, C.c_int32)
+        self.face_partner = arr(d.face_partner, nf, C.c_int32)      # 1-based, 0 = none
+        self.face_wallvel = arr(d.face_wallvel, 3 * nf, C.c_double).reshape(nf, 3)
+        self.facevtex = facevtex
+
+    @property
+    def fc1(self):
+        return self.facecell[:self.nface] - 1
+
+    @property
+    def fc2(self):
+        return self.facecell[self.nface:] - 1
+
+    def to_c(self):
+        """A ty_mesh_desc pointing into this object's arrays (keep the object alive)."""
+        for k in ("facecell", "face_color", "face_bc", "face_partner"):
+            setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.int32))
+        for k in ("face_normal", "face_surface", "face_centre", "cell_centre", "cell_volume", "face_wallvel"):
+            setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.float64))
+        d = _capi.MeshDesc()
+        d.dim, d.ncell_int, d.ncell, d.nface_int, d.nface = (self.dim, self.ncell_int, self.ncell,
+                                                             self.nface_int, self.nface)
+        for k in ("facecell", "face_normal", "face_surface", "face_centre", "cell_centre", "cell_volume",
+                  "face_color", "face_bc", "face_partner", "face_wallvel"):
+            setattr(d, k, getattr(self, k).ctypes.data)
+        return d
+
+
+def preprocess(raw: RawMesh, dim, bcs) -> MeshDesc:
+    """Native preprocessing (ty_umesh_*): faces, geometry, colours, ghosts, periodicity.
+
+    bcs: [(family, kind, partner, translation(3)[, wall_velocity(3)])]
+    """
+    L = _capi.lib()
+    h = C.c_void_p()
+    _capi.check(L.ty_umesh_new(C.byref(h)), "ty_umesh_new")
+    try:
+        vt = np.ascontiguousarray(raw.vtex, np.float64)
+        _capi.check(L.ty_umesh_set_nodes(h, vt.shape[0], vt.ctypes.data), "ty_umesh_set_nodes")
+        for typ, ielem, conn in raw.sections:
+            ie = np.ascontiguousarray(ielem, np.int32)
+            cv = np.ascontiguousarray(conn, np.int32)
+            _capi.check(L.ty_umesh_add_section(h, int(typ), ie.shape[0], ie.ctypes.data, cv.ctypes.data),
+                        "ty_umesh_add_section")
+        for name, tags in raw.marks:
+            t = np.ascontiguousarray(tags, np.int32)
+            _capi.check(L.ty_umesh_add_mark(h, name.encode(), t.shape[0], t.ctypes.data), "ty_umesh_add_mark")
+        for b in bcs:
+            tr = np.ascontiguousarray(b[3] if len(b) > 3 and b[3] is not None else (0, 0, 0), np.float64)
+            wv = np.ascontiguousarray(b[4] if len(b) > 4 else (0, 0, 0), np.float64)
+            _capi.check(L.ty_umesh_add_bc(h, b[0].encode(), int(b[1]), (b[2] or "").encode(),
+                                          tr.ctypes.data, wv.ctypes.data), "ty_umesh_add_bc")
+        _capi.check(L.ty_umesh_build(h, int(dim)), "ty_umesh_build")
+        d = _capi.MeshDesc()
+        _capi.check(L.ty_umesh_desc(h, C.byref(d)), "ty_umesh_desc")
+        fv = np.zeros(4 * d.nface, np.int32)
+        _capi.check(L.ty_umesh_facevtex(h, fv.ctypes.data), "ty_umesh_facevtex")
+        return MeshDesc(d, fv.reshape(d.nface, 4))
+    finally:
+        L.ty_umesh_free(h)
