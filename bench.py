@@ -119,6 +119,19 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def fp64_peak():
+    """Measured DFMA rate of this GPU (typhon_gb300/_lib/fp64_peak), FLOP/s, or None."""
+    probe = ROOT / "typhon_gb300" / "_lib" / "fp64_peak"
+    try:
+        r = subprocess.run([str(probe)], capture_output=True, text=True, timeout=60)
+    except (OSError, subprocess.TimeoutExpired):
+        return None
+    for ln in r.stdout.splitlines():
+        if ln.startswith("DFMA:"):
+            return float(ln.split("=")[1].split()[0]) * 1e12
+    return None
+
+
 def kernel_bytes(md, nslot_avg):
     """Compulsory (algorithmic) DRAM bytes per launch of each kernel: every array element
     the kernel needs is counted once (cells and faces of the whole mesh).  FP64 = 8 B,

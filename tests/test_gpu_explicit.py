@@ -242,3 +242,44 @@ def test_negative_energy_is_reported_and_handle_survives(ty):
 def test_smoke_entry():
     import __graft_entry__ as ge
     ge.smoke()
+
+
+@pytest.mark.parametrize("kind,n", [("vortex", 12), ("tgv", 4)])
+@pytest.mark.parametrize("combo", COMBOS, ids=["-".join(c) for c in COMBOS])
+def test_fast_step_close(ty, kind, n, combo):
+    """Fast mode, every scheme/reconstruction/limiter combination: the state after two RK4
+    steps within 1e-12 relative L2 of the oracle, per conserved variable."""
+    md, om, prim = make_case(ty, kind, n)
+    g, s = pair(ty, md, om, prim, *combo, mode="fast")
+    for _ in range(2):
+        dt = s.timestep()
+        g.treelevel_rungekutta("RK4", dt)
+        s.rk_step(dt)
+    rel = relerr(g.get_cons(), s.get("cons")[:, :md.ncell_int])
+    assert np.all(rel <= FAST_RTOL), rel
+
+
+def test_caller_stream_and_kernel_timing(ty):
+    import torch
+    from typhon_gb300 import _capi
+    md, om, prim = make_case(ty, "tgv", 4)
+    g = ty.Grid(md)
+    g.set_spat("ROE", "MUSCL-UNS", "NONE", "BARTH", mode="fast")
+    g.set_prim(prim)
+    st = torch.cuda.Stream()
+    _capi.check(g.lib.ty_set_stream(g.h, st.cuda_stream), "ty_set_stream")
+    _capi.check(g.lib.ty_profile_enable(g.h, 1), "ty_profile_enable")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(st):
+        e0.record(st)
+        g.run_steps("RK3-SSP", 0.8, 2)
+        e1.record(st)
+    torch.cuda.synchronize()
+    n = len(_capi.KERNEL_NAMES)
+    ms, nl = np.zeros(n), np.zeros(n, np.int32)
+    _capi.check(g.lib.ty_profile_read(g.h, n, ms.ctypes.data, nl.ctypes.data), "ty_profile_read")
+    assert nl[_capi.KERNEL_NAMES.index("rk_update")] == 6
+    assert nl[_capi.KERNEL_NAMES.index("timestep")] == 1
+    assert 0 < ms.sum() <= e0.elapsed_time(e1) * 1.05
+    _capi.check(g.lib.ty_set_stream(g.h, None), "ty_set_stream")
+    g.run_steps("RK3-SSP", 0.8, 1)

@@ -18,6 +18,7 @@ SRC = HERE / "csrc"
 OUT_DIR = HERE / "_lib"
 OBJ_DIR = HERE / "_build"
 LIB = OUT_DIR / "libtyphon_gpu.so"
+PROBE = OUT_DIR / "fp64_peak"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -44,7 +45,7 @@ def sources():
 
 
 def up_to_date():
-    if not LIB.exists():
+    if not LIB.exists() or not PROBE.exists():
         return False
     t = LIB.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in sources())
@@ -69,6 +70,7 @@ def build(force=False, verbose=False):
     for cu, extra in (("kernels_exact.cu", ["-fmad=false"]), ("kernels_fast.cu", ["-fmad=true"])):
         obj = OBJ_DIR / (pathlib.Path(cu).stem + ".o")
         jobs.append([nvcc, *nvflags, *extra, *inc, "-c", str(SRC / cu), "-o", str(obj)])
+    jobs.append([nvcc, "-O3", ARCH, "-o", str(PROBE), str(SRC / "fp64_peak.cu")])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         logs = list(ex.map(_run, jobs))
     if verbose:

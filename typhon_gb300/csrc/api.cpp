@@ -247,9 +247,26 @@ int build_muscl_geometry(ty_mesh* h, int highres) {
     dLR[f] = d;
     uLR[f] = ux / d; uLR[lf + f] = uy / d; uLR[2 * lf + f] = uz / d;
   }
+  // fast mode: 1/dLR and, for MUSCL/-UNS without limiter, the merged weights
+  //   increment = grad q . (CF - (u.CF) u) + (q_nb - q_c) (u.CF)/dLR  (sign of the last term
+  //   folded in for the fc2 side, whose q_nb - q_c is -(q(fc2) - q(fc1)))
+  std::vector<double> inv(lf, 0.0), recw(8 * lf, 0.0);
+  for (int f = 0; f < m.nf; ++f) {
+    inv[f] = 1.0 / dLR[f];
+    if (highres == TY_HRES_MUSCLFAST) continue;
+    double u[3] = {uLR[f], uLR[lf + f], uLR[2 * lf + f]};
+    for (int side = 0; side < 2; ++side) {
+      const std::vector<double>& CF = side ? RF : LF;
+      double c[3] = {CF[f], CF[lf + f], CF[2 * lf + f]};
+      double uc = u[0] * c[0] + u[1] * c[1] + u[2] * c[2];
+      for (int k = 0; k < 3; ++k) recw[(4 * side + k) * lf + f] = c[k] - uc * u[k];
+      recw[(4 * side + 3) * lf + f] = (side ? -uc : uc) / dLR[f];
+    }
+  }
   int rc;
   if ((rc = h->upload(m.uLR, uLR)) || (rc = h->upload(m.dLR, dLR)) || (rc = h->upload(m.kLF, kLF)) ||
-      (rc = h->upload(m.kRF, kRF)) || (rc = h->upload(m.LF, LF)) || (rc = h->upload(m.RF, RF)))
+      (rc = h->upload(m.kRF, kRF)) || (rc = h->upload(m.LF, LF)) || (rc = h->upload(m.RF, RF)) ||
+      (rc = h->upload(m.invdLR, inv)) || (rc = h->upload(m.recw, recw)))
     return rc;
   h->geo_highres = highres;
   return TY_OK;
@@ -429,13 +446,22 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
   if (nslot > kMaxSlot) { tyi::set_error("more than 8 faces per cell"); return bail(TY_ERR_UNSUPPORTED); }
   m.nslot = nslot;
   h->cf.assign((size_t)nslot * nci, -1);
+  std::vector<int> cfn((size_t)nslot * nci, -1);
   std::vector<double> sumS(nci, 0.0);
   for (int c = 0; c < nci; ++c)
     for (size_t i = 0; i < lists[c].size(); ++i) {
       int e = lists[c][i].second;
+      int f = e >> 1;
       h->cf[i * (size_t)nci + c] = e;
-      sumS[c] = sumS[c] + d->face_surface[e >> 1];
+      cfn[i * (size_t)nci + c] = (e & 1) ? h->fc1[f] : h->fc2[f];
+      sumS[c] = sumS[c] + d->face_surface[f];
     }
+  std::vector<double> invV(nci), geo2(nci);
+  for (int c = 0; c < nci; ++c) {
+    if (!(d->cell_volume[c] > 0.0) || !(sumS[c] > 0.0)) { tyi::set_error("non-positive cell volume or surface"); return bail(TY_ERR_MESH); }
+    invV[c] = 1.0 / d->cell_volume[c];
+    geo2[c] = 2.0 * d->cell_volume[c] / sumS[c];
+  }
   // geometry
   h->ccentre.assign(d->cell_centre, d->cell_centre + 3 * (size_t)nc);
   h->fcentre.assign(d->face_centre, d->face_centre + 3 * (size_t)nf);
@@ -452,7 +478,8 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
   if ((rc = h->upload(m.fc1, h->fc1)) || (rc = h->upload(m.fc2, h->fc2)) || (rc = h->upload(m.fbc, fbc)) ||
       (rc = h->upload(m.part, part)) || (rc = h->upload(m.cf, h->cf)) || (rc = h->upload(m.gsrc, gsrc)) ||
       (rc = h->upload(m.gface, gface)) || (rc = h->upload(m.fn, fn)) || (rc = h->upload(m.fs, fs)) ||
-      (rc = h->upload(m.fwall, fw)) || (rc = h->upload(m.cvol, cv)) || (rc = h->upload(m.sumS, sumS)))
+      (rc = h->upload(m.fwall, fw)) || (rc = h->upload(m.cvol, cv)) || (rc = h->upload(m.sumS, sumS)) ||
+      (rc = h->upload(m.cfn, cfn)) || (rc = h->upload(m.invV, invV)) || (rc = h->upload(m.geo2, geo2)))
     return bail(rc);
   // state
   DevState& s = h->s;
@@ -507,11 +534,12 @@ int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
     if ((rc = build_lsq(h, p->gradmeth))) return rc;
   if (p->highres != TY_HRES_NONE && h->geo_highres != p->highres)
     if ((rc = build_muscl_geometry(h, p->highres))) return rc;
-  if (p->postlim != TY_POSTLIM_NONE && !h->s.cl) {
+  if ((p->postlim != TY_POSTLIM_NONE || (p->mode == TY_MODE_FAST && p->highres != TY_HRES_NONE)) && !h->s.cl) {
     if ((rc = h->alloc(h->s.cl, 5 * (size_t)h->m.ldf)) || (rc = h->alloc(h->s.cr, 5 * (size_t)h->m.ldf))) return rc;
   }
   h->o.scheme = p->scheme; h->o.highres = p->highres; h->o.limiter = p->limiter; h->o.postlim = p->postlim;
   h->o.gradmeth = p->gradmeth; h->o.mode = p->mode; h->o.gamma = p->gamma; h->o.entropy_fix = p->entropy_fix;
+  h->o.inv_entropy_fix = p->entropy_fix > 0.0 ? 1.0 / p->entropy_fix : 0.0;
   h->has_params = true;
   h->prim_valid = false;
   return TY_OK;

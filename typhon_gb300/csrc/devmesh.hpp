@@ -45,7 +45,12 @@ struct DevMesh {
   const double* kRF = nullptr;    // [ldf] MUSCL-FAST -|F - C_R|
   const double* LF = nullptr;     // [3][ldf] MUSCL/-UNS F - C_L
   const double* RF = nullptr;     // [3][ldf] MUSCL/-UNS F - C_R
-  const double* recw = nullptr;   // [8][ldf] fast MUSCL-UNS/MUSCL, no limiter: per side w (3), k (1)
+  const double* recw = nullptr;   // [8][ldf] fast MUSCL/-UNS without limiter: per side w (3), k (1),
+                                  // face increment = grad q . w + (q_nb - q_c) k
+  const double* invdLR = nullptr; // [ldf] 1 / dLR (fast mode)
+  const int* cfn = nullptr;       // [nslot][nci] neighbour cell across each gather-list face
+  const double* invV = nullptr;   // [nci] 1 / V (fast mode)
+  const double* geo2 = nullptr;   // [nci] 2 V / sum S (fast mode time step)
 };
 
 struct DevState {
@@ -67,6 +72,7 @@ struct DevState {
 struct SpatOpts {
   int scheme, highres, limiter, postlim, gradmeth, mode;
   double gamma, entropy_fix;
+  double inv_entropy_fix;  // 1 / entropy_fix (fast-mode Roe flux)
 };
 
 // One Runge-Kutta update applied at the end of a stage: partial sum of the state of stage

@@ -112,7 +112,13 @@ __device__ __forceinline__ double apply_lim(int lim, bool uns, bool arrayform, d
 __device__ __forceinline__ void cons_to_prim(double gamma, const double c[5], double q[5]) {
   const double g1 = gamma - 1.0;
   double rho = c[0];
-  double vx = c[2] / rho, vy = c[3] / rho, vz = c[4] / rho;
+  double vx, vy, vz;
+  if constexpr (kFast) {
+    const double ir = 1.0 / rho;
+    vx = c[2] * ir; vy = c[3] * ir; vz = c[4] * ir;
+  } else {
+    vx = c[2] / rho; vy = c[3] / rho; vz = c[4] / rho;
+  }
   double ec = 0.5 * rho * (vx * vx + vy * vy + vz * vz);
   q[0] = rho;
   q[1] = g1 * (c[1] - ec);
@@ -437,13 +443,134 @@ __device__ void flux_roe(double g, double eps, const double* L, const double* R,
   F[4] = 0.5 * ((ml * L[4] + L[1] * nz) + (mr * R[4] + R[1] * nz) - dmz);
 }
 
+// ===========================================================================
+// Fast mode.  Same mathematics, fewer FP64 operations: on GB300 the FP64 pipe (about 2
+// DFMA per SM per clock, a division or square root costing about ten) bounds this path,
+// so reciprocals, reconstruction weights and geometric factors are precomputed once
+// (HBM-resident) and the per-stage work avoids divisions.
+
+// Roe flux with shared reciprocals: 1 division + 3 reciprocal square roots per face.
+__device__ void flux_roe_fast(double g, double eps, double ieps, const double* L, const double* R, double nx,
+                              double ny, double nz, double* F) {
+  const double ig1 = 1.0 / (g - 1.0), gig1 = g * ig1;
+  const double rL = rsqrt(L[0]), rR = rsqrt(R[0]);
+  const double sL = L[0] * rL, sR = R[0] * rR;   // sqrt(rho)
+  const double iL = rL * rL, iR = rR * rR;       // 1/rho
+  const double inv = 1.0 / (sL + sR);
+  const double kl = sL * inv, kr = sR * inv;
+  const double rroe = sL * sR;
+  const double ux = kl * L[2] + kr * R[2], uy = kl * L[3] + kr * R[3], uz = kl * L[4] + kr * R[4];
+  const double sqL = L[2] * L[2] + L[3] * L[3] + L[4] * L[4];
+  const double sqR = R[2] * R[2] + R[3] * R[3] + R[4] * R[4];
+  const double hl = gig1 * L[1] * iL + 0.5 * sqL, hr = gig1 * R[1] * iR + 0.5 * sqR;
+  const double hroe = kl * hl + kr * hr;
+  const double q2 = ux * ux + uy * uy + uz * uz;
+  const double a2 = (g - 1.0) * (hroe - 0.5 * q2);
+  const double ra = rsqrt(a2), a = a2 * ra, ia2 = ra * ra;
+  const double vn = ux * nx + uy * ny + uz * nz;
+  const double vnl = L[2] * nx + L[3] * ny + L[4] * nz, vnr = R[2] * nx + R[3] * ny + R[4] * nz;
+  const double rel = ig1 * L[1] + 0.5 * L[0] * sqL, rer = ig1 * R[1] + 0.5 * R[0] * sqR;
+  const double drho = R[0] - L[0], dp = R[1] - L[1], dvn = vnr - vnl;
+  const double dux = R[2] - L[2], duy = R[3] - L[3], duz = R[4] - L[4];
+  const double h = 0.5 * ia2, rad = rroe * a * dvn;
+  const double al1 = (dp - rad) * h, al5 = (dp + rad) * h, al2 = drho - dp * ia2;
+  const double dutx = dux - dvn * nx, duty = duy - dvn * ny, dutz = duz - dvn * nz;
+  double l1 = fabs(vn - a), l5 = fabs(vn + a);
+  const double l2 = fabs(vn);
+  const double delta = eps * a;
+  if (l1 < delta || l5 < delta) {
+    const double hd = 0.5 * ra * ieps;  // 1 / (2 delta)
+    if (l1 < delta) l1 = (l1 * l1 + delta * delta) * hd;
+    if (l5 < delta) l5 = (l5 * l5 + delta * delta) * hd;
+  }
+  const double w1 = l1 * al1, w2 = l2 * al2, w5 = l5 * al5, ws = l2 * rroe;
+  const double d_mass = w1 + w2 + w5;
+  const double wa = (w5 - w1) * a;
+  const double dmx = d_mass * ux + wa * nx + ws * dutx;
+  const double dmy = d_mass * uy + wa * ny + ws * duty;
+  const double dmz = d_mass * uz + wa * nz + ws * dutz;
+  const double d_ener = (w1 + w5) * hroe + wa * vn + w2 * (0.5 * q2) + ws * ((ux * dux + uy * duy + uz * duz) - vn * dvn);
+  const double ml = vnl * L[0], mr = vnr * R[0];
+  const double pp = L[1] + R[1];
+  F[0] = 0.5 * (ml + mr - d_mass);
+  F[1] = 0.5 * (vnl * (rel + L[1]) + vnr * (rer + R[1]) - d_ener);
+  F[2] = 0.5 * (ml * L[2] + mr * R[2] + pp * nx - dmx);
+  F[3] = 0.5 * (ml * L[3] + mr * R[3] + pp * ny - dmy);
+  F[4] = 0.5 * (ml * L[4] + mr * R[4] + pp * nz - dmz);
+}
+
+// HLLC (calc_flux_hllc.f90 with beta = 1) with shared reciprocals: 3 divisions,
+// 3 square roots and 2 reciprocal square roots per face.
+__device__ void flux_hllc_fast(double g, const double* L, const double* R, double nx, double ny, double nz,
+                               double* F) {
+  const double ig1 = 1.0 / (g - 1.0), gig1 = g * ig1;
+  const double rL = rsqrt(L[0]), rR = rsqrt(R[0]);
+  const double sL = L[0] * rL, sR = R[0] * rR;
+  const double iL = rL * rL, iR = rR * rR;
+  const double inv = 1.0 / (sL + sR);
+  const double kl = sL * inv, kr = sR * inv;
+  const double rux = kl * L[2] + kr * R[2], ruy = kl * L[3] + kr * R[3], ruz = kl * L[4] + kr * R[4];
+  const double sqL = L[2] * L[2] + L[3] * L[3] + L[4] * L[4];
+  const double sqR = R[2] * R[2] + R[3] * R[3] + R[4] * R[4];
+  const double hroe = kl * (gig1 * L[1] * iL + 0.5 * sqL) + kr * (gig1 * R[1] * iR + 0.5 * sqR);
+  const double vnl = L[2] * nx + L[3] * ny + L[4] * nz, vnr = R[2] * nx + R[3] * ny + R[4] * nz;
+  const double al = sqrt(g * L[1] * iL), ar = sqrt(g * R[1] * iR);
+  const double vm = rux * nx + ruy * ny + ruz * nz;
+  const double am = sqrt((g - 1.0) * (hroe - 0.5 * (rux * rux + ruy * ruy + ruz * ruz)));
+  const double rel = ig1 * L[1] + 0.5 * L[0] * sqL, rer = ig1 * R[1] + 0.5 * R[0] * sqR;
+  const double sl = fmin(vnl - al, vm - am), sr = fmax(vnr + ar, vm + am);
+  if (sl >= 0.0) {
+    const double m0 = vnl * L[0];
+    F[0] = m0; F[1] = vnl * (rel + L[1]);
+    F[2] = m0 * L[2] + L[1] * nx; F[3] = m0 * L[3] + L[1] * ny; F[4] = m0 * L[4] + L[1] * nz;
+  } else if (sr <= 0.0) {
+    const double m0 = vnr * R[0];
+    F[0] = m0; F[1] = vnr * (rer + R[1]);
+    F[2] = m0 * R[2] + R[1] * nx; F[3] = m0 * R[3] + R[1] * ny; F[4] = m0 * R[4] + R[1] * nz;
+  } else {
+    const double rqL = L[0] * (sl - vnl), rqR = R[0] * (sr - vnr);
+    const double Sst = (rqR * vnr - rqL * vnl - R[1] + L[1]) / (rqR - rqL);
+    const bool left = Sst >= 0.0;
+    const double* Q = left ? L : R;
+    const double rq = left ? rqL : rqR, s = left ? sl : sr, vnq = left ? vnl : vnr, re = left ? rel : rer;
+    const double iks = 1.0 / (s - Sst);
+    const double pst = Q[1] - rq * (vnq - Sst);
+    const double dp = pst - Q[1];
+    const double m0 = Sst * iks;
+    F[0] = m0 * rq;
+    F[1] = Sst * (iks * (re * (s - vnq) - Q[1] * vnq + pst * Sst) + pst);
+    F[2] = m0 * (rq * Q[2] + dp * nx) + pst * nx;
+    F[3] = m0 * (rq * Q[3] + dp * ny) + pst * ny;
+    F[4] = m0 * (rq * Q[4] + dp * nz) + pst * nz;
+  }
+}
+
+__device__ __forceinline__ void face_flux_fast(const DevMesh& m, const SpatOpts& o, int f, const double* QL,
+                                               const double* QR, double* __restrict__ flux) {
+  const double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
+  double F[5];
+  if (o.scheme == TY_SCH_ROE) flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, F);
+  else if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
+  else flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
+  const double S = m.fs[f];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) flux[v * (size_t)m.ldf + f] = S * F[v];
+}
+
+
 __device__ __forceinline__ void face_flux(const DevMesh& m, const SpatOpts& o, int f, const double* QL,
                                           const double* QR, double* __restrict__ flux) {
   const double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
   double F[5];
-  if (o.scheme == TY_SCH_HLLC) flux_hllc(o.gamma, QL, QR, nx, ny, nz, F);
-  else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
-  else flux_roe(o.gamma, o.entropy_fix, QL, QR, nx, ny, nz, F);
+  if constexpr (kFast) {
+    if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
+    else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
+    else flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, F);
+  } else {
+    if (o.scheme == TY_SCH_HLLC) flux_hllc(o.gamma, QL, QR, nx, ny, nz, F);
+    else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
+    else flux_roe(o.gamma, o.entropy_fix, QL, QR, nx, ny, nz, F);
+  }
   const double S = m.fs[f];
 #pragma unroll
   for (int v = 0; v < 5; ++v) flux[v * (size_t)m.ldf + f] = S * F[v];
@@ -542,6 +669,168 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_lim(DevMesh m, DevState s,
   face_flux(m, o, f, QL, QR, s.flux);
 }
 
+
+// Increment q_face - q_c of the 5 primitive variables on one side of face f, from the
+// cell's gradient gr (15), its value qc and dq = q_nb - q_c.
+__device__ __forceinline__ void delta_fast(const DevMesh& m, const SpatOpts& o, int f, int side, const double* gr,
+                                           const double* dq, double* D) {
+  const size_t lf = m.ldf;
+  if ((o.highres == TY_HRES_MUSCL || o.highres == TY_HRES_MUSCLUNS) && o.limiter == TY_LIM_NONE) {
+    const double wx = m.recw[(4 * side) * lf + f], wy = m.recw[(4 * side + 1) * lf + f];
+    const double wz = m.recw[(4 * side + 2) * lf + f], k = m.recw[(4 * side + 3) * lf + f];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) D[v] = fma(gr[3 * v], wx, fma(gr[3 * v + 1], wy, fma(gr[3 * v + 2], wz, dq[v] * k)));
+    return;
+  }
+  const double ux = d3(m.uLR, m.ldf, f, 0), uy = d3(m.uLR, m.ldf, f, 1), uz = d3(m.uLR, m.ldf, f, 2);
+  const double idLR = m.invdLR[f];
+  const double sgn = side ? -1.0 : 1.0;  // (q(fc2) - q(fc1)) = sgn * dq
+  if (o.highres == TY_HRES_MUSCLFAST) {
+    const double k = side ? m.kRF[f] : m.kLF[f];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double LR = sgn * dq[v] * idLR;
+      double sg = LR;
+      if (o.limiter != TY_LIM_NONE) {
+        const double g = gr[3 * v] * ux + gr[3 * v + 1] * uy + gr[3 * v + 2] * uz;
+        sg = apply_lim(o.limiter, false, v < 2, g, LR);
+      }
+      D[v] = sg * k;
+    }
+    return;
+  }
+  const bool uns = o.highres == TY_HRES_MUSCLUNS;
+  const double* CF = side ? m.RF : m.LF;
+  const double cx = d3(CF, m.ldf, f, 0), cy = d3(CF, m.ldf, f, 1), cz = d3(CF, m.ldf, f, 2);
+  const double uc = ux * cx + uy * cy + uz * cz;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const double LR = sgn * dq[v] * idLR;
+    const double g = gr[3 * v] * ux + gr[3 * v + 1] * uy + gr[3 * v + 2] * uz;
+    const double sg = (o.limiter == TY_LIM_NONE ? LR : apply_lim(o.limiter, uns, v < 2, g, LR)) - g;
+    D[v] = gr[3 * v] * cx + gr[3 * v + 1] * cy + gr[3 * v + 2] * cz + sg * uc;
+  }
+}
+
+// Fused per-cell kernel: least-squares gradient (A^-1 d weights), face increments on every
+// face of the cell, Barth-type ratio without per-face divisions, and the limited face
+// states written once per face side (cl for the fc1 side, cr for the fc2 side).
+// The ratio min_f max(klim (q_nb - q_c)/increment, 0) is tracked as a fraction n/d and
+// compared by cross-multiplication; one division per variable group at the end.
+template <int NS>
+__global__ void __launch_bounds__(kBlock) k_cell_fast(DevMesh m, DevState s, SpatOpts o, double klim) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t ld = m.ldc, lf = m.ldf, ni = m.nci;
+  const double* __restrict__ prim = s.prim;
+  double qc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) qc[v] = prim[v * ld + c];
+  int ef[NS], nb[NS];
+  int ns = 0;
+  double gr[15];
+#pragma unroll
+  for (int k = 0; k < 15; ++k) gr[k] = 0.0;
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    ef[sl] = -1;
+    nb[sl] = 0;
+    if (sl < m.nslot) {
+      const int e = m.cf[sl * ni + c];
+      if (e >= 0) {
+        ef[sl] = e;
+        nb[sl] = m.cfn[sl * ni + c];
+        ns = sl + 1;
+        const int f = e >> 1, side = e & 1;
+        const double wx = m.lsqw[(3 * side) * lf + f], wy = m.lsqw[(3 * side + 1) * lf + f];
+        const double wz = m.lsqw[(3 * side + 2) * lf + f];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          double dq = prim[v * ld + nb[sl]] - qc[v];
+          dq = side ? -dq : dq;  // q(fc2) - q(fc1)
+          gr[3 * v] = fma(dq, wx, gr[3 * v]);
+          gr[3 * v + 1] = fma(dq, wy, gr[3 * v + 1]);
+          gr[3 * v + 2] = fma(dq, wz, gr[3 * v + 2]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 15; ++k) s.grad[k * ld + c] = gr[k];
+  const bool barth = o.postlim != TY_POSTLIM_NONE;
+  double D[NS][5];
+  double bn[3] = {1.0, 1.0, 1.0}, bd[3] = {klim, klim, klim};
+  bool zero[3] = {false, false, false};
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    if (sl < ns) {
+      const int e = ef[sl], f = e >> 1, side = e & 1;
+      double dq[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) dq[v] = prim[v * ld + nb[sl]] - qc[v];
+      delta_fast(m, o, f, side, gr, dq, D[sl]);
+      // increment as the rounded face value minus the cell value, as Typhon forms it
+#pragma unroll
+      for (int v = 0; v < 5; ++v) D[sl][v] = (qc[v] + D[sl][v]) - qc[v];
+      if (barth) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          const int k = v < 2 ? v : 2;
+          const double den = D[sl][v];
+          if (den != 0.0) {
+            if (dq[v] * den <= 0.0) {
+              zero[k] = true;
+            } else {
+              const double a = fabs(dq[v]), b = fabs(den);
+              if (a * bd[k] < bn[k] * b) { bn[k] = a; bd[k] = b; }
+            }
+          }
+        }
+      }
+    }
+  }
+  double r[3] = {1.0, 1.0, 1.0};
+  if (barth) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[k] = zero[k] ? 0.0 : fmin(1.0, klim * bn[k] / bd[k]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) s.ratio[k * ld + c] = r[k];
+  }
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    if (sl < ns) {
+      const int e = ef[sl], f = e >> 1, side = e & 1;
+      double* out = side ? s.cr : s.cl;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) out[v * lf + f] = fma(r[v < 2 ? v : 2], D[sl][v], qc[v]);
+    }
+  }
+}
+
+// face fluxes from the limited states of k_cell_fast
+__global__ void __launch_bounds__(kBlock) k_face_flux_fast(DevMesh m, DevState s, SpatOpts o) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const size_t lf = m.ldf;
+  double QL[5], QR[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) QL[v] = s.cl[v * lf + f];
+  const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
+  if (kind == TY_BC_PERIODIC) {
+    const int p = m.part[f];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) QR[v] = s.cl[v * lf + p];
+  } else if (kind == TY_BC_SYMMETRY) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) QR[v] = QL[v];
+    mirror(m, f, QR);
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) QR[v] = s.cr[v * lf + f];
+  }
+  face_flux_fast(m, o, f, QL, QR, s.flux);
+}
+
 // ---------------------------------------------------------------------------
 // residual R_c = dt/V_c * sum(+-F S), in the colour order of flux_to_res
 __device__ __forceinline__ void gather_residual(const DevMesh& m, const DevState& s, int c, double R[5]) {
@@ -580,7 +869,9 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevMesh m, DevState s, double
 // per-cell stability time step; returns false for negative or NaN internal energy
 __device__ __forceinline__ bool cell_dt(const DevMesh& m, double gamma, double cfl, int c, const double u[5], double& dt) {
   const double gg1 = gamma * (gamma - 1.0);
-  double d = cfl * 2.0 * m.cvol[c] / m.sumS[c];
+  double d;
+  if constexpr (kFast) d = cfl * m.geo2[c];
+  else d = cfl * 2.0 * m.cvol[c] / m.sumS[c];
   double irho = 1.0 / u[0];
   double rv2 = u[2] * u[2] + u[3] * u[3] + u[4] * u[4];
   double a2 = (u[1] - 0.5 * rv2 * irho) * gg1 * irho;
@@ -648,7 +939,9 @@ __global__ void __launch_bounds__(kBlock) k_rk_update(DevMesh m, DevState s, RkS
     const size_t ld = m.ldc;
     double R[5];
     gather_residual(m, s, c, R);
-    const double coef = load_dt(dt, dtbits) / m.cvol[c];
+    double coef;
+    if constexpr (kFast) coef = load_dt(dt, dtbits) * m.invV[c];
+    else coef = load_dt(dt, dtbits) / m.cvol[c];
 #pragma unroll
     for (int v = 0; v < 5; ++v) R[v] = coef * R[v];
     double u0[5];
@@ -714,6 +1007,15 @@ cudaError_t prim_from(const DevMesh& m, const DevState& s, const SpatOpts& o, co
 cudaError_t residual_faces(const DevMesh& m, const DevState& s, const SpatOpts& o, cudaStream_t st, Prof* pr) {
   if (m.ng > 0)
     pr->launch(K_GHOST_PRIM, st, [&] { k_ghost_prim<<<nblk(m.ng), kBlock, 0, st>>>(m, s.prim); });
+  if (kFast && o.highres != TY_HRES_NONE) {
+    const double klim = o.postlim == TY_POSTLIM_SUPERBARTH ? 1.0 : 0.5;
+    if (m.nslot <= 4)
+      pr->launch(K_GRAD, st, [&] { k_cell_fast<4><<<nblk(m.nci), kBlock, 0, st>>>(m, s, o, klim); });
+    else
+      pr->launch(K_GRAD, st, [&] { k_cell_fast<8><<<nblk(m.nci), kBlock, 0, st>>>(m, s, o, klim); });
+    pr->launch(K_FACE_FLUX, st, [&] { k_face_flux_fast<<<nblk(m.nf), kBlock, 0, st>>>(m, s, o); });
+    return cudaGetLastError();
+  }
   if (o.gradmeth != TY_GRAD_NONE) {
     pr->launch(K_GRAD, st, [&] { k_grad<<<nblk(m.nci), kBlock, 0, st>>>(m, s); });
     if (m.ng > 0)
