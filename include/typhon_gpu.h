@@ -162,7 +162,8 @@ int ty_set_stream(ty_mesh* mesh, void* stream);
 /* Per-kernel CUDA-event timing of every launch issued while enabled (enabling clears the
  * record).  ty_profile_read returns, per kernel id (0 prim, 1 ghost_prim, 2 grad,
  * 3 ghost_grad, 4 face_states, 5 barth, 6 face_flux, 7 face_flux_lim, 8 rk_update,
- * 9 gather, 10 timestep), the summed milliseconds and the number of launches. */
+ * 9 gather, 10 timestep, 11 cell_fast, 12 face_flux_fast), the summed milliseconds and the
+ * number of launches. */
 int ty_profile_enable(ty_mesh* mesh, int32_t on);
 int ty_profile_read(ty_mesh* mesh, int32_t n, double* ms, int32_t* launches);
 

@@ -81,7 +81,7 @@ _SIGS = {
 
 
 KERNEL_NAMES = ["prim", "ghost_prim", "grad", "ghost_grad", "face_states", "barth", "face_flux",
-                "face_flux_lim", "rk_update", "gather", "timestep"]
+                "face_flux_lim", "rk_update", "gather", "timestep", "cell_fast", "face_flux_fast"]
 
 
 def exported_names():

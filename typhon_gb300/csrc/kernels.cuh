@@ -1010,10 +1010,10 @@ cudaError_t residual_faces(const DevMesh& m, const DevState& s, const SpatOpts& 
   if (kFast && o.highres != TY_HRES_NONE) {
     const double klim = o.postlim == TY_POSTLIM_SUPERBARTH ? 1.0 : 0.5;
     if (m.nslot <= 4)
-      pr->launch(K_GRAD, st, [&] { k_cell_fast<4><<<nblk(m.nci), kBlock, 0, st>>>(m, s, o, klim); });
+      pr->launch(K_CELL_FAST, st, [&] { k_cell_fast<4><<<nblk(m.nci), kBlock, 0, st>>>(m, s, o, klim); });
     else
-      pr->launch(K_GRAD, st, [&] { k_cell_fast<8><<<nblk(m.nci), kBlock, 0, st>>>(m, s, o, klim); });
-    pr->launch(K_FACE_FLUX, st, [&] { k_face_flux_fast<<<nblk(m.nf), kBlock, 0, st>>>(m, s, o); });
+      pr->launch(K_CELL_FAST, st, [&] { k_cell_fast<8><<<nblk(m.nci), kBlock, 0, st>>>(m, s, o, klim); });
+    pr->launch(K_FACE_FLUX_FAST, st, [&] { k_face_flux_fast<<<nblk(m.nf), kBlock, 0, st>>>(m, s, o); });
     return cudaGetLastError();
   }
   if (o.gradmeth != TY_GRAD_NONE) {
