@@ -167,6 +167,23 @@ int ty_set_stream(ty_mesh* mesh, void* stream);
 int ty_profile_enable(ty_mesh* mesh, int32_t on);
 int ty_profile_read(ty_mesh* mesh, int32_t n, double* ms, int32_t* launches);
 
+/* Global stability time step for callers that cannot let the library allocate device
+ * memory (a host code that owns all device memory through its own allocator, a solver loop
+ * that must not allocate between steps).  No counterpart in the reference: it computes the
+ * same value as ty_timestep in TY_MODE_EXACT, without a ty_mesh handle.
+ *   cons        device [5][ld] conserved state (rho, rhoE, rhou, rhov, rhow), ld >= ncell
+ *   volume      device [ncell] cell volumes
+ *   sum_surface device [ncell] sum of the face surfaces of each cell
+ *   stream      cudaStream_t of the current device (NULL: the default stream)
+ *   dt_out      host: the minimum over cells of CFL*2*V/sum S/(|u|+a)
+ * Allocates nothing: its scratch (a partial minimum per 256 cells, the result and an error
+ * word) lives in a static device array of the library, at most 4,194,304 cells per call
+ * (larger ncell returns TY_ERR_ARG).  The first call on a device looks the array up; make
+ * it before any stream capture.  Calls share the array: calls that overlap on the GPU race.
+ * Synchronises the stream; returns TY_ERR_NEGENERGY / TY_ERR_NANDT like ty_timestep. */
+int ty_timestep_static(int32_t ncell, const double* cons, int32_t ld, const double* volume,
+                       const double* sum_surface, double gamma, double cfl, void* stream, double* dt_out);
+
 /* ---------------------------------------------------------------------------------
  * Host mesh preprocessing (no GPU): builds the ty_mesh_desc arrays from an element mesh
  * the way Typhon's grid_preproc and init_connect_grid do (face creation and order,

@@ -68,6 +68,8 @@ _SIGS = {
     "ty_set_stream": ([C.c_void_p, C.c_void_p], C.c_int),
     "ty_profile_enable": ([C.c_void_p, C.c_int32], C.c_int),
     "ty_profile_read": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
+    "ty_timestep_static": ([C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                            C.c_void_p, C.POINTER(C.c_double)], C.c_int),
     "ty_umesh_new": ([C.POINTER(C.c_void_p)], C.c_int),
     "ty_umesh_free": ([C.c_void_p], C.c_int),
     "ty_umesh_set_nodes": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),

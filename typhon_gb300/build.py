@@ -67,7 +67,8 @@ def build(force=False, verbose=False):
                      *inc, "-c", str(cpp), "-o", str(obj)])
     nvflags = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                "--expt-relaxed-constexpr", "-Xptxas", "-v"]
-    for cu, extra in (("kernels_exact.cu", ["-fmad=false"]), ("kernels_fast.cu", ["-fmad=true"])):
+    for cu, extra in (("kernels_exact.cu", ["-fmad=false"]), ("kernels_fast.cu", ["-fmad=true"]),
+                      ("timestep_static.cu", ["-fmad=false"])):
         obj = OBJ_DIR / (pathlib.Path(cu).stem + ".o")
         jobs.append([nvcc, *nvflags, *extra, *inc, "-c", str(SRC / cu), "-o", str(obj)])
     jobs.append([nvcc, "-O3", ARCH, "-o", str(PROBE), str(SRC / "fp64_peak.cu")])
