@@ -486,6 +486,7 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
   if ((rc = h->alloc(s.u0, 5 * lc)) || (rc = h->alloc(s.cur, 5 * lc)) || (rc = h->alloc(s.acc, 5 * lc)) ||
       (rc = h->alloc(s.prim, 5 * lc)) || (rc = h->alloc(s.grad, 15 * lc)) || (rc = h->alloc(s.ratio, 3 * lc)) ||
       (rc = h->alloc(s.flux, 5 * lf)) || (rc = h->alloc(s.res, 5 * lc)) || (rc = h->alloc(s.dtbits, 4)) ||
+      (rc = h->alloc(s.stage, 5 * (size_t)nci)) ||
       (rc = h->alloc(s.err, 4)))
     return bail(rc);
   TY_CU(cudaMemset(s.grad, 0, 15 * lc * sizeof(double)));
@@ -548,20 +549,13 @@ int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
 int ty_state_upload(ty_mesh* h, const double* rho, const double* rhoE, const double* rhou) {
   if (!h || !rho || !rhoE || !rhou) return TY_ERR_ARG;
   TY_CU(cudaSetDevice(h->device));
-  const int n = h->m.nci;
-  const size_t ld = h->m.ldc;
-  // AoS vector -> SoA components on the host, then one copy per component
-  std::vector<double> tmp(3 * (size_t)n);
-  for (int i = 0; i < n; ++i) {
-    tmp[i] = rhou[3 * (size_t)i];
-    tmp[n + (size_t)i] = rhou[3 * (size_t)i + 1];
-    tmp[2 * (size_t)n + i] = rhou[3 * (size_t)i + 2];
-  }
-  TY_CU(cudaMemcpyAsync(h->s.u0, rho, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  TY_CU(cudaMemcpyAsync(h->s.u0 + ld, rhoE, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  for (int k = 0; k < 3; ++k)
-    TY_CU(cudaMemcpyAsync(h->s.u0 + (2 + k) * ld, tmp.data() + k * (size_t)n, n * sizeof(double),
-                          cudaMemcpyHostToDevice, h->stream));
+  const size_t n = h->m.nci;
+  // copy Typhon's layout as is (pinned caller buffers go straight over DMA), transpose on the GPU
+  TY_CU(cudaMemcpyAsync(h->s.stage, rho, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  TY_CU(cudaMemcpyAsync(h->s.stage + n, rhoE, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  TY_CU(cudaMemcpyAsync(h->s.stage + 2 * n, rhou, 3 * n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  cudaError_t e = tyk::kexact::unpack_state(h->m, h->s, h->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "unpack state");
   TY_CU(cudaStreamSynchronize(h->stream));
   h->has_state = true;
   h->prim_valid = false;
@@ -572,20 +566,13 @@ int ty_state_download(ty_mesh* h, double* rho, double* rhoE, double* rhou) {
   if (!h || !rho || !rhoE || !rhou) return TY_ERR_ARG;
   if (!h->has_state) return TY_ERR_STATE;
   TY_CU(cudaSetDevice(h->device));
-  const int n = h->m.nci;
-  const size_t ld = h->m.ldc;
-  std::vector<double> tmp(3 * (size_t)n);
-  TY_CU(cudaMemcpyAsync(rho, h->s.u0, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  TY_CU(cudaMemcpyAsync(rhoE, h->s.u0 + ld, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  for (int k = 0; k < 3; ++k)
-    TY_CU(cudaMemcpyAsync(tmp.data() + k * (size_t)n, h->s.u0 + (2 + k) * ld, n * sizeof(double),
-                          cudaMemcpyDeviceToHost, h->stream));
+  const size_t n = h->m.nci;
+  cudaError_t e = tyk::kexact::pack_state(h->m, h->s, h->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "pack state");
+  TY_CU(cudaMemcpyAsync(rho, h->s.stage, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TY_CU(cudaMemcpyAsync(rhoE, h->s.stage + n, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TY_CU(cudaMemcpyAsync(rhou, h->s.stage + 2 * n, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   TY_CU(cudaStreamSynchronize(h->stream));
-  for (int i = 0; i < n; ++i) {
-    rhou[3 * (size_t)i] = tmp[i];
-    rhou[3 * (size_t)i + 1] = tmp[n + (size_t)i];
-    rhou[3 * (size_t)i + 2] = tmp[2 * (size_t)n + i];
-  }
   return TY_OK;
 }
 

@@ -65,6 +65,7 @@ struct DevState {
   double* ratio = nullptr; // [3][ldc] post-limiter ratios (rho, p, velocity)
   double* flux = nullptr;  // [5][ldf] face flux times surface
   double* res = nullptr;   // [5][ldc] residual of ty_residual
+  double* stage = nullptr; // [5*nci] host-layout staging: rho, rhoE, rhou as (x,y,z) per cell
   unsigned long long* dtbits = nullptr;  // [4] minimum time step slots (bit pattern of a positive double)
   int* err = nullptr;      // [4] error word, first bad cell, ...
 };
@@ -141,6 +142,8 @@ struct Prof {
                         unsigned long long* dtbits_next, double cfl, cudaStream_t st, Prof* pr);   \
   cudaError_t timestep(const DevMesh& m, const DevState& s, const SpatOpts& o, const double* cons, \
                        double cfl, unsigned long long* dtbits, cudaStream_t st, Prof* pr);         \
+  cudaError_t unpack_state(const DevMesh& m, const DevState& s, cudaStream_t st);                  \
+  cudaError_t pack_state(const DevMesh& m, const DevState& s, cudaStream_t st);                    \
   }
 
 TY_DECLARE_MODE(kexact)

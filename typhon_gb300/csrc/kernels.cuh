@@ -451,7 +451,7 @@ __device__ void flux_roe(double g, double eps, const double* L, const double* R,
 
 // Roe flux with shared reciprocals: 1 division + 3 reciprocal square roots per face.
 __device__ void flux_roe_fast(double g, double eps, double ieps, const double* L, const double* R, double nx,
-                              double ny, double nz, double* F) {
+                              double ny, double nz, double S, double* F) {
   const double ig1 = 1.0 / (g - 1.0), gig1 = g * ig1;
   const double rL = rsqrt(L[0]), rR = rsqrt(R[0]);
   const double sL = L[0] * rL, sR = R[0] * rR;   // sqrt(rho)
@@ -478,7 +478,8 @@ __device__ void flux_roe_fast(double g, double eps, double ieps, const double* L
   double l1 = fabs(vn - a), l5 = fabs(vn + a);
   const double l2 = fabs(vn);
   const double delta = eps * a;
-  if (l1 < delta || l5 < delta) {
+  // non-negative doubles compare like their bit patterns: test on the integer pipe
+  if (__double_as_longlong(l1) < __double_as_longlong(delta) || __double_as_longlong(l5) < __double_as_longlong(delta)) {
     const double hd = 0.5 * ra * ieps;  // 1 / (2 delta)
     if (l1 < delta) l1 = (l1 * l1 + delta * delta) * hd;
     if (l5 < delta) l5 = (l5 * l5 + delta * delta) * hd;
@@ -492,11 +493,12 @@ __device__ void flux_roe_fast(double g, double eps, double ieps, const double* L
   const double d_ener = (w1 + w5) * hroe + wa * vn + w2 * (0.5 * q2) + ws * ((ux * dux + uy * duy + uz * duz) - vn * dvn);
   const double ml = vnl * L[0], mr = vnr * R[0];
   const double pp = L[1] + R[1];
-  F[0] = 0.5 * (ml + mr - d_mass);
-  F[1] = 0.5 * (vnl * (rel + L[1]) + vnr * (rer + R[1]) - d_ener);
-  F[2] = 0.5 * (ml * L[2] + mr * R[2] + pp * nx - dmx);
-  F[3] = 0.5 * (ml * L[3] + mr * R[3] + pp * ny - dmy);
-  F[4] = 0.5 * (ml * L[4] + mr * R[4] + pp * nz - dmz);
+  const double hs = 0.5 * S;  // flux times surface: the 1/2 of the Roe average folded in
+  F[0] = hs * (ml + mr - d_mass);
+  F[1] = hs * (vnl * (rel + L[1]) + vnr * (rer + R[1]) - d_ener);
+  F[2] = hs * (ml * L[2] + mr * R[2] + pp * nx - dmx);
+  F[3] = hs * (ml * L[3] + mr * R[3] + pp * ny - dmy);
+  F[4] = hs * (ml * L[4] + mr * R[4] + pp * nz - dmz);
 }
 
 // HLLC (calc_flux_hllc.f90 with beta = 1) with shared reciprocals: 3 divisions,
@@ -549,12 +551,17 @@ __device__ __forceinline__ void face_flux_fast(const DevMesh& m, const SpatOpts&
                                                const double* QR, double* __restrict__ flux) {
   const double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
   double F[5];
-  if (o.scheme == TY_SCH_ROE) flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, F);
-  else if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
-  else flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
   const double S = m.fs[f];
+  if (o.scheme == TY_SCH_ROE) {
+    flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, S, F);
+  } else {
+    if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
+    else flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
 #pragma unroll
-  for (int v = 0; v < 5; ++v) flux[v * (size_t)m.ldf + f] = S * F[v];
+    for (int v = 0; v < 5; ++v) F[v] = S * F[v];
+  }
+#pragma unroll
+  for (int v = 0; v < 5; ++v) flux[v * (size_t)m.ldf + f] = F[v];
 }
 
 
@@ -565,7 +572,7 @@ __device__ __forceinline__ void face_flux(const DevMesh& m, const SpatOpts& o, i
   if constexpr (kFast) {
     if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
-    else flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, F);
+    else flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, 1.0, F);  // unit surface
   } else {
     if (o.scheme == TY_SCH_HLLC) flux_hllc(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
@@ -715,75 +722,69 @@ __device__ __forceinline__ void delta_fast(const DevMesh& m, const SpatOpts& o, 
 // Fused per-cell kernel: least-squares gradient (A^-1 d weights), face increments on every
 // face of the cell, Barth-type ratio without per-face divisions, and the limited face
 // states written once per face side (cl for the fc1 side, cr for the fc2 side).
-// The ratio min_f max(klim (q_nb - q_c)/increment, 0) is tracked as a fraction n/d and
-// compared by cross-multiplication; one division per variable group at the end.
-template <int NS>
-__global__ void __launch_bounds__(kBlock) k_cell_fast(DevMesh m, DevState s, SpatOpts o, double klim) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+// The ratio min_f max(klim (q_nb - q_c)/increment, 0) is tracked as a fraction n/d; the
+// comparisons run on the integer pipe (positive finite doubles order like their bit
+// patterns), leaving the FP64 pipe to the arithmetic.  One division per variable group.
+// The increments are staged in shared memory ([slot*5+var][thread], conflict-free) so the
+// kernel keeps few registers live and runs two or more blocks per SM.
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+
+template <int NS, int BLK>
+__global__ void __launch_bounds__(BLK, 2) k_cell_fast(DevMesh m, DevState s, SpatOpts o, double klim) {
+  __shared__ double sD[NS * 5][BLK];
+  const int c = blockIdx.x * BLK + threadIdx.x;
   if (c >= m.nci) return;
+  const int t = threadIdx.x;
   const size_t ld = m.ldc, lf = m.ldf, ni = m.nci;
   const double* __restrict__ prim = s.prim;
   double qc[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) qc[v] = prim[v * ld + c];
-  int ef[NS], nb[NS];
-  int ns = 0;
   double gr[15];
 #pragma unroll
   for (int k = 0; k < 15; ++k) gr[k] = 0.0;
+  int ns = 0;
+  for (int sl = 0; sl < m.nslot && sl < NS; ++sl) {
+    const int e = m.cf[sl * ni + c];
+    if (e < 0) break;
+    ns = sl + 1;
+    const int f = e >> 1, side = e & 1, nb = m.cfn[sl * ni + c];
+    const double wx = m.lsqw[(3 * side) * lf + f], wy = m.lsqw[(3 * side + 1) * lf + f];
+    const double wz = m.lsqw[(3 * side + 2) * lf + f];
 #pragma unroll
-  for (int sl = 0; sl < NS; ++sl) {
-    ef[sl] = -1;
-    nb[sl] = 0;
-    if (sl < m.nslot) {
-      const int e = m.cf[sl * ni + c];
-      if (e >= 0) {
-        ef[sl] = e;
-        nb[sl] = m.cfn[sl * ni + c];
-        ns = sl + 1;
-        const int f = e >> 1, side = e & 1;
-        const double wx = m.lsqw[(3 * side) * lf + f], wy = m.lsqw[(3 * side + 1) * lf + f];
-        const double wz = m.lsqw[(3 * side + 2) * lf + f];
-#pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          double dq = prim[v * ld + nb[sl]] - qc[v];
-          dq = side ? -dq : dq;  // q(fc2) - q(fc1)
-          gr[3 * v] = fma(dq, wx, gr[3 * v]);
-          gr[3 * v + 1] = fma(dq, wy, gr[3 * v + 1]);
-          gr[3 * v + 2] = fma(dq, wz, gr[3 * v + 2]);
-        }
-      }
+    for (int v = 0; v < 5; ++v) {
+      double dq = prim[v * ld + nb] - qc[v];
+      dq = side ? -dq : dq;  // q(fc2) - q(fc1)
+      gr[3 * v] = fma(dq, wx, gr[3 * v]);
+      gr[3 * v + 1] = fma(dq, wy, gr[3 * v + 1]);
+      gr[3 * v + 2] = fma(dq, wz, gr[3 * v + 2]);
     }
   }
 #pragma unroll
   for (int k = 0; k < 15; ++k) s.grad[k * ld + c] = gr[k];
   const bool barth = o.postlim != TY_POSTLIM_NONE;
-  double D[NS][5];
   double bn[3] = {1.0, 1.0, 1.0}, bd[3] = {klim, klim, klim};
   bool zero[3] = {false, false, false};
+  for (int sl = 0; sl < ns; ++sl) {
+    const int e = m.cf[sl * ni + c], f = e >> 1, side = e & 1, nb = m.cfn[sl * ni + c];
+    double dq[5], D[5];
 #pragma unroll
-  for (int sl = 0; sl < NS; ++sl) {
-    if (sl < ns) {
-      const int e = ef[sl], f = e >> 1, side = e & 1;
-      double dq[5];
+    for (int v = 0; v < 5; ++v) dq[v] = prim[v * ld + nb] - qc[v];
+    delta_fast(m, o, f, side, gr, dq, D);
 #pragma unroll
-      for (int v = 0; v < 5; ++v) dq[v] = prim[v * ld + nb[sl]] - qc[v];
-      delta_fast(m, o, f, side, gr, dq, D[sl]);
+    for (int v = 0; v < 5; ++v) {
       // increment as the rounded face value minus the cell value, as Typhon forms it
-#pragma unroll
-      for (int v = 0; v < 5; ++v) D[sl][v] = (qc[v] + D[sl][v]) - qc[v];
+      const double den = (qc[v] + D[v]) - qc[v];
+      sD[sl * 5 + v][t] = den;
       if (barth) {
-#pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          const int k = v < 2 ? v : 2;
-          const double den = D[sl][v];
-          if (den != 0.0) {
-            if (dq[v] * den <= 0.0) {
-              zero[k] = true;
-            } else {
-              const double a = fabs(dq[v]), b = fabs(den);
-              if (a * bd[k] < bn[k] * b) { bn[k] = a; bd[k] = b; }
-            }
+        const int k = v < 2 ? v : 2;
+        const long long bden = dbits(den), bdq = dbits(dq[v]);
+        if ((bden << 1) != 0) {                                   // den != 0
+          if ((bdq << 1) == 0 || ((bdq ^ bden) < 0)) {             // dq/den <= 0
+            zero[k] = true;
+          } else {
+            const double x = fabs(dq[v]) * bd[k], y = bn[k] * fabs(den);
+            if (dbits(x) < dbits(y)) { bn[k] = fabs(dq[v]); bd[k] = fabs(den); }
           }
         }
       }
@@ -796,14 +797,11 @@ __global__ void __launch_bounds__(kBlock) k_cell_fast(DevMesh m, DevState s, Spa
 #pragma unroll
     for (int k = 0; k < 3; ++k) s.ratio[k * ld + c] = r[k];
   }
+  for (int sl = 0; sl < ns; ++sl) {
+    const int e = m.cf[sl * ni + c], f = e >> 1, side = e & 1;
+    double* out = side ? s.cr : s.cl;
 #pragma unroll
-  for (int sl = 0; sl < NS; ++sl) {
-    if (sl < ns) {
-      const int e = ef[sl], f = e >> 1, side = e & 1;
-      double* out = side ? s.cr : s.cl;
-#pragma unroll
-      for (int v = 0; v < 5; ++v) out[v * lf + f] = fma(r[v < 2 ? v : 2], D[sl][v], qc[v]);
-    }
+    for (int v = 0; v < 5; ++v) out[v * lf + f] = fma(r[v < 2 ? v : 2], sD[sl * 5 + v][t], qc[v]);
   }
 }
 
@@ -1010,9 +1008,13 @@ cudaError_t residual_faces(const DevMesh& m, const DevState& s, const SpatOpts& 
   if (kFast && o.highres != TY_HRES_NONE) {
     const double klim = o.postlim == TY_POSTLIM_SUPERBARTH ? 1.0 : 0.5;
     if (m.nslot <= 4)
-      pr->launch(K_CELL_FAST, st, [&] { k_cell_fast<4><<<nblk(m.nci), kBlock, 0, st>>>(m, s, o, klim); });
+      pr->launch(K_CELL_FAST, st, [&] {
+        k_cell_fast<4, 256><<<(unsigned)((m.nci + 255) / 256), 256, 0, st>>>(m, s, o, klim);
+      });
     else
-      pr->launch(K_CELL_FAST, st, [&] { k_cell_fast<8><<<nblk(m.nci), kBlock, 0, st>>>(m, s, o, klim); });
+      pr->launch(K_CELL_FAST, st, [&] {
+        k_cell_fast<8, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim);
+      });
     pr->launch(K_FACE_FLUX_FAST, st, [&] { k_face_flux_fast<<<nblk(m.nf), kBlock, 0, st>>>(m, s, o); });
     return cudaGetLastError();
   }
@@ -1052,6 +1054,34 @@ cudaError_t timestep(const DevMesh& m, const DevState& s, const SpatOpts& o, con
   pr->launch(K_TIMESTEP, st, [&] {
     k_timestep<<<nblk(m.nci), kBlock, 0, st>>>(m, cons, o.gamma, cfl, dtbits, s.err);
   });
+  return cudaGetLastError();
+}
+
+// Typhon layout (rho[n], rhoE[n], rhou as (x,y,z)[n]) <-> SoA u0, on the device
+__global__ void k_unpack_state(DevMesh m, const double* __restrict__ stage, double* __restrict__ u0) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t n = m.nci, ld = m.ldc;
+  u0[c] = stage[c];
+  u0[ld + c] = stage[n + c];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) u0[(2 + k) * ld + c] = stage[2 * n + 3 * (size_t)c + k];
+}
+__global__ void k_pack_state(DevMesh m, const double* __restrict__ u0, double* __restrict__ stage) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t n = m.nci, ld = m.ldc;
+  stage[c] = u0[c];
+  stage[n + c] = u0[ld + c];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) stage[2 * n + 3 * (size_t)c + k] = u0[(2 + k) * ld + c];
+}
+cudaError_t unpack_state(const DevMesh& m, const DevState& s, cudaStream_t st) {
+  k_unpack_state<<<nblk(m.nci), kBlock, 0, st>>>(m, s.stage, s.u0);
+  return cudaGetLastError();
+}
+cudaError_t pack_state(const DevMesh& m, const DevState& s, cudaStream_t st) {
+  k_pack_state<<<nblk(m.nci), kBlock, 0, st>>>(m, s.u0, s.stage);
   return cudaGetLastError();
 }
 

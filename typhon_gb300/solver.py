@@ -94,6 +94,21 @@ class Grid:
     def set_prim(self, prim):
         self.set_cons(prim_to_cons(np.asarray(prim, np.float64).reshape(5, -1)[:, :self.nci], self.gamma))
 
+    def upload_typhon(self, rho, rhoE, rhou):
+        """Upload a conserved state given in Typhon's layout without any conversion:
+        rho[ncell_int], rhoE[ncell_int], rhou[ncell_int, 3] (contiguous float64, pinned or not)."""
+        for a in (rho, rhoE, rhou):
+            assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+        _capi.check(self.lib.ty_state_upload(self.h, rho.ctypes.data, rhoE.ctypes.data, rhou.ctypes.data),
+                    "ty_state_upload")
+
+    def download_typhon(self, rho, rhoE, rhou):
+        """Download the conserved state into caller arrays in Typhon's layout."""
+        for a in (rho, rhoE, rhou):
+            assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+        _capi.check(self.lib.ty_state_download(self.h, rho.ctypes.data, rhoE.ctypes.data, rhou.ctypes.data),
+                    "ty_state_download")
+
     def get_cons(self):
         rho = np.zeros(self.nci)
         rhoE = np.zeros(self.nci)
