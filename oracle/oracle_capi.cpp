@@ -196,6 +196,7 @@ int ory_solver_run_steps(void* s, int n, double* dts) {
 // case 1: NRG/TIME/RUNGEKUTTA/<method>  (HLLC, MUSCL-FAST, van Albada, periodic),
 //         probe RHOERR = vol-avg (rho - rho_exact(x - 50 t, y))^2
 // case 2: NRG/MESH/CON/PER2D-TRANS     (Rusanov, first order, periodic),
+// case 3: NRG/MESH/ELEM/TYM-QUAD       (HLLC, first order, symmetry on all sides), probe PAVG = vol-avg p
 //         probe RHODEV = vol-avg (rho - 1.25)^2
 // Writes ncycle probe values into out; returns the number of time steps taken, < 0 on error.
 int ory_run_nrg(int which, void* mesh, int rk_method, double cfl, int ncycle, double duration, double* out) {
@@ -206,6 +207,8 @@ int ory_run_nrg(int which, void* mesh, int rk_method, double cfl, int ncycle, do
     sp.scheme = SCH_HLLC; sp.highres = HRES_MUSCLFAST; sp.limiter = LIM_ALBADA; sp.gradmeth = GRAD_LSQ;
   } else if (which == 2) {
     sp.scheme = SCH_RUSANOV; sp.highres = HRES_NONE; sp.gradmeth = GRAD_NONE;
+  } else if (which == 3) {
+    sp.scheme = SCH_HLLC; sp.highres = HRES_NONE; sp.gradmeth = GRAD_NONE;
   } else {
     return -1;
   }
@@ -215,6 +218,17 @@ int ory_run_nrg(int which, void* mesh, int rk_method, double cfl, int ncycle, do
   for (int c = 0; c < nc; ++c) {  // BLOCK:INIT at cell centres, ghosts included (init_ns_ust.f90)
     double x = m.ccentre[c].x, y = m.ccentre[c].y;
     double rho, vx;
+    if (which == 3) {  // P = 1e5, T = 300, MACH = 0.2 along x (init_ns_ust.f90: density from p/(r T))
+      const double p = 1.0E5, T = 300., rcst = 287.14, gam = 1.4;
+      rho = p / (rcst * T);
+      double vel = std::sqrt((gam * p / rho)) * .2;
+      S.prim[c] = rho;
+      S.prim[nc + c] = p;
+      S.prim[2 * nc + c] = (vel / 1.0) * 1.;
+      S.prim[3 * nc + c] = (vel / 1.0) * 0.;
+      S.prim[4 * nc + c] = (vel / 1.0) * 0.;
+      continue;
+    }
     if (which == 1) {
       double s = std::sin(2 * pi * x) * std::sin(2 * pi * y);
       rho = 1 + (s * s) / 2;
@@ -251,7 +265,9 @@ int ory_run_nrg(int which, void* mesh, int rk_method, double cfl, int ncycle, do
     double num = 0.0, vol = 0.0;
     for (int c = 0; c < m.ncell_int; ++c) {
       double q;
-      if (which == 1) {
+      if (which == 3) {
+        q = S.prim[nc + c];
+      } else if (which == 1) {
         double x = m.ccentre[c].x, y = m.ccentre[c].y;
         double s = std::sin(2 * pi * (x - 50 * curtps)) * std::sin(2 * pi * y);
         double e = S.prim[c] - (1 + (s * s) / 2);

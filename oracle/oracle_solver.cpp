@@ -123,7 +123,7 @@ void Solver::boco_cell_state() {
         int i = m->fc1[f];
         V3 fn = m->fnormal[f];
         V3 u = v3(prim[2 * nc + i], prim[3 * nc + i], prim[4 * nc + i]);
-        V3 ug = u - (2.0 * dot(u, fn)) * fn;
+        V3 ug = u - (2.0 * dot(u - V3(), fn)) * fn;
         prim[g] = prim[i];
         prim[nc + g] = prim[nc + i];
         prim[2 * nc + g] = ug.x;
@@ -156,14 +156,27 @@ void Solver::boco_cell_grad() {
   }
 }
 
-// calcboco_gen(bccon_face_state): cell_r(face) = cell_l(partner face)
+// calcboco_gen(bccon_face_state): periodic cell_r(face) = cell_l(partner face)
+// (calcboco_connect_per_match.f90:56-78); symmetry cell_r(face) = cell_l(face) with the
+// velocity mirrored across the face (calcboco_ust_sym.f90, face-state mode)
 void Solver::boco_face_state() {
   const int nf = m->nface;
   for (auto& b : m->bocos) {
-    if (b.kind != BC_PERIODIC) continue;
     for (size_t k = 0; k < b.iface.size(); ++k) {
-      int f = b.iface[k], fp = b.partner_face[k];
-      for (int v = 0; v < 5; ++v) cell_r[v * nf + f] = cell_l[v * nf + fp];
+      int f = b.iface[k];
+      if (b.kind == BC_PERIODIC) {
+        int fp = b.partner_face[k];
+        for (int v = 0; v < 5; ++v) cell_r[v * nf + f] = cell_l[v * nf + fp];
+      } else if (b.kind == BC_SYMMETRY) {
+        V3 fn = m->fnormal[f];
+        V3 u = v3(cell_l[2 * nf + f], cell_l[3 * nf + f], cell_l[4 * nf + f]);
+        V3 ug = u - (2.0 * dot(u - V3(), fn)) * fn;
+        cell_r[f] = cell_l[f];
+        cell_r[nf + f] = cell_l[nf + f];
+        cell_r[2 * nf + f] = ug.x;
+        cell_r[3 * nf + f] = ug.y;
+        cell_r[4 * nf + f] = ug.z;
+      }
     }
   }
 }

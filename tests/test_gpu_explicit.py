@@ -283,3 +283,25 @@ def test_caller_stream_and_kernel_timing(ty):
     assert 0 < ms.sum() <= e0.elapsed_time(e1) * 1.05
     _capi.check(g.lib.ty_set_stream(g.h, None), "ty_set_stream")
     g.run_steps("RK3-SSP", 0.8, 1)
+
+
+def test_nrg_tym_quad_symmetry_replayed_on_gpu(ty, golden_dir):
+    """NRG/MESH/ELEM/TYM-QUAD (symmetry boundaries) through the GPU, exact mode."""
+    bcs = [(f, 2, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX")]
+    md = ty.preprocess(ty.read_tym(golden_dir / "quad20x10.tym"), 2, bcs)
+    n = md.ncell
+    p, T, rcst, gam = 1.0E5, 300.0, 287.14, 1.4
+    rho = p / (rcst * T)
+    vel = np.sqrt((gam * p / rho)) * 0.2
+    prim = np.stack([np.full(n, rho), np.full(n, p), np.full(n, vel), np.zeros(n), np.zeros(n)])
+    g = ty.Grid(md)
+    g.set_spat("HLLC", "NONE", mode="exact")
+    g.set_prim(prim)
+    vol = md.cell_volume[:md.ncell_int]
+    out = []
+    for _ in range(10):
+        g.integration_cyclezone("RK3-SSP", 1.0, 0.005 / 10)
+        out.append(np.sum(g.get_prim()[1] * vol) / np.sum(vol))
+    gold = np.loadtxt(golden_dir / "TYM-QUAD__PAVG.tmon")[:, 2]
+    err = np.abs(np.array(out) - gold) / _print_ulp(gold)
+    assert err.max() <= 0.5 + 1e-3, err.max()

@@ -52,3 +52,15 @@ def test_quad20_mesh_counts(quad20):
     part = d["face_partner"]
     b = np.where(part >= 0)[0]
     assert len(b) == 80 and np.all(part[part[b]] == b)
+
+
+SYMMETRY_BOX = [(f, op.BC_SYMMETRY, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX")]
+
+
+def test_tym_quad_symmetry_pavg(golden_dir, oracle):
+    """NRG/MESH/ELEM/TYM-QUAD: HLLC first order, symmetry on all four sides, 10 cycles."""
+    m = op.Mesh.from_tym(golden_dir / "quad20x10.tym").build(2, SYMMETRY_BOX)
+    out, nsteps = op.run_nrg(3, m, "RK3-SSP", 1.0, ncycle=10, duration=0.005)
+    gold = np.loadtxt(golden_dir / "TYM-QUAD__PAVG.tmon")
+    err = np.abs(out - gold[:, 2]) / print_ulp(gold[:, 2])
+    assert err.max() <= 0.5 + 1e-6, err.max()
