@@ -132,7 +132,14 @@ struct SpatParams {
   int gradmeth = GRAD_NONE;
   double gamma = 1.4;
   double roe_entropy_fix = 0.1;  // Harten fix width (fraction of local sound speed), Roe only
+  // laminar Navier-Stokes (DYNAMICS = LAMINAR)
+  int viscous = 0;        // 0 Euler, 1 DISSIPATIVE_FLUX = CELL-AVERAGE, 2 = FULL
+  int visc_law = 0;       // 0 KINEMATIC-CONSTANT (mu = nu rho), 1 Sutherland (AIR)
+  double visc_kin = 0.0;  // nu for KINEMATIC-CONSTANT
+  double rgas = 287.14;   // AIR
+  double prandtl = 0.72;
 };
+enum ViscMeth { VISC_NONE = 0, VISC_CELLAVG = 1, VISC_CELLFULL = 2 };
 
 struct RkTable {
   int nstage = 0;
@@ -169,6 +176,9 @@ struct Solver {
   void hres_states();
   void postlimit_barth(double klim);
   void face_fluxes();
+  double viscosity(double rho, double T) const;
+  void viscous_fluxes();
+  void ns_bocoflux();
   void flux_to_res();
   void calc_rhs();               // one residual evaluation at dtloc
   double timestep();             // stab_cond: global min dt over interior cells

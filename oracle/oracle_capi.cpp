@@ -197,6 +197,8 @@ int ory_solver_run_steps(void* s, int n, double* dts) {
 //         probe RHOERR = vol-avg (rho - rho_exact(x - 50 t, y))^2
 // case 2: NRG/MESH/CON/PER2D-TRANS     (Rusanov, first order, periodic),
 // case 3: NRG/MESH/ELEM/TYM-QUAD       (HLLC, first order, symmetry on all sides), probe PAVG = vol-avg p
+// case 4/5: NRG/NS/NUM/FLUX/VISCOUS/CELLAVG | CELLFULL (laminar, nu = 1, moving adiabatic walls);
+//         out[0:ncycle] = VXERR, out[ncycle:2 ncycle] = DELTA
 //         probe RHODEV = vol-avg (rho - 1.25)^2
 // Writes ncycle probe values into out; returns the number of time steps taken, < 0 on error.
 int ory_run_nrg(int which, void* mesh, int rk_method, double cfl, int ncycle, double duration, double* out) {
@@ -209,6 +211,11 @@ int ory_run_nrg(int which, void* mesh, int rk_method, double cfl, int ncycle, do
     sp.scheme = SCH_RUSANOV; sp.highres = HRES_NONE; sp.gradmeth = GRAD_NONE;
   } else if (which == 3) {
     sp.scheme = SCH_HLLC; sp.highres = HRES_NONE; sp.gradmeth = GRAD_NONE;
+  } else if (which == 4 || which == 5) {
+    sp.scheme = SCH_HLLC; sp.highres = HRES_MUSCLFAST; sp.limiter = LIM_ALBADA; sp.gradmeth = GRAD_LSQ;
+    sp.viscous = which == 4 ? VISC_CELLAVG : VISC_CELLFULL;
+    sp.visc_law = 0;
+    sp.visc_kin = 1.;
   } else {
     return -1;
   }
@@ -218,6 +225,14 @@ int ory_run_nrg(int which, void* mesh, int rk_method, double cfl, int ncycle, do
   for (int c = 0; c < nc; ++c) {  // BLOCK:INIT at cell centres, ghosts included (init_ns_ust.f90)
     double x = m.ccentre[c].x, y = m.ccentre[c].y;
     double rho, vx;
+    if (which == 4 || which == 5) {  // DENSITY = 1, P = 100/1.4, VX = erf(y/2/sqrt(1))
+      S.prim[c] = 1.;
+      S.prim[nc + c] = 100 / 1.4;
+      S.prim[2 * nc + c] = std::erf(y / 2 / std::sqrt(1.));
+      S.prim[3 * nc + c] = 0.;
+      S.prim[4 * nc + c] = 0.;
+      continue;
+    }
     if (which == 3) {  // P = 1e5, T = 300, MACH = 0.2 along x (init_ns_ust.f90: density from p/(r T))
       const double p = 1.0E5, T = 300., rcst = 287.14, gam = 1.4;
       rho = p / (rcst * T);
@@ -262,10 +277,15 @@ int ory_run_nrg(int which, void* mesh, int rk_method, double cfl, int ncycle, do
     }
     curtps = curtps + dtbase;
     S.varprim();
-    double num = 0.0, vol = 0.0;
+    double num = 0.0, num2 = 0.0, vol = 0.0;
     for (int c = 0; c < m.ncell_int; ++c) {
-      double q;
-      if (which == 3) {
+      double q, q2 = 0.0;
+      if (which == 4 || which == 5) {  // VXERR and DELTA probes
+        double y = m.ccentre[c].y, vx = S.prim[2 * nc + c];
+        double e = vx - std::erf(y / 2 / std::sqrt(curtps + 1.));
+        q = e * e;
+        q2 = 2 * 50 * (1 - vx * vx);
+      } else if (which == 3) {
         q = S.prim[nc + c];
       } else if (which == 1) {
         double x = m.ccentre[c].x, y = m.ccentre[c].y;
@@ -277,9 +297,11 @@ int ory_run_nrg(int which, void* mesh, int rk_method, double cfl, int ncycle, do
         q = e * e;
       }
       num += q * m.cvol[c];
+      num2 += q2 * m.cvol[c];
       vol += m.cvol[c];
     }
     out[icycle - 1] = num / vol;
+    if (which == 4 || which == 5) out[ncycle + icycle - 1] = num2 / vol;
   }
   return nsteps;
 }

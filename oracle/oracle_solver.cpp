@@ -130,11 +130,22 @@ void Solver::boco_cell_state() {
         prim[3 * nc + g] = ug.y;
         prim[4 * nc + g] = ug.z;
       } else if (b.kind == BC_WALL) {
+        // setboco_ns_flux.f90, cell-state mode, adiabatic wall (lflux = 0): ghost pressure
+        // = cell pressure, ghost temperature = cell temperature - lflux d / conduct, velocity
+        // reflected about the wall velocity
         int i = m->fc1[f];
-        V3 u = v3(prim[2 * nc + i], prim[3 * nc + i], prim[4 * nc + i]);
-        V3 ug = 2.0 * b.wall_velocity - u;
-        prim[g] = prim[i];
+        const double r = sp.rgas;
+        const double lflux = 0.0;
+        V3 cgface = m->fcentre[f], cg = m->ccentre[i], nrm = m->fnormal[f];
+        double d = dot(cgface - cg, cgface - cg) / std::fabs(dot(cgface - cg, nrm));
+        double mu = viscosity(prim[i], prim[nc + i] / (r * prim[i]));
+        double cp = sp.gamma / (sp.gamma - 1.0) * r;
+        double conduct = mu * cp / sp.prandtl;
+        double temp = prim[nc + i] / (prim[i] * r) - lflux * d / conduct;
         prim[nc + g] = prim[nc + i];
+        prim[g] = prim[nc + g] / (r * temp);
+        V3 u = v3(prim[2 * nc + i], prim[3 * nc + i], prim[4 * nc + i]);
+        V3 ug = (2.0 * b.wall_velocity) - u;
         prim[2 * nc + g] = ug.x;
         prim[3 * nc + g] = ug.y;
         prim[4 * nc + g] = ug.z;
@@ -167,6 +178,16 @@ void Solver::boco_face_state() {
       if (b.kind == BC_PERIODIC) {
         int fp = b.partner_face[k];
         for (int v = 0; v < 5; ++v) cell_r[v * nf + f] = cell_l[v * nf + fp];
+      } else if (b.kind == BC_WALL) {
+        // setboco_ns_flux.f90, face-state mode: cell_r takes cell_l's PRESSURE as its density
+        // ("weak BC"), cell_l's pressure, and the velocity reflected about the wall velocity
+        cell_r[f] = cell_l[nf + f];
+        cell_r[nf + f] = cell_l[nf + f];
+        V3 u = v3(cell_l[2 * nf + f], cell_l[3 * nf + f], cell_l[4 * nf + f]);
+        V3 ug = (2.0 * b.wall_velocity) - u;
+        cell_r[2 * nf + f] = ug.x;
+        cell_r[3 * nf + f] = ug.y;
+        cell_r[4 * nf + f] = ug.z;
       } else if (b.kind == BC_SYMMETRY) {
         V3 fn = m->fnormal[f];
         V3 u = v3(cell_l[2 * nf + f], cell_l[3 * nf + f], cell_l[4 * nf + f]);
@@ -650,6 +671,131 @@ void Solver::face_fluxes() {
   }
 }
 
+
+// calc_viscosity (SOURCE/EQNS/EQNS.f90:225-265)
+double Solver::viscosity(double rho, double T) const {
+  if (sp.visc_law == 0) return sp.visc_kin * rho;
+  const double mu0 = 0.0000168, T0 = 273.00, S = 110.50;  // AIR (def_model_ns.f90:170-173)
+  return mu0 * std::pow(T / T0, 1.5) * (T0 + S) / (T + S);
+}
+
+// calc_flux_viscous_cell (SOURCE/EQNS/calc_flux_viscous_cell.f90:71-144) on cell states and
+// cell gradients (integration_ns_ust.f90:139-159), added to the inviscid flux of every face;
+// face gradients from interp_facegradient_vect (SOURCE/MESH/interpface_gradient_vect.f90:59-81)
+// and interp_facegradn_scal (SOURCE/MESH/interpface_gradn_scal.f90:60-90), theta = 1.
+void Solver::viscous_fluxes() {
+  const int nc = m->ncell, nf = m->nface;
+  const double r = sp.rgas;
+  const double cp = sp.gamma * r / (sp.gamma - 1.0);
+  const double theta = 1.0;
+#pragma omp parallel for schedule(static)
+  for (int f = 0; f < nf; ++f) {
+    const int icl = m->fc1[f], icr = m->fc2[f];
+    const V3 F = m->fcentre[f], CL = m->ccentre[icl], CR = m->ccentre[icr], n = m->fnormal[f];
+    double dHL = vabs(F - CL), dHR = vabs(F - CR);
+    const double id = 1.0 / (dHL + dHR);
+    dHL = id * dHL;
+    dHR = id * dHR;
+    const V3 vLR = CR - CL;
+    const V3 vL = v3(prim[2 * nc + icl], prim[3 * nc + icl], prim[4 * nc + icl]);
+    const V3 vR = v3(prim[2 * nc + icr], prim[3 * nc + icr], prim[4 * nc + icr]);
+    const V3 velH = dHR * vL + dHL * vR;
+    const double rL = prim[icl], rR = prim[icr], pL = prim[nc + icl], pR = prim[nc + icr];
+    const double TL = pL / (rL * r), TR = pR / (rR * r);
+    const double TH = dHR * TL + dHL * TR;
+    const double rhoH = dHR * rL + dHL * rR;
+    auto gv = [&](int c, int k) { return v3(grad[(3 * k) * (size_t)nc + c], grad[(3 * k + 1) * (size_t)nc + c],
+                                            grad[(3 * k + 2) * (size_t)nc + c]); };
+    const V3 gTL = (1.0 / (rL * r)) * gv(icl, 1) - (pL / ((rL * rL) * r)) * gv(icl, 0);
+    const V3 gTR = (1.0 / (rR * r)) * gv(icr, 1) - (pR / ((rR * rR) * r)) * gv(icr, 0);
+    const double mu = viscosity(rhoH, TH);
+    // face velocity gradient T(i,j) = du_i/dx_j
+    double GL[3][3], GR[3][3], G[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        GL[i][j] = grad[(6 + 3 * i + j) * (size_t)nc + icl];
+        GR[i][j] = grad[(6 + 3 * i + j) * (size_t)nc + icr];
+        G[i][j] = dHL * GR[i][j] + dHR * GL[i][j];
+      }
+    double gTH;
+    if (sp.viscous == VISC_CELLFULL) {
+      const double dLR2 = sqrabs(vLR);
+      double qL[3] = {vL.x, vL.y, vL.z}, qR[3] = {vR.x, vR.y, vR.z}, w[3] = {vLR.x, vLR.y, vLR.z};
+      const V3 e = (theta / dLR2) * vLR;
+      double ev[3] = {e.x, e.y, e.z};
+      double Fav[3];
+      for (int i = 0; i < 3; ++i) Fav[i] = qR[i] - qL[i] - (G[i][0] * w[0] + G[i][1] * w[1] + G[i][2] * w[2]);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) G[i][j] = G[i][j] + Fav[i] * ev[j];
+      const double pscal = dot(vLR, n) / dLR2;
+      const double Fcomp = pscal * (TR - TL);
+      const V3 vi = n - (theta * pscal) * vLR;
+      const double Favg = dot(dHL * gTR + dHR * gTL, vi);
+      gTH = theta * Fcomp + Favg;
+    } else {
+      gTH = dot(dHL * gTR + dHR * gTL, n);
+    }
+    // sigma = mu (G + G^T - 2/3 tr(G) I)
+    double Sg[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) Sg[i][j] = G[i][j] + G[j][i];
+    const double addvisc = -(2.0 / 3.0) * (G[0][0] + G[1][1] + G[2][2]);
+    for (int i = 0; i < 3; ++i) Sg[i][i] = Sg[i][i] + addvisc;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) Sg[i][j] = mu * Sg[i][j];
+    const V3 sn = v3(Sg[0][0] * n.x + Sg[0][1] * n.y + Sg[0][2] * n.z, Sg[1][0] * n.x + Sg[1][1] * n.y + Sg[1][2] * n.z,
+                     Sg[2][0] * n.x + Sg[2][1] * n.y + Sg[2][2] * n.z);
+    const double svn = dot(sn, velH);
+    flux[2 * nf + f] = flux[2 * nf + f] - sn.x;
+    flux[3 * nf + f] = flux[3 * nf + f] - sn.y;
+    flux[4 * nf + f] = flux[4 * nf + f] - sn.z;
+    flux[nf + f] = flux[nf + f] - svn;
+    const double conduct = mu * cp / sp.prandtl;
+    flux[nf + f] = flux[nf + f] - conduct * gTH;
+  }
+}
+
+// ns_bocoflux (SOURCE/EQNS/ns_bocoflux.f90:47-111): on adiabatic-wall faces the heat flux is
+// replaced by the prescribed one (zero): the conduction term is added back
+void Solver::ns_bocoflux() {
+  const int nc = m->ncell, nf = m->nface;
+  const double r = sp.rgas;
+  const double cp = sp.gamma * r / (sp.gamma - 1.0);
+  for (auto& b : m->bocos) {
+    if (b.kind != BC_WALL) continue;
+    for (int f : b.iface) {
+      const int icl = m->fc1[f], icr = m->fc2[f];
+      const V3 F = m->fcentre[f], CL = m->ccentre[icl], CR = m->ccentre[icr], n = m->fnormal[f];
+      double dHL = vabs(F - CL), dHR = vabs(F - CR);
+      const double id = 1.0 / (dHL + dHR);
+      dHL = id * dHL;
+      dHR = id * dHR;
+      const V3 vLR = CR - CL;
+      const double rL = prim[icl], rR = prim[icr], pL = prim[nc + icl], pR = prim[nc + icr];
+      const double TL = pL / (rL * r), TR = pR / (rR * r);
+      const double TH = dHR * TL + dHL * TR;
+      const double rhoH = dHR * rL + dHL * rR;
+      auto gv = [&](int c, int k) { return v3(grad[(3 * k) * (size_t)nc + c], grad[(3 * k + 1) * (size_t)nc + c],
+                                              grad[(3 * k + 2) * (size_t)nc + c]); };
+      const V3 gTL = (1.0 / (rL * r)) * gv(icl, 1) - (pL / ((rL * rL) * r)) * gv(icl, 0);
+      const V3 gTR = (1.0 / (rR * r)) * gv(icr, 1) - (pR / ((rR * rR) * r)) * gv(icr, 0);
+      const double mu = viscosity(rhoH, TH);
+      double gTH;
+      if (sp.viscous == VISC_CELLFULL) {
+        const double dLR2 = sqrabs(vLR);
+        const double pscal = dot(vLR, n) / dLR2;
+        const double Fcomp = pscal * (TR - TL);
+        const V3 vi = n - (1.0 * pscal) * vLR;
+        gTH = 1.0 * Fcomp + dot(dHL * gTR + dHR * gTL, vi);
+      } else {
+        gTH = dot(dHL * gTR + dHR * gTL, n);
+      }
+      const double conduct = mu * cp / sp.prandtl;
+      flux[nf + f] = flux[nf + f] + conduct * gTH + 0.0;
+    }
+  }
+}
+
 // flux_to_res.f90:47-144: F *= S, colour-ordered scatter, R *= dtloc/V (interior cells)
 void Solver::flux_to_res() {
   const int nc = m->ncell, nci = m->ncell_int, nf = m->nface;
@@ -687,6 +833,10 @@ void Solver::calc_rhs() {
   if (sp.postlim == POSTLIM_SUPERBARTH) postlimit_barth(1.0);
   boco_face_state();
   face_fluxes();
+  if (sp.viscous != VISC_NONE) {
+    viscous_fluxes();
+    ns_bocoflux();
+  }
   flux_to_res();
 }
 

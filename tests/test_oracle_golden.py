@@ -64,3 +64,21 @@ def test_tym_quad_symmetry_pavg(golden_dir, oracle):
     gold = np.loadtxt(golden_dir / "TYM-QUAD__PAVG.tmon")
     err = np.abs(out - gold[:, 2]) / print_ulp(gold[:, 2])
     assert err.max() <= 0.5 + 1e-6, err.max()
+
+
+MXLAY_BCS = [("IMIN", op.BC_PERIODIC, "IMAX", (1.0, 0.0, 0.0)),
+             ("JMIN", op.BC_WALL, "", (0.0, 0.0, 0.0), (-1.0, 0.0, 0.0)),
+             ("JMAX", op.BC_WALL, "", (0.0, 0.0, 0.0), (1.0, 0.0, 0.0))]
+
+
+@pytest.mark.parametrize("which,name", [(4, "CELLAVG"), (5, "CELLFULL")])
+def test_viscous_mixing_layer(golden_dir, oracle, which, name):
+    """NRG/NS/NUM/FLUX/VISCOUS/<name>: laminar (nu = 1), HLLC + MUSCL-FAST + van Albada,
+    periodic in x, adiabatic walls moving at -1 / +1, RK25BB, 10 cycles; monitors VXERR and
+    DELTA.  Wall ghost-cell gradients are taken as zero (Typhon never sets them)."""
+    m = op.Mesh.from_tym(golden_dir / "mxlay2x20quad-h50.tym").build(2, MXLAY_BCS)
+    (vxerr, delta), _ = op.run_nrg(which, m, "RK25BB", 0.5, ncycle=10, duration=10.0)
+    for out, f in ((vxerr, "VXERR"), (delta, "DELTA")):
+        gold = np.loadtxt(golden_dir / f"VISCOUS-{name}-{f}__{f}.tmon")
+        err = np.abs(out - gold[:, 2]) / print_ulp(gold[:, 2])
+        assert err.max() <= 0.5 + 1e-6, (f, err.max())
