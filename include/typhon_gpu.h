@@ -79,7 +79,8 @@ typedef struct ty_mesh_desc {
   const double* cell_volume;   /* [ncell] */
   const int32_t* face_color;   /* [nface] colour group of each face (coo_colorgroup,
                                   0-based); fixes the summation order of the residual */
-  const int32_t* face_bc;      /* [nface] ty_bc kind of each face (0 for interior faces) */
+  const int32_t* face_bc;      /* [nface] ty_bc kind of each face (0 for interior faces);
+                                  TY_BC_WALL: adiabatic wall moving at face_wallvel */
   const int32_t* face_partner; /* [nface] periodic partner face, 1-based, 0 if none */
   const double* face_wallvel;  /* [3*nface] wall velocity of wall faces, or NULL */
 } ty_mesh_desc;
@@ -95,7 +96,17 @@ typedef struct ty_spat_params {
   int32_t mode;       /* ty_mode */
   double gamma;       /* ratio of specific heats (AIR: 1.4) */
   double entropy_fix; /* Roe only: Harten fix width as a fraction of the sound speed */
+  /* laminar Navier-Stokes (MODEL: DYNAMICS = LAMINAR); viscous = 0 for Euler */
+  int32_t viscous;    /* ty_viscous: face gradient (SPAT_PARAM:DISSIPATIVE_FLUX) */
+  int32_t visc_law;   /* ty_visc_law */
+  double visc_kin;    /* kinematic viscosity of TY_VISC_KINEMATIC */
+  double rgas;        /* gas constant (AIR: 287.14) */
+  double prandtl;     /* Prandtl number (AIR: 0.72) */
 } ty_spat_params;
+/* face gradient of the viscous flux (interpface_gradient_vect.f90, interpface_gradn_scal.f90) */
+enum ty_viscous { TY_VISC_NONE = 0, TY_VISC_CELLAVG = 1, TY_VISC_CELLFULL = 2 };
+/* viscosity law (EQNS.f90 calc_viscosity): nu*rho, or Sutherland with AIR's constants */
+enum ty_visc_law { TY_VISC_KINEMATIC = 0, TY_VISC_SUTHERLAND = 1 };
 
 /* Version string of the library. */
 const char* ty_version(void);

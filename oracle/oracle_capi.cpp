@@ -132,14 +132,16 @@ void ory_mesh_facevtex(void* h, int maxv, int* out) {  // nface x maxv, 1-based 
 }
 
 // ---- solver ----
-// iparams: scheme, highres, limiter, postlim, gradmeth, rk_method
-// dparams: gamma, cfl, roe_entropy_fix
+// iparams: scheme, highres, limiter, postlim, gradmeth, rk_method, viscous, visc_law
+// dparams: gamma, cfl, roe_entropy_fix, visc_kin, rgas, prandtl
 void* ory_solver_new(void* mesh, const int* ip, const double* dp) {
   auto* s = new Solver();
   SpatParams sp;
   sp.scheme = ip[0]; sp.highres = ip[1]; sp.limiter = ip[2]; sp.postlim = ip[3]; sp.gradmeth = ip[4];
+  sp.viscous = ip[6]; sp.visc_law = ip[7];
   sp.gamma = dp[0];
   sp.roe_entropy_fix = dp[2];
+  sp.visc_kin = dp[3]; sp.rgas = dp[4]; sp.prandtl = dp[5];
   s->init(&((MeshHandle*)mesh)->m, sp, ip[5], dp[1]);
   return s;
 }

@@ -19,6 +19,7 @@ HRES_NONE, HRES_MUSCL, HRES_MUSCLFAST, HRES_MUSCLUNS = 0, 1, 2, 3
 LIM_NONE, LIM_MINMOD, LIM_ALBADA, LIM_VLEER, LIM_SBEE, LIM_KIM3, LIM_LIM03 = range(7)
 POSTLIM_NONE, POSTLIM_BARTH, POSTLIM_SUPERBARTH = 0, 1, 2
 GRAD_NONE, GRAD_LSQ, GRAD_LSQW = 0, 1, 2
+VISC_NONE, VISC_CELLAVG, VISC_CELLFULL = 0, 1, 2
 RK = {"RK2": 1, "RK2-SSP": 2, "RK3-SSP": 3, "RK4": 4, "RK25BB": 5, "RK26BB": 6, "RK12BS": 7, "RK13BS": 8}
 
 _lib = None
@@ -137,11 +138,11 @@ class Mesh:
 class Solver:
     def __init__(self, mesh, scheme=SCH_HLLC, highres=HRES_NONE, limiter=LIM_ALBADA,
                  postlim=POSTLIM_NONE, gradmeth=GRAD_NONE, rk="RK4", gamma=1.4, cfl=1.0,
-                 entropy_fix=0.1):
+                 entropy_fix=0.1, viscous=0, visc_law=0, visc_kin=0.0, rgas=287.14, prandtl=0.72):
         self.lib = load()
         self.mesh = mesh
-        ip = np.array([scheme, highres, limiter, postlim, gradmeth, RK[rk]], np.int32)
-        dp = np.array([gamma, cfl, entropy_fix], np.float64)
+        ip = np.array([scheme, highres, limiter, postlim, gradmeth, RK[rk], viscous, visc_law], np.int32)
+        dp = np.array([gamma, cfl, entropy_fix, visc_kin, rgas, prandtl], np.float64)
         self.h = C.c_void_p(self.lib.ory_solver_new(mesh.h, _p(ip), _p(dp)))
 
     def __del__(self):

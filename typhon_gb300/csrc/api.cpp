@@ -116,6 +116,7 @@ struct ty_mesh {
   std::vector<double> ccentre, fcentre, fnormal, fsurf, cvol;
   std::vector<int> cf;  // [nslot][nci]
   int lsq_gradmeth = -1, geo_highres = -1;
+  bool visc_ready = false;
   double* dtbits_host = nullptr;  // pinned
   Prof prof;
   cudaStream_t own_stream = nullptr;
@@ -272,6 +273,33 @@ int build_muscl_geometry(ty_mesh* h, int highres) {
   return TY_OK;
 }
 
+// viscous face geometry (calc_flux_viscous_cell.f90:82-90): HL/(HL+HR), HR/(HL+HR), C_R - C_L
+int build_viscous_geometry(ty_mesh* h) {
+  DevMesh& m = h->m;
+  const size_t lf = m.ldf;
+  std::vector<double> g(5 * lf, 0.0);
+  for (int f = 0; f < m.nf; ++f) {
+    const double* CL = &h->ccentre[3 * (size_t)h->fc1[f]];
+    const double* CR = &h->ccentre[3 * (size_t)h->fc2[f]];
+    const double* F = &h->fcentre[3 * (size_t)f];
+    const double a0 = F[0] - CL[0], a1 = F[1] - CL[1], a2 = F[2] - CL[2];
+    const double b0 = F[0] - CR[0], b1 = F[1] - CR[1], b2 = F[2] - CR[2];
+    double dHL = std::sqrt(a0 * a0 + a1 * a1 + a2 * a2), dHR = std::sqrt(b0 * b0 + b1 * b1 + b2 * b2);
+    const double id = 1.0 / (dHL + dHR);
+    dHL = id * dHL;
+    dHR = id * dHR;
+    g[f] = dHL;
+    g[lf + f] = dHR;
+    g[2 * lf + f] = CR[0] - CL[0];
+    g[3 * lf + f] = CR[1] - CL[1];
+    g[4 * lf + f] = CR[2] - CL[2];
+  }
+  int rc = h->upload(m.vgeo, g);
+  if (rc) return rc;
+  h->visc_ready = true;
+  return TY_OK;
+}
+
 int check_err(ty_mesh* h) {
   int e[2] = {0, 0};
   TY_CU(cudaMemcpyAsync(e, h->s.err, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -415,8 +443,8 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
         int p = d->face_partner[f] - 1;
         if (p < nfi || p >= nf || d->face_partner[p] - 1 != f) { tyi::set_error("bad periodic partner"); return bail(TY_ERR_MESH); }
         part[f] = p;
-      } else if (fbc[f] != TY_BC_SYMMETRY) {
-        tyi::set_error("boundary kind not supported by the explicit Euler path");
+      } else if (fbc[f] != TY_BC_SYMMETRY && fbc[f] != TY_BC_WALL) {
+        tyi::set_error("unknown boundary kind");
         return bail(TY_ERR_UNSUPPORTED);
       }
     }
@@ -429,6 +457,17 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
     if (gface[k] >= 0) { tyi::set_error("ghost cell shared by two faces"); return bail(TY_ERR_MESH); }
     gface[k] = f;
     gsrc[k] = part[f] >= 0 ? h->fc1[part[f]] : h->fc1[f];
+  }
+  // wall ghosts: |F - C|^2 / |(F - C).n|  (setboco_ns_flux.f90, cell-state mode)
+  std::vector<double> gdist(std::max(ng, 1), 0.0);
+  for (int k = 0; k < ng; ++k) {
+    const int f = gface[k];
+    if (fbc[f] != TY_BC_WALL) continue;
+    const double* F = &d->face_centre[3 * (size_t)f];
+    const double* Cc = &d->cell_centre[3 * (size_t)h->fc1[f]];
+    const double* n = &d->face_normal[3 * (size_t)f];
+    const double a0 = F[0] - Cc[0], a1 = F[1] - Cc[1], a2 = F[2] - Cc[2];
+    gdist[k] = (a0 * a0 + a1 * a1 + a2 * a2) / std::fabs(a0 * n[0] + a1 * n[1] + a2 * n[2]);
   }
   // gather lists in colour order
   std::vector<std::vector<std::pair<int, int>>> lists(nci);
@@ -479,7 +518,8 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
       (rc = h->upload(m.part, part)) || (rc = h->upload(m.cf, h->cf)) || (rc = h->upload(m.gsrc, gsrc)) ||
       (rc = h->upload(m.gface, gface)) || (rc = h->upload(m.fn, fn)) || (rc = h->upload(m.fs, fs)) ||
       (rc = h->upload(m.fwall, fw)) || (rc = h->upload(m.cvol, cv)) || (rc = h->upload(m.sumS, sumS)) ||
-      (rc = h->upload(m.cfn, cfn)) || (rc = h->upload(m.invV, invV)) || (rc = h->upload(m.geo2, geo2)))
+      (rc = h->upload(m.cfn, cfn)) || (rc = h->upload(m.invV, invV)) || (rc = h->upload(m.geo2, geo2)) ||
+      (rc = h->upload(m.gdist, gdist)))
     return bail(rc);
   // state
   DevState& s = h->s;
@@ -529,6 +569,17 @@ int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
     tyi::set_error("MUSCL reconstruction needs a gradient method");
     return TY_ERR_ARG;
   }
+  if (p->viscous < TY_VISC_NONE || p->viscous > TY_VISC_CELLFULL || p->visc_law < TY_VISC_KINEMATIC ||
+      p->visc_law > TY_VISC_SUTHERLAND) {
+    tyi::set_error("ty_spat_params: viscous option out of range");
+    return TY_ERR_ARG;
+  }
+  if (p->viscous != TY_VISC_NONE &&
+      (p->gradmeth == TY_GRAD_NONE || !(p->rgas > 0.0) || !(p->prandtl > 0.0) ||
+       (p->visc_law == TY_VISC_KINEMATIC && !(p->visc_kin >= 0.0)))) {
+    tyi::set_error("the viscous flux needs cell gradients, rgas > 0, prandtl > 0 and a viscosity");
+    return TY_ERR_ARG;
+  }
   TY_CU(cudaSetDevice(h->device));
   int rc;
   if (p->gradmeth != TY_GRAD_NONE && h->lsq_gradmeth != p->gradmeth)
@@ -541,6 +592,8 @@ int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
   h->o.scheme = p->scheme; h->o.highres = p->highres; h->o.limiter = p->limiter; h->o.postlim = p->postlim;
   h->o.gradmeth = p->gradmeth; h->o.mode = p->mode; h->o.gamma = p->gamma; h->o.entropy_fix = p->entropy_fix;
   h->o.inv_entropy_fix = p->entropy_fix > 0.0 ? 1.0 / p->entropy_fix : 0.0;
+  h->o.viscous = p->viscous; h->o.visc_law = p->visc_law; h->o.visc_kin = p->visc_kin;
+  h->o.rgas = p->rgas; h->o.prandtl = p->prandtl;
   h->has_params = true;
   h->prim_valid = false;
   return TY_OK;

@@ -51,6 +51,8 @@ struct DevMesh {
   const int* cfn = nullptr;       // [nslot][nci] neighbour cell across each gather-list face
   const double* invV = nullptr;   // [nci] 1 / V (fast mode)
   const double* geo2 = nullptr;   // [nci] 2 V / sum S (fast mode time step)
+  const double* vgeo = nullptr;   // [5][ldf] viscous flux: HL/(HL+HR), HR/(HL+HR), C_R - C_L (3)
+  const double* gdist = nullptr;  // [ng] wall ghosts: |F - C|^2 / |(F - C).n| (setboco_ns_flux.f90)
 };
 
 struct DevState {
@@ -74,6 +76,8 @@ struct SpatOpts {
   int scheme, highres, limiter, postlim, gradmeth, mode;
   double gamma, entropy_fix;
   double inv_entropy_fix;  // 1 / entropy_fix (fast-mode Roe flux)
+  int viscous, visc_law;
+  double visc_kin, rgas, prandtl;
 };
 
 // One Runge-Kutta update applied at the end of a stage: partial sum of the state of stage

@@ -136,16 +136,39 @@ __global__ void k_prim(DevMesh m, const double* __restrict__ cons, double* __res
   for (int v = 0; v < 5; ++v) prim[v * (size_t)m.ldc + c] = q[v];
 }
 
-// ghost states: periodic copy, symmetry mirror (velocity reflected across the face)
-__global__ void k_ghost_prim(DevMesh m, double* __restrict__ prim) {
+// calc_viscosity (SOURCE/EQNS/EQNS.f90:225-265): nu rho, or Sutherland with AIR's constants
+__device__ __forceinline__ double viscosity(const SpatOpts& o, double rho, double T) {
+  if (o.visc_law == TY_VISC_KINEMATIC) return o.visc_kin * rho;
+  const double mu0 = 0.0000168, T0 = 273.00, S = 110.50;
+  return mu0 * pow(T / T0, 1.5) * (T0 + S) / (T + S);
+}
+
+// ghost states: periodic copy, symmetry mirror (velocity reflected across the face),
+// adiabatic moving wall (setboco_ns_flux.f90, cell-state mode: pressure copied, temperature
+// of the cell minus lflux d / conduct with lflux = 0, velocity reflected about the wall's)
+__global__ void k_ghost_prim(DevMesh m, double* __restrict__ prim, SpatOpts o) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= m.ng) return;
   const int g = m.nci + k, src = m.gsrc[k], f = m.gface[k];
   const size_t ld = m.ldc;
   const int kind = m.fbc[f];
+  double vx = prim[2 * ld + src], vy = prim[3 * ld + src], vz = prim[4 * ld + src];
+  if (kind == TY_BC_WALL) {
+    const double r = o.rgas, lflux = 0.0;
+    const double rho = prim[src], p = prim[ld + src];
+    const double mu = viscosity(o, rho, p / (r * rho));
+    const double cp = o.gamma / (o.gamma - 1.0) * r;
+    const double conduct = mu * cp / o.prandtl;
+    const double temp = p / (rho * r) - lflux * m.gdist[k] / conduct;
+    prim[ld + g] = p;
+    prim[g] = p / (r * temp);
+    prim[2 * ld + g] = (2.0 * d3(m.fwall, m.ldf, f, 0)) - vx;
+    prim[3 * ld + g] = (2.0 * d3(m.fwall, m.ldf, f, 1)) - vy;
+    prim[4 * ld + g] = (2.0 * d3(m.fwall, m.ldf, f, 2)) - vz;
+    return;
+  }
   prim[g] = prim[src];
   prim[ld + g] = prim[ld + src];
-  double vx = prim[2 * ld + src], vy = prim[3 * ld + src], vz = prim[4 * ld + src];
   if (kind == TY_BC_SYMMETRY) {
     double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
     double wx = vx - 0.0, wy = vy - 0.0, wz = vz - 0.0;
@@ -304,6 +327,16 @@ __device__ void recon(const DevMesh& m, const DevState& s, const SpatOpts& o, in
     double t0 = T[3 * i] + sgv[i] * ux, t1 = T[3 * i + 1] + sgv[i] * uy, t2 = T[3 * i + 2] + sgv[i] * uz;
     q[2 + i] = q[2 + i] + (t0 * cx + t1 * cy + t2 * cz);
   }
+}
+
+// moving adiabatic wall, face-state mode (setboco_ns_flux.f90): the right state takes the left
+// state's pressure as its density, its pressure, and the velocity reflected about the wall's
+__device__ __forceinline__ void wall_state(const DevMesh& m, int f, const double* QL, double* QR) {
+  QR[0] = QL[1];
+  QR[1] = QL[1];
+  QR[2] = (2.0 * d3(m.fwall, m.ldf, f, 0)) - QL[2];
+  QR[3] = (2.0 * d3(m.fwall, m.ldf, f, 1)) - QL[3];
+  QR[4] = (2.0 * d3(m.fwall, m.ldf, f, 2)) - QL[4];
 }
 
 // velocity mirrored across the face plane (calcboco_ust_sym.f90, face-state mode)
@@ -547,16 +580,105 @@ __device__ void flux_hllc_fast(double g, const double* L, const double* R, doubl
   }
 }
 
-__device__ __forceinline__ void face_flux_fast(const DevMesh& m, const SpatOpts& o, int f, const double* QL,
-                                               const double* QR, double* __restrict__ flux) {
+// Laminar viscous flux added to F (per unit area), calc_flux_viscous_cell.f90:71-144, on the
+// cell states and cell gradients of the face's two cells (integration_ns_ust.f90:139-159).
+// Face gradients: CELL-AVERAGE a.grad_R + b.grad_L, or FULL with the compact correction along
+// C_L C_R (interpface_gradient_vect.f90:59-81, interpface_gradn_scal.f90:60-90, theta = 1).
+// On adiabatic-wall faces the conduction term is added back (ns_bocoflux.f90:60-108).
+__device__ void add_viscous(const DevMesh& m, const DevState& s, const SpatOpts& o, int f, double* F) {
+  const size_t ld = m.ldc, lf = m.ldf;
+  const int icl = m.fc1[f], icr = m.fc2[f];
+  const double* __restrict__ q = s.prim;
+  const double* __restrict__ gr = s.grad;
+  const double r = o.rgas;
+  const double cp = o.gamma * r / (o.gamma - 1.0);
+  const double dHL = m.vgeo[f], dHR = m.vgeo[lf + f];
+  const double wx = m.vgeo[2 * lf + f], wy = m.vgeo[3 * lf + f], wz = m.vgeo[4 * lf + f];
+  const double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
+  const double vL[3] = {q[2 * ld + icl], q[3 * ld + icl], q[4 * ld + icl]};
+  const double vR[3] = {q[2 * ld + icr], q[3 * ld + icr], q[4 * ld + icr]};
+  double velH[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) velH[i] = dHR * vL[i] + dHL * vR[i];
+  const double rL = q[icl], rR = q[icr], pL = q[ld + icl], pR = q[ld + icr];
+  const double TL = pL / (rL * r), TR = pR / (rR * r);
+  const double TH = dHR * TL + dHL * TR;
+  const double rhoH = dHR * rL + dHL * rR;
+  const double aL = 1.0 / (rL * r), bL = pL / ((rL * rL) * r);
+  const double aR = 1.0 / (rR * r), bR = pR / ((rR * rR) * r);
+  double gT[3];  // dHL gradT_R + dHR gradT_L
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double gTL = aL * gr[(3 + k) * ld + icl] - bL * gr[k * ld + icl];
+    const double gTR = aR * gr[(3 + k) * ld + icr] - bR * gr[k * ld + icr];
+    gT[k] = dHL * gTR + dHR * gTL;
+  }
+  const double mu = viscosity(o, rhoH, TH);
+  double G[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      G[i][j] = dHL * gr[(6 + 3 * i + j) * ld + icr] + dHR * gr[(6 + 3 * i + j) * ld + icl];
+  double gTH;
+  if (o.viscous == TY_VISC_CELLFULL) {
+    const double dLR2 = wx * wx + wy * wy + wz * wz;
+    const double it = 1.0 / dLR2;
+    const double ex = it * wx, ey = it * wy, ez = it * wz;
+    double Fav[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) Fav[i] = vR[i] - vL[i] - (G[i][0] * wx + G[i][1] * wy + G[i][2] * wz);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      G[i][0] = G[i][0] + Fav[i] * ex;
+      G[i][1] = G[i][1] + Fav[i] * ey;
+      G[i][2] = G[i][2] + Fav[i] * ez;
+    }
+    const double pscal = (wx * nx + wy * ny + wz * nz) / dLR2;
+    const double Fcomp = pscal * (TR - TL);
+    const double tp = 1.0 * pscal;
+    const double vix = nx - tp * wx, viy = ny - tp * wy, viz = nz - tp * wz;
+    gTH = 1.0 * Fcomp + (gT[0] * vix + gT[1] * viy + gT[2] * viz);
+  } else {
+    gTH = gT[0] * nx + gT[1] * ny + gT[2] * nz;
+  }
+  double Sg[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Sg[i][j] = G[i][j] + G[j][i];
+  const double addvisc = -(2.0 / 3.0) * (G[0][0] + G[1][1] + G[2][2]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) Sg[i][i] = Sg[i][i] + addvisc;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Sg[i][j] = mu * Sg[i][j];
+  const double snx = Sg[0][0] * nx + Sg[0][1] * ny + Sg[0][2] * nz;
+  const double sny = Sg[1][0] * nx + Sg[1][1] * ny + Sg[1][2] * nz;
+  const double snz = Sg[2][0] * nx + Sg[2][1] * ny + Sg[2][2] * nz;
+  const double svn = snx * velH[0] + sny * velH[1] + snz * velH[2];
+  F[2] = F[2] - snx;
+  F[3] = F[3] - sny;
+  F[4] = F[4] - snz;
+  F[1] = F[1] - svn;
+  const double conduct = mu * cp / o.prandtl;
+  F[1] = F[1] - conduct * gTH;
+  if (f >= m.nfi && m.fbc[f] == TY_BC_WALL) F[1] = F[1] + conduct * gTH + 0.0;
+}
+
+__device__ __forceinline__ void face_flux_fast(const DevMesh& m, const DevState& s, const SpatOpts& o, int f,
+                                               const double* QL, const double* QR, double* __restrict__ flux) {
   const double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
   double F[5];
   const double S = m.fs[f];
-  if (o.scheme == TY_SCH_ROE) {
+  if (o.scheme == TY_SCH_ROE && o.viscous == TY_VISC_NONE) {
     flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, S, F);
   } else {
-    if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
+    if (o.scheme == TY_SCH_ROE) flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, 1.0, F);
+    else if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
+    if (o.viscous != TY_VISC_NONE) add_viscous(m, s, o, f, F);
 #pragma unroll
     for (int v = 0; v < 5; ++v) F[v] = S * F[v];
   }
@@ -565,8 +687,8 @@ __device__ __forceinline__ void face_flux_fast(const DevMesh& m, const SpatOpts&
 }
 
 
-__device__ __forceinline__ void face_flux(const DevMesh& m, const SpatOpts& o, int f, const double* QL,
-                                          const double* QR, double* __restrict__ flux) {
+__device__ __forceinline__ void face_flux(const DevMesh& m, const DevState& s, const SpatOpts& o, int f,
+                                          const double* QL, const double* QR, double* __restrict__ flux) {
   const double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
   double F[5];
   if constexpr (kFast) {
@@ -578,6 +700,7 @@ __device__ __forceinline__ void face_flux(const DevMesh& m, const SpatOpts& o, i
     else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_roe(o.gamma, o.entropy_fix, QL, QR, nx, ny, nz, F);
   }
+  if (o.viscous != TY_VISC_NONE) add_viscous(m, s, o, f, F);
   const double S = m.fs[f];
 #pragma unroll
   for (int v = 0; v < 5; ++v) flux[v * (size_t)m.ldf + f] = S * F[v];
@@ -592,6 +715,8 @@ __global__ void __launch_bounds__(kBlock) k_face_flux(DevMesh m, DevState s, Spa
   const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
   if (kind == TY_BC_PERIODIC) {
     recon(m, s, o, m.part[f], 0, QR);  // cell_r(face) = cell_l(partner face)
+  } else if (kind == TY_BC_WALL) {
+    wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_SYMMETRY) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = QL[v];
@@ -599,7 +724,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux(DevMesh m, DevState s, Spa
   } else {
     recon(m, s, o, f, 1, QR);
   }
-  face_flux(m, o, f, QL, QR, s.flux);
+  face_flux(m, s, o, f, QL, QR, s.flux);
 }
 
 // post-limiter path, 1: unlimited face states
@@ -666,6 +791,8 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_lim(DevMesh m, DevState s,
   const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
   if (kind == TY_BC_PERIODIC) {
     limited(m.part[f], 0, QR);
+  } else if (kind == TY_BC_WALL) {
+    wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_SYMMETRY) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = QL[v];
@@ -673,7 +800,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_lim(DevMesh m, DevState s,
   } else {
     limited(f, 1, QR);
   }
-  face_flux(m, o, f, QL, QR, s.flux);
+  face_flux(m, s, o, f, QL, QR, s.flux);
 }
 
 
@@ -818,6 +945,8 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_fast(DevMesh m, DevState s
     const int p = m.part[f];
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = s.cl[v * lf + p];
+  } else if (kind == TY_BC_WALL) {
+    wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_SYMMETRY) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = QL[v];
@@ -826,7 +955,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_fast(DevMesh m, DevState s
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = s.cr[v * lf + f];
   }
-  face_flux_fast(m, o, f, QL, QR, s.flux);
+  face_flux_fast(m, s, o, f, QL, QR, s.flux);
 }
 
 // ---------------------------------------------------------------------------
@@ -1004,7 +1133,7 @@ cudaError_t prim_from(const DevMesh& m, const DevState& s, const SpatOpts& o, co
 // everything between the primitive variables of a stage state and the face fluxes
 cudaError_t residual_faces(const DevMesh& m, const DevState& s, const SpatOpts& o, cudaStream_t st, Prof* pr) {
   if (m.ng > 0)
-    pr->launch(K_GHOST_PRIM, st, [&] { k_ghost_prim<<<nblk(m.ng), kBlock, 0, st>>>(m, s.prim); });
+    pr->launch(K_GHOST_PRIM, st, [&] { k_ghost_prim<<<nblk(m.ng), kBlock, 0, st>>>(m, s.prim, o); });
   if (kFast && o.highres != TY_HRES_NONE) {
     const double klim = o.postlim == TY_POSTLIM_SUPERBARTH ? 1.0 : 0.5;
     if (m.nslot <= 4)
@@ -1015,6 +1144,8 @@ cudaError_t residual_faces(const DevMesh& m, const DevState& s, const SpatOpts& 
       pr->launch(K_CELL_FAST, st, [&] {
         k_cell_fast<8, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim);
       });
+    if (o.viscous != TY_VISC_NONE && m.ng > 0)
+      pr->launch(K_GHOST_GRAD, st, [&] { k_ghost_grad<<<nblk(m.ng), kBlock, 0, st>>>(m, s.grad); });
     pr->launch(K_FACE_FLUX_FAST, st, [&] { k_face_flux_fast<<<nblk(m.nf), kBlock, 0, st>>>(m, s, o); });
     return cudaGetLastError();
   }

@@ -29,6 +29,8 @@ POSTLIM = {"NONE": 0, "BARTH": 1, "SUPERBARTH": 2}
 GRADMETH = {"NONE": 0, "LSQ": 1, "W-LSQ": 2}
 RK_METHOD = {"RK2": 1, "RK2-SSP": 2, "RK3-SSP": 3, "RK4": 4, "RK25BB": 5, "RK26BB": 6, "RK12BS": 7, "RK13BS": 8}
 MODE = {"exact": 0, "fast": 1}
+DISSIPATIVE_FLUX = {"NONE": 0, "CELL-AVERAGE": 1, "FULL": 2}
+VISC_LAW = {"KINEMATIC-CONSTANT": 0, "SUTHERLAND": 1}
 
 
 def prim_to_cons(prim, gamma=1.4):
@@ -71,13 +73,18 @@ class Grid:
 
     # -- def_spat --------------------------------------------------------------------------
     def set_spat(self, scheme="HLLC", highres="NONE", limiter="ALBADA", postlim="NONE", gradmeth=None,
-                 mode="exact", gamma=1.4, entropy_fix=0.1):
+                 mode="exact", gamma=1.4, entropy_fix=0.1, dissipative_flux="NONE", viscosity="KINEMATIC-CONSTANT",
+                 kin_visc=0.0, rgas=287.14, prandtl=0.72):
         """SPAT_PARAM: SCHEME, HIGHRES, LIMITER, POST-LIMITER, GRADMETH (LSQ by default with
-        MUSCL, none for first order, as get_gradientmethod in SOURCE/PARAM/MENU_NUM.f90)."""
+        MUSCL or a viscous flux, none otherwise, as get_gradientmethod in
+        SOURCE/PARAM/MENU_NUM.f90); DISSIPATIVE_FLUX (CELL-AVERAGE | FULL) turns on the laminar
+        viscous flux with MODEL: VISCOSITY (KINEMATIC-CONSTANT with KIN_VISC, or SUTHERLAND)."""
+        visc = DISSIPATIVE_FLUX[dissipative_flux]
         if gradmeth is None:
-            gradmeth = "NONE" if highres == "NONE" else "LSQ"
+            gradmeth = "NONE" if (highres == "NONE" and visc == 0) else "LSQ"
         p = _capi.SpatParams(SCHEME[scheme], HIGHRES[highres], LIMITER[limiter], POSTLIM[postlim],
-                             GRADMETH[gradmeth], MODE[mode], float(gamma), float(entropy_fix))
+                             GRADMETH[gradmeth], MODE[mode], float(gamma), float(entropy_fix), visc,
+                             VISC_LAW[viscosity], float(kin_visc), float(rgas), float(prandtl))
         _capi.check(self.lib.ty_set_params(self.h, C.byref(p)), "ty_set_params")
         self.gamma = gamma
 
