@@ -66,7 +66,14 @@ def pair(ty, md, om, prim, scheme, highres, limiter, postlim="NONE", mode="exact
 
 
 def relerr(a, b):
-    return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+    """Relative L2 error per conserved variable of Typhon's field: rho, rhoE and the momentum
+    vector rho u (the field holds two scalars and one vector, and update_field.f90:54-60
+    measures the vector by its norm, so a momentum component that is near zero is measured
+    against the momentum, not against itself)."""
+    d = a - b
+    num = [np.linalg.norm(d[0]), np.linalg.norm(d[1]), np.linalg.norm(d[2:5])]
+    den = [np.linalg.norm(b[0]), np.linalg.norm(b[1]), np.linalg.norm(b[2:5])]
+    return np.array(num) / np.maximum(np.array(den), 1e-300)
 
 
 COMBOS = [

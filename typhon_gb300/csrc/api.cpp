@@ -344,6 +344,12 @@ int ready(ty_mesh* h) {
 }
 
 int stage_faces(ty_mesh* h) {
+  // every table a kernel of this configuration reads must exist before any launch
+  if ((h->o.viscous != TY_VISC_NONE && !h->m.vgeo) || (h->o.gradmeth != TY_GRAD_NONE && !h->m.lsq) ||
+      (h->o.highres != TY_HRES_NONE && !h->m.dLR)) {
+    tyi::set_error("internal: a geometry table of the selected scheme is missing");
+    return TY_ERR_STATE;
+  }
   cudaError_t e = MODE_CALL(h, residual_faces, h->m, h->s, h->o, h->stream, &h->prof);
   if (e != cudaSuccess) return cuda_fail(e, "residual faces");
   return TY_OK;
@@ -586,6 +592,8 @@ int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
     if ((rc = build_lsq(h, p->gradmeth))) return rc;
   if (p->highres != TY_HRES_NONE && h->geo_highres != p->highres)
     if ((rc = build_muscl_geometry(h, p->highres))) return rc;
+  if (p->viscous != TY_VISC_NONE && !h->visc_ready)
+    if ((rc = build_viscous_geometry(h))) return rc;
   if ((p->postlim != TY_POSTLIM_NONE || (p->mode == TY_MODE_FAST && p->highres != TY_HRES_NONE)) && !h->s.cl) {
     if ((rc = h->alloc(h->s.cl, 5 * (size_t)h->m.ldf)) || (rc = h->alloc(h->s.cr, 5 * (size_t)h->m.ldf))) return rc;
   }
