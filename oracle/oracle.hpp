@@ -181,6 +181,23 @@ struct Solver {
   void ns_bocoflux();
   void flux_to_res();
   void calc_rhs();               // one residual evaluation at dtloc
+
+  // ---- implicit (backward Euler) step: HLL flux Jacobians, BDLU, GMRES ----
+  bool calc_jac = false;
+  std::vector<double> jacL, jacR;         // 25*nface, row-major 5x5 per face (times S after flux_to_res)
+  std::vector<double> bdiag;              // 25*ncell
+  std::vector<double> bupper, blower;     // 25*nface
+  int nkrylov = 50, imp_max_it = 50;
+  double inv_res = 1.e-4;
+  int gmres_iters = 0;
+  void ns_bocojacobian();
+  void build_implicit_bdlu();
+  void bdlu_yeqax(const double* x, double* y) const;
+  void bdlu_yeqmaxpz(const double* x, const double* z, double* y) const;
+  int bdlu_gmres(double* sol);                   // sol: RHS in, solution out (5*ncell, per cell)
+  // one implicit step: time step (global min or local), residual + Jacobians, solve, update;
+  // returns GMRES restarts (info) and the L1 norm of the update per variable in l1[5]
+  int implicit_step(double cfl_, bool local_dt, double* l1);
   double timestep();             // stab_cond: global min dt over interior cells
   void rk_step(double dt);       // treelevel_rungekutta + update_field
 };

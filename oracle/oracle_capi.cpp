@@ -155,7 +155,8 @@ void ory_solver_set_prim(void* s, const double* p) {
   std::memcpy(S->prim.data(), p, S->prim.size() * sizeof(double));
   S->varcons();
 }
-// which: 0 cons, 1 prim, 2 grad, 3 residu, 4 flux, 5 cell_l, 6 cell_r, 7 dtloc, 8 limratio
+// which: 0 cons, 1 prim, 2 grad, 3 residu, 4 flux, 5 cell_l, 6 cell_r, 7 dtloc, 8 limratio,
+//        9 jacL, 10 jacR (25 per face, row-major), 11 BDLU diag (25 per cell), 12 upper, 13 lower
 int ory_solver_get(void* s, int which, double* out) {
   auto* S = (Solver*)s;
   const std::vector<double>* v = nullptr;
@@ -169,6 +170,11 @@ int ory_solver_get(void* s, int which, double* out) {
     case 6: v = &S->cell_r; break;
     case 7: v = &S->dtloc; break;
     case 8: v = &S->limratio; break;
+    case 9: v = &S->jacL; break;
+    case 10: v = &S->jacR; break;
+    case 11: v = &S->bdiag; break;
+    case 12: v = &S->bupper; break;
+    case 13: v = &S->blower; break;
     default: return -1;
   }
   std::memcpy(out, v->data(), v->size() * sizeof(double));
@@ -193,6 +199,22 @@ int ory_solver_run_steps(void* s, int n, double* dts) {
   }
   return 0;
 }
+
+// ---- implicit step (backward Euler, BDLU matrix, restarted GMRES) ----
+// cfl: stability number of the step; local_dt: 1 = LOCAL_STABILITY_CONDITION, 0 = global minimum;
+// nkrylov, max_it, inv_res: NKRYLOV, IMP_MAX_IT, INV_RES.  l1 (5, may be null) receives the L1
+// norm of the update per variable, iters (may be null) the GMRES restarts taken.
+// Returns GMRES info (restarts - 1, or -1 when not converged), -2 on a bad time step.
+int ory_solver_implicit_step(void* s, double cfl, int local_dt, int nkrylov, int max_it, double inv_res,
+                             double* l1, int* iters) {
+  auto* S = (Solver*)s;
+  S->nkrylov = nkrylov; S->imp_max_it = max_it; S->inv_res = inv_res;
+  int info = S->implicit_step(cfl, local_dt != 0, l1);
+  if (iters) *iters = S->gmres_iters;
+  return info;
+}
+// y = A x with the BDLU matrix of the last implicit step (x, y: 5 per cell, per-cell blocks)
+void ory_solver_bdlu_matvec(void* s, const double* x, double* y) { ((Solver*)s)->bdlu_yeqax(x, y); }
 
 // ---- Typhon non-regression cases with .tym meshes ----
 // case 1: NRG/TIME/RUNGEKUTTA/<method>  (HLLC, MUSCL-FAST, van Albada, periodic),

@@ -590,6 +590,33 @@ static void roe_flux(double g, const State& L, const State& R, V3 n, double delt
   F[2] = fm.x; F[3] = fm.y; F[4] = fm.z;
 }
 
+// calc_jacflux (SOURCE/EQNS/calc_jacflux.f90:49-77): Jacobian of the physical flux along n
+// with respect to (rho, rhoE, rhou, rhov, rhow), for one state; row-major 5x5
+static void jacflux(double g, const double* st /* rho, p, u, v, w */, V3 fn, double vn, double* J) {
+  const double g1 = g - 1.0, ig1 = 1.0 / g1;
+  const V3 u = v3(st[2], st[3], st[4]);
+  const double v2 = sqrabs(u);
+  const double en = ig1 * st[1] / st[0] + .5 * v2;
+  for (int k = 0; k < 25; ++k) J[k] = 0.0;
+  auto A = [&](int i, int j) -> double& { return J[(i - 1) * 5 + (j - 1)]; };
+  A(1, 1) = 0.0; A(1, 2) = 0.0;
+  A(1, 3) = fn.x; A(1, 4) = fn.y; A(1, 5) = fn.z;
+  A(2, 1) = vn * (g1 * v2 - g * en);
+  A(2, 2) = vn * g;
+  const double c23 = g * en - .5 * g1 * v2;
+  const double t[3] = {fn.x, fn.y, fn.z}, uu[3] = {u.x, u.y, u.z};
+  for (int k = 0; k < 3; ++k) A(2, 3 + k) = c23 * t[k] - g1 * vn * uu[k];
+  for (int k = 0; k < 3; ++k) A(3 + k, 1) = .5 * g1 * v2 * t[k] - vn * uu[k];
+  for (int k = 0; k < 3; ++k) A(3 + k, 2) = g1 * t[k];
+  const V3 g1n = g1 * fn;
+  const double gn[3] = {g1n.x, g1n.y, g1n.z};
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) A(3 + i, 3 + j) = uu[i] * t[j] - gn[i] * uu[j];
+  A(3, 3) = A(3, 3) + vn;
+  A(4, 4) = A(4, 4) + vn;
+  A(5, 5) = A(5, 5) + vn;
+}
+
 void Solver::face_fluxes() {
   const int nf = m->nface;
   const double g = sp.gamma;
@@ -620,6 +647,16 @@ void Solver::face_fluxes() {
       const double beta = 1.0;
       double sl = std::min(vnl - beta * al, vm - am);
       double sr = std::max(vnr + beta * ar, vm + am);
+      if (calc_jac) {  // calc_flux_hllc.f90:178-203 -> calc_jac_hll.f90:46-57
+        double qL[5] = {L.rho, L.p, L.u.x, L.u.y, L.u.z}, qR[5] = {R.rho, R.p, R.u.x, R.u.y, R.u.z};
+        double JL[25], JR[25];
+        double slc = std::min(sl, 0.0), src = std::max(sr, 0.0);
+        jacflux(g, qL, fn, vnl, JL);
+        jacflux(g, qR, fn, vnr, JR);
+        for (int i = 0; i < 5; ++i) { JL[i * 5 + i] = JL[i * 5 + i] - slc; JR[i * 5 + i] = JR[i * 5 + i] - src; }
+        const double cl_ = src / (src - slc), cr_ = -slc / (src - slc);
+        for (int k = 0; k < 25; ++k) { jacL[25 * (size_t)f + k] = cl_ * JL[k]; jacR[25 * (size_t)f + k] = cr_ * JR[k]; }
+      }
       if (sl >= 0.0) {
         F[0] = vnl * L.rho;
         F[1] = vnl * (rel + L.p);
@@ -658,6 +695,14 @@ void Solver::face_fluxes() {
       double vnl = dot(L.u, fn), vnr = dot(R.u, fn);
       double al = std::sqrt(g * L.p / L.rho), ar = std::sqrt(g * R.p / R.rho);
       double ray = std::max(std::fabs(vnl) + al, std::fabs(vnr) + ar);
+      if (calc_jac) {  // calc_jac_rusanov.f90: (A_L + ray I)/2, (A_R - ray I)/2
+        double qL[5] = {L.rho, L.p, L.u.x, L.u.y, L.u.z}, qR[5] = {R.rho, R.p, R.u.x, R.u.y, R.u.z};
+        double JL[25], JR[25];
+        jacflux(g, qL, fn, vnl, JL);
+        jacflux(g, qR, fn, vnr, JR);
+        for (int i = 0; i < 5; ++i) { JL[i * 5 + i] = JL[i * 5 + i] + ray; JR[i * 5 + i] = JR[i * 5 + i] - ray; }
+        for (int k = 0; k < 25; ++k) { jacL[25 * (size_t)f + k] = .5 * JL[k]; jacR[25 * (size_t)f + k] = .5 * JR[k]; }
+      }
       double rel = ig1 * L.p + 0.5 * L.rho * sqrabs(L.u);
       double rer = ig1 * R.p + 0.5 * R.rho * sqrabs(R.u);
       F[0] = 0.5 * ((vnl + ray) * L.rho + (vnr - ray) * R.rho);
@@ -666,6 +711,24 @@ void Solver::face_fluxes() {
       F[2] = mo.x; F[3] = mo.y; F[4] = mo.z;
     } else {
       roe_flux(g, L, R, fn, sp.roe_entropy_fix, F);
+      if (calc_jac) {  // new: HLL Jacobian with Davis-Einfeldt wave speeds from the Roe average
+        double t1 = std::sqrt(R.rho / L.rho);
+        double kl = 1.0 / (1.0 + t1), kr = t1 * kl;
+        V3 ur = kl * L.u + kr * R.u;
+        double hl = g / (g - 1.0) * L.p / L.rho + 0.5 * sqrabs(L.u);
+        double hr = g / (g - 1.0) * R.p / R.rho + 0.5 * sqrabs(R.u);
+        double am = std::sqrt((g - 1.0) * (kl * hl + kr * hr - 0.5 * sqrabs(ur)));
+        double vm = dot(ur, fn), vnl = dot(L.u, fn), vnr = dot(R.u, fn);
+        double al = std::sqrt(g * L.p / L.rho), ar = std::sqrt(g * R.p / R.rho);
+        double sl = std::min(std::min(vnl - al, vm - am), 0.0), sr = std::max(std::max(vnr + ar, vm + am), 0.0);
+        double qL[5] = {L.rho, L.p, L.u.x, L.u.y, L.u.z}, qR[5] = {R.rho, R.p, R.u.x, R.u.y, R.u.z};
+        double JL[25], JR[25];
+        jacflux(g, qL, fn, vnl, JL);
+        jacflux(g, qR, fn, vnr, JR);
+        for (int i = 0; i < 5; ++i) { JL[i * 5 + i] = JL[i * 5 + i] - sl; JR[i * 5 + i] = JR[i * 5 + i] - sr; }
+        const double cl_ = sr / (sr - sl), cr_ = -sl / (sr - sl);
+        for (int k = 0; k < 25; ++k) { jacL[25 * (size_t)f + k] = cl_ * JL[k]; jacR[25 * (size_t)f + k] = cr_ * JR[k]; }
+      }
     }
     for (int v = 0; v < 5; ++v) flux[v * nf + f] = F[v];
   }
@@ -752,6 +815,13 @@ void Solver::viscous_fluxes() {
     flux[nf + f] = flux[nf + f] - svn;
     const double conduct = mu * cp / sp.prandtl;
     flux[nf + f] = flux[nf + f] - conduct * gTH;
+    if (calc_jac) {  // calc_flux_viscous_cell.f90:149-158
+      double idj = mu / (dHR * rL + dHL * rR) / vabs(CR - CL);
+      for (int i = 0; i < 5; ++i) {
+        jacR[25 * (size_t)f + i * 5 + i] = jacR[25 * (size_t)f + i * 5 + i] - idj;
+        jacL[25 * (size_t)f + i * 5 + i] = jacL[25 * (size_t)f + i * 5 + i] + idj;
+      }
+    }
   }
 }
 
@@ -800,8 +870,14 @@ void Solver::ns_bocoflux() {
 void Solver::flux_to_res() {
   const int nc = m->ncell, nci = m->ncell_int, nf = m->nface;
 #pragma omp parallel for schedule(static)
-  for (int f = 0; f < nf; ++f)
+  for (int f = 0; f < nf; ++f) {
     for (int v = 0; v < 5; ++v) flux[v * nf + f] = m->fsurf[f] * flux[v * nf + f];
+    if (calc_jac)
+      for (int k = 0; k < 25; ++k) {
+        jacL[25 * (size_t)f + k] = m->fsurf[f] * jacL[25 * (size_t)f + k];
+        jacR[25 * (size_t)f + k] = m->fsurf[f] * jacR[25 * (size_t)f + k];
+      }
+  }
   std::fill(residu.begin(), residu.end(), 0.0);
   for (auto& col : m->colors)  // faces of one colour touch distinct cells
 #pragma omp parallel for schedule(static)
@@ -818,6 +894,188 @@ void Solver::flux_to_res() {
     double coef = dtloc[c] / m->cvol[c];
     for (int v = 0; v < 5; ++v) residu[v * nc + c] = coef * residu[v * nc + c];
   }
+}
+
+
+// init_implicit_bdlu.f90:37-49 + build_implicit_bdlu.f90:44-83: row-major 5x5 blocks
+void Solver::build_implicit_bdlu() {
+  const int nc = m->ncell, nci = m->ncell_int, nf = m->nface, nfi = m->nface_int;
+  bdiag.assign(25 * (size_t)nc, 0.0);
+  bupper.assign(25 * (size_t)nf, 0.0);
+  blower.assign(25 * (size_t)nf, 0.0);
+  for (int c = 0; c < nci; ++c)
+    for (int i = 0; i < 5; ++i) bdiag[25 * (size_t)c + i * 5 + i] = 1.0;
+  for (int f = 0; f < nfi; ++f) {
+    const int c1 = m->fc1[f], c2 = m->fc2[f];
+    for (int k = 0; k < 25; ++k) {
+      bdiag[25 * (size_t)c1 + k] = bdiag[25 * (size_t)c1 + k] + jacL[25 * (size_t)f + k] * dtloc[c1] / m->cvol[c1];
+      bupper[25 * (size_t)f + k] = +jacR[25 * (size_t)f + k] * dtloc[c1] / m->cvol[c1];
+      bdiag[25 * (size_t)c2 + k] = bdiag[25 * (size_t)c2 + k] - jacR[25 * (size_t)f + k] * dtloc[c2] / m->cvol[c2];
+      blower[25 * (size_t)f + k] = -jacL[25 * (size_t)f + k] * dtloc[c2] / m->cvol[c2];
+    }
+  }
+  for (int f = nfi; f < nf; ++f) {
+    const int c1 = m->fc1[f], c2 = m->fc2[f];
+    for (int k = 0; k < 25; ++k) {
+      bdiag[25 * (size_t)c1 + k] = bdiag[25 * (size_t)c1 + k] + jacL[25 * (size_t)f + k] * dtloc[c1] / m->cvol[c1];
+      bupper[25 * (size_t)f + k] = +jacR[25 * (size_t)f + k] * dtloc[c1] / m->cvol[c1];
+    }
+    for (int k = 0; k < 25; ++k) bdiag[25 * (size_t)c2 + k] = 0.0;
+    for (int i = 0; i < 5; ++i) bdiag[25 * (size_t)c2 + i * 5 + i] = 1.0;
+    for (int k = 0; k < 25; ++k) blower[25 * (size_t)f + k] = 0.0;
+  }
+}
+
+static inline void matvec5(const double* A, const double* x, double* y) {  // matmul(A, x)
+  for (int i = 0; i < 5; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < 5; ++j) s = s + A[i * 5 + j] * x[j];
+    y[i] = s;
+  }
+}
+
+// SPMAT_BDLU.f90:139-157 (bdlu_yeqax): y = A x, diagonal blocks first, then faces in order
+void Solver::bdlu_yeqax(const double* x, double* y) const {
+  const int nc = m->ncell, nf = m->nface;
+  double t[5];
+  for (int c = 0; c < nc; ++c) matvec5(&bdiag[25 * (size_t)c], &x[5 * (size_t)c], &y[5 * (size_t)c]);
+  for (int f = 0; f < nf; ++f) {
+    const int c1 = m->fc1[f], c2 = m->fc2[f];
+    matvec5(&blower[25 * (size_t)f], &x[5 * (size_t)c1], t);
+    for (int i = 0; i < 5; ++i) y[5 * (size_t)c2 + i] = y[5 * (size_t)c2 + i] + t[i];
+    matvec5(&bupper[25 * (size_t)f], &x[5 * (size_t)c2], t);
+    for (int i = 0; i < 5; ++i) y[5 * (size_t)c1 + i] = y[5 * (size_t)c1 + i] + t[i];
+  }
+}
+
+// SPMAT_BDLU.f90:240-262 (bdlu_yeqmaxpz): y = z - A x
+void Solver::bdlu_yeqmaxpz(const double* x, const double* z, double* y) const {
+  const int nc = m->ncell, nf = m->nface;
+  double t[5];
+  for (int c = 0; c < nc; ++c) {
+    matvec5(&bdiag[25 * (size_t)c], &x[5 * (size_t)c], t);
+    for (int i = 0; i < 5; ++i) y[5 * (size_t)c + i] = z[5 * (size_t)c + i] - t[i];
+  }
+  for (int f = 0; f < nf; ++f) {
+    const int c1 = m->fc1[f], c2 = m->fc2[f];
+    matvec5(&blower[25 * (size_t)f], &x[5 * (size_t)c1], t);
+    for (int i = 0; i < 5; ++i) y[5 * (size_t)c2 + i] = y[5 * (size_t)c2 + i] - t[i];
+    matvec5(&bupper[25 * (size_t)f], &x[5 * (size_t)c2], t);
+    for (int i = 0; i < 5; ++i) y[5 * (size_t)c1 + i] = y[5 * (size_t)c1 + i] - t[i];
+  }
+}
+
+static double dotp(const std::vector<double>& a, const std::vector<double>& b, size_t n) {
+  double s = 0.0;  // dot_product, sequential
+  for (size_t i = 0; i < n; ++i) s = s + a[i] * b[i];
+  return s;
+}
+
+// bdlu_gmres (SOURCE/MATH/bdlu_gmres.f90:50-217): restarted GMRES, modified Gram-Schmidt,
+// Givens rotations, x0 = b / diag, stop when |r|/|b| < INV_RES * |x0|_1, at most 2*max_it
+// restarts.  Returns the number of restarts - 1 (info), or -1 if not converged.
+int Solver::bdlu_gmres(double* sol) {
+  const size_t dim = 5 * (size_t)m->ncell;
+  const int nk = nkrylov;
+  std::vector<double> qc(nk), qs(nk), ss(nk + 1), yy(nk), hh((nk + 1) * (size_t)nk);
+  auto H = [&](int i, int j) -> double& { return hh[(size_t)(i - 1) * nk + (j - 1)]; };
+  std::vector<double> r1(dim), p1(dim);
+  std::vector<std::vector<double>> w1(nk, std::vector<double>(dim)), v1(nk, std::vector<double>(dim));
+  for (size_t i = 0; i < dim; ++i) p1[i] = sol[i];
+  for (int c = 0; c < m->ncell; ++c)
+    for (int b = 0; b < 5; ++b) sol[5 * (size_t)c + b] = p1[5 * (size_t)c + b] / bdiag[25 * (size_t)c + b * 5 + b];
+  double ref = 0.0;
+  for (size_t i = 0; i < dim; ++i) ref = ref + std::fabs(sol[i]);
+  const double normp1 = std::sqrt(dotp(p1, p1, dim));
+  const double eps = std::numeric_limits<double>::epsilon();
+  double errgmres = std::numeric_limits<double>::max();
+  int nit = 0;
+  while (errgmres >= ref * inv_res && nit <= imp_max_it * 2) {
+    bdlu_yeqmaxpz(sol, p1.data(), r1.data());
+    double beta = std::sqrt(dotp(r1, r1, dim));
+    double fact = 1.0 / beta;
+    for (size_t i = 0; i < dim; ++i) v1[0][i] = fact * r1[i];
+    std::fill(ss.begin(), ss.end(), 0.0);
+    ss[0] = beta;
+    std::fill(hh.begin(), hh.end(), 0.0);
+    int jk;
+    for (jk = 1; jk <= nk; ++jk) {
+      bdlu_yeqax(v1[jk - 1].data(), w1[jk - 1].data());
+      for (int ik = 1; ik <= jk; ++ik) {
+        H(ik, jk) = dotp(w1[jk - 1], v1[ik - 1], dim);
+        for (size_t i = 0; i < dim; ++i) w1[jk - 1][i] = w1[jk - 1][i] - H(ik, jk) * v1[ik - 1][i];
+      }
+      H(jk + 1, jk) = std::sqrt(dotp(w1[jk - 1], w1[jk - 1], dim));
+      for (int ik = 1; ik <= jk - 1; ++ik) {
+        double tmp = H(ik, jk);
+        H(ik, jk) = qc[ik - 1] * tmp + qs[ik - 1] * H(ik + 1, jk);
+        H(ik + 1, jk) = -qs[ik - 1] * tmp + qc[ik - 1] * H(ik + 1, jk);
+      }
+      if (H(jk + 1, jk) > eps * 10 * normp1) {
+        if (jk < nk) {
+          fact = 1.0 / H(jk + 1, jk);
+          for (size_t i = 0; i < dim; ++i) v1[jk][i] = fact * w1[jk - 1][i];
+        }
+        if (H(jk, jk) == 0) break;
+        double tmp = std::sqrt(H(jk, jk) * H(jk, jk) + H(jk + 1, jk) * H(jk + 1, jk));
+        qc[jk - 1] = H(jk, jk) / tmp;
+        qs[jk - 1] = H(jk + 1, jk) / tmp;
+        H(jk, jk) = tmp;
+        H(jk + 1, jk) = 0.0;
+        ss[jk] = -qs[jk - 1] * ss[jk - 1];
+        ss[jk - 1] = qc[jk - 1] * ss[jk - 1];
+        if (std::fabs(ss[jk]) < inv_res * std::fabs(ss[0])) break;
+      } else {
+        break;
+      }
+    }
+    const int nkk = std::min(jk, nk);
+    for (int j = nkk; j >= 1; --j) {
+      double tmp = ss[j - 1];
+      for (int ik = j + 1; ik <= nkk; ++ik) tmp = tmp - H(j, ik) * yy[ik - 1];
+      yy[j - 1] = tmp / H(j, j);
+      for (size_t i = 0; i < dim; ++i) sol[i] = sol[i] + yy[j - 1] * v1[j - 1][i];
+    }
+    bdlu_yeqmaxpz(sol, p1.data(), r1.data());
+    ss[nkk] = std::sqrt(dotp(r1, r1, dim));
+    errgmres = ss[nkk] / normp1;
+    nit = nit + 1;
+  }
+  gmres_iters = nit;
+  return nit <= imp_max_it ? nit - 1 : -1;
+}
+
+// calc_rhs with the implicit method (calc_rhs.f90:121-138) then update_field (U += dU):
+// steady backward Euler with the stability time step at CFL (global minimum or local)
+int Solver::implicit_step(double cfl_, bool local_dt, double* l1) {
+  cfl = cfl_;
+  double dt = timestep();
+  if (!(dt > 0.0)) return -2;
+  const int nc = m->ncell, nci = m->ncell_int;
+  if (!local_dt) std::fill(dtloc.begin(), dtloc.begin() + nci, dt);
+  calc_jac = true;
+  jacL.assign(25 * (size_t)m->nface, 0.0);
+  jacR.assign(25 * (size_t)m->nface, 0.0);
+  calc_rhs();
+  calc_jac = false;
+  build_implicit_bdlu();
+  for (int v = 0; v < 5; ++v)  // build_implicit.f90:66-74: ghost rows of the RHS are zero
+    for (int c = nci; c < nc; ++c) residu[v * (size_t)nc + c] = 0.0;
+  // packst (implicit_solve.f90:40): per cell (rho, rhoE, rhou, rhov, rhow)
+  std::vector<double> x(5 * (size_t)nc);
+  for (int c = 0; c < nc; ++c)
+    for (int v = 0; v < 5; ++v) x[5 * (size_t)c + v] = residu[v * (size_t)nc + c];
+  int info = bdlu_gmres(x.data());
+  for (int c = 0; c < nc; ++c)
+    for (int v = 0; v < 5; ++v) residu[v * (size_t)nc + c] = x[5 * (size_t)c + v];
+  for (size_t k = 0; k < cons.size(); ++k) cons[k] = cons[k] + residu[k];  // update_field.f90:38
+  if (l1)
+    for (int v = 0; v < 5; ++v) {
+      double a = 0.0;
+      for (int c = 0; c < nci; ++c) a += std::fabs(residu[v * (size_t)nc + c]);
+      l1[v] = a;
+    }
+  return info;
 }
 
 // calc_rhs.f90 explicit part: prim, ghost states, gradient, face states, fluxes, residual
@@ -837,7 +1095,35 @@ void Solver::calc_rhs() {
     viscous_fluxes();
     ns_bocoflux();
   }
+  if (calc_jac) ns_bocojacobian();
   flux_to_res();
+}
+
+// ns_bocojacobian.f90:47-85: on symmetry faces the ghost state is the mirrored cell state, so
+// J_L += J_R dQr/dQl with dQr/dQl = I - 2 n n^T on the momentum block, and J_R = 0.
+// Other boundary kinds (periodic, wall) keep their Jacobians.
+void Solver::ns_bocojacobian() {
+  for (const Boco& b : m->bocos) {
+    if (b.kind != BC_SYMMETRY) continue;
+    for (int f : b.iface) {
+      const V3 n = m->fnormal[f];
+      const double nn[3] = {n.x, n.y, n.z};
+      double M[25];
+      for (int k = 0; k < 25; ++k) M[k] = 0.0;
+      for (int i = 0; i < 5; ++i) M[i * 5 + i] = 1.0;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) M[(2 + i) * 5 + 2 + j] = M[(2 + i) * 5 + 2 + j] - 2.0 * (nn[i] * nn[j]);
+      double* JL = &jacL[25 * (size_t)f];
+      double* JR = &jacR[25 * (size_t)f];
+      for (int i = 0; i < 5; ++i)
+        for (int j = 0; j < 5; ++j) {
+          double a = 0.0;
+          for (int k = 0; k < 5; ++k) a = a + JR[i * 5 + k] * M[k * 5 + j];
+          JL[i * 5 + j] = JL[i * 5 + j] + a;
+        }
+      for (int k = 0; k < 25; ++k) JR[k] = 0.0;
+    }
+  }
 }
 
 // calc_ns_timestep.f90:52-103 + calc_zonetimestep.f90 min over interior cells

@@ -56,6 +56,9 @@ def load():
         lib.ory_solver_rhs.argtypes = [vp, C.c_double]
         lib.ory_solver_rk_step.argtypes = [vp, C.c_double]
         lib.ory_solver_run_steps.argtypes = [vp, C.c_int, vp]
+        lib.ory_solver_implicit_step.argtypes = [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp]
+        lib.ory_solver_implicit_step.restype = C.c_int
+        lib.ory_solver_bdlu_matvec.argtypes = [vp, vp, vp]
         lib.ory_run_nrg.argtypes = [C.c_int, vp, C.c_int, C.c_double, C.c_int, C.c_double, vp]
         _lib = lib
     return _lib
@@ -174,6 +177,32 @@ class Solver:
 
     def timestep(self):
         return self.lib.ory_solver_timestep(self.h)
+
+    def get_implicit(self, which):
+        """Jacobians and BDLU blocks of the last implicit step: jacL, jacR, upper, lower are
+        (nface, 5, 5), diag (ncell, 5, 5); rows are (rho, rhoE, rhou, rhov, rhow)."""
+        code, n = {"jacL": (9, self.mesh.nface), "jacR": (10, self.mesh.nface), "diag": (11, self.mesh.ncell),
+                   "upper": (12, self.mesh.nface), "lower": (13, self.mesh.nface)}[which]
+        out = np.zeros(25 * n)
+        assert self.lib.ory_solver_get(self.h, code, _p(out)) == 25 * n
+        return out.reshape(n, 5, 5)
+
+    def implicit_step(self, cfl, local_dt=False, nkrylov=50, max_it=50, inv_res=1e-4):
+        """One backward-Euler step; returns (info, gmres restarts, L1 of the update per variable)."""
+        l1 = np.zeros(5)
+        it = C.c_int()
+        info = self.lib.ory_solver_implicit_step(self.h, float(cfl), int(local_dt), int(nkrylov), int(max_it),
+                                                 float(inv_res), _p(l1), C.byref(it))
+        if info == -2:
+            raise RuntimeError("oracle implicit step: bad time step")
+        return info, it.value, l1
+
+    def bdlu_matvec(self, x):
+        """y = A x with the BDLU matrix of the last implicit step; x is (ncell, 5)."""
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        self.lib.ory_solver_bdlu_matvec(self.h, _p(x), _p(y))
+        return y
 
     def rhs(self, dt):
         self.lib.ory_solver_rhs(self.h, dt)
