@@ -173,10 +173,60 @@ int ty_set_stream(ty_mesh* mesh, void* stream);
 /* Per-kernel CUDA-event timing of every launch issued while enabled (enabling clears the
  * record).  ty_profile_read returns, per kernel id (0 prim, 1 ghost_prim, 2 grad,
  * 3 ghost_grad, 4 face_states, 5 barth, 6 face_flux, 7 face_flux_lim, 8 rk_update,
- * 9 gather, 10 timestep, 11 cell_fast, 12 face_flux_fast), the summed milliseconds and the
- * number of launches. */
+ * 9 gather, 10 timestep, 11 cell_fast, 12 face_flux_fast, 13 imp_face, 14 imp_diag,
+ * 15 imp_matvec, 16 imp_precond, 17 imp_ortho), the summed milliseconds and the number of
+ * launches. */
 int ty_profile_enable(ty_mesh* mesh, int32_t on);
 int ty_profile_read(ty_mesh* mesh, int32_t n, double* ms, int32_t* launches);
+
+/* ---------------------------------------------------------------------------------
+ * Implicit (backward Euler) step.  Replaces calc_rhs.f90:121-138 with calc_jacobian set
+ * (integration_grid + build_implicit + tstep_implicit/implicit_solve) and update_field.f90:38.
+ */
+typedef enum {
+  TY_KRYLOV_GMRES = 0,   /* Typhon's bdlu_gmres (bdlu_gmres.f90:50-217): MGS, no preconditioner */
+  TY_KRYLOV_FGMRES = 1,  /* flexible GMRES(m), CGS2, right block-Jacobi, assembled matrix (new) */
+  TY_KRYLOV_JFNK = 2     /* flexible GMRES(m), CGS2, block-Jacobi, Jacobian-free products (new) */
+} ty_krylov;
+typedef enum {
+  TY_PREC_FP64 = 0,      /* everything in FP64 */
+  TY_PREC_MIXED = 1      /* TY_KRYLOV_FGMRES only: FP32 blocks, mat-vec and preconditioner; FP64
+                            residual, basis, CGS2 orthogonalisation and update */
+} ty_precision;
+typedef struct ty_imp_params {
+  int32_t krylov;        /* ty_krylov (INVERSION = GMRES is TY_KRYLOV_GMRES) */
+  int32_t precision;     /* ty_precision */
+  int32_t nkrylov;       /* NKRYLOV: Krylov vectors per cycle (GMRES <= 64, others <= 32) */
+  int32_t max_it;        /* IMP_MAX_IT: GMRES stops after 2*max_it+1 cycles (Typhon), the
+                            others after max_it cycles */
+  int32_t local_dt;      /* DTCALC: 1 = LOCAL_STABILITY_CONDITION, 0 = STABILITY_CONDITION */
+  int32_t reserved;
+  double inv_res;        /* INV_RES: GMRES uses Typhon's test |r|/|b| < INV_RES |x0|_1; the
+                            others |r|/|b| <= INV_RES */
+  double cfl;            /* stability number of this step (the caller ramps it) */
+} ty_imp_params;
+typedef struct ty_imp_stats {
+  int32_t info;          /* GMRES: cycles - 1 when converged, -1 otherwise (bdlu_gmres info) */
+  int32_t restarts;      /* Krylov cycles run */
+  int32_t matvecs;       /* operator applications */
+  int32_t reserved;
+  double dt_min;         /* smallest cell time step of the step */
+  double res_l2[5];      /* L2 norm over cells of -sum(F S)/V per variable, before the update */
+  double du_l1[5];       /* L1 norm of the update per variable (update_field.f90:54-60) */
+  double lin_res;        /* final relative linear residual |b - A x| / |b| */
+} ty_imp_stats;
+/* One implicit step on the resident state: time step (per cell or global at p->cfl),
+ * residual with flux Jacobians (HLL for HLLC and Roe, Rusanov's for Rusanov, viscous
+ * diagonal, symmetry mirror), BDLU assembly, linear solve, U += dU. */
+int ty_implicit_step(ty_mesh* mesh, const ty_imp_params* p, ty_imp_stats* stats);
+/* Parity access after ty_implicit_step (host, row-major 5x5 blocks):
+ * which = 0 jacL [nface][25], 1 jacR [nface][25] (times S), 2 diagonal blocks [ncell_int][25],
+ *         3 upper [nface_int][25], 4 lower [nface_int][25], 5 dtloc [ncell_int],
+ *         6 right-hand side [ncell_int][5], 7 solution dU [ncell_int][5]. */
+int ty_implicit_get(ty_mesh* mesh, int32_t which, double* out);
+/* y = A x with the FP64 BDLU matrix of the last implicit step; x, y host [ncell_int][5]
+ * (Typhon's bdlu_yeqax, SPMAT_BDLU.f90:139-157). */
+int ty_implicit_matvec(ty_mesh* mesh, const double* x, double* y);
 
 /* Global stability time step for callers that cannot let the library allocate device
  * memory (a host code that owns all device memory through its own allocator, a solver loop

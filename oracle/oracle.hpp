@@ -190,6 +190,7 @@ struct Solver {
   int nkrylov = 50, imp_max_it = 50;
   double inv_res = 1.e-4;
   int gmres_iters = 0;
+  std::vector<double> rhs_b;              // right-hand side of the last implicit solve (per cell)
   void ns_bocojacobian();
   void build_implicit_bdlu();
   void bdlu_yeqax(const double* x, double* y) const;

@@ -156,7 +156,8 @@ void ory_solver_set_prim(void* s, const double* p) {
   S->varcons();
 }
 // which: 0 cons, 1 prim, 2 grad, 3 residu, 4 flux, 5 cell_l, 6 cell_r, 7 dtloc, 8 limratio,
-//        9 jacL, 10 jacR (25 per face, row-major), 11 BDLU diag (25 per cell), 12 upper, 13 lower
+//        9 jacL, 10 jacR (25 per face, row-major), 11 BDLU diag (25 per cell), 12 upper, 13 lower,
+//        14 right-hand side of the last implicit solve (5 per cell)
 int ory_solver_get(void* s, int which, double* out) {
   auto* S = (Solver*)s;
   const std::vector<double>* v = nullptr;
@@ -175,6 +176,7 @@ int ory_solver_get(void* s, int which, double* out) {
     case 11: v = &S->bdiag; break;
     case 12: v = &S->bupper; break;
     case 13: v = &S->blower; break;
+    case 14: v = &S->rhs_b; break;
     default: return -1;
   }
   std::memcpy(out, v->data(), v->size() * sizeof(double));

@@ -1065,6 +1065,7 @@ int Solver::implicit_step(double cfl_, bool local_dt, double* l1) {
   std::vector<double> x(5 * (size_t)nc);
   for (int c = 0; c < nc; ++c)
     for (int v = 0; v < 5; ++v) x[5 * (size_t)c + v] = residu[v * (size_t)nc + c];
+  rhs_b = x;
   int info = bdlu_gmres(x.data());
   for (int c = 0; c < nc; ++c)
     for (int v = 0; v < 5; ++v) residu[v * (size_t)nc + c] = x[5 * (size_t)c + v];

@@ -187,6 +187,12 @@ class Solver:
         assert self.lib.ory_solver_get(self.h, code, _p(out)) == 25 * n
         return out.reshape(n, 5, 5)
 
+    def implicit_rhs(self):
+        """Right-hand side of the last implicit solve, (ncell, 5)."""
+        out = np.zeros(5 * self.mesh.ncell)
+        assert self.lib.ory_solver_get(self.h, 14, _p(out)) == out.size
+        return out.reshape(self.mesh.ncell, 5)
+
     def implicit_step(self, cfl, local_dt=False, nkrylov=50, max_it=50, inv_res=1e-4):
         """One backward-Euler step; returns (info, gmres restarts, L1 of the update per variable)."""
         l1 = np.zeros(5)

@@ -1,0 +1,184 @@
+"""GPU implicit step (ty_implicit_step) against the oracle, through the C ABI.
+
+Exact mode: the flux Jacobians, the BDLU blocks, the local time steps, the right-hand side
+and the block mat-vec are bit for bit the oracle's.  The Krylov solvers reduce dot products
+in a different order than the oracle's sequential sums, so their solutions are compared with
+a tolerance: Typhon's GMRES against the oracle's GMRES, the flexible GMRES (FP64, mixed FP32)
+against the oracle's converged solution, and the Jacobian-free solver through the steady
+convergence it produces.
+"""
+import numpy as np
+import pytest
+
+import oracle_py as op
+
+pytestmark = pytest.mark.gpu
+
+SYMMETRY_BOX = [(f, op.BC_SYMMETRY, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX")]
+MXLAY_BCS = [("IMIN", op.BC_PERIODIC, "IMAX", (1.0, 0.0, 0.0)),
+             ("JMIN", op.BC_WALL, "", (0.0, 0.0, 0.0), (-1.0, 0.0, 0.0)),
+             ("JMAX", op.BC_WALL, "", (0.0, 0.0, 0.0), (1.0, 0.0, 0.0))]
+OSCH = {"HLLC": op.SCH_HLLC, "RUSANOV": op.SCH_RUSANOV, "ROE": op.SCH_ROE}
+OHRES = {"NONE": op.HRES_NONE, "MUSCL": op.HRES_MUSCL, "MUSCL-FAST": op.HRES_MUSCLFAST, "MUSCL-UNS": op.HRES_MUSCLUNS}
+OLIM = {"NONE": op.LIM_NONE, "ALBADA": op.LIM_ALBADA, "MINMOD": op.LIM_MINMOD}
+OPOST = {"NONE": op.POSTLIM_NONE, "BARTH": op.POSTLIM_BARTH}
+
+
+@pytest.fixture(scope="module")
+def ty():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from typhon_gb300 import build
+    build.build()
+    import typhon_gb300
+    return typhon_gb300
+
+
+def vortex_at_rest(cc, strength=0.3):
+    x, y = cc[:, 0] - 0.5, cc[:, 1] - 0.5
+    r2 = (x * x + y * y) / 0.01
+    n = len(x)
+    return np.stack([np.ones(n) + 0.05 * np.exp(-r2), 1 / 1.4 - 0.5 * strength ** 2 * 0.01 * np.exp(-r2),
+                     -strength * y * np.exp(-r2 / 2), strength * x * np.exp(-r2 / 2), np.zeros(n)])
+
+
+def case_2d(ty, golden_dir, name, bcs_gpu, bcs_or=None):
+    raw = ty.read_tym(golden_dir / name)
+    md = ty.preprocess(raw, 2, bcs_gpu)
+    om = op.Mesh.from_tym(golden_dir / name).build(2, bcs_or or bcs_gpu)
+    return md, om
+
+
+def pair(ty, md, om, prim, scheme="HLLC", highres="NONE", limiter="NONE", postlim="NONE", gradmeth=None,
+         mode="exact", viscous="NONE", kin_visc=0.0):
+    g = ty.Grid(md)
+    g.set_spat(scheme, highres, limiter, postlim, gradmeth=gradmeth, mode=mode, dissipative_flux=viscous,
+               kin_visc=kin_visc)
+    g.set_prim(prim)
+    gm = gradmeth or ("NONE" if (highres == "NONE" and viscous == "NONE") else "LSQ")
+    s = op.Solver(om, OSCH[scheme], OHRES[highres], OLIM[limiter], OPOST[postlim],
+                  op.GRAD_NONE if gm == "NONE" else op.GRAD_LSQ, cfl=1.0,
+                  viscous={"NONE": 0, "CELL-AVERAGE": op.VISC_CELLAVG, "FULL": op.VISC_CELLFULL}[viscous],
+                  visc_kin=kin_visc)
+    s.set_prim(prim)
+    return g, s
+
+
+def assert_blocks_equal(g, s, md):
+    nci, nfi = md.ncell_int, md.nface_int
+    for name in ("jacL", "jacR"):
+        assert np.array_equal(g.implicit_get(name), s.get_implicit(name)), name
+    assert np.array_equal(g.implicit_get("diag"), s.get_implicit("diag")[:nci]), "diag"
+    assert np.array_equal(g.implicit_get("upper"), s.get_implicit("upper")[:nfi]), "upper"
+    assert np.array_equal(g.implicit_get("lower"), s.get_implicit("lower")[:nfi]), "lower"
+    assert np.array_equal(g.implicit_get("dtloc"), s.get("dtloc")[0, :nci]), "dtloc"
+    assert np.array_equal(g.implicit_get("rhs"), s.implicit_rhs()[:nci]), "rhs"
+
+
+def relerr(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+CASES = [
+    # mesh, bcs, scheme, highres, limiter, postlim, viscous, local_dt
+    ("quad20x20.tym", "periodic", "HLLC", "NONE", "NONE", "NONE", "NONE", True),
+    ("quad20x10.tym", "symmetry", "RUSANOV", "NONE", "NONE", "NONE", "NONE", False),
+    ("quad20x20.tym", "periodic", "ROE", "MUSCL-UNS", "NONE", "BARTH", "NONE", True),
+    ("quad20x20.tym", "periodic", "HLLC", "MUSCL-FAST", "ALBADA", "NONE", "NONE", False),
+    ("mxlay2x20quad-h50.tym", "mxlay", "HLLC", "MUSCL", "ALBADA", "NONE", "CELL-AVERAGE", True),
+    ("mxlay2x20quad-h50.tym", "mxlay", "RUSANOV", "NONE", "NONE", "NONE", "FULL", False),
+]
+
+
+def _bcs(kind):
+    return {"periodic": op.PERIODIC_UNIT_SQUARE, "symmetry": SYMMETRY_BOX, "mxlay": MXLAY_BCS}[kind]
+
+
+def _prim(md, kind):
+    if kind == "mxlay":
+        from scipy.special import erf
+        y = md.cell_centre[:, 1]
+        n = md.ncell
+        return np.stack([np.ones(n), np.full(n, 100 / 1.4), erf(y / 2), np.zeros(n), np.zeros(n)])
+    cc = md.cell_centre
+    if kind == "symmetry":
+        cc = cc / np.array([2.0, 1.0, 1.0])
+    return vortex_at_rest(cc)
+
+
+@pytest.mark.parametrize("name,bck,scheme,highres,limiter,postlim,viscous,local", CASES)
+def test_exact_assembly_and_gmres(ty, golden_dir, name, bck, scheme, highres, limiter, postlim, viscous, local):
+    md, om = case_2d(ty, golden_dir, name, _bcs(bck))
+    prim = _prim(md, bck)
+    kv = 1.0 if viscous != "NONE" else 0.0
+    g, s = pair(ty, md, om, prim, scheme, highres, limiter, postlim, viscous=viscous, kin_visc=kv)
+    cfl = 20.0
+    U0 = g.get_cons()
+    st = g.implicit_step(cfl, "GMRES", nkrylov=30, max_it=20, inv_res=1e-10, local_dt=local)
+    info, it, l1 = s.implicit_step(cfl, local_dt=local, nkrylov=30, max_it=20, inv_res=1e-10)
+    assert_blocks_equal(g, s, md)
+    # block mat-vec, bit for bit
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((md.ncell_int, 5))
+    xo = np.zeros((md.ncell, 5))
+    xo[:md.ncell_int] = x
+    assert np.array_equal(g.implicit_matvec(x), s.bdlu_matvec(xo)[:md.ncell_int])
+    # Typhon's GMRES: same restarts, solution within rounding of the oracle's
+    assert st["info"] == info and st["restarts"] == it
+    du = g.get_cons() - U0
+    du_o = (s.get("cons") - 0)[:, :md.ncell_int] - U0
+    assert relerr(du, du_o) < 1e-9
+    assert np.allclose(st["du_l1"], l1, rtol=1e-9, atol=0)
+
+
+@pytest.mark.parametrize("inversion,precision,tol", [("FGMRES", "fp64", 1e-8), ("FGMRES", "mixed", 2e-5)])
+def test_fgmres_reaches_the_oracle_solution(ty, golden_dir, inversion, precision, tol):
+    md, om = case_2d(ty, golden_dir, "quad20x20.tym", op.PERIODIC_UNIT_SQUARE)
+    prim = vortex_at_rest(md.cell_centre)
+    g, s = pair(ty, md, om, prim, "ROE", "MUSCL-UNS", "NONE", "BARTH", mode="fast")
+    U0 = g.get_cons()
+    st = g.implicit_step(50.0, inversion, nkrylov=30, max_it=10, inv_res=1e-11 if precision == "fp64" else 1e-7,
+                         local_dt=True, precision=precision)
+    s.implicit_step(50.0, local_dt=True, nkrylov=60, max_it=40, inv_res=1e-13)
+    du = g.get_cons() - U0
+    du_o = s.get("cons")[:, :md.ncell_int] - U0
+    assert relerr(du, du_o) < tol, (relerr(du, du_o), st)
+    assert st["matvecs"] < 200
+
+
+@pytest.mark.parametrize("inversion,precision", [("GMRES", "fp64"), ("FGMRES", "fp64"), ("FGMRES", "mixed"),
+                                                 ("JFNK", "fp64")])
+def test_steady_convergence(ty, golden_dir, inversion, precision):
+    """Implicit steps with a growing CFL drive a vortex at rest to its discrete steady state."""
+    md, om = case_2d(ty, golden_dir, "quad20x20.tym", op.PERIODIC_UNIT_SQUARE)
+    g = ty.Grid(md)
+    g.set_spat("HLLC", "MUSCL", "ALBADA", mode="fast")
+    g.set_prim(vortex_at_rest(md.cell_centre))
+    hist = []
+    cfl = 10.0
+    for it in range(40):
+        st = g.implicit_step(cfl, inversion, nkrylov=30 if inversion != "GMRES" else 50, max_it=5,
+                             inv_res=1e-3, local_dt=True, precision=precision)
+        hist.append(np.linalg.norm(st["res_l2"]))
+        cfl = min(cfl * 1.5, 1e4)
+        if hist[-1] < 1e-10 * hist[0]:
+            break
+    assert hist[-1] < 1e-6 * hist[0], hist
+
+
+def test_implicit_errors(ty, golden_dir):
+    md, _ = case_2d(ty, golden_dir, "quad10x10.tym", op.PERIODIC_UNIT_SQUARE)
+    g = ty.Grid(md)
+    g.set_spat("HLLC")
+    with pytest.raises(ty.TyphonError):            # no state yet
+        g.implicit_step(1.0)
+    g.set_prim(vortex_at_rest(md.cell_centre))
+    with pytest.raises(ty.TyphonError):            # Typhon's GMRES is FP64 only
+        g.implicit_step(1.0, "GMRES", precision="mixed")
+    with pytest.raises(ty.TyphonError):            # restart length of the flexible GMRES
+        g.implicit_step(1.0, "FGMRES", nkrylov=40)
+    with pytest.raises(ty.TyphonError):            # nothing assembled in FP64 yet
+        g.implicit_matvec(np.zeros((md.ncell_int, 5)))
+    st = g.implicit_step(1.0, "FGMRES", precision="mixed")
+    assert st["lin_res"] <= 1e-4

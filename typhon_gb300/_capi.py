@@ -48,6 +48,19 @@ class SpatParams(C.Structure):
 
 _lib = None
 
+class ImpParams(C.Structure):
+    """ty_imp_params"""
+    _fields_ = [("krylov", C.c_int32), ("precision", C.c_int32), ("nkrylov", C.c_int32), ("max_it", C.c_int32),
+                ("local_dt", C.c_int32), ("reserved", C.c_int32), ("inv_res", C.c_double), ("cfl", C.c_double)]
+
+
+class ImpStats(C.Structure):
+    """ty_imp_stats"""
+    _fields_ = [("info", C.c_int32), ("restarts", C.c_int32), ("matvecs", C.c_int32), ("reserved", C.c_int32),
+                ("dt_min", C.c_double), ("res_l2", C.c_double * 5), ("du_l1", C.c_double * 5),
+                ("lin_res", C.c_double)]
+
+
 _SIGS = {
     "ty_version": ([], C.c_char_p),
     "ty_error_string": ([C.c_int], C.c_char_p),
@@ -72,6 +85,9 @@ _SIGS = {
     "ty_profile_read": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "ty_timestep_static": ([C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                             C.c_void_p, C.POINTER(C.c_double)], C.c_int),
+    "ty_implicit_step": ([C.c_void_p, C.POINTER(ImpParams), C.POINTER(ImpStats)], C.c_int),
+    "ty_implicit_get": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "ty_implicit_matvec": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "ty_umesh_new": ([C.POINTER(C.c_void_p)], C.c_int),
     "ty_umesh_free": ([C.c_void_p], C.c_int),
     "ty_umesh_set_nodes": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
@@ -85,7 +101,8 @@ _SIGS = {
 
 
 KERNEL_NAMES = ["prim", "ghost_prim", "grad", "ghost_grad", "face_states", "barth", "face_flux",
-                "face_flux_lim", "rk_update", "gather", "timestep", "cell_fast", "face_flux_fast"]
+                "face_flux_lim", "rk_update", "gather", "timestep", "cell_fast", "face_flux_fast",
+                "imp_face", "imp_diag", "imp_matvec", "imp_precond", "imp_ortho"]
 
 
 def exported_names():

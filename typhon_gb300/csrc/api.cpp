@@ -21,9 +21,12 @@
 
 #include "../../include/typhon_gpu.h"
 #include "devmesh.hpp"
+#include "handle.hpp"
 #include "internal.hpp"
 
 using namespace tyk;
+using tyi::cuda_fail;
+using tyi::pad32;
 
 namespace tyi {
 static thread_local std::string g_last_error;
@@ -33,17 +36,6 @@ const char* last_error() { return g_last_error.c_str(); }
 
 namespace {
 
-int cuda_fail(cudaError_t e, const char* where) {
-  tyi::set_error(std::string(where) + ": " + cudaGetErrorString(e));
-  return TY_ERR_CUDA;
-}
-#define TY_CU(call)                                            \
-  do {                                                         \
-    cudaError_t e_ = (call);                                   \
-    if (e_ != cudaSuccess) return cuda_fail(e_, #call);        \
-  } while (0)
-
-inline int pad32(int n) { return (n + 31) / 32 * 32; }
 
 struct RkTab {
   int n = 0;
@@ -101,46 +93,6 @@ void make_plans(const RkTab& t, RkStagePlan* plans) {
 }
 
 }  // namespace
-
-struct ty_mesh {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  DevMesh m;
-  DevState s;
-  SpatOpts o{};
-  bool has_params = false, has_state = false, prim_valid = false, fast_ready = false;
-  int nslot = 0;
-  std::vector<void*> allocs;
-  // host copies needed to derive mode-dependent arrays
-  std::vector<int> fc1, fc2;
-  std::vector<double> ccentre, fcentre, fnormal, fsurf, cvol;
-  std::vector<int> cf;  // [nslot][nci]
-  int lsq_gradmeth = -1, geo_highres = -1;
-  bool visc_ready = false;
-  double* dtbits_host = nullptr;  // pinned
-  Prof prof;
-  cudaStream_t own_stream = nullptr;
-
-  template <class T>
-  int alloc(T*& p, size_t n) {
-    void* q = nullptr;
-    if (n == 0) n = 1;
-    cudaError_t e = cudaMalloc(&q, n * sizeof(T));
-    if (e != cudaSuccess) { tyi::set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e)); return TY_ERR_NOMEM; }
-    allocs.push_back(q);
-    p = (T*)q;
-    return TY_OK;
-  }
-  template <class T>
-  int upload(const T*& dst, const std::vector<T>& src) {
-    T* d = nullptr;
-    int rc = alloc(d, src.size());
-    if (rc) return rc;
-    if (!src.empty()) TY_CU(cudaMemcpy(d, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
-    dst = d;
-    return TY_OK;
-  }
-};
 
 namespace {
 
@@ -300,6 +252,10 @@ int build_viscous_geometry(ty_mesh* h) {
   return TY_OK;
 }
 
+}  // namespace
+
+namespace tyi {
+
 int check_err(ty_mesh* h) {
   int e[2] = {0, 0};
   TY_CU(cudaMemcpyAsync(e, h->s.err, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -322,8 +278,6 @@ int set_dt_slot(ty_mesh* h, int slot, double v) {
   return TY_OK;
 }
 
-#define MODE_CALL(h, fn, ...) \
-  ((h)->o.mode == TY_MODE_FAST ? tyk::kfast::fn(__VA_ARGS__) : tyk::kexact::fn(__VA_ARGS__))
 
 int ensure_prim(ty_mesh* h) {
   if (h->prim_valid) return TY_OK;
@@ -354,6 +308,12 @@ int stage_faces(ty_mesh* h) {
   if (e != cudaSuccess) return cuda_fail(e, "residual faces");
   return TY_OK;
 }
+
+}  // namespace tyi
+
+using namespace tyi;
+
+namespace {
 
 int ensure_pk(ty_mesh* h, const RkStagePlan* plans, int n) {
   for (int i = 0; i < n; ++i)
@@ -535,6 +495,7 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
       (rc = h->alloc(s.stage, 5 * (size_t)nci)) ||
       (rc = h->alloc(s.err, 4)))
     return bail(rc);
+  TY_CU(cudaMemset(s.u0, 0, 5 * lc * sizeof(double)));
   TY_CU(cudaMemset(s.grad, 0, 15 * lc * sizeof(double)));
   TY_CU(cudaMemset(s.prim, 0, 5 * lc * sizeof(double)));
   TY_CU(cudaMemset(s.err, 0, 4 * sizeof(int)));
@@ -551,6 +512,7 @@ int ty_mesh_destroy(ty_mesh* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (void* p : h->allocs) cudaFree(p);
   if (h->dtbits_host) cudaFreeHost(h->dtbits_host);
+  if (h->imp.pinned) cudaFreeHost(h->imp.pinned);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return TY_OK;

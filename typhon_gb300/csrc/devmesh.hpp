@@ -101,7 +101,8 @@ struct RkStagePlan {
 // Kernel identifiers for the per-kernel timing of ty_profile_read.
 enum KernelId {
   K_PRIM = 0, K_GHOST_PRIM, K_GRAD, K_GHOST_GRAD, K_FACE_STATES, K_BARTH, K_FACE_FLUX, K_FACE_FLUX_LIM,
-  K_RK_UPDATE, K_GATHER, K_TIMESTEP, K_CELL_FAST, K_FACE_FLUX_FAST, K_NUM
+  K_RK_UPDATE, K_GATHER, K_TIMESTEP, K_CELL_FAST, K_FACE_FLUX_FAST, K_IMP_FACE, K_IMP_DIAG, K_IMP_MATVEC,
+  K_IMP_PRECOND, K_IMP_ORTHO, K_NUM
 };
 
 // Optional CUDA-event timing of every launch (host side only).

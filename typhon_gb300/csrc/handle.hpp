@@ -1,0 +1,84 @@
+// The ty_mesh handle and the helpers that the host translation units of libtyphon_gpu share.
+#pragma once
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/typhon_gpu.h"
+#include "devmesh.hpp"
+#include "implicit.hpp"
+#include "internal.hpp"
+
+namespace tyi {
+inline int cuda_fail(cudaError_t e, const char* where) {
+  set_error(std::string(where) + ": " + cudaGetErrorString(e));
+  return TY_ERR_CUDA;
+}
+inline int pad32(int n) { return (n + 31) / 32 * 32; }
+}  // namespace tyi
+
+#define TY_CU(call)                                                  \
+  do {                                                               \
+    cudaError_t e_ = (call);                                         \
+    if (e_ != cudaSuccess) return tyi::cuda_fail(e_, #call);         \
+  } while (0)
+
+#define MODE_CALL(h, fn, ...) \
+  ((h)->o.mode == TY_MODE_FAST ? tyk::kfast::fn(__VA_ARGS__) : tyk::kexact::fn(__VA_ARGS__))
+
+using tyk::DevMesh;
+using tyk::DevState;
+using tyk::Prof;
+using tyk::SpatOpts;
+
+struct ty_mesh {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DevMesh m;
+  DevState s;
+  SpatOpts o{};
+  bool has_params = false, has_state = false, prim_valid = false, fast_ready = false;
+  int nslot = 0;
+  std::vector<void*> allocs;
+  // host copies needed to derive mode-dependent arrays
+  std::vector<int> fc1, fc2;
+  std::vector<double> ccentre, fcentre, fnormal, fsurf, cvol;
+  std::vector<int> cf;  // [nslot][nci]
+  int lsq_gradmeth = -1, geo_highres = -1;
+  bool visc_ready = false;
+  double* dtbits_host = nullptr;  // pinned
+  Prof prof;
+  tyk::ImpState imp;  // implicit-step matrices and Krylov workspace (allocated on first use)
+  cudaStream_t own_stream = nullptr;
+
+  template <class T>
+  int alloc(T*& p, size_t n) {
+    void* q = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(&q, n * sizeof(T));
+    if (e != cudaSuccess) { tyi::set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e)); return TY_ERR_NOMEM; }
+    allocs.push_back(q);
+    p = (T*)q;
+    return TY_OK;
+  }
+  template <class T>
+  int upload(const T*& dst, const std::vector<T>& src) {
+    T* d = nullptr;
+    int rc = alloc(d, src.size());
+    if (rc) return rc;
+    if (!src.empty()) TY_CU(cudaMemcpy(d, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+    dst = d;
+    return TY_OK;
+  }
+};
+
+
+namespace tyi {
+// shared steps of the pipelines (api.cpp)
+int check_err(ty_mesh* h);                       // read and clear the device error word
+int set_dt_slot(ty_mesh* h, int slot, double v); // dtbits[slot] = v (stream-ordered)
+int ensure_prim(ty_mesh* h);                     // primitive variables of the resident state
+int ready(ty_mesh* h);                           // parameters and state present; device set
+int stage_faces(ty_mesh* h);                     // ghost states .. face fluxes of s.prim
+}  // namespace tyi

@@ -3,3 +3,4 @@
 #define TY_KNS kexact
 #define TY_FAST 0
 #include "kernels.cuh"
+#include "implicit.cuh"

@@ -2,3 +2,4 @@
 #define TY_KNS kfast
 #define TY_FAST 1
 #include "kernels.cuh"
+#include "implicit.cuh"

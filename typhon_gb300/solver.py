@@ -31,6 +31,8 @@ RK_METHOD = {"RK2": 1, "RK2-SSP": 2, "RK3-SSP": 3, "RK4": 4, "RK25BB": 5, "RK26B
 MODE = {"exact": 0, "fast": 1}
 DISSIPATIVE_FLUX = {"NONE": 0, "CELL-AVERAGE": 1, "FULL": 2}
 VISC_LAW = {"KINEMATIC-CONSTANT": 0, "SUTHERLAND": 1}
+KRYLOV = {"GMRES": 0, "FGMRES": 1, "JFNK": 2}
+PRECISION = {"fp64": 0, "mixed": 1}
 
 
 def prim_to_cons(prim, gamma=1.4):
@@ -173,6 +175,36 @@ class Grid:
             nstep += 1
             if end:
                 return nstep
+
+    # -- implicit step (calc_rhs.f90:121-138 with the Jacobians, implicit_solve, update_field) --
+    def implicit_step(self, cfl, inversion="GMRES", nkrylov=50, max_it=50, inv_res=1e-4, local_dt=False,
+                      precision="fp64"):
+        """One backward-Euler step on the resident state.  inversion: GMRES (Typhon's
+        bdlu_gmres), FGMRES (CGS2, block Jacobi) or JFNK; precision fp64 | mixed (FGMRES).
+        Returns the ty_imp_stats fields as a dict."""
+        p = _capi.ImpParams(KRYLOV[inversion], PRECISION[precision], int(nkrylov), int(max_it), int(local_dt), 0,
+                            float(inv_res), float(cfl))
+        st = _capi.ImpStats()
+        _capi.check(self.lib.ty_implicit_step(self.h, C.byref(p), C.byref(st)), "ty_implicit_step")
+        return dict(info=st.info, restarts=st.restarts, matvecs=st.matvecs, dt_min=st.dt_min,
+                    res_l2=np.array(st.res_l2[:]), du_l1=np.array(st.du_l1[:]), lin_res=st.lin_res)
+
+    def implicit_get(self, which):
+        """Blocks and vectors of the last implicit step (row-major 5x5 blocks)."""
+        m = self.mesh
+        code, shape = {"jacL": (0, (m.nface, 5, 5)), "jacR": (1, (m.nface, 5, 5)), "diag": (2, (m.ncell_int, 5, 5)),
+                       "upper": (3, (m.nface_int, 5, 5)), "lower": (4, (m.nface_int, 5, 5)),
+                       "dtloc": (5, (m.ncell_int,)), "rhs": (6, (m.ncell_int, 5)), "du": (7, (m.ncell_int, 5))}[which]
+        out = np.zeros(shape)
+        _capi.check(self.lib.ty_implicit_get(self.h, code, out.ctypes.data), "ty_implicit_get")
+        return out
+
+    def implicit_matvec(self, x):
+        """y = A x with the FP64 BDLU matrix of the last implicit step; x is (ncell_int, 5)."""
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        _capi.check(self.lib.ty_implicit_matvec(self.h, x.ctypes.data, y.ctypes.data), "ty_implicit_matvec")
+        return y
 
     def debug(self, which):
         m = self.mesh
