@@ -52,7 +52,13 @@ enum ty_rk {
   TY_RK2 = 1, TY_RK2SSP = 2, TY_RK3SSP = 3, TY_RK4 = 4, TY_LSRK25BB = 5, TY_LSRK26BB = 6,
   TY_LSRK12BS = 7, TY_LSRK13BS = 8
 };
-enum ty_bc { TY_BC_INTERIOR = 0, TY_BC_PERIODIC = 1, TY_BC_SYMMETRY = 2, TY_BC_WALL = 3 };
+/* TY_BC_FARFIELD (new: Typhon parses FAR-FIELD but has no Navier-Stokes implementation):
+ * the kind of each far-field face follows the free-stream normal velocity vn = u_inf.n (n
+ * outward) against the free-stream sound speed c: vn <= -c supersonic inflow (free stream),
+ * vn < 0 subsonic inflow (free-stream density and velocity, inside pressure), vn < c subsonic
+ * outflow (inside density and velocity, free-stream pressure), else supersonic outflow
+ * (inside state).  The free stream is ty_spat_params.farfield. */
+enum ty_bc { TY_BC_INTERIOR = 0, TY_BC_PERIODIC = 1, TY_BC_SYMMETRY = 2, TY_BC_WALL = 3, TY_BC_FARFIELD = 4 };
 /* Arithmetic mode of the kernels.
  *   TY_MODE_EXACT: every FP64 operation in the order Typhon evaluates it, each rounded
  *                  separately (no fused multiply-add); results match the CPU restatement
@@ -102,6 +108,7 @@ typedef struct ty_spat_params {
   double visc_kin;    /* kinematic viscosity of TY_VISC_KINEMATIC */
   double rgas;        /* gas constant (AIR: 287.14) */
   double prandtl;     /* Prandtl number (AIR: 0.72) */
+  double farfield[5]; /* free stream of TY_BC_FARFIELD faces: rho, p, u, v, w */
 } ty_spat_params;
 /* face gradient of the viscous flux (interpface_gradient_vect.f90, interpface_gradn_scal.f90) */
 enum ty_viscous { TY_VISC_NONE = 0, TY_VISC_CELLAVG = 1, TY_VISC_CELLFULL = 2 };

@@ -74,7 +74,7 @@ struct RawMesh {
 bool read_tym(const std::string& path, RawMesh& out, std::string& err);
 
 // Boundary families and how the solver treats them.
-enum BcKind { BC_PERIODIC = 1, BC_SYMMETRY = 2, BC_WALL = 3 };
+enum BcKind { BC_PERIODIC = 1, BC_SYMMETRY = 2, BC_WALL = 3, BC_FARFIELD = 4 };
 struct BcDef {
   std::string family;   // family name as in the mesh marks
   int kind = 0;
@@ -138,7 +138,20 @@ struct SpatParams {
   double visc_kin = 0.0;  // nu for KINEMATIC-CONSTANT
   double rgas = 287.14;   // AIR
   double prandtl = 0.72;
+  // far field (new: Typhon parses FAR-FIELD but has no Navier-Stokes implementation):
+  // free-stream primitive state rho, p, u, v, w
+  double farfield[5] = {1.0, 1.0 / 1.4, 0.0, 0.0, 0.0};
 };
+
+// Far-field ghost state (new).  The kind of each far-field face is fixed by the free-stream
+// normal velocity vn = u_inf . n (n outward) against the free-stream sound speed c:
+//   vn <= -c  supersonic inflow:  the free stream
+//   vn <  0   subsonic inflow:    free-stream density and velocity, pressure from inside
+//   vn <  c   subsonic outflow:   inside density and velocity, free-stream pressure
+//   else      supersonic outflow: the inside state
+// q: inside primitive state (rho, p, u, v, w); out: ghost primitive state.
+void farfield_state(double gamma, const double* qinf, V3 n, const double* q, double* out);
+bool farfield_jacobian(double gamma, const double* qinf, V3 n, const double* q, double* M);
 enum ViscMeth { VISC_NONE = 0, VISC_CELLAVG = 1, VISC_CELLFULL = 2 };
 
 struct RkTable {
@@ -183,6 +196,7 @@ struct Solver {
   void calc_rhs();               // one residual evaluation at dtloc
 
   // ---- implicit (backward Euler) step: HLL flux Jacobians, BDLU, GMRES ----
+  // ns_bocojacobian: symmetry (Typhon) and far-field (new) fold J_R dQ_ghost/dQ_inside into J_L
   bool calc_jac = false;
   std::vector<double> jacL, jacR;         // 25*nface, row-major 5x5 per face (times S after flux_to_res)
   std::vector<double> bdiag;              // 25*ncell

@@ -133,7 +133,7 @@ void ory_mesh_facevtex(void* h, int maxv, int* out) {  // nface x maxv, 1-based 
 
 // ---- solver ----
 // iparams: scheme, highres, limiter, postlim, gradmeth, rk_method, viscous, visc_law
-// dparams: gamma, cfl, roe_entropy_fix, visc_kin, rgas, prandtl
+// dparams: gamma, cfl, roe_entropy_fix, visc_kin, rgas, prandtl, far-field rho, p, u, v, w
 void* ory_solver_new(void* mesh, const int* ip, const double* dp) {
   auto* s = new Solver();
   SpatParams sp;
@@ -142,6 +142,7 @@ void* ory_solver_new(void* mesh, const int* ip, const double* dp) {
   sp.gamma = dp[0];
   sp.roe_entropy_fix = dp[2];
   sp.visc_kin = dp[3]; sp.rgas = dp[4]; sp.prandtl = dp[5];
+  for (int v = 0; v < 5; ++v) sp.farfield[v] = dp[6 + v];
   s->init(&((MeshHandle*)mesh)->m, sp, ip[5], dp[1]);
   return s;
 }

@@ -109,6 +109,41 @@ void Solver::varcons() {
 
 // calcboco_gen(bccon_cell_state): periodic copy (calcboco_connect_per_match.f90:56-78) and
 // physical ghost states (calcboco_ust.f90 -> calcboco_ust_sym / wall)
+// d(ghost conservative state)/d(inside conservative state) of the far-field kinds, row-major
+// in (rho, rhoE, rhou, rhov, rhow); u is the inside velocity.  Returns false for the
+// supersonic inflow (ghost independent of the inside state).
+bool farfield_jacobian(double gamma, const double* qinf, V3 n, const double* q, double* M) {
+  const double vn = qinf[2] * n.x + qinf[3] * n.y + qinf[4] * n.z;
+  const double c = std::sqrt(gamma * qinf[1] / qinf[0]);
+  for (int k = 0; k < 25; ++k) M[k] = 0.0;
+  if (vn <= -c) return false;
+  const double u2 = q[2] * q[2] + q[3] * q[3] + q[4] * q[4];
+  if (vn < 0.0) {            // subsonic inflow: rhoE_g = p / (gamma - 1) + const
+    M[5] = 0.5 * u2; M[6] = 1.0; M[7] = -q[2]; M[8] = -q[3]; M[9] = -q[4];
+  } else if (vn < c) {       // subsonic outflow: rho, rhou kept, rhoE_g = p_inf / (gamma - 1) + |m|^2 / (2 rho)
+    M[0] = 1.0;
+    M[5] = -0.5 * u2; M[7] = q[2]; M[8] = q[3]; M[9] = q[4];
+    M[12] = 1.0; M[18] = 1.0; M[24] = 1.0;
+  } else {                   // supersonic outflow: identity
+    for (int i = 0; i < 5; ++i) M[i * 6] = 1.0;
+  }
+  return true;
+}
+
+void farfield_state(double gamma, const double* qinf, V3 n, const double* q, double* out) {
+  const double vn = qinf[2] * n.x + qinf[3] * n.y + qinf[4] * n.z;
+  const double c = std::sqrt(gamma * qinf[1] / qinf[0]);
+  if (vn <= -c) {
+    for (int v = 0; v < 5; ++v) out[v] = qinf[v];
+  } else if (vn < 0.0) {
+    out[0] = qinf[0]; out[1] = q[1]; out[2] = qinf[2]; out[3] = qinf[3]; out[4] = qinf[4];
+  } else if (vn < c) {
+    out[0] = q[0]; out[1] = qinf[1]; out[2] = q[2]; out[3] = q[3]; out[4] = q[4];
+  } else {
+    for (int v = 0; v < 5; ++v) out[v] = q[v];
+  }
+}
+
 void Solver::boco_cell_state() {
   const int nc = m->ncell;
   for (auto& b : m->bocos) {
@@ -149,6 +184,12 @@ void Solver::boco_cell_state() {
         prim[2 * nc + g] = ug.x;
         prim[3 * nc + g] = ug.y;
         prim[4 * nc + g] = ug.z;
+      } else if (b.kind == BC_FARFIELD) {
+        int i = m->fc1[f];
+        double q[5], o[5];
+        for (int v = 0; v < 5; ++v) q[v] = prim[v * nc + i];
+        farfield_state(sp.gamma, sp.farfield, m->fnormal[f], q, o);
+        for (int v = 0; v < 5; ++v) prim[v * nc + g] = o[v];
       }
     }
   }
@@ -197,6 +238,11 @@ void Solver::boco_face_state() {
         cell_r[2 * nf + f] = ug.x;
         cell_r[3 * nf + f] = ug.y;
         cell_r[4 * nf + f] = ug.z;
+      } else if (b.kind == BC_FARFIELD) {
+        double q[5], o[5];
+        for (int v = 0; v < 5; ++v) q[v] = cell_l[v * nf + f];
+        farfield_state(sp.gamma, sp.farfield, m->fnormal[f], q, o);
+        for (int v = 0; v < 5; ++v) cell_r[v * nf + f] = o[v];
       }
     }
   }
@@ -1104,7 +1150,26 @@ void Solver::calc_rhs() {
 // J_L += J_R dQr/dQl with dQr/dQl = I - 2 n n^T on the momentum block, and J_R = 0.
 // Other boundary kinds (periodic, wall) keep their Jacobians.
 void Solver::ns_bocojacobian() {
+  const int nf = m->nface;
   for (const Boco& b : m->bocos) {
+    if (b.kind == BC_FARFIELD) {
+      for (int f : b.iface) {
+        double ql[5];
+        for (int v = 0; v < 5; ++v) ql[v] = cell_l[v * (size_t)nf + f];
+        double M[25];
+        if (!farfield_jacobian(sp.gamma, sp.farfield, m->fnormal[f], ql, M)) continue;
+        double* JL = &jacL[25 * (size_t)f];
+        double* JR = &jacR[25 * (size_t)f];
+        for (int i = 0; i < 5; ++i)
+          for (int j = 0; j < 5; ++j) {
+            double a = 0.0;
+            for (int k = 0; k < 5; ++k) a = a + JR[i * 5 + k] * M[k * 5 + j];
+            JL[i * 5 + j] = JL[i * 5 + j] + a;
+          }
+        for (int k = 0; k < 25; ++k) JR[k] = 0.0;
+      }
+      continue;
+    }
     if (b.kind != BC_SYMMETRY) continue;
     for (int f : b.iface) {
       const V3 n = m->fnormal[f];

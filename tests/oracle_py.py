@@ -13,7 +13,7 @@ ROOT = pathlib.Path(__file__).resolve().parents[1]
 LIB = ROOT / "oracle" / "build" / "liboracle.so"
 
 # enums of oracle/oracle.hpp
-BC_PERIODIC, BC_SYMMETRY, BC_WALL = 1, 2, 3
+BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD = 1, 2, 3, 4
 SCH_HLLC, SCH_RUSANOV, SCH_ROE = 1, 2, 3
 HRES_NONE, HRES_MUSCL, HRES_MUSCLFAST, HRES_MUSCLUNS = 0, 1, 2, 3
 LIM_NONE, LIM_MINMOD, LIM_ALBADA, LIM_VLEER, LIM_SBEE, LIM_KIM3, LIM_LIM03 = range(7)
@@ -141,11 +141,12 @@ class Mesh:
 class Solver:
     def __init__(self, mesh, scheme=SCH_HLLC, highres=HRES_NONE, limiter=LIM_ALBADA,
                  postlim=POSTLIM_NONE, gradmeth=GRAD_NONE, rk="RK4", gamma=1.4, cfl=1.0,
-                 entropy_fix=0.1, viscous=0, visc_law=0, visc_kin=0.0, rgas=287.14, prandtl=0.72):
+                 entropy_fix=0.1, viscous=0, visc_law=0, visc_kin=0.0, rgas=287.14, prandtl=0.72,
+                 farfield=(1.0, 1.0 / 1.4, 0.0, 0.0, 0.0)):
         self.lib = load()
         self.mesh = mesh
         ip = np.array([scheme, highres, limiter, postlim, gradmeth, RK[rk], viscous, visc_law], np.int32)
-        dp = np.array([gamma, cfl, entropy_fix, visc_kin, rgas, prandtl], np.float64)
+        dp = np.array([gamma, cfl, entropy_fix, visc_kin, rgas, prandtl, *farfield], np.float64)
         self.h = C.c_void_p(self.lib.ory_solver_new(mesh.h, _p(ip), _p(dp)))
 
     def __del__(self):

@@ -99,6 +99,21 @@ def test_preprocess_tet_box_matches_oracle(ty, n):
     assert abs(md.cell_volume[:md.ncell_int].sum() - L ** 3) < 1e-9 * L ** 3
 
 
+def test_preprocess_flatplate_prisms_tets_matches_oracle(ty):
+    """Mixed prism/tetrahedron mesh with wall, symmetry and far-field families."""
+    raw = ty.umesh.gen_flatplate(nx=12, nz=3, n_prism=4, n_tet=3)
+    bcs = ty.umesh.flatplate_bcs()
+    md = ty.preprocess(raw, 3, bcs)
+    d = op.Mesh.from_raw(raw).build(3, bcs).export()
+    assert all(_same(md, d).values()), _same(md, d)
+    assert md.ncell_int == 2 * 12 * 3 * 4 + 6 * 12 * 3 * 3
+    assert np.all(md.cell_volume[:md.ncell_int] > 0)
+    top = raw.vtex[:, 1].max()
+    assert abs(md.cell_volume[:md.ncell_int].sum() - 1.5 * 0.2 * top) < 1e-12
+    kinds = md.face_bc[md.nface_int:]
+    assert set(np.unique(kinds)) == {ty.BC_WALL, ty.BC_SYMMETRY, ty.BC_FARFIELD}
+
+
 def test_tym_roundtrip(ty, tmp_path):
     raw = ty.gen_grid2d(6, 5, 3.0, 2.0, "quad")
     p = tmp_path / "m.tym"

@@ -18,6 +18,8 @@ SYMMETRY_BOX = [(f, op.BC_SYMMETRY, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX
 MXLAY_BCS = [("IMIN", op.BC_PERIODIC, "IMAX", (1.0, 0.0, 0.0)),
              ("JMIN", op.BC_WALL, "", (0.0, 0.0, 0.0), (-1.0, 0.0, 0.0)),
              ("JMAX", op.BC_WALL, "", (0.0, 0.0, 0.0), (1.0, 0.0, 0.0))]
+FARFIELD_BOX = [(f, op.BC_FARFIELD, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX")]
+FREESTREAM = (1.0, 1.0 / 1.4, 0.5, 0.1, 0.0)   # M = 0.5 at a small angle
 OSCH = {"HLLC": op.SCH_HLLC, "RUSANOV": op.SCH_RUSANOV, "ROE": op.SCH_ROE}
 OHRES = {"NONE": op.HRES_NONE, "MUSCL": op.HRES_MUSCL, "MUSCL-FAST": op.HRES_MUSCLFAST, "MUSCL-UNS": op.HRES_MUSCLUNS}
 OLIM = {"NONE": op.LIM_NONE, "ALBADA": op.LIM_ALBADA, "MINMOD": op.LIM_MINMOD}
@@ -43,6 +45,29 @@ def vortex_at_rest(cc, strength=0.3):
                      -strength * y * np.exp(-r2 / 2), strength * x * np.exp(-r2 / 2), np.zeros(n)])
 
 
+def perturbed_stream(cc, amp=0.1):
+    """The free stream with a Gaussian bump of density, pressure and transverse velocity."""
+    x, y = cc[:, 0] - 0.5, cc[:, 1] - 0.5
+    b = amp * np.exp(-(x * x + y * y) / 0.02)
+    n = len(x)
+    return np.stack([FREESTREAM[0] * (1 + b), FREESTREAM[1] * (1 + b), np.full(n, FREESTREAM[2]),
+                     FREESTREAM[3] + b, np.zeros(n)])
+
+
+def sine_state(cc):
+    """Smooth periodic state with every variable varying and no symmetry: no neighbour
+    difference or face increment is rounding noise (where both are, Barth's ratio of the two
+    depends on the last bits, and the fast mode may limit a cell differently from the exact
+    mode)."""
+    x, y = cc[:, 0], cc[:, 1]
+    t = 2 * np.pi
+    return np.stack([1 + 0.1 * np.sin(t * x + 0.3) * np.sin(t * y + 1.1),
+                     (1 + 0.1 * np.cos(t * (x + y) + 0.2)) / 1.4,
+                     0.3 + 0.1 * np.sin(t * y + 0.5) + 0.05 * np.cos(t * x),
+                     0.2 * np.cos(t * x + 0.7) + 0.03 * np.sin(t * y + 0.1),
+                     np.zeros_like(x)])
+
+
 def case_2d(ty, golden_dir, name, bcs_gpu, bcs_or=None):
     raw = ty.read_tym(golden_dir / name)
     md = ty.preprocess(raw, 2, bcs_gpu)
@@ -54,13 +79,13 @@ def pair(ty, md, om, prim, scheme="HLLC", highres="NONE", limiter="NONE", postli
          mode="exact", viscous="NONE", kin_visc=0.0):
     g = ty.Grid(md)
     g.set_spat(scheme, highres, limiter, postlim, gradmeth=gradmeth, mode=mode, dissipative_flux=viscous,
-               kin_visc=kin_visc)
+               kin_visc=kin_visc, farfield=FREESTREAM)
     g.set_prim(prim)
     gm = gradmeth or ("NONE" if (highres == "NONE" and viscous == "NONE") else "LSQ")
     s = op.Solver(om, OSCH[scheme], OHRES[highres], OLIM[limiter], OPOST[postlim],
                   op.GRAD_NONE if gm == "NONE" else op.GRAD_LSQ, cfl=1.0,
                   viscous={"NONE": 0, "CELL-AVERAGE": op.VISC_CELLAVG, "FULL": op.VISC_CELLFULL}[viscous],
-                  visc_kin=kin_visc)
+                  visc_kin=kin_visc, farfield=FREESTREAM)
     s.set_prim(prim)
     return g, s
 
@@ -88,11 +113,14 @@ CASES = [
     ("quad20x20.tym", "periodic", "HLLC", "MUSCL-FAST", "ALBADA", "NONE", "NONE", False),
     ("mxlay2x20quad-h50.tym", "mxlay", "HLLC", "MUSCL", "ALBADA", "NONE", "CELL-AVERAGE", True),
     ("mxlay2x20quad-h50.tym", "mxlay", "RUSANOV", "NONE", "NONE", "NONE", "FULL", False),
+    ("quad20x20.tym", "farfield", "HLLC", "MUSCL", "ALBADA", "NONE", "NONE", True),
+    ("quad20x20.tym", "farfield", "ROE", "NONE", "NONE", "NONE", "NONE", False),
 ]
 
 
 def _bcs(kind):
-    return {"periodic": op.PERIODIC_UNIT_SQUARE, "symmetry": SYMMETRY_BOX, "mxlay": MXLAY_BCS}[kind]
+    return {"periodic": op.PERIODIC_UNIT_SQUARE, "symmetry": SYMMETRY_BOX, "mxlay": MXLAY_BCS,
+            "farfield": FARFIELD_BOX}[kind]
 
 
 def _prim(md, kind):
@@ -102,6 +130,8 @@ def _prim(md, kind):
         n = md.ncell
         return np.stack([np.ones(n), np.full(n, 100 / 1.4), erf(y / 2), np.zeros(n), np.zeros(n)])
     cc = md.cell_centre
+    if kind == "farfield":
+        return perturbed_stream(cc)
     if kind == "symmetry":
         cc = cc / np.array([2.0, 1.0, 1.0])
     return vortex_at_rest(cc)
@@ -132,39 +162,80 @@ def test_exact_assembly_and_gmres(ty, golden_dir, name, bck, scheme, highres, li
     assert np.allclose(st["du_l1"], l1, rtol=1e-9, atol=0)
 
 
-@pytest.mark.parametrize("inversion,precision,tol", [("FGMRES", "fp64", 1e-8), ("FGMRES", "mixed", 2e-5)])
-def test_fgmres_reaches_the_oracle_solution(ty, golden_dir, inversion, precision, tol):
+@pytest.mark.parametrize("scheme,highres,limiter,postlim", [("ROE", "MUSCL-UNS", "NONE", "BARTH"),
+                                                            ("HLLC", "MUSCL", "ALBADA", "NONE"),
+                                                            ("RUSANOV", "NONE", "NONE", "NONE")])
+def test_fast_assembly_close(ty, golden_dir, scheme, highres, limiter, postlim):
+    """Fast-mode Jacobians, blocks, time steps and right-hand side within rounding of the oracle."""
     md, om = case_2d(ty, golden_dir, "quad20x20.tym", op.PERIODIC_UNIT_SQUARE)
-    prim = vortex_at_rest(md.cell_centre)
-    g, s = pair(ty, md, om, prim, "ROE", "MUSCL-UNS", "NONE", "BARTH", mode="fast")
+    prim = sine_state(md.cell_centre)
+    g, s = pair(ty, md, om, prim, scheme, highres, limiter, postlim, mode="fast")
+    g.implicit_step(50.0, "FGMRES", nkrylov=30, max_it=1, inv_res=1e-3, local_dt=True)
+    s.implicit_step(50.0, local_dt=True, nkrylov=30, max_it=1, inv_res=1e-3)
+    nci, nfi = md.ncell_int, md.nface_int
+    errs = {
+        "jacL": relerr(g.implicit_get("jacL"), s.get_implicit("jacL")),
+        "jacR": relerr(g.implicit_get("jacR"), s.get_implicit("jacR")),
+        "diag": relerr(g.implicit_get("diag"), s.get_implicit("diag")[:nci]),
+        "upper": relerr(g.implicit_get("upper"), s.get_implicit("upper")[:nfi]),
+        "lower": relerr(g.implicit_get("lower"), s.get_implicit("lower")[:nfi]),
+        "dtloc": relerr(g.implicit_get("dtloc"), s.get("dtloc")[0, :nci]),
+        "rhs": relerr(g.implicit_get("rhs"), s.implicit_rhs()[:nci]),
+    }
+    assert all(e < 1e-11 for e in errs.values()), errs
+
+
+def _dense(s, nc):
+    cols = []
+    for j in range(5 * nc):
+        e = np.zeros(5 * nc)
+        e[j] = 1.0
+        cols.append(s.bdlu_matvec(e.reshape(nc, 5)).ravel())
+    return np.array(cols).T
+
+
+@pytest.mark.parametrize("inversion,precision,mode,tol", [("FGMRES", "fp64", "exact", 1e-9),
+                                                          ("FGMRES", "fp64", "fast", 1e-9),
+                                                          ("FGMRES", "mixed", "fast", 1e-5),
+                                                          ("GMRES", "fp64", "fast", 1e-9)])
+def test_krylov_solution_against_dense_solve(ty, golden_dir, inversion, precision, mode, tol):
+    """The update of one implicit step against a dense solve of the oracle's BDLU system."""
+    md, om = case_2d(ty, golden_dir, "quad20x20.tym", op.PERIODIC_UNIT_SQUARE)
+    prim = sine_state(md.cell_centre)
+    g, s = pair(ty, md, om, prim, "ROE", "MUSCL-UNS", "NONE", "BARTH", mode=mode)
     U0 = g.get_cons()
-    st = g.implicit_step(50.0, inversion, nkrylov=30, max_it=10, inv_res=1e-11 if precision == "fp64" else 1e-7,
-                         local_dt=True, precision=precision)
-    s.implicit_step(50.0, local_dt=True, nkrylov=60, max_it=40, inv_res=1e-13)
+    tight = 1e-12 if precision == "fp64" else 1e-7
+    st = g.implicit_step(50.0, inversion, nkrylov=30, max_it=40, inv_res=tight, local_dt=True, precision=precision)
+    s.implicit_step(50.0, local_dt=True, nkrylov=30, max_it=1, inv_res=1e-3)
+    A = _dense(s, md.ncell)
+    b = s.implicit_rhs()
+    xs = np.linalg.solve(A, b.ravel()).reshape(md.ncell, 5)[:md.ncell_int].T
     du = g.get_cons() - U0
-    du_o = s.get("cons")[:, :md.ncell_int] - U0
-    assert relerr(du, du_o) < tol, (relerr(du, du_o), st)
-    assert st["matvecs"] < 200
+    assert relerr(du, xs) < tol, (relerr(du, xs), st)
 
 
-@pytest.mark.parametrize("inversion,precision", [("GMRES", "fp64"), ("FGMRES", "fp64"), ("FGMRES", "mixed"),
-                                                 ("JFNK", "fp64")])
-def test_steady_convergence(ty, golden_dir, inversion, precision):
-    """Implicit steps with a growing CFL drive a vortex at rest to its discrete steady state."""
-    md, om = case_2d(ty, golden_dir, "quad20x20.tym", op.PERIODIC_UNIT_SQUARE)
+@pytest.mark.parametrize("inversion,precision,scheme,highres,steps",
+                         [("GMRES", "fp64", "RUSANOV", "NONE", 20), ("FGMRES", "fp64", "RUSANOV", "NONE", 20),
+                          ("FGMRES", "mixed", "RUSANOV", "NONE", 25), ("JFNK", "fp64", "RUSANOV", "NONE", 20),
+                          ("JFNK", "fp64", "HLLC", "MUSCL", 30)])
+def test_steady_convergence(ty, golden_dir, inversion, precision, scheme, highres, steps):
+    """Implicit steps with a growing CFL drive a perturbed free stream through far-field
+    boundaries to the uniform steady state: Newton-fast when the operator is the residual's
+    Jacobian (Rusanov with its own Jacobian; Jacobian-free products for a second-order HLLC)."""
+    md, _ = case_2d(ty, golden_dir, "quad20x20.tym", FARFIELD_BOX)
     g = ty.Grid(md)
-    g.set_spat("HLLC", "MUSCL", "ALBADA", mode="fast")
-    g.set_prim(vortex_at_rest(md.cell_centre))
+    g.set_spat(scheme, highres, "NONE", mode="fast", farfield=FREESTREAM)
+    g.set_prim(perturbed_stream(md.cell_centre))
     hist = []
     cfl = 10.0
-    for it in range(40):
-        st = g.implicit_step(cfl, inversion, nkrylov=30 if inversion != "GMRES" else 50, max_it=5,
-                             inv_res=1e-3, local_dt=True, precision=precision)
+    for it in range(steps):
+        st = g.implicit_step(cfl, inversion, nkrylov=30, max_it=10, inv_res=1e-6, local_dt=True, precision=precision)
         hist.append(np.linalg.norm(st["res_l2"]))
-        cfl = min(cfl * 1.5, 1e4)
+        cfl = min(cfl * 2.0, 1e6)
         if hist[-1] < 1e-10 * hist[0]:
             break
-    assert hist[-1] < 1e-6 * hist[0], hist
+    assert hist[-1] < 1e-10 * hist[0], hist
+    assert np.allclose(g.get_prim(), np.array(FREESTREAM)[:, None], rtol=0, atol=1e-8)
 
 
 def test_implicit_errors(ty, golden_dir):
@@ -180,5 +251,5 @@ def test_implicit_errors(ty, golden_dir):
         g.implicit_step(1.0, "FGMRES", nkrylov=40)
     with pytest.raises(ty.TyphonError):            # nothing assembled in FP64 yet
         g.implicit_matvec(np.zeros((md.ncell_int, 5)))
-    st = g.implicit_step(1.0, "FGMRES", precision="mixed")
+    st = g.implicit_step(1.0, "FGMRES", nkrylov=30, precision="mixed")
     assert st["lin_res"] <= 1e-4

@@ -135,3 +135,58 @@ def test_implicit_steps_converge_vortex_at_rest(golden_dir, oracle):
         assert info >= 0
         hist.append(l1.sum())
     assert hist[-1] < 0.05 * hist[0], hist
+
+
+FARFIELD_BOX = [(f, op.BC_FARFIELD, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX")]
+
+
+def test_farfield_states():
+    """The four far-field kinds of the free-stream normal velocity."""
+    g = 1.4
+    qinf = np.array([1.0, 1.0 / g, 0.5, 0.0, 0.0])      # c = 1, M = 0.5 along x
+    q = np.array([2.0, 3.0, 0.1, 0.2, 0.3])
+    cases = {(-1.0, 0.0): [1.0, 3.0, 0.5, 0.0, 0.0],     # subsonic inflow: inside pressure
+             (1.0, 0.0): [2.0, 1.0 / g, 0.1, 0.2, 0.3],  # subsonic outflow: free-stream pressure
+             (0.0, 1.0): [2.0, 1.0 / g, 0.1, 0.2, 0.3],  # vn = 0 counts as outflow
+             (0.0, -1.0): [2.0, 1.0 / g, 0.1, 0.2, 0.3]}
+    m = op.Mesh.from_tym(__import__("pathlib").Path(__file__).parent / "golden" / "quad10x10.tym").build(
+        2, FARFIELD_BOX)
+    ex = m.export()
+    s = op.Solver(m, op.SCH_RUSANOV, cfl=1.0, farfield=tuple(qinf))
+    prim = np.tile(q[:, None], (1, m.ncell))
+    s.set_prim(prim)
+    s.rhs(1e-3)
+    right = s.get("cell_r")                  # face-state mode: the ghost state of each boundary face
+    for f in range(m.nface_int, m.nface):
+        n = tuple(np.round(ex["fnormal"][f, :2], 12) + 0.0)
+        assert n in cases
+        assert np.allclose(right[:, f], cases[n], rtol=0, atol=1e-15), (n, right[:, f])
+    sup = op.Solver(m, op.SCH_RUSANOV, cfl=1.0, farfield=(1.0, 1.0 / g, 3.0, 0.0, 0.0))   # M = 3
+    sup.set_prim(prim)
+    sup.rhs(1e-3)
+    rs = sup.get("cell_r")
+    for f in range(m.nface_int, m.nface):
+        nx = ex["fnormal"][f, 0]
+        want = [1.0, 1.0 / g, 3.0, 0.0, 0.0] if nx < -0.5 else (q if nx > 0.5 else [2.0, 1.0 / g, 0.1, 0.2, 0.3])
+        assert np.allclose(rs[:, f], want, rtol=0, atol=1e-15)
+
+
+def test_farfield_newton_convergence(golden_dir, oracle):
+    """Rusanov with its own Jacobian through far-field boundaries: the implicit step is a
+    Newton step as the CFL grows, and a perturbed free stream converges to machine zero."""
+    m = _mesh(golden_dir, "quad20x20.tym", FARFIELD_BOX)
+    ex = m.export()
+    x, y = ex["ccentre"][:, 0] - 0.5, ex["ccentre"][:, 1] - 0.5
+    b = 0.1 * np.exp(-(x * x + y * y) / 0.02)
+    n = m.ncell
+    qinf = (1.0, 1.0 / 1.4, 0.5, 0.1, 0.0)
+    prim = np.stack([1 + b, (1 + b) / 1.4, np.full(n, 0.5), 0.1 + b, np.zeros(n)])
+    s = op.Solver(m, op.SCH_RUSANOV, cfl=1.0, farfield=qinf)
+    s.set_prim(prim)
+    cfl, hist = 10.0, []
+    for _ in range(16):
+        info, _, l1 = s.implicit_step(cfl, local_dt=True, nkrylov=50, max_it=10, inv_res=1e-8)
+        hist.append(l1.sum())
+        cfl = min(2 * cfl, 1e6)
+    assert hist[-1] < 1e-11 * hist[0], hist
+    assert np.allclose(s.get("prim")[:, :m.ncell_int], np.array(qinf)[:, None], atol=1e-10)

@@ -42,7 +42,7 @@ class SpatParams(C.Structure):
         ("postlim", C.c_int32), ("gradmeth", C.c_int32), ("mode", C.c_int32),
         ("gamma", C.c_double), ("entropy_fix", C.c_double),
         ("viscous", C.c_int32), ("visc_law", C.c_int32), ("visc_kin", C.c_double), ("rgas", C.c_double),
-        ("prandtl", C.c_double),
+        ("prandtl", C.c_double), ("farfield", C.c_double * 5),
     ]
 
 

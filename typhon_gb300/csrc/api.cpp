@@ -409,7 +409,7 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
         int p = d->face_partner[f] - 1;
         if (p < nfi || p >= nf || d->face_partner[p] - 1 != f) { tyi::set_error("bad periodic partner"); return bail(TY_ERR_MESH); }
         part[f] = p;
-      } else if (fbc[f] != TY_BC_SYMMETRY && fbc[f] != TY_BC_WALL) {
+      } else if (fbc[f] != TY_BC_SYMMETRY && fbc[f] != TY_BC_WALL && fbc[f] != TY_BC_FARFIELD) {
         tyi::set_error("unknown boundary kind");
         return bail(TY_ERR_UNSUPPORTED);
       }
@@ -564,6 +564,7 @@ int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
   h->o.inv_entropy_fix = p->entropy_fix > 0.0 ? 1.0 / p->entropy_fix : 0.0;
   h->o.viscous = p->viscous; h->o.visc_law = p->visc_law; h->o.visc_kin = p->visc_kin;
   h->o.rgas = p->rgas; h->o.prandtl = p->prandtl;
+  for (int v = 0; v < 5; ++v) h->o.farfield[v] = p->farfield[v];
   h->has_params = true;
   h->prim_valid = false;
   return TY_OK;

@@ -78,6 +78,7 @@ struct SpatOpts {
   double inv_entropy_fix;  // 1 / entropy_fix (fast-mode Roe flux)
   int viscous, visc_law;
   double visc_kin, rgas, prandtl;
+  double farfield[5];  // free stream of far-field faces (rho, p, u, v, w)
 };
 
 // One Runge-Kutta update applied at the end of a stage: partial sum of the state of stage

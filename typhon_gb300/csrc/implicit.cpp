@@ -415,6 +415,8 @@ int ty_implicit_step(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
   IMP_CU(IMP_CALL(h, imp_res_norms, m, im, a, im.b, im.part, im.scal + kScalMisc + 2, s));
   IMP_CU(cudaMemcpyAsync(&st->dt_min, S.dtbits, sizeof(double), cudaMemcpyDeviceToHost, s));
   if ((rc = fetch(h, kScalMisc + 2, 5))) return rc;
+  im.last_local = a.local_dt;
+  im.last_dt = st->dt_min;
   for (int v = 0; v < 5; ++v) st->res_l2[v] = std::sqrt(im.pinned[kScalMisc + 2 + v]);
   // 3. solve
   if (p->krylov == TY_KRYLOV_GMRES) {
@@ -460,7 +462,10 @@ int ty_implicit_get(ty_mesh* h, int32_t which, double* out) {
     case 2: return blocks(im.diag, m.nci);
     case 3: return blocks(im.upper, m.nfi);
     case 4: return blocks(im.lower, m.nfi);
-    case 5: IMP_CU(cudaMemcpy(out, im.dtloc, m.nci * sizeof(double), cudaMemcpyDeviceToHost)); return TY_OK;
+    case 5:
+      if (im.last_local) IMP_CU(cudaMemcpy(out, im.dtloc, m.nci * sizeof(double), cudaMemcpyDeviceToHost));
+      else std::fill(out, out + m.nci, im.last_dt);
+      return TY_OK;
     case 6: IMP_CU(cudaMemcpy(out, im.b, 5 * (size_t)m.nci * sizeof(double), cudaMemcpyDeviceToHost)); return TY_OK;
     case 7: IMP_CU(cudaMemcpy(out, im.x, 5 * (size_t)m.nci * sizeof(double), cudaMemcpyDeviceToHost)); return TY_OK;
     default: return TY_ERR_ARG;

@@ -4,7 +4,8 @@
 // restatement bit for bit:
 //   flux Jacobians       calc_jacflux.f90:49-77, calc_jac_hll.f90:46-57 (HLLC, Roe),
 //                        calc_jac_rusanov.f90 (Rusanov), viscous diagonal
-//                        calc_flux_viscous_cell.f90:149-158, symmetry ns_bocojacobian.f90:47-85,
+//                        calc_flux_viscous_cell.f90:149-158, symmetry ns_bocojacobian.f90:47-85
+//                        (and, new, the far-field ghost dependence folded in the same way),
 //                        surface scaling flux_to_res.f90:74-80
 //   BDLU blocks          build_implicit_bdlu.f90:44-83 (diagonal contributions of a cell
 //                        summed in ascending face order, as the face loop there does)
@@ -102,6 +103,29 @@ __device__ void face_jacobians(const SpatOpts& o, const double* L, const double*
   for (int k = 0; k < 25; ++k) { JL[k] = cl * JL[k]; JR[k] = cr * JR[k]; }
 }
 
+// d(ghost conservative state)/d(inside conservative state) of a far-field face (new), rows
+// and columns (rho, rhoE, rhou, rhov, rhow); false when the ghost does not depend on the inside
+__device__ bool farfield_jacobian(const SpatOpts& o, double nx, double ny, double nz, const double* q, double* M) {
+  const double* qi = o.farfield;
+  const double vn = qi[2] * nx + qi[3] * ny + qi[4] * nz;
+  const double c = sqrt(o.gamma * qi[1] / qi[0]);
+#pragma unroll
+  for (int k = 0; k < 25; ++k) M[k] = 0.0;
+  if (vn <= -c) return false;
+  const double u2 = q[2] * q[2] + q[3] * q[3] + q[4] * q[4];
+  if (vn < 0.0) {
+    M[5] = 0.5 * u2; M[6] = 1.0; M[7] = -q[2]; M[8] = -q[3]; M[9] = -q[4];
+  } else if (vn < c) {
+    M[0] = 1.0;
+    M[5] = -0.5 * u2; M[7] = q[2]; M[8] = q[3]; M[9] = q[4];
+    M[12] = 1.0; M[18] = 1.0; M[24] = 1.0;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) M[i * 6] = 1.0;
+  }
+  return true;
+}
+
 // face states exactly as the flux kernels of the residual build them
 __device__ void implicit_face_states(const DevMesh& m, const DevState& s, const SpatOpts& o, int src, int f,
                                      double* QL, double* QR) {
@@ -130,6 +154,8 @@ __device__ void implicit_face_states(const DevMesh& m, const DevState& s, const 
     side_state(m.part[f], 0, QR);
   } else if (kind == TY_BC_WALL) {
     wall_state(m, f, QL, QR);
+  } else if (kind == TY_BC_FARFIELD) {
+    farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);
   } else if (kind == TY_BC_SYMMETRY) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = QL[v];
@@ -230,9 +256,11 @@ __global__ void __launch_bounds__(128) k_imp_face(DevMesh m, DevState s, SpatOpt
       JL[i * 6] = JL[i * 6] + id;
     }
   }
-  if (f >= m.nfi && m.fbc[f] == TY_BC_SYMMETRY) {
+  const int bkind = f >= m.nfi ? m.fbc[f] : TY_BC_INTERIOR;
+  bool fold = false;
+  double M[25];
+  if (bkind == TY_BC_SYMMETRY) {
     const double nn[3] = {nx, ny, nz};
-    double M[25];
 #pragma unroll
     for (int k = 0; k < 25; ++k) M[k] = 0.0;
 #pragma unroll
@@ -241,6 +269,11 @@ __global__ void __launch_bounds__(128) k_imp_face(DevMesh m, DevState s, SpatOpt
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) M[(2 + i) * 5 + 2 + j] = M[(2 + i) * 5 + 2 + j] - 2.0 * (nn[i] * nn[j]);
+    fold = true;
+  } else if (bkind == TY_BC_FARFIELD) {
+    fold = farfield_jacobian(o, nx, ny, nz, QL, M);
+  }
+  if (fold) {
 #pragma unroll
     for (int i = 0; i < 5; ++i)
 #pragma unroll

@@ -55,6 +55,8 @@ struct ImpState {
   double* upert = nullptr;    // [5][ldc] perturbed state (Jacobian-free products)
   double* r0 = nullptr;       // [5 nci] residual at the unperturbed state (Jacobian-free)
   double* pinned = nullptr;   // host mirror of scal (pinned)
+  int last_local = 1;         // time step of the last step: per cell, or last_dt everywhere
+  double last_dt = 0.0;
 };
 
 // Arguments of the assembly kernels.

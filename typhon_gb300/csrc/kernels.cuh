@@ -143,6 +143,25 @@ __device__ __forceinline__ double viscosity(const SpatOpts& o, double rho, doubl
   return mu0 * pow(T / T0, 1.5) * (T0 + S) / (T + S);
 }
 
+// far-field ghost state (new), kind fixed by the free-stream normal velocity (see ty_bc)
+__device__ __forceinline__ void farfield_state(const SpatOpts& o, double nx, double ny, double nz, const double* q,
+                                               double* out) {
+  const double* qi = o.farfield;
+  const double vn = qi[2] * nx + qi[3] * ny + qi[4] * nz;
+  const double c = sqrt(o.gamma * qi[1] / qi[0]);
+  if (vn <= -c) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) out[v] = qi[v];
+  } else if (vn < 0.0) {
+    out[0] = qi[0]; out[1] = q[1]; out[2] = qi[2]; out[3] = qi[3]; out[4] = qi[4];
+  } else if (vn < c) {
+    out[0] = q[0]; out[1] = qi[1]; out[2] = q[2]; out[3] = q[3]; out[4] = q[4];
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) out[v] = q[v];
+  }
+}
+
 // ghost states: periodic copy, symmetry mirror (velocity reflected across the face),
 // adiabatic moving wall (setboco_ns_flux.f90, cell-state mode: pressure copied, temperature
 // of the cell minus lflux d / conduct with lflux = 0, velocity reflected about the wall's)
@@ -153,6 +172,15 @@ __global__ void k_ghost_prim(DevMesh m, double* __restrict__ prim, SpatOpts o) {
   const size_t ld = m.ldc;
   const int kind = m.fbc[f];
   double vx = prim[2 * ld + src], vy = prim[3 * ld + src], vz = prim[4 * ld + src];
+  if (kind == TY_BC_FARFIELD) {
+    double q[5], out[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) q[v] = prim[v * ld + src];
+    farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), q, out);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) prim[v * ld + g] = out[v];
+    return;
+  }
   if (kind == TY_BC_WALL) {
     const double r = o.rgas, lflux = 0.0;
     const double rho = prim[src], p = prim[ld + src];
@@ -717,6 +745,8 @@ __global__ void __launch_bounds__(kBlock) k_face_flux(DevMesh m, DevState s, Spa
     recon(m, s, o, m.part[f], 0, QR);  // cell_r(face) = cell_l(partner face)
   } else if (kind == TY_BC_WALL) {
     wall_state(m, f, QL, QR);
+  } else if (kind == TY_BC_FARFIELD) {
+    farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);
   } else if (kind == TY_BC_SYMMETRY) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = QL[v];
@@ -793,6 +823,8 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_lim(DevMesh m, DevState s,
     limited(m.part[f], 0, QR);
   } else if (kind == TY_BC_WALL) {
     wall_state(m, f, QL, QR);
+  } else if (kind == TY_BC_FARFIELD) {
+    farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);
   } else if (kind == TY_BC_SYMMETRY) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = QL[v];
@@ -947,6 +979,8 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_fast(DevMesh m, DevState s
     for (int v = 0; v < 5; ++v) QR[v] = s.cl[v * lf + p];
   } else if (kind == TY_BC_WALL) {
     wall_state(m, f, QL, QR);
+  } else if (kind == TY_BC_FARFIELD) {
+    farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);
   } else if (kind == TY_BC_SYMMETRY) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = QL[v];

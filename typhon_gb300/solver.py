@@ -76,17 +76,19 @@ class Grid:
     # -- def_spat --------------------------------------------------------------------------
     def set_spat(self, scheme="HLLC", highres="NONE", limiter="ALBADA", postlim="NONE", gradmeth=None,
                  mode="exact", gamma=1.4, entropy_fix=0.1, dissipative_flux="NONE", viscosity="KINEMATIC-CONSTANT",
-                 kin_visc=0.0, rgas=287.14, prandtl=0.72):
+                 kin_visc=0.0, rgas=287.14, prandtl=0.72, farfield=(1.0, 1.0 / 1.4, 0.0, 0.0, 0.0)):
         """SPAT_PARAM: SCHEME, HIGHRES, LIMITER, POST-LIMITER, GRADMETH (LSQ by default with
         MUSCL or a viscous flux, none otherwise, as get_gradientmethod in
         SOURCE/PARAM/MENU_NUM.f90); DISSIPATIVE_FLUX (CELL-AVERAGE | FULL) turns on the laminar
-        viscous flux with MODEL: VISCOSITY (KINEMATIC-CONSTANT with KIN_VISC, or SUTHERLAND)."""
+        viscous flux with MODEL: VISCOSITY (KINEMATIC-CONSTANT with KIN_VISC, or SUTHERLAND).
+        farfield: free-stream primitive state (rho, p, u, v, w) of far-field boundaries."""
         visc = DISSIPATIVE_FLUX[dissipative_flux]
         if gradmeth is None:
             gradmeth = "NONE" if (highres == "NONE" and visc == 0) else "LSQ"
         p = _capi.SpatParams(SCHEME[scheme], HIGHRES[highres], LIMITER[limiter], POSTLIM[postlim],
                              GRADMETH[gradmeth], MODE[mode], float(gamma), float(entropy_fix), visc,
-                             VISC_LAW[viscosity], float(kin_visc), float(rgas), float(prandtl))
+                             VISC_LAW[viscosity], float(kin_visc), float(rgas), float(prandtl),
+                             (C.c_double * 5)(*map(float, farfield)))
         _capi.check(self.lib.ty_set_params(self.h, C.byref(p)), "ty_set_params")
         self.gamma = gamma
 

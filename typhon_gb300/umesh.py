@@ -25,7 +25,7 @@ ELEM_BAR2, ELEM_TRI3, ELEM_QUAD4, ELEM_TETRA4, ELEM_PENTA6, ELEM_HEXA8 = 2, 13, 
 NVTEX = {ELEM_BAR2: 2, ELEM_TRI3: 3, ELEM_QUAD4: 4, ELEM_TETRA4: 4, ELEM_PENTA6: 6, ELEM_HEXA8: 8}
 DIM = {ELEM_BAR2: 1, ELEM_TRI3: 2, ELEM_QUAD4: 2, ELEM_TETRA4: 3, ELEM_PENTA6: 3, ELEM_HEXA8: 3}
 
-BC_PERIODIC, BC_SYMMETRY, BC_WALL = 1, 2, 3
+BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD = 1, 2, 3, 4
 
 
 @dataclass
@@ -290,6 +290,112 @@ def gen_tet_box(n, length, jitter=0.0, seed=1234):
     secs = [(ELEM_TETRA4, np.arange(1, len(conn) + 1, dtype=np.int32), conn),
             (ELEM_TRI3, np.arange(1, len(fconn) + 1, dtype=np.int32), fconn)]
     return RawMesh(vtex=vt, sections=secs, marks=marks)
+
+
+def gen_flatplate(nx=200, nz=20, n_prism=50, n_tet=25, x0=-0.5, x1=1.0, width=0.2, y1=1.74e-3, growth=1.1):
+    """Flat-plate box: prisms stretched to the plate, tetrahedra above.
+
+    The (x, z) plane [x0, x1] x [0, width] carries nx x nz quadrilaterals, each split along
+    its (i, k)-(i+1, k+1) diagonal into two triangles.  The triangles are extruded in y into
+    n_prism layers of prisms (PENTA6), the first layer y1 thick, each layer `growth` times the
+    previous one.  Above, n_tet layers of hexahedra as thick as the last prism layer are split
+    into 6 tetrahedra each (the Kuhn split along the (0,0,0)-(1,1,1) diagonal, which cuts
+    every hexahedron face along its lowest-to-highest-corner diagonal, so the tetrahedra
+    conform with each other and with the prisms' top triangles).  Cells: 2 nx nz n_prism
+    prisms + 6 nx nz n_tet tetrahedra.
+
+    Boundary marks: WALL (y = 0, x >= 0), UPSTREAM (y = 0, x < 0), INLET (x = x0),
+    OUTLET (x = x1), TOP (y = top), SIDE0 / SIDE1 (z = 0 / width)."""
+    yp = y1 * (growth ** np.arange(n_prism + 1) - 1.0) / (growth - 1.0)
+    dyl = yp[-1] - yp[-2]
+    y = np.concatenate([yp, yp[-1] + dyl * np.arange(1, n_tet + 1)])
+    ny = len(y) - 1
+    xs = np.linspace(x0, x1, nx + 1)
+    zs = np.linspace(0.0, width, nz + 1)
+    X, Y, Z = np.meshgrid(xs, y, zs, indexing="ij")
+    vt = np.stack([X, Y, Z], axis=-1).reshape(-1, 3).astype(np.float64)
+
+    def vid(i, j, k):
+        return (i * (ny + 1) + j) * (nz + 1) + k + 1
+
+    # prisms: triangles (i,k)(i+1,k)(i+1,k+1) and (i,k)(i+1,k+1)(i,k+1), layer j -> j+1
+    I, J, K = np.meshgrid(np.arange(nx), np.arange(n_prism), np.arange(nz), indexing="ij")
+    I, J, K = I.reshape(-1), J.reshape(-1), K.reshape(-1)
+    tri = [((0, 0), (1, 0), (1, 1)), ((0, 0), (1, 1), (0, 1))]
+    prisms = []
+    for t in tri:
+        bot = [vid(I + a, J, K + b) for a, b in t]
+        top = [vid(I + a, J + 1, K + b) for a, b in t]
+        prisms.append(np.stack(bot + top, axis=1))
+    prisms = np.stack(prisms, axis=1).reshape(-1, 6).astype(np.int32)
+    # tetrahedra: Kuhn split of hexahedra j = n_prism .. ny-1
+    I, J, K = np.meshgrid(np.arange(nx), np.arange(n_prism, ny), np.arange(nz), indexing="ij")
+    I, J, K = I.reshape(-1), J.reshape(-1), K.reshape(-1)
+    tets = []
+    axes = {"x": (1, 0, 0), "y": (0, 1, 0), "z": (0, 0, 1)}
+    for perm in ("xyz", "xzy", "yxz", "yzx", "zxy", "zyx"):
+        p0 = np.zeros(3, int)
+        path = [p0.copy()]
+        for a in perm[:2]:
+            p0 = p0 + np.array(axes[a])
+            path.append(p0.copy())
+        path.append(np.array((1, 1, 1)))
+        tets.append(np.stack([vid(I + d[0], J + d[1], K + d[2]) for d in path], axis=1))
+    tets = np.stack(tets, axis=1).reshape(-1, 4).astype(np.int32)
+    # positive orientation for every tetrahedron
+    a, b, c, d = (vt[tets[:, q] - 1] for q in range(4))
+    neg = np.einsum("ij,ij->i", np.cross(b - a, c - a), d - a) < 0
+    tets[neg, 1], tets[neg, 2] = tets[neg, 2].copy(), tets[neg, 1].copy()
+    # boundary faces: faces seen once
+    ptri = np.concatenate([prisms[:, [0, 1, 2]], prisms[:, [3, 4, 5]]])
+    pquad = np.concatenate([prisms[:, [0, 2, 5, 3]], prisms[:, [0, 1, 4, 3]], prisms[:, [1, 2, 5, 4]]])
+    ttri = np.concatenate([tets[:, [0, 2, 1]], tets[:, [0, 1, 3]], tets[:, [1, 2, 3]], tets[:, [2, 0, 3]]])
+    alltri = np.concatenate([ptri, ttri])
+
+    def once(f):
+        key = np.sort(f, axis=1)
+        _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+        return f[cnt[inv.reshape(-1)] == 1]
+
+    btri, bquad = once(alltri), once(pquad)
+    top = y[-1]
+    tol = 1e-9
+
+    def classify(f):
+        c = vt[f - 1].mean(axis=1)
+        lab = np.full(len(f), "", dtype=object)
+        lab[np.abs(c[:, 2]) < tol] = "SIDE0"
+        lab[np.abs(c[:, 2] - width) < tol] = "SIDE1"
+        lab[np.abs(c[:, 0] - x0) < tol] = "INLET"
+        lab[np.abs(c[:, 0] - x1) < tol] = "OUTLET"
+        lab[np.abs(c[:, 1] - top) < tol] = "TOP"
+        lab[(np.abs(c[:, 1]) < tol) & (c[:, 0] >= 0.0)] = "WALL"
+        lab[(np.abs(c[:, 1]) < tol) & (c[:, 0] < 0.0)] = "UPSTREAM"
+        assert (lab != "").all()
+        return lab
+
+    lt, lq = classify(btri), classify(bquad)
+    nt = len(btri)
+    marks = []
+    for name in ("WALL", "UPSTREAM", "INLET", "OUTLET", "TOP", "SIDE0", "SIDE1"):
+        ids = np.concatenate([np.nonzero(lt == name)[0] + 1, nt + np.nonzero(lq == name)[0] + 1]).astype(np.int32)
+        marks.append((name, ids))
+    ncp = len(prisms)
+    secs = [(ELEM_PENTA6, np.arange(1, ncp + 1, dtype=np.int32), prisms),
+            (ELEM_TETRA4, np.arange(ncp + 1, ncp + len(tets) + 1, dtype=np.int32), tets),
+            (ELEM_TRI3, np.arange(1, nt + 1, dtype=np.int32), btri.astype(np.int32)),
+            (ELEM_QUAD4, np.arange(nt + 1, nt + len(bquad) + 1, dtype=np.int32), bquad.astype(np.int32))]
+    return RawMesh(vtex=vt, sections=secs, marks=marks)
+
+
+def flatplate_bcs(wall_velocity=(0.0, 0.0, 0.0)):
+    """Adiabatic no-slip plate, symmetry upstream of it and on the span sides, far field
+    at the inlet, outlet and top."""
+    return [("WALL", BC_WALL, "", (0.0, 0.0, 0.0), tuple(wall_velocity)),
+            ("UPSTREAM", BC_SYMMETRY, "", (0.0, 0.0, 0.0)),
+            ("SIDE0", BC_SYMMETRY, "", (0.0, 0.0, 0.0)), ("SIDE1", BC_SYMMETRY, "", (0.0, 0.0, 0.0)),
+            ("INLET", BC_FARFIELD, "", (0.0, 0.0, 0.0)), ("OUTLET", BC_FARFIELD, "", (0.0, 0.0, 0.0)),
+            ("TOP", BC_FARFIELD, "", (0.0, 0.0, 0.0))]
 
 
 # ---------------------------------------------------------------------------
