@@ -55,10 +55,17 @@ enum ty_rk {
 /* TY_BC_FARFIELD (new: Typhon parses FAR-FIELD but has no Navier-Stokes implementation):
  * the kind of each far-field face follows the free-stream normal velocity vn = u_inf.n (n
  * outward) against the free-stream sound speed c: vn <= -c supersonic inflow (free stream),
- * vn < 0 subsonic inflow (free-stream density and velocity, inside pressure), vn < c subsonic
- * outflow (inside density and velocity, free-stream pressure), else supersonic outflow
- * (inside state).  The free stream is ty_spat_params.farfield. */
-enum ty_bc { TY_BC_INTERIOR = 0, TY_BC_PERIODIC = 1, TY_BC_SYMMETRY = 2, TY_BC_WALL = 3, TY_BC_FARFIELD = 4 };
+ * vn < -1e-8 c subsonic inflow (free-stream density and velocity, inside pressure), vn < c
+ * subsonic outflow (inside density and velocity, free-stream pressure; also a boundary
+ * tangent to the free stream), else supersonic outflow (inside state).  The free stream is
+ * ty_spat_params.farfield. */
+/* TY_BC_NOSLIP (new): the adiabatic wall of TY_BC_WALL with the inside density in its face
+ * state.  TY_BC_WALL keeps Typhon's face state, whose density is the inside PRESSURE
+ * (setboco_ns_flux.f90:136, "density / weak BC"), for parity with Typhon. */
+enum ty_bc {
+  TY_BC_INTERIOR = 0, TY_BC_PERIODIC = 1, TY_BC_SYMMETRY = 2, TY_BC_WALL = 3, TY_BC_FARFIELD = 4,
+  TY_BC_NOSLIP = 5
+};
 /* Arithmetic mode of the kernels.
  *   TY_MODE_EXACT: every FP64 operation in the order Typhon evaluates it, each rounded
  *                  separately (no fused multiply-add); results match the CPU restatement

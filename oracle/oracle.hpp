@@ -74,7 +74,9 @@ struct RawMesh {
 bool read_tym(const std::string& path, RawMesh& out, std::string& err);
 
 // Boundary families and how the solver treats them.
-enum BcKind { BC_PERIODIC = 1, BC_SYMMETRY = 2, BC_WALL = 3, BC_FARFIELD = 4 };
+// BC_NOSLIP (new): BC_WALL with the inside density in the face state (BC_WALL keeps Typhon's
+// face state, whose density is the inside pressure, setboco_ns_flux.f90:136)
+enum BcKind { BC_PERIODIC = 1, BC_SYMMETRY = 2, BC_WALL = 3, BC_FARFIELD = 4, BC_NOSLIP = 5 };
 struct BcDef {
   std::string family;   // family name as in the mesh marks
   int kind = 0;
@@ -146,12 +148,14 @@ struct SpatParams {
 // Far-field ghost state (new).  The kind of each far-field face is fixed by the free-stream
 // normal velocity vn = u_inf . n (n outward) against the free-stream sound speed c:
 //   vn <= -c  supersonic inflow:  the free stream
-//   vn <  0   subsonic inflow:    free-stream density and velocity, pressure from inside
-//   vn <  c   subsonic outflow:   inside density and velocity, free-stream pressure
+//   vn < -1e-8 c  subsonic inflow: free-stream density and velocity, pressure from inside
+//   vn <  c   subsonic outflow:   inside density and velocity, free-stream pressure (a face
+//             tangent to the free stream counts as outflow, whatever the rounding of n)
 //   else      supersonic outflow: the inside state
 // q: inside primitive state (rho, p, u, v, w); out: ghost primitive state.
 void farfield_state(double gamma, const double* qinf, V3 n, const double* q, double* out);
 bool farfield_jacobian(double gamma, const double* qinf, V3 n, const double* q, double* M);
+void noslip_jacobian(V3 uw, double* M);
 enum ViscMeth { VISC_NONE = 0, VISC_CELLAVG = 1, VISC_CELLFULL = 2 };
 
 struct RkTable {

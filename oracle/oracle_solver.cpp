@@ -118,7 +118,7 @@ bool farfield_jacobian(double gamma, const double* qinf, V3 n, const double* q, 
   for (int k = 0; k < 25; ++k) M[k] = 0.0;
   if (vn <= -c) return false;
   const double u2 = q[2] * q[2] + q[3] * q[3] + q[4] * q[4];
-  if (vn < 0.0) {            // subsonic inflow: rhoE_g = p / (gamma - 1) + const
+  if (vn < -1e-8 * c) {      // subsonic inflow: rhoE_g = p / (gamma - 1) + const
     M[5] = 0.5 * u2; M[6] = 1.0; M[7] = -q[2]; M[8] = -q[3]; M[9] = -q[4];
   } else if (vn < c) {       // subsonic outflow: rho, rhou kept, rhoE_g = p_inf / (gamma - 1) + |m|^2 / (2 rho)
     M[0] = 1.0;
@@ -130,12 +130,28 @@ bool farfield_jacobian(double gamma, const double* qinf, V3 n, const double* q, 
   return true;
 }
 
+// d(ghost conservative state)/d(inside conservative state) of the no-slip wall face state
+// (rho_g = rho, p_g = p, u_g = 2 u_w - u): rho E_g = rho E + 2 rho |u_w|^2 - 2 u_w.m,
+// m_g = 2 rho u_w - m (new; Typhon folds no wall Jacobian)
+void noslip_jacobian(V3 uw, double* M) {
+  const double w[3] = {uw.x, uw.y, uw.z};
+  for (int k = 0; k < 25; ++k) M[k] = 0.0;
+  M[0] = 1.0;
+  M[5] = 2.0 * (w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+  M[6] = 1.0;
+  for (int j = 0; j < 3; ++j) M[7 + j] = -2.0 * w[j];
+  for (int i = 0; i < 3; ++i) {
+    M[(2 + i) * 5] = 2.0 * w[i];
+    M[(2 + i) * 5 + 2 + i] = -1.0;
+  }
+}
+
 void farfield_state(double gamma, const double* qinf, V3 n, const double* q, double* out) {
   const double vn = qinf[2] * n.x + qinf[3] * n.y + qinf[4] * n.z;
   const double c = std::sqrt(gamma * qinf[1] / qinf[0]);
   if (vn <= -c) {
     for (int v = 0; v < 5; ++v) out[v] = qinf[v];
-  } else if (vn < 0.0) {
+  } else if (vn < -1e-8 * c) {
     out[0] = qinf[0]; out[1] = q[1]; out[2] = qinf[2]; out[3] = qinf[3]; out[4] = qinf[4];
   } else if (vn < c) {
     out[0] = q[0]; out[1] = qinf[1]; out[2] = q[2]; out[3] = q[3]; out[4] = q[4];
@@ -164,7 +180,7 @@ void Solver::boco_cell_state() {
         prim[2 * nc + g] = ug.x;
         prim[3 * nc + g] = ug.y;
         prim[4 * nc + g] = ug.z;
-      } else if (b.kind == BC_WALL) {
+      } else if (b.kind == BC_WALL || b.kind == BC_NOSLIP) {
         // setboco_ns_flux.f90, cell-state mode, adiabatic wall (lflux = 0): ghost pressure
         // = cell pressure, ghost temperature = cell temperature - lflux d / conduct, velocity
         // reflected about the wall velocity
@@ -219,10 +235,11 @@ void Solver::boco_face_state() {
       if (b.kind == BC_PERIODIC) {
         int fp = b.partner_face[k];
         for (int v = 0; v < 5; ++v) cell_r[v * nf + f] = cell_l[v * nf + fp];
-      } else if (b.kind == BC_WALL) {
+      } else if (b.kind == BC_WALL || b.kind == BC_NOSLIP) {
         // setboco_ns_flux.f90, face-state mode: cell_r takes cell_l's PRESSURE as its density
-        // ("weak BC"), cell_l's pressure, and the velocity reflected about the wall velocity
-        cell_r[f] = cell_l[nf + f];
+        // ("weak BC"), cell_l's pressure, and the velocity reflected about the wall velocity;
+        // BC_NOSLIP (new) takes cell_l's density
+        cell_r[f] = b.kind == BC_NOSLIP ? cell_l[f] : cell_l[nf + f];
         cell_r[nf + f] = cell_l[nf + f];
         V3 u = v3(cell_l[2 * nf + f], cell_l[3 * nf + f], cell_l[4 * nf + f]);
         V3 ug = (2.0 * b.wall_velocity) - u;
@@ -878,7 +895,7 @@ void Solver::ns_bocoflux() {
   const double r = sp.rgas;
   const double cp = sp.gamma * r / (sp.gamma - 1.0);
   for (auto& b : m->bocos) {
-    if (b.kind != BC_WALL) continue;
+    if (b.kind != BC_WALL && b.kind != BC_NOSLIP) continue;
     for (int f : b.iface) {
       const int icl = m->fc1[f], icr = m->fc2[f];
       const V3 F = m->fcentre[f], CL = m->ccentre[icl], CR = m->ccentre[icr], n = m->fnormal[f];
@@ -1152,12 +1169,13 @@ void Solver::calc_rhs() {
 void Solver::ns_bocojacobian() {
   const int nf = m->nface;
   for (const Boco& b : m->bocos) {
-    if (b.kind == BC_FARFIELD) {
+    if (b.kind == BC_FARFIELD || b.kind == BC_NOSLIP) {
       for (int f : b.iface) {
         double ql[5];
         for (int v = 0; v < 5; ++v) ql[v] = cell_l[v * (size_t)nf + f];
         double M[25];
-        if (!farfield_jacobian(sp.gamma, sp.farfield, m->fnormal[f], ql, M)) continue;
+        if (b.kind == BC_NOSLIP) noslip_jacobian(b.wall_velocity, M);
+        else if (!farfield_jacobian(sp.gamma, sp.farfield, m->fnormal[f], ql, M)) continue;
         double* JL = &jacL[25 * (size_t)f];
         double* JR = &jacR[25 * (size_t)f];
         for (int i = 0; i < 5; ++i)

@@ -13,7 +13,7 @@ ROOT = pathlib.Path(__file__).resolve().parents[1]
 LIB = ROOT / "oracle" / "build" / "liboracle.so"
 
 # enums of oracle/oracle.hpp
-BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD = 1, 2, 3, 4
+BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD, BC_NOSLIP = 1, 2, 3, 4, 5
 SCH_HLLC, SCH_RUSANOV, SCH_ROE = 1, 2, 3
 HRES_NONE, HRES_MUSCL, HRES_MUSCLFAST, HRES_MUSCLUNS = 0, 1, 2, 3
 LIM_NONE, LIM_MINMOD, LIM_ALBADA, LIM_VLEER, LIM_SBEE, LIM_KIM3, LIM_LIM03 = range(7)

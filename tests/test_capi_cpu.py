@@ -111,7 +111,7 @@ def test_preprocess_flatplate_prisms_tets_matches_oracle(ty):
     top = raw.vtex[:, 1].max()
     assert abs(md.cell_volume[:md.ncell_int].sum() - 1.5 * 0.2 * top) < 1e-12
     kinds = md.face_bc[md.nface_int:]
-    assert set(np.unique(kinds)) == {ty.BC_WALL, ty.BC_SYMMETRY, ty.BC_FARFIELD}
+    assert set(np.unique(kinds)) == {ty.BC_NOSLIP, ty.BC_SYMMETRY, ty.BC_FARFIELD}
 
 
 def test_tym_roundtrip(ty, tmp_path):

@@ -409,7 +409,8 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
         int p = d->face_partner[f] - 1;
         if (p < nfi || p >= nf || d->face_partner[p] - 1 != f) { tyi::set_error("bad periodic partner"); return bail(TY_ERR_MESH); }
         part[f] = p;
-      } else if (fbc[f] != TY_BC_SYMMETRY && fbc[f] != TY_BC_WALL && fbc[f] != TY_BC_FARFIELD) {
+      } else if (fbc[f] != TY_BC_SYMMETRY && fbc[f] != TY_BC_WALL && fbc[f] != TY_BC_FARFIELD &&
+                 fbc[f] != TY_BC_NOSLIP) {
         tyi::set_error("unknown boundary kind");
         return bail(TY_ERR_UNSUPPORTED);
       }
@@ -428,7 +429,7 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
   std::vector<double> gdist(std::max(ng, 1), 0.0);
   for (int k = 0; k < ng; ++k) {
     const int f = gface[k];
-    if (fbc[f] != TY_BC_WALL) continue;
+    if (fbc[f] != TY_BC_WALL && fbc[f] != TY_BC_NOSLIP) continue;
     const double* F = &d->face_centre[3 * (size_t)f];
     const double* Cc = &d->cell_centre[3 * (size_t)h->fc1[f]];
     const double* n = &d->face_normal[3 * (size_t)f];

@@ -25,6 +25,8 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <vector>
@@ -295,6 +297,8 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
   IMP_CU(IMP_CALL(h, imp_dot, im.b, im.b, n, im.part, im.scal + kScalMisc, s));
   if (int rc = fetch(h, kScalMisc, 1)) return rc;
   const double beta0 = std::sqrt(P[kScalMisc]);
+  const char* tv = std::getenv("TY_IMPLICIT_TRACE");  // Arnoldi history on stderr when set to 1
+  const bool trace = tv && tv[0] == '1';
   int matvecs = 0, cycles = 0;
   double rel = beta0 > 0.0 ? 1.0 : 0.0;
   if (beta0 > 0.0) {
@@ -345,6 +349,9 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
         g[j + 1] = -sn[j] * g[j];
         g[j] = cs[j] * g[j];
         nused = j + 1;
+        if (trace)
+          std::fprintf(stderr, "ty_implicit fgmres cycle %d j %d h_jj %.6e h_j+1,j %.6e |g|/|b| %.6e\n", cycles, j,
+                       Hm(j, j), hn, std::fabs(g[j + 1]) / beta0);
         if (std::fabs(g[j + 1]) <= tol || !(hn > 0.0)) break;
         const double hinv = 1.0 / hn;
         if (int rc = put(h, kScalHinv, &hinv, 1)) return rc;

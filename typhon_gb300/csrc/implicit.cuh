@@ -5,7 +5,8 @@
 //   flux Jacobians       calc_jacflux.f90:49-77, calc_jac_hll.f90:46-57 (HLLC, Roe),
 //                        calc_jac_rusanov.f90 (Rusanov), viscous diagonal
 //                        calc_flux_viscous_cell.f90:149-158, symmetry ns_bocojacobian.f90:47-85
-//                        (and, new, the far-field ghost dependence folded in the same way),
+//                        (and, new, the far-field and no-slip wall ghost dependences folded in
+//                        the same way),
 //                        surface scaling flux_to_res.f90:74-80
 //   BDLU blocks          build_implicit_bdlu.f90:44-83 (diagonal contributions of a cell
 //                        summed in ascending face order, as the face loop there does)
@@ -113,7 +114,7 @@ __device__ bool farfield_jacobian(const SpatOpts& o, double nx, double ny, doubl
   for (int k = 0; k < 25; ++k) M[k] = 0.0;
   if (vn <= -c) return false;
   const double u2 = q[2] * q[2] + q[3] * q[3] + q[4] * q[4];
-  if (vn < 0.0) {
+  if (vn < -1e-8 * c) {
     M[5] = 0.5 * u2; M[6] = 1.0; M[7] = -q[2]; M[8] = -q[3]; M[9] = -q[4];
   } else if (vn < c) {
     M[0] = 1.0;
@@ -152,7 +153,7 @@ __device__ void implicit_face_states(const DevMesh& m, const DevState& s, const 
   const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
   if (kind == TY_BC_PERIODIC) {
     side_state(m.part[f], 0, QR);
-  } else if (kind == TY_BC_WALL) {
+  } else if (kind == TY_BC_WALL || kind == TY_BC_NOSLIP) {
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {
     farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);
@@ -272,6 +273,21 @@ __global__ void __launch_bounds__(128) k_imp_face(DevMesh m, DevState s, SpatOpt
     fold = true;
   } else if (bkind == TY_BC_FARFIELD) {
     fold = farfield_jacobian(o, nx, ny, nz, QL, M);
+  } else if (bkind == TY_BC_NOSLIP) {  // new: d(2 rho u_w - m, rho E + 2 rho |u_w|^2 - 2 u_w.m)/dU
+    const double w[3] = {d3(m.fwall, m.ldf, f, 0), d3(m.fwall, m.ldf, f, 1), d3(m.fwall, m.ldf, f, 2)};
+#pragma unroll
+    for (int k = 0; k < 25; ++k) M[k] = 0.0;
+    M[0] = 1.0;
+    M[5] = 2.0 * (w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    M[6] = 1.0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) M[7 + j] = -2.0 * w[j];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      M[(2 + i) * 5] = 2.0 * w[i];
+      M[(2 + i) * 5 + 2 + i] = -1.0;
+    }
+    fold = true;
   }
   if (fold) {
 #pragma unroll

@@ -152,7 +152,7 @@ __device__ __forceinline__ void farfield_state(const SpatOpts& o, double nx, dou
   if (vn <= -c) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) out[v] = qi[v];
-  } else if (vn < 0.0) {
+  } else if (vn < -1e-8 * c) {
     out[0] = qi[0]; out[1] = q[1]; out[2] = qi[2]; out[3] = qi[3]; out[4] = qi[4];
   } else if (vn < c) {
     out[0] = q[0]; out[1] = qi[1]; out[2] = q[2]; out[3] = q[3]; out[4] = q[4];
@@ -181,7 +181,7 @@ __global__ void k_ghost_prim(DevMesh m, double* __restrict__ prim, SpatOpts o) {
     for (int v = 0; v < 5; ++v) prim[v * ld + g] = out[v];
     return;
   }
-  if (kind == TY_BC_WALL) {
+  if (kind == TY_BC_WALL || kind == TY_BC_NOSLIP) {
     const double r = o.rgas, lflux = 0.0;
     const double rho = prim[src], p = prim[ld + src];
     const double mu = viscosity(o, rho, p / (r * rho));
@@ -360,7 +360,7 @@ __device__ void recon(const DevMesh& m, const DevState& s, const SpatOpts& o, in
 // moving adiabatic wall, face-state mode (setboco_ns_flux.f90): the right state takes the left
 // state's pressure as its density, its pressure, and the velocity reflected about the wall's
 __device__ __forceinline__ void wall_state(const DevMesh& m, int f, const double* QL, double* QR) {
-  QR[0] = QL[1];
+  QR[0] = m.fbc[f] == TY_BC_NOSLIP ? QL[0] : QL[1];  // TY_BC_NOSLIP: the inside density (new)
   QR[1] = QL[1];
   QR[2] = (2.0 * d3(m.fwall, m.ldf, f, 0)) - QL[2];
   QR[3] = (2.0 * d3(m.fwall, m.ldf, f, 1)) - QL[3];
@@ -692,7 +692,7 @@ __device__ void add_viscous(const DevMesh& m, const DevState& s, const SpatOpts&
   F[1] = F[1] - svn;
   const double conduct = mu * cp / o.prandtl;
   F[1] = F[1] - conduct * gTH;
-  if (f >= m.nfi && m.fbc[f] == TY_BC_WALL) F[1] = F[1] + conduct * gTH + 0.0;
+  if (f >= m.nfi && (m.fbc[f] == TY_BC_WALL || m.fbc[f] == TY_BC_NOSLIP)) F[1] = F[1] + conduct * gTH + 0.0;
 }
 
 __device__ __forceinline__ void face_flux_fast(const DevMesh& m, const DevState& s, const SpatOpts& o, int f,
@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux(DevMesh m, DevState s, Spa
   const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
   if (kind == TY_BC_PERIODIC) {
     recon(m, s, o, m.part[f], 0, QR);  // cell_r(face) = cell_l(partner face)
-  } else if (kind == TY_BC_WALL) {
+  } else if (kind == TY_BC_WALL || kind == TY_BC_NOSLIP) {
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {
     farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);
@@ -821,7 +821,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_lim(DevMesh m, DevState s,
   const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
   if (kind == TY_BC_PERIODIC) {
     limited(m.part[f], 0, QR);
-  } else if (kind == TY_BC_WALL) {
+  } else if (kind == TY_BC_WALL || kind == TY_BC_NOSLIP) {
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {
     farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);
@@ -977,7 +977,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_fast(DevMesh m, DevState s
     const int p = m.part[f];
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = s.cl[v * lf + p];
-  } else if (kind == TY_BC_WALL) {
+  } else if (kind == TY_BC_WALL || kind == TY_BC_NOSLIP) {
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {
     farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);

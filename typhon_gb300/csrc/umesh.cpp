@@ -137,7 +137,7 @@ int ty_umesh_add_mark(ty_umesh* um, const char* family, int32_t ntag, const int3
 }
 int ty_umesh_add_bc(ty_umesh* um, const char* family, int32_t kind, const char* partner,
                     const double* t3, const double* w3) {
-  if (!um || !family || kind < TY_BC_PERIODIC || kind > TY_BC_FARFIELD) return TY_ERR_ARG;
+  if (!um || !family || kind < TY_BC_PERIODIC || kind > TY_BC_NOSLIP) return TY_ERR_ARG;
   BcIn b;
   b.family = upper(family);
   b.partner = partner ? upper(partner) : "";

@@ -25,7 +25,7 @@ ELEM_BAR2, ELEM_TRI3, ELEM_QUAD4, ELEM_TETRA4, ELEM_PENTA6, ELEM_HEXA8 = 2, 13, 
 NVTEX = {ELEM_BAR2: 2, ELEM_TRI3: 3, ELEM_QUAD4: 4, ELEM_TETRA4: 4, ELEM_PENTA6: 6, ELEM_HEXA8: 8}
 DIM = {ELEM_BAR2: 1, ELEM_TRI3: 2, ELEM_QUAD4: 2, ELEM_TETRA4: 3, ELEM_PENTA6: 3, ELEM_HEXA8: 3}
 
-BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD = 1, 2, 3, 4
+BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD, BC_NOSLIP = 1, 2, 3, 4, 5
 
 
 @dataclass
@@ -391,7 +391,7 @@ def gen_flatplate(nx=200, nz=20, n_prism=50, n_tet=25, x0=-0.5, x1=1.0, width=0.
 def flatplate_bcs(wall_velocity=(0.0, 0.0, 0.0)):
     """Adiabatic no-slip plate, symmetry upstream of it and on the span sides, far field
     at the inlet, outlet and top."""
-    return [("WALL", BC_WALL, "", (0.0, 0.0, 0.0), tuple(wall_velocity)),
+    return [("WALL", BC_NOSLIP, "", (0.0, 0.0, 0.0), tuple(wall_velocity)),
             ("UPSTREAM", BC_SYMMETRY, "", (0.0, 0.0, 0.0)),
             ("SIDE0", BC_SYMMETRY, "", (0.0, 0.0, 0.0)), ("SIDE1", BC_SYMMETRY, "", (0.0, 0.0, 0.0)),
             ("INLET", BC_FARFIELD, "", (0.0, 0.0, 0.0)), ("OUTLET", BC_FARFIELD, "", (0.0, 0.0, 0.0)),
