@@ -8,7 +8,10 @@ A "step" is one full SSP-RK3 step (3 residual evaluations) of every cell; one
 cell-update = one cell advanced by one step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload tgv3d|vortex2d] [--n 64] [--mode fast|exact]
+                  [--workload tgv3d|vortex2d|ffbox3d-implicit] [--n 64] [--mode fast|exact]
+
+--workload ffbox3d-implicit: time to a 1e-10 relative residual of the implicit solvers (FP64
+flexible GMRES, mixed FP32/FP64, FP64 Jacobian-free) on a steady 3D far-field box.
 
 --impl reference times the CPU restatement of Typhon's solver (oracle/, OpenMP on all
 host cores) on the same configuration: Typhon itself is Fortran and cannot be built here.
@@ -39,7 +42,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="tgv3d", choices=["tgv3d", "vortex2d"])
+    ap.add_argument("--workload", default="tgv3d", choices=["tgv3d", "vortex2d", "ffbox3d-implicit"])
     ap.add_argument("--n", type=int, default=None, help="cells per direction (default: the workload's)")
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
     ap.add_argument("--e2e-steps", type=int, default=None)
@@ -302,9 +305,82 @@ def cpu_sample(args, n_steps):
                       f"threads ({dt:.1f} s)"}
 
 
+def run_implicit(args):
+    """Steady implicit solve of the far-field box to a 1e-10 relative residual with three
+    solvers: FP64 flexible GMRES (assembled BDLU, block Jacobi), the mixed form (FP32 BDLU
+    mat-vec and block Jacobi, FP64 residual / CGS2 / update) and FP64 Jacobian-free
+    Newton-Krylov.  Times to the target (wall clock, synchronised) and the mixed and JFNK
+    converged states against the FP64 assembled one."""
+    import torch
+    import typhon_gb300 as ty
+    from typhon_gb300 import build, cases
+    build.build()
+    torch.cuda.set_device(0)
+    w = cases.FFBOX
+    md = cases.make_ffbox(args.n)
+    nci = md.ncell_int
+    ff = w["freestream"]
+    L = w["length"]
+    prim0 = cases.perturbed_freestream(md.cell_centre, ff, (L / 2, L / 2, L / 2))
+    scale = np.array([ff[0], ff[1] / 0.4, 0.3, 0.3, 0.3])
+    variants = {}
+    states = {}
+    with ClockSampler(0) as clk:
+        for name, inv, prec in (("fgmres_fp64", "FGMRES", "fp64"), ("fgmres_mixed", "FGMRES", "mixed"),
+                                ("jfnk_fp64", "JFNK", "fp64")):
+            g = ty.Grid(md)
+            g.set_spat(w["scheme"], w["highres"], w["limiter"], w["postlim"], mode="fast", farfield=ff)
+            g.set_prim(prim0)
+            g.implicit_step(1e-3, inv, nkrylov=w["nkrylov"], max_it=1, inv_res=0.5, local_dt=True, precision=prec)
+            g.set_prim(prim0)                     # warm-up step above allocates the workspace
+            g.synchronize()
+            cfl, r0, steps, matvecs, rel = w["cfl0"], None, 0, 0, 1.0
+            t0 = time.perf_counter()
+            while steps < w["max_steps"]:
+                st = g.implicit_step(cfl, inv, nkrylov=w["nkrylov"], max_it=w["max_it"], inv_res=w["inv_res"],
+                                     local_dt=True, precision=prec)
+                steps += 1
+                matvecs += st["matvecs"]
+                r = float(np.sqrt(np.sum((st["res_l2"] / scale) ** 2)))
+                r0 = r0 or r
+                rel = r / r0
+                if rel < w["target"]:
+                    break
+                cfl = min(max(w["cfl0"] * r0 / r, w["cfl0"]), w["cfl_max"])
+            g.synchronize()
+            t = time.perf_counter() - t0
+            states[name] = g.get_cons()
+            variants[name] = {"seconds": round(t, 3), "steps": steps, "matvecs": matvecs, "final_rel_residual": rel,
+                              "reached": bool(rel < w["target"])}
+            g.close()
+    ref = states["fgmres_fp64"]
+    for name in ("fgmres_mixed", "jfnk_fp64"):
+        d = states[name] - ref
+        variants[name]["state_vs_fp64"] = [float(np.linalg.norm(d[0]) / np.linalg.norm(ref[0])),
+                                           float(np.linalg.norm(d[1]) / np.linalg.norm(ref[1])),
+                                           float(np.linalg.norm(d[2:5]) / np.linalg.norm(ref[2:5]))]
+    out = {"metric": "seconds to a 1e-10 relative residual, mixed FP32/FP64 implicit", "unit": "s",
+           "value": variants["fgmres_mixed"]["seconds"], "higher_is_better": False, "n_gpus": 1,
+           "steps": variants["fgmres_mixed"]["steps"], "warmup": 1, "dtype": "f64+f32", "data": "synthetic",
+           "scaling": "weak", "vs_baseline": None,
+           "config": {"workload": f"ffbox3d {args.n or w['n']}^3x5 tets far field, Rusanov, backward Euler",
+                      "cells": nci, "cfl": f"{w['cfl0']} -> {w['cfl_max']} (SER)",
+                      "krylov": f"FGMRES({w['nkrylov']}) x {w['max_it']}, INV_RES {w['inv_res']}"},
+           "variants": variants,
+           "speedup_mixed_vs_fp64": round(variants["fgmres_fp64"]["seconds"] / variants["fgmres_mixed"]["seconds"], 3),
+           "clocks": clk.summary()}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "ffbox3d-implicit":
+        if rank == 0 and args.impl == "ours":
+            run_implicit(args)
+        elif rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the implicit comparison has no CPU arm"}))
+        return
     if args.impl == "reference":
         if rank != 0:
             return

@@ -7,7 +7,10 @@
              [0,2 pi]^3 box, 64^3 hexahedra split into 5 tetrahedra (1,310,720 cells),
              interior nodes jittered by +-5% of h (seed 1234); least-squares gradients,
              MUSCL-UNS with the Barth post-limiter, Roe flux, SSP-RK3.
-Both are nondimensional (rho_inf = 1).  The initial states are evaluated at cell centres.
+  ffbox3d    3D steady far-field box for the implicit solvers (FFBOX below): 48^3
+             hexahedra split into 5 tetrahedra, far field on all faces, M = 0.3 at 20 degrees,
+             Rusanov, a Gaussian bump relaxing to the uniform free stream.
+All are nondimensional (rho_inf = 1).  The initial states are evaluated at cell centres.
 """
 import numpy as np
 
@@ -39,6 +42,33 @@ def taylor_green(xyz, mach=0.1, gamma=1.4):
     p = p0 + (np.cos(2 * x) + np.cos(2 * y)) * (np.cos(2 * z) + 2.0) / 16.0
     rho = p / p0
     return np.stack([rho, p, u, v, np.zeros_like(x)])
+
+
+def perturbed_freestream(xyz, ff, centre, amp=0.2, width=1.0):
+    """The free stream ff = (rho, p, u, v, w) with a Gaussian bump of density, pressure and
+    velocity around `centre`."""
+    r2 = ((xyz - np.asarray(centre)) ** 2).sum(1)
+    b = amp * np.exp(-r2 / width)
+    return np.stack([ff[0] * (1 + b), ff[1] * (1 + b), ff[2] + 0.5 * b, ff[3] - 0.5 * b, ff[4] + 0.25 * b])
+
+
+_ANG = np.deg2rad(20.0)
+# 3D steady far-field box: free stream M = 0.3 at 20 degrees through far-field boundaries on all
+# six faces of the [0, 2 pi]^3 tetrahedral box, a Gaussian bump in the initial state; the steady
+# state is the uniform free stream.  Rusanov flux with its own Jacobian (Newton-consistent).
+FFBOX = dict(dim=3, n=48, length=2 * np.pi, jitter=0.05, seed=1234, scheme="RUSANOV", highres="NONE",
+             limiter="NONE", postlim="NONE",
+             freestream=(1.0, 1.0 / 1.4, 0.3 * np.cos(_ANG), 0.3 * np.sin(_ANG) * 0.6, 0.3 * np.sin(_ANG) * 0.8),
+             cfl0=10.0, cfl_max=25.0, nkrylov=30, max_it=2, inv_res=1e-2, target=1e-10, max_steps=1500)
+
+
+def make_ffbox(n=None):
+    """Preprocessed far-field tetrahedral box of FFBOX (native preprocessing)."""
+    w = FFBOX
+    n = n or w["n"]
+    raw = umesh.gen_tet_box(n, w["length"], jitter=w["jitter"], seed=w["seed"])
+    bcs = [(f, umesh.BC_FARFIELD, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX", "KMIN", "KMAX")]
+    return umesh.preprocess(raw, 3, bcs)
 
 
 WORKLOADS = {
