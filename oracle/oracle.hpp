@@ -221,4 +221,37 @@ struct Solver {
   void rk_step(double dt);       // treelevel_rungekutta + update_field
 };
 
+// ---------------------------------------------------------------------------
+// Heat conduction (KDIF), oracle_kdif.cpp
+enum KdifScheme { KDIF_COMPACT = 0, KDIF_CELLAVG = 1, KDIF_FULL = 2 };
+// boundary kinds of KDIF faces (periodic faces come from the mesh)
+enum KdifBc { KBC_NONE = 0, KBC_ISOTHERMAL = 1, KBC_FLUX = 2, KBC_EXTRAPOLATE = 3, KBC_PERIODIC = 4 };
+struct KdifSolver {
+  const UMesh* m = nullptr;
+  int scheme = KDIF_FULL;
+  double cp = 1.0;
+  std::vector<double> kcell;   // ncell conductivity (ghosts: the inside cell's)
+  std::vector<int> fkind;      // nface KdifBc
+  std::vector<double> fval;    // nface wall temperature or imposed flux
+  std::vector<double> T;       // ncell temperature
+  std::vector<double> grad;    // 3*ncell
+  std::vector<double> flux;    // nface flux times S
+  std::vector<double> jac;     // nface J_R times S (0 on imposed-flux faces)
+  std::vector<double> residu;  // ncell dt/V sum(+-F S)
+  std::vector<double> balance; // ncell_int sum(+-F S)
+  std::vector<double> diag;    // ncell_int diagonal of the symmetrised implicit matrix
+  Solver lsq;                  // least-squares gradient machinery of the NS path
+  void init(const UMesh* mesh, int flux_scheme, double heat_capacity, const double* kc, const int* kind,
+            const double* value);
+  void ghosts();
+  void gradient();
+  double face_k(int f, double dHL, double dHR) const;
+  void fluxes();
+  void rhs(double dt);
+  void assemble(double dt);
+  void matvec(const double* x, double* y) const;
+  int cg(const std::vector<double>& b, std::vector<double>& x, double tol, int max_it, double* rel);
+  int implicit_step(double dt, double tol, int max_it, double* rel);
+};
+
 }  // namespace ory

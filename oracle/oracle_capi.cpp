@@ -334,3 +334,43 @@ int ory_run_nrg(int which, void* mesh, int rk_method, double cfl, int ncycle, do
 }
 
 }  // extern "C"
+
+// ---- heat conduction (KDIF) ----
+extern "C" {
+// scheme: 0 compact, 1 cell-average, 2 full; kc[ncell_int] conductivity; kind/value[nface]:
+// KdifBc and the wall temperature or imposed flux of each boundary face
+void* ory_kdif_new(void* mesh, int scheme, double cp, const double* kc, const int* kind, const double* value) {
+  auto* k = new KdifSolver();
+  k->init(&((MeshHandle*)mesh)->m, scheme, cp, kc, kind, value);
+  return k;
+}
+void ory_kdif_free(void* k) { delete (KdifSolver*)k; }
+void ory_kdif_set_T(void* k, const double* T) {
+  auto* K = (KdifSolver*)k;
+  for (int c = 0; c < K->m->ncell_int; ++c) K->T[c] = T[c];
+}
+void ory_kdif_rhs(void* k, double dt) { ((KdifSolver*)k)->rhs(dt); }
+void ory_kdif_assemble(void* k, double dt) { ((KdifSolver*)k)->assemble(dt); }
+void ory_kdif_matvec(void* k, const double* x, double* y) { ((KdifSolver*)k)->matvec(x, y); }
+// which: 0 T [ncell], 1 grad [3][ncell], 2 flux*S [nface], 3 J_R*S [nface], 4 residu [ncell],
+//        5 flux balance [ncell_int], 6 diagonal [ncell_int]
+int ory_kdif_get(void* k, int which, double* out) {
+  auto* K = (KdifSolver*)k;
+  const std::vector<double>* v = nullptr;
+  switch (which) {
+    case 0: v = &K->T; break;
+    case 1: v = &K->grad; break;
+    case 2: v = &K->flux; break;
+    case 3: v = &K->jac; break;
+    case 4: v = &K->residu; break;
+    case 5: v = &K->balance; break;
+    case 6: v = &K->diag; break;
+    default: return -1;
+  }
+  std::memcpy(out, v->data(), v->size() * sizeof(double));
+  return (int)v->size();
+}
+int ory_kdif_implicit_step(void* k, double dt, double tol, int max_it, double* rel) {
+  return ((KdifSolver*)k)->implicit_step(dt, tol, max_it, rel);
+}
+}

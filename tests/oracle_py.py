@@ -59,6 +59,16 @@ def load():
         lib.ory_solver_implicit_step.argtypes = [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp]
         lib.ory_solver_implicit_step.restype = C.c_int
         lib.ory_solver_bdlu_matvec.argtypes = [vp, vp, vp]
+        lib.ory_kdif_new.argtypes = [vp, C.c_int, C.c_double, vp, vp, vp]
+        lib.ory_kdif_new.restype = vp
+        lib.ory_kdif_free.argtypes = [vp]
+        lib.ory_kdif_set_T.argtypes = [vp, vp]
+        lib.ory_kdif_rhs.argtypes = [vp, C.c_double]
+        lib.ory_kdif_assemble.argtypes = [vp, C.c_double]
+        lib.ory_kdif_matvec.argtypes = [vp, vp, vp]
+        lib.ory_kdif_get.argtypes = [vp, C.c_int, vp]
+        lib.ory_kdif_implicit_step.argtypes = [vp, C.c_double, C.c_double, C.c_int, vp]
+        lib.ory_kdif_implicit_step.restype = C.c_int
         lib.ory_run_nrg.argtypes = [C.c_int, vp, C.c_int, C.c_double, C.c_int, C.c_double, vp]
         _lib = lib
     return _lib
@@ -238,3 +248,53 @@ def run_nrg(which, mesh, rk, cfl, ncycle=100, duration=0.1):
 
 PERIODIC_UNIT_SQUARE = [("IMIN", BC_PERIODIC, "IMAX", (1.0, 0.0, 0.0)),
                         ("JMIN", BC_PERIODIC, "JMAX", (0.0, 1.0, 0.0))]
+
+
+KDIF_COMPACT, KDIF_CELLAVG, KDIF_FULL = 0, 1, 2
+KBC_ISOTHERMAL, KBC_FLUX, KBC_EXTRAPOLATE = 1, 2, 3
+
+
+class Kdif:
+    """Heat-conduction oracle (oracle_kdif.cpp) on a built Mesh."""
+
+    def __init__(self, mesh, scheme, cp, conductivity, face_kind, face_value):
+        self.lib = load()
+        self.mesh = mesh
+        kc = np.ascontiguousarray(conductivity, np.float64)
+        fk = np.ascontiguousarray(face_kind, np.int32)
+        fv = np.ascontiguousarray(face_value, np.float64)
+        self.h = C.c_void_p(self.lib.ory_kdif_new(mesh.h, int(scheme), float(cp), _p(kc), _p(fk), _p(fv)))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.ory_kdif_free(self.h)
+            self.h = None
+
+    def set_T(self, T):
+        t = np.ascontiguousarray(T[:self.mesh.ncell_int], np.float64)
+        self.lib.ory_kdif_set_T(self.h, _p(t))
+
+    def rhs(self, dt):
+        self.lib.ory_kdif_rhs(self.h, float(dt))
+
+    def assemble(self, dt):
+        self.lib.ory_kdif_assemble(self.h, float(dt))
+
+    def get(self, which):
+        m = self.mesh
+        code, n = {"T": (0, m.ncell), "grad": (1, 3 * m.ncell), "flux": (2, m.nface), "jac": (3, m.nface),
+                   "residu": (4, m.ncell), "balance": (5, m.ncell_int), "diag": (6, m.ncell_int)}[which]
+        out = np.zeros(n)
+        assert self.lib.ory_kdif_get(self.h, code, _p(out)) == n
+        return out.reshape(3, m.ncell) if which == "grad" else out
+
+    def matvec(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        self.lib.ory_kdif_matvec(self.h, _p(x), _p(y))
+        return y
+
+    def implicit_step(self, dt, tol=1e-12, max_it=10000):
+        rel = C.c_double()
+        it = self.lib.ory_kdif_implicit_step(self.h, float(dt), float(tol), int(max_it), C.byref(rel))
+        return it, rel.value
