@@ -242,6 +242,60 @@ int ty_implicit_get(ty_mesh* mesh, int32_t which, double* out);
  * (Typhon's bdlu_yeqax, SPMAT_BDLU.f90:139-157). */
 int ty_implicit_matvec(ty_mesh* mesh, const double* x, double* y);
 
+/* ---------------------------------------------------------------------------------
+ * Heat conduction (KDIF: SOLVER = HEAT).  The temperature T lives per cell of the handle's
+ * mesh; U = Cp T.  Replaces integration_kdif_ust (SOURCE/EQKDIF/integration_kdif_ust.f90) and
+ * the implicit step of the HEAT solver (calc_rhs.f90:121-138 with its DLU matrix).
+ */
+enum ty_kdif_flux {     /* SPAT_PARAM:DISSIPATIVE_FLUX of calc_kdif_flux.f90:106-137 */
+  TY_KDIF_COMPACT = 0,  /* two-point: -k (T_R - T_L) (d.n) / |d|^2 */
+  TY_KDIF_CELLAVG = 1,  /* -k (a grad T_R + b grad T_L).n */
+  TY_KDIF_FULL = 2      /* compact along d plus the averaged gradient across it */
+};
+enum ty_kdif_bc {       /* boundary kind of each boundary face (periodic faces: from the mesh) */
+  TY_KBC_ISOTHERMAL = 1,  /* ISOTHERMAL_WALL: ghost temperature = face value (setboco_kdif_isoth.f90) */
+  TY_KBC_FLUX = 2,        /* imposed flux entering the domain = face value; 0 is adiabatic */
+  TY_KBC_EXTRAPOLATE = 3  /* ghost temperature = inside temperature */
+};
+typedef struct ty_kdif_params {
+  int32_t flux;          /* ty_kdif_flux */
+  int32_t reserved;
+  double heat_capacity;  /* MODEL: HEATCAPA (rho Cp per unit volume) */
+} ty_kdif_params;
+/* conductivity [ncell_int] (new: per cell; the face value is the distance-weighted harmonic
+ * mean, or the common value when both cells agree, which is Typhon's uniform CONDUCT);
+ * face_kind [nface] ty_kdif_bc of boundary faces (ignored for interior and periodic faces);
+ * face_value [nface] wall temperature or imposed flux. */
+int ty_kdif_setup(ty_mesh* mesh, const ty_kdif_params* p, const double* conductivity, const int32_t* face_kind,
+                  const double* face_value);
+int ty_kdif_set_temperature(ty_mesh* mesh, const double* T);   /* host [ncell_int] */
+int ty_kdif_get_temperature(ty_mesh* mesh, double* T);         /* host [ncell_int] */
+/* residual dt/V sum(+-F S) of U = Cp T (host [ncell_int], may be NULL) */
+int ty_kdif_residual(ty_mesh* mesh, double dt, double* R);
+typedef enum {
+  TY_KSOLVE_CG = 0,          /* conjugate gradients + Jacobi, FP64 (new: Typhon has CGS/BiCG/GMRES) */
+  TY_KSOLVE_CG32_REFINE = 1  /* FP32 conjugate gradients inside FP64 iterative refinement */
+} ty_kdif_solver;
+typedef struct ty_kdif_solve {
+  int32_t solver;        /* ty_kdif_solver */
+  int32_t max_it;        /* iterations (CG) or inner iterations per refinement (CG32) */
+  double tol;            /* relative residual of the symmetrised system */
+  double inner_tol;      /* CG32: relative residual of each inner FP32 solve */
+} ty_kdif_solve;
+typedef struct ty_kdif_stats {
+  int32_t iterations;    /* CG iterations (all inner iterations for CG32) */
+  int32_t refinements;   /* outer FP64 refinements (CG32) */
+  double rel_res;        /* final |b - S x| / |b| */
+} ty_kdif_stats;
+/* One backward-Euler step of size dt: residual, symmetrised matrix diag(V/dt) A, solve,
+ * T += dU / Cp. */
+int ty_kdif_implicit_step(ty_mesh* mesh, double dt, const ty_kdif_solve* s, ty_kdif_stats* stats);
+/* Parity access (host): which = 0 T [ncell] (ghosts included), 1 grad T [3][ncell_int],
+ * 2 flux*S [nface], 3 J_R*S [nface], 4 diagonal [ncell_int], 5 flux balance [ncell_int]. */
+int ty_kdif_get(ty_mesh* mesh, int32_t which, double* out);
+/* y = S x with the last assembled symmetrised matrix, host [ncell_int]. */
+int ty_kdif_matvec(ty_mesh* mesh, const double* x, double* y);
+
 /* Global stability time step for callers that cannot let the library allocate device
  * memory (a host code that owns all device memory through its own allocator, a solver loop
  * that must not allocate between steps).  No counterpart in the reference: it computes the

@@ -1,0 +1,126 @@
+"""GPU heat conduction (KDIF) against the oracle, through the C ABI.
+
+Exact mode: ghost temperatures, gradients, face fluxes, Jacobians, the symmetrised
+implicit matrix and its mat-vec are bit for bit the oracle's; the conjugate-gradient
+update agrees with the oracle's to the solve tolerance.  The FP32 conjugate gradients
+inside FP64 iterative refinement reach a 1e-12 relative residual and the FP64 solution.
+"""
+import numpy as np
+import pytest
+
+import oracle_py as op
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ty():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from typhon_gb300 import build
+    build.build()
+    import typhon_gb300
+    return typhon_gb300
+
+
+def box_case(ty, n=6, jitter=0.1, seed=5):
+    from typhon_gb300 import umesh
+    raw = umesh.gen_tet_box(n, 1.0, jitter=jitter, seed=seed)
+    bcs = [(f, umesh.BC_WALL, "", (0, 0, 0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX", "KMIN", "KMAX")]
+    md = ty.preprocess(raw, 3, bcs)
+    om = op.Mesh.from_raw(raw).build(3, bcs)
+    fc = md.face_centre
+    kind = np.zeros(md.nface, np.int32)
+    val = np.zeros(md.nface)
+    for f in range(md.nface_int, md.nface):
+        if abs(fc[f, 0]) < 1e-12:
+            kind[f], val[f] = op.KBC_ISOTHERMAL, 0.0
+        elif abs(fc[f, 0] - 1.0) < 1e-12:
+            kind[f], val[f] = op.KBC_ISOTHERMAL, 1.0
+        elif abs(fc[f, 1]) < 1e-12:
+            kind[f], val[f] = op.KBC_FLUX, 0.25
+        elif abs(fc[f, 1] - 1.0) < 1e-12:
+            kind[f], val[f] = op.KBC_EXTRAPOLATE, 0.0
+        else:
+            kind[f], val[f] = op.KBC_FLUX, 0.0
+    rng = np.random.default_rng(seed)
+    kc = np.exp(0.5 * rng.standard_normal(md.ncell_int))
+    T0 = rng.uniform(0.2, 0.8, md.ncell)
+    return md, om, kind, val, kc, T0
+
+
+@pytest.mark.parametrize("scheme", ["COMPACT", "CELL-AVERAGE", "FULL"])
+def test_exact_kdif_bitwise(ty, scheme):
+    md, om, kind, val, kc, T0 = box_case(ty)
+    osch = {"COMPACT": op.KDIF_COMPACT, "CELL-AVERAGE": op.KDIF_CELLAVG, "FULL": op.KDIF_FULL}[scheme]
+    g = ty.Grid(md)
+    g.set_spat("HLLC", mode="exact")
+    g.kdif_setup(kc, kind, val, flux=scheme, heat_capacity=1.7)
+    g.kdif_set_temperature(T0)
+    k = op.Kdif(om, osch, 1.7, kc, kind, val)
+    k.set_T(T0)
+    dt = 2e-3
+    R = g.kdif_residual(dt)
+    k.rhs(dt)
+    nci = md.ncell_int
+    assert np.array_equal(g.kdif_get("T"), k.get("T")), "ghost temperatures"
+    if scheme != "COMPACT":
+        assert np.array_equal(g.kdif_get("grad"), k.get("grad")[:, :nci]), "gradient"
+    assert np.array_equal(g.kdif_get("flux"), k.get("flux")), "face flux"
+    assert np.array_equal(g.kdif_get("jac"), k.get("jac")), "Jacobian"
+    assert np.array_equal(g.kdif_get("balance"), k.get("balance")), "balance"
+    assert np.array_equal(R, k.get("residu")[:nci]), "residual"
+    st = g.kdif_implicit_step(dt, "CG", tol=1e-13)
+    it, rel = k.implicit_step(dt, tol=1e-13)
+    assert np.array_equal(g.kdif_get("diag"), k.get("diag")), "diagonal"
+    x = np.random.default_rng(1).standard_normal(nci)
+    assert np.array_equal(g.kdif_matvec(x), k.matvec(x)), "mat-vec"
+    assert st["rel_res"] < 1e-13
+    dT, dTo = g.kdif_temperature() - T0[:nci], k.get("T")[:nci] - T0[:nci]
+    assert np.linalg.norm(dT - dTo) / np.linalg.norm(dTo) < 1e-11
+
+
+def test_fp32_cg_with_refinement_reaches_fp64(ty):
+    md, om, kind, val, kc, T0 = box_case(ty, n=8)
+    sols = {}
+    for solver in ("CG", "CG32"):
+        g = ty.Grid(md)
+        g.set_spat("HLLC", mode="fast")
+        g.kdif_setup(kc, kind, val, flux="FULL", heat_capacity=1.0)
+        g.kdif_set_temperature(T0)
+        for _ in range(3):
+            st = g.kdif_implicit_step(1e-2, solver, tol=1e-12)
+            assert st["rel_res"] < 1e-12, st
+        sols[solver] = g.kdif_temperature()
+        if solver == "CG32":
+            assert st["refinements"] >= 2
+    assert np.linalg.norm(sols["CG32"] - sols["CG"]) / np.linalg.norm(sols["CG"]) < 1e-11
+
+
+def test_fast_kdif_close(ty):
+    md, om, kind, val, kc, T0 = box_case(ty)
+    g = ty.Grid(md)
+    g.set_spat("HLLC", mode="fast")
+    g.kdif_setup(kc, kind, val, flux="FULL", heat_capacity=1.0)
+    g.kdif_set_temperature(T0)
+    k = op.Kdif(om, op.KDIF_FULL, 1.0, kc, kind, val)
+    k.set_T(T0)
+    for _ in range(3):
+        g.kdif_implicit_step(5e-3, "CG", tol=1e-13)
+        k.implicit_step(5e-3, tol=1e-13)
+    T, To = g.kdif_temperature(), k.get("T")[:md.ncell_int]
+    assert np.linalg.norm(T - To) / np.linalg.norm(To) < 1e-12
+
+
+def test_kdif_errors(ty):
+    md, om, kind, val, kc, T0 = box_case(ty, n=2)
+    g = ty.Grid(md)
+    with pytest.raises(ty.TyphonError):
+        g.kdif_residual(1e-3)                        # no set-up
+    bad = kind.copy()
+    bad[md.nface - 1] = 0
+    with pytest.raises(ty.TyphonError):
+        g.kdif_setup(kc, bad, val)                   # boundary face without a kind
+    with pytest.raises(ty.TyphonError):
+        g.kdif_setup(-kc, kind, val)                 # non-positive conductivity

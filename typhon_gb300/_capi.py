@@ -61,6 +61,21 @@ class ImpStats(C.Structure):
                 ("lin_res", C.c_double)]
 
 
+class KdifParams(C.Structure):
+    """ty_kdif_params"""
+    _fields_ = [("flux", C.c_int32), ("reserved", C.c_int32), ("heat_capacity", C.c_double)]
+
+
+class KdifSolve(C.Structure):
+    """ty_kdif_solve"""
+    _fields_ = [("solver", C.c_int32), ("max_it", C.c_int32), ("tol", C.c_double), ("inner_tol", C.c_double)]
+
+
+class KdifStats(C.Structure):
+    """ty_kdif_stats"""
+    _fields_ = [("iterations", C.c_int32), ("refinements", C.c_int32), ("rel_res", C.c_double)]
+
+
 _SIGS = {
     "ty_version": ([], C.c_char_p),
     "ty_error_string": ([C.c_int], C.c_char_p),
@@ -88,6 +103,13 @@ _SIGS = {
     "ty_implicit_step": ([C.c_void_p, C.POINTER(ImpParams), C.POINTER(ImpStats)], C.c_int),
     "ty_implicit_get": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
     "ty_implicit_matvec": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "ty_kdif_setup": ([C.c_void_p, C.POINTER(KdifParams), C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "ty_kdif_set_temperature": ([C.c_void_p, C.c_void_p], C.c_int),
+    "ty_kdif_get_temperature": ([C.c_void_p, C.c_void_p], C.c_int),
+    "ty_kdif_residual": ([C.c_void_p, C.c_double, C.c_void_p], C.c_int),
+    "ty_kdif_implicit_step": ([C.c_void_p, C.c_double, C.POINTER(KdifSolve), C.POINTER(KdifStats)], C.c_int),
+    "ty_kdif_get": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "ty_kdif_matvec": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "ty_umesh_new": ([C.POINTER(C.c_void_p)], C.c_int),
     "ty_umesh_free": ([C.c_void_p], C.c_int),
     "ty_umesh_set_nodes": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),

@@ -309,6 +309,11 @@ int stage_faces(ty_mesh* h) {
   return TY_OK;
 }
 
+int ensure_lsq(ty_mesh* h) {
+  if (h->lsq_gradmeth == TY_GRAD_LSQ) return TY_OK;
+  return build_lsq(h, TY_GRAD_LSQ);
+}
+
 }  // namespace tyi
 
 using namespace tyi;
@@ -471,6 +476,8 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
   // geometry
   h->ccentre.assign(d->cell_centre, d->cell_centre + 3 * (size_t)nc);
   h->fcentre.assign(d->face_centre, d->face_centre + 3 * (size_t)nf);
+  h->fnormal.assign(d->face_normal, d->face_normal + 3 * (size_t)nf);
+  h->cvol.assign(d->cell_volume, d->cell_volume + (size_t)nc);
   std::vector<double> fn(3 * lf, 0.0), fs(lf, 0.0), fw(3 * lf, 0.0), cv(lc, 0.0);
   for (int f = 0; f < nf; ++f) {
     for (int k = 0; k < 3; ++k) {
@@ -514,6 +521,7 @@ int ty_mesh_destroy(ty_mesh* h) {
   for (void* p : h->allocs) cudaFree(p);
   if (h->dtbits_host) cudaFreeHost(h->dtbits_host);
   if (h->imp.pinned) cudaFreeHost(h->imp.pinned);
+  if (h->kd.pinned) cudaFreeHost(h->kd.pinned);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return TY_OK;

@@ -8,6 +8,7 @@
 #include "../../include/typhon_gpu.h"
 #include "devmesh.hpp"
 #include "implicit.hpp"
+#include "kdif.hpp"
 #include "internal.hpp"
 
 namespace tyi {
@@ -50,6 +51,7 @@ struct ty_mesh {
   double* dtbits_host = nullptr;  // pinned
   Prof prof;
   tyk::ImpState imp;  // implicit-step matrices and Krylov workspace (allocated on first use)
+  tyk::KdifState kd;  // heat-conduction state (ty_kdif_setup)
   cudaStream_t own_stream = nullptr;
 
   template <class T>
@@ -81,4 +83,5 @@ int set_dt_slot(ty_mesh* h, int slot, double v); // dtbits[slot] = v (stream-ord
 int ensure_prim(ty_mesh* h);                     // primitive variables of the resident state
 int ready(ty_mesh* h);                           // parameters and state present; device set
 int stage_faces(ty_mesh* h);                     // ghost states .. face fluxes of s.prim
+int ensure_lsq(ty_mesh* h);                      // least-squares factors (LSQ) on the device
 }  // namespace tyi

@@ -4,3 +4,4 @@
 #define TY_FAST 0
 #include "kernels.cuh"
 #include "implicit.cuh"
+#include "kdif.cuh"

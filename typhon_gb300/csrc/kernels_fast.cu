@@ -3,3 +3,4 @@
 #define TY_FAST 1
 #include "kernels.cuh"
 #include "implicit.cuh"
+#include "kdif.cuh"

@@ -33,6 +33,8 @@ DISSIPATIVE_FLUX = {"NONE": 0, "CELL-AVERAGE": 1, "FULL": 2}
 VISC_LAW = {"KINEMATIC-CONSTANT": 0, "SUTHERLAND": 1}
 KRYLOV = {"GMRES": 0, "FGMRES": 1, "JFNK": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
+KDIF_FLUX = {"COMPACT": 0, "CELL-AVERAGE": 1, "FULL": 2}
+KBC_ISOTHERMAL, KBC_FLUX, KBC_EXTRAPOLATE = 1, 2, 3
 
 
 def prim_to_cons(prim, gamma=1.4):
@@ -206,6 +208,55 @@ class Grid:
         x = np.ascontiguousarray(x, np.float64)
         y = np.zeros_like(x)
         _capi.check(self.lib.ty_implicit_matvec(self.h, x.ctypes.data, y.ctypes.data), "ty_implicit_matvec")
+        return y
+
+    # -- heat conduction (SOLVER = HEAT) ------------------------------------------------------
+    def kdif_setup(self, conductivity, face_kind, face_value, flux="FULL", heat_capacity=1.0):
+        """KDIF on this mesh: per-cell conductivity [ncell_int], boundary kind (KBC) and value
+        (wall temperature or imposed flux) per face [nface]; flux COMPACT | CELL-AVERAGE | FULL
+        (SPAT_PARAM:DISSIPATIVE_FLUX), heat_capacity (MODEL:HEATCAPA)."""
+        kc = np.ascontiguousarray(conductivity, np.float64)
+        fk = np.ascontiguousarray(face_kind, np.int32)
+        fv = np.ascontiguousarray(face_value, np.float64)
+        p = _capi.KdifParams(KDIF_FLUX[flux], 0, float(heat_capacity))
+        _capi.check(self.lib.ty_kdif_setup(self.h, C.byref(p), kc.ctypes.data, fk.ctypes.data, fv.ctypes.data),
+                    "ty_kdif_setup")
+
+    def kdif_set_temperature(self, T):
+        t = np.ascontiguousarray(np.asarray(T, np.float64)[:self.nci])
+        _capi.check(self.lib.ty_kdif_set_temperature(self.h, t.ctypes.data), "ty_kdif_set_temperature")
+
+    def kdif_temperature(self):
+        out = np.zeros(self.nci)
+        _capi.check(self.lib.ty_kdif_get_temperature(self.h, out.ctypes.data), "ty_kdif_get_temperature")
+        return out
+
+    def kdif_residual(self, dt):
+        R = np.zeros(self.nci)
+        _capi.check(self.lib.ty_kdif_residual(self.h, float(dt), R.ctypes.data), "ty_kdif_residual")
+        return R
+
+    def kdif_implicit_step(self, dt, solver="CG", tol=1e-12, max_it=20000, inner_tol=1e-5):
+        """One backward-Euler step; solver CG (FP64, Jacobi) or CG32 (FP32 CG inside FP64
+        iterative refinement).  Returns iterations, refinements, final relative residual."""
+        s = _capi.KdifSolve({"CG": 0, "CG32": 1}[solver], int(max_it), float(tol), float(inner_tol))
+        st = _capi.KdifStats()
+        _capi.check(self.lib.ty_kdif_implicit_step(self.h, float(dt), C.byref(s), C.byref(st)),
+                    "ty_kdif_implicit_step")
+        return dict(iterations=st.iterations, refinements=st.refinements, rel_res=st.rel_res)
+
+    def kdif_get(self, which):
+        m = self.mesh
+        code, shape = {"T": (0, (m.ncell,)), "grad": (1, (3, m.ncell_int)), "flux": (2, (m.nface,)),
+                       "jac": (3, (m.nface,)), "diag": (4, (m.ncell_int,)), "balance": (5, (m.ncell_int,))}[which]
+        out = np.zeros(shape)
+        _capi.check(self.lib.ty_kdif_get(self.h, code, out.ctypes.data), "ty_kdif_get")
+        return out
+
+    def kdif_matvec(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        _capi.check(self.lib.ty_kdif_matvec(self.h, x.ctypes.data, y.ctypes.data), "ty_kdif_matvec")
         return y
 
     def debug(self, which):
