@@ -8,10 +8,11 @@ A "step" is one full SSP-RK3 step (3 residual evaluations) of every cell; one
 cell-update = one cell advanced by one step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload tgv3d|vortex2d|ffbox3d-implicit] [--n 64] [--mode fast|exact]
+                  [--workload tgv3d|vortex2d|ffbox3d-implicit|kdif3d] [--n 64] [--mode fast|exact]
 
 --workload ffbox3d-implicit: time to a 1e-10 relative residual of the implicit solvers (FP64
 flexible GMRES, mixed FP32/FP64, FP64 Jacobian-free) on a steady 3D far-field box.
+--workload kdif3d: 50 implicit heat-conduction steps, FP64 CG vs FP32 CG with FP64 refinement.
 
 --impl reference times the CPU restatement of Typhon's solver (oracle/, OpenMP on all
 host cores) on the same configuration: Typhon itself is Fortran and cannot be built here.
@@ -42,7 +43,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="tgv3d", choices=["tgv3d", "vortex2d", "ffbox3d-implicit"])
+    ap.add_argument("--workload", default="tgv3d", choices=["tgv3d", "vortex2d", "ffbox3d-implicit", "kdif3d"])
     ap.add_argument("--n", type=int, default=None, help="cells per direction (default: the workload's)")
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
     ap.add_argument("--e2e-steps", type=int, default=None)
@@ -372,9 +373,64 @@ def run_implicit(args):
     print(json.dumps(out))
 
 
+def run_kdif(args):
+    """Heat conduction: 50 backward-Euler steps of the KDIF config with FP64 conjugate
+    gradients + Jacobi and with FP32 conjugate gradients inside FP64 iterative refinement,
+    both to a 1e-12 relative residual per step.  Wall-clock time of the steps (synchronised),
+    iterations, and the FP32-refined final temperature against the FP64 one."""
+    import torch
+    import typhon_gb300 as ty
+    from typhon_gb300 import build, cases
+    build.build()
+    torch.cuda.set_device(0)
+    w = cases.KDIF3D
+    md, kc, kind, val = cases.make_kdif3d(args.n)
+    nci = md.ncell_int
+    variants, temps = {}, {}
+    with ClockSampler(0) as clk:
+        for name, solver in (("cg_fp64", "CG"), ("cg32_refined", "CG32")):
+            g = ty.Grid(md)
+            g.set_spat("HLLC", mode="fast")
+            g.kdif_setup(kc, kind, val, flux="FULL", heat_capacity=w["heat_capacity"])
+            g.kdif_set_temperature(np.zeros(md.ncell))
+            g.kdif_implicit_step(w["dt"], solver, tol=1e-3)          # warm-up (workspace, clocks)
+            g.kdif_set_temperature(np.zeros(md.ncell))
+            g.synchronize()
+            its, worst = 0, 0.0
+            t0 = time.perf_counter()
+            for _ in range(w["steps"]):
+                st = g.kdif_implicit_step(w["dt"], solver, tol=w["tol"])
+                its += st["iterations"]
+                worst = max(worst, st["rel_res"])
+            g.synchronize()
+            t = time.perf_counter() - t0
+            temps[name] = g.kdif_temperature()
+            variants[name] = {"seconds": round(t, 3), "iterations": its, "worst_rel_res": worst,
+                              "ms_per_step": round(1e3 * t / w["steps"], 3)}
+            g.close()
+    d = temps["cg32_refined"] - temps["cg_fp64"]
+    variants["cg32_refined"]["T_vs_fp64"] = float(np.linalg.norm(d) / np.linalg.norm(temps["cg_fp64"]))
+    out = {"metric": "seconds for 50 implicit KDIF steps to 1e-12, FP32 CG + FP64 refinement", "unit": "s",
+           "value": variants["cg32_refined"]["seconds"], "higher_is_better": False, "n_gpus": 1,
+           "steps": w["steps"], "warmup": 1, "dtype": "f64+f32", "data": "synthetic", "scaling": "weak",
+           "vs_baseline": None,
+           "config": {"workload": f"kdif3d {args.n or w['n']}^3x6 tets, lognormal k with 8 inclusions x100",
+                      "cells": nci, "dt": w["dt"], "flux": "FULL"},
+           "variants": variants,
+           "speedup_cg32_vs_fp64": round(variants["cg_fp64"]["seconds"] / variants["cg32_refined"]["seconds"], 3),
+           "clocks": clk.summary()}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "kdif3d":
+        if rank == 0 and args.impl == "ours":
+            run_kdif(args)
+        elif rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the KDIF comparison has no CPU arm"}))
+        return
     if args.workload == "ffbox3d-implicit":
         if rank == 0 and args.impl == "ours":
             run_implicit(args)

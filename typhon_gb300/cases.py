@@ -10,6 +10,8 @@
   ffbox3d    3D steady far-field box for the implicit solvers (FFBOX below): 48^3
              hexahedra split into 5 tetrahedra, far field on all faces, M = 0.3 at 20 degrees,
              Rusanov, a Gaussian bump relaxing to the uniform free stream.
+  kdif3d     3D heat conduction (KDIF3D below): 70^3 x 6 tetrahedra, lognormal
+             conductivity with inclusions, two isothermal faces, implicit Euler.
 All are nondimensional (rho_inf = 1).  The initial states are evaluated at cell centres.
 """
 import numpy as np
@@ -69,6 +71,38 @@ def make_ffbox(n=None):
     raw = umesh.gen_tet_box(n, w["length"], jitter=w["jitter"], seed=w["seed"])
     bcs = [(f, umesh.BC_FARFIELD, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX", "KMIN", "KMAX")]
     return umesh.preprocess(raw, 3, bcs)
+
+
+# 3D heat conduction: unit cube of 70^3 hexahedra x 6 tetrahedra (2,058,000 cells), seeded
+# lognormal conductivity (sigma = 1) with 8 random spherical inclusions of radius 0.1 at 100x,
+# T = 0 / 1 on the x faces, adiabatic elsewhere, backward Euler dt = 1e-3 for 50 steps.
+KDIF3D = dict(n=70, sigma=1.0, inclusions=8, radius=0.1, contrast=100.0, seed=1234, dt=1e-3, steps=50,
+              heat_capacity=1.0, tol=1e-12)
+
+
+def make_kdif3d(n=None):
+    """Mesh (MeshDesc), per-cell conductivity, boundary kinds and values of KDIF3D."""
+    w = KDIF3D
+    n = n or w["n"]
+    raw = umesh.gen_kuhn_box(n, 1.0)
+    bcs = [(f, umesh.BC_WALL, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX", "KMIN", "KMAX")]
+    md = umesh.preprocess(raw, 3, bcs)
+    rng = np.random.default_rng(w["seed"])
+    nci = md.ncell_int
+    k = np.exp(w["sigma"] * rng.standard_normal(nci))
+    cc = md.cell_centre[:nci]
+    for c in rng.uniform(w["radius"], 1.0 - w["radius"], size=(w["inclusions"], 3)):
+        k[((cc - c) ** 2).sum(1) < w["radius"] ** 2] *= w["contrast"]
+    kind = np.zeros(md.nface, np.int32)
+    val = np.zeros(md.nface)
+    fc = md.face_centre
+    b = np.arange(md.nface_int, md.nface)
+    kind[b] = 2                                       # imposed flux 0: adiabatic
+    x0 = b[np.abs(fc[b, 0]) < 1e-12]
+    x1 = b[np.abs(fc[b, 0] - 1.0) < 1e-12]
+    kind[x0], val[x0] = 1, 0.0                        # isothermal T = 0
+    kind[x1], val[x1] = 1, 1.0                        # isothermal T = 1
+    return md, k, kind, val
 
 
 WORKLOADS = {

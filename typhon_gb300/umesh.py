@@ -388,6 +388,53 @@ def gen_flatplate(nx=200, nz=20, n_prism=50, n_tet=25, x0=-0.5, x1=1.0, width=0.
     return RawMesh(vtex=vt, sections=secs, marks=marks)
 
 
+def gen_kuhn_box(n, length=1.0):
+    """n^3 hexahedra on [0, length]^3, each split into 6 tetrahedra along its
+    (0,0,0)-(1,1,1) diagonal (the Kuhn split: conforming, every face cut along its
+    lowest-to-highest-corner diagonal).  Boundary triangles are marked IMIN/IMAX (x),
+    JMIN/JMAX (y), KMIN/KMAX (z)."""
+    g = np.arange(n + 1) * (length / n)
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    vt = np.stack([X, Y, Z], axis=-1).reshape(-1, 3).astype(np.float64)
+
+    def vid(i, j, k):
+        return (i * (n + 1) + j) * (n + 1) + k + 1
+
+    I, J, K = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    I, J, K = I.reshape(-1), J.reshape(-1), K.reshape(-1)
+    axes = {"x": (1, 0, 0), "y": (0, 1, 0), "z": (0, 0, 1)}
+    tets = []
+    for perm in ("xyz", "xzy", "yxz", "yzx", "zxy", "zyx"):
+        p0 = np.zeros(3, int)
+        path = [p0.copy()]
+        for a in perm[:2]:
+            p0 = p0 + np.array(axes[a])
+            path.append(p0.copy())
+        path.append(np.array((1, 1, 1)))
+        tets.append(np.stack([vid(I + d[0], J + d[1], K + d[2]) for d in path], axis=1))
+    tets = np.stack(tets, axis=1).reshape(-1, 4).astype(np.int32)
+    a, b, c, d = (vt[tets[:, q] - 1] for q in range(4))
+    neg = np.einsum("ij,ij->i", np.cross(b - a, c - a), d - a) < 0
+    tets[neg, 1], tets[neg, 2] = tets[neg, 2].copy(), tets[neg, 1].copy()
+    fl = np.concatenate([tets[:, [0, 2, 1]], tets[:, [0, 1, 3]], tets[:, [1, 2, 3]], tets[:, [2, 0, 3]]])
+    key = np.sort(fl, axis=1)
+    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    bnd = fl[cnt[inv.reshape(-1)] == 1]
+    cen = vt[bnd - 1].mean(axis=1)
+    tol = 1e-9 * length
+    faces, marks, nextid = [], [], 1
+    for name, ax, v in (("IMIN", 0, 0.0), ("IMAX", 0, length), ("JMIN", 1, 0.0), ("JMAX", 1, length),
+                        ("KMIN", 2, 0.0), ("KMAX", 2, length)):
+        sel = bnd[np.abs(cen[:, ax] - v) < tol]
+        faces.append(sel)
+        marks.append((name, np.arange(nextid, nextid + len(sel), dtype=np.int32)))
+        nextid += len(sel)
+    fconn = np.concatenate(faces).astype(np.int32)
+    secs = [(ELEM_TETRA4, np.arange(1, len(tets) + 1, dtype=np.int32), tets),
+            (ELEM_TRI3, np.arange(1, len(fconn) + 1, dtype=np.int32), fconn)]
+    return RawMesh(vtex=vt, sections=secs, marks=marks)
+
+
 def flatplate_bcs(wall_velocity=(0.0, 0.0, 0.0)):
     """Adiabatic no-slip plate, symmetry upstream of it and on the span sides, far field
     at the inlet, outlet and top."""
