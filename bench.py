@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-sample-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kdif-inner-tol", type=float, default=1e-3, help="kdif3d: FP32 inner CG tolerance")
+    ap.add_argument("--kdif-inner-max", type=int, default=300, help="kdif3d: FP32 inner CG iterations at most")
     return ap.parse_args()
 
 
@@ -399,7 +401,11 @@ def run_kdif(args):
             its, worst = 0, 0.0
             t0 = time.perf_counter()
             for _ in range(w["steps"]):
-                st = g.kdif_implicit_step(w["dt"], solver, tol=w["tol"])
+                if solver == "CG":
+                    st = g.kdif_implicit_step(w["dt"], solver, tol=w["tol"])
+                else:
+                    st = g.kdif_implicit_step(w["dt"], solver, tol=w["tol"], max_it=args.kdif_inner_max,
+                                              inner_tol=args.kdif_inner_tol)
                 its += st["iterations"]
                 worst = max(worst, st["rel_res"])
             g.synchronize()
@@ -415,7 +421,8 @@ def run_kdif(args):
            "steps": w["steps"], "warmup": 1, "dtype": "f64+f32", "data": "synthetic", "scaling": "weak",
            "vs_baseline": None,
            "config": {"workload": f"kdif3d {args.n or w['n']}^3x6 tets, lognormal k with 8 inclusions x100",
-                      "cells": nci, "dt": w["dt"], "flux": "FULL"},
+                      "cells": nci, "dt": w["dt"], "flux": "FULL",
+                      "inner": f"FP32 CG to {args.kdif_inner_tol:g} or {args.kdif_inner_max} iterations"},
            "variants": variants,
            "speedup_cg32_vs_fp64": round(variants["cg_fp64"]["seconds"] / variants["cg32_refined"]["seconds"], 3),
            "clocks": clk.summary()}
