@@ -296,6 +296,18 @@ int ty_kdif_get(ty_mesh* mesh, int32_t which, double* out);
 /* y = S x with the last assembled symmetrised matrix, host [ncell_int]. */
 int ty_kdif_matvec(ty_mesh* mesh, const double* x, double* y);
 
+/* ---------------------------------------------------------------------------------
+ * Adjoint (new: Typhon has no adjoint).  Both calls act on the resident state set by
+ * ty_state_upload_device and work on caller DEVICE buffers [5][ncell_int] (rho, rhoE, rhou,
+ * rhov, rhow), queued on the handle's stream.
+ *   ty_residual_device: R = dt/V sum(+-F S), ty_residual's value.
+ *   ty_adjoint_vjp:     lambda_U = (dR/dU)^T lambda_R of the first-order inviscid residual
+ *                       (HIGHRES = NONE, no viscous flux; TY_ERR_UNSUPPORTED otherwise):
+ *                       a reversed face loop (face products with dual-number flux
+ *                       Jacobians, then a per-cell gather). */
+int ty_residual_device(ty_mesh* mesh, double dt, double* R);
+int ty_adjoint_vjp(ty_mesh* mesh, double dt, const double* lambda_R, double* lambda_U);
+
 /* Global stability time step for callers that cannot let the library allocate device
  * memory (a host code that owns all device memory through its own allocator, a solver loop
  * that must not allocate between steps).  No counterpart in the reference: it computes the

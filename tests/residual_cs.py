@@ -1,0 +1,119 @@
+"""Complex-step reference of the first-order residual (test infrastructure).
+
+A numpy restatement of the first-order residual R = dt/V sum(+-F S) (Rusanov and Roe
+fluxes, periodic and symmetry boundaries) written so that it is analytic in the state: the
+absolute value is z sign(Re z), max/min compare real parts, the square root is the complex
+one.  Evaluated at U + i h d it gives dR/dU d to machine precision (complex step), and with
+the Runge-Kutta tables of typhon_gb300.adjoint the derivative of a whole explicit run.
+"""
+import numpy as np
+
+
+def cabs(z):
+    return z * np.sign(z.real)
+
+
+def cmax(a, b):
+    return np.where(a.real >= b.real, a, b)
+
+
+def prim(U, g):
+    rho = U[0]
+    u, v, w = U[2] / rho, U[3] / rho, U[4] / rho
+    p = (g - 1.0) * (U[1] - 0.5 * rho * (u * u + v * v + w * w))
+    return np.stack([rho, p, u, v, w])
+
+
+def rusanov(L, R, n, g):
+    ig1 = 1.0 / (g - 1.0)
+    vnl = L[2] * n[0] + L[3] * n[1] + L[4] * n[2]
+    vnr = R[2] * n[0] + R[3] * n[1] + R[4] * n[2]
+    al, ar = np.sqrt(g * L[1] / L[0]), np.sqrt(g * R[1] / R[0])
+    ray = cmax(cabs(vnl) + al, cabs(vnr) + ar)
+    rel = ig1 * L[1] + 0.5 * L[0] * (L[2] ** 2 + L[3] ** 2 + L[4] ** 2)
+    rer = ig1 * R[1] + 0.5 * R[0] * (R[2] ** 2 + R[3] ** 2 + R[4] ** 2)
+    a, b = (vnl + ray) * L[0], (vnr - ray) * R[0]
+    F = [0.5 * (a + b), 0.5 * ((vnl + ray) * rel + (vnr - ray) * rer + vnl * L[1] + vnr * R[1])]
+    for k in range(3):
+        F.append(0.5 * ((a * L[2 + k] + b * R[2 + k]) + (L[1] + R[1]) * n[k]))
+    return np.stack(F)
+
+
+def roe(L, R, n, g, eps=0.1):
+    ig1, gig1 = 1.0 / (g - 1.0), g / (g - 1.0)
+    t1 = np.sqrt(R[0] / L[0])
+    rroe = L[0] * t1
+    kl = 1.0 / (1.0 + t1)
+    kr = t1 * kl
+    u = [kl * L[2 + k] + kr * R[2 + k] for k in range(3)]
+    sqL = L[2] ** 2 + L[3] ** 2 + L[4] ** 2
+    sqR = R[2] ** 2 + R[3] ** 2 + R[4] ** 2
+    hroe = kl * (gig1 * L[1] / L[0] + 0.5 * sqL) + kr * (gig1 * R[1] / R[0] + 0.5 * sqR)
+    q2 = u[0] ** 2 + u[1] ** 2 + u[2] ** 2
+    a2 = (g - 1.0) * (hroe - 0.5 * q2)
+    a = np.sqrt(a2)
+    vn = u[0] * n[0] + u[1] * n[1] + u[2] * n[2]
+    vnl = L[2] * n[0] + L[3] * n[1] + L[4] * n[2]
+    vnr = R[2] * n[0] + R[3] * n[1] + R[4] * n[2]
+    rel = ig1 * L[1] + 0.5 * L[0] * sqL
+    rer = ig1 * R[1] + 0.5 * R[0] * sqR
+    drho, dp, dvn = R[0] - L[0], R[1] - L[1], vnr - vnl
+    du = [R[2 + k] - L[2 + k] for k in range(3)]
+    al1 = (dp - rroe * a * dvn) / (2.0 * a2)
+    al5 = (dp + rroe * a * dvn) / (2.0 * a2)
+    al2 = drho - dp / a2
+    dut = [du[k] - dvn * n[k] for k in range(3)]
+    l1, l5, l2 = cabs(vn - a), cabs(vn + a), cabs(vn)
+    delta = eps * a
+    l1 = np.where(l1.real < delta.real, (l1 * l1 + delta * delta) / (2.0 * delta), l1)
+    l5 = np.where(l5.real < delta.real, (l5 * l5 + delta * delta) / (2.0 * delta), l5)
+    w1, w2, w5, ws = l1 * al1, l2 * al2, l5 * al5, l2 * rroe
+    dm = [w1 * (u[k] - a * n[k]) + w2 * u[k] + w5 * (u[k] + a * n[k]) + ws * dut[k] for k in range(3)]
+    de = w1 * (hroe - a * vn) + w2 * (0.5 * q2) + w5 * (hroe + a * vn) + ws * (
+        (u[0] * du[0] + u[1] * du[1] + u[2] * du[2]) - vn * dvn)
+    ml, mr = vnl * L[0], vnr * R[0]
+    F = [0.5 * (ml + mr - (w1 + w2 + w5)), 0.5 * (vnl * (rel + L[1]) + vnr * (rer + R[1]) - de)]
+    for k in range(3):
+        F.append(0.5 * ((ml * L[2 + k] + L[1] * n[k]) + (mr * R[2 + k] + R[1] * n[k]) - dm[k]))
+    return np.stack(F)
+
+
+def residual(md, U, dt, scheme="RUSANOV", g=1.4):
+    """R [5, ncell_int] of the first-order residual at U [5, ncell_int] (real or complex)."""
+    nci, nf, nfi = md.ncell_int, md.nface, md.nface_int
+    fc1, fc2 = md.fc1, md.fc2
+    P = prim(U, g)
+    QL = P[:, fc1]
+    right = np.where(np.arange(nf) < nfi, fc2, 0)
+    QR = P[:, np.minimum(right, nci - 1)].copy()
+    n = md.face_normal.T
+    b = np.arange(nfi, nf)
+    per = b[md.face_bc[b] == 1]
+    QR[:, per] = P[:, fc1[md.face_partner[per] - 1]]
+    sym = b[md.face_bc[b] == 2]
+    dn = 2.0 * (QL[2, sym] * n[0, sym] + QL[3, sym] * n[1, sym] + QL[4, sym] * n[2, sym])
+    QR[:, sym] = QL[:, sym]
+    for k in range(3):
+        QR[2 + k, sym] = QL[2 + k, sym] - dn * n[k, sym]
+    F = (rusanov if scheme == "RUSANOV" else roe)(QL, QR, n, g) * md.face_surface
+    R = np.zeros((5, nci), dtype=U.dtype)
+    np.subtract.at(R.T, fc1, F.T)
+    inner = np.arange(nfi)
+    np.add.at(R.T, fc2[inner], F[:, inner].T)
+    return dt / md.cell_volume[:nci] * R
+
+
+def rk_run(md, U0, dts, table, scheme="RUSANOV"):
+    U = U0
+    for dt in dts:
+        Rs = []
+        for k in range(len(table)):
+            Uk = U.copy()
+            for s in range(k):
+                if table[k - 1][s] != 0.0:
+                    Uk = Uk + table[k - 1][s] * Rs[s]
+            Rs.append(residual(md, Uk, dt, scheme))
+        for s, c in enumerate(table[-1]):
+            if c != 0.0:
+                U = U + c * Rs[s]
+    return U

@@ -1,0 +1,119 @@
+"""GPU adjoint of the first-order residual and of explicit runs.
+
+* ty_adjoint_vjp against central finite differences of ty_residual_device (periodic,
+  symmetry and far-field boundaries; HLLC, Rusanov, Roe; exact and fast modes).
+* The gradient of J = sum over a sub-box of rho^2 V after an RK3-SSP run, through
+  typhon_gb300.adjoint (binomial checkpointing, torch.autograd), against the complex-step
+  derivative of the numpy restatement in tests/residual_cs.py: agreement to 1e-8.
+"""
+import numpy as np
+import pytest
+
+import oracle_py as op
+import residual_cs as cs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from typhon_gb300 import build
+    build.build()
+    import typhon_gb300 as ty
+    from typhon_gb300 import adjoint
+    return torch, ty, adjoint
+
+
+def jittered(ty, n=10):
+    raw = ty.gen_grid2d(n, n, 1.0, 1.0, "tri", jitter=0.1, seed=3)
+    return ty.preprocess(raw, 2, op.PERIODIC_UNIT_SQUARE)
+
+
+def smooth_cons(ty, md, amp=0.1):
+    x, y = md.cell_centre[:md.ncell_int, 0], md.cell_centre[:md.ncell_int, 1]
+    t = 2 * np.pi
+    prim = np.stack([1 + amp * np.sin(t * x + 0.3) * np.sin(t * y + 1.1), (1 + amp * np.cos(t * (x + y))) / 1.4,
+                     0.3 + amp * np.sin(t * y + 0.5), 0.2 * np.cos(t * x + 0.7), 0.05 * np.sin(t * x)])
+    return ty.prim_to_cons(prim)
+
+
+CASES = [("periodic", "HLLC"), ("periodic", "RUSANOV"), ("periodic", "ROE"), ("symmetry", "ROE"),
+         ("farfield", "HLLC")]
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+@pytest.mark.parametrize("bc,scheme", CASES)
+def test_vjp_matches_finite_differences(env, golden_dir, bc, scheme, mode):
+    torch, ty, adjoint = env
+    if bc == "periodic":
+        md = jittered(ty)
+    else:
+        kind = op.BC_SYMMETRY if bc == "symmetry" else op.BC_FARFIELD
+        md = ty.preprocess(ty.read_tym(golden_dir / "quad20x10.tym"), 2,
+                           [(f, kind, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX")])
+    g = ty.Grid(md)
+    g.set_spat(scheme, mode=mode, farfield=(1.0, 1.0 / 1.4, 0.3, 0.1, 0.0))
+    st = adjoint.Stepper(g, "RK3-SSP")
+    U = torch.tensor(smooth_cons(ty, md), device="cuda")
+    rng = np.random.default_rng(0)
+    lamR = torch.tensor(rng.standard_normal(U.shape), device="cuda")
+    d = torch.tensor(rng.standard_normal(U.shape), device="cuda") * U.abs().mean(dim=1, keepdim=True)
+    dt = 1e-3
+    lamU = st.vjp(U, dt, lamR)
+    eps = 1e-6
+    fd = ((st.residual(U + eps * d, dt) - st.residual(U - eps * d, dt)) * lamR).sum() / (2 * eps)
+    ad = (lamU * d).sum()
+    assert abs(float(fd - ad)) <= 1e-7 * abs(float(ad)), (float(fd), float(ad))
+    g.close()
+
+
+@pytest.mark.parametrize("scheme", ["RUSANOV", "ROE"])
+def test_unsteady_gradient_against_complex_step(env, scheme):
+    torch, ty, adjoint = env
+    md = jittered(ty, 8)
+    g = ty.Grid(md)
+    g.set_spat(scheme, mode="exact")
+    U0 = smooth_cons(ty, md)
+    dts = [2e-3] * 12
+    nci = md.ncell_int
+    cc = md.cell_centre[:nci]
+    box = ((np.abs(cc[:, 0] - 0.5) < 0.25) & (np.abs(cc[:, 1] - 0.5) < 0.25)).astype(float)
+    V = md.cell_volume[:nci]
+    Ut = torch.tensor(U0, device="cuda", requires_grad=True)
+    Uf = adjoint.rk_solve(Ut, g, "RK3-SSP", dts, snaps=3)
+    w = torch.tensor(box * V, device="cuda")
+    J = (Uf[0] ** 2 * w).sum()
+    J.backward()
+    grad = Ut.grad.cpu().numpy()
+    # the same run on the host, real: the final states agree
+    Uf_np = cs.rk_run(md, U0, dts, adjoint.RK_TABLES["RK3-SSP"], scheme)
+    assert np.allclose(Uf.detach().cpu().numpy(), Uf_np, rtol=1e-11, atol=0)
+    # complex-step directional derivatives
+    rng = np.random.default_rng(4)
+    for _ in range(3):
+        d = rng.standard_normal(U0.shape) * np.abs(U0).mean(axis=1, keepdims=True)
+        h = 1e-30
+        Uc = cs.rk_run(md, U0 + 1j * h * d, dts, adjoint.RK_TABLES["RK3-SSP"], scheme)
+        dJ = float(np.sum(box * V * Uc[0] ** 2).imag / h)
+        ad = float(np.sum(grad * d))
+        assert abs(ad - dJ) <= 1e-8 * abs(dJ), (ad, dJ)
+    # fewer snapshots, same gradient
+    Ut2 = torch.tensor(U0, device="cuda", requires_grad=True)
+    J2 = (adjoint.rk_solve(Ut2, g, "RK3-SSP", dts, snaps=0)[0] ** 2 * w).sum()
+    J2.backward()
+    assert torch.allclose(Ut2.grad, Ut.grad, rtol=1e-13, atol=0)
+    g.close()
+
+
+def test_adjoint_rejects_second_order(env):
+    torch, ty, adjoint = env
+    md = jittered(ty, 4)
+    g = ty.Grid(md)
+    g.set_spat("HLLC", "MUSCL", "ALBADA")
+    st = adjoint.Stepper(g, "RK2")
+    U = torch.tensor(smooth_cons(ty, md), device="cuda")
+    with pytest.raises(ty.TyphonError):
+        st.vjp(U, 1e-3, torch.ones_like(U))

@@ -110,6 +110,8 @@ _SIGS = {
     "ty_kdif_implicit_step": ([C.c_void_p, C.c_double, C.POINTER(KdifSolve), C.POINTER(KdifStats)], C.c_int),
     "ty_kdif_get": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
     "ty_kdif_matvec": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "ty_residual_device": ([C.c_void_p, C.c_double, C.c_void_p], C.c_int),
+    "ty_adjoint_vjp": ([C.c_void_p, C.c_double, C.c_void_p, C.c_void_p], C.c_int),
     "ty_umesh_new": ([C.POINTER(C.c_void_p)], C.c_int),
     "ty_umesh_free": ([C.c_void_p], C.c_int),
     "ty_umesh_set_nodes": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),

@@ -1,0 +1,60 @@
+// Residual on device buffers and its adjoint (vector-Jacobian product), C ABI.
+//
+// Both act on the handle's resident state U (ty_state_upload_device): ty_residual_device
+// writes R = dt/V sum(+-F S) (ty_residual's value) to a caller device buffer, and
+// ty_adjoint_vjp writes lambda_U = (dR/dU)^T lambda_R for the first-order residual
+// (HIGHRES = NONE, inviscid).  New: Typhon has no adjoint; the unsteady gradient of a
+// functional (RK stages, checkpointing, torch.autograd) is composed from these two calls in
+// typhon_gb300/adjoint.py.
+#include <vector>
+
+#include "handle.hpp"
+
+using namespace tyk;
+using namespace tyi;
+
+#define ADJ_CALL(h, fn, ...) \
+  ((h)->o.mode == TY_MODE_FAST ? tyk::kfast::fn(__VA_ARGS__) : tyk::kexact::fn(__VA_ARGS__))
+
+extern "C" {
+
+int ty_residual_device(ty_mesh* h, double dt, double* R) {
+  int rc;
+  if ((rc = ready(h))) return rc;
+  if (!R) return TY_ERR_ARG;
+  if ((rc = ensure_prim(h))) return rc;
+  if ((rc = stage_faces(h))) return rc;
+  cudaError_t e = ADJ_CALL(h, residual_gather, h->m, h->s, dt, nullptr, h->stream, &h->prof);
+  if (e != cudaSuccess) return cuda_fail(e, "residual gather");
+  const size_t n = h->m.nci;
+  TY_CU(cudaMemcpy2DAsync(R, n * sizeof(double), h->s.res, h->m.ldc * sizeof(double), n * sizeof(double), 5,
+                          cudaMemcpyDeviceToDevice, h->stream));
+  return TY_OK;
+}
+
+int ty_adjoint_vjp(ty_mesh* h, double dt, const double* lamR, double* lamU) {
+  if (int rc = ready(h)) return rc;
+  if (!lamR || !lamU) return TY_ERR_ARG;
+  if (h->o.highres != TY_HRES_NONE || h->o.viscous != TY_VISC_NONE) {
+    tyi::set_error("ty_adjoint_vjp: first-order inviscid residual only (HIGHRES = NONE, no viscous flux)");
+    return TY_ERR_UNSUPPORTED;
+  }
+  DevMesh& m = h->m;
+  int rc;
+  if (!h->adj_face) {
+    if ((rc = h->alloc(h->adj_face, 10 * (size_t)m.ldf)) || (rc = h->alloc(h->adj_buf, 10 * (size_t)m.ldc)))
+      return rc;
+  }
+  const size_t n = m.nci, ld = m.ldc;
+  double* bR = h->adj_buf;
+  double* bU = h->adj_buf + 5 * ld;
+  TY_CU(cudaMemcpy2DAsync(bR, ld * sizeof(double), lamR, n * sizeof(double), n * sizeof(double), 5,
+                          cudaMemcpyDeviceToDevice, h->stream));
+  cudaError_t e = ADJ_CALL(h, adjoint_vjp, m, h->o, h->s.u0, bR, dt, h->adj_face, bU, h->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint");
+  TY_CU(cudaMemcpy2DAsync(lamU, n * sizeof(double), bU, ld * sizeof(double), n * sizeof(double), 5,
+                          cudaMemcpyDeviceToDevice, h->stream));
+  return TY_OK;
+}
+
+}  // extern "C"

@@ -9,6 +9,7 @@
 #include "devmesh.hpp"
 #include "implicit.hpp"
 #include "kdif.hpp"
+#include "adjoint.hpp"
 #include "internal.hpp"
 
 namespace tyi {
@@ -52,6 +53,8 @@ struct ty_mesh {
   Prof prof;
   tyk::ImpState imp;  // implicit-step matrices and Krylov workspace (allocated on first use)
   tyk::KdifState kd;  // heat-conduction state (ty_kdif_setup)
+  double* adj_face = nullptr;  // [10][ldf] adjoint face products (first use)
+  double* adj_buf = nullptr;   // [2][5][ldc] adjoint staging
   cudaStream_t own_stream = nullptr;
 
   template <class T>

@@ -5,3 +5,4 @@
 #include "kernels.cuh"
 #include "implicit.cuh"
 #include "kdif.cuh"
+#include "adjoint.cuh"
