@@ -181,7 +181,8 @@ int ty_synchronize(ty_mesh* mesh);
 
 /* Run the handle's work on the caller's CUDA stream (a cudaStream_t of the handle's
  * device, e.g. a PyTorch stream), or on the handle's own stream again when stream is NULL.
- * Waits for work already queued on the previous stream. */
+ * The legacy default stream is named by cudaStreamLegacy ((void*)1), since NULL means the
+ * handle's own stream.  Waits for work already queued on the previous stream. */
 int ty_set_stream(ty_mesh* mesh, void* stream);
 
 /* Per-kernel CUDA-event timing of every launch issued while enabled (enabling clears the

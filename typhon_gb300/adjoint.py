@@ -53,7 +53,10 @@ class Stepper:
         self.n = len(self.table)
         self.nci = grid.nci
         self.stream = torch.cuda.current_stream()
-        _capi.check(self.lib.ty_set_stream(grid.h, C.c_void_p(self.stream.cuda_stream)), "ty_set_stream")
+        # torch's default stream is the legacy default stream (handle 0), which the library
+        # takes as "its own stream": name it by cudaStreamLegacy (1) instead
+        handle = self.stream.cuda_stream or 1
+        _capi.check(self.lib.ty_set_stream(grid.h, C.c_void_p(handle)), "ty_set_stream")
 
     def _set(self, U):
         _capi.check(self.lib.ty_state_upload_device(self.g.h, C.c_void_p(U.data_ptr())), "ty_state_upload_device")
