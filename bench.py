@@ -8,11 +8,12 @@ A "step" is one full SSP-RK3 step (3 residual evaluations) of every cell; one
 cell-update = one cell advanced by one step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload tgv3d|vortex2d|ffbox3d-implicit|kdif3d] [--n 64] [--mode fast|exact]
+                  [--workload tgv3d|vortex2d|ffbox3d-implicit|kdif3d|adjoint3d] [--n 64] [--mode fast|exact]
 
 --workload ffbox3d-implicit: time to a 1e-10 relative residual of the implicit solvers (FP64
 flexible GMRES, mixed FP32/FP64, FP64 Jacobian-free) on a steady 3D far-field box.
 --workload kdif3d: 50 implicit heat-conduction steps, FP64 CG vs FP32 CG with FP64 refinement.
+--workload adjoint3d: unsteady adjoint gradient, its cost against the primal, FD checks.
 
 --impl reference times the CPU restatement of Typhon's solver (oracle/, OpenMP on all
 host cores) on the same configuration: Typhon itself is Fortran and cannot be built here.
@@ -43,7 +44,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="tgv3d", choices=["tgv3d", "vortex2d", "ffbox3d-implicit", "kdif3d"])
+    ap.add_argument("--workload", default="tgv3d", choices=["tgv3d", "vortex2d", "ffbox3d-implicit", "kdif3d", "adjoint3d"])
     ap.add_argument("--n", type=int, default=None, help="cells per direction (default: the workload's)")
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
     ap.add_argument("--e2e-steps", type=int, default=None)
@@ -429,9 +430,89 @@ def run_kdif(args):
     print(json.dumps(out))
 
 
+def run_adjoint(args):
+    """Unsteady adjoint: primal run (library RK steps and the same steps composed through the
+    device residual), the gradient of J by the adjoint with binomial checkpointing, its cost
+    against the primal, and seeded directional derivatives against central finite
+    differences."""
+    import torch
+    import typhon_gb300 as ty
+    from typhon_gb300 import adjoint, build, cases
+    build.build()
+    torch.cuda.set_device(0)
+    w = cases.ADJOINT3D
+    n = args.n or w["n"]
+    md = cases.make_mesh("tgv3d", n)
+    nci = md.ncell_int
+    prim = cases.taylor_green(md.cell_centre)
+    g = ty.Grid(md)
+    g.set_spat(w["scheme"], mode="fast")
+    g.set_prim(prim)
+    dt = g.calc_zonetimestep(w["cfl"])
+    dts = [dt] * w["steps"]
+    U0 = torch.tensor(ty.prim_to_cons(prim[:, :nci]), device="cuda")
+    cc = md.cell_centre[:nci]
+    L = 2 * np.pi
+    box = np.all(np.abs(cc - L / 2) < L / 4, axis=1).astype(float) * md.cell_volume[:nci]
+    wbox = torch.tensor(box, device="cuda")
+    st = adjoint.Stepper(g, w["rk"])
+
+    def J_of(U):
+        return float((U[0] ** 2 * wbox).sum())
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    with ClockSampler(0) as clk:
+        adjoint.forward_steps(st, U0, dts[:2])                            # warm-up
+        Uf, t_primal = timed(lambda: adjoint.forward_steps(st, U0, dts))
+        # the library's own fused RK steps on the same fixed dt (the optimised primal)
+        g.set_cons_device(U0.data_ptr())
+        g.synchronize()
+        t0 = time.perf_counter()
+        for d in dts:
+            g.treelevel_rungekutta(w["rk"], d)
+        g.synchronize()
+        t_lib = time.perf_counter() - t0
+        lam = (2.0 * Uf[0] * wbox).unsqueeze(0) * torch.tensor([1.0, 0, 0, 0, 0], device="cuda").unsqueeze(1)
+        grad, t_adj = timed(lambda: adjoint.adjoint_steps(st, U0, dts, lam.contiguous(), w["snaps"]))
+    rng = np.random.default_rng(w["seed"])
+    errs = []
+    J0 = J_of(Uf)
+    for _ in range(w["directions"]):
+        d = torch.tensor(rng.standard_normal((5, nci)), device="cuda") * U0.abs().mean(dim=1, keepdim=True)
+        eps = 1e-6
+        Jp = J_of(adjoint.forward_steps(st, U0 + eps * d, dts))
+        Jm = J_of(adjoint.forward_steps(st, U0 - eps * d, dts))
+        fd = (Jp - Jm) / (2 * eps)
+        ad = float((grad * d).sum())
+        errs.append(abs(ad - fd) / max(abs(fd), 1e-300))
+    out = {"metric": "adjoint / primal time, unsteady gradient of int rho^2 (20 stored states)", "unit": "ratio",
+           "value": round(t_adj / t_primal, 3), "higher_is_better": False, "n_gpus": 1, "steps": w["steps"],
+           "warmup": 2, "dtype": "f64", "data": "synthetic", "scaling": "weak", "vs_baseline": None,
+           "config": {"workload": f"adjoint3d TGV {n}^3x5 tets, first-order {w['scheme']}, {w['rk']}",
+                      "cells": nci, "dt": dt, "snapshots": w["snaps"], "J": J0},
+           "primal_s": round(t_primal, 4), "primal_library_rk_s": round(t_lib, 4), "adjoint_s": round(t_adj, 4),
+           "adjoint_vs_library_primal": round(t_adj / t_lib, 3),
+           "recomputed_steps": adjoint.checkpoint_cost(w["steps"], w["snaps"]),
+           "fd_check": {"directions": w["directions"], "max_rel_err": max(errs), "median_rel_err": float(np.median(errs))},
+           "clocks": clk.summary()}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "adjoint3d":
+        if rank == 0 and args.impl == "ours":
+            run_adjoint(args)
+        elif rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "Typhon has no adjoint"}))
+        return
     if args.workload == "kdif3d":
         if rank == 0 and args.impl == "ours":
             run_kdif(args)
