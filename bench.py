@@ -235,9 +235,27 @@ def run_ours(args, rank, world, local):
                          "achieved_gbs": round(kb[name] / (avg_ms * 1e-3) / 1e9, 1)}
     dom = max(per, key=lambda k: per[k]["total_ms"])
     ach = per[dom]["achieved_gbs"]
+    # DRAM traffic and FP64 instructions per unit, from one ncu capture of the same kernels on
+    # the 40^3x5 mesh (320,000 cells, 646,400 faces; profiles/cell_fast_face_flux_fast__tgv3d_n40.md),
+    # scaled by the units of this mesh
+    per_unit = {"cell_fast": (nci, (97.1e6 + 54.9e6) / 320000, 349),
+                "face_flux_fast": (md.nface, (72.2e6 + 4.2e6) / 646400, 160)}
+    traffic = None
+    fp64_roof = None
+    if dom in per_unit and args.mode == "fast":
+        units, bpu, ipu = per_unit[dom]
+        traffic = int(bpu * units)
+        peak64 = fp64_peak()
+        if peak64:
+            inst = ipu * units / (per[dom]["avg_ms"] * 1e-3) / 1e12
+            fp64_roof = {"instr_per_unit": ipu, "units": int(units), "achieved_tinstr_s": round(inst, 4),
+                    "peak_tinstr_s": round(peak64 / 2e12, 4), "frac": round(inst / (peak64 / 2e12), 4),
+                    "note": "FP64 instructions (DFMA/DADD/DMUL, one each) per unit counted by ncu; peak = the "
+                            "DFMA instruction rate measured on this GPU by typhon_gb300/_lib/fp64_peak"}
     roofline = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
-                "frac": round(ach / peak, 4), "peak_source": peak_kind, "traffic": None,
-                "algorithmic_bytes_per_launch": int(kb[dom])}
+                "frac": round(ach / peak, 4), "peak_source": peak_kind, "traffic": traffic,
+                "traffic_source": "ncu, 40^3x5 mesh, scaled by units" if traffic else None,
+                "algorithmic_bytes_per_launch": int(kb[dom]), "fp64_pipe": fp64_roof}
     # end to end through the public API with host buffers, per step: H2D of the state from
     # pinned host memory (Typhon's layout: rho, rhoE, rhou AoS), one step, D2H of the state
     e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))

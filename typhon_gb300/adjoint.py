@@ -75,8 +75,8 @@ class Stepper:
                                             C.c_void_p(out.data_ptr())), "ty_adjoint_vjp")
         return out
 
-    def stages(self, U0, dt):
-        """Stage states U_1..U_n and residuals R_1..R_n of one step."""
+    def stages(self, U0, dt, last_residual=True):
+        """Stage states U_1..U_n and residuals R_1..R_n of one step (R_n only when asked)."""
         Us, Rs = [], []
         for k in range(self.n):
             U = U0.clone()
@@ -85,7 +85,8 @@ class Stepper:
                 if c != 0.0:
                     U += c * Rs[s]
             Us.append(U)
-            Rs.append(self.residual(U, dt))
+            if k < self.n - 1 or last_residual:
+                Rs.append(self.residual(U, dt))
         return Us, Rs
 
     def step(self, U0, dt):
@@ -97,7 +98,7 @@ class Stepper:
         return U
 
     def step_adjoint(self, U0, dt, lam):
-        Us, _ = self.stages(U0, dt)
+        Us, _ = self.stages(U0, dt, last_residual=False)
         lam_stage = [None] * self.n
         out = lam.clone()
         for s in reversed(range(self.n)):

@@ -236,7 +236,7 @@ __device__ void bc_state_t(const DevMesh& m, const SpatOpts& o, int f, int kind,
   }
 }
 
-template <class T>
+template <int SCH, class T>
 __device__ void face_flux_t(const DevMesh& m, const SpatOpts& o, int f, const T* UL, const T* UR, T* F) {
   T QL[5], QR[5];
   prim_t(o.gamma, UL, QL);
@@ -244,12 +244,13 @@ __device__ void face_flux_t(const DevMesh& m, const SpatOpts& o, int f, const T*
   if (kind == TY_BC_INTERIOR || kind == TY_BC_PERIODIC) prim_t(o.gamma, UR, QR);
   else bc_state_t(m, o, f, kind, QL, QR);
   const double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
-  if (o.scheme == TY_SCH_HLLC) flux_hllc_t(o.gamma, QL, QR, nx, ny, nz, F);
-  else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov_t(o.gamma, QL, QR, nx, ny, nz, F);
+  if constexpr (SCH == TY_SCH_HLLC) flux_hllc_t(o.gamma, QL, QR, nx, ny, nz, F);
+  else if constexpr (SCH == TY_SCH_RUSANOV) flux_rusanov_t(o.gamma, QL, QR, nx, ny, nz, F);
   else flux_roe_t(o.gamma, o.entropy_fix, QL, QR, nx, ny, nz, F);
 }
 
 // per face: lambda_F, then (dF/dU_L)^T lambda_F and (dF/dU_R)^T lambda_F into lam_face [10][ldf]
+template <int SCH>
 __global__ void __launch_bounds__(128) k_adj_face(DevMesh m, SpatOpts o, const double* __restrict__ u,
                                                   const double* __restrict__ lamR, double dt,
                                                   double* __restrict__ lam_face) {
@@ -270,7 +271,14 @@ __global__ void __launch_bounds__(128) k_adj_face(DevMesh m, SpatOpts o, const d
   double uL[5], uR[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) { uL[v] = u[v * ld + c1]; uR[v] = u[v * ld + cr]; }
+  const int nside = (kind == TY_BC_INTERIOR || kind == TY_BC_PERIODIC) ? 2 : 1;
+#pragma unroll 1
   for (int side = 0; side < 2; ++side) {
+    if (side >= nside) {  // the right state is built from the left one: no right product
+#pragma unroll
+      for (int j = 0; j < 5; ++j) lam_face[(5 + j) * lf + f] = 0.0;
+      break;
+    }
     Dual<5> UL[5], UR[5], F[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
@@ -279,7 +287,7 @@ __global__ void __launch_bounds__(128) k_adj_face(DevMesh m, SpatOpts o, const d
       if (side == 0) UL[v].d[v] = 1.0;
       else UR[v].d[v] = 1.0;
     }
-    face_flux_t(m, o, f, UL, UR, F);
+    face_flux_t<SCH>(m, o, f, UL, UR, F);
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
       double s = 0.0;
@@ -314,7 +322,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(DevMesh m, const double* __
 
 cudaError_t adjoint_vjp(const DevMesh& m, const SpatOpts& o, const double* u, const double* lamR, double dt,
                         double* lam_face, double* lamU, cudaStream_t st) {
-  k_adj_face<<<(unsigned)((m.nf + 127) / 128), 128, 0, st>>>(m, o, u, lamR, dt, lam_face);
+  const unsigned gf = (unsigned)((m.nf + 127) / 128);
+  if (o.scheme == TY_SCH_HLLC) k_adj_face<TY_SCH_HLLC><<<gf, 128, 0, st>>>(m, o, u, lamR, dt, lam_face);
+  else if (o.scheme == TY_SCH_RUSANOV) k_adj_face<TY_SCH_RUSANOV><<<gf, 128, 0, st>>>(m, o, u, lamR, dt, lam_face);
+  else k_adj_face<TY_SCH_ROE><<<gf, 128, 0, st>>>(m, o, u, lamR, dt, lam_face);
   k_adj_cell<<<nblk(m.nci), kBlock, 0, st>>>(m, lam_face, lamU);
   return cudaGetLastError();
 }
