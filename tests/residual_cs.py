@@ -1,6 +1,6 @@
 """Complex-step reference of the first-order residual (test infrastructure).
 
-A numpy restatement of the first-order residual R = dt/V sum(+-F S) (Rusanov and Roe
+A numpy restatement of the first-order residual R = dt/V sum(+-F S) (Rusanov, HLLC and Roe
 fluxes, periodic and symmetry boundaries) written so that it is analytic in the state: the
 absolute value is z sign(Re z), max/min compare real parts, the square root is the complex
 one.  Evaluated at U + i h d it gives dR/dU d to machine precision (complex step), and with
@@ -37,6 +37,53 @@ def rusanov(L, R, n, g):
     for k in range(3):
         F.append(0.5 * ((a * L[2 + k] + b * R[2 + k]) + (L[1] + R[1]) * n[k]))
     return np.stack(F)
+
+
+def cmin(a, b):
+    return np.where(b.real < a.real, b, a)
+
+
+def hllc(L, R, n, g):
+    """HLLC with Roe-averaged wave-speed estimates (SOURCE/VALE/calc_flux_hllc.f90)."""
+    ig1, gig1 = 1.0 / (g - 1.0), g / (g - 1.0)
+    t1 = np.sqrt(R[0] / L[0])
+    roe_rho = L[0] * t1
+    kl = 1.0 / (1.0 + t1)
+    kr = t1 * kl
+    ru = [kl * L[2 + k] + kr * R[2 + k] for k in range(3)]
+    sqL = L[2] ** 2 + L[3] ** 2 + L[4] ** 2
+    sqR = R[2] ** 2 + R[3] ** 2 + R[4] ** 2
+    h = kl * (gig1 * L[1] / L[0] + 0.5 * sqL) + kr * (gig1 * R[1] / R[0] + 0.5 * sqR)
+    roe_p = (h - 0.5 * (ru[0] ** 2 + ru[1] ** 2 + ru[2] ** 2)) * roe_rho / gig1
+    vnl = L[2] * n[0] + L[3] * n[1] + L[4] * n[2]
+    vnr = R[2] * n[0] + R[3] * n[1] + R[4] * n[2]
+    al, ar = np.sqrt(g * L[1] / L[0]), np.sqrt(g * R[1] / R[0])
+    vm = ru[0] * n[0] + ru[1] * n[1] + ru[2] * n[2]
+    am = np.sqrt(g * roe_p / roe_rho)
+    rel = ig1 * L[1] + 0.5 * L[0] * sqL
+    rer = ig1 * R[1] + 0.5 * R[0] * sqR
+    sl = cmin(vnl - al, vm - am)
+    sr = cmax(vm + am, vnr + ar)
+
+    def side_flux(Q, vq, re):
+        m0 = vq * Q[0]
+        return np.stack([m0, vq * (re + Q[1])] + [m0 * Q[2 + k] + Q[1] * n[k] for k in range(3)])
+
+    rqL, rqR = L[0] * (sl - vnl), R[0] * (sr - vnr)
+    Sst = (rqR * vnr - rqL * vnl - R[1] + L[1]) / (rqR - rqL)
+    left = Sst.real >= 0.0
+
+    def star_flux(Q, s, vq, rq, re):
+        iks = 1.0 / (s - Sst)
+        pst = Q[1] - rq * (vq - Sst)
+        dp = pst - Q[1]
+        rest = iks * (re * (s - vq) - Q[1] * vq + pst * Sst)
+        return np.stack([Sst * (rq * iks), Sst * (rest + pst)] +
+                        [Sst * (iks * (rq * Q[2 + k] + dp * n[k])) + pst * n[k] for k in range(3)])
+
+    Fs = np.where(left, star_flux(L, sl, vnl, rqL, rel), star_flux(R, sr, vnr, rqR, rer))
+    F = np.where(sr.real <= 0.0, side_flux(R, vnr, rer), Fs)
+    return np.where(sl.real >= 0.0, side_flux(L, vnl, rel), F)
 
 
 def roe(L, R, n, g, eps=0.1):
@@ -95,7 +142,7 @@ def residual(md, U, dt, scheme="RUSANOV", g=1.4):
     QR[:, sym] = QL[:, sym]
     for k in range(3):
         QR[2 + k, sym] = QL[2 + k, sym] - dn * n[k, sym]
-    F = (rusanov if scheme == "RUSANOV" else roe)(QL, QR, n, g) * md.face_surface
+    F = {"RUSANOV": rusanov, "HLLC": hllc, "ROE": roe}[scheme](QL, QR, n, g) * md.face_surface
     R = np.zeros((5, nci), dtype=U.dtype)
     np.subtract.at(R.T, fc1, F.T)
     inner = np.arange(nfi)

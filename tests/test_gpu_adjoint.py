@@ -1,10 +1,12 @@
 """GPU adjoint of the first-order residual and of explicit runs.
 
 * ty_adjoint_vjp against central finite differences of ty_residual_device (periodic,
-  symmetry and far-field boundaries; HLLC, Rusanov, Roe; exact and fast modes).
+  symmetry, far-field, slip and no-slip wall boundaries; HLLC, Rusanov, Roe; exact and fast
+  modes).
 * The gradient of J = sum over a sub-box of rho^2 V after an RK3-SSP run, through
-  typhon_gb300.adjoint (binomial checkpointing, torch.autograd), against the complex-step
-  derivative of the numpy restatement in tests/residual_cs.py: agreement to 1e-8.
+  typhon_gb300.adjoint (binomial checkpointing or stored stage states, torch.autograd),
+  against the complex-step derivative of the numpy restatement in tests/residual_cs.py:
+  agreement to 1e-8.
 """
 import numpy as np
 import pytest
@@ -41,7 +43,9 @@ def smooth_cons(ty, md, amp=0.1):
 
 
 CASES = [("periodic", "HLLC"), ("periodic", "RUSANOV"), ("periodic", "ROE"), ("symmetry", "ROE"),
-         ("farfield", "HLLC")]
+         ("symmetry", "HLLC"), ("farfield", "HLLC"), ("farfield", "ROE"), ("wall", "RUSANOV"),
+         ("noslip", "ROE")]
+BC_KIND = {"symmetry": op.BC_SYMMETRY, "farfield": op.BC_FARFIELD, "wall": op.BC_WALL, "noslip": op.BC_NOSLIP}
 
 
 @pytest.mark.parametrize("mode", ["exact", "fast"])
@@ -51,7 +55,7 @@ def test_vjp_matches_finite_differences(env, golden_dir, bc, scheme, mode):
     if bc == "periodic":
         md = jittered(ty)
     else:
-        kind = op.BC_SYMMETRY if bc == "symmetry" else op.BC_FARFIELD
+        kind = BC_KIND[bc]
         md = ty.preprocess(ty.read_tym(golden_dir / "quad20x10.tym"), 2,
                            [(f, kind, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX")])
     g = ty.Grid(md)
@@ -70,7 +74,7 @@ def test_vjp_matches_finite_differences(env, golden_dir, bc, scheme, mode):
     g.close()
 
 
-@pytest.mark.parametrize("scheme", ["RUSANOV", "ROE"])
+@pytest.mark.parametrize("scheme", ["RUSANOV", "HLLC", "ROE"])
 def test_unsteady_gradient_against_complex_step(env, scheme):
     torch, ty, adjoint = env
     md = jittered(ty, 8)
@@ -105,6 +109,16 @@ def test_unsteady_gradient_against_complex_step(env, scheme):
     J2 = (adjoint.rk_solve(Ut2, g, "RK3-SSP", dts, snaps=0)[0] ** 2 * w).sum()
     J2.backward()
     assert torch.allclose(Ut2.grad, Ut.grad, rtol=1e-13, atol=0)
+    # every stage state kept by the forward pass: the same gradient, nothing recomputed
+    Ut3 = torch.tensor(U0, device="cuda", requires_grad=True)
+    J3 = (adjoint.rk_solve(Ut3, g, "RK3-SSP", dts, snaps="stages")[0] ** 2 * w).sum()
+    J3.backward()
+    assert torch.allclose(Ut3.grad, Ut.grad, rtol=1e-13, atol=0)
+    # the default storage policy (a small run: every stage state fits)
+    Ut4 = torch.tensor(U0, device="cuda", requires_grad=True)
+    J4 = (adjoint.rk_solve(Ut4, g, "RK3-SSP", dts)[0] ** 2 * w).sum()
+    J4.backward()
+    assert torch.equal(Ut4.grad, Ut3.grad)
     g.close()
 
 

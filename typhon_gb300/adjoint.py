@@ -10,9 +10,11 @@ SOURCE/MAIN/inverse_calc_sensi.f90:62-114).
 * Its adjoint runs the stages backwards: lambda_R_s = c(n, s) lambda' + sum_{k>s} c(k-1, s)
   lambda_k, lambda_s = (dR/dU at U_s)^T lambda_R_s (ty_adjoint_vjp), lambda_U0 = lambda' +
   sum_s lambda_s.  The stage states of a step are recomputed from the step's initial state.
-* The steps are reversed with binomial checkpointing: the schedule minimises the number of
-  recomputed steps for a given number of stored states (Griewank's recursion, solved here by
-  dynamic programming).
+* Storage: when every stage state of the run fits in device memory (5 x ncell_int doubles
+  per stage and step; a few GB for hundreds of steps on a million cells) the forward pass
+  keeps them and the reverse sweep recomputes nothing.  Otherwise the steps are reversed
+  with binomial checkpointing: the schedule minimises the number of recomputed steps for a
+  given number of stored states (Griewank's recursion, solved here by dynamic programming).
 * ``RKSolve`` is a ``torch.autograd.Function`` over CUDA tensors [5, ncell_int] (rho, rhoE,
   rhou, rhov, rhow), so a functional written in torch differentiates through the solver.
 
@@ -89,16 +91,22 @@ class Stepper:
                 Rs.append(self.residual(U, dt))
         return Us, Rs
 
-    def step(self, U0, dt):
-        _, Rs = self.stages(U0, dt)
+    def step(self, U0, dt, tape=None):
+        """U0 -> U' (one step); the step's stage states are appended to `tape` when given."""
+        Us, Rs = self.stages(U0, dt)
         U = U0.clone()
         for s, c in enumerate(self.table[-1]):
             if c != 0.0:
                 U += c * Rs[s]
+        if tape is not None:
+            tape.append(Us)
         return U
 
-    def step_adjoint(self, U0, dt, lam):
-        Us, _ = self.stages(U0, dt, last_residual=False)
+    def step_adjoint(self, U0, dt, lam, Us=None):
+        """lambda' -> lambda_U0 for one step; the stage states are recomputed from U0 unless
+        given (Us, as stored by step(..., tape))."""
+        if Us is None:
+            Us, _ = self.stages(U0, dt, last_residual=False)
         lam_stage = [None] * self.n
         out = lam.clone()
         for s in reversed(range(self.n)):
@@ -143,6 +151,38 @@ def forward_steps(stepper, U0, dts):
     return U
 
 
+def forward_steps_stored(stepper, U0, dts):
+    """Forward steps that keep every stage state: (U_final, tape), tape[i] the stage states of
+    step i.  n_stages x 5 x ncell_int doubles per step of device memory."""
+    tape = []
+    U = U0
+    for dt in dts:
+        U = stepper.step(U, dt, tape)
+    return U, tape
+
+
+def adjoint_steps_stored(stepper, dts, lam, tape):
+    """dJ/dU0 from the stage states stored by forward_steps_stored: one reverse sweep, no
+    recomputation."""
+    for i in reversed(range(len(dts))):
+        lam = stepper.step_adjoint(None, dts[i], lam, Us=tape[i])
+    return lam
+
+
+def plan_storage(nci, nstages, nsteps, budget_bytes=None):
+    """Storage policy of the reverse sweep: "stages" when every stage state of the run fits in
+    `budget_bytes` (default: half of the device's free memory), else the number of stored
+    states (binomial checkpointing) that fit, at least 1."""
+    state = 5 * nci * 8
+    if budget_bytes is None:
+        import torch
+        free, _ = torch.cuda.mem_get_info()
+        budget_bytes = free // 2
+    if nsteps * nstages * state <= budget_bytes:
+        return "stages"
+    return int(max(1, min(nsteps, budget_bytes // state)))
+
+
 def adjoint_steps(stepper, U0, dts, lam, snaps=20):
     """dJ/dU0 given lam = dJ/dU_final: the steps reversed from U0 with at most `snaps` states
     held besides U0, placed by the binomial schedule (stepper: step(U, dt) and
@@ -177,21 +217,34 @@ def _make_function():
 
     class RKSolve(torch.autograd.Function):
         """U_final = RKSolve.apply(U0, grid, method, dts, snaps): explicit steps at fixed dts,
-        differentiable with respect to U0 (a CUDA float64 tensor [5, ncell_int])."""
+        differentiable with respect to U0 (a CUDA float64 tensor [5, ncell_int]).  With snaps
+        "stages" the forward pass keeps every stage state and the backward pass recomputes
+        nothing; with a number it stores that many states and reverses by binomial
+        checkpointing."""
 
         @staticmethod
-        def forward(ctx, U0, grid, method, dts, snaps=20):
+        def forward(ctx, U0, grid, method, dts, snaps=None):
             st = Stepper(grid, method)
-            ctx.st, ctx.dts, ctx.snaps = st, list(dts), snaps
+            dts = list(dts)
+            if snaps is None:
+                snaps = plan_storage(st.nci, st.n, len(dts))
+            ctx.st, ctx.dts, ctx.snaps, ctx.tape = st, dts, snaps, None
             ctx.save_for_backward(U0)
             with torch.no_grad():
-                return forward_steps(st, U0.contiguous(), ctx.dts)
+                if snaps == "stages":
+                    U, ctx.tape = forward_steps_stored(st, U0.contiguous(), dts)
+                    return U
+                return forward_steps(st, U0.contiguous(), dts)
 
         @staticmethod
         def backward(ctx, lam):
             (U0,) = ctx.saved_tensors
             with torch.no_grad():
-                g = adjoint_steps(ctx.st, U0.contiguous(), ctx.dts, lam.contiguous(), ctx.snaps)
+                if ctx.tape is not None:
+                    g = adjoint_steps_stored(ctx.st, ctx.dts, lam.contiguous(), ctx.tape)
+                    ctx.tape = None
+                else:
+                    g = adjoint_steps(ctx.st, U0.contiguous(), ctx.dts, lam.contiguous(), ctx.snaps)
             return g, None, None, None, None
 
     return RKSolve
@@ -200,8 +253,9 @@ def _make_function():
 _RKSolve = None
 
 
-def rk_solve(U0, grid, method, dts, snaps=20):
-    """Differentiable explicit solve (see RKSolve)."""
+def rk_solve(U0, grid, method, dts, snaps=None):
+    """Differentiable explicit solve (see RKSolve).  snaps: "stages" (keep every stage state),
+    a number of stored states (binomial checkpointing), or None (the policy of plan_storage)."""
     global _RKSolve
     if _RKSolve is None:
         _RKSolve = _make_function()
