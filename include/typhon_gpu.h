@@ -62,9 +62,16 @@ enum ty_rk {
 /* TY_BC_NOSLIP (new): the adiabatic wall of TY_BC_WALL with the inside density in its face
  * state.  TY_BC_WALL keeps Typhon's face state, whose density is the inside PRESSURE
  * (setboco_ns_flux.f90:136, "density / weak BC"), for parity with Typhon. */
+/* TY_BC_HEAT: a heat-conduction (KDIF) boundary, implemented as Typhon implements every
+ * KDIF wall and the EXTRAPOLATE condition: by a ghost FACE (bctype_of_kdifboco, MENU_KDIF.f90:
+ * 103-125; bctype_of_boco, MENU_BOCO.f90:126-150; init_ustboco_ghostface.f90), a ghost cell
+ * at the face centre with zero volume.  The thermal kind and value of each face come from
+ * ty_kdif_setup.  Not a Navier-Stokes boundary: the Navier-Stokes operations (residual,
+ * steps, implicit, adjoint) refuse a mesh that has one; ty_set_params still sets the
+ * arithmetic mode used by the KDIF calls. */
 enum ty_bc {
   TY_BC_INTERIOR = 0, TY_BC_PERIODIC = 1, TY_BC_SYMMETRY = 2, TY_BC_WALL = 3, TY_BC_FARFIELD = 4,
-  TY_BC_NOSLIP = 5
+  TY_BC_NOSLIP = 5, TY_BC_HEAT = 6
 };
 /* Arithmetic mode of the kernels.
  *   TY_MODE_EXACT: every FP64 operation in the order Typhon evaluates it, each rounded
@@ -287,10 +294,16 @@ typedef struct ty_kdif_stats {
   int32_t iterations;    /* CG iterations (all inner iterations for CG32) */
   int32_t refinements;   /* outer FP64 refinements (CG32) */
   double rel_res;        /* final |b - S x| / |b| */
+  double du_l1;          /* sum over cells of |dU| (U = Cp T), Typhon's steady residual
+                            (update_field.f90:45-52) before its division by the reference */
 } ty_kdif_stats;
 /* One backward-Euler step of size dt: residual, symmetrised matrix diag(V/dt) A, solve,
  * T += dU / Cp. */
 int ty_kdif_implicit_step(ty_mesh* mesh, double dt, const ty_kdif_solve* s, ty_kdif_stats* stats);
+/* Typhon's stability time step of the heat equation (calc_kdif_timestep.f90:38-62 with the
+ * global minimum of calc_zonetimestep.f90): min over cells of 2 fourier V^2 / sum_f S^2 times
+ * Cp / k, k the cell's conductivity (Typhon's linear material: one k). */
+int ty_kdif_fourier_dt(ty_mesh* mesh, double fourier, double* dt);
 /* Parity access (host): which = 0 T [ncell] (ghosts included), 1 grad T [3][ncell_int],
  * 2 flux*S [nface], 3 J_R*S [nface], 4 diagonal [ncell_int], 5 flux balance [ncell_int]. */
 int ty_kdif_get(ty_mesh* mesh, int32_t which, double* out);
@@ -340,7 +353,11 @@ int ty_umesh_free(ty_umesh* um);
 int ty_umesh_set_nodes(ty_umesh* um, int32_t nvtex, const double* xyz);
 int ty_umesh_add_section(ty_umesh* um, int32_t elemtype, int32_t nelem, const int32_t* ielem,
                          const int32_t* vtex);
+/* A boundary family given by face element numbers (a .tym mark, a CGNS FaceCenter or
+ * ElementList BC), or by vertex numbers: every boundary face whose vertices are all in the
+ * list (a CGNS Vertex BC; CFDTOOLS/Mesh/seek_bcface_vtex.f90:38-45). */
 int ty_umesh_add_mark(ty_umesh* um, const char* family, int32_t ntag, const int32_t* tags);
+int ty_umesh_add_vertex_mark(ty_umesh* um, const char* family, int32_t ntag, const int32_t* tags);
 /* Boundary definitions, then preprocessing.  kind: ty_bc; periodic families give their
  * partner family and the translation from this family to the partner. */
 int ty_umesh_add_bc(ty_umesh* um, const char* family, int32_t kind, const char* partner,
@@ -350,6 +367,10 @@ int ty_umesh_build(ty_umesh* um, int32_t dim);
 int ty_umesh_desc(const ty_umesh* um, ty_mesh_desc* out);
 /* Face -> vertex lists of the built mesh: [nface*4] 1-based, 0 padded. */
 int ty_umesh_facevtex(const ty_umesh* um, int32_t* out);
+/* Boundary definition of each face [nface]: the index (0-based, in ty_umesh_add_bc order)
+ * of the definition its family matched, -1 for interior faces.  Lets a caller give per-face
+ * values (KDIF wall kinds and temperatures, ...) by family. */
+int ty_umesh_face_family(const ty_umesh* um, int32_t* out);
 
 #ifdef __cplusplus
 }

@@ -61,7 +61,8 @@ struct ElemSection {
 
 struct Mark {
   std::string family;
-  std::vector<int> tags;  // element numbers of boundary face elements
+  std::vector<int> tags;  // element numbers of boundary face elements, or vertex numbers
+  bool vertex = false;    // tags are vertices (a CGNS Vertex BC)
 };
 
 // Content of a Typhon .tym mesh (TYFMT_MESH.f90 reader) or of a generator.
@@ -76,7 +77,9 @@ bool read_tym(const std::string& path, RawMesh& out, std::string& err);
 // Boundary families and how the solver treats them.
 // BC_NOSLIP (new): BC_WALL with the inside density in the face state (BC_WALL keeps Typhon's
 // face state, whose density is the inside pressure, setboco_ns_flux.f90:136)
-enum BcKind { BC_PERIODIC = 1, BC_SYMMETRY = 2, BC_WALL = 3, BC_FARFIELD = 4, BC_NOSLIP = 5 };
+// BC_HEAT: a KDIF boundary with a ghost face (init_ustboco_ghostface.f90), as Typhon
+// implements every KDIF wall and EXTRAPOLATE
+enum BcKind { BC_PERIODIC = 1, BC_SYMMETRY = 2, BC_WALL = 3, BC_FARFIELD = 4, BC_NOSLIP = 5, BC_HEAT = 6 };
 struct BcDef {
   std::string family;   // family name as in the mesh marks
   int kind = 0;
@@ -252,6 +255,29 @@ struct KdifSolver {
   void matvec(const double* x, double* y) const;
   int cg(const std::vector<double>& b, std::vector<double>& x, double tol, int max_it, double* rel);
   int implicit_step(double dt, double tol, int max_it, double* rel);
+  // Typhon's own implicit iteration: DLU system I + dt/V J, CGS, steady cycles
+  std::vector<double> dlu_diag, dlu_upper, dlu_lower;  // ncell, nface, nface
+  double fourier_dt(double fourier, double conduct) const;
+  void typhon_dlu(double dt);
+  void dlu_yeqax(const double* x, double* y) const;
+  void dlu_yeqmaxpz(const double* x, const double* z, double* y) const;
+  int dlu_cgs(std::vector<double>& sol, double maxres, int max_it) const;
 };
+
+// Typhon's steady driver for one KDIF zone (integration.f90, integration_cycle.f90,
+// integration_cyclezone.f90, check_end_cycle.f90), implicit DLU + CGS.
+struct KdifSteadyParams {
+  double fourier = 1.0, conduct = 1.0;
+  double cycle_res = 0.1, global_res = 1e-5;  // TIME_PARAM and PROJECT RESIDUALS
+  double cgs_maxres = 1e-4;                    // INV_RES
+  int cgs_max_it = 10;                         // IMP_MAX_IT
+  int max_iters = 100000, max_cycles = 1000;
+};
+struct KdifSteadyOut {
+  std::vector<double> log_res;    // log10 of the residual of every iteration (monres)
+  std::vector<double> cycle_avg;  // volume-averaged temperature after each cycle
+  std::vector<int> cycle_end;     // total iterations at the end of each cycle
+};
+void kdif_typhon_steady(KdifSolver& k, std::vector<double>& U, const KdifSteadyParams& p, KdifSteadyOut& out);
 
 }  // namespace ory

@@ -68,6 +68,10 @@ void ory_raw_add_mark(void* h, const char* name, int ntag, const int* tags) {
   mk.tags.assign(tags, tags + ntag);
   ((MeshHandle*)h)->raw.marks.push_back(std::move(mk));
 }
+void ory_raw_add_vertex_mark(void* h, const char* name, int ntag, const int* tags) {
+  ory_raw_add_mark(h, name, ntag, tags);
+  ((MeshHandle*)h)->raw.marks.back().vertex = true;
+}
 int ory_raw_counts(void* h, int* out) {  // nvtex, nsections, nmarks
   auto& r = ((MeshHandle*)h)->raw;
   out[0] = (int)r.vtex.size();
@@ -369,6 +373,26 @@ int ory_kdif_get(void* k, int which, double* out) {
   }
   std::memcpy(out, v->data(), v->size() * sizeof(double));
   return (int)v->size();
+}
+// Typhon's steady KDIF run from the temperature set by ory_kdif_set_T.  dp: fourier,
+// conduct, cycle_res, global_res, cgs_maxres; ip: cgs_max_it, max_iters, max_cycles.  Writes
+// up to cap iterations' log10 residuals and cycles' averages and end iterations; returns the
+// iteration count (negative cycle count in *ncycle_out).
+int ory_kdif_typhon_steady(void* k, const double* dp, const int* ip, int cap, double* log_res, double* cycle_avg,
+                           int* cycle_end, int* ncycle_out) {
+  KdifSolver* s = (KdifSolver*)k;
+  KdifSteadyParams p;
+  p.fourier = dp[0]; p.conduct = dp[1]; p.cycle_res = dp[2]; p.global_res = dp[3]; p.cgs_maxres = dp[4];
+  p.cgs_max_it = ip[0]; p.max_iters = ip[1]; p.max_cycles = ip[2];
+  std::vector<double> U(s->T.begin(), s->T.begin() + s->m->ncell_int);
+  for (auto& u : U) u = u * s->cp;
+  KdifSteadyOut out;
+  kdif_typhon_steady(*s, U, p, out);
+  const int n = (int)out.log_res.size(), nc = (int)out.cycle_avg.size();
+  for (int i = 0; i < n && i < cap; ++i) log_res[i] = out.log_res[i];
+  for (int i = 0; i < nc && i < cap; ++i) { cycle_avg[i] = out.cycle_avg[i]; cycle_end[i] = out.cycle_end[i]; }
+  *ncycle_out = nc;
+  return n;
 }
 int ory_kdif_implicit_step(void* k, double dt, double tol, int max_it, double* rel) {
   return ((KdifSolver*)k)->implicit_step(dt, tol, max_it, rel);

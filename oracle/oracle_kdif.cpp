@@ -16,6 +16,8 @@
 // CGS, BiCG and GMRES).
 #include <cmath>
 #include <cstring>
+#include <limits>
+#include <algorithm>
 #include <vector>
 
 #include "oracle.hpp"
@@ -196,6 +198,172 @@ int KdifSolver::implicit_step(double dt, double tol, int max_it, double* rel) {
   int it = cg(balance, x, tol, max_it, rel);
   for (int c = 0; c < m->ncell_int; ++c) T[c] = T[c] + x[c] / cp;
   return it;
+}
+
+// calc_kdif_timestep.f90:38-62 (linear material), then the global minimum over the cells
+// (calc_zonetimestep.f90, stability condition)
+double KdifSolver::fourier_dt(double fourier, double conduct) const {
+  const int nci = m->ncell_int;
+  std::vector<double> d(nci, 0.0);
+  for (int f = 0; f < m->nface_int; ++f) {
+    const double s2 = m->fsurf[f] * m->fsurf[f];
+    d[m->fc1[f]] = d[m->fc1[f]] + s2;
+    d[m->fc2[f]] = d[m->fc2[f]] + s2;
+  }
+  for (int f = m->nface_int; f < m->nface; ++f) d[m->fc1[f]] = d[m->fc1[f]] + m->fsurf[f] * m->fsurf[f];
+  double dt = std::numeric_limits<double>::max();
+  for (int c = 0; c < nci; ++c) {
+    const double v = m->cvol[c];
+    double x = 2.0 * fourier * (v * v) / d[c];
+    x = x * cp / conduct;
+    dt = std::min(dt, x);
+  }
+  return dt;
+}
+
+// init_implicit_dlu.f90 (unit diagonal) + build_implicit_dlu.f90:44-66 with J_L = -J_R,
+// both times S (flux_to_res.f90:76-80); rows and columns over all cells, ghosts included
+void KdifSolver::typhon_dlu(double dt) {
+  const int nc = m->ncell, nci = m->ncell_int, nf = m->nface, nfi = m->nface_int;
+  dlu_diag.assign(nc, 0.0);
+  dlu_upper.assign(nf, 0.0);
+  dlu_lower.assign(nf, 0.0);
+  for (int c = 0; c < nci; ++c) dlu_diag[c] = 1.0;
+  for (int f = 0; f < nfi; ++f) {
+    const int c1 = m->fc1[f], c2 = m->fc2[f];
+    const double jR = jac[f], jL = -jac[f];
+    dlu_diag[c1] = dlu_diag[c1] + jL * dt / m->cvol[c1];
+    dlu_upper[f] = jR * dt / m->cvol[c1];
+    dlu_diag[c2] = dlu_diag[c2] - jR * dt / m->cvol[c2];
+    dlu_lower[f] = -(jL * dt / m->cvol[c2]);
+  }
+  for (int f = nfi; f < nf; ++f) {
+    const int c1 = m->fc1[f], c2 = m->fc2[f];
+    const double jR = jac[f], jL = -jac[f];
+    dlu_diag[c1] = dlu_diag[c1] + jL * dt / m->cvol[c1];
+    dlu_upper[f] = jR * dt / m->cvol[c1];
+    dlu_diag[c2] = 1.0;
+    dlu_lower[f] = 0.0;
+  }
+}
+
+// SPMAT_DLU.f90 dlu_yeqax (y = A x) and dlu_yeqmaxpz (y = z - A x), face order
+void KdifSolver::dlu_yeqax(const double* x, double* y) const {
+  for (int c = 0; c < m->ncell; ++c) y[c] = dlu_diag[c] * x[c];
+  for (int f = 0; f < m->nface; ++f) {
+    const int lo = m->fc1[f], hi = m->fc2[f];
+    y[hi] = y[hi] + dlu_lower[f] * x[lo];
+    y[lo] = y[lo] + dlu_upper[f] * x[hi];
+  }
+}
+void KdifSolver::dlu_yeqmaxpz(const double* x, const double* z, double* y) const {
+  for (int c = 0; c < m->ncell; ++c) y[c] = z[c] - dlu_diag[c] * x[c];
+  for (int f = 0; f < m->nface; ++f) {
+    const int lo = m->fc1[f], hi = m->fc2[f];
+    y[hi] = y[hi] - dlu_lower[f] * x[lo];
+    y[lo] = y[lo] - dlu_upper[f] * x[hi];
+  }
+}
+
+// dlu_cgs.f90:41-98: conjugate gradient squared, initial guess b / diag, stopped when the
+// step |alpha| sum|u + q| falls below maxres sum|x0| or after max_it + 1 iterations; returns
+// the iterations - 1, or -1 when not converged
+int KdifSolver::dlu_cgs(std::vector<double>& sol, double maxres, int max_it) const {
+  const int n = m->ncell;
+  std::vector<double> r1(n), r2(n), p1(n), q1(n), u(n), v(n);
+  auto dotp = [&](const std::vector<double>& a, const std::vector<double>& b) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s = s + a[i] * b[i];
+    return s;
+  };
+  auto asum = [&](const std::vector<double>& a) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s = s + std::fabs(a[i]);
+    return s;
+  };
+  p1 = sol;
+  for (int i = 0; i < n; ++i) sol[i] = p1[i] / dlu_diag[i];
+  const double ref = asum(sol);
+  dlu_yeqmaxpz(sol.data(), p1.data(), r1.data());
+  r2 = r1;
+  double err = std::numeric_limits<double>::max(), rho0 = 0.0;
+  int nit = 0;
+  while (err >= ref * maxres && nit <= max_it) {
+    const double rho1 = dotp(r1, r2);
+    if (nit == 0) {
+      u = r1;
+      p1 = r1;
+    } else {
+      const double beta = rho1 / rho0;
+      for (int i = 0; i < n; ++i) u[i] = r1[i] + beta * q1[i];
+      for (int i = 0; i < n; ++i) v[i] = q1[i] + beta * p1[i];
+      for (int i = 0; i < n; ++i) p1[i] = u[i] + beta * v[i];
+    }
+    dlu_yeqax(p1.data(), v.data());
+    const double alpha = rho1 / dotp(r2, v);
+    for (int i = 0; i < n; ++i) q1[i] = u[i] - alpha * v[i];
+    for (int i = 0; i < n; ++i) v[i] = u[i] + q1[i];
+    err = std::fabs(alpha) * asum(v);
+    for (int i = 0; i < n; ++i) sol[i] = sol[i] + alpha * v[i];
+    dlu_yeqax(v.data(), u.data());
+    for (int i = 0; i < n; ++i) r1[i] = r1[i] - alpha * u[i];
+    rho0 = rho1;
+    ++nit;
+  }
+  return nit <= max_it ? nit - 1 : -1;
+}
+
+void kdif_typhon_steady(KdifSolver& k, std::vector<double>& U, const KdifSteadyParams& p, KdifSteadyOut& out) {
+  const UMesh* m = k.m;
+  const int nc = m->ncell, nci = m->ncell_int;
+  // calc_refcons.f90: volume average of U; zone_preproc.f90: total volume
+  double refsca = 0.0, totvol = 0.0;
+  for (int c = 0; c < nci; ++c) refsca = refsca + U[c] * m->cvol[c];
+  for (int c = 0; c < nci; ++c) totvol = totvol + m->cvol[c];
+  refsca = refsca / totvol;
+  const double tiny = std::numeric_limits<double>::min();
+  double w_ref = 1.0, w_cur = 1.0, z_reforig = 0.0;
+  int iter_tot = 0;
+  std::vector<double> x(nc);
+  for (int icycle = 1; icycle <= p.max_cycles; ++icycle) {
+    w_cur = tiny;
+    double z_ref = w_cur, z_cur = z_ref;
+    const int maxit = p.max_iters - iter_tot;
+    int iter_loc = 0;
+    bool end = false;
+    while (!end) {
+      ++iter_loc;
+      ++iter_tot;
+      const double dt = k.fourier_dt(p.fourier, p.conduct);
+      for (int c = 0; c < nci; ++c) k.T[c] = U[c] / k.cp;  // calc_varprim_kdif
+      k.rhs(dt);
+      k.typhon_dlu(dt);
+      for (int c = 0; c < nc; ++c) x[c] = c < nci ? k.residu[c] : 0.0;
+      k.dlu_cgs(x, p.cgs_maxres, p.cgs_max_it);
+      double s = 0.0;  // update_field.f90: U += dU, residual sum|dU| / refsca
+      for (int c = 0; c < nci; ++c) {
+        U[c] = U[c] + x[c];
+        s = s + std::fabs(x[c]);
+      }
+      z_cur = 0.0 + s / refsca;
+      z_ref = std::max(z_ref, z_cur);  // check_end_cycle.f90
+      if (z_cur / z_ref <= p.cycle_res) end = true;
+      if (iter_loc == maxit) end = true;
+      out.log_res.push_back(std::log10(z_cur));
+    }
+    if (icycle == 1) z_reforig = z_ref;
+    if (z_cur / z_reforig >= w_cur / w_ref) {
+      w_cur = z_cur;
+      w_ref = z_reforig;
+    }
+    double tv = 0.0, vol = 0.0;  // VOL_AVERAGE probe of the temperature
+    for (int c = 0; c < nci; ++c) tv = tv + (U[c] / k.cp) * m->cvol[c];
+    for (int c = 0; c < nci; ++c) vol = vol + m->cvol[c];
+    out.cycle_avg.push_back(tv / vol);
+    out.cycle_end.push_back(iter_tot);
+    if (w_cur / w_ref <= p.global_res || iter_tot >= p.max_iters) break;
+  }
+  for (int c = 0; c < nci; ++c) k.T[c] = U[c] / k.cp;
 }
 
 }  // namespace ory

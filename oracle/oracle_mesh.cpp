@@ -7,7 +7,7 @@
 //                                  CFDTOOLS/Mesh/MESHCONNECT.f90:34-163 (ust_create_face,
 //                                  scanface_vtexface, same_face)
 //   face reordering                MESHCONNECT.f90:511-606 (reorder_ustconnect)
-//   boundary marks -> faces        CFDTOOLS/Mesh/seek_bcface_face.f90
+//   boundary marks -> faces        CFDTOOLS/Mesh/seek_bcface_face.f90, seek_bcface_vtex.f90
 //   geometry                       CFDTOOLS/Mesh/MESHGEOM.f90:37-461
 //   greedy face colouring          CFDTOOLS/Base/COLOR.f90:33-84
 //   ghost cells and periodicity    SOURCE/ZONE/init_connect_grid.f90:60-246,
@@ -315,6 +315,20 @@ bool build_umesh(const RawMesh& raw, int geo_dim, const std::vector<BcDef>& bcs,
   for (auto& mk : raw.marks) {
     Boco b;
     b.family = upper(mk.family);
+    if (mk.vertex) {  // seek_bcface_vtex.f90:38-45 with face_invtexlist (MESHCONNECT.f90)
+      for (int f = nfi; f < nface; ++f) {
+        bool same = false;
+        for (int v : m.facevtex[f]) {
+          same = false;
+          for (int t : mk.tags)
+            if (v == t || v == 0) { same = true; break; }
+          if (!same) break;
+        }
+        if (same) b.iface.push_back(f);
+      }
+      if (!b.iface.empty()) m.bocos.push_back(std::move(b));
+      continue;
+    }
     for (int tag : mk.tags) {
       const std::vector<int>* found = nullptr;
       std::vector<int> face;
@@ -475,7 +489,10 @@ bool build_umesh(const RawMesh& raw, int geo_dim, const std::vector<BcDef>& bcs,
         int g = ncell_int + ncell_lim - 1;
         if (c2[f] != 0) { err = "ghost cell already assigned"; return false; }
         c2[f] = g + 1;
-        if (d.kind == BC_SYMMETRY) {
+        if (d.kind == BC_HEAT) {  // init_ustboco_ghostface.f90:46-56
+          m.cvol[g] = 0.0;
+          m.ccentre[g] = m.fcentre[f];
+        } else if (d.kind == BC_SYMMETRY) {
           V3 fn = m.fnormal[f], gc = m.ccentre[i1];
           m.cvol[g] = m.cvol[i1];
           m.ccentre[g] = gc + (2.0 * dot(m.fcentre[f] - gc, fn)) * fn;

@@ -3,9 +3,10 @@
 Run once in a container where the reference checkout is mounted (default path
 below, or pass it as the first argument).  It copies, unchanged:
 
-* the XBIN/TYPHON meshes of NRG/COMMON that the cases use (``*.tym``);
-* the monitor files written by Typhon for those cases (``*.tmon``), renamed
-  ``<case>__<file>``.
+* the XBIN/TYPHON meshes of NRG/COMMON that the cases use (``*.tym``) and the CGNS
+  (ADF) meshes of the implicit and heat-conduction cases (``*.cgns``);
+* the monitor files written by Typhon for those cases (``*.tmon``, residual histories
+  ``monres.*``, boundary histories ``histo*``), renamed ``<case>__<file>``.
 
 The copies are committed so that the tests never read the reference at run time.
 """
@@ -16,7 +17,8 @@ import sys
 REF = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
 HERE = pathlib.Path(__file__).resolve().parent
 
-MESHES = ["quad20x20.tym", "quad20x10.tym", "quad10x10.tym", "tri5x10.tym", "mxlay2x20quad-h50.tym"]
+MESHES = ["quad20x20.tym", "quad20x10.tym", "quad10x10.tym", "tri5x10.tym", "mxlay2x20quad-h50.tym",
+          "tube.cgns", "square-quad10.cgns", "rect4x1.cgns"]
 CASES = {
     "RK2": "NRG/TIME/RUNGEKUTTA/RK2/RHOERR.tmon",
     "RK2-SSP": "NRG/TIME/RUNGEKUTTA/RK2-SSP/RHOERR.tmon",
@@ -32,14 +34,19 @@ CASES = {
     "VISCOUS-CELLAVG-VXERR": "NRG/NS/NUM/FLUX/VISCOUS/CELLAVG/VXERR.tmon",
     "VISCOUS-CELLFULL-DELTA": "NRG/NS/NUM/FLUX/VISCOUS/CELLFULL/DELTA.tmon",
     "VISCOUS-CELLFULL-VXERR": "NRG/NS/NUM/FLUX/VISCOUS/CELLFULL/VXERR.tmon",
+    "KDIF-ISOTH-CGS": ["NRG/KDIF/ISOTH-CGS/monres.001", "NRG/KDIF/ISOTH-CGS/Average_T.tmon"],
+    "KDIF-ISOTH-GMRES": ["NRG/KDIF/ISOTH-GMRES/monres.001", "NRG/KDIF/ISOTH-GMRES/Average_T.tmon"],
+    "IMPLICIT-GMRES": ["NRG/TIME/IMPLICIT/GMRES/histofluxNS_RIGHT", "NRG/TIME/IMPLICIT/GMRES/histovarNS_RIGHT"],
+    "IMPLICIT-BICGSTAB-RUSANOV": ["NRG/TIME/IMPLICIT/BICGSTAB-RUSANOV/histovarNS_DOWN"],
 }
 
 def main():
     for m in MESHES:
         shutil.copyfile(REF / "NRG/COMMON" / m, HERE / m)
-    for name, rel in CASES.items():
-        src = REF / rel
-        shutil.copyfile(src, HERE / f"{name}__{src.name}")
+    for name, rels in CASES.items():
+        for rel in [rels] if isinstance(rels, str) else rels:
+            src = REF / rel
+            shutil.copyfile(src, HERE / f"{name}__{src.name}")
     print("copied", len(MESHES), "meshes and", len(CASES), "monitor files into", HERE)
 
 if __name__ == "__main__":

@@ -13,7 +13,7 @@ ROOT = pathlib.Path(__file__).resolve().parents[1]
 LIB = ROOT / "oracle" / "build" / "liboracle.so"
 
 # enums of oracle/oracle.hpp
-BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD, BC_NOSLIP = 1, 2, 3, 4, 5
+BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD, BC_NOSLIP, BC_HEAT = 1, 2, 3, 4, 5, 6
 SCH_HLLC, SCH_RUSANOV, SCH_ROE = 1, 2, 3
 HRES_NONE, HRES_MUSCL, HRES_MUSCLFAST, HRES_MUSCLUNS = 0, 1, 2, 3
 LIM_NONE, LIM_MINMOD, LIM_ALBADA, LIM_VLEER, LIM_SBEE, LIM_KIM3, LIM_LIM03 = range(7)
@@ -41,6 +41,7 @@ def load():
         lib.ory_raw_set_vtex.argtypes = [vp, C.c_int, vp]
         lib.ory_raw_add_section.argtypes = [vp, C.c_int, C.c_int, vp, vp]
         lib.ory_raw_add_mark.argtypes = [vp, C.c_char_p, C.c_int, vp]
+        lib.ory_raw_add_vertex_mark.argtypes = [vp, C.c_char_p, C.c_int, vp]
         lib.ory_mesh_build.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, vp, C.c_char_p, C.c_int]
         lib.ory_mesh_sizes.argtypes = [vp, vp]
         lib.ory_mesh_export.argtypes = [vp] + [vp] * 11
@@ -69,6 +70,8 @@ def load():
         lib.ory_kdif_get.argtypes = [vp, C.c_int, vp]
         lib.ory_kdif_implicit_step.argtypes = [vp, C.c_double, C.c_double, C.c_int, vp]
         lib.ory_kdif_implicit_step.restype = C.c_int
+        lib.ory_kdif_typhon_steady.argtypes = [vp, vp, vp, C.c_int, vp, vp, vp, vp]
+        lib.ory_kdif_typhon_steady.restype = C.c_int
         lib.ory_run_nrg.argtypes = [C.c_int, vp, C.c_int, C.c_double, C.c_int, C.c_double, vp]
         _lib = lib
     return _lib
@@ -108,9 +111,10 @@ class Mesh:
             ie = np.ascontiguousarray(ielem, dtype=np.int32)
             cv = np.ascontiguousarray(conn, dtype=np.int32)
             m.lib.ory_raw_add_section(m.h, int(typ), ie.shape[0], _p(ie), _p(cv))
-        for name, tags in raw.marks:
+        for name, tags, *loc in raw.marks:
             t = np.ascontiguousarray(tags, dtype=np.int32)
-            m.lib.ory_raw_add_mark(m.h, name.encode(), t.shape[0], _p(t))
+            add = m.lib.ory_raw_add_vertex_mark if loc and loc[0] == "vertex" else m.lib.ory_raw_add_mark
+            add(m.h, name.encode(), t.shape[0], _p(t))
         return m
 
     def build(self, dim, bcs):
@@ -298,3 +302,15 @@ class Kdif:
         rel = C.c_double()
         it = self.lib.ory_kdif_implicit_step(self.h, float(dt), float(tol), int(max_it), C.byref(rel))
         return it, rel.value
+
+    def typhon_steady(self, fourier, conduct, cycle_res=0.1, global_res=1e-5, cgs_maxres=1e-4, cgs_max_it=10,
+                      max_iters=100000, max_cycles=1000):
+        """Typhon's steady implicit run (DLU + CGS) from the current temperature: log10 residual
+        per iteration, volume-averaged temperature and total iterations after each cycle."""
+        cap = max_iters + 1
+        dp = np.array([fourier, conduct, cycle_res, global_res, cgs_maxres], np.float64)
+        ip = np.array([cgs_max_it, max_iters, max_cycles], np.int32)
+        lr, avg, end = np.zeros(cap), np.zeros(cap), np.zeros(cap, np.int32)
+        nc = C.c_int()
+        n = self.lib.ory_kdif_typhon_steady(self.h, _p(dp), _p(ip), cap, _p(lr), _p(avg), _p(end), C.byref(nc))
+        return lr[:n], avg[:nc.value], end[:nc.value]

@@ -124,3 +124,46 @@ def test_kdif_errors(ty):
         g.kdif_setup(kc, bad, val)                   # boundary face without a kind
     with pytest.raises(ty.TyphonError):
         g.kdif_setup(-kc, kind, val)                 # non-positive conductivity
+
+
+def test_typhon_steady_run_reproduces_isoth_cgs(ty, golden_dir):
+    """NRG/KDIF/ISOTH-CGS through the GPU: Typhon's steady driver (Grid.kdif_steady) over
+    ty_kdif_implicit_step.  The GPU solves each step to 1e-13 where Typhon's CGS stops at
+    INV_RES 1e-4: on this 10-cell system both are converged to about 1e-8 in the log10
+    residual, which is the tolerance; the cycle structure and the printed averages agree."""
+    from typhon_gb300 import cgns, umesh
+    raw = cgns.read_cgns(golden_dir / "tube.cgns")
+    bcs = [(f, umesh.BC_HEAT, "", (0, 0, 0)) for f in ("SYM", "INFINI", "WALL")]
+    md = ty.preprocess(raw, 2, bcs)
+    kind = np.zeros(md.nface, np.int32)
+    val = np.zeros(md.nface)
+    kind[md.faces_of("SYM")] = op.KBC_EXTRAPOLATE
+    kind[md.faces_of("INFINI")], val[md.faces_of("INFINI")] = op.KBC_ISOTHERMAL, 2000.0
+    kind[md.faces_of("WALL")], val[md.faces_of("WALL")] = op.KBC_ISOTHERMAL, 1000.0
+    for mode in ("exact", "fast"):
+        g = ty.Grid(md)
+        g.set_spat("HLLC", mode=mode)
+        g.kdif_setup(np.full(md.ncell_int, 10.0), kind, val, flux="FULL", heat_capacity=1.0)
+        g.kdif_set_temperature(np.full(md.ncell_int, 100.0))
+        assert g.kdif_fourier_dt(20.0) == 2.0 * 20.0 * 100.0 ** 2 / 850.0 * 1.0 / 10.0
+        out = g.kdif_steady(20.0, cycle_res=0.1, global_res=1e-5, tol=1e-13)
+        gold = np.loadtxt(golden_dir / "KDIF-ISOTH-CGS__monres.001")[:, 1]
+        assert len(out["log_res"]) == len(gold) == 929
+        assert np.abs(out["log_res"] - gold).max() < 1e-7
+        assert list(out["cycle_end"]) == [125, 326, 527, 728, 929]
+        probe = [float(ln.split()[2]) for ln in open(golden_dir / "KDIF-ISOTH-CGS__Average_T.tmon") if ln.strip()]
+        assert ["%.7E" % a for a in out["cycle_avg"]] == ["%.7E" % p for p in probe]
+        g.close()
+
+
+def test_heat_boundary_mesh_refuses_navier_stokes(ty, golden_dir):
+    from typhon_gb300 import cgns, umesh
+    raw = cgns.read_cgns(golden_dir / "tube.cgns")
+    md = ty.preprocess(raw, 2, [(f, umesh.BC_HEAT, "", (0, 0, 0)) for f in ("SYM", "INFINI", "WALL")])
+    g = ty.Grid(md)
+    g.set_spat("HLLC", mode="exact")
+    prim = np.tile(np.array([[1.0], [1.0], [0.1], [0.0], [0.0]]), (1, md.ncell))
+    g.set_prim(prim)
+    with pytest.raises(ty.TyphonError):
+        g.integration_grid(1e-3)
+    g.close()

@@ -73,7 +73,8 @@ class KdifSolve(C.Structure):
 
 class KdifStats(C.Structure):
     """ty_kdif_stats"""
-    _fields_ = [("iterations", C.c_int32), ("refinements", C.c_int32), ("rel_res", C.c_double)]
+    _fields_ = [("iterations", C.c_int32), ("refinements", C.c_int32), ("rel_res", C.c_double),
+                ("du_l1", C.c_double)]
 
 
 _SIGS = {
@@ -108,6 +109,7 @@ _SIGS = {
     "ty_kdif_get_temperature": ([C.c_void_p, C.c_void_p], C.c_int),
     "ty_kdif_residual": ([C.c_void_p, C.c_double, C.c_void_p], C.c_int),
     "ty_kdif_implicit_step": ([C.c_void_p, C.c_double, C.POINTER(KdifSolve), C.POINTER(KdifStats)], C.c_int),
+    "ty_kdif_fourier_dt": ([C.c_void_p, C.c_double, C.POINTER(C.c_double)], C.c_int),
     "ty_kdif_get": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
     "ty_kdif_matvec": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "ty_residual_device": ([C.c_void_p, C.c_double, C.c_void_p], C.c_int),
@@ -117,6 +119,8 @@ _SIGS = {
     "ty_umesh_set_nodes": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
     "ty_umesh_add_section": ([C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "ty_umesh_add_mark": ([C.c_void_p, C.c_char_p, C.c_int32, C.c_void_p], C.c_int),
+    "ty_umesh_add_vertex_mark": ([C.c_void_p, C.c_char_p, C.c_int32, C.c_void_p], C.c_int),
+    "ty_umesh_face_family": ([C.c_void_p, C.c_void_p], C.c_int),
     "ty_umesh_add_bc": ([C.c_void_p, C.c_char_p, C.c_int32, C.c_char_p, C.c_void_p, C.c_void_p], C.c_int),
     "ty_umesh_build": ([C.c_void_p, C.c_int32], C.c_int),
     "ty_umesh_desc": ([C.c_void_p, C.POINTER(MeshDesc)], C.c_int),

@@ -293,6 +293,10 @@ int ready(ty_mesh* h) {
     tyi::set_error("set the parameters and upload a state first");
     return TY_ERR_STATE;
   }
+  if (h->heat_bc) {
+    tyi::set_error("the mesh has heat-conduction (TY_BC_HEAT) boundaries: no Navier-Stokes boundary state");
+    return TY_ERR_UNSUPPORTED;
+  }
   TY_CU(cudaSetDevice(h->device));
   return TY_OK;
 }
@@ -414,6 +418,8 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
         int p = d->face_partner[f] - 1;
         if (p < nfi || p >= nf || d->face_partner[p] - 1 != f) { tyi::set_error("bad periodic partner"); return bail(TY_ERR_MESH); }
         part[f] = p;
+      } else if (fbc[f] == TY_BC_HEAT) {
+        h->heat_bc = true;
       } else if (fbc[f] != TY_BC_SYMMETRY && fbc[f] != TY_BC_WALL && fbc[f] != TY_BC_FARFIELD &&
                  fbc[f] != TY_BC_NOSLIP) {
         tyi::set_error("unknown boundary kind");

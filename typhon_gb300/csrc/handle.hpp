@@ -41,6 +41,8 @@ struct ty_mesh {
   DevState s;
   SpatOpts o{};
   bool has_params = false, has_state = false, prim_valid = false, fast_ready = false;
+  bool heat_bc = false;  // the mesh has TY_BC_HEAT (ghost-face) boundaries
+  std::vector<double> kd_k;  // host copy of the KDIF conductivity [nci]
   int nslot = 0;
   std::vector<void*> allocs;
   // host copies needed to derive mode-dependent arrays

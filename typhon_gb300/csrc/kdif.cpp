@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 #include "handle.hpp"
@@ -71,6 +72,7 @@ int ty_kdif_setup(ty_mesh* h, const ty_kdif_params* p, const double* conductivit
     }
   }
   for (int g = 0; g < nc - nci; ++g) kc[nci + g] = kc[gsrc[g]];
+  h->kd_k.assign(kc.begin(), kc.begin() + nci);
   // calc_kdif_flux.f90:83-91 geometry, in the oracle's operation order
   const size_t lf = m.ldf;
   std::vector<double> geo(7 * lf, 0.0);
@@ -234,7 +236,31 @@ int ty_kdif_implicit_step(ty_mesh* h, double dt, const ty_kdif_solve* s, ty_kdif
     st->rel_res = rel;
   }
   TY_CU(KD_CALL(h, kdif_update_T, m, k, q));
-  TY_CU(cudaStreamSynchronize(q));
+  TY_CU(KD_CALL(h, imp_asum, k.x, (size_t)m.nci, k.part, k.scal + 6, q));
+  if (int rc = fetch(h, 6, 1)) return rc;
+  st->du_l1 = P[6];
+  return TY_OK;
+}
+
+int ty_kdif_fourier_dt(ty_mesh* h, double fourier, double* dt) {
+  if (int rc = kd_ready(h)) return rc;
+  if (!dt || !(fourier > 0.0)) return TY_ERR_ARG;
+  const int nci = h->m.nci, nfi = h->m.nfi, nf = h->m.nf;
+  std::vector<double> s2(nci, 0.0);
+  for (int f = 0; f < nfi; ++f) {
+    const double a = h->fsurf[f] * h->fsurf[f];
+    s2[h->fc1[f]] = s2[h->fc1[f]] + a;
+    s2[h->fc2[f]] = s2[h->fc2[f]] + a;
+  }
+  for (int f = nfi; f < nf; ++f) s2[h->fc1[f]] = s2[h->fc1[f]] + h->fsurf[f] * h->fsurf[f];
+  double best = std::numeric_limits<double>::max();
+  for (int c = 0; c < nci; ++c) {
+    const double v = h->cvol[c];
+    double x = 2.0 * fourier * (v * v) / s2[c];
+    x = x * h->kd.cp / h->kd_k[c];
+    best = std::min(best, x);
+  }
+  *dt = best;
   return TY_OK;
 }
 

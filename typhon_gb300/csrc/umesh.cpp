@@ -5,11 +5,13 @@
 // every geometric value come out as Typhon computes them:
 //   faces of each element, created cell by cell   CFDTOOLS/Mesh/create_facevtex.f90:60-210
 //   interior faces first, boundary faces reversed  CFDTOOLS/Mesh/MESHCONNECT.f90:538-598
-//   boundary marks matched to faces                CFDTOOLS/Mesh/seek_bcface_face.f90
+//   boundary marks matched to faces                CFDTOOLS/Mesh/seek_bcface_face.f90 (face
+//                                                  elements), seek_bcface_vtex.f90 (vertices)
 //   face/cell geometry                             CFDTOOLS/Mesh/MESHGEOM.f90:37-330
 //   greedy first-fit face colouring                CFDTOOLS/Base/COLOR.f90:55-81
 //   ghost cells, periodic partners                 SOURCE/ZONE/init_connect_grid.f90:60-246,
-//                                                  SOURCE/ZONE/init_ustboco_ghostcell.f90:44-80
+//                                                  SOURCE/ZONE/init_ustboco_ghostcell.f90:44-80,
+//                                                  init_ustboco_ghostface.f90 (TY_BC_HEAT)
 // Data structures differ from Typhon's (hash maps instead of vertex->face scans, a spatial
 // hash for periodic matching) so that meshes of millions of cells preprocess in seconds.
 #include <algorithm>
@@ -57,7 +59,7 @@ int elem_dim(int t) {
 }
 
 struct Section { int type; std::vector<int> ielem, vtex; };
-struct Mark { std::string family; std::vector<int> tags; };
+struct Mark { std::string family; std::vector<int> tags; bool vertex = false; };
 struct BcIn { std::string family, partner; int kind; V3 trans, wallvel; };
 
 std::string upper(std::string s) {
@@ -97,7 +99,7 @@ struct ty_umesh {
   std::vector<int32_t> facecell;          // [2*nface], 1-based, column-major
   std::vector<int32_t> facevtex;          // [4*nface], 1-based, 0 padded
   std::vector<double> fnormal, fcentre, fsurf, ccentre, cvol, fwallvel;
-  std::vector<int32_t> fcolor, fbc, fpartner;
+  std::vector<int32_t> fcolor, fbc, fpartner, ffamily;
 };
 
 extern "C" {
@@ -135,9 +137,14 @@ int ty_umesh_add_mark(ty_umesh* um, const char* family, int32_t ntag, const int3
   um->marks.push_back(std::move(m));
   return TY_OK;
 }
+int ty_umesh_add_vertex_mark(ty_umesh* um, const char* family, int32_t ntag, const int32_t* tags) {
+  int rc = ty_umesh_add_mark(um, family, ntag, tags);
+  if (rc == TY_OK) um->marks.back().vertex = true;
+  return rc;
+}
 int ty_umesh_add_bc(ty_umesh* um, const char* family, int32_t kind, const char* partner,
                     const double* t3, const double* w3) {
-  if (!um || !family || kind < TY_BC_PERIODIC || kind > TY_BC_NOSLIP) return TY_ERR_ARG;
+  if (!um || !family || kind < TY_BC_PERIODIC || kind > TY_BC_HEAT) return TY_ERR_ARG;
   BcIn b;
   b.family = upper(family);
   b.partner = partner ? upper(partner) : "";
@@ -245,6 +252,20 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
     for (auto& mkr : um->marks) {
       Boco b;
       b.family = upper(mkr.family);
+      if (mkr.vertex) {  // every vertex of the boundary face in the list (seek_bcface_vtex.f90:38-45)
+        std::vector<int> sorted(mkr.tags);
+        std::sort(sorted.begin(), sorted.end());
+        for (int f = nfi; f < nface; ++f) {
+          bool all = true;
+          for (int k = 0; k < 4 && all; ++k) {
+            const int v = FV[4 * (size_t)f + k];
+            all = v == 0 || std::binary_search(sorted.begin(), sorted.end(), v);
+          }
+          if (all) b.iface.push_back(f);
+        }
+        if (!b.iface.empty()) bocos.push_back(std::move(b));
+        continue;
+      }
       for (int tag : mkr.tags) {
         auto it = face_elem.find(tag);
         if (it == face_elem.end()) continue;
@@ -367,7 +388,7 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
   }
 
   // ---- ghost cells: physical boundaries first, then periodic connections ----
-  std::vector<int> fbc(nface, TY_BC_INTERIOR), fpart(nface, 0);
+  std::vector<int> fbc(nface, TY_BC_INTERIOR), fpart(nface, 0), ffam(nface, -1);
   std::vector<double> fwall(3 * (size_t)nface, 0.0);
   int nlim = 0;
   for (auto& b : bocos) {
@@ -381,9 +402,13 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
         int a = F1[f] - 1, g = ncell_int + nlim - 1;
         F2[f] = g + 1;
         fbc[f] = d.kind;
+        ffam[f] = b.def;
         fwall[3 * (size_t)f] = d.wallvel.x; fwall[3 * (size_t)f + 1] = d.wallvel.y; fwall[3 * (size_t)f + 2] = d.wallvel.z;
         cv[g] = cv[a];
-        if (d.kind == TY_BC_SYMMETRY) {
+        if (d.kind == TY_BC_HEAT) {  // ghost face (init_ustboco_ghostface.f90:46-56)
+          cv[g] = 0.0;
+          cc[g] = fc[f];
+        } else if (d.kind == TY_BC_SYMMETRY) {
           V3 n = fn[f], gc = cc[a];
           cc[g] = add(gc, scl(2.0 * dot(sub(fc[f], gc), n), n));
         } else {
@@ -455,6 +480,7 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
       cv[g] = cv[icper];
       cc[g] = add(fc[f], dfc);
       fbc[f] = TY_BC_PERIODIC;
+      ffam[f] = b.def;
       fpart[f] = fp + 1;
     }
   }
@@ -482,6 +508,7 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
   um->fbc = fbc;
   um->fpartner = fpart;
   um->fwallvel = fwall;
+  um->ffamily = ffam;
   um->built = true;
   return TY_OK;
 }
@@ -501,6 +528,12 @@ int ty_umesh_desc(const ty_umesh* um, ty_mesh_desc* d) {
   d->face_bc = um->fbc.data();
   d->face_partner = um->fpartner.data();
   d->face_wallvel = um->fwallvel.data();
+  return TY_OK;
+}
+
+int ty_umesh_face_family(const ty_umesh* um, int32_t* out) {
+  if (!um || !out || !um->built) return TY_ERR_STATE;
+  std::memcpy(out, um->ffamily.data(), um->ffamily.size() * sizeof(int32_t));
   return TY_OK;
 }
 

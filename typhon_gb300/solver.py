@@ -219,6 +219,7 @@ class Grid:
         fk = np.ascontiguousarray(face_kind, np.int32)
         fv = np.ascontiguousarray(face_value, np.float64)
         p = _capi.KdifParams(KDIF_FLUX[flux], 0, float(heat_capacity))
+        self._kdif_cp = float(heat_capacity)
         _capi.check(self.lib.ty_kdif_setup(self.h, C.byref(p), kc.ctypes.data, fk.ctypes.data, fv.ctypes.data),
                     "ty_kdif_setup")
 
@@ -243,7 +244,61 @@ class Grid:
         st = _capi.KdifStats()
         _capi.check(self.lib.ty_kdif_implicit_step(self.h, float(dt), C.byref(s), C.byref(st)),
                     "ty_kdif_implicit_step")
-        return dict(iterations=st.iterations, refinements=st.refinements, rel_res=st.rel_res)
+        return dict(iterations=st.iterations, refinements=st.refinements, rel_res=st.rel_res, du_l1=st.du_l1)
+
+    def kdif_fourier_dt(self, fourier):
+        """Typhon's heat-equation time step for a Fourier number (TIME_PARAM:FOURIER)."""
+        dt = C.c_double()
+        _capi.check(self.lib.ty_kdif_fourier_dt(self.h, float(fourier), C.byref(dt)), "ty_kdif_fourier_dt")
+        return dt.value
+
+    def kdif_steady(self, fourier, cycle_res=0.1, global_res=1e-5, solver="CG", tol=1e-13, max_it=20000,
+                    max_iters=100000, max_cycles=1000, cycle_max_it=None):
+        """Typhon's steady implicit heat-conduction run from the current temperature
+        (integration.f90, integration_cycle.f90, integration_cyclezone.f90, check_end_cycle.f90,
+        update_field.f90 for one zone): the time step of `fourier` (stability condition, global
+        minimum); each iteration one backward-Euler step; the residual sum|dU| / U_ref with U_ref
+        the initial volume average of U = Cp T (calc_refcons.f90); a cycle ends when the residual
+        falls to cycle_res times the cycle's largest (TIME_PARAM:RESIDUALS) or after
+        cycle_max_it iterations; the run ends when the last cycle's residual falls to
+        global_res times the first cycle's largest (PROJECT:RESIDUALS).  Returns dict(log_res:
+        log10 residual per iteration as Typhon's monres file, cycle_avg: volume-averaged
+        temperature after each cycle as a VOL_AVERAGE probe, cycle_end: iterations at each
+        cycle's end).  The linear solves run on the GPU (solver, tol, max_it as in
+        kdif_implicit_step); only two scalars per iteration come back to the host."""
+        V = self.mesh.cell_volume[:self.nci]
+        T = self.kdif_temperature()
+        cp = self._kdif_cp
+        u_ref = float(np.sum(cp * T * V)) / float(np.sum(V))
+        dt = self.kdif_fourier_dt(fourier)
+        tiny = np.finfo(np.float64).tiny
+        w_ref, z_reforig = 1.0, None
+        log_res, cycle_avg, cycle_end = [], [], []
+        iters = 0
+        for icycle in range(1, max_cycles + 1):
+            w_cur = tiny
+            z_ref, z_cur = w_cur, w_cur
+            maxit = min(cycle_max_it or max_iters, max_iters - iters)
+            it_loc = 0
+            while True:
+                it_loc += 1
+                iters += 1
+                st = self.kdif_implicit_step(dt, solver=solver, tol=tol, max_it=max_it)
+                z_cur = st["du_l1"] / u_ref
+                z_ref = max(z_ref, z_cur)
+                log_res.append(np.log10(z_cur))
+                if z_cur / z_ref <= cycle_res or it_loc == maxit:
+                    break
+            if icycle == 1:
+                z_reforig = z_ref
+            if z_cur / z_reforig >= w_cur / w_ref:
+                w_cur, w_ref = z_cur, z_reforig
+            T = self.kdif_temperature()
+            cycle_avg.append(float(np.sum(T * V)) / float(np.sum(V)))
+            cycle_end.append(iters)
+            if w_cur / w_ref <= global_res or iters >= max_iters:
+                break
+        return dict(log_res=np.array(log_res), cycle_avg=np.array(cycle_avg), cycle_end=np.array(cycle_end))
 
     def kdif_get(self, which):
         m = self.mesh

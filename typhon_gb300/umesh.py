@@ -25,14 +25,15 @@ ELEM_BAR2, ELEM_TRI3, ELEM_QUAD4, ELEM_TETRA4, ELEM_PENTA6, ELEM_HEXA8 = 2, 13, 
 NVTEX = {ELEM_BAR2: 2, ELEM_TRI3: 3, ELEM_QUAD4: 4, ELEM_TETRA4: 4, ELEM_PENTA6: 6, ELEM_HEXA8: 8}
 DIM = {ELEM_BAR2: 1, ELEM_TRI3: 2, ELEM_QUAD4: 2, ELEM_TETRA4: 3, ELEM_PENTA6: 3, ELEM_HEXA8: 3}
 
-BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD, BC_NOSLIP = 1, 2, 3, 4, 5
+BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD, BC_NOSLIP, BC_HEAT = 1, 2, 3, 4, 5, 6
 
 
 @dataclass
 class RawMesh:
     vtex: np.ndarray                                   # (nvtex, 3) float64
     sections: list = field(default_factory=list)       # [(elemtype, ielem int32[n], conn int32[n, nv])]
-    marks: list = field(default_factory=list)          # [(family, tags int32[])]
+    # [(family, tags int32[])]: face element numbers; [(family, tags, "vertex")]: vertex numbers
+    marks: list = field(default_factory=list)
 
     @property
     def ncell(self):
@@ -56,7 +57,10 @@ def _section_head(f, datatype, name, usertype, params=(), string=b""):
 
 
 def write_tym(path, raw: RawMesh):
-    """Write a TYPHON mesh file (XBIN version 2, TYPHON format version 3)."""
+    """Write a TYPHON mesh file (XBIN version 2, TYPHON format version 3).  Marks must be face
+    element numbers (the format has no vertex marks)."""
+    if any(len(m) > 2 and m[2] == "vertex" for m in raw.marks):
+        raise ValueError("vertex-located boundary marks cannot be written to a .tym file")
     cells = [s for s in raw.sections if DIM[s[0]] == max(DIM[t] for t, _, _ in raw.sections)]
     faces = [s for s in raw.sections if s not in cells]
     with open(path, "wb") as f:
@@ -84,7 +88,7 @@ def write_tym(path, raw: RawMesh):
             f.write(np.asarray(ielem, "<i4").tobytes())
             f.write(np.asarray(conn, "<i4").tobytes())
             f.write(b"END")
-        for name, tags in raw.marks:
+        for name, tags, *_ in raw.marks:
             _section_head(f, 10, name, 20)
             f.write(struct.pack("<iii", 1, len(tags), 0))
             f.write(np.asarray(tags, "<i4").tobytes())
@@ -458,7 +462,7 @@ def periodic_box_bcs(lengths):
 class MeshDesc:
     """Preprocessed mesh (numpy copies of the ty_mesh_desc arrays, 0-based where noted)."""
 
-    def __init__(self, d, facevtex):
+    def __init__(self, d, facevtex, face_family=None, families=()):
         nf, nc = d.nface, d.ncell
 
         def arr(ptr, n, dt):
@@ -477,6 +481,13 @@ class MeshDesc:
         self.face_partner = arr(d.face_partner, nf, C.c_int32)      # 1-based, 0 = none
         self.face_wallvel = arr(d.face_wallvel, 3 * nf, C.c_double).reshape(nf, 3)
         self.facevtex = facevtex
+        # boundary definition index of each face (bcs order given to preprocess), -1 interior
+        self.face_family = face_family if face_family is not None else np.full(nf, -1, np.int32)
+        self.families = list(families)
+
+    def faces_of(self, family):
+        """Faces (0-based) of a boundary family, in face order."""
+        return np.nonzero(self.face_family == self.families.index(family.upper()))[0]
 
     @property
     def fc1(self):
@@ -517,9 +528,13 @@ def preprocess(raw: RawMesh, dim, bcs) -> MeshDesc:
             cv = np.ascontiguousarray(conn, np.int32)
             _capi.check(L.ty_umesh_add_section(h, int(typ), ie.shape[0], ie.ctypes.data, cv.ctypes.data),
                         "ty_umesh_add_section")
-        for name, tags in raw.marks:
+        for name, tags, *loc in raw.marks:
             t = np.ascontiguousarray(tags, np.int32)
-            _capi.check(L.ty_umesh_add_mark(h, name.encode(), t.shape[0], t.ctypes.data), "ty_umesh_add_mark")
+            if loc and loc[0] == "vertex":
+                _capi.check(L.ty_umesh_add_vertex_mark(h, name.encode(), t.shape[0], t.ctypes.data),
+                            "ty_umesh_add_vertex_mark")
+            else:
+                _capi.check(L.ty_umesh_add_mark(h, name.encode(), t.shape[0], t.ctypes.data), "ty_umesh_add_mark")
         for b in bcs:
             tr = np.ascontiguousarray(b[3] if len(b) > 3 and b[3] is not None else (0, 0, 0), np.float64)
             wv = np.ascontiguousarray(b[4] if len(b) > 4 else (0, 0, 0), np.float64)
@@ -530,6 +545,8 @@ def preprocess(raw: RawMesh, dim, bcs) -> MeshDesc:
         _capi.check(L.ty_umesh_desc(h, C.byref(d)), "ty_umesh_desc")
         fv = np.zeros(4 * d.nface, np.int32)
         _capi.check(L.ty_umesh_facevtex(h, fv.ctypes.data), "ty_umesh_facevtex")
-        return MeshDesc(d, fv.reshape(d.nface, 4))
+        ff = np.zeros(d.nface, np.int32)
+        _capi.check(L.ty_umesh_face_family(h, ff.ctypes.data), "ty_umesh_face_family")
+        return MeshDesc(d, fv.reshape(d.nface, 4), ff, [b[0].upper() for b in bcs])
     finally:
         L.ty_umesh_free(h)
