@@ -145,7 +145,7 @@ def test_typhon_steady_run_reproduces_isoth_cgs(ty, golden_dir):
         g.set_spat("HLLC", mode=mode)
         g.kdif_setup(np.full(md.ncell_int, 10.0), kind, val, flux="FULL", heat_capacity=1.0)
         g.kdif_set_temperature(np.full(md.ncell_int, 100.0))
-        assert g.kdif_fourier_dt(20.0) == 2.0 * 20.0 * 100.0 ** 2 / 850.0 * 1.0 / 10.0
+        assert g.kdif_fourier_dt(20.0) == pytest.approx(2.0 * 20.0 * 100.0 ** 2 / 850.0 / 10.0, rel=1e-14)
         out = g.kdif_steady(20.0, cycle_res=0.1, global_res=1e-5, tol=1e-13)
         gold = np.loadtxt(golden_dir / "KDIF-ISOTH-CGS__monres.001")[:, 1]
         assert len(out["log_res"]) == len(gold) == 929

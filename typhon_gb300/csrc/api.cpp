@@ -484,6 +484,7 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
   h->fcentre.assign(d->face_centre, d->face_centre + 3 * (size_t)nf);
   h->fnormal.assign(d->face_normal, d->face_normal + 3 * (size_t)nf);
   h->cvol.assign(d->cell_volume, d->cell_volume + (size_t)nc);
+  h->fsurf.assign(d->face_surface, d->face_surface + (size_t)nf);
   std::vector<double> fn(3 * lf, 0.0), fs(lf, 0.0), fw(3 * lf, 0.0), cv(lc, 0.0);
   for (int f = 0; f < nf; ++f) {
     for (int k = 0; k < 3; ++k) {
