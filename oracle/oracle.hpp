@@ -79,7 +79,15 @@ bool read_tym(const std::string& path, RawMesh& out, std::string& err);
 // face state, whose density is the inside pressure, setboco_ns_flux.f90:136)
 // BC_HEAT: a KDIF boundary with a ghost face (init_ustboco_ghostface.f90), as Typhon
 // implements every KDIF wall and EXTRAPOLATE
-enum BcKind { BC_PERIODIC = 1, BC_SYMMETRY = 2, BC_WALL = 3, BC_FARFIELD = 4, BC_NOSLIP = 5, BC_HEAT = 6 };
+// Inlets and outlets (setboco_ns_inlet_sub.f90, setboco_ns_outlet_sub.f90,
+// setboco_ns_inlet_sup.f90, setboco_ns_outlet_sup.f90), ghost faces as in Typhon
+// (bctype_of_nsboco, MENU_NS.f90:91-115).  Parameters (BcDef::data):
+//   BC_INLET_SUB  total pressure, total temperature, direction (3)
+//   BC_OUTLET_SUB static pressure
+//   BC_INLET_SUP  total pressure, total temperature, Mach number, direction (3)
+enum BcKind { BC_PERIODIC = 1, BC_SYMMETRY = 2, BC_WALL = 3, BC_FARFIELD = 4, BC_NOSLIP = 5, BC_HEAT = 6,
+              BC_INLET_SUB = 7, BC_OUTLET_SUB = 8, BC_INLET_SUP = 9, BC_OUTLET_SUP = 10 };
+inline bool ghost_face_kind(int k) { return k == BC_HEAT || (k >= BC_INLET_SUB && k <= BC_OUTLET_SUP); }
 struct BcDef {
   std::string family;   // family name as in the mesh marks
   int kind = 0;
@@ -88,6 +96,7 @@ struct BcDef {
   V3 translation;
   // wall: wall velocity
   V3 wall_velocity;
+  double data[6] = {0, 0, 0, 0, 0, 0};  // inlet / outlet parameters (BcKind)
 };
 
 struct Boco {
@@ -98,6 +107,7 @@ struct Boco {
   double rlink = 0;        // +1 for FAMILY1 side, -1 for FAMILY2 side
   std::vector<int> partner_face;  // periodic: partner face of each face
   V3 wall_velocity;
+  double data[6] = {0, 0, 0, 0, 0, 0};
 };
 
 // Preprocessed mesh in Typhon's numbering (st_ustmesh).
@@ -120,7 +130,7 @@ bool build_umesh(const RawMesh& raw, int geo_dim, const std::vector<BcDef>& bcs,
 
 // ---------------------------------------------------------------------------
 // Solver
-enum Scheme { SCH_HLLC = 1, SCH_RUSANOV = 2, SCH_ROE = 3, SCH_HLLCK = 4 };
+enum Scheme { SCH_HLLC = 1, SCH_RUSANOV = 2, SCH_ROE = 3, SCH_HLLE = 5 };
 enum HighRes { HRES_NONE = 0, HRES_MUSCL = 1, HRES_MUSCLFAST = 2, HRES_MUSCLUNS = 3 };
 enum Limiter { LIM_NONE = 0, LIM_MINMOD = 1, LIM_ALBADA = 2, LIM_VLEER = 3, LIM_SBEE = 4,
                LIM_KIM3 = 5, LIM_LIM03 = 6 };
@@ -157,6 +167,8 @@ struct SpatParams {
 //   else      supersonic outflow: the inside state
 // q: inside primitive state (rho, p, u, v, w); out: ghost primitive state.
 void farfield_state(double gamma, const double* qinf, V3 n, const double* q, double* out);
+// inlet / outlet state (BcKind 7..10) from the inside primitive state
+void inout_state(int kind, double g, double r, const double* data, const double* qi, double* qo);
 bool farfield_jacobian(double gamma, const double* qinf, V3 n, const double* q, double* M);
 void noslip_jacobian(V3 uw, double* M);
 enum ViscMeth { VISC_NONE = 0, VISC_CELLAVG = 1, VISC_CELLFULL = 2 };
@@ -279,5 +291,23 @@ struct KdifSteadyOut {
   std::vector<int> cycle_end;     // total iterations at the end of each cycle
 };
 void kdif_typhon_steady(KdifSolver& k, std::vector<double>& U, const KdifSteadyParams& p, KdifSteadyOut& out);
+
+// Typhon's steady driver for one Navier-Stokes zone with the implicit step (integration.f90,
+// integration_cycle.f90, integration_cyclezone.f90, check_end_cycle.f90, calc_zonetimestep.f90
+// CFL law, update_field.f90 residual) and the boundary histories of one family
+// (integ_ustboco.f90, write_bocohisto.f90).
+struct NsSteadyParams {
+  double cfl = 1.0, cfl_max = 1.0;             // TIME_PARAM CFL, CFL_MAX
+  double cycle_res = 0.1, global_res = 1e-5;   // TIME_PARAM and PROJECT RESIDUALS
+  int max_iters = 100000, max_cycles = 1000;
+  std::vector<int> history_faces;              // faces of the family with SAVE_HISTORY
+};
+struct NsSteadyOut {
+  std::vector<double> log_res;      // log10 residual of every iteration
+  std::vector<double> flux_sum;     // per cycle: sum over the family of F S (5 values)
+  std::vector<double> ghost_avg;    // per cycle: S-weighted average of the ghost primitive state (5)
+  std::vector<int> cycle_end;
+};
+void ns_typhon_steady(Solver& s, const NsSteadyParams& p, NsSteadyOut& out);
 
 }  // namespace ory

@@ -27,7 +27,7 @@ void set_err(char* buf, int len, const std::string& s) {
   }
 }
 std::vector<BcDef> make_bcs(int nbc, const char* const* fam, const int* kind, const char* const* partner,
-                            const double* trans, const double* wallvel) {
+                            const double* trans, const double* wallvel, const double* data = nullptr) {
   std::vector<BcDef> bcs(nbc);
   for (int i = 0; i < nbc; ++i) {
     bcs[i].family = fam[i];
@@ -35,6 +35,8 @@ std::vector<BcDef> make_bcs(int nbc, const char* const* fam, const int* kind, co
     if (partner && partner[i]) bcs[i].partner = partner[i];
     if (trans) bcs[i].translation = v3(trans[3 * i], trans[3 * i + 1], trans[3 * i + 2]);
     if (wallvel) bcs[i].wall_velocity = v3(wallvel[3 * i], wallvel[3 * i + 1], wallvel[3 * i + 2]);
+    if (data)
+      for (int q = 0; q < 6; ++q) bcs[i].data[q] = data[6 * i + q];
   }
   return bcs;
 }
@@ -81,12 +83,13 @@ int ory_raw_counts(void* h, int* out) {  // nvtex, nsections, nmarks
 }
 
 // ---- preprocessing ----
+// bcdata: 6 parameters per boundary definition (inlets and outlets), may be NULL
 int ory_mesh_build(void* h, int geo_dim, int nbc, const char* const* fam, const int* kind,
-                   const char* const* partner, const double* trans, const double* wallvel, char* err,
-                   int errlen) {
+                   const char* const* partner, const double* trans, const double* wallvel, const double* bcdata,
+                   char* err, int errlen) {
   auto* mh = (MeshHandle*)h;
   std::string e;
-  if (!build_umesh(mh->raw, geo_dim, make_bcs(nbc, fam, kind, partner, trans, wallvel), mh->m, e)) {
+  if (!build_umesh(mh->raw, geo_dim, make_bcs(nbc, fam, kind, partner, trans, wallvel, bcdata), mh->m, e)) {
     set_err(err, errlen, e);
     return -1;
   }
@@ -219,6 +222,29 @@ int ory_solver_implicit_step(void* s, double cfl, int local_dt, int nkrylov, int
   int info = S->implicit_step(cfl, local_dt != 0, l1);
   if (iters) *iters = S->gmres_iters;
   return info;
+}
+// Typhon's steady implicit run (ns_typhon_steady).  dp: cfl, cfl_max, cycle_res, global_res,
+// inv_res; ip: nkrylov, imp_max_it, max_iters, max_cycles; hist: faces of the history family.
+// Writes up to cap log10 residuals and, per cycle, 5 flux sums, 5 ghost averages and the end
+// iteration; returns the iteration count and the cycle count in *ncycle.
+int ory_solver_typhon_steady(void* s, const double* dp, const int* ip, int nhist, const int* hist, int cap,
+                             double* log_res, double* flux_sum, double* ghost_avg, int* cycle_end, int* ncycle) {
+  auto* S = (Solver*)s;
+  NsSteadyParams p;
+  p.cfl = dp[0]; p.cfl_max = dp[1]; p.cycle_res = dp[2]; p.global_res = dp[3];
+  S->inv_res = dp[4]; S->nkrylov = ip[0]; S->imp_max_it = ip[1];
+  p.max_iters = ip[2]; p.max_cycles = ip[3];
+  p.history_faces.assign(hist, hist + nhist);
+  NsSteadyOut out;
+  ns_typhon_steady(*S, p, out);
+  const int n = (int)out.log_res.size(), ncy = (int)out.cycle_end.size();
+  for (int i = 0; i < n && i < cap; ++i) log_res[i] = out.log_res[i];
+  for (int i = 0; i < ncy && i < cap; ++i) {
+    cycle_end[i] = out.cycle_end[i];
+    for (int v = 0; v < 5; ++v) { flux_sum[5 * i + v] = out.flux_sum[5 * i + v]; ghost_avg[5 * i + v] = out.ghost_avg[5 * i + v]; }
+  }
+  *ncycle = ncy;
+  return n;
 }
 // y = A x with the BDLU matrix of the last implicit step (x, y: 5 per cell, per-cell blocks)
 void ory_solver_bdlu_matvec(void* s, const double* x, double* y) { ((Solver*)s)->bdlu_yeqax(x, y); }

@@ -483,13 +483,14 @@ bool build_umesh(const RawMesh& raw, int geo_dim, const std::vector<BcDef>& bcs,
       const BcDef& d = bcs[b.def];
       b.kind = d.kind;
       b.wall_velocity = d.wall_velocity;
+      for (int q = 0; q < 6; ++q) b.data[q] = d.data[q];
       for (int f : b.iface) {
         ++ncell_lim;
         int i1 = c1[f] - 1;
         int g = ncell_int + ncell_lim - 1;
         if (c2[f] != 0) { err = "ghost cell already assigned"; return false; }
         c2[f] = g + 1;
-        if (d.kind == BC_HEAT) {  // init_ustboco_ghostface.f90:46-56
+        if (ghost_face_kind(d.kind)) {  // init_ustboco_ghostface.f90:46-56
           m.cvol[g] = 0.0;
           m.ccentre[g] = m.fcentre[f];
         } else if (d.kind == BC_SYMMETRY) {

@@ -160,6 +160,61 @@ void farfield_state(double gamma, const double* qinf, V3 n, const double* q, dou
   }
 }
 
+// Isentropic conversions of EQNS.f90:139-219 on one primitive state q = (rho, p, u, v, w)
+static V3 unit_dir(const double* d) {  // dir / abs(dir)
+  V3 v = v3(d[0], d[1], d[2]);
+  const double a = std::sqrt(sqrabs(v));
+  return v3(v.x / a, v.y / a, v.z / a);
+}
+static void pi_ti_mach_dir2prim(double g, double r, double pi, double ti, double mach, V3 dir, double* q) {
+  const double g1 = g - 1.0;
+  const double fm = 1.0 / (1.0 + .5 * g1 * (mach * mach));
+  const double ts = ti * fm;
+  const double a = std::sqrt(g * r * ts);
+  q[1] = pi * std::pow(fm, g / g1);
+  q[0] = q[1] / (r * ts);
+  const V3 u = (mach * a) * dir;
+  q[2] = u.x; q[3] = u.y; q[4] = u.z;
+}
+static void pi_ti_ps_dir2prim(double g, double r, double pi, double ti, double ps, V3 dir, double* q) {
+  const double g1 = g - 1.0;
+  double fm = std::pow(pi / ps, g1 / g);
+  if (fm < 1.0) fm = 1.0;  // "Bad ratio Pi/P : truncated to 1."
+  q[1] = ps;
+  q[0] = ps / (r * ti) * fm;
+  const V3 u = (std::sqrt((fm - 1.0) * 2.0 / g1) * std::sqrt(g * ps / q[0])) * dir;
+  q[2] = u.x; q[3] = u.y; q[4] = u.z;
+}
+static void prim2pi_ti_mach_dir(double g, double r, const double* q, double& pi, double& ti, double& mach, V3& dir) {
+  const double g1 = g - 1.0;
+  const V3 u = v3(q[2], q[3], q[4]);
+  double fmv = sqrabs(u);
+  const double n = std::sqrt(fmv);
+  dir = v3(u.x / n, u.y / n, u.z / n);
+  fmv = fmv / (g * q[1]) * q[0];
+  mach = std::sqrt(fmv);
+  fmv = 1.0 + 0.5 * g1 * fmv;
+  pi = q[1] * std::pow(fmv, g / g1);
+  ti = q[1] / r / q[0] * fmv;
+}
+
+// Inlet / outlet state from the inside state qi (setboco_ns_inlet_sub.f90:64-96,
+// setboco_ns_outlet_sub.f90:31-60, setboco_ns_inlet_sup.f90:75-101, setboco_ns_outlet_sup.f90)
+void inout_state(int kind, double g, double r, const double* data, const double* qi, double* qo) {
+  if (kind == BC_INLET_SUB) {
+    pi_ti_ps_dir2prim(g, r, data[0], data[1], qi[1], unit_dir(data + 2), qo);
+  } else if (kind == BC_OUTLET_SUB) {
+    double pi, ti, mach;
+    V3 dir;
+    prim2pi_ti_mach_dir(g, r, qi, pi, ti, mach, dir);
+    pi_ti_ps_dir2prim(g, r, pi, ti, data[0], dir, qo);
+  } else if (kind == BC_INLET_SUP) {
+    pi_ti_mach_dir2prim(g, r, data[0], data[1], data[2], unit_dir(data + 3), qo);
+  } else {
+    for (int v = 0; v < 5; ++v) qo[v] = qi[v];
+  }
+}
+
 void Solver::boco_cell_state() {
   const int nc = m->ncell;
   for (auto& b : m->bocos) {
@@ -205,6 +260,12 @@ void Solver::boco_cell_state() {
         double q[5], o[5];
         for (int v = 0; v < 5; ++v) q[v] = prim[v * nc + i];
         farfield_state(sp.gamma, sp.farfield, m->fnormal[f], q, o);
+        for (int v = 0; v < 5; ++v) prim[v * nc + g] = o[v];
+      } else if (b.kind >= BC_INLET_SUB && b.kind <= BC_OUTLET_SUP) {
+        int i = m->fc1[f];
+        double q[5], o[5];
+        for (int v = 0; v < 5; ++v) q[v] = prim[v * nc + i];
+        inout_state(b.kind, sp.gamma, sp.rgas, b.data, q, o);
         for (int v = 0; v < 5; ++v) prim[v * nc + g] = o[v];
       }
     }
@@ -259,6 +320,11 @@ void Solver::boco_face_state() {
         double q[5], o[5];
         for (int v = 0; v < 5; ++v) q[v] = cell_l[v * nf + f];
         farfield_state(sp.gamma, sp.farfield, m->fnormal[f], q, o);
+        for (int v = 0; v < 5; ++v) cell_r[v * nf + f] = o[v];
+      } else if (b.kind >= BC_INLET_SUB && b.kind <= BC_OUTLET_SUP) {
+        double q[5], o[5];
+        for (int v = 0; v < 5; ++v) q[v] = cell_l[v * nf + f];
+        inout_state(b.kind, sp.gamma, sp.rgas, b.data, q, o);
         for (int v = 0; v < 5; ++v) cell_r[v * nf + f] = o[v];
       }
     }
@@ -754,6 +820,40 @@ void Solver::face_fluxes() {
         V3 mo = (Sst * rvst) + (pst * fn);
         F[2] = mo.x; F[3] = mo.y; F[4] = mo.z;
       }
+    } else if (sp.scheme == SCH_HLLE) {  // calc_flux_hlle.f90:83-150, beta = 1
+      const double gig1 = g / (g - 1.0);
+      double t1 = std::sqrt(R.rho / L.rho);  // calc_roe_states.f90:35-53
+      double roe_rho = L.rho * t1;
+      double kl0 = 1.0 / (1.0 + t1);
+      double kr0 = t1 * kl0;
+      V3 roe_u = kl0 * L.u + kr0 * R.u;
+      double h1 = gig1 * L.p / L.rho + 0.5 * sqrabs(L.u);
+      double h2 = gig1 * R.p / R.rho + 0.5 * sqrabs(R.u);
+      h1 = kl0 * h1 + kr0 * h2;
+      double roe_p = (h1 - 0.5 * sqrabs(roe_u)) * roe_rho / gig1;
+      double vnl = dot(L.u, fn), vnr = dot(R.u, fn);
+      double al = std::sqrt(g * L.p / L.rho), ar = std::sqrt(g * R.p / R.rho);
+      double vm = dot(roe_u, fn);
+      double am = std::sqrt(g * roe_p / roe_rho);
+      double rel = ig1 * L.p + .5 * L.rho * sqrabs(L.u);
+      double rer = ig1 * R.p + .5 * R.rho * sqrabs(R.u);
+      double sl = std::min(std::min(0.0, vnl - al), vm - am);
+      double sr = std::max(std::max(0.0, vnr + ar), vm + am);
+      double iks = 1.0 / (sr - sl);
+      double kl = sr * iks, kr = -sl * iks, ku = sl * sr * iks;
+      F[0] = (kl * vnl - ku) * L.rho + (kr * vnr + ku) * R.rho;
+      F[1] = (kl * vnl - ku) * rel + (kr * vnr + ku) * rer + (kl * vnl * L.p + kr * vnr * R.p);
+      V3 mo = ((kl * vnl - ku) * L.rho) * L.u + ((kr * vnr + ku) * R.rho) * R.u + (kl * L.p + kr * R.p) * fn;
+      F[2] = mo.x; F[3] = mo.y; F[4] = mo.z;
+      if (calc_jac) {  // calc_jac_hll.f90:46-57 with the flux's wave speeds
+        double qL[5] = {L.rho, L.p, L.u.x, L.u.y, L.u.z}, qR[5] = {R.rho, R.p, R.u.x, R.u.y, R.u.z};
+        double JL[25], JR[25];
+        jacflux(g, qL, fn, vnl, JL);
+        jacflux(g, qR, fn, vnr, JR);
+        for (int i = 0; i < 5; ++i) { JL[i * 5 + i] = JL[i * 5 + i] - sl; JR[i * 5 + i] = JR[i * 5 + i] - sr; }
+        const double cl_ = sr / (sr - sl), cr_ = -sl / (sr - sl);
+        for (int k = 0; k < 25; ++k) { jacL[25 * (size_t)f + k] = cl_ * JL[k]; jacR[25 * (size_t)f + k] = cr_ * JR[k]; }
+      }
     } else if (sp.scheme == SCH_RUSANOV) {  // calc_flux_rusanov.f90:57-83
       double vnl = dot(L.u, fn), vnr = dot(R.u, fn);
       double al = std::sqrt(g * L.p / L.rho), ar = std::sqrt(g * R.p / R.rho);
@@ -1188,6 +1288,15 @@ void Solver::ns_bocojacobian() {
       }
       continue;
     }
+    if (b.kind == BC_OUTLET_SUP) {  // ns_bocojacobian.f90: dQr/dQl = I
+      for (int f : b.iface) {
+        double* JL = &jacL[25 * (size_t)f];
+        double* JR = &jacR[25 * (size_t)f];
+        for (int k = 0; k < 25; ++k) JL[k] = JL[k] + JR[k];
+        for (int k = 0; k < 25; ++k) JR[k] = 0.0;
+      }
+      continue;
+    }
     if (b.kind != BC_SYMMETRY) continue;
     for (int f : b.iface) {
       const V3 n = m->fnormal[f];
@@ -1273,6 +1382,73 @@ void Solver::rk_step(double dt) {
 #pragma omp parallel for schedule(static)
   for (size_t k = 0; k < nk; ++k) cons[k] = cons[k] + residu[k];
   (void)nc;
+}
+
+void ns_typhon_steady(Solver& s, const NsSteadyParams& p, NsSteadyOut& out) {
+  const UMesh* m = s.m;
+  const int nc = m->ncell, nci = m->ncell_int, nf = m->nface;
+  // calc_refcons.f90 + define_refcons (MENU_SOLVER.f90:260-275)
+  double ref0 = 0.0, ref1 = 0.0, totvol = 0.0;
+  for (int c = 0; c < nci; ++c) ref0 = ref0 + s.cons[c] * m->cvol[c];
+  for (int c = 0; c < nci; ++c) ref1 = ref1 + s.cons[nc + c] * m->cvol[c];
+  for (int c = 0; c < nci; ++c) totvol = totvol + m->cvol[c];
+  ref0 = ref0 / totvol;
+  ref1 = ref1 / totvol;
+  const double refv = std::sqrt(ref0 * ref1);
+  const double tiny = std::numeric_limits<double>::min();
+  double w_ref = 1.0, w_cur = 1.0, z_reforig = 0.0;
+  int iters = 0;
+  for (int icycle = 1; icycle <= p.max_cycles; ++icycle) {
+    const double wcur_res = w_cur, wres_ref = w_ref;
+    w_cur = tiny;
+    double z_ref = w_cur, z_cur = z_ref;
+    const int maxit = p.max_iters - iters;
+    int it_loc = 0;
+    bool end = false;
+    while (!end) {
+      ++it_loc;
+      ++iters;
+      double cfl = p.cfl * std::max(1.0, 1.0 - std::log10(z_cur / z_ref) - std::log10(wcur_res / wres_ref));
+      cfl = std::min(cfl, p.cfl_max);
+      s.implicit_step(cfl, false, nullptr);
+      // update_field.f90:45-60: scalars rho, rho E, then the momentum vector cell by cell
+      double a = 0.0, b = 0.0;
+      for (int c = 0; c < nci; ++c) a = a + std::fabs(s.residu[c]);
+      for (int c = 0; c < nci; ++c) b = b + std::fabs(s.residu[nc + c]);
+      z_cur = 0.0 + a / ref0;
+      z_cur = z_cur + b / ref1;
+      for (int c = 0; c < nci; ++c) {
+        const double mx = s.residu[2 * nc + c], my = s.residu[3 * nc + c], mz = s.residu[4 * nc + c];
+        z_cur = z_cur + std::sqrt(mx * mx + my * my + mz * mz) / refv;
+      }
+      z_ref = std::max(z_ref, z_cur);
+      if (z_cur / z_ref <= p.cycle_res) end = true;
+      if (it_loc == maxit) end = true;
+      out.log_res.push_back(std::log10(z_cur));
+    }
+    if (icycle == 1) z_reforig = z_ref;
+    if (z_cur / z_reforig >= w_cur / w_ref) {
+      w_cur = z_cur;
+      w_ref = z_reforig;
+    }
+    // integ_ustboco.f90: flux of the last right-hand side, ghost primitive state
+    double fs[5] = {0, 0, 0, 0, 0}, qa[5] = {0, 0, 0, 0, 0}, area = 0.0;
+    for (int f : p.history_faces) {
+      const int g = m->fc2[f];
+      const double S = m->fsurf[f];
+      for (int v = 0; v < 5; ++v) {
+        qa[v] = qa[v] + S * s.prim[v * (size_t)nc + g];
+        fs[v] = fs[v] + s.flux[v * (size_t)nf + f];
+      }
+    }
+    for (int f : p.history_faces) area = area + m->fsurf[f];
+    for (int v = 0; v < 5; ++v) {
+      out.flux_sum.push_back(fs[v]);
+      out.ghost_avg.push_back(qa[v] / area);
+    }
+    out.cycle_end.push_back(iters);
+    if (w_cur / w_ref <= p.global_res || iters >= p.max_iters) break;
+  }
 }
 
 }  // namespace ory

@@ -14,7 +14,8 @@ LIB = ROOT / "oracle" / "build" / "liboracle.so"
 
 # enums of oracle/oracle.hpp
 BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD, BC_NOSLIP, BC_HEAT = 1, 2, 3, 4, 5, 6
-SCH_HLLC, SCH_RUSANOV, SCH_ROE = 1, 2, 3
+BC_INLET_SUB, BC_OUTLET_SUB, BC_INLET_SUP, BC_OUTLET_SUP = 7, 8, 9, 10
+SCH_HLLC, SCH_RUSANOV, SCH_ROE, SCH_HLLE = 1, 2, 3, 5
 HRES_NONE, HRES_MUSCL, HRES_MUSCLFAST, HRES_MUSCLUNS = 0, 1, 2, 3
 LIM_NONE, LIM_MINMOD, LIM_ALBADA, LIM_VLEER, LIM_SBEE, LIM_KIM3, LIM_LIM03 = range(7)
 POSTLIM_NONE, POSTLIM_BARTH, POSTLIM_SUPERBARTH = 0, 1, 2
@@ -42,7 +43,7 @@ def load():
         lib.ory_raw_add_section.argtypes = [vp, C.c_int, C.c_int, vp, vp]
         lib.ory_raw_add_mark.argtypes = [vp, C.c_char_p, C.c_int, vp]
         lib.ory_raw_add_vertex_mark.argtypes = [vp, C.c_char_p, C.c_int, vp]
-        lib.ory_mesh_build.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, vp, C.c_char_p, C.c_int]
+        lib.ory_mesh_build.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, C.c_char_p, C.c_int]
         lib.ory_mesh_sizes.argtypes = [vp, vp]
         lib.ory_mesh_export.argtypes = [vp] + [vp] * 11
         lib.ory_mesh_facevtex.argtypes = [vp, C.c_int, vp]
@@ -58,6 +59,8 @@ def load():
         lib.ory_solver_rk_step.argtypes = [vp, C.c_double]
         lib.ory_solver_run_steps.argtypes = [vp, C.c_int, vp]
         lib.ory_solver_implicit_step.argtypes = [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp]
+        lib.ory_solver_typhon_steady.argtypes = [vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp, vp, vp]
+        lib.ory_solver_typhon_steady.restype = C.c_int
         lib.ory_solver_implicit_step.restype = C.c_int
         lib.ory_solver_bdlu_matvec.argtypes = [vp, vp, vp]
         lib.ory_kdif_new.argtypes = [vp, C.c_int, C.c_double, vp, vp, vp]
@@ -118,16 +121,19 @@ class Mesh:
         return m
 
     def build(self, dim, bcs):
-        """bcs: list of (family, kind, partner, translation(3), wall_velocity(3))."""
+        """bcs: list of (family, kind, partner, translation(3)[, wall_velocity(3)[, data(6)]]),
+        data the inlet / outlet parameters of BcKind."""
         n = len(bcs)
         fam = (C.c_char_p * n)(*[b[0].encode() for b in bcs])
         kind = np.array([b[1] for b in bcs], dtype=np.int32)
         par = (C.c_char_p * n)(*[(b[2] or "").encode() for b in bcs])
         tr = np.array([b[3] for b in bcs], dtype=np.float64).reshape(-1)
         wv = np.array([b[4] if len(b) > 4 else (0, 0, 0) for b in bcs], dtype=np.float64).reshape(-1)
+        bd = np.array([tuple(b[5]) + (0.0,) * (6 - len(b[5])) if len(b) > 5 else (0.0,) * 6 for b in bcs],
+                      dtype=np.float64).reshape(-1)
         err = C.create_string_buffer(256)
         rc = self.lib.ory_mesh_build(self.h, dim, n, C.cast(fam, C.c_void_p), _p(kind),
-                                     C.cast(par, C.c_void_p), _p(tr), _p(wv), err, 256)
+                                     C.cast(par, C.c_void_p), _p(tr), _p(wv), _p(bd), err, 256)
         if rc != 0:
             raise RuntimeError(err.value.decode())
         s = np.zeros(7, dtype=np.int32)
@@ -217,6 +223,22 @@ class Solver:
         if info == -2:
             raise RuntimeError("oracle implicit step: bad time step")
         return info, it.value, l1
+
+    def typhon_steady(self, cfl, cfl_max=None, cycle_res=0.1, global_res=1e-4, nkrylov=50, max_it=50,
+                      inv_res=1e-4, history_faces=(), max_iters=100000, max_cycles=1000):
+        """Typhon's steady implicit run from the current state: log10 residual per iteration,
+        per cycle the flux sums (F S) and S-weighted ghost primitive averages over
+        history_faces, and the iteration count at each cycle's end."""
+        cap = max_iters + 1
+        dp = np.array([cfl, cfl if cfl_max is None else cfl_max, cycle_res, global_res, inv_res], np.float64)
+        ip = np.array([nkrylov, max_it, max_iters, max_cycles], np.int32)
+        hist = np.ascontiguousarray(history_faces, np.int32)
+        lr, fs, ga, end = np.zeros(cap), np.zeros(5 * cap), np.zeros(5 * cap), np.zeros(cap, np.int32)
+        nc = C.c_int()
+        n = self.lib.ory_solver_typhon_steady(self.h, _p(dp), _p(ip), hist.size, _p(hist), cap, _p(lr), _p(fs),
+                                              _p(ga), _p(end), C.byref(nc))
+        k = nc.value
+        return lr[:n], fs[:5 * k].reshape(k, 5), ga[:5 * k].reshape(k, 5), end[:k]
 
     def bdlu_matvec(self, x):
         """y = A x with the BDLU matrix of the last implicit step; x is (ncell, 5)."""
