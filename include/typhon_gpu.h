@@ -40,7 +40,8 @@ extern "C" {
 #define TY_ERR_LSQ -9          /* least-squares matrix not positive definite */
 
 /* ---- option enums (values match the oracle and the Python binding) ---- */
-enum ty_scheme { TY_SCH_HLLC = 1, TY_SCH_RUSANOV = 2, TY_SCH_ROE = 3 };
+/* TY_SCH_HLLE: calc_flux_hlle.f90 (beta = 1) with the HLL Jacobian of its wave speeds. */
+enum ty_scheme { TY_SCH_HLLC = 1, TY_SCH_RUSANOV = 2, TY_SCH_ROE = 3, TY_SCH_HLLE = 5 };
 enum ty_highres { TY_HRES_NONE = 0, TY_HRES_MUSCL = 1, TY_HRES_MUSCLFAST = 2, TY_HRES_MUSCLUNS = 3 };
 enum ty_limiter {
   TY_LIM_NONE = 0, TY_LIM_MINMOD = 1, TY_LIM_ALBADA = 2, TY_LIM_VLEER = 3,
@@ -69,9 +70,21 @@ enum ty_rk {
  * ty_kdif_setup.  Not a Navier-Stokes boundary: the Navier-Stokes operations (residual,
  * steps, implicit, adjoint) refuse a mesh that has one; ty_set_params still sets the
  * arithmetic mode used by the KDIF calls. */
+/* Inlets and outlets (Typhon's SUBSONIC_INLET, SUBSONIC_OUTLET, SUPERSONIC_INLET,
+ * SUPERSONIC_OUTLET: setboco_ns_inlet_sub.f90, setboco_ns_outlet_sub.f90,
+ * setboco_ns_inlet_sup.f90, setboco_ns_outlet_sup.f90), ghost faces as in Typhon
+ * (bctype_of_nsboco, MENU_NS.f90:91-115).  Per-face parameters come from ty_set_bc_data:
+ *   TY_BC_INLET_SUB   total pressure, total temperature, flow direction (3): the state of
+ *                     those totals and direction at the inside static pressure
+ *   TY_BC_OUTLET_SUB  static pressure: the inside state's totals and direction, expanded
+ *                     isentropically to it
+ *   TY_BC_INLET_SUP   total pressure, total temperature, Mach number, direction (3)
+ *   TY_BC_OUTLET_SUP  none: the inside state (its Jacobian folded, ns_bocojacobian.f90)
+ * They need ty_spat_params.rgas > 0. */
 enum ty_bc {
   TY_BC_INTERIOR = 0, TY_BC_PERIODIC = 1, TY_BC_SYMMETRY = 2, TY_BC_WALL = 3, TY_BC_FARFIELD = 4,
-  TY_BC_NOSLIP = 5, TY_BC_HEAT = 6
+  TY_BC_NOSLIP = 5, TY_BC_HEAT = 6, TY_BC_INLET_SUB = 7, TY_BC_OUTLET_SUB = 8, TY_BC_INLET_SUP = 9,
+  TY_BC_OUTLET_SUP = 10
 };
 /* Arithmetic mode of the kernels.
  *   TY_MODE_EXACT: every FP64 operation in the order Typhon evaluates it, each rounded
@@ -183,6 +196,10 @@ int ty_rk_steps(ty_mesh* mesh, int32_t rk_method, double cfl, int32_t nsteps, do
  *         3 limiter ratios [3][ncell] (Barth post-limiter). */
 int ty_debug_get(ty_mesh* mesh, int32_t which, double* out);
 
+/* Inlet / outlet parameters per face: host [nface][6] (see ty_bc; rows of other faces are
+ * ignored).  Required before a Navier-Stokes operation on a mesh with inlets or outlets. */
+int ty_set_bc_data(ty_mesh* mesh, const double* data);
+
 /* Wait for the handle's stream. */
 int ty_synchronize(ty_mesh* mesh);
 
@@ -236,6 +253,8 @@ typedef struct ty_imp_stats {
   double res_l2[5];      /* L2 norm over cells of -sum(F S)/V per variable, before the update */
   double du_l1[5];       /* L1 norm of the update per variable (update_field.f90:54-60) */
   double lin_res;        /* final relative linear residual |b - A x| / |b| */
+  double du_mom;         /* sum over cells of the Euclidean norm of the momentum update (the
+                            vector part of Typhon's steady residual, update_field.f90:54-60) */
 } ty_imp_stats;
 /* One implicit step on the resident state: time step (per cell or global at p->cfl),
  * residual with flux Jacobians (HLL for HLLC and Roe, Rusanov's for Rusanov, viscous

@@ -58,7 +58,7 @@ class ImpStats(C.Structure):
     """ty_imp_stats"""
     _fields_ = [("info", C.c_int32), ("restarts", C.c_int32), ("matvecs", C.c_int32), ("reserved", C.c_int32),
                 ("dt_min", C.c_double), ("res_l2", C.c_double * 5), ("du_l1", C.c_double * 5),
-                ("lin_res", C.c_double)]
+                ("lin_res", C.c_double), ("du_mom", C.c_double)]
 
 
 class KdifParams(C.Structure):
@@ -95,6 +95,7 @@ _SIGS = {
     "ty_rk_step": ([C.c_void_p, C.c_int32, C.c_double], C.c_int),
     "ty_rk_steps": ([C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_double)], C.c_int),
     "ty_debug_get": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "ty_set_bc_data": ([C.c_void_p, C.c_void_p], C.c_int),
     "ty_synchronize": ([C.c_void_p], C.c_int),
     "ty_set_stream": ([C.c_void_p, C.c_void_p], C.c_int),
     "ty_profile_enable": ([C.c_void_p, C.c_int32], C.c_int),

@@ -39,6 +39,10 @@ int ty_adjoint_vjp(ty_mesh* h, double dt, const double* lamR, double* lamU) {
     tyi::set_error("ty_adjoint_vjp: first-order inviscid residual only (HIGHRES = NONE, no viscous flux)");
     return TY_ERR_UNSUPPORTED;
   }
+  if (h->o.scheme == TY_SCH_HLLE || h->inout_bc) {
+    tyi::set_error("ty_adjoint_vjp: HLLE flux and inlet / outlet boundaries have no adjoint");
+    return TY_ERR_UNSUPPORTED;
+  }
   DevMesh& m = h->m;
   int rc;
   if (!h->adj_face) {

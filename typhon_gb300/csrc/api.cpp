@@ -297,6 +297,10 @@ int ready(ty_mesh* h) {
     tyi::set_error("the mesh has heat-conduction (TY_BC_HEAT) boundaries: no Navier-Stokes boundary state");
     return TY_ERR_UNSUPPORTED;
   }
+  if (h->inout_bc && (!h->bcdata_set || !(h->o.rgas > 0.0))) {
+    tyi::set_error("inlets / outlets need ty_set_bc_data and ty_spat_params.rgas > 0");
+    return TY_ERR_STATE;
+  }
   TY_CU(cudaSetDevice(h->device));
   return TY_OK;
 }
@@ -420,6 +424,8 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
         part[f] = p;
       } else if (fbc[f] == TY_BC_HEAT) {
         h->heat_bc = true;
+      } else if (fbc[f] >= TY_BC_INLET_SUB && fbc[f] <= TY_BC_OUTLET_SUP) {
+        h->inout_bc = true;
       } else if (fbc[f] != TY_BC_SYMMETRY && fbc[f] != TY_BC_WALL && fbc[f] != TY_BC_FARFIELD &&
                  fbc[f] != TY_BC_NOSLIP) {
         tyi::set_error("unknown boundary kind");
@@ -540,9 +546,27 @@ int ty_mesh_info(const ty_mesh* h, int32_t* out) {
   return TY_OK;
 }
 
+int ty_set_bc_data(ty_mesh* h, const double* data) {
+  if (!h || !data) return TY_ERR_ARG;
+  TY_CU(cudaSetDevice(h->device));
+  const int nf = h->m.nf;
+  const size_t lf = h->m.ldf;
+  std::vector<double> d(6 * lf, 0.0);
+  for (int f = 0; f < nf; ++f)
+    for (int q = 0; q < 6; ++q) d[q * lf + f] = data[6 * (size_t)f + q];
+  if (!h->m.fbcd) {
+    if (int rc = h->upload(h->m.fbcd, d)) return rc;
+  } else {
+    TY_CU(cudaMemcpy(const_cast<double*>(h->m.fbcd), d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  h->bcdata_set = true;
+  h->prim_valid = false;
+  return TY_OK;
+}
+
 int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
   if (!h || !p) return TY_ERR_ARG;
-  if (p->scheme < TY_SCH_HLLC || p->scheme > TY_SCH_ROE || p->highres < 0 || p->highres > TY_HRES_MUSCLUNS ||
+  if (p->scheme < TY_SCH_HLLC || p->scheme > TY_SCH_HLLE || p->scheme == 4 || p->highres < 0 || p->highres > TY_HRES_MUSCLUNS ||
       p->limiter < 0 || p->limiter > TY_LIM_LIM03 || p->postlim < 0 || p->postlim > TY_POSTLIM_SUPERBARTH ||
       p->gradmeth < 0 || p->gradmeth > TY_GRAD_LSQW || (p->mode != TY_MODE_EXACT && p->mode != TY_MODE_FAST) ||
       !(p->gamma > 1.0)) {

@@ -34,6 +34,7 @@ struct DevMesh {
   const double* fn = nullptr;     // [3][ldf] unit normal
   const double* fs = nullptr;     // [ldf] surface
   const double* fwall = nullptr;  // [3][ldf] wall velocity
+  const double* fbcd = nullptr;   // [6][ldf] inlet / outlet parameters (ty_set_bc_data)
   const double* cvol = nullptr;   // [ldc]
   const double* sumS = nullptr;   // [nci] sum of face surfaces, colour order (time step)
   const double* dcg = nullptr;    // [3][ldf] centre(fc2) - centre(fc1) (LSQ, weighted for W-LSQ)

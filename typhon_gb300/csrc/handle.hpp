@@ -42,6 +42,7 @@ struct ty_mesh {
   SpatOpts o{};
   bool has_params = false, has_state = false, prim_valid = false, fast_ready = false;
   bool heat_bc = false;  // the mesh has TY_BC_HEAT (ghost-face) boundaries
+  bool inout_bc = false, bcdata_set = false;  // inlets / outlets, and their parameters uploaded
   std::vector<double> kd_k;  // host copy of the KDIF conductivity [nci]
   int nslot = 0;
   std::vector<void*> allocs;

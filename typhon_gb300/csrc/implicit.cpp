@@ -442,8 +442,9 @@ int ty_implicit_step(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
   if (rc) return rc;
   // 4. update U += dU
   IMP_CU(IMP_CALL(h, imp_update_state, m, S, im.x, im.part, im.scal + kScalMisc + 10, s));
-  if ((rc = fetch(h, kScalMisc + 10, 5))) return rc;
+  if ((rc = fetch(h, kScalMisc + 10, 6))) return rc;
   for (int v = 0; v < 5; ++v) st->du_l1[v] = im.pinned[kScalMisc + 10 + v];
+  st->du_mom = im.pinned[kScalMisc + 15];
   h->prim_valid = false;
   return TY_OK;
 }

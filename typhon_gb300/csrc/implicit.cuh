@@ -67,7 +67,7 @@ __device__ void face_jacobians(const SpatOpts& o, const double* L, const double*
     return;
   }
   double sl, sr;
-  if (o.scheme == TY_SCH_HLLC) {  // HLLC wave speeds (calc_flux_hllc.f90:86-118, beta = 1)
+  if (o.scheme == TY_SCH_HLLC || o.scheme == TY_SCH_HLLE) {  // HLLC / HLLE wave speeds (calc_flux_hllc.f90:86-118, calc_flux_hlle.f90:83-110, beta = 1)
     const double gig1 = g / (g - 1.0);
     double t1 = sqrt(R[0] / L[0]);
     double roe_rho = L[0] * t1;
@@ -157,6 +157,8 @@ __device__ void implicit_face_states(const DevMesh& m, const DevState& s, const 
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {
     farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);
+  } else if (kind >= TY_BC_INLET_SUB) {
+    inout_state(m, o, f, kind, QL, QR);
   } else if (kind == TY_BC_SYMMETRY) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = QL[v];
@@ -273,6 +275,12 @@ __global__ void __launch_bounds__(128) k_imp_face(DevMesh m, DevState s, SpatOpt
     fold = true;
   } else if (bkind == TY_BC_FARFIELD) {
     fold = farfield_jacobian(o, nx, ny, nz, QL, M);
+  } else if (bkind == TY_BC_OUTLET_SUP) {  // ns_bocojacobian.f90: dQr/dQl = I
+#pragma unroll
+    for (int k = 0; k < 25; ++k) M[k] = 0.0;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) M[i * 6] = 1.0;
+    fold = true;
   } else if (bkind == TY_BC_NOSLIP) {  // new: d(2 rho u_w - m, rho E + 2 rho |u_w|^2 - 2 u_w.m)/dU
     const double w[3] = {d3(m.fwall, m.ldf, f, 0), d3(m.fwall, m.ldf, f, 1), d3(m.fwall, m.ldf, f, 2)};
 #pragma unroll
@@ -676,7 +684,7 @@ __global__ void k_axpy_multi(double* __restrict__ x, const double* __restrict__ 
 // U += x (update_field.f90:38) on the resident state; partial sums of |x| per variable
 __global__ void __launch_bounds__(kRedThreads) k_imp_update(DevMesh m, double* __restrict__ u0,
                                                              const double* __restrict__ x, double* __restrict__ part) {
-  double s[5] = {0, 0, 0, 0, 0};
+  double s[6] = {0, 0, 0, 0, 0, 0};
   for (int c = blockIdx.x * kRedThreads + threadIdx.x; c < m.nci; c += gridDim.x * kRedThreads) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
@@ -684,9 +692,11 @@ __global__ void __launch_bounds__(kRedThreads) k_imp_update(DevMesh m, double* _
       u0[v * (size_t)m.ldc + c] = u0[v * (size_t)m.ldc + c] + d;
       s[v] += fabs(d);
     }
+    const double mx = x[5 * (size_t)c + 2], my = x[5 * (size_t)c + 3], mz = x[5 * (size_t)c + 4];
+    s[5] += sqrt(mx * mx + my * my + mz * mz);
   }
 #pragma unroll
-  for (int v = 0; v < 5; ++v) {
+  for (int v = 0; v < 6; ++v) {
     double t = block_sum(s[v]);
     if (threadIdx.x == 0) part[(size_t)v * kRedBlocks + blockIdx.x] = t;
   }
@@ -827,7 +837,7 @@ cudaError_t imp_update_state(const DevMesh& m, DevState& s, const double* x, dou
                              cudaStream_t st) {
   const unsigned g = red_grid(m.nci);
   k_imp_update<<<g, kRedThreads, 0, st>>>(m, s.u0, x, part);
-  k_red_final<<<5, kRedThreads, 0, st>>>(part, (int)g, kRedBlocks, out);
+  k_red_final<<<6, kRedThreads, 0, st>>>(part, (int)g, kRedBlocks, out);
   return cudaGetLastError();
 }
 

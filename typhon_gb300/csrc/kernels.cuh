@@ -162,6 +162,56 @@ __device__ __forceinline__ void farfield_state(const SpatOpts& o, double nx, dou
   }
 }
 
+// inlet / outlet states from the inside state qi (setboco_ns_inlet_sub.f90:64-96,
+// setboco_ns_outlet_sub.f90:31-60, setboco_ns_inlet_sup.f90:75-101, setboco_ns_outlet_sup.f90)
+// with the isentropic relations of EQNS.f90:139-219 (pi_ti_mach_dir2nspri,
+// pi_ti_ps_dir2nspri, nspri2pi_ti_mach_dir), in their operation order
+__device__ void inout_state(const DevMesh& m, const SpatOpts& o, int f, int kind, const double* qi, double* qo) {
+  if (kind == TY_BC_OUTLET_SUP) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) qo[v] = qi[v];
+    return;
+  }
+  const double g = o.gamma, r = o.rgas, g1 = g - 1.0;
+  const size_t lf = m.ldf;
+  const double* D = m.fbcd + f;
+  if (kind == TY_BC_INLET_SUP) {
+    const double dx = D[3 * lf], dy = D[4 * lf], dz = D[5 * lf];
+    const double dn = sqrt(dx * dx + dy * dy + dz * dz);
+    const double mach = D[2 * lf];
+    const double fm = 1.0 / (1.0 + .5 * g1 * (mach * mach));
+    const double ts = D[lf] * fm;
+    const double a = sqrt(g * r * ts);
+    qo[1] = D[0] * pow(fm, g / g1);
+    qo[0] = qo[1] / (r * ts);
+    const double va = mach * a;
+    qo[2] = va * (dx / dn); qo[3] = va * (dy / dn); qo[4] = va * (dz / dn);
+    return;
+  }
+  double pi, ti, ps, ux, uy, uz;
+  if (kind == TY_BC_INLET_SUB) {
+    pi = D[0]; ti = D[lf]; ps = qi[1];
+    const double dx = D[2 * lf], dy = D[3 * lf], dz = D[4 * lf];
+    const double dn = sqrt(dx * dx + dy * dy + dz * dz);
+    ux = dx / dn; uy = dy / dn; uz = dz / dn;
+  } else {  // TY_BC_OUTLET_SUB: totals and direction of the inside state
+    double fmv = qi[2] * qi[2] + qi[3] * qi[3] + qi[4] * qi[4];
+    const double n = sqrt(fmv);
+    ux = qi[2] / n; uy = qi[3] / n; uz = qi[4] / n;
+    fmv = fmv / (g * qi[1]) * qi[0];
+    fmv = 1.0 + 0.5 * g1 * fmv;
+    pi = qi[1] * pow(fmv, g / g1);
+    ti = qi[1] / r / qi[0] * fmv;
+    ps = D[0];
+  }
+  double fm = pow(pi / ps, g1 / g);
+  if (fm < 1.0) fm = 1.0;  // Typhon: "Bad ratio Pi/P : truncated to 1."
+  qo[1] = ps;
+  qo[0] = ps / (r * ti) * fm;
+  const double va = sqrt((fm - 1.0) * 2.0 / g1) * sqrt(g * ps / qo[0]);
+  qo[2] = va * ux; qo[3] = va * uy; qo[4] = va * uz;
+}
+
 // ghost states: periodic copy, symmetry mirror (velocity reflected across the face),
 // adiabatic moving wall (setboco_ns_flux.f90, cell-state mode: pressure copied, temperature
 // of the cell minus lflux d / conduct with lflux = 0, velocity reflected about the wall's)
@@ -172,11 +222,14 @@ __global__ void k_ghost_prim(DevMesh m, double* __restrict__ prim, SpatOpts o) {
   const size_t ld = m.ldc;
   const int kind = m.fbc[f];
   double vx = prim[2 * ld + src], vy = prim[3 * ld + src], vz = prim[4 * ld + src];
-  if (kind == TY_BC_FARFIELD) {
+  if (kind == TY_BC_FARFIELD || kind >= TY_BC_INLET_SUB) {
     double q[5], out[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) q[v] = prim[v * ld + src];
-    farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), q, out);
+    if (kind == TY_BC_FARFIELD)
+      farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), q, out);
+    else
+      inout_state(m, o, f, kind, q, out);
 #pragma unroll
     for (int v = 0; v < 5; ++v) prim[v * ld + g] = out[v];
     return;
@@ -377,6 +430,42 @@ __device__ __forceinline__ void mirror(const DevMesh& m, int f, double q[5]) {
 
 // ---------------------------------------------------------------------------
 // Riemann fluxes per unit area, F = (mass, energy, momentum x, y, z)
+
+// calc_flux_hlle.f90:83-150 (beta = 1), the Roe average of calc_roe_states.f90:37-53
+__device__ void flux_hlle(double g, const double* L, const double* R, double nx, double ny, double nz, double* F) {
+  const double ig1 = 1.0 / (g - 1.0);
+  const double gig1 = g / (g - 1.0);
+  double t1 = sqrt(R[0] / L[0]);
+  double roe_rho = L[0] * t1;
+  double kl0 = 1.0 / (1.0 + t1);
+  double kr0 = t1 * kl0;
+  double rux = kl0 * L[2] + kr0 * R[2], ruy = kl0 * L[3] + kr0 * R[3], ruz = kl0 * L[4] + kr0 * R[4];
+  double sqL = L[2] * L[2] + L[3] * L[3] + L[4] * L[4];
+  double sqR = R[2] * R[2] + R[3] * R[3] + R[4] * R[4];
+  double h1 = gig1 * L[1] / L[0] + 0.5 * sqL;
+  double h2 = gig1 * R[1] / R[0] + 0.5 * sqR;
+  h1 = kl0 * h1 + kr0 * h2;
+  double roe_p = (h1 - 0.5 * (rux * rux + ruy * ruy + ruz * ruz)) * roe_rho / gig1;
+  double vnl = L[2] * nx + L[3] * ny + L[4] * nz;
+  double vnr = R[2] * nx + R[3] * ny + R[4] * nz;
+  double al = sqrt(g * L[1] / L[0]);
+  double ar = sqrt(g * R[1] / R[0]);
+  double vm = rux * nx + ruy * ny + ruz * nz;
+  double am = sqrt(g * roe_p / roe_rho);
+  double rel = ig1 * L[1] + .5 * L[0] * sqL;
+  double rer = ig1 * R[1] + .5 * R[0] * sqR;
+  double sl = fmin(fmin(0.0, vnl - al), vm - am);
+  double sr = fmax(fmax(0.0, vnr + ar), vm + am);
+  double iks = 1.0 / (sr - sl);
+  double kl = sr * iks, kr = -sl * iks, ku = sl * sr * iks;
+  double wl = kl * vnl - ku, wr = kr * vnr + ku;
+  F[0] = wl * L[0] + wr * R[0];
+  F[1] = wl * rel + wr * rer + (kl * vnl * L[1] + kr * vnr * R[1]);
+  double ml = wl * L[0], mr = wr * R[0], pp = kl * L[1] + kr * R[1];
+  F[2] = ml * L[2] + mr * R[2] + pp * nx;
+  F[3] = ml * L[3] + mr * R[3] + pp * ny;
+  F[4] = ml * L[4] + mr * R[4] + pp * nz;
+}
 __device__ void flux_hllc(double g, const double* L, const double* R, double nx, double ny, double nz, double* F) {
   const double ig1 = 1.0 / (g - 1.0);
   const double gig1 = g / (g - 1.0);
@@ -705,6 +794,7 @@ __device__ __forceinline__ void face_flux_fast(const DevMesh& m, const DevState&
   } else {
     if (o.scheme == TY_SCH_ROE) flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, 1.0, F);
     else if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
+    else if (o.scheme == TY_SCH_HLLE) flux_hlle(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
     if (o.viscous != TY_VISC_NONE) add_viscous(m, s, o, f, F);
 #pragma unroll
@@ -722,10 +812,12 @@ __device__ __forceinline__ void face_flux(const DevMesh& m, const DevState& s, c
   if constexpr (kFast) {
     if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
+    else if (o.scheme == TY_SCH_HLLE) flux_hlle(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, 1.0, F);  // unit surface
   } else {
     if (o.scheme == TY_SCH_HLLC) flux_hllc(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
+    else if (o.scheme == TY_SCH_HLLE) flux_hlle(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_roe(o.gamma, o.entropy_fix, QL, QR, nx, ny, nz, F);
   }
   if (o.viscous != TY_VISC_NONE) add_viscous(m, s, o, f, F);
@@ -747,6 +839,8 @@ __global__ void __launch_bounds__(kBlock) k_face_flux(DevMesh m, DevState s, Spa
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {
     farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);
+  } else if (kind >= TY_BC_INLET_SUB) {
+    inout_state(m, o, f, kind, QL, QR);
   } else if (kind == TY_BC_SYMMETRY) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = QL[v];
@@ -825,6 +919,8 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_lim(DevMesh m, DevState s,
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {
     farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);
+  } else if (kind >= TY_BC_INLET_SUB) {
+    inout_state(m, o, f, kind, QL, QR);
   } else if (kind == TY_BC_SYMMETRY) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = QL[v];
@@ -981,6 +1077,8 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_fast(DevMesh m, DevState s
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {
     farfield_state(o, d3(m.fn, m.ldf, f, 0), d3(m.fn, m.ldf, f, 1), d3(m.fn, m.ldf, f, 2), QL, QR);
+  } else if (kind >= TY_BC_INLET_SUB) {
+    inout_state(m, o, f, kind, QL, QR);
   } else if (kind == TY_BC_SYMMETRY) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = QL[v];

@@ -144,7 +144,7 @@ int ty_umesh_add_vertex_mark(ty_umesh* um, const char* family, int32_t ntag, con
 }
 int ty_umesh_add_bc(ty_umesh* um, const char* family, int32_t kind, const char* partner,
                     const double* t3, const double* w3) {
-  if (!um || !family || kind < TY_BC_PERIODIC || kind > TY_BC_HEAT) return TY_ERR_ARG;
+  if (!um || !family || kind < TY_BC_PERIODIC || kind > TY_BC_OUTLET_SUP) return TY_ERR_ARG;
   BcIn b;
   b.family = upper(family);
   b.partner = partner ? upper(partner) : "";
@@ -405,7 +405,7 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
         ffam[f] = b.def;
         fwall[3 * (size_t)f] = d.wallvel.x; fwall[3 * (size_t)f + 1] = d.wallvel.y; fwall[3 * (size_t)f + 2] = d.wallvel.z;
         cv[g] = cv[a];
-        if (d.kind == TY_BC_HEAT) {  // ghost face (init_ustboco_ghostface.f90:46-56)
+        if (d.kind == TY_BC_HEAT || d.kind >= TY_BC_INLET_SUB) {  // ghost face (init_ustboco_ghostface.f90:46-56)
           cv[g] = 0.0;
           cc[g] = fc[f];
         } else if (d.kind == TY_BC_SYMMETRY) {

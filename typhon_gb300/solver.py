@@ -21,7 +21,7 @@ from .umesh import MeshDesc
 
 # option names as in Typhon's SPAT_PARAM / TIME_PARAM blocks (SOURCE/PARAM/def_spat.f90,
 # def_time.f90) -> C ABI enum values
-SCHEME = {"HLLC": 1, "RUSANOV": 2, "ROE": 3}
+SCHEME = {"HLLC": 1, "RUSANOV": 2, "ROE": 3, "HLLE": 5, "HLL": 5}
 HIGHRES = {"NONE": 0, "MUSCL": 1, "MUSCL-FAST": 2, "MUSCL-UNS": 3}
 LIMITER = {"NONE": 0, "MINMOD": 1, "ALBADA": 2, "VAN_ALBADA": 2, "VAN_LEER": 3, "VANLEER": 3, "SUPERBEE": 4,
            "KIM3": 5, "LIM03": 6}
@@ -191,7 +191,70 @@ class Grid:
         st = _capi.ImpStats()
         _capi.check(self.lib.ty_implicit_step(self.h, C.byref(p), C.byref(st)), "ty_implicit_step")
         return dict(info=st.info, restarts=st.restarts, matvecs=st.matvecs, dt_min=st.dt_min,
-                    res_l2=np.array(st.res_l2[:]), du_l1=np.array(st.du_l1[:]), lin_res=st.lin_res)
+                    res_l2=np.array(st.res_l2[:]), du_l1=np.array(st.du_l1[:]), lin_res=st.lin_res,
+                    du_mom=st.du_mom)
+
+    def set_boundary_params(self, params):
+        """Inlet / outlet parameters by family: {family: values} with, per kind (BCS of
+        Typhon's BOCO blocks), SUBSONIC_INLET (PI, TI, dir_x, dir_y, dir_z), SUBSONIC_OUTLET
+        (P,), SUPERSONIC_INLET (PI, TI, MACH, dir_x, dir_y, dir_z)."""
+        m = self.mesh
+        data = np.zeros((m.nface, 6))
+        for fam, vals in params.items():
+            vals = tuple(map(float, vals))
+            data[m.faces_of(fam), :len(vals)] = vals
+        _capi.check(self.lib.ty_set_bc_data(self.h, np.ascontiguousarray(data).ctypes.data), "ty_set_bc_data")
+
+    def ns_steady(self, cfl, cfl_max=None, cycle_res=0.1, global_res=1e-4, inversion="GMRES", nkrylov=50,
+                  max_it=50, inv_res=1e-4, precision="fp64", history=None, max_iters=100000, max_cycles=1000,
+                  cycle_max_it=None):
+        """Typhon's steady implicit run of one zone from the resident state (integration.f90,
+        integration_cycle.f90, integration_cyclezone.f90, check_end_cycle.f90; the CFL law of
+        calc_zonetimestep.f90, cfl (1 - log10 of the zone's and the world's residual drops,
+        at least 1) capped at cfl_max; the residual of update_field.f90 with the reference
+        state of calc_refcons.f90).  history: a family whose summed face fluxes F S after each
+        cycle are returned (integ_ustboco.f90's QUANTITY-FLUX history: mass, energy,
+        momentum).  Each iteration is one implicit_step on the GPU; three scalars per
+        iteration come back to the host.  Returns dict(log_res, cycle_end, flux)."""
+        m, nci = self.mesh, self.nci
+        V = m.cell_volume[:nci]
+        U = self.get_cons()[:, :nci]
+        tot = float(np.sum(V))
+        ref0, ref1 = float(np.sum(U[0] * V)) / tot, float(np.sum(U[1] * V)) / tot
+        refv = np.sqrt(ref0 * ref1)
+        hist = m.faces_of(history) if history else None
+        tiny = np.finfo(np.float64).tiny
+        cfl_max = cfl if cfl_max is None else cfl_max
+        w_ref, w_cur, z_reforig = 1.0, 1.0, None
+        log_res, cycle_end, flux = [], [], []
+        iters = 0
+        for icycle in range(1, max_cycles + 1):
+            wcur_res, wres_ref = w_cur, w_ref
+            w_cur = tiny
+            z_ref = z_cur = w_cur
+            maxit = min(cycle_max_it or max_iters, max_iters - iters)
+            it_loc = 0
+            while True:
+                it_loc += 1
+                iters += 1
+                c = cfl * max(1.0, 1.0 - np.log10(z_cur / z_ref) - np.log10(wcur_res / wres_ref))
+                st = self.implicit_step(min(c, cfl_max), inversion=inversion, nkrylov=nkrylov, max_it=max_it,
+                                        inv_res=inv_res, precision=precision)
+                z_cur = st["du_l1"][0] / ref0 + st["du_l1"][1] / ref1 + st["du_mom"] / refv
+                z_ref = max(z_ref, z_cur)
+                log_res.append(np.log10(z_cur))
+                if z_cur / z_ref <= cycle_res or it_loc == maxit:
+                    break
+            if icycle == 1:
+                z_reforig = z_ref
+            if z_cur / z_reforig >= w_cur / w_ref:
+                w_cur, w_ref = z_cur, z_reforig
+            if hist is not None:
+                flux.append(self.debug("flux")[:, hist].sum(axis=1))
+            cycle_end.append(iters)
+            if w_cur / w_ref <= global_res or iters >= max_iters:
+                break
+        return dict(log_res=np.array(log_res), cycle_end=np.array(cycle_end), flux=np.array(flux))
 
     def implicit_get(self, which):
         """Blocks and vectors of the last implicit step (row-major 5x5 blocks)."""

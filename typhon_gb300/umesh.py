@@ -26,6 +26,8 @@ NVTEX = {ELEM_BAR2: 2, ELEM_TRI3: 3, ELEM_QUAD4: 4, ELEM_TETRA4: 4, ELEM_PENTA6:
 DIM = {ELEM_BAR2: 1, ELEM_TRI3: 2, ELEM_QUAD4: 2, ELEM_TETRA4: 3, ELEM_PENTA6: 3, ELEM_HEXA8: 3}
 
 BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD, BC_NOSLIP, BC_HEAT = 1, 2, 3, 4, 5, 6
+# inlets and outlets (parameters per face through Grid.set_boundary_params)
+BC_INLET_SUB, BC_OUTLET_SUB, BC_INLET_SUP, BC_OUTLET_SUP = 7, 8, 9, 10
 
 
 @dataclass
