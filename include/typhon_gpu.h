@@ -225,7 +225,11 @@ int ty_profile_read(ty_mesh* mesh, int32_t n, double* ms, int32_t* launches);
 typedef enum {
   TY_KRYLOV_GMRES = 0,   /* Typhon's bdlu_gmres (bdlu_gmres.f90:50-217): MGS, no preconditioner */
   TY_KRYLOV_FGMRES = 1,  /* flexible GMRES(m), CGS2, right block-Jacobi, assembled matrix (new) */
-  TY_KRYLOV_JFNK = 2     /* flexible GMRES(m), CGS2, block-Jacobi, Jacobian-free products (new) */
+  TY_KRYLOV_JFNK = 2,    /* flexible GMRES(m), CGS2, block-Jacobi, Jacobian-free products (new) */
+  TY_KRYLOV_BICGSTAB = 3 /* Typhon's bdlu_bicgstab (bdlu_bicgstab.f90:40-80), its default for the
+                            Navier-Stokes implicit method: x0 = b / diag, stopped when
+                            sum|alpha p + omega s| < INV_RES sum|x0| or after max_it + 1
+                            iterations; nkrylov is not used */
 } ty_krylov;
 typedef enum {
   TY_PREC_FP64 = 0,      /* everything in FP64 */

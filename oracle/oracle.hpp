@@ -229,6 +229,8 @@ struct Solver {
   void bdlu_yeqax(const double* x, double* y) const;
   void bdlu_yeqmaxpz(const double* x, const double* z, double* y) const;
   int bdlu_gmres(double* sol);                   // sol: RHS in, solution out (5*ncell, per cell)
+  int bdlu_bicgstab(double* sol);                // bdlu_bicgstab.f90, same convention
+  int inversion = 0;                             // 0 GMRES, 1 BICGSTAB
   // one implicit step: time step (global min or local), residual + Jacobians, solve, update;
   // returns GMRES restarts (info) and the L1 norm of the update per variable in l1[5]
   int implicit_step(double cfl_, bool local_dt, double* l1);

@@ -246,6 +246,8 @@ int ory_solver_typhon_steady(void* s, const double* dp, const int* ip, int nhist
   *ncycle = ncy;
   return n;
 }
+// linear solver of the implicit step: 0 Typhon's GMRES, 1 Typhon's BiCGSTAB
+void ory_solver_set_inversion(void* s, int kind) { ((Solver*)s)->inversion = kind; }
 // y = A x with the BDLU matrix of the last implicit step (x, y: 5 per cell, per-cell blocks)
 void ory_solver_bdlu_matvec(void* s, const double* x, double* y) { ((Solver*)s)->bdlu_yeqax(x, y); }
 

@@ -1137,6 +1137,51 @@ static double dotp(const std::vector<double>& a, const std::vector<double>& b, s
 // bdlu_gmres (SOURCE/MATH/bdlu_gmres.f90:50-217): restarted GMRES, modified Gram-Schmidt,
 // Givens rotations, x0 = b / diag, stop when |r|/|b| < INV_RES * |x0|_1, at most 2*max_it
 // restarts.  Returns the number of restarts - 1 (info), or -1 if not converged.
+// bdlu_bicgstab.f90:40-80 over all cells (ghost rows are identity with a zero right-hand side)
+int Solver::bdlu_bicgstab(double* sol) {
+  const size_t dim = 5 * (size_t)m->ncell;
+  std::vector<double> r1(dim), r2(dim), p(dim), s(dim), t(dim), v(dim);
+  auto dotv = [&](const std::vector<double>& a, const std::vector<double>& b) {
+    double x = 0.0;
+    for (size_t i = 0; i < dim; ++i) x = x + a[i] * b[i];
+    return x;
+  };
+  for (size_t i = 0; i < dim; ++i) p[i] = sol[i];
+  for (int c = 0; c < m->ncell; ++c)
+    for (int b = 0; b < 5; ++b) sol[5 * (size_t)c + b] = p[5 * (size_t)c + b] / bdiag[25 * (size_t)c + b * 5 + b];
+  double ref = 0.0;
+  for (size_t i = 0; i < dim; ++i) ref = ref + std::fabs(sol[i]);
+  bdlu_yeqmaxpz(sol, p.data(), r1.data());
+  r2 = r1;
+  double err = std::numeric_limits<double>::max(), rho0 = 0.0, rho1, beta, alpha = 0.0, omega = 0.0;
+  int nit = 0;
+  while (err >= ref * inv_res && nit <= imp_max_it) {
+    rho1 = dotv(r1, r2);
+    if (nit == 0) {
+      p = r1;
+    } else {
+      beta = (rho1 / rho0) * (alpha / omega);
+      for (size_t i = 0; i < dim; ++i) p[i] = p[i] - omega * v[i];
+      for (size_t i = 0; i < dim; ++i) p[i] = r1[i] + beta * p[i];
+    }
+    bdlu_yeqax(p.data(), v.data());
+    alpha = rho1 / dotv(r2, v);
+    for (size_t i = 0; i < dim; ++i) s[i] = r1[i] - alpha * v[i];
+    bdlu_yeqax(s.data(), t.data());
+    double tt = 0.0;
+    for (size_t i = 0; i < dim; ++i) tt = tt + t[i] * t[i];
+    omega = dotv(t, s) / tt;
+    err = 0.0;
+    for (size_t i = 0; i < dim; ++i) err = err + std::fabs(alpha * p[i] + omega * s[i]);
+    for (size_t i = 0; i < dim; ++i) sol[i] = sol[i] + alpha * p[i] + omega * s[i];
+    for (size_t i = 0; i < dim; ++i) r1[i] = s[i] - omega * t[i];
+    rho0 = rho1;
+    ++nit;
+  }
+  gmres_iters = nit;
+  return nit <= imp_max_it ? nit - 1 : -1;
+}
+
 int Solver::bdlu_gmres(double* sol) {
   const size_t dim = 5 * (size_t)m->ncell;
   const int nk = nkrylov;
@@ -1229,7 +1274,7 @@ int Solver::implicit_step(double cfl_, bool local_dt, double* l1) {
   for (int c = 0; c < nc; ++c)
     for (int v = 0; v < 5; ++v) x[5 * (size_t)c + v] = residu[v * (size_t)nc + c];
   rhs_b = x;
-  int info = bdlu_gmres(x.data());
+  int info = inversion == 1 ? bdlu_bicgstab(x.data()) : bdlu_gmres(x.data());
   for (int c = 0; c < nc; ++c)
     for (int v = 0; v < 5; ++v) residu[v * (size_t)nc + c] = x[5 * (size_t)c + v];
   for (size_t k = 0; k < cons.size(); ++k) cons[k] = cons[k] + residu[k];  // update_field.f90:38

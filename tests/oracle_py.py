@@ -61,6 +61,7 @@ def load():
         lib.ory_solver_implicit_step.argtypes = [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp]
         lib.ory_solver_typhon_steady.argtypes = [vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp, vp, vp]
         lib.ory_solver_typhon_steady.restype = C.c_int
+        lib.ory_solver_set_inversion.argtypes = [vp, C.c_int]
         lib.ory_solver_implicit_step.restype = C.c_int
         lib.ory_solver_bdlu_matvec.argtypes = [vp, vp, vp]
         lib.ory_kdif_new.argtypes = [vp, C.c_int, C.c_double, vp, vp, vp]
@@ -223,6 +224,10 @@ class Solver:
         if info == -2:
             raise RuntimeError("oracle implicit step: bad time step")
         return info, it.value, l1
+
+    def set_inversion(self, name):
+        """Linear solver of the implicit step: GMRES or BICGSTAB (Typhon's bdlu_*)."""
+        self.lib.ory_solver_set_inversion(self.h, {"GMRES": 0, "BICGSTAB": 1}[name])
 
     def typhon_steady(self, cfl, cfl_max=None, cycle_res=0.1, global_res=1e-4, nkrylov=50, max_it=50,
                       inv_res=1e-4, history_faces=(), max_iters=100000, max_cycles=1000):

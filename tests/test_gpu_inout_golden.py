@@ -111,3 +111,33 @@ def test_gmres_golden_history(ty, golden_dir, mode):
     for c in range(7):
         assert ["%.5E" % v for v in out["flux"][c]] == ["%.5E" % v for v in gold[c]], c
     g.close()
+
+
+def test_bicgstab_step_matches_oracle(ty, golden_dir):
+    md, om, g, s = setup(ty, golden_dir, SUPERSONIC_CASE, perturb=0.05)
+    s.set_inversion("BICGSTAB")
+    nci = md.ncell_int
+    U0 = g.get_cons()
+    st = g.implicit_step(8.0, "BICGSTAB", max_it=50, inv_res=1e-8)
+    info, it, l1 = s.implicit_step(8.0, max_it=50, inv_res=1e-8)
+    du = g.get_cons() - U0
+    du_o = s.get("cons")[:, :nci] - U0
+    assert st["info"] >= 0 and info >= 0
+    assert abs(st["restarts"] - it) <= 1          # iterations, up to a tie at the stopping test
+    assert np.linalg.norm(du - du_o) <= 1e-7 * np.linalg.norm(du_o)
+    assert st["lin_res"] < 1e-6
+
+
+def test_bicgstab_golden_run(ty, golden_dir):
+    """NRG/TIME/IMPLICIT/BICGSTAB-RUSANOV on the GPU: fifteen cycles as in the golden file,
+    and the converged state of the oracle's run."""
+    md, om, g, s = setup(ty, golden_dir, SUPERSONIC_CASE)
+    out = g.ns_steady(2.0, 50.0, cycle_res=0.3, global_res=1e-12, inversion="BICGSTAB", max_it=50, inv_res=1e-1)
+    s.set_inversion("BICGSTAB")
+    lr, _, _, end = s.typhon_steady(2.0, 50.0, cycle_res=0.3, global_res=1e-12, max_it=50, inv_res=1e-1)
+    assert len(out["cycle_end"]) == len(end) == 15
+    nci = md.ncell_int
+    U, Uo = g.get_cons(), s.get("cons")[:, :nci]
+    for v in range(5):
+        assert np.abs(U[v] - Uo[v]).max() <= 1e-9 * np.abs(Uo[v]).max() + 1e-12, v
+    g.close()

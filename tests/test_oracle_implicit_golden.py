@@ -8,9 +8,10 @@ The oracle's restatement (mesh, ghost faces, HLLE, boundary states, flux Jacobia
 assembly, GMRES, the steady driver's CFL law and residual, integ_ustboco's sums) reproduces
 every printed digit of both history files over the seven cycles.
 
-NRG/TIME/IMPLICIT/BICGSTAB-RUSANOV writes only the S-weighted average of the ghost state at
-a symmetry plane, which first-order runs never update: it checks the Mach-4 initial state
-(init_ns_ust.f90) and the rect4x1.cgns mesh.
+NRG/TIME/IMPLICIT/BICGSTAB-RUSANOV (rect4x1.cgns, Rusanov, supersonic inlets and outlet,
+Typhon's BiCGSTAB with the CFL ramp from 2 to 50) writes only the S-weighted average of the
+ghost state at a symmetry plane, which first-order runs never update: the file pins the
+Mach-4 initial state (init_ns_ust.f90) and, by its length, the fifteen cycles the run takes.
 """
 import numpy as np
 
@@ -80,12 +81,17 @@ def test_bicgstab_case_initial_state(golden_dir):
     rho, p, u = init_state(1e5, 300.0, 4.0)
     hv = read_history(golden_dir / "IMPLICIT-BICGSTAB-RUSANOV__histovarNS_DOWN")
     assert [fortran_e(v) for v in (rho, p, u[0], u[1], u[2])] == [fortran_e(v) for v in hv[0]]
-    # the ghost states the driver averages are that initial state after a few implicit steps
+    # the full run: Typhon's BiCGSTAB (its default, INV_RES 1e-1, IMP_MAX_IT 50), CFL 2 ramped
+    # to 50 by the residual, RESIDUALS 0.3 per cycle down to 1e-12: fifteen cycles, as the
+    # golden file has, each printing the initial ghost state
     prim = np.zeros((5, m.ncell))
     prim[0], prim[1], prim[2] = rho, p, u[0]
     s = op.Solver(m, op.SCH_RUSANOV, gamma=GAMMA, rgas=RGAS)
     s.set_prim(prim)
-    lr, flux, ghost, end = s.typhon_steady(2.0, 50.0, cycle_res=0.3, global_res=1e-12, nkrylov=10, max_it=50,
-                                          inv_res=1e-4, history_faces=down, max_iters=6, max_cycles=3)
+    s.set_inversion("BICGSTAB")
+    lr, flux, ghost, end = s.typhon_steady(2.0, 50.0, cycle_res=0.3, global_res=1e-12, max_it=50, inv_res=1e-1,
+                                          history_faces=down)
+    assert len(end) == len(hv) == 15
+    assert lr[-1] - lr[0] < -12.0
     for c in range(len(end)):
         assert [fortran_e(v) for v in ghost[c]] == [fortran_e(v) for v in hv[c]]

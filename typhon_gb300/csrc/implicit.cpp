@@ -121,11 +121,12 @@ int ensure_buffers(ty_mesh* h, const ty_imp_params* p) {
     im.fp32_blocks = true;
   }
   const size_t n = 5 * (size_t)m.nci;
-  const int nk = p->nkrylov;
-  if (im.nk < nk || (need32 && !im.Z32) || (!need32 && p->krylov != TY_KRYLOV_GMRES && !im.Z)) {
+  const int nk = p->krylov == TY_KRYLOV_BICGSTAB ? std::max(p->nkrylov, 5) : p->nkrylov;
+  const bool gm = p->krylov == TY_KRYLOV_GMRES || p->krylov == TY_KRYLOV_BICGSTAB;  // no preconditioned basis
+  if (im.nk < nk || (need32 && !im.Z32) || (!need32 && !gm && !im.Z)) {
     const int cap = std::max(nk, im.nk);
     if ((rc = grow(h, im.V, (size_t)(cap + 1) * n))) return rc;
-    if (p->krylov != TY_KRYLOV_GMRES || im.Z || im.Z32) {
+    if (!gm || im.Z || im.Z32) {
       if (need32 || im.Z32) { if ((rc = grow(h, im.Z32, (size_t)cap * n))) return rc; }
       if (!need32 || im.Z) { if ((rc = grow(h, im.Z, (size_t)cap * n))) return rc; }
     }
@@ -150,6 +151,44 @@ int put(ty_mesh* h, int off, const double* v, int k) {
   std::memcpy(h->imp.pinned + off, v, k * sizeof(double));
   IMP_CU(cudaMemcpyAsync(h->imp.scal + off, h->imp.pinned + off, k * sizeof(double), cudaMemcpyHostToDevice,
                          h->stream));
+  return TY_OK;
+}
+
+// ---- Typhon's bdlu_bicgstab on the device (bdlu_bicgstab.f90:40-80) ----
+// r1 = im.r, and r2, p, v, s, t in the first five Krylov vectors
+int bicgstab_typhon(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
+  ImpState& im = h->imp;
+  const DevMesh& m = h->m;
+  const size_t n = 5 * (size_t)m.nci;
+  cudaStream_t s = h->stream;
+  double* P = im.pinned;
+  auto V = [&](int i) { return im.V + (size_t)i * n; };
+  double* sc = im.scal + kScalMisc + 4;  // 8 device scalars
+  IMP_CU(IMP_CALL(h, imp_x0_diag, m, im, im.b, im.x, s));
+  IMP_CU(IMP_CALL(h, imp_asum, im.x, n, im.part, im.scal + kScalMisc, s));
+  if (int rc = fetch(h, kScalMisc, 1)) return rc;
+  const double ref = P[kScalMisc];
+  IMP_CU(IMP_CALL(h, imp_matvec, m, im, im.x, im.b, im.r, s, &h->prof));  // r1 = b - A x0
+  IMP_CU(cudaMemcpyAsync(V(0), im.r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));  // r2 = r1
+  double err = DBL_MAX;
+  int nit = 0, matvecs = 1;
+  while (err >= ref * p->inv_res && nit <= p->max_it) {
+    IMP_CU(IMP_CALL(h, imp_bicgstab_iter, m, im, im.x, im.r, V(0), V(1), V(2), V(3), V(4), nit == 0 ? 1 : 0,
+                    im.part, sc, s, &h->prof));
+    matvecs += 2;
+    if (int rc = fetch(h, kScalMisc + 4 + 7, 1)) return rc;
+    err = P[kScalMisc + 4 + 7];
+    ++nit;
+    if (!(err == err)) break;  // a breakdown (zero r2.v or t.t): stop with the iterate reached
+  }
+  st->info = nit <= p->max_it ? nit - 1 : -1;
+  st->restarts = nit;
+  st->matvecs = matvecs;
+  IMP_CU(IMP_CALL(h, imp_matvec, m, im, im.x, im.b, im.r, s, &h->prof));
+  IMP_CU(IMP_CALL(h, imp_dot, im.r, im.r, n, im.part, im.scal + kScalMisc, s));
+  IMP_CU(IMP_CALL(h, imp_dot, im.b, im.b, n, im.part, im.scal + kScalMisc + 1, s));
+  if (int rc = fetch(h, kScalMisc, 2)) return rc;
+  st->lin_res = P[kScalMisc + 1] > 0.0 ? std::sqrt(P[kScalMisc] / P[kScalMisc + 1]) : 0.0;
   return TY_OK;
 }
 
@@ -382,12 +421,11 @@ extern "C" {
 int ty_implicit_step(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
   if (!p || !st) return TY_ERR_ARG;
   if (int rc = ready(h)) return rc;
-  if (p->krylov < TY_KRYLOV_GMRES || p->krylov > TY_KRYLOV_JFNK || p->precision < TY_PREC_FP64 ||
+  if (p->krylov < TY_KRYLOV_GMRES || p->krylov > TY_KRYLOV_BICGSTAB || p->precision < TY_PREC_FP64 ||
       p->precision > TY_PREC_MIXED || p->nkrylov < 1 || p->max_it < 0 || !(p->inv_res > 0.0) || !(p->cfl > 0.0) ||
-      (p->krylov == TY_KRYLOV_GMRES && p->nkrylov > kMaxKrylov) ||
-      (p->krylov != TY_KRYLOV_GMRES && p->nkrylov > kMaxCgs) ||
-      (p->krylov == TY_KRYLOV_JFNK && p->precision != TY_PREC_FP64) ||
-      (p->krylov == TY_KRYLOV_GMRES && p->precision != TY_PREC_FP64)) {
+      ((p->krylov == TY_KRYLOV_GMRES || p->krylov == TY_KRYLOV_BICGSTAB) && p->nkrylov > kMaxKrylov) ||
+      ((p->krylov == TY_KRYLOV_FGMRES || p->krylov == TY_KRYLOV_JFNK) && p->nkrylov > kMaxCgs) ||
+      (p->krylov != TY_KRYLOV_FGMRES && p->precision != TY_PREC_FP64)) {
     tyi::set_error("ty_imp_params: option out of range (GMRES: nkrylov <= 64, FP64; FGMRES/JFNK: nkrylov <= 32)");
     return TY_ERR_ARG;
   }
@@ -428,6 +466,8 @@ int ty_implicit_step(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
   // 3. solve
   if (p->krylov == TY_KRYLOV_GMRES) {
     rc = gmres_typhon(h, p, st);
+  } else if (p->krylov == TY_KRYLOV_BICGSTAB) {
+    rc = bicgstab_typhon(h, p, st);
   } else {
     Operator op{h, mixed ? 1 : (p->krylov == TY_KRYLOV_JFNK ? 2 : 0)};
     op.a = a;

@@ -603,6 +603,69 @@ __global__ void __launch_bounds__(kRedThreads) k_red_final(const double* __restr
   if (threadIdx.x == 0) out[blockIdx.x] = s;
 }
 
+// ---- BiCGSTAB of bdlu_bicgstab.f90:52-75, scalars kept on the device: sc[0] rho1, sc[1] rho0,
+// sc[2] alpha, sc[3] omega (of the previous iteration), sc[4] r2.v, sc[5] t.s, sc[6] t.t,
+// sc[7] err.  Each kernel derives the step's alpha, beta, omega from them itself.
+// p = r1 (first iteration) or r1 + beta (p - omega v), beta = (rho1/rho0)(alpha/omega)
+__global__ void k_bicg_p(const double* __restrict__ r1, const double* __restrict__ v, double* __restrict__ p,
+                         const double* __restrict__ sc, int first, size_t n) {
+  const double beta = first ? 0.0 : (sc[0] / sc[1]) * (sc[2] / sc[3]);
+  const double om = sc[3];
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if (first) p[i] = r1[i];
+    else {
+      const double q = p[i] - om * v[i];
+      p[i] = r1[i] + beta * q;
+    }
+  }
+}
+// s = r1 - alpha v, alpha = rho1 / (r2.v)
+__global__ void k_bicg_s(const double* __restrict__ r1, const double* __restrict__ v, double* __restrict__ s,
+                         const double* __restrict__ sc, size_t n) {
+  const double alpha = sc[0] / sc[4];
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    s[i] = r1[i] - alpha * v[i];
+}
+// partial sums of t.s and t.t
+__global__ void __launch_bounds__(kRedThreads) k_bicg_ts(const double* __restrict__ t, const double* __restrict__ s,
+                                                          size_t n, double* __restrict__ part) {
+  double a = 0.0, b = 0.0;
+  for (size_t i = blockIdx.x * (size_t)kRedThreads + threadIdx.x; i < n; i += (size_t)gridDim.x * kRedThreads) {
+    a += t[i] * s[i];
+    b += t[i] * t[i];
+  }
+  a = block_sum(a);
+  b = block_sum(b);
+  if (threadIdx.x == 0) { part[blockIdx.x] = a; part[kRedBlocks + blockIdx.x] = b; }
+}
+// omega = (t.s)/(t.t); err partials of |alpha p + omega s|; x += alpha p + omega s; r1 = s - omega t
+__global__ void __launch_bounds__(kRedThreads) k_bicg_update(double* __restrict__ x, double* __restrict__ r1,
+                                                              const double* __restrict__ p,
+                                                              const double* __restrict__ s,
+                                                              const double* __restrict__ t,
+                                                              const double* __restrict__ sc, size_t n,
+                                                              double* __restrict__ part) {
+  const double alpha = sc[0] / sc[4], omega = sc[5] / sc[6];
+  double e = 0.0;
+  for (size_t i = blockIdx.x * (size_t)kRedThreads + threadIdx.x; i < n; i += (size_t)gridDim.x * kRedThreads) {
+    const double ap = alpha * p[i], os = omega * s[i];
+    e += fabs(ap + os);
+    x[i] = x[i] + ap + os;
+    r1[i] = s[i] - omega * t[i];
+  }
+  e = block_sum(e);
+  if (threadIdx.x == 0) part[blockIdx.x] = e;
+}
+// end of an iteration: rho0 = rho1, alpha and omega kept for the next beta
+__global__ void k_bicg_shift(double* sc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const double alpha = sc[0] / sc[4], omega = sc[5] / sc[6];
+    sc[1] = sc[0];
+    sc[2] = alpha;
+    sc[3] = omega;
+  }
+}
+
 // modified Gram-Schmidt pass: w = w - hprev * vprev (when vprev), then partial sums of w . vnext
 __global__ void __launch_bounds__(kRedThreads) k_mgs_pass(const double* __restrict__ vprev,
                                                            const double* __restrict__ hprev, double* __restrict__ w,
@@ -818,6 +881,28 @@ cudaError_t imp_cgs_pass(const double* V, size_t ldv, int j, const double* h, do
       k_cgs_pass<kMaxCgs><<<g, kRedThreads, 0, st>>>(V, ldv, j, h, w, mode, n, part);
     k_red_final<<<mode < 2 ? j : 1, kRedThreads, 0, st>>>(part, (int)g, kRedBlocks, out);
   });
+  return cudaGetLastError();
+}
+
+cudaError_t imp_bicgstab_iter(const DevMesh& m, const ImpState& im, double* x, double* r1, const double* r2,
+                              double* p, double* v, double* s, double* t, int first, double* part, double* sc,
+                              cudaStream_t st, Prof* pr) {
+  const size_t n = 5 * (size_t)m.nci;
+  const unsigned gv = (unsigned)std::min<size_t>(grid_of(n, 256), 4 * kRedBlocks);
+  const unsigned g = red_grid(n);
+  k_red_part<<<g, kRedThreads, 0, st>>>(r1, r2, n, 0, part);                // rho1 = r1.r2
+  k_red_final<<<1, kRedThreads, 0, st>>>(part, (int)g, kRedBlocks, sc + 0);
+  k_bicg_p<<<gv, 256, 0, st>>>(r1, v, p, sc, first, n);
+  pr->launch(K_IMP_MATVEC, st, [&] { k_imp_matvec<<<grid_of(m.nci, 128), 128, 0, st>>>(m, im, p, nullptr, v); });
+  k_red_part<<<g, kRedThreads, 0, st>>>(r2, v, n, 0, part);                 // r2.v
+  k_red_final<<<1, kRedThreads, 0, st>>>(part, (int)g, kRedBlocks, sc + 4);
+  k_bicg_s<<<gv, 256, 0, st>>>(r1, v, s, sc, n);
+  pr->launch(K_IMP_MATVEC, st, [&] { k_imp_matvec<<<grid_of(m.nci, 128), 128, 0, st>>>(m, im, s, nullptr, t); });
+  k_bicg_ts<<<g, kRedThreads, 0, st>>>(t, s, n, part);
+  k_red_final<<<2, kRedThreads, 0, st>>>(part, (int)g, kRedBlocks, sc + 5);
+  k_bicg_update<<<g, kRedThreads, 0, st>>>(x, r1, p, s, t, sc, n, part);
+  k_red_final<<<1, kRedThreads, 0, st>>>(part, (int)g, kRedBlocks, sc + 7);
+  k_bicg_shift<<<1, 32, 0, st>>>(sc);
   return cudaGetLastError();
 }
 

@@ -91,6 +91,9 @@ struct ImpArgs {
   cudaError_t imp_cgs_pass(const double* V, size_t ldv, int j, const double* h, double* w, int mode,     \
                            size_t n, double* part, double* out, cudaStream_t st, Prof* pr);             \
   cudaError_t imp_scale(const double* w, double s, double* v, size_t n, cudaStream_t st);                \
+  cudaError_t imp_bicgstab_iter(const DevMesh& m, const ImpState& im, double* x, double* r1,             \
+                                const double* r2, double* p, double* v, double* s, double* t, int first,  \
+                                double* part, double* sc, cudaStream_t st, Prof* pr);                      \
   cudaError_t imp_axpy_multi(double* x, const double* V, const float* V32, size_t ldv, int j,            \
                              const double* y, int descending, size_t n, cudaStream_t st);               \
   cudaError_t imp_update_state(const DevMesh& m, DevState& s, const double* x, double* part,            \

@@ -31,7 +31,7 @@ RK_METHOD = {"RK2": 1, "RK2-SSP": 2, "RK3-SSP": 3, "RK4": 4, "RK25BB": 5, "RK26B
 MODE = {"exact": 0, "fast": 1}
 DISSIPATIVE_FLUX = {"NONE": 0, "CELL-AVERAGE": 1, "FULL": 2}
 VISC_LAW = {"KINEMATIC-CONSTANT": 0, "SUTHERLAND": 1}
-KRYLOV = {"GMRES": 0, "FGMRES": 1, "JFNK": 2}
+KRYLOV = {"GMRES": 0, "FGMRES": 1, "JFNK": 2, "BICGSTAB": 3}
 PRECISION = {"fp64": 0, "mixed": 1}
 KDIF_FLUX = {"COMPACT": 0, "CELL-AVERAGE": 1, "FULL": 2}
 KBC_ISOTHERMAL, KBC_FLUX, KBC_EXTRAPOLATE = 1, 2, 3
