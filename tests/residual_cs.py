@@ -125,11 +125,93 @@ def roe(L, R, n, g, eps=0.1):
     return np.stack(F)
 
 
-def residual(md, U, dt, scheme="RUSANOV", g=1.4):
-    """R [5, ncell_int] of the first-order residual at U [5, ncell_int] (real or complex)."""
+def _ghost_source(md):
+    """Cell whose state each cell carries: itself, or for a periodic ghost the partner's cell."""
+    src = np.arange(md.ncell)
+    b = np.arange(md.nface_int, md.nface)
+    per = b[md.face_bc[b] == 1]
+    src[md.fc2[per]] = md.fc1[md.face_partner[per] - 1]
+    return src
+
+
+def lsq_weights(md):
+    """w[side, f] = A_c^-1 d_f for the cell c on that side of face f (precalc_grad_lsq.f90: A_c
+    = sum of d d^T over the cell's faces, d = C(fc2) - C(fc1); one added to A_zz in 2D)."""
+    nci, nf = md.ncell_int, md.nface
+    d = md.cell_centre[md.fc2] - md.cell_centre[md.fc1]
+    A = np.zeros((nci, 3, 3))
+    dd = d[:, :, None] * d[:, None, :]
+    np.add.at(A, md.fc1, dd)
+    inner = np.arange(md.nface_int)
+    np.add.at(A, md.fc2[inner], dd[inner])
+    if md.dim == 2:
+        A[:, 2, 2] += 1.0
+    Ainv = np.linalg.inv(A)
+    w = np.zeros((2, nf, 3))
+    w[0] = np.einsum("fij,fj->fi", Ainv[md.fc1], d)
+    w[1, inner] = np.einsum("fij,fj->fi", Ainv[md.fc2[inner]], d[inner])
+    return w
+
+
+def gradient(md, P, w):
+    """G [5, ncell_int, 3] = sum over the cell's faces of w (P(fc2) - P(fc1))."""
+    nci = md.ncell_int
+    dP = P[:, md.fc2] - P[:, md.fc1]                        # [5, nf] (ghosts carry their source)
+    G = np.zeros((5, nci, 3), dtype=P.dtype)
+    inner = np.arange(md.nface_int)
+    for k in range(3):
+        np.add.at(G[:, :, k].T, md.fc1, (dP * w[0, :, k]).T)
+        np.add.at(G[:, :, k].T, md.fc2[inner], (dP[:, inner] * w[1, inner, k]).T)
+    return G
+
+
+def muscl(md, P, G, faces, side, limiter):
+    """MUSCL (HIGHRES = MUSCL) state of one side of `faces`: q_c + G_c.CF + sg (u.CF), sg =
+    phi(2g - LR, LR) - g with van Albada's phi (or LR - g without limiter)."""
+    fc1, fc2 = md.fc1[faces], md.fc2[faces]
+    c = fc2 if side else fc1
+    CL, CR = md.cell_centre[fc1], md.cell_centre[fc2]
+    dv = CR - CL
+    dLR = np.sqrt(np.sum(dv * dv, axis=1))
+    u = dv / dLR[:, None]
+    CF = md.face_centre[faces] - (CR if side else CL)
+    uc = np.sum(u * CF, axis=1)
+    LR = (P[:, fc2] - P[:, fc1]) / dLR
+    Gc = G[:, c, :]
+    g = np.einsum("vfk,fk->vf", Gc, u)
+    if limiter == "ALBADA":
+        a, b = 2.0 * g - LR, LR
+        pos = (a.real * b.real) > 0.0
+        den = np.where(pos, a * a + b * b, 1.0)
+        phi = np.where(pos, a * b * (a + b) / den, 0.0)
+        sg = phi - g
+    else:
+        sg = LR - g
+    return P[:, c] + np.einsum("vfk,fk->vf", Gc, CF) + sg * uc
+
+
+def residual(md, U, dt, scheme="RUSANOV", g=1.4, highres="NONE", limiter="NONE"):
+    """R [5, ncell_int] of the residual at U [5, ncell_int] (real or complex): first order, or
+    least-squares gradients and MUSCL with no limiter or van Albada (periodic boundaries)."""
     nci, nf, nfi = md.ncell_int, md.nface, md.nface_int
     fc1, fc2 = md.fc1, md.fc2
     P = prim(U, g)
+    if highres != "NONE":
+        P = P[:, _ghost_source(md)]
+        G = gradient(md, P, lsq_weights(md))
+        allf = np.arange(nf)
+        QL = muscl(md, P, G, allf, 0, limiter)
+        QR = np.empty_like(QL)
+        inner = np.arange(nfi)
+        QR[:, inner] = muscl(md, P, G, inner, 1, limiter)
+        b = np.arange(nfi, nf)
+        QR[:, b] = muscl(md, P, G, md.face_partner[b] - 1, 0, limiter)
+        n = md.face_normal.T
+        F = {"RUSANOV": rusanov, "HLLC": hllc, "ROE": roe}[scheme](QL, QR, n, g) * md.face_surface
+        R = np.zeros((5, nci), dtype=U.dtype)
+        np.subtract.at(R.T, fc1, F.T)
+        np.add.at(R.T, fc2[inner], F[:, inner].T)
+        return dt / md.cell_volume[:nci] * R
     QL = P[:, fc1]
     right = np.where(np.arange(nf) < nfi, fc2, 0)
     QR = P[:, np.minimum(right, nci - 1)].copy()
@@ -150,7 +232,7 @@ def residual(md, U, dt, scheme="RUSANOV", g=1.4):
     return dt / md.cell_volume[:nci] * R
 
 
-def rk_run(md, U0, dts, table, scheme="RUSANOV"):
+def rk_run(md, U0, dts, table, scheme="RUSANOV", highres="NONE", limiter="NONE"):
     U = U0
     for dt in dts:
         Rs = []
@@ -159,7 +241,7 @@ def rk_run(md, U0, dts, table, scheme="RUSANOV"):
             for s in range(k):
                 if table[k - 1][s] != 0.0:
                     Uk = Uk + table[k - 1][s] * Rs[s]
-            Rs.append(residual(md, Uk, dt, scheme))
+            Rs.append(residual(md, Uk, dt, scheme, highres=highres, limiter=limiter))
         for s, c in enumerate(table[-1]):
             if c != 0.0:
                 U = U + c * Rs[s]

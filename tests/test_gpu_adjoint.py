@@ -2,7 +2,8 @@
 
 * ty_adjoint_vjp against central finite differences of ty_residual_device (periodic,
   symmetry, far-field, slip and no-slip wall boundaries; HLLC, Rusanov, Roe; exact and fast
-  modes).
+  modes); the second-order VJP (least-squares gradients, MUSCL, van Albada) likewise on
+  periodic meshes, and through a whole unsteady run against the complex step.
 * The gradient of J = sum over a sub-box of rho^2 V after an RK3-SSP run, through
   typhon_gb300.adjoint (binomial checkpointing or stored stage states, torch.autograd),
   against the complex-step derivative of the numpy restatement in tests/residual_cs.py:
@@ -122,12 +123,81 @@ def test_unsteady_gradient_against_complex_step(env, scheme):
     g.close()
 
 
-def test_adjoint_rejects_second_order(env):
+def test_adjoint_rejects_unsupported_second_order(env, golden_dir):
     torch, ty, adjoint = env
     md = jittered(ty, 4)
-    g = ty.Grid(md)
+    for highres, limiter, postlim in (("MUSCL-UNS", "ALBADA", "NONE"), ("MUSCL", "MINMOD", "NONE"),
+                                      ("MUSCL", "ALBADA", "BARTH")):
+        g = ty.Grid(md)
+        g.set_spat("HLLC", highres, limiter, postlim)
+        st = adjoint.Stepper(g, "RK2")
+        U = torch.tensor(smooth_cons(ty, md), device="cuda")
+        with pytest.raises(ty.TyphonError):
+            st.vjp(U, 1e-3, torch.ones_like(U))
+        g.close()
+    # MUSCL on a mesh with a non-periodic boundary
+    md2 = ty.preprocess(ty.read_tym(golden_dir / "quad20x10.tym"), 2,
+                        [(f, op.BC_SYMMETRY, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX")])
+    g = ty.Grid(md2)
     g.set_spat("HLLC", "MUSCL", "ALBADA")
     st = adjoint.Stepper(g, "RK2")
-    U = torch.tensor(smooth_cons(ty, md), device="cuda")
+    U = torch.tensor(smooth_cons(ty, md2), device="cuda")
     with pytest.raises(ty.TyphonError):
         st.vjp(U, 1e-3, torch.ones_like(U))
+    g.close()
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+@pytest.mark.parametrize("scheme,limiter", [("HLLC", "ALBADA"), ("ROE", "ALBADA"), ("RUSANOV", "NONE")])
+def test_muscl_vjp_matches_finite_differences(env, scheme, limiter, mode):
+    """Second order (least-squares gradients, MUSCL, van Albada) on a jittered periodic mesh."""
+    torch, ty, adjoint = env
+    md = jittered(ty)
+    g = ty.Grid(md)
+    g.set_spat(scheme, "MUSCL", limiter, mode=mode)
+    st = adjoint.Stepper(g, "RK3-SSP")
+    U = torch.tensor(smooth_cons(ty, md), device="cuda")
+    rng = np.random.default_rng(1)
+    lamR = torch.tensor(rng.standard_normal(U.shape), device="cuda")
+    d = torch.tensor(rng.standard_normal(U.shape), device="cuda") * U.abs().mean(dim=1, keepdim=True)
+    dt = 1e-3
+    lamU = st.vjp(U, dt, lamR)
+    eps = 1e-6
+    fd = ((st.residual(U + eps * d, dt) - st.residual(U - eps * d, dt)) * lamR).sum() / (2 * eps)
+    ad = (lamU * d).sum()
+    assert abs(float(fd - ad)) <= 1e-6 * abs(float(ad)), (float(fd), float(ad))
+    g.close()
+
+
+@pytest.mark.parametrize("scheme", ["HLLC", "ROE"])
+def test_muscl_unsteady_gradient_against_complex_step(env, scheme):
+    """J = sum over a sub-box of rho^2 V after an SSP-RK3 run with MUSCL + van Albada: the
+    adjoint's directional derivatives against the complex step of the numpy restatement."""
+    torch, ty, adjoint = env
+    md = jittered(ty, 8)
+    g = ty.Grid(md)
+    g.set_spat(scheme, "MUSCL", "ALBADA", mode="exact")
+    U0 = smooth_cons(ty, md)
+    dts = [2e-3] * 10
+    nci = md.ncell_int
+    cc = md.cell_centre[:nci]
+    box = ((np.abs(cc[:, 0] - 0.5) < 0.25) & (np.abs(cc[:, 1] - 0.5) < 0.25)).astype(float)
+    V = md.cell_volume[:nci]
+    Ut = torch.tensor(U0, device="cuda", requires_grad=True)
+    Uf = adjoint.rk_solve(Ut, g, "RK3-SSP", dts)
+    w = torch.tensor(box * V, device="cuda")
+    J = (Uf[0] ** 2 * w).sum()
+    J.backward()
+    grad = Ut.grad.cpu().numpy()
+    Uf_np = cs.rk_run(md, U0, dts, adjoint.RK_TABLES["RK3-SSP"], scheme, highres="MUSCL", limiter="ALBADA")
+    assert np.allclose(Uf.detach().cpu().numpy(), Uf_np, rtol=1e-11, atol=0)
+    rng = np.random.default_rng(5)
+    for _ in range(3):
+        d = rng.standard_normal(U0.shape) * np.abs(U0).mean(axis=1, keepdims=True)
+        h = 1e-30
+        Uc = cs.rk_run(md, U0 + 1j * h * d, dts, adjoint.RK_TABLES["RK3-SSP"], scheme, highres="MUSCL",
+                       limiter="ALBADA")
+        dJ = float(np.sum(box * V * Uc[0] ** 2).imag / h)
+        ad = float(np.sum(grad * d))
+        assert abs(ad - dJ) <= 1e-8 * abs(dJ), (ad, dJ)
+    g.close()

@@ -18,8 +18,10 @@ SOURCE/MAIN/inverse_calc_sensi.f90:62-114).
 * ``RKSolve`` is a ``torch.autograd.Function`` over CUDA tensors [5, ncell_int] (rho, rhoE,
   rhou, rhov, rhow), so a functional written in torch differentiates through the solver.
 
-The residual must be first order and inviscid (HIGHRES = NONE); the time steps are fixed
-(the stability time step is not differentiated).
+The residual must be inviscid: first order, or least-squares gradients with MUSCL
+(HIGHRES = MUSCL) and no limiter or van Albada's, on a periodic mesh (the derivative of the
+smooth van Albada limiter is exact; there is no post-limiter).  The time steps are fixed (the
+stability time step is not differentiated).
 """
 import ctypes as C
 from functools import lru_cache

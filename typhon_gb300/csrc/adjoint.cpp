@@ -35,8 +35,12 @@ int ty_residual_device(ty_mesh* h, double dt, double* R) {
 int ty_adjoint_vjp(ty_mesh* h, double dt, const double* lamR, double* lamU) {
   if (int rc = ready(h)) return rc;
   if (!lamR || !lamU) return TY_ERR_ARG;
-  if (h->o.highres != TY_HRES_NONE || h->o.viscous != TY_VISC_NONE) {
-    tyi::set_error("ty_adjoint_vjp: first-order inviscid residual only (HIGHRES = NONE, no viscous flux)");
+  const bool second = h->o.highres != TY_HRES_NONE;
+  if (h->o.viscous != TY_VISC_NONE ||
+      (second && (h->o.highres != TY_HRES_MUSCL || (h->o.limiter != TY_LIM_NONE && h->o.limiter != TY_LIM_ALBADA) ||
+                  h->o.postlim != TY_POSTLIM_NONE || h->nonperiodic_bc))) {
+    tyi::set_error("ty_adjoint_vjp: inviscid residual, first order or MUSCL with no limiter or van Albada "
+                   "(no post-limiter, periodic boundaries)");
     return TY_ERR_UNSUPPORTED;
   }
   if (h->o.scheme == TY_SCH_HLLE || h->inout_bc) {
@@ -54,7 +58,16 @@ int ty_adjoint_vjp(ty_mesh* h, double dt, const double* lamR, double* lamU) {
   double* bU = h->adj_buf + 5 * ld;
   TY_CU(cudaMemcpy2DAsync(bR, ld * sizeof(double), lamR, n * sizeof(double), n * sizeof(double), 5,
                           cudaMemcpyDeviceToDevice, h->stream));
-  cudaError_t e = ADJ_CALL(h, adjoint_vjp, m, h->o, h->s.u0, bR, dt, h->adj_face, bU, h->stream);
+  cudaError_t e;
+  if (second) {
+    if (!h->adj_rec &&
+        ((rc = h->alloc(h->adj_rec, 50 * (size_t)m.ldf)) || (rc = h->alloc(h->adj_qg, 20 * (size_t)m.ldc))))
+      return rc;
+    e = ADJ_CALL(h, adjoint_vjp_muscl, m, h->s, h->o, h->s.u0, bR, dt, h->adj_rec, h->adj_qg, bU, h->stream);
+    h->prim_valid = false;  // s.prim now holds this state's primitive variables and ghosts
+  } else {
+    e = ADJ_CALL(h, adjoint_vjp, m, h->o, h->s.u0, bR, dt, h->adj_face, bU, h->stream);
+  }
   if (e != cudaSuccess) return cuda_fail(e, "adjoint");
   TY_CU(cudaMemcpy2DAsync(lamU, n * sizeof(double), bU, ld * sizeof(double), n * sizeof(double), 5,
                           cudaMemcpyDeviceToDevice, h->stream));

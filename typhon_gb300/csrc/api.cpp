@@ -418,6 +418,7 @@ int ty_mesh_create(const ty_mesh_desc* d, int device, ty_mesh** out) {
     if (f < nfi && b >= nci) { tyi::set_error("interior face with a ghost cell"); return bail(TY_ERR_MESH); }
     if (f >= nfi) {
       if (b < nci) { tyi::set_error("boundary face without ghost cell"); return bail(TY_ERR_MESH); }
+      if (fbc[f] != TY_BC_PERIODIC) h->nonperiodic_bc = true;
       if (fbc[f] == TY_BC_PERIODIC) {
         int p = d->face_partner[f] - 1;
         if (p < nfi || p >= nf || d->face_partner[p] - 1 != f) { tyi::set_error("bad periodic partner"); return bail(TY_ERR_MESH); }

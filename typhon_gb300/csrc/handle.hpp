@@ -43,6 +43,7 @@ struct ty_mesh {
   bool has_params = false, has_state = false, prim_valid = false, fast_ready = false;
   bool heat_bc = false;  // the mesh has TY_BC_HEAT (ghost-face) boundaries
   bool inout_bc = false, bcdata_set = false;  // inlets / outlets, and their parameters uploaded
+  bool nonperiodic_bc = false;  // a boundary face that is not periodic
   std::vector<double> kd_k;  // host copy of the KDIF conductivity [nci]
   int nslot = 0;
   std::vector<void*> allocs;
@@ -58,6 +59,8 @@ struct ty_mesh {
   tyk::KdifState kd;  // heat-conduction state (ty_kdif_setup)
   double* adj_face = nullptr;  // [10][ldf] adjoint face products (first use)
   double* adj_buf = nullptr;   // [2][5][ldc] adjoint staging
+  double* adj_rec = nullptr;   // [50][ldf] reversed reconstructions (second-order adjoint)
+  double* adj_qg = nullptr;    // [20][ldc] adjoints of q and of the gradients (second order)
   cudaStream_t own_stream = nullptr;
 
   template <class T>
