@@ -464,7 +464,7 @@ def run_adjoint(args):
     nci = md.ncell_int
     prim = cases.taylor_green(md.cell_centre)
     g = ty.Grid(md)
-    g.set_spat(w["scheme"], mode="fast")
+    g.set_spat(w["scheme"], w["highres"], w["limiter"], mode="fast")
     g.set_prim(prim)
     dt = g.calc_zonetimestep(w["cfl"])
     dts = [dt] * w["steps"]
@@ -523,7 +523,8 @@ def run_adjoint(args):
                      "states)", "unit": "ratio",
            "value": round(t_rev / t_primal, 3), "higher_is_better": False, "n_gpus": 1, "steps": w["steps"],
            "warmup": 2, "dtype": "f64", "data": "synthetic", "scaling": "weak", "vs_baseline": None,
-           "config": {"workload": f"adjoint3d TGV {n}^3x5 tets, first-order {w['scheme']}, {w['rk']}",
+           "config": {"workload": f"adjoint3d TGV {n}^3x5 tets, {w['scheme']} + {w['highres']} {w['limiter']} "
+                                  f"(least-squares gradients), {w['rk']}",
                       "cells": nci, "dt": dt, "storage_policy": policy, "J": J0},
            "primal_s": round(t_primal, 4), "primal_library_rk_s": round(t_lib, 4),
            "primal_storing_stages_s": round(t_fwd_store, 4), "stage_storage_bytes": tape_bytes,

@@ -10,8 +10,8 @@
   ffbox3d    3D steady far-field box for the implicit solvers (FFBOX below): 48^3
              hexahedra split into 5 tetrahedra, far field on all faces, M = 0.3 at 20 degrees,
              Rusanov, a Gaussian bump relaxing to the uniform free stream.
-  adjoint3d  TGV 40^3 x 5 tets, first-order Roe, SSP-RK3: gradient of int rho^2 over a
-             sub-box with respect to the initial state (ADJOINT3D below).
+  adjoint3d  TGV 40^3 x 5 tets, HLLC with MUSCL and van Albada, SSP-RK3, 200 steps: gradient
+             of int rho^2 over a sub-box with respect to the initial state (ADJOINT3D below).
   kdif3d     3D heat conduction (KDIF3D below): 70^3 x 6 tetrahedra, lognormal
              conductivity with inclusions, two isothermal faces, implicit Euler.
 All are nondimensional (rho_inf = 1).  The initial states are evaluated at cell centres.
@@ -112,7 +112,8 @@ def make_kdif3d(n=None):
 # J = integral of rho^2 over the centred sub-box [pi/2, 3 pi/2]^3 at the final time; its
 # gradient with respect to the initial state by the adjoint with 20 stored states, and 16
 # seeded directional derivatives of it checked by central finite differences.
-ADJOINT3D = dict(n=40, steps=100, snaps=20, directions=16, scheme="ROE", rk="RK3-SSP", cfl=0.8, seed=1234)
+ADJOINT3D = dict(n=40, steps=200, snaps=20, directions=16, scheme="HLLC", highres="MUSCL", limiter="ALBADA",
+                 rk="RK3-SSP", cfl=0.8, seed=1234)
 
 
 WORKLOADS = {
