@@ -201,3 +201,36 @@ def test_muscl_unsteady_gradient_against_complex_step(env, scheme):
         ad = float(np.sum(grad * d))
         assert abs(ad - dJ) <= 1e-8 * abs(dJ), (ad, dJ)
     g.close()
+
+
+def test_muscl_tgv3d_gradient_against_complex_step(env):
+    """The benchmark's configuration at a small size: Taylor-Green vortex on 6^3 x 5 jittered
+    periodic tetrahedra, HLLC with MUSCL and van Albada, 20 SSP-RK3 steps, J = sum over the
+    centred sub-box of rho^2 V: adjoint directional derivatives against the complex step."""
+    torch, ty, adjoint = env
+    from typhon_gb300 import cases
+    md = cases.make_mesh("tgv3d", 6)
+    nci = md.ncell_int
+    g = ty.Grid(md)
+    g.set_spat("HLLC", "MUSCL", "ALBADA", mode="fast")
+    prim = cases.taylor_green(md.cell_centre)
+    U0 = ty.prim_to_cons(prim[:, :nci])
+    g.set_prim(prim)
+    dt = g.calc_zonetimestep(0.8)
+    dts = [dt] * 20
+    cc = md.cell_centre[:nci]
+    L = 2 * np.pi
+    box = np.all(np.abs(cc - L / 2) < L / 4, axis=1).astype(float) * md.cell_volume[:nci]
+    Ut = torch.tensor(U0, device="cuda", requires_grad=True)
+    J = (adjoint.rk_solve(Ut, g, "RK3-SSP", dts)[0] ** 2 * torch.tensor(box, device="cuda")).sum()
+    J.backward()
+    grad = Ut.grad.cpu().numpy()
+    rng = np.random.default_rng(7)
+    for _ in range(2):
+        d = rng.standard_normal(U0.shape) * np.abs(U0).mean(axis=1, keepdims=True)
+        Uc = cs.rk_run(md, U0 + 1j * 1e-30 * d, dts, adjoint.RK_TABLES["RK3-SSP"], "HLLC", highres="MUSCL",
+                       limiter="ALBADA")
+        dJ = float(np.sum(box * Uc[0] ** 2).imag / 1e-30)
+        ad = float(np.sum(grad * d))
+        assert abs(ad - dJ) <= 1e-8 * abs(dJ), (ad, dJ)
+    g.close()
