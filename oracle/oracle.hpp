@@ -275,7 +275,10 @@ struct KdifSolver {
   void typhon_dlu(double dt);
   void dlu_yeqax(const double* x, double* y) const;
   void dlu_yeqmaxpz(const double* x, const double* z, double* y) const;
+  void dlu_yeqatx(const double* x, double* y) const;
   int dlu_cgs(std::vector<double>& sol, double maxres, int max_it) const;
+  int dlu_bicg(std::vector<double>& sol, double maxres, int max_it) const;
+  int dlu_gmres(std::vector<double>& sol, double maxres, int max_it, int nkrylov) const;
 };
 
 // Typhon's steady driver for one KDIF zone (integration.f90, integration_cycle.f90,
@@ -285,6 +288,8 @@ struct KdifSteadyParams {
   double cycle_res = 0.1, global_res = 1e-5;  // TIME_PARAM and PROJECT RESIDUALS
   double cgs_maxres = 1e-4;                    // INV_RES
   int cgs_max_it = 10;                         // IMP_MAX_IT
+  int inversion = 0;                           // INVERSION: 0 CGS, 1 BICG, 2 GMRES
+  int nkrylov = 10;                            // NKRYLOV (GMRES)
   int max_iters = 100000, max_cycles = 1000;
 };
 struct KdifSteadyOut {

@@ -403,7 +403,8 @@ int ory_kdif_get(void* k, int which, double* out) {
   return (int)v->size();
 }
 // Typhon's steady KDIF run from the temperature set by ory_kdif_set_T.  dp: fourier,
-// conduct, cycle_res, global_res, cgs_maxres; ip: cgs_max_it, max_iters, max_cycles.  Writes
+// conduct, cycle_res, global_res, inv_res; ip: imp_max_it, max_iters, max_cycles, inversion
+// (0 CGS, 1 BICG, 2 GMRES), nkrylov.  Writes
 // up to cap iterations' log10 residuals and cycles' averages and end iterations; returns the
 // iteration count (negative cycle count in *ncycle_out).
 int ory_kdif_typhon_steady(void* k, const double* dp, const int* ip, int cap, double* log_res, double* cycle_avg,
@@ -411,7 +412,7 @@ int ory_kdif_typhon_steady(void* k, const double* dp, const int* ip, int cap, do
   KdifSolver* s = (KdifSolver*)k;
   KdifSteadyParams p;
   p.fourier = dp[0]; p.conduct = dp[1]; p.cycle_res = dp[2]; p.global_res = dp[3]; p.cgs_maxres = dp[4];
-  p.cgs_max_it = ip[0]; p.max_iters = ip[1]; p.max_cycles = ip[2];
+  p.cgs_max_it = ip[0]; p.max_iters = ip[1]; p.max_cycles = ip[2]; p.inversion = ip[3]; p.nkrylov = ip[4];
   std::vector<double> U(s->T.begin(), s->T.begin() + s->m->ncell_int);
   for (auto& u : U) u = u * s->cp;
   KdifSteadyOut out;

@@ -313,6 +313,133 @@ int KdifSolver::dlu_cgs(std::vector<double>& sol, double maxres, int max_it) con
   return nit <= max_it ? nit - 1 : -1;
 }
 
+// SPMAT_DLU.f90 dlu_yeqatx: y = A^T x
+void KdifSolver::dlu_yeqatx(const double* x, double* y) const {
+  for (int c = 0; c < m->ncell; ++c) y[c] = dlu_diag[c] * x[c];
+  for (int f = 0; f < m->nface; ++f) {
+    const int lo = m->fc1[f], hi = m->fc2[f];
+    y[hi] = y[hi] + dlu_upper[f] * x[lo];
+    y[lo] = y[lo] + dlu_lower[f] * x[hi];
+  }
+}
+
+// dlu_bicg.f90: bi-conjugate gradients, stopped like dlu_cgs
+int KdifSolver::dlu_bicg(std::vector<double>& sol, double maxres, int max_it) const {
+  const int n = m->ncell;
+  std::vector<double> r1(n), r2(n), p1(n), p2(n), q1(n), q2(n);
+  auto dotp = [&](const std::vector<double>& a, const std::vector<double>& b) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s = s + a[i] * b[i];
+    return s;
+  };
+  p1 = sol;
+  for (int i = 0; i < n; ++i) sol[i] = p1[i] / dlu_diag[i];
+  double ref = 0.0;
+  for (int i = 0; i < n; ++i) ref = ref + std::fabs(sol[i]);
+  dlu_yeqmaxpz(sol.data(), p1.data(), r1.data());
+  r2 = r1;
+  double err = std::numeric_limits<double>::max(), rho0 = 0.0;
+  int nit = 0;
+  while (err >= ref * maxres && nit <= max_it) {
+    const double rho1 = dotp(r1, r2);
+    if (nit == 0) {
+      p1 = r1;
+      p2 = r2;
+    } else {
+      const double beta = rho1 / rho0;
+      for (int i = 0; i < n; ++i) p1[i] = r1[i] + beta * p1[i];
+      for (int i = 0; i < n; ++i) p2[i] = r2[i] + beta * p2[i];
+    }
+    dlu_yeqax(p1.data(), q1.data());
+    dlu_yeqatx(p2.data(), q2.data());
+    const double alpha = rho1 / dotp(p2, q1);
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s = s + std::fabs(p1[i]);
+    err = std::fabs(alpha) * s;
+    for (int i = 0; i < n; ++i) sol[i] = sol[i] + alpha * p1[i];
+    for (int i = 0; i < n; ++i) r1[i] = r1[i] - alpha * q1[i];
+    for (int i = 0; i < n; ++i) r2[i] = r2[i] - alpha * q2[i];
+    rho0 = rho1;
+    ++nit;
+  }
+  return nit <= max_it ? nit - 1 : -1;
+}
+
+// dlu_gmres.f90: restarted GMRES(nkrylov), modified Gram-Schmidt, Givens rotations
+int KdifSolver::dlu_gmres(std::vector<double>& sol, double maxres, int max_it, int nk) const {
+  const int n = m->ncell;
+  auto dotp = [&](const double* a, const double* b) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s = s + a[i] * b[i];
+    return s;
+  };
+  std::vector<double> qc(nk + 1), qs(nk + 1), ss(nk + 2), yy(nk + 1), hh((size_t)(nk + 2) * (nk + 1));
+  auto H = [&](int i, int j) -> double& { return hh[(size_t)i * (nk + 1) + j]; };  // 1-based
+  std::vector<double> r1(n), p1(n), w1((size_t)nk * n), v1((size_t)nk * n);
+  auto W = [&](int j) { return &w1[(size_t)(j - 1) * n]; };
+  auto V = [&](int j) { return &v1[(size_t)(j - 1) * n]; };
+  p1 = sol;
+  for (int i = 0; i < n; ++i) sol[i] = p1[i] / dlu_diag[i];
+  double ref = 0.0;
+  for (int i = 0; i < n; ++i) ref = ref + std::fabs(sol[i]);
+  const double normp1 = std::sqrt(dotp(p1.data(), p1.data()));
+  const double eps = std::numeric_limits<double>::epsilon();
+  double errgmres = std::numeric_limits<double>::max();
+  int nit = 0;
+  while (errgmres >= ref * maxres && nit <= max_it * 2) {
+    dlu_yeqmaxpz(sol.data(), p1.data(), r1.data());
+    const double beta = std::sqrt(dotp(r1.data(), r1.data()));
+    double fact = 1.0 / beta;
+    for (int i = 0; i < n; ++i) V(1)[i] = fact * r1[i];
+    std::fill(ss.begin(), ss.end(), 0.0);
+    ss[1] = beta;
+    std::fill(hh.begin(), hh.end(), 0.0);
+    int jk;
+    for (jk = 1; jk <= nk; ++jk) {
+      dlu_yeqax(V(jk), W(jk));
+      for (int ik = 1; ik <= jk; ++ik) {
+        H(ik, jk) = dotp(W(jk), V(ik));
+        for (int i = 0; i < n; ++i) W(jk)[i] = W(jk)[i] - H(ik, jk) * V(ik)[i];
+      }
+      H(jk + 1, jk) = std::sqrt(dotp(W(jk), W(jk)));
+      for (int ik = 1; ik <= jk - 1; ++ik) {
+        const double tmp = H(ik, jk);
+        H(ik, jk) = qc[ik] * tmp + qs[ik] * H(ik + 1, jk);
+        H(ik + 1, jk) = -qs[ik] * tmp + qc[ik] * H(ik + 1, jk);
+      }
+      if (H(jk + 1, jk) > eps * 10 * normp1) {
+        if (jk < nk) {
+          fact = 1.0 / H(jk + 1, jk);
+          for (int i = 0; i < n; ++i) V(jk + 1)[i] = fact * W(jk)[i];
+        }
+        if (H(jk, jk) == 0) break;
+        const double tmp = std::sqrt(H(jk, jk) * H(jk, jk) + H(jk + 1, jk) * H(jk + 1, jk));
+        qc[jk] = H(jk, jk) / tmp;
+        qs[jk] = H(jk + 1, jk) / tmp;
+        H(jk, jk) = tmp;
+        H(jk + 1, jk) = 0.0;
+        ss[jk + 1] = -qs[jk] * ss[jk];
+        ss[jk] = qc[jk] * ss[jk];
+        if (std::fabs(ss[jk + 1]) < maxres * std::fabs(ss[1])) break;
+      } else {
+        break;
+      }
+    }
+    const int nkk = std::min(jk, nk);
+    for (jk = nkk; jk >= 1; --jk) {
+      double tmp = ss[jk];
+      for (int ik = jk + 1; ik <= nkk; ++ik) tmp = tmp - H(jk, ik) * yy[ik];
+      yy[jk] = tmp / H(jk, jk);
+      for (int i = 0; i < n; ++i) sol[i] = sol[i] + yy[jk] * V(jk)[i];
+    }
+    dlu_yeqmaxpz(sol.data(), p1.data(), r1.data());
+    ss[nkk + 1] = std::sqrt(dotp(r1.data(), r1.data()));
+    errgmres = ss[nkk + 1] / normp1;
+    ++nit;
+  }
+  return nit <= max_it ? nit - 1 : -1;
+}
+
 void kdif_typhon_steady(KdifSolver& k, std::vector<double>& U, const KdifSteadyParams& p, KdifSteadyOut& out) {
   const UMesh* m = k.m;
   const int nc = m->ncell, nci = m->ncell_int;
@@ -339,7 +466,9 @@ void kdif_typhon_steady(KdifSolver& k, std::vector<double>& U, const KdifSteadyP
       k.rhs(dt);
       k.typhon_dlu(dt);
       for (int c = 0; c < nc; ++c) x[c] = c < nci ? k.residu[c] : 0.0;
-      k.dlu_cgs(x, p.cgs_maxres, p.cgs_max_it);
+      if (p.inversion == 1) k.dlu_bicg(x, p.cgs_maxres, p.cgs_max_it);
+      else if (p.inversion == 2) k.dlu_gmres(x, p.cgs_maxres, p.cgs_max_it, p.nkrylov);
+      else k.dlu_cgs(x, p.cgs_maxres, p.cgs_max_it);
       double s = 0.0;  // update_field.f90: U += dU, residual sum|dU| / refsca
       for (int c = 0; c < nci; ++c) {
         U[c] = U[c] + x[c];

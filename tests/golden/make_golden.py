@@ -36,6 +36,7 @@ CASES = {
     "VISCOUS-CELLFULL-VXERR": "NRG/NS/NUM/FLUX/VISCOUS/CELLFULL/VXERR.tmon",
     "KDIF-ISOTH-CGS": ["NRG/KDIF/ISOTH-CGS/monres.001", "NRG/KDIF/ISOTH-CGS/Average_T.tmon"],
     "KDIF-ISOTH-GMRES": ["NRG/KDIF/ISOTH-GMRES/monres.001", "NRG/KDIF/ISOTH-GMRES/Average_T.tmon"],
+    "KDIF-ISOTH-BICG": ["NRG/KDIF/ISOTH-BICG/monres.001", "NRG/KDIF/ISOTH-BICG/Average_T.tmon"],
     "IMPLICIT-GMRES": ["NRG/TIME/IMPLICIT/GMRES/histofluxNS_RIGHT", "NRG/TIME/IMPLICIT/GMRES/histovarNS_RIGHT"],
     "IMPLICIT-BICGSTAB-RUSANOV": ["NRG/TIME/IMPLICIT/BICGSTAB-RUSANOV/histovarNS_DOWN"],
 }

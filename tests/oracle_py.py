@@ -331,12 +331,13 @@ class Kdif:
         return it, rel.value
 
     def typhon_steady(self, fourier, conduct, cycle_res=0.1, global_res=1e-5, cgs_maxres=1e-4, cgs_max_it=10,
-                      max_iters=100000, max_cycles=1000):
+                      max_iters=100000, max_cycles=1000, inversion="CGS", nkrylov=10):
         """Typhon's steady implicit run (DLU + CGS) from the current temperature: log10 residual
         per iteration, volume-averaged temperature and total iterations after each cycle."""
         cap = max_iters + 1
         dp = np.array([fourier, conduct, cycle_res, global_res, cgs_maxres], np.float64)
-        ip = np.array([cgs_max_it, max_iters, max_cycles], np.int32)
+        ip = np.array([cgs_max_it, max_iters, max_cycles, {"CGS": 0, "BICG": 1, "GMRES": 2}[inversion], nkrylov],
+                      np.int32)
         lr, avg, end = np.zeros(cap), np.zeros(cap), np.zeros(cap, np.int32)
         nc = C.c_int()
         n = self.lib.ory_kdif_typhon_steady(self.h, _p(dp), _p(ip), cap, _p(lr), _p(avg), _p(end), C.byref(nc))

@@ -4,13 +4,11 @@
   file with vertex-located boundary conditions (tube.cgns) and little-endian files with
   face-element ones (square-quad10.cgns, rect4x1.cgns); the native preprocessing and the
   oracle's agree face by face on them.
-* The oracle's restatement of Typhon's steady implicit KDIF run (DLU matrix, CGS, cycles,
-  residual, VOL_AVERAGE probe) reproduces NRG/KDIF/ISOTH-CGS: the 929 residuals of monres.001
-  to 1e-10 in log10 (the file prints 15 digits) and the five cycle averages of Average_T.tmon
-  as printed (8 digits).  The same run against NRG/KDIF/ISOTH-GMRES agrees to 1e-5 (residuals)
-  and 1e-6 (averages): that case
-  solves each step by GMRES(10) stopped at INV_RES 1e-4, the oracle by CGS, and the two
-  inexact solves differ at that level.
+* The oracle's restatement of Typhon's steady implicit KDIF run (DLU matrix, cycles,
+  residual, VOL_AVERAGE probe) with each of Typhon's DLU solvers (dlu_cgs, dlu_bicg,
+  dlu_gmres) reproduces NRG/KDIF/ISOTH-CGS, -BICG and -GMRES: the 929 residuals of monres.001
+  to 1e-10 in log10 (the files print 15 digits) and the five cycle averages of
+  Average_T.tmon as printed (8 digits).
 """
 import numpy as np
 import pytest
@@ -85,29 +83,21 @@ def read_probe(path):
     return [ln.split()[2] for ln in open(path) if ln.strip()]
 
 
-def test_oracle_reproduces_isoth_cgs(golden_dir):
-    """NRG/KDIF/ISOTH-CGS: tube.cgns, CONDUCT 10, HEATCAPA 1, FOURIER 20, IMPLICIT + CGS,
-    DISSIPATIVE_FLUX FULL, T0 100, walls at 1000 and 2000, RESIDUALS 0.1 per cycle and 1e-5."""
+@pytest.mark.parametrize("inversion,max_it", [("CGS", 10), ("BICG", 10), ("GMRES", 50)])
+def test_oracle_reproduces_isoth(golden_dir, inversion, max_it):
+    """NRG/KDIF/ISOTH-{CGS,BICG,GMRES}: tube.cgns, CONDUCT 10, HEATCAPA 1, FOURIER 20, IMPLICIT
+    with Typhon's dlu_cgs, dlu_bicg or dlu_gmres (NKRYLOV 10) at their default IMP_MAX_IT and
+    INV_RES 1e-4, DISSIPATIVE_FLUX FULL, T0 100, walls at 1000 and 2000, RESIDUALS 0.1 per
+    cycle and 1e-5 overall."""
     md, om, kind, value = tube_kdif(golden_dir)
     k = op.Kdif(om, op.KDIF_FULL, 1.0, np.full(om.ncell_int, 10.0), kind, value)
     k.set_T(np.full(om.ncell, 100.0))
-    lr, avg, end = k.typhon_steady(20.0, 10.0, cycle_res=0.1, global_res=1e-5, cgs_maxres=1e-4, cgs_max_it=10)
-    gold = read_monres(golden_dir / "KDIF-ISOTH-CGS__monres.001")
+    lr, avg, end = k.typhon_steady(20.0, 10.0, cycle_res=0.1, global_res=1e-5, cgs_maxres=1e-4, cgs_max_it=max_it,
+                                   inversion=inversion, nkrylov=10)
+    gold = read_monres(golden_dir / f"KDIF-ISOTH-{inversion}__monres.001")
     assert len(lr) == len(gold) == 929
     assert np.abs(lr - gold).max() < 1e-10
     assert list(end) == [125, 326, 527, 728, 929]
     # Typhon prints 0.dddddddd E+xx: eight significant digits
     assert ["%.7E" % a for a in avg] == ["%.7E" % float(v) for v in
-                                         read_probe(golden_dir / "KDIF-ISOTH-CGS__Average_T.tmon")]
-
-
-def test_oracle_against_isoth_gmres(golden_dir):
-    md, om, kind, value = tube_kdif(golden_dir)
-    k = op.Kdif(om, op.KDIF_FULL, 1.0, np.full(om.ncell_int, 10.0), kind, value)
-    k.set_T(np.full(om.ncell, 100.0))
-    lr, avg, _ = k.typhon_steady(20.0, 10.0, cycle_res=0.1, global_res=1e-5, cgs_maxres=1e-4, cgs_max_it=10)
-    gold = read_monres(golden_dir / "KDIF-ISOTH-GMRES__monres.001")
-    assert len(lr) == len(gold)
-    assert np.abs(lr - gold).max() < 1e-5
-    probe = [float(v) for v in read_probe(golden_dir / "KDIF-ISOTH-GMRES__Average_T.tmon")]
-    assert np.allclose(avg, probe, rtol=1e-6, atol=0)
+                                         read_probe(golden_dir / f"KDIF-ISOTH-{inversion}__Average_T.tmon")]

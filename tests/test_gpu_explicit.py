@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 FAST_RTOL = 1e-12   # relative L2 per conserved variable, fast mode vs oracle
 
-OSCH = {"HLLC": op.SCH_HLLC, "RUSANOV": op.SCH_RUSANOV, "ROE": op.SCH_ROE}
+OSCH = {"HLLC": op.SCH_HLLC, "RUSANOV": op.SCH_RUSANOV, "ROE": op.SCH_ROE, "HLLE": op.SCH_HLLE}
 OHRES = {"NONE": op.HRES_NONE, "MUSCL": op.HRES_MUSCL, "MUSCL-FAST": op.HRES_MUSCLFAST,
          "MUSCL-UNS": op.HRES_MUSCLUNS}
 OLIM = {"NONE": op.LIM_NONE, "MINMOD": op.LIM_MINMOD, "ALBADA": op.LIM_ALBADA, "VAN_LEER": op.LIM_VLEER,
@@ -87,6 +87,8 @@ COMBOS = [
     ("HLLC", "MUSCL", "SUPERBEE", "SUPERBARTH"),
     ("RUSANOV", "MUSCL-FAST", "KIM3", "NONE"),
     ("HLLC", "MUSCL-FAST", "LIM03", "NONE"),
+    ("HLLE", "NONE", "NONE", "NONE"),
+    ("HLLE", "MUSCL", "ALBADA", "NONE"),
 ]
 
 
