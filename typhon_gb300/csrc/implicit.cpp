@@ -89,8 +89,9 @@ int build_lists(ty_mesh* h) {
       (rc = h->alloc(im.jacR, (size_t)m.nf * kBlk)) || (rc = h->alloc(im.b, 5 * (size_t)nci)) ||
       (rc = h->alloc(im.x, 5 * (size_t)nci)) || (rc = h->alloc(im.r, 5 * (size_t)nci)) ||
       (rc = h->alloc(im.w, 5 * (size_t)nci)) || (rc = h->alloc(im.part, (size_t)(kMaxKrylov + 1) * kRedBlocks)) ||
-      (rc = h->alloc(im.scal, (size_t)kScalCount)))
+      (rc = h->alloc(im.scal, (size_t)kScalCount)) || (rc = h->alloc(im.done, 1)))
     return rc;
+  IMP_CU(cudaMemset(im.done, 0, sizeof(unsigned)));
   IMP_CU(cudaMemcpy(im.cfo, cfo.data(), cfo.size() * sizeof(int), cudaMemcpyHostToDevice));
   IMP_CU(cudaMemcpy(im.cfon, cfon.data(), cfon.size() * sizeof(int), cudaMemcpyHostToDevice));
   if (!im.pinned && cudaMallocHost((void**)&im.pinned, kScalCount * sizeof(double)) != cudaSuccess)
@@ -366,10 +367,11 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
         IMP_CU(IMP_CALL(h, imp_precond, m, im, j > 0 ? im.w : nullptr, im.scal + kScalHinv, V(j), Z(j), Z32(j), s,
                         &h->prof));
         if (int rc = op.apply(Z(j), Z32(j), im.w, &matvecs)) return rc;
-        IMP_CU(IMP_CALL(h, imp_cgs_pass, im.V, n, j + 1, nullptr, im.w, 0, n, im.part, im.scal, s, &h->prof));
-        IMP_CU(IMP_CALL(h, imp_cgs_pass, im.V, n, j + 1, im.scal, im.w, 1, n, im.part, im.scal + kScalH2, s,
+        IMP_CU(IMP_CALL(h, imp_cgs_pass, im.V, n, j + 1, nullptr, im.w, 0, n, im.part, im.done, im.scal, s,
                         &h->prof));
-        IMP_CU(IMP_CALL(h, imp_cgs_pass, im.V, n, j + 1, im.scal + kScalH2, im.w, 2, n, im.part,
+        IMP_CU(IMP_CALL(h, imp_cgs_pass, im.V, n, j + 1, im.scal, im.w, 1, n, im.part, im.done, im.scal + kScalH2,
+                        s, &h->prof));
+        IMP_CU(IMP_CALL(h, imp_cgs_pass, im.V, n, j + 1, im.scal + kScalH2, im.w, 2, n, im.part, im.done,
                         im.scal + kScalNorm, s, &h->prof));
         if (int rc = fetch(h, 0, kScalNorm + 1)) return rc;
         for (int i = 0; i <= j; ++i) Hm(i, j) = P[i] + P[kScalH2 + i];

@@ -168,6 +168,14 @@ __device__ void implicit_face_states(const DevMesh& m, const DevState& s, const 
   }
 }
 
+// J dt / V of build_implicit_bdlu.f90:51-55: two roundings per entry in exact mode, a product
+// with the per-cell quotient q = dt / V in fast mode
+#if TY_FAST
+#define TY_DTV(J, dt, V, q) ((J) * (q))
+#else
+#define TY_DTV(J, dt, V, q) ((J) * (dt) / (V))
+#endif
+
 __device__ __forceinline__ double imp_dt(const ImpState& im, const ImpArgs& a, int c) {
   return a.local_dt ? im.dtloc[c] : __longlong_as_double((long long)*a.dtg);
 }
@@ -320,12 +328,15 @@ __global__ void __launch_bounds__(128) k_imp_face(DevMesh m, DevState s, SpatOpt
     const double dt1 = imp_dt(im, a, c1), dt2 = imp_dt(im, a, c2);
     const double V1 = m.cvol[c1], V2 = m.cvol[c2];
     double U[25];
+#if TY_FAST
+    const double q1 = dt1 / V1, q2 = dt2 / V2;
+#endif
 #pragma unroll
-    for (int k = 0; k < 25; ++k) U[k] = +JR[k] * dt1 / V1;
+    for (int k = 0; k < 25; ++k) U[k] = +TY_DTV(JR[k], dt1, V1, q1);
     if (a.want64) store_block(im.upper + (size_t)f * kBlk, U);
     if (a.want32) store_block32(im.upper32 + (size_t)f * kBlk32, U);
 #pragma unroll
-    for (int k = 0; k < 25; ++k) U[k] = -JL[k] * dt2 / V2;
+    for (int k = 0; k < 25; ++k) U[k] = -TY_DTV(JL[k], dt2, V2, q2);
     if (a.want64) store_block(im.lower + (size_t)f * kBlk, U);
     if (a.want32) store_block32(im.lower32 + (size_t)f * kBlk32, U);
   }
@@ -348,11 +359,17 @@ __device__ bool inv5(const double* A, double* X) {
       if (v > best) { best = v; p = r; }
     }
     if (!(best > 0.0)) return false;
-    if (p != col) {
+    // row swap with compile-time indices only (selects), so that a and X stay in registers
+#pragma unroll
+    for (int r = col + 1; r < 5; ++r) {
+      const bool sw = r == p;
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        double t = a[col * 5 + k]; a[col * 5 + k] = a[p * 5 + k]; a[p * 5 + k] = t;
-        t = X[col * 5 + k]; X[col * 5 + k] = X[p * 5 + k]; X[p * 5 + k] = t;
+        const double ta = a[col * 5 + k], tx = X[col * 5 + k];
+        a[col * 5 + k] = sw ? a[r * 5 + k] : ta;
+        a[r * 5 + k] = sw ? ta : a[r * 5 + k];
+        X[col * 5 + k] = sw ? X[r * 5 + k] : tx;
+        X[r * 5 + k] = sw ? tx : X[r * 5 + k];
       }
     }
     const double ip = 1.0 / a[col * 5 + col];
@@ -380,6 +397,9 @@ __global__ void __launch_bounds__(128) k_imp_diag(DevMesh m, ImpState im, ImpArg
 #pragma unroll
   for (int i = 0; i < 5; ++i) D[i * 6] = 1.0;
   const double dt = imp_dt(im, a, c), V = m.cvol[c];
+#if TY_FAST
+  const double q = dt / V;  // one division per cell; exact mode keeps Typhon's (J dt) / V per entry
+#endif
   for (int sl = 0; sl < m.nslot; ++sl) {
     const int e = im.cfo[sl * (size_t)m.nci + c];
     if (e < 0) break;
@@ -388,11 +408,11 @@ __global__ void __launch_bounds__(128) k_imp_diag(DevMesh m, ImpState im, ImpArg
     if (e & 1) {
       load_block(im.jacR + (size_t)f * kBlk, J);
 #pragma unroll
-      for (int k = 0; k < 25; ++k) D[k] = D[k] - J[k] * dt / V;
+      for (int k = 0; k < 25; ++k) D[k] = D[k] - TY_DTV(J[k], dt, V, q);
     } else {
       load_block(im.jacL + (size_t)f * kBlk, J);
 #pragma unroll
-      for (int k = 0; k < 25; ++k) D[k] = D[k] + J[k] * dt / V;
+      for (int k = 0; k < 25; ++k) D[k] = D[k] + TY_DTV(J[k], dt, V, q);
     }
   }
   if (a.want64) store_block(im.diag + (size_t)c * kBlk, D);
@@ -686,43 +706,78 @@ __global__ void __launch_bounds__(kRedThreads) k_mgs_pass(const double* __restri
 }
 
 // classical Gram-Schmidt pass over the basis V (j vectors, stride ldv):
-//   mode 0: partial sums of V_i . w                       (first projection)
-//   mode 1: w = w - sum_i h_i V_i, then partial V_i . w    (re-orthogonalisation projection)
-//   mode 2: w = w - sum_i h_i V_i, then partial w . w      (norm)
+//   mode 0: out_i = V_i . w                               (first projection)
+//   mode 1: w = w - sum_i h_i V_i, then out_i = V_i . w    (re-orthogonalisation projection)
+//   mode 2: w = w - sum_i h_i V_i, then out_0 = w . w      (norm)
+// One row per thread per trip: the row's j basis entries are loaded together (independent
+// loads in flight) and kept in registers; the per-thread sums live in shared memory, so the
+// register count does not grow with j.  Each block reduces its sums once, writes one partial
+// per output, and the last block to finish adds the partials in block order: one launch, and
+// the same result for the same grid.
 template <int J>
-__global__ void __launch_bounds__(kRedThreads) k_cgs_pass(const double* __restrict__ V, size_t ldv, int j,
+__global__ void __launch_bounds__(kCgsThreads) k_cgs_pass(const double* __restrict__ V, size_t ldv, int j,
                                                            const double* __restrict__ h, double* __restrict__ w,
-                                                           int mode, size_t n, double* __restrict__ part) {
+                                                           int mode, size_t n, double* __restrict__ part,
+                                                           unsigned* __restrict__ done, double* __restrict__ out) {
   __shared__ double hl[J];
-  if (threadIdx.x < J) hl[threadIdx.x] = (mode > 0 && (int)threadIdx.x < j) ? h[threadIdx.x] : 0.0;
-  __syncthreads();
-  double acc[J];
+  __shared__ double acc[J][kCgsThreads];
+  __shared__ bool last;
+  const int t = threadIdx.x;
+  if (t < J) hl[t] = (mode > 0 && t < j) ? h[t] : 0.0;
 #pragma unroll
-  for (int i = 0; i < J; ++i) acc[i] = 0.0;
-  for (size_t k = blockIdx.x * (size_t)kRedThreads + threadIdx.x; k < n; k += (size_t)gridDim.x * kRedThreads) {
+  for (int i = 0; i < J; ++i) acc[i][t] = 0.0;
+  __syncthreads();
+  double a2 = 0.0;
+  for (size_t k = blockIdx.x * (size_t)kCgsThreads + t; k < n; k += (size_t)gridDim.x * kCgsThreads) {
+    double v[J];
+    const double* pv = V + k;
+#pragma unroll
+    for (int i = 0; i < J; ++i) {
+      v[i] = i < j ? *pv : 0.0;
+      pv += ldv;
+    }
     double wk = w[k];
     if (mode > 0) {
 #pragma unroll
       for (int i = 0; i < J; ++i)
-        if (i < j) wk = wk - hl[i] * V[i * ldv + k];
+        if (i < j) wk = wk - hl[i] * v[i];
       w[k] = wk;
     }
     if (mode < 2) {
 #pragma unroll
       for (int i = 0; i < J; ++i)
-        if (i < j) acc[i] += V[i * ldv + k] * wk;
+        if (i < j) acc[i][t] += v[i] * wk;
     } else {
-      acc[0] += wk * wk;
+      a2 += wk * wk;
     }
   }
+  if (mode == 2) acc[0][t] = a2;
+  __syncthreads();
   const int nout = mode < 2 ? j : 1;
+  const int lane = t & 31, wid = t >> 5;
+  for (int i = wid; i < nout; i += kCgsThreads / 32) {
+    double x = 0.0;
 #pragma unroll
-  for (int i = 0; i < J; ++i) {
-    if (i < nout) {
-      double s = block_sum(acc[i]);
-      if (threadIdx.x == 0) part[(size_t)i * kRedBlocks + blockIdx.x] = s;
-    }
+    for (int q = 0; q < kCgsThreads / 32; ++q) x += acc[i][q * 32 + lane];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) part[(size_t)i * kRedBlocks + blockIdx.x] = x;
   }
+  __threadfence();
+  __syncthreads();
+  if (t == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int i = wid; i < nout; i += kCgsThreads / 32) {
+    const double* p = part + (size_t)i * kRedBlocks;
+    double x = 0.0;
+    for (unsigned b = lane; b < gridDim.x; b += 32) x += __ldcg(p + b);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) out[i] = x;
+  }
+  if (t == 0) *done = 0u;  // ready for the next launch on the stream
 }
 
 __global__ void k_scale(const double* __restrict__ w, double s, double* __restrict__ v, size_t n) {
@@ -869,17 +924,32 @@ cudaError_t imp_mgs_pass(const double* vprev, const double* hprev, double* w, co
   return cudaGetLastError();
 }
 
+// blocks of a CGS2 pass: the resident blocks of the whole GPU (at most kRedBlocks), fewer
+// for short vectors; a fixed function of n and the device, so sums repeat from run to run
+template <int J>
+unsigned cgs_grid(size_t n) {
+  static const unsigned cap = [] {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cgs_pass<J>, kCgsThreads, 0);
+    const long c = (long)std::max(sms, 1) * std::max(per, 1);
+    return (unsigned)std::min<long>(c, kRedBlocks);
+  }();
+  const size_t g = (n + kCgsThreads - 1) / kCgsThreads;
+  return (unsigned)std::max<size_t>(1, std::min<size_t>(g, cap));
+}
+
 cudaError_t imp_cgs_pass(const double* V, size_t ldv, int j, const double* h, double* w, int mode, size_t n,
-                         double* part, double* out, cudaStream_t st, Prof* pr) {
-  const unsigned g = red_grid(n);
+                         double* part, unsigned* done, double* out, cudaStream_t st, Prof* pr) {
   pr->launch(K_IMP_ORTHO, st, [&] {
     if (j <= 8)
-      k_cgs_pass<8><<<g, kRedThreads, 0, st>>>(V, ldv, j, h, w, mode, n, part);
+      k_cgs_pass<8><<<cgs_grid<8>(n), kCgsThreads, 0, st>>>(V, ldv, j, h, w, mode, n, part, done, out);
     else if (j <= 16)
-      k_cgs_pass<16><<<g, kRedThreads, 0, st>>>(V, ldv, j, h, w, mode, n, part);
+      k_cgs_pass<16><<<cgs_grid<16>(n), kCgsThreads, 0, st>>>(V, ldv, j, h, w, mode, n, part, done, out);
     else
-      k_cgs_pass<kMaxCgs><<<g, kRedThreads, 0, st>>>(V, ldv, j, h, w, mode, n, part);
-    k_red_final<<<mode < 2 ? j : 1, kRedThreads, 0, st>>>(part, (int)g, kRedBlocks, out);
+      k_cgs_pass<kMaxCgs><<<cgs_grid<kMaxCgs>(n), kCgsThreads, 0, st>>>(V, ldv, j, h, w, mode, n, part, done,
+                                                                          out);
   });
   return cudaGetLastError();
 }

@@ -25,6 +25,7 @@ constexpr int kMaxKrylov = 64;   // largest NKRYLOV of Typhon's GMRES
 constexpr int kMaxCgs = 32;      // largest restart length of the flexible GMRES (CGS2)
 constexpr int kRedBlocks = 1216; // blocks of a reduction (152 SMs x 8), fixed for determinism
 constexpr int kRedThreads = 256;
+constexpr int kCgsThreads = 128;  // threads of a CGS2 pass block (its sums: kMaxCgs x 128 doubles of shared memory)
 
 struct ImpState {
   bool lists = false;
@@ -52,6 +53,7 @@ struct ImpState {
   float* Z32 = nullptr;       // [nk][5 nci] preconditioned basis (mixed precision)
   double* part = nullptr;     // [kMaxKrylov + 1][kRedBlocks] partial sums
   double* scal = nullptr;     // [4 * kMaxKrylov] device scalars (Hessenberg column, step sizes)
+  unsigned* done = nullptr;   // [1] blocks finished in a one-launch reduction (zero between launches)
   double* upert = nullptr;    // [5][ldc] perturbed state (Jacobian-free products)
   double* r0 = nullptr;       // [5 nci] residual at the unperturbed state (Jacobian-free)
   double* pinned = nullptr;   // host mirror of scal (pinned)
@@ -89,7 +91,8 @@ struct ImpArgs {
   cudaError_t imp_mgs_pass(const double* vprev, const double* hprev, double* w, const double* vnext,    \
                            size_t n, double* part, double* out, cudaStream_t st);                        \
   cudaError_t imp_cgs_pass(const double* V, size_t ldv, int j, const double* h, double* w, int mode,     \
-                           size_t n, double* part, double* out, cudaStream_t st, Prof* pr);             \
+                           size_t n, double* part, unsigned* done, double* out, cudaStream_t st,        \
+                           Prof* pr);                                                                   \
   cudaError_t imp_scale(const double* w, double s, double* v, size_t n, cudaStream_t st);                \
   cudaError_t imp_bicgstab_iter(const DevMesh& m, const ImpState& im, double* x, double* r1,             \
                                 const double* r2, double* p, double* v, double* s, double* t, int first,  \
