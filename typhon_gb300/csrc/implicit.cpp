@@ -46,9 +46,10 @@ using namespace tyi;
 
 namespace {
 
-constexpr int kScalH2 = kMaxKrylov + 1;       // scal offsets: h, h' (CGS2), norm, 1/h
-constexpr int kScalNorm = 2 * kMaxKrylov + 2;
-constexpr int kScalHinv = 2 * kMaxKrylov + 3;
+constexpr int kScalGram = 0;                  // scal offsets of the flexible GMRES: V^T v_j, v_j . v_j
+constexpr int kScalProj = kMaxCgs + 1;        // V^T w, w . w (both fetched in one copy)
+constexpr int kScalCoef = 2 * kMaxCgs + 4;    // c of the next basis vector (after the fetched range)
+constexpr int kScalInvNu = 3 * kMaxCgs + 5;   // 1 / nu of the next basis vector
 constexpr int kScalY = 2 * kMaxKrylov + 4;    // solution coefficients (kMaxKrylov)
 constexpr int kScalMisc = 3 * kMaxKrylov + 4; // reductions of the step (16)
 constexpr int kScalCount = 3 * kMaxKrylov + 20;
@@ -128,7 +129,9 @@ int ensure_buffers(ty_mesh* h, const ty_imp_params* p) {
     const int cap = std::max(nk, im.nk);
     if ((rc = grow(h, im.V, (size_t)(cap + 1) * n))) return rc;
     if (!gm || im.Z || im.Z32) {
-      if (need32 || im.Z32) { if ((rc = grow(h, im.Z32, (size_t)cap * n))) return rc; }
+      if (need32 || im.Z32) {
+        if ((rc = grow(h, im.Z32, (size_t)cap * n)) || (rc = grow(h, im.V32, (size_t)(cap + 1) * n))) return rc;
+      }
       if (!need32 || im.Z) { if ((rc = grow(h, im.Z, (size_t)cap * n))) return rc; }
     }
     im.nk = cap;
@@ -320,6 +323,22 @@ int Operator::apply(const double* z, const float* z32, double* w, int* matvecs) 
   return TY_OK;
 }
 
+// Restarted flexible GMRES with a block-Jacobi preconditioner and one host synchronisation per
+// Krylov vector.  The basis V is not forced to be orthonormal; its Gram matrix G = R^T R is
+// measured instead.  Iteration j:
+//   1. v_j = (w_{j-1} - V c) / nu (v_0 = r / beta), stored, with its Gram column V^T v_j,
+//      v_j . v_j, in one sweep over the basis;
+//   2. z_j = M^-1 v_j, w_j = A z_j;
+//   3. V^T w_j and w_j . w_j in a second sweep, then on the host c = G^-1 V^T w_j, so that
+//      w_j - V c is orthogonal to the basis in exact arithmetic whatever V's rounding, and
+//      nu^2 = |w_j|^2 - |R^-T V^T w_j|^2.
+// A z_j = V c + nu v_{j+1} holds for the stored vectors, and |V (beta e1 - H y)| =
+// |R (beta e1 - H y)|: Givens rotations of R H minimise the true residual norm.  The Gram
+// column of v_{j+1} is only measured in the next iteration, so column j of R H is first
+// rotated with v_{j+1} taken as orthonormal and rotated again one iteration later.  A
+// cancellation of nu^2 below 1e-12 |w_j|^2 means the Krylov space is invariant to working
+// precision (breakdown; 1e-10 for the FP32 basis of the mixed solve, whose sweeps run in FP32
+// arithmetic): the cycle ends there.
 int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
   ImpState& im = h->imp;
   const DevMesh& m = h->m;
@@ -328,11 +347,40 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
   const bool f32 = op.kind == 1;
   cudaStream_t s = h->stream;
   double* P = im.pinned;
-  auto V = [&](int i) { return im.V + (size_t)i * n; };
+  double* V64 = f32 ? nullptr : im.V;
+  float* V32 = f32 ? im.V32 : nullptr;
+  auto Vd = [&](int i) { return V64 ? V64 + (size_t)i * n : nullptr; };
+  auto Vf = [&](int i) { return V32 ? V32 + (size_t)i * n : nullptr; };
   auto Z = [&](int i) { return f32 ? nullptr : im.Z + (size_t)i * n; };
   auto Z32 = [&](int i) { return f32 ? im.Z32 + (size_t)i * n : nullptr; };
-  std::vector<double> H((size_t)(mk + 1) * mk), cs(mk), sn(mk), g(mk + 1), y(mk);
-  auto Hm = [&](int i, int j) -> double& { return H[(size_t)i * mk + j]; };
+  const int ld = mk + 1;
+  std::vector<double> R((size_t)ld * ld, 0.0), Hc((size_t)ld * mk, 0.0), T((size_t)ld * mk, 0.0);
+  std::vector<double> cs(mk), sn(mk), a(mk + 1), gr(mk), y(mk), u(mk + 1), c(mk + 1), t(mk + 2);
+  auto Rm = [&](int i, int j) -> double& { return R[(size_t)i * ld + j]; };
+  auto Hm = [&](int i, int j) -> double& { return Hc[(size_t)i * mk + j]; };
+  auto Tm = [&](int i, int j) -> double& { return T[(size_t)i * mk + j]; };
+  // column jc of R H (R's column jc + 1 measured, or taken as e_{jc+1}), rotated by the
+  // earlier rotations; then its own rotation and the rotated right-hand side
+  auto rotate_column = [&](int jc, bool measured) {
+    for (int i = 0; i <= jc + 1; ++i) {
+      double v = 0.0;
+      for (int l = i; l <= jc; ++l) v += Rm(i, l) * Hm(l, jc);
+      v += (measured ? Rm(i, jc + 1) : (i == jc + 1 ? 1.0 : 0.0)) * Hm(jc + 1, jc);
+      t[i] = v;
+    }
+    for (int i = 0; i < jc; ++i) {
+      const double q = cs[i] * t[i] + sn[i] * t[i + 1];
+      t[i + 1] = -sn[i] * t[i] + cs[i] * t[i + 1];
+      t[i] = q;
+    }
+    const double den = std::hypot(t[jc], t[jc + 1]);
+    cs[jc] = den > 0.0 ? t[jc] / den : 1.0;
+    sn[jc] = den > 0.0 ? t[jc + 1] / den : 0.0;
+    t[jc] = den;
+    for (int i = 0; i <= jc; ++i) Tm(i, jc) = t[i];
+    gr[jc] = cs[jc] * a[jc];
+    a[jc + 1] = -sn[jc] * a[jc];
+  };
   IMP_CU(cudaMemsetAsync(im.x, 0, n * sizeof(double), s));
   IMP_CU(IMP_CALL(h, imp_dot, im.b, im.b, n, im.part, im.scal + kScalMisc, s));
   if (int rc = fetch(h, kScalMisc, 1)) return rc;
@@ -345,8 +393,8 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
     const double tol = p->inv_res * beta0;
     for (cycles = 0; cycles < std::max(p->max_it, 1); ++cycles) {
       double beta;
+      const double* src = im.b;
       if (cycles == 0) {
-        IMP_CU(cudaMemcpyAsync(im.r, im.b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         beta = beta0;
       } else {  // r = b - A x
         if (f32) IMP_CU(IMP_CALL(h, imp_to_f32, im.x, Z32(0), n, s));
@@ -357,56 +405,73 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
         beta = std::sqrt(P[kScalMisc]);
         rel = beta / beta0;
         if (beta <= tol) break;
+        src = im.r;
       }
-      IMP_CU(IMP_CALL(h, imp_scale, im.r, 1.0 / beta, V(0), n, s));
-      std::fill(g.begin(), g.end(), 0.0);
-      g[0] = beta;
+      const double binv = 1.0 / beta;
+      if (int rc = put(h, kScalInvNu, &binv, 1)) return rc;
+      a[0] = beta;
       int j, nused = 0;
       for (j = 0; j < mk; ++j) {
-        // z_j = M^-1 v_j (v_j = w / h(j, j-1) written by the same kernel for j > 0)
-        IMP_CU(IMP_CALL(h, imp_precond, m, im, j > 0 ? im.w : nullptr, im.scal + kScalHinv, V(j), Z(j), Z32(j), s,
-                        &h->prof));
+        IMP_CU(IMP_CALL(h, imp_basis_pass, V64, V32, n, j, im.scal + kScalCoef, j == 0 ? src : im.w,
+                        im.scal + kScalInvNu, 1, n, im.part, im.done, im.scal + kScalGram, s, &h->prof));
+        IMP_CU(IMP_CALL(h, imp_precond, m, im, Vd(j), Vf(j), Z(j), Z32(j), s, &h->prof));
         if (int rc = op.apply(Z(j), Z32(j), im.w, &matvecs)) return rc;
-        IMP_CU(IMP_CALL(h, imp_cgs_pass, im.V, n, j + 1, nullptr, im.w, 0, n, im.part, im.done, im.scal, s,
-                        &h->prof));
-        IMP_CU(IMP_CALL(h, imp_cgs_pass, im.V, n, j + 1, im.scal, im.w, 1, n, im.part, im.done, im.scal + kScalH2,
-                        s, &h->prof));
-        IMP_CU(IMP_CALL(h, imp_cgs_pass, im.V, n, j + 1, im.scal + kScalH2, im.w, 2, n, im.part, im.done,
-                        im.scal + kScalNorm, s, &h->prof));
-        if (int rc = fetch(h, 0, kScalNorm + 1)) return rc;
-        for (int i = 0; i <= j; ++i) Hm(i, j) = P[i] + P[kScalH2 + i];
-        Hm(j + 1, j) = std::sqrt(P[kScalNorm]);
+        IMP_CU(IMP_CALL(h, imp_basis_pass, V64, V32, n, j + 1, nullptr, im.w, nullptr, 0, n, im.part, im.done,
+                        im.scal + kScalProj, s, &h->prof));
+        if (int rc = fetch(h, 0, kScalProj + j + 2)) return rc;
+        // column j of the Cholesky factor of G
+        double d = P[kScalGram + j];
         for (int i = 0; i < j; ++i) {
-          const double t = cs[i] * Hm(i, j) + sn[i] * Hm(i + 1, j);
-          Hm(i + 1, j) = -sn[i] * Hm(i, j) + cs[i] * Hm(i + 1, j);
-          Hm(i, j) = t;
+          double v = P[kScalGram + i];
+          for (int l = 0; l < i; ++l) v -= Rm(l, i) * Rm(l, j);
+          Rm(i, j) = v / Rm(i, i);
+          d -= Rm(i, j) * Rm(i, j);
         }
-        const double hn = Hm(j + 1, j);
-        const double den = std::hypot(Hm(j, j), hn);
-        cs[j] = den > 0.0 ? Hm(j, j) / den : 1.0;
-        sn[j] = den > 0.0 ? hn / den : 0.0;
-        Hm(j, j) = den;
-        Hm(j + 1, j) = 0.0;
-        g[j + 1] = -sn[j] * g[j];
-        g[j] = cs[j] * g[j];
+        if (!(d > 1e-10 * P[kScalGram + j])) break;  // v_j no longer independent of the basis
+        Rm(j, j) = std::sqrt(d);
+        if (j == 0) a[0] = beta * Rm(0, 0);
+        else rotate_column(j - 1, true);
+        // c = G^-1 V^T w: R^T u = V^T w, R c = u
+        const double ww = P[kScalProj + j + 1];
+        double uu = 0.0;
+        for (int i = 0; i <= j; ++i) {
+          double v = P[kScalProj + i];
+          for (int l = 0; l < i; ++l) v -= Rm(l, i) * u[l];
+          u[i] = v / Rm(i, i);
+          uu += u[i] * u[i];
+        }
+        for (int i = j; i >= 0; --i) {
+          double v = u[i];
+          for (int l = i + 1; l <= j; ++l) v -= Rm(i, l) * c[l];
+          c[i] = v / Rm(i, i);
+        }
+        const double nu2 = ww - uu;
+        const bool invariant = !(nu2 > (f32 ? 1e-10 : 1e-12) * ww);
+        const double nu = invariant ? 0.0 : std::sqrt(nu2);
+        for (int i = 0; i <= j; ++i) Hm(i, j) = c[i];
+        Hm(j + 1, j) = nu;
+        rotate_column(j, false);
         nused = j + 1;
         if (trace)
-          std::fprintf(stderr, "ty_implicit fgmres cycle %d j %d h_jj %.6e h_j+1,j %.6e |g|/|b| %.6e\n", cycles, j,
-                       Hm(j, j), hn, std::fabs(g[j + 1]) / beta0);
-        if (std::fabs(g[j + 1]) <= tol || !(hn > 0.0)) break;
-        const double hinv = 1.0 / hn;
-        if (int rc = put(h, kScalHinv, &hinv, 1)) return rc;
+          std::fprintf(stderr, "ty_implicit fgmres cycle %d j %d r_jj %.6e nu %.6e |g|/|b| %.6e\n", cycles, j,
+                       Rm(j, j), nu, std::fabs(a[j + 1]) / beta0);
+        if (std::fabs(a[j + 1]) <= tol || invariant) break;
+        const double ninv = 1.0 / nu;
+        if (int rc = put(h, kScalCoef, c.data(), j + 1)) return rc;
+        if (int rc = put(h, kScalInvNu, &ninv, 1)) return rc;
       }
       for (int i = nused - 1; i >= 0; --i) {
-        double t = g[i];
-        for (int k = i + 1; k < nused; ++k) t -= Hm(i, k) * y[k];
-        y[i] = t / Hm(i, i);
+        double v = gr[i];
+        for (int k = i + 1; k < nused; ++k) v -= Tm(i, k) * y[k];
+        y[i] = v / Tm(i, i);
       }
-      if (int rc = put(h, kScalY, y.data(), nused)) return rc;
-      IMP_CU(IMP_CALL(h, imp_axpy_multi, im.x, f32 ? nullptr : im.Z, f32 ? im.Z32 : nullptr, n, nused,
-                      im.scal + kScalY, 0, n, s));
-      rel = std::fabs(g[nused]) / beta0;
-      if (std::fabs(g[nused]) <= tol) { ++cycles; break; }
+      if (nused > 0) {
+        if (int rc = put(h, kScalY, y.data(), nused)) return rc;
+        IMP_CU(IMP_CALL(h, imp_axpy_multi, im.x, f32 ? nullptr : im.Z, f32 ? im.Z32 : nullptr, n, nused,
+                        im.scal + kScalY, 0, n, s));
+      }
+      rel = std::fabs(a[nused]) / beta0;
+      if (std::fabs(a[nused]) <= tol) { ++cycles; break; }
     }
   }
   st->restarts = cycles;

@@ -16,6 +16,7 @@
 // rounding, not bitwise.
 #pragma once
 #include <algorithm>
+#include <type_traits>
 
 #include "implicit.hpp"
 
@@ -532,25 +533,17 @@ __global__ void __launch_bounds__(128) k_imp_matvec32(DevMesh m, ImpState im, co
 
 // v = w * hinv[0] (when w is given), then the block-Jacobi preconditioned z = D^-1 v
 // (FP64 into z, or FP32 into z32)
-__global__ void __launch_bounds__(128) k_imp_precond(DevMesh m, ImpState im, const double* __restrict__ w,
-                                                      const double* __restrict__ hinv, double* __restrict__ v,
-                                                      double* __restrict__ z, float* __restrict__ z32) {
+// z = D^-1 v, the block-Jacobi preconditioner of the flexible GMRES: FP64 (v, dinv, z) or
+// FP32 (v32, dinv32, z32)
+__global__ void __launch_bounds__(128) k_imp_precond(DevMesh m, ImpState im, const double* __restrict__ v,
+                                                      const float* __restrict__ v32, double* __restrict__ z,
+                                                      float* __restrict__ z32) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nci) return;
-  double vv[5];
-  if (w) {
-    const double s = *hinv;
-#pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      vv[k] = w[5 * (size_t)c + k] * s;
-      v[5 * (size_t)c + k] = vv[k];
-    }
-  } else {
+  if (z) {
+    double A[25], vv[5], t[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) vv[k] = v[5 * (size_t)c + k];
-  }
-  if (z) {
-    double A[25], t[5];
     load_block(im.dinv + (size_t)c * kBlk, A);
     mv5(A, vv, t);
 #pragma unroll
@@ -559,7 +552,7 @@ __global__ void __launch_bounds__(128) k_imp_precond(DevMesh m, ImpState im, con
     float A[28], vf[5];
     load_block32(im.dinv32 + (size_t)c * kBlk32, A);
 #pragma unroll
-    for (int k = 0; k < 5; ++k) vf[k] = (float)vv[k];
+    for (int k = 0; k < 5; ++k) vf[k] = v32 ? v32[5 * (size_t)c + k] : (float)v[5 * (size_t)c + k];
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
       float s = 0.f;
@@ -705,55 +698,96 @@ __global__ void __launch_bounds__(kRedThreads) k_mgs_pass(const double* __restri
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-// classical Gram-Schmidt pass over the basis V (j vectors, stride ldv):
-//   mode 0: out_i = V_i . w                               (first projection)
-//   mode 1: w = w - sum_i h_i V_i, then out_i = V_i . w    (re-orthogonalisation projection)
-//   mode 2: w = w - sum_i h_i V_i, then out_0 = w . w      (norm)
-// One row per thread per trip: the row's j basis entries are loaded together (independent
-// loads in flight) and kept in registers; the per-thread sums live in shared memory, so the
-// register count does not grow with j.  Each block reduces its sums once, writes one partial
-// per output, and the last block to finish adds the partials in block order: one launch, and
-// the same result for the same grid.
-template <int J>
-__global__ void __launch_bounds__(kCgsThreads) k_cgs_pass(const double* __restrict__ V, size_t ldv, int j,
-                                                           const double* __restrict__ h, double* __restrict__ w,
-                                                           int mode, size_t n, double* __restrict__ part,
-                                                           unsigned* __restrict__ done, double* __restrict__ out) {
-  __shared__ double hl[J];
-  __shared__ double acc[J][kCgsThreads];
+// Krylov basis pass of the flexible GMRES (basis vector i at V + i ldv, stored as T):
+//   extend 0: out_i = V_i . src (i < nv), out_nv = src . src
+//   extend 1: v = (src - sum_{i<nv} c_i V_i) s is stored as V_nv (rounded to T), then
+//             out_i = V_i . v (i < nv), out_nv = v . v, of the stored values
+// An FP64 basis is swept in FP64; an FP32 basis (mixed-precision solve) in FP32 arithmetic
+// with FP64 block sums.  The first form projects A z_j on the basis; the second forms the next
+// basis vector and the new column of the basis' Gram matrix in the same sweep, so one iteration reads the basis
+// twice and synchronises with the host once.  One row per thread per trip: the row's basis
+// entries are loaded together and kept in registers; the per-thread sums live in shared
+// memory.  Each block reduces its sums once, writes one partial per output, and the last block
+// to finish adds the partials in block order: one launch, the same result for the same grid.
+template <int J, class T>
+__global__ void __launch_bounds__(kCgsThreads) k_basis_pass(T* V, size_t ldv, int nv, const double* __restrict__ c,
+                                                             const double* __restrict__ src,
+                                                             const double* __restrict__ sp, int extend, size_t n,
+                                                             double* __restrict__ part, unsigned* __restrict__ done,
+                                                             double* __restrict__ out) {
+  __shared__ double cl[J];
+  __shared__ double acc[J + 1][kCgsThreads];
   __shared__ bool last;
   const int t = threadIdx.x;
-  if (t < J) hl[t] = (mode > 0 && t < j) ? h[t] : 0.0;
+  if (t < J) cl[t] = (extend && t < nv) ? c[t] : 0.0;
 #pragma unroll
-  for (int i = 0; i < J; ++i) acc[i][t] = 0.0;
+  for (int i = 0; i <= J; ++i) acc[i][t] = 0.0;
+  const double sc = extend ? *sp : 1.0;
   __syncthreads();
-  double a2 = 0.0;
-  for (size_t k = blockIdx.x * (size_t)kCgsThreads + t; k < n; k += (size_t)gridDim.x * kCgsThreads) {
-    double v[J];
-    const double* pv = V + k;
+  T* vout = V + (size_t)nv * ldv;
+  if constexpr (std::is_same<T, double>::value) {
+    double xx = 0.0;
+    for (size_t k = blockIdx.x * (size_t)kCgsThreads + t; k < n; k += (size_t)gridDim.x * kCgsThreads) {
+      double v[J];
+      const double* pv = V + k;
+#pragma unroll
+      for (int i = 0; i < J; ++i) {
+        v[i] = i < nv ? *pv : 0.0;
+        pv += ldv;
+      }
+      double x = src[k];
+      if (extend) {
+#pragma unroll
+        for (int i = 0; i < J; ++i)
+          if (i < nv) x = x - cl[i] * v[i];
+        x = x * sc;
+        vout[k] = x;
+      }
+#pragma unroll
+      for (int i = 0; i < J; ++i)
+        if (i < nv) acc[i][t] += v[i] * x;
+      xx += x * x;
+    }
+    acc[nv][t] = xx;
+  } else {
+    // FP32 basis: FP32 arithmetic per row (GB300 issues FP32 at about 60x its FP64 rate),
+    // per-thread sums in FP32 registers over the thread's rows, FP64 from the block sums on
+    float cf[J], af[J];
 #pragma unroll
     for (int i = 0; i < J; ++i) {
-      v[i] = i < j ? *pv : 0.0;
-      pv += ldv;
+      cf[i] = (float)cl[i];
+      af[i] = 0.f;
     }
-    double wk = w[k];
-    if (mode > 0) {
+    const float sf = (float)sc;
+    float xx = 0.f;
+    for (size_t k = blockIdx.x * (size_t)kCgsThreads + t; k < n; k += (size_t)gridDim.x * kCgsThreads) {
+      float v[J];
+      const float* pv = V + k;
+#pragma unroll
+      for (int i = 0; i < J; ++i) {
+        v[i] = i < nv ? *pv : 0.f;
+        pv += ldv;
+      }
+      float x = (float)src[k];
+      if (extend) {
+#pragma unroll
+        for (int i = 0; i < J; ++i)
+          if (i < nv) x = fmaf(-cf[i], v[i], x);
+        x = x * sf;
+        vout[k] = x;
+      }
 #pragma unroll
       for (int i = 0; i < J; ++i)
-        if (i < j) wk = wk - hl[i] * v[i];
-      w[k] = wk;
+        if (i < nv) af[i] = fmaf(v[i], x, af[i]);
+      xx = fmaf(x, x, xx);
     }
-    if (mode < 2) {
 #pragma unroll
-      for (int i = 0; i < J; ++i)
-        if (i < j) acc[i][t] += v[i] * wk;
-    } else {
-      a2 += wk * wk;
-    }
+    for (int i = 0; i < J; ++i)
+      if (i < nv) acc[i][t] = (double)af[i];
+    acc[nv][t] = (double)xx;
   }
-  if (mode == 2) acc[0][t] = a2;
   __syncthreads();
-  const int nout = mode < 2 ? j : 1;
+  const int nout = nv + 1;
   const int lane = t & 31, wid = t >> 5;
   for (int i = wid; i < nout; i += kCgsThreads / 32) {
     double x = 0.0;
@@ -890,10 +924,10 @@ cudaError_t imp_matvec32(const DevMesh& m, const ImpState& im, const float* z, d
   return cudaGetLastError();
 }
 
-cudaError_t imp_precond(const DevMesh& m, const ImpState& im, const double* w, const double* hinv, double* v,
-                        double* z, float* z32, cudaStream_t st, Prof* pr) {
+cudaError_t imp_precond(const DevMesh& m, const ImpState& im, const double* v, const float* v32, double* z,
+                        float* z32, cudaStream_t st, Prof* pr) {
   pr->launch(K_IMP_PRECOND, st,
-             [&] { k_imp_precond<<<grid_of(m.nci, 128), 128, 0, st>>>(m, im, w, hinv, v, z, z32); });
+             [&] { k_imp_precond<<<grid_of(m.nci, 128), 128, 0, st>>>(m, im, v, v32, z, z32); });
   return cudaGetLastError();
 }
 
@@ -924,15 +958,15 @@ cudaError_t imp_mgs_pass(const double* vprev, const double* hprev, double* w, co
   return cudaGetLastError();
 }
 
-// blocks of a CGS2 pass: the resident blocks of the whole GPU (at most kRedBlocks), fewer
+// blocks of a basis pass: the resident blocks of the whole GPU (at most kRedBlocks), fewer
 // for short vectors; a fixed function of n and the device, so sums repeat from run to run
-template <int J>
-unsigned cgs_grid(size_t n) {
+template <int J, class T>
+unsigned basis_grid(size_t n) {
   static const unsigned cap = [] {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cgs_pass<J>, kCgsThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_basis_pass<J, T>, kCgsThreads, 0);
     const long c = (long)std::max(sms, 1) * std::max(per, 1);
     return (unsigned)std::min<long>(c, kRedBlocks);
   }();
@@ -940,16 +974,27 @@ unsigned cgs_grid(size_t n) {
   return (unsigned)std::max<size_t>(1, std::min<size_t>(g, cap));
 }
 
-cudaError_t imp_cgs_pass(const double* V, size_t ldv, int j, const double* h, double* w, int mode, size_t n,
-                         double* part, unsigned* done, double* out, cudaStream_t st, Prof* pr) {
+template <class T>
+void basis_launch(T* V, size_t ldv, int nv, const double* c, const double* src, const double* sp, int extend,
+                  size_t n, double* part, unsigned* done, double* out, cudaStream_t st) {
+  if (nv <= 8)
+    k_basis_pass<8, T><<<basis_grid<8, T>(n), kCgsThreads, 0, st>>>(V, ldv, nv, c, src, sp, extend, n, part, done,
+                                                                     out);
+  else if (nv <= 16)
+    k_basis_pass<16, T><<<basis_grid<16, T>(n), kCgsThreads, 0, st>>>(V, ldv, nv, c, src, sp, extend, n, part,
+                                                                       done, out);
+  else
+    k_basis_pass<kMaxCgs, T><<<basis_grid<kMaxCgs, T>(n), kCgsThreads, 0, st>>>(V, ldv, nv, c, src, sp, extend, n,
+                                                                                 part, done, out);
+}
+
+cudaError_t imp_basis_pass(double* V, float* V32, size_t ldv, int nv, const double* c, const double* src,
+                           const double* sp, int extend, size_t n, double* part, unsigned* done, double* out,
+                           cudaStream_t st, Prof* pr) {
+  if (nv < 0 || nv > kMaxCgs) return cudaErrorInvalidValue;
   pr->launch(K_IMP_ORTHO, st, [&] {
-    if (j <= 8)
-      k_cgs_pass<8><<<cgs_grid<8>(n), kCgsThreads, 0, st>>>(V, ldv, j, h, w, mode, n, part, done, out);
-    else if (j <= 16)
-      k_cgs_pass<16><<<cgs_grid<16>(n), kCgsThreads, 0, st>>>(V, ldv, j, h, w, mode, n, part, done, out);
-    else
-      k_cgs_pass<kMaxCgs><<<cgs_grid<kMaxCgs>(n), kCgsThreads, 0, st>>>(V, ldv, j, h, w, mode, n, part, done,
-                                                                          out);
+    if (V32) basis_launch(V32, ldv, nv, c, src, sp, extend, n, part, done, out, st);
+    else basis_launch(V, ldv, nv, c, src, sp, extend, n, part, done, out, st);
   });
   return cudaGetLastError();
 }

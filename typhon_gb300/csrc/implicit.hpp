@@ -25,7 +25,7 @@ constexpr int kMaxKrylov = 64;   // largest NKRYLOV of Typhon's GMRES
 constexpr int kMaxCgs = 32;      // largest restart length of the flexible GMRES (CGS2)
 constexpr int kRedBlocks = 1216; // blocks of a reduction (152 SMs x 8), fixed for determinism
 constexpr int kRedThreads = 256;
-constexpr int kCgsThreads = 128;  // threads of a CGS2 pass block (its sums: kMaxCgs x 128 doubles of shared memory)
+constexpr int kCgsThreads = 128;  // threads of a Krylov basis pass block (sums: (kMaxCgs + 1) x 128 doubles of shared memory)
 
 struct ImpState {
   bool lists = false;
@@ -49,6 +49,7 @@ struct ImpState {
   double* r = nullptr;        // [5 nci]
   double* w = nullptr;        // [5 nci]
   double* V = nullptr;        // [nk + 1][5 nci] Krylov basis
+  float* V32 = nullptr;       // [nk + 1][5 nci] Krylov basis of the mixed-precision flexible GMRES
   double* Z = nullptr;        // [nk][5 nci] preconditioned basis (flexible GMRES, FP64)
   float* Z32 = nullptr;       // [nk][5 nci] preconditioned basis (mixed precision)
   double* part = nullptr;     // [kMaxKrylov + 1][kRedBlocks] partial sums
@@ -81,8 +82,8 @@ struct ImpArgs {
                          double* y, cudaStream_t st, Prof* pr);                                         \
   cudaError_t imp_matvec32(const DevMesh& m, const ImpState& im, const float* z, double* y,              \
                            cudaStream_t st, Prof* pr);                                                  \
-  cudaError_t imp_precond(const DevMesh& m, const ImpState& im, const double* w, const double* hinv,     \
-                          double* v, double* z, float* z32, cudaStream_t st, Prof* pr);                  \
+  cudaError_t imp_precond(const DevMesh& m, const ImpState& im, const double* v, const float* v32,       \
+                          double* z, float* z32, cudaStream_t st, Prof* pr);                             \
   cudaError_t imp_x0_diag(const DevMesh& m, const ImpState& im, const double* b, double* x,             \
                           cudaStream_t st);                                                             \
   cudaError_t imp_dot(const double* a, const double* b, size_t n, double* part, double* out,              \
@@ -90,9 +91,9 @@ struct ImpArgs {
   cudaError_t imp_asum(const double* a, size_t n, double* part, double* out, cudaStream_t st);           \
   cudaError_t imp_mgs_pass(const double* vprev, const double* hprev, double* w, const double* vnext,    \
                            size_t n, double* part, double* out, cudaStream_t st);                        \
-  cudaError_t imp_cgs_pass(const double* V, size_t ldv, int j, const double* h, double* w, int mode,     \
-                           size_t n, double* part, unsigned* done, double* out, cudaStream_t st,        \
-                           Prof* pr);                                                                   \
+  cudaError_t imp_basis_pass(double* V, float* V32, size_t ldv, int nv, const double* c,                \
+                             const double* src, const double* sp, int extend, size_t n, double* part,   \
+                             unsigned* done, double* out, cudaStream_t st, Prof* pr);                   \
   cudaError_t imp_scale(const double* w, double s, double* v, size_t n, cudaStream_t st);                \
   cudaError_t imp_bicgstab_iter(const DevMesh& m, const ImpState& im, double* x, double* r1,             \
                                 const double* r2, double* p, double* v, double* s, double* t, int first,  \
