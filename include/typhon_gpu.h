@@ -224,8 +224,9 @@ int ty_profile_read(ty_mesh* mesh, int32_t n, double* ms, int32_t* launches);
  */
 typedef enum {
   TY_KRYLOV_GMRES = 0,   /* Typhon's bdlu_gmres (bdlu_gmres.f90:50-217): MGS, no preconditioner */
-  TY_KRYLOV_FGMRES = 1,  /* flexible GMRES(m), CGS2, right block-Jacobi, assembled matrix (new) */
-  TY_KRYLOV_JFNK = 2,    /* flexible GMRES(m), CGS2, block-Jacobi, Jacobian-free products (new) */
+  TY_KRYLOV_FGMRES = 1,  /* flexible GMRES(m), right block-Jacobi, assembled matrix (new); the
+                            basis' Gram matrix is measured, one host synchronisation per vector */
+  TY_KRYLOV_JFNK = 2,    /* the same flexible GMRES(m) on Jacobian-free products (new) */
   TY_KRYLOV_BICGSTAB = 3 /* Typhon's bdlu_bicgstab (bdlu_bicgstab.f90:40-80), its default for the
                             Navier-Stokes implicit method: x0 = b / diag, stopped when
                             sum|alpha p + omega s| < INV_RES sum|x0| or after max_it + 1
@@ -233,8 +234,9 @@ typedef enum {
 } ty_krylov;
 typedef enum {
   TY_PREC_FP64 = 0,      /* everything in FP64 */
-  TY_PREC_MIXED = 1      /* TY_KRYLOV_FGMRES only: FP32 blocks, mat-vec and preconditioner; FP64
-                            residual, basis, CGS2 orthogonalisation and update */
+  TY_PREC_MIXED = 1      /* TY_KRYLOV_FGMRES only: FP32 blocks, mat-vec, preconditioner and
+                            Krylov basis (swept in FP32, FP64 block sums); FP64 residual of the
+                            step and of each restart, Hessenberg algebra and update */
 } ty_precision;
 typedef struct ty_imp_params {
   int32_t krylov;        /* ty_krylov (INVERSION = GMRES is TY_KRYLOV_GMRES) */

@@ -184,7 +184,7 @@ class Grid:
     def implicit_step(self, cfl, inversion="GMRES", nkrylov=50, max_it=50, inv_res=1e-4, local_dt=False,
                       precision="fp64"):
         """One backward-Euler step on the resident state.  inversion: GMRES (Typhon's
-        bdlu_gmres), FGMRES (CGS2, block Jacobi) or JFNK; precision fp64 | mixed (FGMRES).
+        bdlu_gmres), FGMRES (block Jacobi, measured Gram matrix) or JFNK; precision fp64 | mixed (FGMRES).
         Returns the ty_imp_stats fields as a dict."""
         p = _capi.ImpParams(KRYLOV[inversion], PRECISION[precision], int(nkrylov), int(max_it), int(local_dt), 0,
                             float(inv_res), float(cfl))
