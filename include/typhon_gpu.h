@@ -41,7 +41,8 @@ extern "C" {
 
 /* ---- option enums (values match the oracle and the Python binding) ---- */
 /* TY_SCH_HLLE: calc_flux_hlle.f90 (beta = 1) with the HLL Jacobian of its wave speeds. */
-enum ty_scheme { TY_SCH_HLLC = 1, TY_SCH_RUSANOV = 2, TY_SCH_ROE = 3, TY_SCH_HLLE = 5 };
+/* TY_SCH_AUSMM: calc_flux_ausmm.f90 (explicit only: Typhon has no AUSM-M Jacobian). */
+enum ty_scheme { TY_SCH_HLLC = 1, TY_SCH_RUSANOV = 2, TY_SCH_ROE = 3, TY_SCH_AUSMM = 4, TY_SCH_HLLE = 5 };
 enum ty_highres { TY_HRES_NONE = 0, TY_HRES_MUSCL = 1, TY_HRES_MUSCLFAST = 2, TY_HRES_MUSCLUNS = 3 };
 enum ty_limiter {
   TY_LIM_NONE = 0, TY_LIM_MINMOD = 1, TY_LIM_ALBADA = 2, TY_LIM_VLEER = 3,
@@ -50,6 +51,7 @@ enum ty_limiter {
 enum ty_postlim { TY_POSTLIM_NONE = 0, TY_POSTLIM_BARTH = 1, TY_POSTLIM_SUPERBARTH = 2 };
 enum ty_gradmeth { TY_GRAD_NONE = 0, TY_GRAD_LSQ = 1, TY_GRAD_LSQW = 2 };
 enum ty_rk {
+  TY_RK_EXPLICIT = 0,  /* TIME_PARAM METHOD = EXPLICIT (treelevel_explicit.f90): forward Euler */
   TY_RK2 = 1, TY_RK2SSP = 2, TY_RK3SSP = 3, TY_RK4 = 4, TY_LSRK25BB = 5, TY_LSRK26BB = 6,
   TY_LSRK12BS = 7, TY_LSRK13BS = 8
 };
@@ -190,6 +192,14 @@ int ty_rk_step(ty_mesh* mesh, int32_t rk_method, double dt);
  * the device (no host synchronisation between steps).  dt_last: the last step's dt (host)
  * or NULL. */
 int ty_rk_steps(ty_mesh* mesh, int32_t rk_method, double cfl, int32_t nsteps, double* dt_last);
+
+/* One iteration of Typhon's steady explicit run (integration_cyclezone.f90:80-170 with
+ * TIME = STEADY): the global stability time step at CFL cfl (calc_zonetimestep.f90:54-126),
+ * one step of rk_method, and update_field.f90:45-60's residual terms of the step's update
+ * res_l1[3] = (sum |d rho|, sum |d rho E|, sum |d rho u|) over the interior cells (host).
+ * dt_out: the time step (host) or NULL.  The caller divides by the reference state and runs
+ * the cycle logic (the Python side's Grid.ns_steady). */
+int ty_steady_iteration(ty_mesh* mesh, int32_t rk_method, double cfl, double* dt_out, double* res_l1);
 
 /* Debug/parity access to intermediate fields of the last residual evaluation (host):
  * which = 0 prim [5][ncell], 1 grad [15][ncell], 2 face flux*S [5][nface],

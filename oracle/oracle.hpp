@@ -130,13 +130,13 @@ bool build_umesh(const RawMesh& raw, int geo_dim, const std::vector<BcDef>& bcs,
 
 // ---------------------------------------------------------------------------
 // Solver
-enum Scheme { SCH_HLLC = 1, SCH_RUSANOV = 2, SCH_ROE = 3, SCH_HLLE = 5 };
+enum Scheme { SCH_HLLC = 1, SCH_RUSANOV = 2, SCH_ROE = 3, SCH_AUSMM = 4, SCH_HLLE = 5 };
 enum HighRes { HRES_NONE = 0, HRES_MUSCL = 1, HRES_MUSCLFAST = 2, HRES_MUSCLUNS = 3 };
 enum Limiter { LIM_NONE = 0, LIM_MINMOD = 1, LIM_ALBADA = 2, LIM_VLEER = 3, LIM_SBEE = 4,
                LIM_KIM3 = 5, LIM_LIM03 = 6 };
 enum PostLim { POSTLIM_NONE = 0, POSTLIM_BARTH = 1, POSTLIM_SUPERBARTH = 2 };
 enum GradMeth { GRAD_NONE = 0, GRAD_LSQ = 1, GRAD_LSQW = 2 };
-enum RkMethod { RK2 = 1, RK2SSP = 2, RK3SSP = 3, RK4 = 4, LSRK25BB = 5, LSRK26BB = 6,
+enum RkMethod { EXPLICIT = 0, RK2 = 1, RK2SSP = 2, RK3SSP = 3, RK4 = 4, LSRK25BB = 5, LSRK26BB = 6,
                 LSRK12BS = 7, LSRK13BS = 8 };
 
 struct SpatParams {
@@ -308,6 +308,7 @@ struct NsSteadyParams {
   double cycle_res = 0.1, global_res = 1e-5;   // TIME_PARAM and PROJECT RESIDUALS
   int max_iters = 100000, max_cycles = 1000;
   std::vector<int> history_faces;              // faces of the family with SAVE_HISTORY
+  int rk_method = -1;                          // >= 0: explicit steps (0 = METHOD EXPLICIT), else implicit
 };
 struct NsSteadyOut {
   std::vector<double> log_res;      // log10 residual of every iteration

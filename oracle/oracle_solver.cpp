@@ -37,6 +37,7 @@ RkTable rk_table(int method) {
     }
   };
   switch (method) {
+    case EXPLICIT: set(1, {{1.}}); break;  // treelevel_explicit.f90: calc_rhs, then U += residu
     case RK2: set(2, {{.5}, {0., 1.}}); break;
     case RK2SSP: set(2, {{1.}, {.5, .5}}); break;
     case RK3SSP: set(3, {{1.}, {.25, .25}, {1. / 6., 1. / 6., 4. / 6.}}); break;
@@ -854,6 +855,25 @@ void Solver::face_fluxes() {
         const double cl_ = sr / (sr - sl), cr_ = -sl / (sr - sl);
         for (int k = 0; k < 25; ++k) { jacL[25 * (size_t)f + k] = cl_ * JL[k]; jacR[25 * (size_t)f + k] = cr_ * JR[k]; }
       }
+    } else if (sp.scheme == SCH_AUSMM) {  // calc_flux_ausmm.f90:62-118 (no Jacobian in Typhon)
+      const double gig1 = g / (g - 1.0);
+      const double al = std::sqrt(g * L.p / L.rho), ar = std::sqrt(g * R.p / R.rho);
+      const double mnl = dot(L.u, fn) / al, mnr = dot(R.u, fn) / ar;
+      double mp, pp, mm, pm;
+      if (mnl >= 1.0) { mp = mnl; pp = 1.0; }
+      else if (mnl <= -1.0) { mp = 0.0; pp = 0.0; }
+      else { mp = .25 * ((mnl + 1.0) * (mnl + 1.0)); pp = mp * (2.0 - mnl); }
+      if (mnr <= -1.0) { mm = mnr; pm = 1.0; }
+      else if (mnr >= 1.0) { mm = 0.0; pm = 0.0; }
+      else { mm = -.25 * ((mnr - 1.0) * (mnr - 1.0)); pm = -mm * (2.0 + mnr); }
+      const double ms = mp + mm;
+      const double wl = al * std::max(0.0, ms), wr = ar * std::min(0.0, ms);
+      const double rhl = gig1 * L.p + .5 * L.rho * sqrabs(L.u);
+      const double rhr = gig1 * R.p + .5 * R.rho * sqrabs(R.u);
+      F[0] = wl * L.rho + wr * R.rho;
+      F[1] = wl * rhl + wr * rhr;
+      V3 mo = ((wl * L.rho) * L.u + (wr * R.rho) * R.u) + (pp * L.p + pm * R.p) * fn;
+      F[2] = mo.x; F[3] = mo.y; F[4] = mo.z;
     } else if (sp.scheme == SCH_RUSANOV) {  // calc_flux_rusanov.f90:57-83
       double vnl = dot(L.u, fn), vnr = dot(R.u, fn);
       double al = std::sqrt(g * L.p / L.rho), ar = std::sqrt(g * R.p / R.rho);
@@ -1431,6 +1451,7 @@ void Solver::rk_step(double dt) {
 
 void ns_typhon_steady(Solver& s, const NsSteadyParams& p, NsSteadyOut& out) {
   const UMesh* m = s.m;
+  if (p.rk_method >= 0) s.rk = rk_table(p.rk_method);
   const int nc = m->ncell, nci = m->ncell_int, nf = m->nface;
   // calc_refcons.f90 + define_refcons (MENU_SOLVER.f90:260-275)
   double ref0 = 0.0, ref1 = 0.0, totvol = 0.0;
@@ -1455,7 +1476,12 @@ void ns_typhon_steady(Solver& s, const NsSteadyParams& p, NsSteadyOut& out) {
       ++iters;
       double cfl = p.cfl * std::max(1.0, 1.0 - std::log10(z_cur / z_ref) - std::log10(wcur_res / wres_ref));
       cfl = std::min(cfl, p.cfl_max);
-      s.implicit_step(cfl, false, nullptr);
+      if (p.rk_method >= 0) {  // explicit: global stability time step (calc_zonetimestep.f90:93-106)
+        s.cfl = cfl;
+        s.rk_step(s.timestep());
+      } else {
+        s.implicit_step(cfl, false, nullptr);
+      }
       // update_field.f90:45-60: scalars rho, rho E, then the momentum vector cell by cell
       double a = 0.0, b = 0.0;
       for (int c = 0; c < nci; ++c) a = a + std::fabs(s.residu[c]);

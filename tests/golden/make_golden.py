@@ -6,7 +6,8 @@ below, or pass it as the first argument).  It copies, unchanged:
 * the XBIN/TYPHON meshes of NRG/COMMON that the cases use (``*.tym``) and the CGNS
   (ADF) meshes of the implicit and heat-conduction cases (``*.cgns``);
 * the monitor files written by Typhon for those cases (``*.tmon``, residual histories
-  ``monres.*``, boundary histories ``histo*``), renamed ``<case>__<file>``.
+  ``monres.*``, boundary histories ``histo*``) and one VTK output file, renamed
+  ``<case>__<file>``.
 
 The copies are committed so that the tests never read the reference at run time.
 """
@@ -18,7 +19,7 @@ REF = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
 HERE = pathlib.Path(__file__).resolve().parent
 
 MESHES = ["quad20x20.tym", "quad20x10.tym", "quad10x10.tym", "tri5x10.tym", "mxlay2x20quad-h50.tym",
-          "tube.cgns", "square-quad10.cgns", "rect4x1.cgns"]
+          "tube.cgns", "square-quad10.cgns", "rect4x1.cgns", "expansion-10.cgns"]
 CASES = {
     "RK2": "NRG/TIME/RUNGEKUTTA/RK2/RHOERR.tmon",
     "RK2-SSP": "NRG/TIME/RUNGEKUTTA/RK2-SSP/RHOERR.tmon",
@@ -39,6 +40,12 @@ CASES = {
     "KDIF-ISOTH-BICG": ["NRG/KDIF/ISOTH-BICG/monres.001", "NRG/KDIF/ISOTH-BICG/Average_T.tmon"],
     "IMPLICIT-GMRES": ["NRG/TIME/IMPLICIT/GMRES/histofluxNS_RIGHT", "NRG/TIME/IMPLICIT/GMRES/histovarNS_RIGHT"],
     "IMPLICIT-BICGSTAB-RUSANOV": ["NRG/TIME/IMPLICIT/BICGSTAB-RUSANOV/histovarNS_DOWN"],
+    "HLLC-MUSCL": "NRG/NS/NUM/HRES/MUSCL/HLLC-MUSCL/monres.001",
+    "AUSM-MUSCLFAST": ["NRG/NS/NUM/HRES/MUSCL/AUSM-MUSCLFAST/monres.001",
+                       "NRG/NS/NUM/HRES/MUSCL/AUSM-MUSCLFAST/typhonNS.vtk"],
+    "AUSM-MUSCLUNS": ["NRG/NS/NUM/HRES/MUSCL/AUSM-MUSCLUNS/MAXV.tmon",
+                      "NRG/NS/NUM/HRES/MUSCL/AUSM-MUSCLUNS/MINP.tmon",
+                      "NRG/NS/NUM/HRES/MUSCL/AUSM-MUSCLUNS/VCOMP.tmon"],
 }
 
 def main():

@@ -15,13 +15,13 @@ LIB = ROOT / "oracle" / "build" / "liboracle.so"
 # enums of oracle/oracle.hpp
 BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD, BC_NOSLIP, BC_HEAT = 1, 2, 3, 4, 5, 6
 BC_INLET_SUB, BC_OUTLET_SUB, BC_INLET_SUP, BC_OUTLET_SUP = 7, 8, 9, 10
-SCH_HLLC, SCH_RUSANOV, SCH_ROE, SCH_HLLE = 1, 2, 3, 5
+SCH_HLLC, SCH_RUSANOV, SCH_ROE, SCH_AUSMM, SCH_HLLE = 1, 2, 3, 4, 5
 HRES_NONE, HRES_MUSCL, HRES_MUSCLFAST, HRES_MUSCLUNS = 0, 1, 2, 3
 LIM_NONE, LIM_MINMOD, LIM_ALBADA, LIM_VLEER, LIM_SBEE, LIM_KIM3, LIM_LIM03 = range(7)
 POSTLIM_NONE, POSTLIM_BARTH, POSTLIM_SUPERBARTH = 0, 1, 2
 GRAD_NONE, GRAD_LSQ, GRAD_LSQW = 0, 1, 2
 VISC_NONE, VISC_CELLAVG, VISC_CELLFULL = 0, 1, 2
-RK = {"RK2": 1, "RK2-SSP": 2, "RK3-SSP": 3, "RK4": 4, "RK25BB": 5, "RK26BB": 6, "RK12BS": 7, "RK13BS": 8}
+RK = {"EXPLICIT": 0, "RK2": 1, "RK2-SSP": 2, "RK3-SSP": 3, "RK4": 4, "RK25BB": 5, "RK26BB": 6, "RK12BS": 7, "RK13BS": 8}
 
 _lib = None
 
@@ -230,13 +230,13 @@ class Solver:
         self.lib.ory_solver_set_inversion(self.h, {"GMRES": 0, "BICGSTAB": 1}[name])
 
     def typhon_steady(self, cfl, cfl_max=None, cycle_res=0.1, global_res=1e-4, nkrylov=50, max_it=50,
-                      inv_res=1e-4, history_faces=(), max_iters=100000, max_cycles=1000):
-        """Typhon's steady implicit run from the current state: log10 residual per iteration,
-        per cycle the flux sums (F S) and S-weighted ghost primitive averages over
-        history_faces, and the iteration count at each cycle's end."""
+                      inv_res=1e-4, history_faces=(), max_iters=100000, max_cycles=1000, method="IMPLICIT"):
+        """Typhon's steady run from the current state (implicit, or an explicit method of RK):
+        log10 residual per iteration, per cycle the flux sums (F S) and S-weighted ghost
+        primitive averages over history_faces, and the iteration count at each cycle's end."""
         cap = max_iters + 1
         dp = np.array([cfl, cfl if cfl_max is None else cfl_max, cycle_res, global_res, inv_res], np.float64)
-        ip = np.array([nkrylov, max_it, max_iters, max_cycles], np.int32)
+        ip = np.array([nkrylov, max_it, max_iters, max_cycles, -1 if method == "IMPLICIT" else RK[method]], np.int32)
         hist = np.ascontiguousarray(history_faces, np.int32)
         lr, fs, ga, end = np.zeros(cap), np.zeros(5 * cap), np.zeros(5 * cap), np.zeros(cap, np.int32)
         nc = C.c_int()

@@ -1,0 +1,101 @@
+"""Typhon's steady explicit MUSCL runs on the GPU (expansion-10.cgns, NRG/NS/NUM/HRES/MUSCL).
+
+Grid.ns_steady(method="EXPLICIT") runs the forward-Euler steady driver through
+ty_steady_iteration: the residual history equals Typhon's monres.001 at every iteration
+(1e-10 in log10) and stops at the same iteration, and the state stays bit-identical to the
+oracle's in exact mode (within 1e-12 in fast mode).  From the final state Grid.write_vtk
+writes Typhon's typhonNS.vtk byte for byte and Grid.probe gives the MINP / MAXV / VCOMP
+probes of AUSM-MUSCLUNS as printed.  The AUSM-M flux has no Jacobian in Typhon: an implicit step
+with it is refused.
+"""
+import numpy as np
+import pytest
+
+import oracle_py as op
+from test_explicit_steady_golden import BCS, CASES, GAMMA, RGAS, init_state, oracle_case
+
+pytestmark = pytest.mark.gpu
+
+NAMES = {op.SCH_HLLC: "HLLC", op.SCH_AUSMM: "AUSMM"}
+HRES = {op.HRES_MUSCL: "MUSCL", op.HRES_MUSCLFAST: "MUSCL-FAST", op.HRES_MUSCLUNS: "MUSCL-UNS"}
+LIM = {op.LIM_VLEER: "VANLEER", op.LIM_ALBADA: "ALBADA"}
+
+
+@pytest.fixture(scope="module")
+def ty():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from typhon_gb300 import build
+    build.build()
+    import typhon_gb300
+    return typhon_gb300
+
+
+def gpu_case(ty, golden_dir, name, mode):
+    from typhon_gb300 import cgns
+    raw = cgns.read_cgns(golden_dir / "expansion-10.cgns")
+    md = ty.preprocess(raw, 2, [(f, k, "", (0.0, 0.0, 0.0)) for f, k, _ in BCS])
+    sch, hres, lim, res = CASES[name]
+    g = ty.Grid(md)
+    g.set_spat(NAMES[sch], HRES[hres], LIM[lim], gradmeth="LSQ", mode=mode, gamma=GAMMA, rgas=RGAS)
+    g.set_boundary_params({f: d for f, _, d in BCS if d})
+    rho, p, u = init_state(1e5, 300.0, 2.0)
+    prim = np.zeros((5, md.ncell))
+    prim[0], prim[1], prim[2] = rho, p, u
+    g.set_prim(prim)
+    out = g.ns_steady(1.0, 1.0, cycle_res=res, global_res=res, method="EXPLICIT", max_iters=20000)
+    return raw, md, g, out
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+@pytest.mark.parametrize("name,niter", [("HLLC-MUSCL", 152), ("AUSM-MUSCLFAST", 159)])
+def test_gpu_reproduces_monres(ty, golden_dir, name, niter, mode):
+    raw, md, g, out = gpu_case(ty, golden_dir, name, mode)
+    gold = np.loadtxt(golden_dir / f"{name}__monres.001")
+    assert len(out["log_res"]) == niter and list(out["cycle_end"]) == [niter]
+    assert np.abs(out["log_res"] - gold[:, 1]).max() < 1e-10
+    _, om, s, _, _ = oracle_case(golden_dir, name)
+    U, Uo = g.get_cons(), s.get("cons")[:, :md.ncell_int]
+    if mode == "exact":
+        assert np.array_equal(U, Uo)
+    else:
+        for v in range(5):
+            assert np.abs(U[v] - Uo[v]).max() <= 1e-12 * np.abs(Uo[v]).max(), v
+    g.close()
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+@pytest.mark.parametrize("binary", [False, True])
+def test_gpu_vtk_output(ty, golden_dir, tmp_path, mode, binary):
+    raw, md, g, out = gpu_case(ty, golden_dir, "AUSM-MUSCLFAST", mode)
+    path = tmp_path / "typhonNS.vtk"
+    g.write_vtk(path, raw, binary=binary)
+    if not binary:
+        assert path.read_bytes() == (golden_dir / "AUSM-MUSCLFAST__typhonNS.vtk").read_bytes()
+    else:
+        from typhon_gb300 import vtk
+        ref = tmp_path / "ref.vtk"
+        q = g.get_prim()
+        vtk.write_vtk(ref, raw, scalars=[("RHO", q[0]), ("PS", q[1])], vectors=[("V", q[2:5])], binary=True)
+        assert path.read_bytes() == ref.read_bytes()
+    g.close()
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+def test_gpu_probes(ty, golden_dir, mode):
+    raw, md, g, out = gpu_case(ty, golden_dir, "AUSM-MUSCLUNS", mode)
+    assert list(out["cycle_end"]) == [461]
+    for name, kind, expr in (("MINP", "VOL_MIN", "sqrt(PS)"), ("MAXV", "VOL_MAX", "V"),
+                             ("VCOMP", "VOL_AVERAGE", "V_Y-V_X")):
+        gold = float(open(golden_dir / f"AUSM-MUSCLUNS__{name}.tmon").read().split()[2])
+        assert "%.7E" % g.probe(kind, expr) == "%.7E" % gold, name
+    g.close()
+
+
+def test_ausmm_has_no_implicit_step(ty, golden_dir):
+    raw, md, g, out = gpu_case(ty, golden_dir, "HLLC-MUSCL", "exact")
+    g.set_spat("AUSMM", "MUSCL-FAST", "ALBADA", gradmeth="LSQ", gamma=GAMMA, rgas=RGAS)
+    with pytest.raises(ty.TyphonError):
+        g.implicit_step(1.0, "GMRES")
+    g.close()

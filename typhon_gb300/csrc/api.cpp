@@ -48,6 +48,7 @@ bool rk_table(int method, RkTab& t) {
     for (double x : v) t.c[i][j++] = x;
   };
   switch (method) {
+    case TY_RK_EXPLICIT: t.n = 1; row(0, {1.}); break;  // treelevel_explicit.f90: U += residu
     case TY_RK2: t.n = 2; row(0, {.5}); row(1, {0., 1.}); break;
     case TY_RK2SSP: t.n = 2; row(0, {1.}); row(1, {.5, .5}); break;
     case TY_RK3SSP: t.n = 3; row(0, {1.}); row(1, {.25, .25}); row(2, {1. / 6., 1. / 6., 4. / 6.}); break;
@@ -343,9 +344,10 @@ int ensure_pk(ty_mesh* h, const RkStagePlan* plans, int n) {
 // one RK step; dt either host value or device slot dtbits_cur.  dtbits_next: where the
 // final stage writes the next step's stability time step (or null).
 int run_step(ty_mesh* h, const RkTab& t, double dt, const unsigned long long* dtbits_cur,
-             unsigned long long* dtbits_next, double cfl) {
+             unsigned long long* dtbits_next, double cfl, bool store_acc = false) {
   RkStagePlan plans[kMaxStage];
   make_plans(t, plans);
+  plans[t.n - 1].store_acc = store_acc ? 1 : 0;
   int rc = ensure_pk(h, plans, t.n);
   if (rc) return rc;
   rc = ensure_prim(h);
@@ -567,7 +569,7 @@ int ty_set_bc_data(ty_mesh* h, const double* data) {
 
 int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
   if (!h || !p) return TY_ERR_ARG;
-  if (p->scheme < TY_SCH_HLLC || p->scheme > TY_SCH_HLLE || p->scheme == 4 || p->highres < 0 || p->highres > TY_HRES_MUSCLUNS ||
+  if (p->scheme < TY_SCH_HLLC || p->scheme > TY_SCH_HLLE || p->highres < 0 || p->highres > TY_HRES_MUSCLUNS ||
       p->limiter < 0 || p->limiter > TY_LIM_LIM03 || p->postlim < 0 || p->postlim > TY_POSTLIM_SUPERBARTH ||
       p->gradmeth < 0 || p->gradmeth > TY_GRAD_LSQW || (p->mode != TY_MODE_EXACT && p->mode != TY_MODE_FAST) ||
       !(p->gamma > 1.0)) {
@@ -736,6 +738,30 @@ int ty_rk_steps(ty_mesh* h, int32_t method, double cfl, int32_t nsteps, double* 
     TY_CU(cudaMemcpyAsync(&b, h->s.dtbits + ((nsteps - 1) & 1), 8, cudaMemcpyDeviceToHost, h->stream));
     TY_CU(cudaStreamSynchronize(h->stream));
     std::memcpy(dt_last, &b, 8);
+  }
+  TY_CU(cudaStreamSynchronize(h->stream));
+  return check_err(h);
+}
+
+int ty_steady_iteration(ty_mesh* h, int32_t method, double cfl, double* dt_out, double* res_l1) {
+  int rc = ready(h);
+  if (rc) return rc;
+  RkTab t;
+  if (!rk_table(method, t) || !(cfl > 0.0) || !res_l1) return TY_ERR_ARG;
+  if (!h->steady_red && (rc = h->alloc(h->steady_red, 3 * (size_t)tyk::kRedBlocks + 3))) return rc;
+  if ((rc = set_dt_slot(h, 0, 1.7976931348623157e308))) return rc;
+  cudaError_t e = MODE_CALL(h, timestep, h->m, h->s, h->o, h->s.u0, cfl, h->s.dtbits, h->stream, &h->prof);
+  if (e != cudaSuccess) return cuda_fail(e, "timestep");
+  if ((rc = run_step(h, t, 0.0, h->s.dtbits, nullptr, cfl, true))) return rc;
+  double* out = h->steady_red + 3 * (size_t)tyk::kRedBlocks;
+  e = MODE_CALL(h, res_l1, h->m.nci, h->s.acc, (size_t)h->m.ldc, h->steady_red, out, h->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "residual sums");
+  TY_CU(cudaMemcpyAsync(res_l1, out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (dt_out) {
+    unsigned long long b;
+    TY_CU(cudaMemcpyAsync(&b, h->s.dtbits, 8, cudaMemcpyDeviceToHost, h->stream));
+    TY_CU(cudaStreamSynchronize(h->stream));
+    std::memcpy(dt_out, &b, 8);
   }
   TY_CU(cudaStreamSynchronize(h->stream));
   return check_err(h);

@@ -98,6 +98,7 @@ struct RkStagePlan {
   double c_acc = 0;
   int final_stage = 0;  // 1: u0 <- u0 + acc
   int has_acc = 1;
+  int store_acc = 0;    // final stage: also store acc (the residual of update_field)
 };
 
 // Kernel identifiers for the per-kernel timing of ty_profile_read.

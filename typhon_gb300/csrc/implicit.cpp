@@ -496,6 +496,10 @@ int ty_implicit_step(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
     tyi::set_error("ty_imp_params: option out of range (GMRES: nkrylov <= 64, FP64; FGMRES/JFNK: nkrylov <= 32)");
     return TY_ERR_ARG;
   }
+  if (h->o.scheme == TY_SCH_AUSMM) {  // calc_flux_ausmm.f90:121-137: no AUSM-M Jacobian in Typhon
+    tyi::set_error("ty_implicit_step: the AUSM-M flux has no Jacobian");
+    return TY_ERR_UNSUPPORTED;
+  }
   std::memset(st, 0, sizeof(*st));
   int rc;
   if ((rc = ensure_buffers(h, p))) return rc;

@@ -943,6 +943,35 @@ cudaError_t imp_dot(const double* a, const double* b, size_t n, double* part, do
   return cudaGetLastError();
 }
 
+// update_field.f90:45-60's residual terms of an explicit step: per block the sums over its
+// interior cells of |acc_rho|, |acc_rhoE| and |acc_m| (acc: the step's combination of stage
+// residuals, [5][ld])
+__global__ void __launch_bounds__(kRedThreads) k_res_l1(int nci, const double* __restrict__ acc, size_t ld,
+                                                         double* __restrict__ part) {
+  double a = 0.0, b = 0.0, q = 0.0;
+  for (int c = blockIdx.x * kRedThreads + threadIdx.x; c < nci; c += gridDim.x * kRedThreads) {
+    a += fabs(acc[c]);
+    b += fabs(acc[ld + c]);
+    const double mx = acc[2 * ld + c], my = acc[3 * ld + c], mz = acc[4 * ld + c];
+    q += sqrt(mx * mx + my * my + mz * mz);
+  }
+  a = block_sum(a);
+  b = block_sum(b);
+  q = block_sum(q);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = a;
+    part[kRedBlocks + blockIdx.x] = b;
+    part[2 * kRedBlocks + blockIdx.x] = q;
+  }
+}
+
+cudaError_t res_l1(int nci, const double* acc, size_t ld, double* part, double* out, cudaStream_t st) {
+  const unsigned g = red_grid((size_t)nci);
+  k_res_l1<<<g, kRedThreads, 0, st>>>(nci, acc, ld, part);
+  k_red_final<<<3, kRedThreads, 0, st>>>(part, (int)g, kRedBlocks, out);
+  return cudaGetLastError();
+}
+
 cudaError_t imp_asum(const double* a, size_t n, double* part, double* out, cudaStream_t st) {
   const unsigned g = red_grid(n);
   k_red_part<<<g, kRedThreads, 0, st>>>(a, nullptr, n, 1, part);

@@ -89,6 +89,7 @@ struct ImpArgs {
   cudaError_t imp_dot(const double* a, const double* b, size_t n, double* part, double* out,              \
                       cudaStream_t st);                                                                 \
   cudaError_t imp_asum(const double* a, size_t n, double* part, double* out, cudaStream_t st);           \
+  cudaError_t res_l1(int nci, const double* acc, size_t ld, double* part, double* out, cudaStream_t st);  \
   cudaError_t imp_mgs_pass(const double* vprev, const double* hprev, double* w, const double* vnext,    \
                            size_t n, double* part, double* out, cudaStream_t st);                        \
   cudaError_t imp_basis_pass(double* V, float* V32, size_t ldv, int nv, const double* c,                \

@@ -466,6 +466,31 @@ __device__ void flux_hlle(double g, const double* L, const double* R, double nx,
   F[3] = ml * L[3] + mr * R[3] + pp * ny;
   F[4] = ml * L[4] + mr * R[4] + pp * nz;
 }
+// calc_flux_ausmm.f90:62-118: AUSM-M, van Leer's Mach and pressure splittings (no Jacobian)
+__device__ void flux_ausmm(double g, const double* L, const double* R, double nx, double ny, double nz, double* F) {
+  const double gig1 = g / (g - 1.0);
+  const double al = sqrt(g * L[1] / L[0]);
+  const double ar = sqrt(g * R[1] / R[0]);
+  const double mnl = (L[2] * nx + L[3] * ny + L[4] * nz) / al;
+  const double mnr = (R[2] * nx + R[3] * ny + R[4] * nz) / ar;
+  double mp, pp, mm, pm;
+  if (mnl >= 1.0) { mp = mnl; pp = 1.0; }
+  else if (mnl <= -1.0) { mp = 0.0; pp = 0.0; }
+  else { mp = .25 * ((mnl + 1.0) * (mnl + 1.0)); pp = mp * (2.0 - mnl); }
+  if (mnr <= -1.0) { mm = mnr; pm = 1.0; }
+  else if (mnr >= 1.0) { mm = 0.0; pm = 0.0; }
+  else { mm = -(.25 * ((mnr - 1.0) * (mnr - 1.0))); pm = -mm * (2.0 + mnr); }
+  const double ms = mp + mm;
+  const double wl = al * fmax(0.0, ms), wr = ar * fmin(0.0, ms);
+  const double rhl = gig1 * L[1] + .5 * L[0] * (L[2] * L[2] + L[3] * L[3] + L[4] * L[4]);
+  const double rhr = gig1 * R[1] + .5 * R[0] * (R[2] * R[2] + R[3] * R[3] + R[4] * R[4]);
+  F[0] = wl * L[0] + wr * R[0];
+  F[1] = wl * rhl + wr * rhr;
+  const double ml = wl * L[0], mr = wr * R[0], pf = pp * L[1] + pm * R[1];
+  F[2] = ml * L[2] + mr * R[2] + pf * nx;
+  F[3] = ml * L[3] + mr * R[3] + pf * ny;
+  F[4] = ml * L[4] + mr * R[4] + pf * nz;
+}
 __device__ void flux_hllc(double g, const double* L, const double* R, double nx, double ny, double nz, double* F) {
   const double ig1 = 1.0 / (g - 1.0);
   const double gig1 = g / (g - 1.0);
@@ -795,6 +820,7 @@ __device__ __forceinline__ void face_flux_fast(const DevMesh& m, const DevState&
     if (o.scheme == TY_SCH_ROE) flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, 1.0, F);
     else if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_HLLE) flux_hlle(o.gamma, QL, QR, nx, ny, nz, F);
+    else if (o.scheme == TY_SCH_AUSMM) flux_ausmm(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
     if (o.viscous != TY_VISC_NONE) add_viscous(m, s, o, f, F);
 #pragma unroll
@@ -813,11 +839,13 @@ __device__ __forceinline__ void face_flux(const DevMesh& m, const DevState& s, c
     if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_HLLE) flux_hlle(o.gamma, QL, QR, nx, ny, nz, F);
+    else if (o.scheme == TY_SCH_AUSMM) flux_ausmm(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, 1.0, F);  // unit surface
   } else {
     if (o.scheme == TY_SCH_HLLC) flux_hllc(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_HLLE) flux_hlle(o.gamma, QL, QR, nx, ny, nz, F);
+    else if (o.scheme == TY_SCH_AUSMM) flux_ausmm(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_roe(o.gamma, o.entropy_fix, QL, QR, nx, ny, nz, F);
   }
   if (o.viscous != TY_VISC_NONE) add_viscous(m, s, o, f, F);
@@ -1225,7 +1253,7 @@ __global__ void __launch_bounds__(kBlock) k_rk_update(DevMesh m, DevState s, RkS
       for (int v = 0; v < 5; ++v) {
         double a = plan.acc_init ? plan.c_acc * R[v] : s.acc[v * ld + c] + plan.c_acc * R[v];
         if (plan.final_stage) next[v] = u0[v] + a;
-        else s.acc[v * ld + c] = a;
+        if (!plan.final_stage || plan.store_acc) s.acc[v * ld + c] = a;
       }
       if (plan.final_stage) have_next = true;
     }

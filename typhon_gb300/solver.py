@@ -21,13 +21,13 @@ from .umesh import MeshDesc
 
 # option names as in Typhon's SPAT_PARAM / TIME_PARAM blocks (SOURCE/PARAM/def_spat.f90,
 # def_time.f90) -> C ABI enum values
-SCHEME = {"HLLC": 1, "RUSANOV": 2, "ROE": 3, "HLLE": 5, "HLL": 5}
+SCHEME = {"HLLC": 1, "RUSANOV": 2, "ROE": 3, "AUSMM": 4, "HLLE": 5, "HLL": 5}
 HIGHRES = {"NONE": 0, "MUSCL": 1, "MUSCL-FAST": 2, "MUSCL-UNS": 3}
 LIMITER = {"NONE": 0, "MINMOD": 1, "ALBADA": 2, "VAN_ALBADA": 2, "VAN_LEER": 3, "VANLEER": 3, "SUPERBEE": 4,
            "KIM3": 5, "LIM03": 6}
 POSTLIM = {"NONE": 0, "BARTH": 1, "SUPERBARTH": 2}
 GRADMETH = {"NONE": 0, "LSQ": 1, "W-LSQ": 2}
-RK_METHOD = {"RK2": 1, "RK2-SSP": 2, "RK3-SSP": 3, "RK4": 4, "RK25BB": 5, "RK26BB": 6, "RK12BS": 7, "RK13BS": 8}
+RK_METHOD = {"EXPLICIT": 0, "RK2": 1, "RK2-SSP": 2, "RK3-SSP": 3, "RK4": 4, "RK25BB": 5, "RK26BB": 6, "RK12BS": 7, "RK13BS": 8}
 MODE = {"exact": 0, "fast": 1}
 DISSIPATIVE_FLUX = {"NONE": 0, "CELL-AVERAGE": 1, "FULL": 2}
 VISC_LAW = {"KINEMATIC-CONSTANT": 0, "SUTHERLAND": 1}
@@ -135,6 +135,23 @@ class Grid:
         _capi.check(self.lib.ty_prim_download(self.h, out.ctypes.data), "ty_prim_download")
         return out
 
+    def probe(self, kind, quantity, time=0.0):
+        """A volume probe of the resident state (BLOCK:PROBE, TYPE = VOL_MIN | VOL_MAX |
+        VOL_AVERAGE, QUANTITY an expression of RHO, PS, V, V_X, V_Y, V_Z, x, y, z, t;
+        PROBECALC.f90:22-212) over the interior cells."""
+        from . import probes
+        m = self.mesh
+        env = probes.ns_environment(self.get_prim(), m.cell_centre[:self.nci], time)
+        return probes.vol_probe(kind, quantity, env, m.cell_volume[:self.nci])
+
+    def write_vtk(self, path, raw, binary=False):
+        """The resident state as Typhon's OUTPUT FORMAT = VTK | VTK-BIN file
+        (output_zone.f90): the mesh `raw` (the RawMesh this grid was preprocessed from) and
+        the primitive fields RHO, PS, V of the interior cells, downloaded from the device."""
+        from . import vtk
+        q = self.get_prim()
+        vtk.write_vtk(path, raw, scalars=[("RHO", q[0]), ("PS", q[1])], vectors=[("V", q[2:5])], binary=binary)
+
     def set_cons_device(self, ptr):
         _capi.check(self.lib.ty_state_upload_device(self.h, C.c_void_p(ptr)), "ty_state_upload_device")
 
@@ -207,15 +224,18 @@ class Grid:
 
     def ns_steady(self, cfl, cfl_max=None, cycle_res=0.1, global_res=1e-4, inversion="GMRES", nkrylov=50,
                   max_it=50, inv_res=1e-4, precision="fp64", history=None, max_iters=100000, max_cycles=1000,
-                  cycle_max_it=None):
-        """Typhon's steady implicit run of one zone from the resident state (integration.f90,
+                  cycle_max_it=None, method="IMPLICIT"):
+        """Typhon's steady run of one zone from the resident state (integration.f90,
         integration_cycle.f90, integration_cyclezone.f90, check_end_cycle.f90; the CFL law of
         calc_zonetimestep.f90, cfl (1 - log10 of the zone's and the world's residual drops,
         at least 1) capped at cfl_max; the residual of update_field.f90 with the reference
-        state of calc_refcons.f90).  history: a family whose summed face fluxes F S after each
-        cycle are returned (integ_ustboco.f90's QUANTITY-FLUX history: mass, energy,
-        momentum).  Each iteration is one implicit_step on the GPU; three scalars per
-        iteration come back to the host.  Returns dict(log_res, cycle_end, flux)."""
+        state of calc_refcons.f90).  method: IMPLICIT (TIME_PARAM METHOD = IMPLICIT, one
+        implicit_step per iteration with inversion / nkrylov / max_it / inv_res / precision)
+        or an explicit method (EXPLICIT, RK2, ..., one ty_steady_iteration: global stability
+        time step, one step, the update's residual sums).  history: a family whose summed
+        face fluxes F S after each cycle are returned (integ_ustboco.f90's QUANTITY-FLUX
+        history: mass, energy, momentum).  Three scalars per iteration come back to the host.
+        Returns dict(log_res, cycle_end, flux)."""
         m, nci = self.mesh, self.nci
         V = m.cell_volume[:nci]
         U = self.get_cons()[:, :nci]
@@ -227,6 +247,7 @@ class Grid:
         cfl_max = cfl if cfl_max is None else cfl_max
         w_ref, w_cur, z_reforig = 1.0, 1.0, None
         log_res, cycle_end, flux = [], [], []
+        res3 = np.zeros(3)
         iters = 0
         for icycle in range(1, max_cycles + 1):
             wcur_res, wres_ref = w_cur, w_ref
@@ -238,9 +259,15 @@ class Grid:
                 it_loc += 1
                 iters += 1
                 c = cfl * max(1.0, 1.0 - np.log10(z_cur / z_ref) - np.log10(wcur_res / wres_ref))
-                st = self.implicit_step(min(c, cfl_max), inversion=inversion, nkrylov=nkrylov, max_it=max_it,
-                                        inv_res=inv_res, precision=precision)
-                z_cur = st["du_l1"][0] / ref0 + st["du_l1"][1] / ref1 + st["du_mom"] / refv
+                if method == "IMPLICIT":
+                    st = self.implicit_step(min(c, cfl_max), inversion=inversion, nkrylov=nkrylov, max_it=max_it,
+                                            inv_res=inv_res, precision=precision)
+                    z_cur = st["du_l1"][0] / ref0 + st["du_l1"][1] / ref1 + st["du_mom"] / refv
+                else:
+                    dt = C.c_double()
+                    _capi.check(self.lib.ty_steady_iteration(self.h, RK_METHOD[method], float(min(c, cfl_max)),
+                                                             C.byref(dt), res3.ctypes.data), "ty_steady_iteration")
+                    z_cur = res3[0] / ref0 + res3[1] / ref1 + res3[2] / refv
                 z_ref = max(z_ref, z_cur)
                 log_res.append(np.log10(z_cur))
                 if z_cur / z_ref <= cycle_res or it_loc == maxit:
@@ -294,6 +321,11 @@ class Grid:
         out = np.zeros(self.nci)
         _capi.check(self.lib.ty_kdif_get_temperature(self.h, out.ctypes.data), "ty_kdif_get_temperature")
         return out
+
+    def kdif_write_vtk(self, path, raw, binary=False):
+        """The resident temperature as Typhon's VTK output of a heat-conduction zone (TS)."""
+        from . import vtk
+        vtk.write_vtk(path, raw, scalars=[("TS", self.kdif_temperature())], binary=binary)
 
     def kdif_residual(self, dt):
         R = np.zeros(self.nci)
