@@ -41,6 +41,9 @@ CASES = {
     "IMPLICIT-GMRES": ["NRG/TIME/IMPLICIT/GMRES/histofluxNS_RIGHT", "NRG/TIME/IMPLICIT/GMRES/histovarNS_RIGHT"],
     "IMPLICIT-BICGSTAB-RUSANOV": ["NRG/TIME/IMPLICIT/BICGSTAB-RUSANOV/histovarNS_DOWN"],
     "HLLC-MUSCL": "NRG/NS/NUM/HRES/MUSCL/HLLC-MUSCL/monres.001",
+    "HLLC-MUSCLUNS": "NRG/NS/NUM/FLUX/HLLC-MUSCLUNS/monres.001",
+    "HLLC-MPI": "NRG/NS/HLLC-MPI/monres.001",
+    "HLLE-EXPLICIT": ["NRG/NS/NUM/FLUX/HLLE/histofluxNS_RIGHT", "NRG/NS/NUM/FLUX/HLLE/histovarNS_RIGHT"],
     "AUSM-MUSCLFAST": ["NRG/NS/NUM/HRES/MUSCL/AUSM-MUSCLFAST/monres.001",
                        "NRG/NS/NUM/HRES/MUSCL/AUSM-MUSCLFAST/typhonNS.vtk"],
     "AUSM-MUSCLUNS": ["NRG/NS/NUM/HRES/MUSCL/AUSM-MUSCLUNS/MAXV.tmon",

@@ -6,9 +6,15 @@ outlet; symmetry walls), started from Pi 1e5, Ti 300, Mach 2; TIME = STEADY with
 default METHOD = EXPLICIT (forward Euler) and global stability time step at CFL 1; least-
 squares gradients.
 
-* HLLC-MUSCL (HLLC, MUSCL, van Leer) and AUSM-MUSCLFAST (AUSM-M, MUSCL-FAST, van Albada):
-  the oracle's residual history equals monres.001 (every iteration, 15 printed digits, to
-  1e-10 in log10) and ends at the same iteration.
+* HLLC-MUSCL (HLLC, MUSCL, van Leer), AUSM-MUSCLFAST (AUSM-M, MUSCL-FAST, van Albada),
+  NS/NUM/FLUX/HLLC-MUSCLUNS (HLLC, MUSCL-UNS, van Leer, to 1e-3) and NS/HLLC-MPI (HLLC,
+  first order; Typhon ran it on two MPI ranks): the oracle's residual history equals
+  monres.001 (every iteration, 15 printed digits, to 1e-10 in log10) and ends at the same
+  iteration.
+* NS/NUM/FLUX/HLLE on square-quad10.cgns (HLLE, subsonic inlets and outlet, RESIDUALS 0.3
+  per cycle, 1e-4 overall): after each of the eight cycles the outlet's summed fluxes and
+  S-weighted ghost primitive averages equal histofluxNS_RIGHT and histovarNS_RIGHT as
+  printed (six digits).
 * AUSM-MUSCLFAST's VTK output (typhonNS.vtk): the writer reproduces Typhon's file byte for
   byte from the oracle's state (mesh, cell types, RHO, PS, V).
 * AUSM-MUSCLUNS (MUSCL-UNS, run to 1e-6): the VOL_MIN of sqrt(PS), VOL_MAX of V and
@@ -29,6 +35,8 @@ Z3 = (0.0, 0.0, 0.0)
 INLET = (1e5, 400.0, 2.0, 1.0, 0.0, 0.0)        # PI, TI, MACH, DIRECTION
 BCS = [("WALL", op.BC_SYMMETRY, None), ("INLET", op.BC_INLET_SUP, INLET), ("OUTLET", op.BC_OUTLET_SUP, None)]
 CASES = {"HLLC-MUSCL": (op.SCH_HLLC, op.HRES_MUSCL, op.LIM_VLEER, 1e-2),
+         "HLLC-MUSCLUNS": (op.SCH_HLLC, op.HRES_MUSCLUNS, op.LIM_VLEER, 1e-3),
+         "HLLC-MPI": (op.SCH_HLLC, op.HRES_NONE, op.LIM_ALBADA, 1e-2),
          "AUSM-MUSCLFAST": (op.SCH_AUSMM, op.HRES_MUSCLFAST, op.LIM_ALBADA, 1e-2),
          "AUSM-MUSCLUNS": (op.SCH_AUSMM, op.HRES_MUSCLUNS, op.LIM_ALBADA, 1e-6)}
 
@@ -46,7 +54,8 @@ def oracle_case(golden_dir, name):
     ob = [(f, k, "", Z3, Z3, d) if d else (f, k, "", Z3) for f, k, d in BCS]
     om = op.Mesh.from_raw(raw).build(2, ob)
     sch, hres, lim, res = CASES[name]
-    s = op.Solver(om, sch, highres=hres, limiter=lim, gradmeth=op.GRAD_LSQ, gamma=GAMMA, rgas=RGAS, rk="EXPLICIT")
+    s = op.Solver(om, sch, highres=hres, limiter=lim, gradmeth=op.GRAD_LSQ if hres else op.GRAD_NONE, gamma=GAMMA,
+                  rgas=RGAS, rk="EXPLICIT")
     rho, p, u = init_state(1e5, 300.0, 2.0)
     prim = np.zeros((5, om.ncell))
     prim[0], prim[1], prim[2] = rho, p, u
@@ -75,7 +84,8 @@ def op_bar2():
     return ELEM_BAR2
 
 
-@pytest.mark.parametrize("name,niter", [("HLLC-MUSCL", 152), ("AUSM-MUSCLFAST", 159)])
+@pytest.mark.parametrize("name,niter", [("HLLC-MUSCL", 152), ("AUSM-MUSCLFAST", 159), ("HLLC-MUSCLUNS", 227),
+                                        ("HLLC-MPI", 174)])
 def test_oracle_reproduces_monres(golden_dir, name, niter):
     _, _, _, lr, end = oracle_case(golden_dir, name)
     gold = np.loadtxt(golden_dir / f"{name}__monres.001")
@@ -136,3 +146,33 @@ def test_probe_expressions():
     for bad in ("__import__('os')", "PS.real", "[PS]", "Q + 1"):
         with pytest.raises(probes.ProbeError):
             probes.evaluate(bad, env)
+
+
+HLLE_BCS = [("LEFT-UP", op.BC_INLET_SUB, (1.7e5, 200.0, 1.0, 0.0, 0.0)),
+            ("LEFT-DOWN", op.BC_INLET_SUB, (1.2e5, 600.0, 1.0, 0.0, 0.0)),
+            ("RIGHT", op.BC_OUTLET_SUB, (1e5,)), ("TOP", op.BC_SYMMETRY, None), ("BOTTOM", op.BC_SYMMETRY, None)]
+
+
+def read_histo(path):
+    return np.array([[float(x) for x in ln.split()[1:]] for ln in open(path) if not ln.startswith("#")])
+
+
+def test_oracle_reproduces_hlle_histories(golden_dir):
+    import typhon_gb300 as ty
+    raw = cgns.read_cgns(golden_dir / "square-quad10.cgns")
+    ob = [(f, k, "", Z3, Z3, d) if d else (f, k, "", Z3) for f, k, d in HLLE_BCS]
+    om = op.Mesh.from_raw(raw).build(2, ob)
+    md = ty.preprocess(raw, 2, [(f, k, "", Z3) for f, k, _ in HLLE_BCS])
+    s = op.Solver(om, op.SCH_HLLE, gamma=GAMMA, rgas=RGAS, rk="EXPLICIT")
+    rho, p, u = init_state(1e5, 300.0, 2.0)
+    prim = np.zeros((5, om.ncell))
+    prim[0], prim[1], prim[2] = rho, p, u
+    s.set_prim(prim)
+    lr, fs, ga, end = s.typhon_steady(1.0, 1.0, cycle_res=0.3, global_res=1e-4, method="EXPLICIT",
+                                      history_faces=md.faces_of("RIGHT"))
+    gf = read_histo(golden_dir / "HLLE-EXPLICIT__histofluxNS_RIGHT")
+    gv = read_histo(golden_dir / "HLLE-EXPLICIT__histovarNS_RIGHT")
+    assert len(end) == len(gf) == len(gv) == 8
+    for c in range(8):
+        assert ["%.5E" % v for v in fs[c]] == ["%.5E" % v for v in gf[c]], c
+        assert ["%.5E" % v for v in ga[c]] == ["%.5E" % v for v in gv[c]], c

@@ -5,14 +5,16 @@ ty_steady_iteration: the residual history equals Typhon's monres.001 at every it
 (1e-10 in log10) and stops at the same iteration, and the state stays bit-identical to the
 oracle's in exact mode (within 1e-12 in fast mode).  From the final state Grid.write_vtk
 writes Typhon's typhonNS.vtk byte for byte and Grid.probe gives the MINP / MAXV / VCOMP
-probes of AUSM-MUSCLUNS as printed.  The AUSM-M flux has no Jacobian in Typhon: an implicit step
-with it is refused.
+probes of AUSM-MUSCLUNS as printed; NS/NUM/FLUX/HLLE's outlet flux history comes out as
+printed (its histovar file, of a first-order run, reports ghost conservative states that
+accumulate the raw boundary fluxes, which only the oracle keeps).  The AUSM-M flux has no Jacobian in Typhon: an implicit step with it
+is refused.
 """
 import numpy as np
 import pytest
 
 import oracle_py as op
-from test_explicit_steady_golden import BCS, CASES, GAMMA, RGAS, init_state, oracle_case
+from test_explicit_steady_golden import BCS, CASES, GAMMA, HLLE_BCS, RGAS, init_state, oracle_case, read_histo
 
 pytestmark = pytest.mark.gpu
 
@@ -38,7 +40,8 @@ def gpu_case(ty, golden_dir, name, mode):
     md = ty.preprocess(raw, 2, [(f, k, "", (0.0, 0.0, 0.0)) for f, k, _ in BCS])
     sch, hres, lim, res = CASES[name]
     g = ty.Grid(md)
-    g.set_spat(NAMES[sch], HRES[hres], LIM[lim], gradmeth="LSQ", mode=mode, gamma=GAMMA, rgas=RGAS)
+    g.set_spat(NAMES[sch], HRES.get(hres, "NONE"), LIM[lim], gradmeth="LSQ" if hres else "NONE", mode=mode,
+               gamma=GAMMA, rgas=RGAS)
     g.set_boundary_params({f: d for f, _, d in BCS if d})
     rho, p, u = init_state(1e5, 300.0, 2.0)
     prim = np.zeros((5, md.ncell))
@@ -49,7 +52,8 @@ def gpu_case(ty, golden_dir, name, mode):
 
 
 @pytest.mark.parametrize("mode", ["exact", "fast"])
-@pytest.mark.parametrize("name,niter", [("HLLC-MUSCL", 152), ("AUSM-MUSCLFAST", 159)])
+@pytest.mark.parametrize("name,niter", [("HLLC-MUSCL", 152), ("AUSM-MUSCLFAST", 159), ("HLLC-MUSCLUNS", 227),
+                                        ("HLLC-MPI", 174)])
 def test_gpu_reproduces_monres(ty, golden_dir, name, niter, mode):
     raw, md, g, out = gpu_case(ty, golden_dir, name, mode)
     gold = np.loadtxt(golden_dir / f"{name}__monres.001")
@@ -98,4 +102,25 @@ def test_ausmm_has_no_implicit_step(ty, golden_dir):
     g.set_spat("AUSMM", "MUSCL-FAST", "ALBADA", gradmeth="LSQ", gamma=GAMMA, rgas=RGAS)
     with pytest.raises(ty.TyphonError):
         g.implicit_step(1.0, "GMRES")
+    g.close()
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+def test_gpu_hlle_histories(ty, golden_dir, mode):
+    from typhon_gb300 import cgns
+    raw = cgns.read_cgns(golden_dir / "square-quad10.cgns")
+    md = ty.preprocess(raw, 2, [(f, k, "", (0.0, 0.0, 0.0)) for f, k, _ in HLLE_BCS])
+    g = ty.Grid(md)
+    g.set_spat("HLLE", mode=mode, gamma=GAMMA, rgas=RGAS)
+    g.set_boundary_params({f: d for f, _, d in HLLE_BCS if d})
+    rho, p, u = init_state(1e5, 300.0, 2.0)
+    prim = np.zeros((5, md.ncell))
+    prim[0], prim[1], prim[2] = rho, p, u
+    g.set_prim(prim)
+    out = g.ns_steady(1.0, 1.0, cycle_res=0.3, global_res=1e-4, method="EXPLICIT", history="RIGHT")
+    gf = read_histo(golden_dir / "HLLE-EXPLICIT__histofluxNS_RIGHT")
+    gv = read_histo(golden_dir / "HLLE-EXPLICIT__histovarNS_RIGHT")
+    assert len(out["cycle_end"]) == 8 and len(gv) == 8
+    for c in range(8):
+        assert ["%.5E" % v for v in out["flux"][c]] == ["%.5E" % v for v in gf[c]], c
     g.close()

@@ -233,9 +233,14 @@ class Grid:
         implicit_step per iteration with inversion / nkrylov / max_it / inv_res / precision)
         or an explicit method (EXPLICIT, RK2, ..., one ty_steady_iteration: global stability
         time step, one step, the update's residual sums).  history: a family whose summed
-        face fluxes F S after each cycle are returned (integ_ustboco.f90's QUANTITY-FLUX
-        history: mass, energy, momentum).  Three scalars per iteration come back to the host.
-        Returns dict(log_res, cycle_end, flux)."""
+        face fluxes F S (integ_ustboco.f90's histoflux file) and the S-weighted average of
+        the ghost primitive states the fluxes were computed from after each cycle are
+        returned.  The second equals Typhon's histovar file when Typhon writes the boundary
+        states into its ghost cells (runs with gradients); in a first-order run Typhon's
+        ghost cells instead carry conservative states that accumulate the raw boundary
+        fluxes F S (flux_to_res.f90 adds them unscaled to the ghost rows, update_field.f90
+        adds those rows), which this library does not keep.  Three scalars per
+        iteration come back to the host.  Returns dict(log_res, cycle_end, flux, ghost)."""
         m, nci = self.mesh, self.nci
         V = m.cell_volume[:nci]
         U = self.get_cons()[:, :nci]
@@ -246,7 +251,7 @@ class Grid:
         tiny = np.finfo(np.float64).tiny
         cfl_max = cfl if cfl_max is None else cfl_max
         w_ref, w_cur, z_reforig = 1.0, 1.0, None
-        log_res, cycle_end, flux = [], [], []
+        log_res, cycle_end, flux, ghost = [], [], [], []
         res3 = np.zeros(3)
         iters = 0
         for icycle in range(1, max_cycles + 1):
@@ -277,11 +282,22 @@ class Grid:
             if z_cur / z_reforig >= w_cur / w_ref:
                 w_cur, w_ref = z_cur, z_reforig
             if hist is not None:
-                flux.append(self.debug("flux")[:, hist].sum(axis=1))
+                # integ_ustboco.f90: sum of F S over the family's faces, and the S-weighted
+                # average of the ghost primitive states, face by face
+                fl, q = self.debug("flux"), self.debug("prim")
+                fs, qa, area = np.zeros(5), np.zeros(5), 0.0
+                for f in hist:
+                    fs = fs + fl[:, f]
+                    qa = qa + m.face_surface[f] * q[:, m.fc2[f]]
+                for f in hist:
+                    area = area + m.face_surface[f]
+                flux.append(fs)
+                ghost.append(qa / area)
             cycle_end.append(iters)
             if w_cur / w_ref <= global_res or iters >= max_iters:
                 break
-        return dict(log_res=np.array(log_res), cycle_end=np.array(cycle_end), flux=np.array(flux))
+        return dict(log_res=np.array(log_res), cycle_end=np.array(cycle_end), flux=np.array(flux),
+                    ghost=np.array(ghost))
 
     def implicit_get(self, which):
         """Blocks and vectors of the last implicit step (row-major 5x5 blocks)."""
