@@ -336,7 +336,7 @@ def run_implicit(args):
     converged states against the FP64 assembled one."""
     import torch
     import typhon_gb300 as ty
-    from typhon_gb300 import build, cases
+    from typhon_gb300 import _capi, build, cases
     build.build()
     torch.cuda.set_device(0)
     w = cases.FFBOX
@@ -372,9 +372,23 @@ def run_implicit(args):
                 cfl = min(max(w["cfl0"] * r0 / r, w["cfl0"]), w["cfl_max"])
             g.synchronize()
             t = time.perf_counter() - t0
+            # per-kernel device time of one more step at the final CFL (CUDA events per launch)
+            nk = len(_capi.KERNEL_NAMES)
+            kms, kl = np.zeros(nk), np.zeros(nk, np.int32)
+            _capi.check(g.lib.ty_profile_enable(g.h, 1), "ty_profile_enable")
+            t1 = time.perf_counter()
+            g.implicit_step(cfl, inv, nkrylov=w["nkrylov"], max_it=w["max_it"], inv_res=w["inv_res"], local_dt=True,
+                            precision=prec)
+            g.synchronize()
+            wall = time.perf_counter() - t1
+            _capi.check(g.lib.ty_profile_read(g.h, nk, kms.ctypes.data, kl.ctypes.data), "ty_profile_read")
+            _capi.check(g.lib.ty_profile_enable(g.h, 0), "ty_profile_enable")
+            prof = {n: {"launches": int(kl[i]), "ms": round(float(kms[i]), 4)}
+                    for i, n in enumerate(_capi.KERNEL_NAMES) if kl[i] > 0}
             states[name] = g.get_cons()
             variants[name] = {"seconds": round(t, 3), "steps": steps, "matvecs": matvecs, "final_rel_residual": rel,
-                              "reached": bool(rel < w["target"])}
+                              "reached": bool(rel < w["target"]),
+                              "profiled_step": {"wall_ms": round(wall * 1e3, 3), "kernels": prof}}
             g.close()
     ref = states["fgmres_fp64"]
     for name in ("fgmres_mixed", "jfnk_fp64"):

@@ -126,7 +126,7 @@ def test_kdif_errors(ty):
         g.kdif_setup(-kc, kind, val)                 # non-positive conductivity
 
 
-def test_typhon_steady_run_reproduces_isoth_cgs(ty, golden_dir):
+def test_typhon_steady_run_reproduces_isoth_cgs(ty, golden_dir, tmp_path):
     """NRG/KDIF/ISOTH-CGS through the GPU: Typhon's steady driver (Grid.kdif_steady) over
     ty_kdif_implicit_step.  The GPU solves each step to 1e-13 where Typhon's CGS stops at
     INV_RES 1e-4: on this 10-cell system both are converged to about 1e-8 in the log10
@@ -153,6 +153,14 @@ def test_typhon_steady_run_reproduces_isoth_cgs(ty, golden_dir):
         assert list(out["cycle_end"]) == [125, 326, 527, 728, 929]
         probe = [float(ln.split()[2]) for ln in open(golden_dir / "KDIF-ISOTH-CGS__Average_T.tmon") if ln.strip()]
         assert ["%.7E" % a for a in out["cycle_avg"]] == ["%.7E" % p for p in probe]
+        if mode == "exact":
+            # VTK output of a heat-conduction zone: the quad cells and the scalar TS
+            from typhon_gb300 import vtk
+            path = tmp_path / "tube.vtk"
+            g.kdif_write_vtk(path, raw)
+            f = vtk.read_vtk_ascii(path)
+            assert f["types"] == [9] * 10 and len(f["points"]) == 18
+            assert np.allclose(f["TS"], g.kdif_temperature(), rtol=1e-8, atol=0)
         g.close()
 
 
