@@ -760,26 +760,37 @@ __global__ void __launch_bounds__(kCgsThreads) k_basis_pass(T* V, size_t ldv, in
     }
     const float sf = (float)sc;
     float xx = 0.f;
-    for (size_t k = blockIdx.x * (size_t)kCgsThreads + t; k < n; k += (size_t)gridDim.x * kCgsThreads) {
-      float v[J];
-      const float* pv = V + k;
+    // R rows per trip (R x nv independent 4-byte loads in flight) for the short bases
+    constexpr int R = J <= 8 ? 4 : (J <= 16 ? 2 : 1);
+    const size_t stride = (size_t)gridDim.x * kCgsThreads;
+    for (size_t k0 = blockIdx.x * (size_t)kCgsThreads + t; k0 < n; k0 += R * stride) {
+      float v[R][J], x[R];
 #pragma unroll
-      for (int i = 0; i < J; ++i) {
-        v[i] = i < nv ? *pv : 0.f;
-        pv += ldv;
+      for (int r = 0; r < R; ++r) {
+        const size_t k = k0 + r * stride;
+        const bool ok = k < n;
+        const float* pv = V + k;
+#pragma unroll
+        for (int i = 0; i < J; ++i) {
+          v[r][i] = (ok && i < nv) ? *pv : 0.f;
+          pv += ldv;
+        }
+        x[r] = ok ? (float)src[k] : 0.f;
       }
-      float x = (float)src[k];
-      if (extend) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (extend) {
+#pragma unroll
+          for (int i = 0; i < J; ++i)
+            if (i < nv) x[r] = fmaf(-cf[i], v[r][i], x[r]);
+          x[r] = x[r] * sf;
+          if (k0 + r * stride < n) vout[k0 + r * stride] = x[r];
+        }
 #pragma unroll
         for (int i = 0; i < J; ++i)
-          if (i < nv) x = fmaf(-cf[i], v[i], x);
-        x = x * sf;
-        vout[k] = x;
+          if (i < nv) af[i] = fmaf(v[r][i], x[r], af[i]);
+        xx = fmaf(x[r], x[r], xx);
       }
-#pragma unroll
-      for (int i = 0; i < J; ++i)
-        if (i < nv) af[i] = fmaf(v[i], x, af[i]);
-      xx = fmaf(x, x, xx);
     }
 #pragma unroll
     for (int i = 0; i < J; ++i)
