@@ -725,7 +725,38 @@ __global__ void __launch_bounds__(kCgsThreads) k_basis_pass(T* V, size_t ldv, in
   const double sc = extend ? *sp : 1.0;
   __syncthreads();
   T* vout = V + (size_t)nv * ldv;
-  if constexpr (std::is_same<T, double>::value) {
+  if constexpr (std::is_same<T, double>::value && J <= 16) {
+    // short bases: per-thread sums in registers, written to shared memory once
+    double ad[J];
+#pragma unroll
+    for (int i = 0; i < J; ++i) ad[i] = 0.0;
+    double xx = 0.0;
+    for (size_t k = blockIdx.x * (size_t)kCgsThreads + t; k < n; k += (size_t)gridDim.x * kCgsThreads) {
+      double v[J];
+      const double* pv = V + k;
+#pragma unroll
+      for (int i = 0; i < J; ++i) {
+        v[i] = i < nv ? *pv : 0.0;
+        pv += ldv;
+      }
+      double x = src[k];
+      if (extend) {
+#pragma unroll
+        for (int i = 0; i < J; ++i)
+          if (i < nv) x = x - cl[i] * v[i];
+        x = x * sc;
+        vout[k] = x;
+      }
+#pragma unroll
+      for (int i = 0; i < J; ++i)
+        if (i < nv) ad[i] += v[i] * x;
+      xx += x * x;
+    }
+#pragma unroll
+    for (int i = 0; i < J; ++i)
+      if (i < nv) acc[i][t] = ad[i];
+    acc[nv][t] = xx;
+  } else if constexpr (std::is_same<T, double>::value) {
     double xx = 0.0;
     for (size_t k = blockIdx.x * (size_t)kCgsThreads + t; k < n; k += (size_t)gridDim.x * kCgsThreads) {
       double v[J];
