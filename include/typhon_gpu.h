@@ -194,12 +194,14 @@ int ty_rk_step(ty_mesh* mesh, int32_t rk_method, double dt);
 int ty_rk_steps(ty_mesh* mesh, int32_t rk_method, double cfl, int32_t nsteps, double* dt_last);
 
 /* One iteration of Typhon's steady explicit run (integration_cyclezone.f90:80-170 with
- * TIME = STEADY): the global stability time step at CFL cfl (calc_zonetimestep.f90:54-126),
- * one step of rk_method, and update_field.f90:45-60's residual terms of the step's update
+ * TIME = STEADY): the stability time step at CFL cfl (calc_zonetimestep.f90:54-126; global
+ * minimum, or per cell when local_dt is non-zero: DTCALC = LOCAL_STABILITY_CONDITION), one
+ * step of rk_method, and update_field.f90:45-60's residual terms of the step's update
  * res_l1[3] = (sum |d rho|, sum |d rho E|, sum |d rho u|) over the interior cells (host).
- * dt_out: the time step (host) or NULL.  The caller divides by the reference state and runs
- * the cycle logic (the Python side's Grid.ns_steady). */
-int ty_steady_iteration(ty_mesh* mesh, int32_t rk_method, double cfl, double* dt_out, double* res_l1);
+ * dt_out: the (minimum) time step (host) or NULL.  The caller divides by the reference state
+ * and runs the cycle logic (the Python side's Grid.ns_steady). */
+int ty_steady_iteration(ty_mesh* mesh, int32_t rk_method, double cfl, int32_t local_dt, double* dt_out,
+                        double* res_l1);
 
 /* Debug/parity access to intermediate fields of the last residual evaluation (host):
  * which = 0 prim [5][ncell], 1 grad [15][ncell], 2 face flux*S [5][nface],

@@ -235,7 +235,7 @@ struct Solver {
   // returns GMRES restarts (info) and the L1 norm of the update per variable in l1[5]
   int implicit_step(double cfl_, bool local_dt, double* l1);
   double timestep();             // stab_cond: global min dt over interior cells
-  void rk_step(double dt);       // treelevel_rungekutta + update_field
+  void rk_step(double dt, bool local = false);  // treelevel_rungekutta + update_field
 };
 
 // ---------------------------------------------------------------------------
@@ -309,6 +309,7 @@ struct NsSteadyParams {
   int max_iters = 100000, max_cycles = 1000;
   std::vector<int> history_faces;              // faces of the family with SAVE_HISTORY
   int rk_method = -1;                          // >= 0: explicit steps (0 = METHOD EXPLICIT), else implicit
+  bool local_dt = false;                       // explicit: DTCALC = LOCAL_STABILITY_CONDITION
 };
 struct NsSteadyOut {
   std::vector<double> log_res;      // log10 residual of every iteration

@@ -233,7 +233,7 @@ int ory_solver_typhon_steady(void* s, const double* dp, const int* ip, int nhist
   NsSteadyParams p;
   p.cfl = dp[0]; p.cfl_max = dp[1]; p.cycle_res = dp[2]; p.global_res = dp[3];
   S->inv_res = dp[4]; S->nkrylov = ip[0]; S->imp_max_it = ip[1];
-  p.max_iters = ip[2]; p.max_cycles = ip[3]; p.rk_method = ip[4];
+  p.max_iters = ip[2]; p.max_cycles = ip[3]; p.rk_method = ip[4]; p.local_dt = ip[5] != 0;
   p.history_faces.assign(hist, hist + nhist);
   NsSteadyOut out;
   ns_typhon_steady(*S, p, out);

@@ -1414,11 +1414,12 @@ double Solver::timestep() {
   return bad ? -1.0 : dt;
 }
 
-// treelevel_rungekutta.f90:48-113 then update_field.f90:38 (U += residu) with a global dt
-void Solver::rk_step(double dt) {
+// treelevel_rungekutta.f90:48-113 then update_field.f90:38 (U += residu) with a global dt, or
+// with the per-cell dtloc of timestep() when local (DTCALC = LOCAL_STABILITY_CONDITION)
+void Solver::rk_step(double dt, bool local) {
   const int nc = m->ncell;
   const int n = rk.nstage;
-  std::fill(dtloc.begin(), dtloc.end(), dt);
+  if (!local) std::fill(dtloc.begin(), dtloc.end(), dt);
   std::vector<double> u0 = cons;
   std::vector<std::vector<double>> rhs(n);
   for (int i = 1; i <= n; ++i) {
@@ -1476,9 +1477,9 @@ void ns_typhon_steady(Solver& s, const NsSteadyParams& p, NsSteadyOut& out) {
       ++iters;
       double cfl = p.cfl * std::max(1.0, 1.0 - std::log10(z_cur / z_ref) - std::log10(wcur_res / wres_ref));
       cfl = std::min(cfl, p.cfl_max);
-      if (p.rk_method >= 0) {  // explicit: global stability time step (calc_zonetimestep.f90:93-106)
+      if (p.rk_method >= 0) {  // explicit: stability time step (calc_zonetimestep.f90:93-117)
         s.cfl = cfl;
-        s.rk_step(s.timestep());
+        s.rk_step(s.timestep(), p.local_dt);
       } else {
         s.implicit_step(cfl, false, nullptr);
       }

@@ -230,13 +230,15 @@ class Solver:
         self.lib.ory_solver_set_inversion(self.h, {"GMRES": 0, "BICGSTAB": 1}[name])
 
     def typhon_steady(self, cfl, cfl_max=None, cycle_res=0.1, global_res=1e-4, nkrylov=50, max_it=50,
-                      inv_res=1e-4, history_faces=(), max_iters=100000, max_cycles=1000, method="IMPLICIT"):
+                      inv_res=1e-4, history_faces=(), max_iters=100000, max_cycles=1000, method="IMPLICIT",
+                      local_dt=False):
         """Typhon's steady run from the current state (implicit, or an explicit method of RK):
         log10 residual per iteration, per cycle the flux sums (F S) and S-weighted ghost
         primitive averages over history_faces, and the iteration count at each cycle's end."""
         cap = max_iters + 1
         dp = np.array([cfl, cfl if cfl_max is None else cfl_max, cycle_res, global_res, inv_res], np.float64)
-        ip = np.array([nkrylov, max_it, max_iters, max_cycles, -1 if method == "IMPLICIT" else RK[method]], np.int32)
+        ip = np.array([nkrylov, max_it, max_iters, max_cycles, -1 if method == "IMPLICIT" else RK[method],
+                       int(local_dt)], np.int32)
         hist = np.ascontiguousarray(history_faces, np.int32)
         lr, fs, ga, end = np.zeros(cap), np.zeros(5 * cap), np.zeros(5 * cap), np.zeros(cap, np.int32)
         nc = C.c_int()

@@ -176,3 +176,20 @@ def test_oracle_reproduces_hlle_histories(golden_dir):
     for c in range(8):
         assert ["%.5E" % v for v in fs[c]] == ["%.5E" % v for v in gf[c]], c
         assert ["%.5E" % v for v in ga[c]] == ["%.5E" % v for v in gv[c]], c
+
+
+def test_oracle_local_time_step_converges_faster(golden_dir):
+    """DTCALC = LOCAL_STABILITY_CONDITION on HLLC-MUSCL's case: per-cell time steps reach the
+    same 1e-2 residual drop in fewer iterations than the global one (152)."""
+    raw = cgns.read_cgns(golden_dir / "expansion-10.cgns")
+    ob = [(f, k, "", Z3, Z3, d) if d else (f, k, "", Z3) for f, k, d in BCS]
+    om = op.Mesh.from_raw(raw).build(2, ob)
+    s = op.Solver(om, op.SCH_HLLC, highres=op.HRES_MUSCL, limiter=op.LIM_VLEER, gradmeth=op.GRAD_LSQ, gamma=GAMMA,
+                  rgas=RGAS, rk="EXPLICIT")
+    rho, p, u = init_state(1e5, 300.0, 2.0)
+    prim = np.zeros((5, om.ncell))
+    prim[0], prim[1], prim[2] = rho, p, u
+    s.set_prim(prim)
+    lr, _, _, end = s.typhon_steady(1.0, 1.0, cycle_res=1e-2, global_res=1e-2, method="EXPLICIT", local_dt=True)
+    assert 0 < end[0] < 152
+    assert lr[-1] - lr.max() <= -2.0

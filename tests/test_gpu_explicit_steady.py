@@ -124,3 +124,35 @@ def test_gpu_hlle_histories(ty, golden_dir, mode):
     for c in range(8):
         assert ["%.5E" % v for v in out["flux"][c]] == ["%.5E" % v for v in gf[c]], c
     g.close()
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+def test_gpu_local_time_step_matches_oracle(ty, golden_dir, mode):
+    """DTCALC = LOCAL_STABILITY_CONDITION: the same iterations as the oracle, and in exact mode
+    the same state bit for bit."""
+    from typhon_gb300 import cgns
+    raw = cgns.read_cgns(golden_dir / "expansion-10.cgns")
+    md = ty.preprocess(raw, 2, [(f, k, "", (0.0, 0.0, 0.0)) for f, k, _ in BCS])
+    g = ty.Grid(md)
+    g.set_spat("HLLC", "MUSCL", "VANLEER", gradmeth="LSQ", mode=mode, gamma=GAMMA, rgas=RGAS)
+    g.set_boundary_params({f: d for f, _, d in BCS if d})
+    rho, p, u = init_state(1e5, 300.0, 2.0)
+    prim = np.zeros((5, md.ncell))
+    prim[0], prim[1], prim[2] = rho, p, u
+    g.set_prim(prim)
+    out = g.ns_steady(1.0, 1.0, cycle_res=1e-2, global_res=1e-2, method="EXPLICIT", local_dt=True)
+    om = op.Mesh.from_raw(raw).build(2, [(f, k, "", (0.0,) * 3, (0.0,) * 3, d) if d else (f, k, "", (0.0,) * 3)
+                                          for f, k, d in BCS])
+    s = op.Solver(om, op.SCH_HLLC, highres=op.HRES_MUSCL, limiter=op.LIM_VLEER, gradmeth=op.GRAD_LSQ, gamma=GAMMA,
+                  rgas=RGAS, rk="EXPLICIT")
+    s.set_prim(prim)
+    lr, _, _, end = s.typhon_steady(1.0, 1.0, cycle_res=1e-2, global_res=1e-2, method="EXPLICIT", local_dt=True)
+    assert list(out["cycle_end"]) == list(end)
+    assert np.abs(out["log_res"] - lr).max() < 1e-10
+    U, Uo = g.get_cons(), s.get("cons")[:, :md.ncell_int]
+    if mode == "exact":
+        assert np.array_equal(U, Uo)
+    else:
+        for v in range(5):
+            assert np.abs(U[v] - Uo[v]).max() <= 1e-12 * np.abs(Uo[v]).max(), v
+    g.close()

@@ -94,7 +94,8 @@ _SIGS = {
     "ty_residual": ([C.c_void_p, C.c_double, C.c_void_p], C.c_int),
     "ty_rk_step": ([C.c_void_p, C.c_int32, C.c_double], C.c_int),
     "ty_rk_steps": ([C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_double)], C.c_int),
-    "ty_steady_iteration": ([C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double), C.c_void_p], C.c_int),
+    "ty_steady_iteration": ([C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_double), C.c_void_p],
+                            C.c_int),
     "ty_debug_get": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
     "ty_set_bc_data": ([C.c_void_p, C.c_void_p], C.c_int),
     "ty_synchronize": ([C.c_void_p], C.c_int),

@@ -344,10 +344,12 @@ int ensure_pk(ty_mesh* h, const RkStagePlan* plans, int n) {
 // one RK step; dt either host value or device slot dtbits_cur.  dtbits_next: where the
 // final stage writes the next step's stability time step (or null).
 int run_step(ty_mesh* h, const RkTab& t, double dt, const unsigned long long* dtbits_cur,
-             unsigned long long* dtbits_next, double cfl, bool store_acc = false) {
+             unsigned long long* dtbits_next, double cfl, bool store_acc = false,
+             const double* dtloc = nullptr) {
   RkStagePlan plans[kMaxStage];
   make_plans(t, plans);
   plans[t.n - 1].store_acc = store_acc ? 1 : 0;
+  for (int i = 0; i < t.n; ++i) plans[i].dtloc = dtloc;
   int rc = ensure_pk(h, plans, t.n);
   if (rc) return rc;
   rc = ensure_prim(h);
@@ -743,16 +745,24 @@ int ty_rk_steps(ty_mesh* h, int32_t method, double cfl, int32_t nsteps, double* 
   return check_err(h);
 }
 
-int ty_steady_iteration(ty_mesh* h, int32_t method, double cfl, double* dt_out, double* res_l1) {
+int ty_steady_iteration(ty_mesh* h, int32_t method, double cfl, int32_t local_dt, double* dt_out, double* res_l1) {
   int rc = ready(h);
   if (rc) return rc;
   RkTab t;
   if (!rk_table(method, t) || !(cfl > 0.0) || !res_l1) return TY_ERR_ARG;
   if (!h->steady_red && (rc = h->alloc(h->steady_red, 3 * (size_t)tyk::kRedBlocks + 3))) return rc;
+  if (local_dt && !h->steady_dtloc && (rc = h->alloc(h->steady_dtloc, (size_t)h->m.nci))) return rc;
   if ((rc = set_dt_slot(h, 0, 1.7976931348623157e308))) return rc;
-  cudaError_t e = MODE_CALL(h, timestep, h->m, h->s, h->o, h->s.u0, cfl, h->s.dtbits, h->stream, &h->prof);
+  cudaError_t e;
+  if (local_dt) {  // calc_ns_timestep per cell, kept per cell (calc_zonetimestep.f90:93-117, loc_stab_cond)
+    tyk::ImpState im = h->imp;
+    im.dtloc = h->steady_dtloc;
+    e = MODE_CALL(h, imp_dtloc, h->m, h->s, h->o, im, cfl, h->s.dtbits, h->stream);
+  } else {
+    e = MODE_CALL(h, timestep, h->m, h->s, h->o, h->s.u0, cfl, h->s.dtbits, h->stream, &h->prof);
+  }
   if (e != cudaSuccess) return cuda_fail(e, "timestep");
-  if ((rc = run_step(h, t, 0.0, h->s.dtbits, nullptr, cfl, true))) return rc;
+  if ((rc = run_step(h, t, 0.0, h->s.dtbits, nullptr, cfl, true, local_dt ? h->steady_dtloc : nullptr))) return rc;
   double* out = h->steady_red + 3 * (size_t)tyk::kRedBlocks;
   e = MODE_CALL(h, res_l1, h->m.nci, h->s.acc, (size_t)h->m.ldc, h->steady_red, out, h->stream);
   if (e != cudaSuccess) return cuda_fail(e, "residual sums");

@@ -99,6 +99,7 @@ struct RkStagePlan {
   int final_stage = 0;  // 1: u0 <- u0 + acc
   int has_acc = 1;
   int store_acc = 0;    // final stage: also store acc (the residual of update_field)
+  const double* dtloc = nullptr;  // per-cell time step [nci] (LOCAL_STABILITY_CONDITION), else the global one
 };
 
 // Kernel identifiers for the per-kernel timing of ty_profile_read.

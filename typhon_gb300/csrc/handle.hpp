@@ -62,6 +62,7 @@ struct ty_mesh {
   double* adj_rec = nullptr;   // [50][ldf] reversed reconstructions (second-order adjoint)
   double* adj_qg = nullptr;    // [20][ldc] adjoints of q and of the gradients (second order)
   double* steady_red = nullptr;  // [3 kRedBlocks + 3] partial and final residual sums of ty_steady_iteration
+  double* steady_dtloc = nullptr;  // [nci] per-cell time step of ty_steady_iteration (local_dt)
   cudaStream_t own_stream = nullptr;
 
   template <class T>

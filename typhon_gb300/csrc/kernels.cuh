@@ -1226,9 +1226,10 @@ __global__ void __launch_bounds__(kBlock) k_rk_update(DevMesh m, DevState s, RkS
     const size_t ld = m.ldc;
     double R[5];
     gather_residual(m, s, c, R);
+    const double dtv = plan.dtloc ? plan.dtloc[c] : load_dt(dt, dtbits);
     double coef;
-    if constexpr (kFast) coef = load_dt(dt, dtbits) * m.invV[c];
-    else coef = load_dt(dt, dtbits) / m.cvol[c];
+    if constexpr (kFast) coef = dtv * m.invV[c];
+    else coef = dtv / m.cvol[c];
 #pragma unroll
     for (int v = 0; v < 5; ++v) R[v] = coef * R[v];
     double u0[5];

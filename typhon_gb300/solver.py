@@ -224,7 +224,7 @@ class Grid:
 
     def ns_steady(self, cfl, cfl_max=None, cycle_res=0.1, global_res=1e-4, inversion="GMRES", nkrylov=50,
                   max_it=50, inv_res=1e-4, precision="fp64", history=None, max_iters=100000, max_cycles=1000,
-                  cycle_max_it=None, method="IMPLICIT"):
+                  cycle_max_it=None, method="IMPLICIT", local_dt=False):
         """Typhon's steady run of one zone from the resident state (integration.f90,
         integration_cycle.f90, integration_cyclezone.f90, check_end_cycle.f90; the CFL law of
         calc_zonetimestep.f90, cfl (1 - log10 of the zone's and the world's residual drops,
@@ -232,7 +232,8 @@ class Grid:
         state of calc_refcons.f90).  method: IMPLICIT (TIME_PARAM METHOD = IMPLICIT, one
         implicit_step per iteration with inversion / nkrylov / max_it / inv_res / precision)
         or an explicit method (EXPLICIT, RK2, ..., one ty_steady_iteration: global stability
-        time step, one step, the update's residual sums).  history: a family whose summed
+        time step, one step, the update's residual sums).  local_dt: DTCALC =
+        LOCAL_STABILITY_CONDITION (per-cell time steps) for either method.  history: a family whose summed
         face fluxes F S (integ_ustboco.f90's histoflux file) and the S-weighted average of
         the ghost primitive states the fluxes were computed from after each cycle are
         returned.  The second equals Typhon's histovar file when Typhon writes the boundary
@@ -266,12 +267,13 @@ class Grid:
                 c = cfl * max(1.0, 1.0 - np.log10(z_cur / z_ref) - np.log10(wcur_res / wres_ref))
                 if method == "IMPLICIT":
                     st = self.implicit_step(min(c, cfl_max), inversion=inversion, nkrylov=nkrylov, max_it=max_it,
-                                            inv_res=inv_res, precision=precision)
+                                            inv_res=inv_res, precision=precision, local_dt=local_dt)
                     z_cur = st["du_l1"][0] / ref0 + st["du_l1"][1] / ref1 + st["du_mom"] / refv
                 else:
                     dt = C.c_double()
                     _capi.check(self.lib.ty_steady_iteration(self.h, RK_METHOD[method], float(min(c, cfl_max)),
-                                                             C.byref(dt), res3.ctypes.data), "ty_steady_iteration")
+                                                             int(bool(local_dt)), C.byref(dt), res3.ctypes.data),
+                                "ty_steady_iteration")
                     z_cur = res3[0] / ref0 + res3[1] / ref1 + res3[2] / refv
                 z_ref = max(z_ref, z_cur)
                 log_res.append(np.log10(z_cur))
