@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-sample-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--imp-steps", type=int, default=0,
+                    help="ffbox3d-implicit: time this many implicit steps per precision at the starting CFL "
+                         "instead of the runs to 1e-10 (a short sequence of launches for ncu)")
     ap.add_argument("--kdif-inner-tol", type=float, default=1e-3, help="kdif3d: FP32 inner CG tolerance")
     ap.add_argument("--kdif-inner-max", type=int, default=300, help="kdif3d: FP32 inner CG iterations at most")
     return ap.parse_args()
@@ -346,6 +349,26 @@ def run_implicit(args):
     L = w["length"]
     prim0 = cases.perturbed_freestream(md.cell_centre, ff, (L / 2, L / 2, L / 2))
     scale = np.array([ff[0], ff[1] / 0.4, 0.3, 0.3, 0.3])
+    if args.imp_steps:
+        # a fixed number of FGMRES steps (FP64, then mixed) at the starting CFL, after one warm-up
+        res = {}
+        for prec in ("fp64", "mixed"):
+            g = ty.Grid(md)
+            g.set_spat(w["scheme"], w["highres"], w["limiter"], w["postlim"], mode="fast", farfield=ff)
+            g.set_prim(prim0)
+            kw = dict(nkrylov=w["nkrylov"], max_it=w["max_it"], inv_res=w["inv_res"], local_dt=True, precision=prec)
+            g.implicit_step(w["cfl0"], "FGMRES", **kw)
+            g.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.imp_steps):
+                st = g.implicit_step(w["cfl0"], "FGMRES", **kw)
+            g.synchronize()
+            res[prec] = {"ms_per_step": round((time.perf_counter() - t0) / args.imp_steps * 1e3, 3),
+                         "matvecs_per_step": st["matvecs"]}
+            g.close()
+        print(json.dumps({"workload": f"ffbox3d {args.n or w['n']}^3x5 FGMRES steps", "cells": nci,
+                          "steps": args.imp_steps, "variants": res}))
+        return
     variants = {}
     states = {}
     with ClockSampler(0) as clk:
