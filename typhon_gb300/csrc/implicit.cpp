@@ -48,8 +48,7 @@ namespace {
 
 constexpr int kScalGram = 0;                  // scal offsets of the flexible GMRES: V^T v_j, v_j . v_j
 constexpr int kScalProj = kMaxCgs + 1;        // V^T w, w . w (both fetched in one copy)
-constexpr int kScalCoef = 2 * kMaxCgs + 4;    // c of the next basis vector (after the fetched range)
-constexpr int kScalInvNu = 3 * kMaxCgs + 5;   // 1 / nu of the next basis vector
+constexpr int kScalCoef = 2 * kMaxCgs + 4;    // c of the next basis vector v_j, then 1 / nu at + j (one copy)
 constexpr int kScalY = 2 * kMaxKrylov + 4;    // solution coefficients (kMaxKrylov)
 constexpr int kScalMisc = 3 * kMaxKrylov + 4; // reductions of the step (16)
 constexpr int kScalCount = 3 * kMaxKrylov + 20;
@@ -408,12 +407,12 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
         src = im.r;
       }
       const double binv = 1.0 / beta;
-      if (int rc = put(h, kScalInvNu, &binv, 1)) return rc;
+      if (int rc = put(h, kScalCoef, &binv, 1)) return rc;
       a[0] = beta;
       int j, nused = 0;
       for (j = 0; j < mk; ++j) {
         IMP_CU(IMP_CALL(h, imp_basis_pass, V64, V32, n, j, im.scal + kScalCoef, j == 0 ? src : im.w,
-                        im.scal + kScalInvNu, 1, n, im.part, im.done, im.scal + kScalGram, s, &h->prof));
+                        im.scal + kScalCoef + j, 1, n, im.part, im.done, im.scal + kScalGram, s, &h->prof));
         IMP_CU(IMP_CALL(h, imp_precond, m, im, Vd(j), Vf(j), Z(j), Z32(j), s, &h->prof));
         if (int rc = op.apply(Z(j), Z32(j), im.w, &matvecs)) return rc;
         IMP_CU(IMP_CALL(h, imp_basis_pass, V64, V32, n, j + 1, nullptr, im.w, nullptr, 0, n, im.part, im.done,
@@ -456,9 +455,8 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
           std::fprintf(stderr, "ty_implicit fgmres cycle %d j %d r_jj %.6e nu %.6e |g|/|b| %.6e\n", cycles, j,
                        Rm(j, j), nu, std::fabs(a[j + 1]) / beta0);
         if (std::fabs(a[j + 1]) <= tol || invariant) break;
-        const double ninv = 1.0 / nu;
-        if (int rc = put(h, kScalCoef, c.data(), j + 1)) return rc;
-        if (int rc = put(h, kScalInvNu, &ninv, 1)) return rc;
+        c[j + 1] = 1.0 / nu;  // c of v_{j+1}, then its scale, in one copy
+        if (int rc = put(h, kScalCoef, c.data(), j + 2)) return rc;
       }
       for (int i = nused - 1; i >= 0; --i) {
         double v = gr[i];
