@@ -228,6 +228,12 @@ __device__ __forceinline__ void store_block32(float* dst, const double* J) {
     d4[k] = make_float4((float)J[4 * k], (float)J[4 * k + 1], (float)J[4 * k + 2], (float)J[4 * k + 3]);
   d4[6] = make_float4((float)J[24], 0.f, 0.f, 0.f);
 }
+__device__ __forceinline__ void store_block32f(float* dst, const float* J) {
+  float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) d4[k] = make_float4(J[4 * k], J[4 * k + 1], J[4 * k + 2], J[4 * k + 3]);
+  d4[6] = make_float4(J[24], 0.f, 0.f, 0.f);
+}
 __device__ __forceinline__ void load_block32(const float* src, float* J) {
   const float4* s4 = reinterpret_cast<const float4*>(src);
 #pragma unroll
@@ -344,42 +350,43 @@ __global__ void __launch_bounds__(128) k_imp_face(DevMesh m, DevState s, SpatOpt
 }
 
 // 5x5 inverse by Gauss-Jordan elimination with partial pivoting; false if singular
-__device__ bool inv5(const double* A, double* X) {
-  double a[25];
+template <class T>
+__device__ bool inv5(const T* A, T* X) {
+  T a[25];
 #pragma unroll
-  for (int k = 0; k < 25; ++k) { a[k] = A[k]; X[k] = 0.0; }
+  for (int k = 0; k < 25; ++k) { a[k] = A[k]; X[k] = T(0); }
 #pragma unroll
-  for (int i = 0; i < 5; ++i) X[i * 6] = 1.0;
+  for (int i = 0; i < 5; ++i) X[i * 6] = T(1);
 #pragma unroll
   for (int col = 0; col < 5; ++col) {
     int p = col;
-    double best = fabs(a[col * 5 + col]);
+    T best = fabs(a[col * 5 + col]);
 #pragma unroll
     for (int r = col + 1; r < 5; ++r) {
-      double v = fabs(a[r * 5 + col]);
+      T v = fabs(a[r * 5 + col]);
       if (v > best) { best = v; p = r; }
     }
-    if (!(best > 0.0)) return false;
+    if (!(best > T(0))) return false;
     // row swap with compile-time indices only (selects), so that a and X stay in registers
 #pragma unroll
     for (int r = col + 1; r < 5; ++r) {
       const bool sw = r == p;
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        const double ta = a[col * 5 + k], tx = X[col * 5 + k];
+        const T ta = a[col * 5 + k], tx = X[col * 5 + k];
         a[col * 5 + k] = sw ? a[r * 5 + k] : ta;
         a[r * 5 + k] = sw ? ta : a[r * 5 + k];
         X[col * 5 + k] = sw ? X[r * 5 + k] : tx;
         X[r * 5 + k] = sw ? tx : X[r * 5 + k];
       }
     }
-    const double ip = 1.0 / a[col * 5 + col];
+    const T ip = T(1) / a[col * 5 + col];
 #pragma unroll
     for (int k = 0; k < 5; ++k) { a[col * 5 + k] *= ip; X[col * 5 + k] *= ip; }
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
       if (r == col) continue;
-      const double fct = a[r * 5 + col];
+      const T fct = a[r * 5 + col];
 #pragma unroll
       for (int k = 0; k < 5; ++k) { a[r * 5 + k] -= fct * a[col * 5 + k]; X[r * 5 + k] -= fct * X[col * 5 + k]; }
     }
@@ -418,7 +425,19 @@ __global__ void __launch_bounds__(128) k_imp_diag(DevMesh m, ImpState im, ImpArg
   }
   if (a.want64) store_block(im.diag + (size_t)c * kBlk, D);
   if (a.want32) store_block32(im.diag32 + (size_t)c * kBlk32, D);
-  if (want_inv) {
+  if (want_inv && !a.want64) {  // mixed solve: only the FP32 inverse is used, so invert in FP32
+    float Df[25], Xf[25];
+#pragma unroll
+    for (int k = 0; k < 25; ++k) Df[k] = (float)D[k];
+    if (!inv5(Df, Xf)) {
+      flag_error(err, TY_ERR_STATE, c);
+#pragma unroll
+      for (int k = 0; k < 25; ++k) Xf[k] = 0.f;
+#pragma unroll
+      for (int i = 0; i < 5; ++i) Xf[i * 6] = 1.f;
+    }
+    store_block32f(im.dinv32 + (size_t)c * kBlk32, Xf);
+  } else if (want_inv) {
     double X[25];
     if (!inv5(D, X)) {
       flag_error(err, TY_ERR_STATE, c);
