@@ -11,7 +11,9 @@ cell-update = one cell advanced by one step.
                   [--workload tgv3d|vortex2d|ffbox3d-implicit|kdif3d|adjoint3d] [--n 64] [--mode fast|exact]
 
 --workload ffbox3d-implicit: time to a 1e-10 relative residual of the implicit solvers (FP64
-flexible GMRES, mixed FP32/FP64, FP64 Jacobian-free) on a steady 3D far-field box.
+flexible GMRES, mixed FP32/FP64, FP64 Jacobian-free) on a steady 3D far-field box, with a
+per-kernel profile of one more step of each; --imp-steps K times K flexible-GMRES steps per
+precision instead (a short launch sequence for ncu).
 --workload kdif3d: 50 implicit heat-conduction steps, FP64 CG vs FP32 CG with FP64 refinement.
 --workload adjoint3d: unsteady adjoint gradient, its cost against the primal, FD checks.
 
