@@ -133,8 +133,13 @@ def measured_peaks():
 
 
 def fp64_peak():
-    """Measured DFMA rate of this GPU (typhon_gb300/_lib/fp64_peak), FLOP/s, or None."""
-    probe = ROOT / "typhon_gb300" / "_lib" / "fp64_peak"
+    """Measured DFMA rate of this GPU (the probe fp64_peak.cu, built to _build/fp64_peak),
+    FLOP/s, or None."""
+    from typhon_gb300 import build as tybuild
+    try:
+        probe = tybuild.build_fp64_probe()
+    except (OSError, RuntimeError):
+        return None
     try:
         r = subprocess.run([str(probe)], capture_output=True, text=True, timeout=60)
     except (OSError, subprocess.TimeoutExpired):
@@ -242,8 +247,7 @@ def run_ours(args, rank, world, local):
     dom = max(per, key=lambda k: per[k]["total_ms"])
     ach = per[dom]["achieved_gbs"]
     # DRAM traffic and FP64 instructions per unit, from one ncu capture of the same kernels on
-    # the 40^3x5 mesh (320,000 cells, 646,400 faces; profiles/cell_fast_face_flux_fast__tgv3d_n40.md),
-    # scaled by the units of this mesh
+    # the 40^3x5 mesh (320,000 cells, 646,400 faces), scaled by the units of this mesh
     per_unit = {"cell_fast": (nci, (97.1e6 + 54.9e6) / 320000, 349),
                 "face_flux_fast": (md.nface, (72.2e6 + 4.2e6) / 646400, 160)}
     traffic = None
@@ -257,7 +261,7 @@ def run_ours(args, rank, world, local):
             fp64_roof = {"instr_per_unit": ipu, "units": int(units), "achieved_tinstr_s": round(inst, 4),
                     "peak_tinstr_s": round(peak64 / 2e12, 4), "frac": round(inst / (peak64 / 2e12), 4),
                     "note": "FP64 instructions (DFMA/DADD/DMUL, one each) per unit counted by ncu; peak = the "
-                            "DFMA instruction rate measured on this GPU by typhon_gb300/_lib/fp64_peak"}
+                            "DFMA instruction rate measured on this GPU by fp64_peak.cu"}
     roofline = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": peak_kind, "traffic": traffic,
                 "traffic_source": "ncu, 40^3x5 mesh, scaled by units" if traffic else None,

@@ -352,10 +352,12 @@ int ty_kdif_matvec(ty_mesh* mesh, const double* x, double* y);
  * ty_state_upload_device and work on caller DEVICE buffers [5][ncell_int] (rho, rhoE, rhou,
  * rhov, rhow), queued on the handle's stream.
  *   ty_residual_device: R = dt/V sum(+-F S), ty_residual's value.
- *   ty_adjoint_vjp:     lambda_U = (dR/dU)^T lambda_R of the first-order inviscid residual
- *                       (HIGHRES = NONE, no viscous flux; TY_ERR_UNSUPPORTED otherwise):
- *                       a reversed face loop (face products with dual-number flux
- *                       Jacobians, then a per-cell gather). */
+ *   ty_adjoint_vjp:     lambda_U = (dR/dU)^T lambda_R of the inviscid residual, first order
+ *                       (HIGHRES = NONE, any boundary) or second order (least-squares
+ *                       gradients, HIGHRES = MUSCL with no limiter or van Albada, periodic
+ *                       boundaries); TY_ERR_UNSUPPORTED otherwise.  A reversed face loop
+ *                       (hand-written reverse-mode flux derivatives, reversed
+ *                       reconstruction) and per-cell gathers, no atomics. */
 int ty_residual_device(ty_mesh* mesh, double dt, double* R);
 int ty_adjoint_vjp(ty_mesh* mesh, double dt, const double* lambda_R, double* lambda_U);
 
@@ -370,8 +372,11 @@ int ty_adjoint_vjp(ty_mesh* mesh, double dt, const double* lambda_R, double* lam
  *   dt_out      host: the minimum over cells of CFL*2*V/sum S/(|u|+a)
  * Allocates nothing: its scratch (a partial minimum per 256 cells, the result and an error
  * word) lives in a static device array of the library, at most 4,194,304 cells per call
- * (larger ncell returns TY_ERR_ARG).  The first call on a device looks the array up; make
- * it before any stream capture.  Calls share the array: calls that overlap on the GPU race.
+ * (larger ncell returns TY_ERR_ARG).  Every call looks up the array's address in the CUDA
+ * context current on the calling thread.  The first call in a context loads the library's
+ * module (CUDA loads modules lazily) and that load allocates device memory for the code and
+ * the array: make one call at set-up, before any stream capture and before the phase that
+ * must not allocate.  Calls share the array: calls that overlap on the GPU race.
  * Synchronises the stream; returns TY_ERR_NEGENERGY / TY_ERR_NANDT like ty_timestep. */
 int ty_timestep_static(int32_t ncell, const double* cons, int32_t ld, const double* volume,
                        const double* sum_surface, double gamma, double cfl, void* stream, double* dt_out);

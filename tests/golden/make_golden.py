@@ -1,7 +1,7 @@
 """Copy the golden data of Typhon's non-regression suite used by the tests.
 
-Run once in a container where the reference checkout is mounted (default path
-below, or pass it as the first argument).  It copies, unchanged:
+Run once where a checkout of the reference is available, with its path as the only
+argument (``python tests/golden/make_golden.py <typhon checkout>``).  It copies, unchanged:
 
 * the XBIN/TYPHON meshes of NRG/COMMON that the cases use (``*.tym``) and the CGNS
   (ADF) meshes of the implicit and heat-conduction cases (``*.cgns``);
@@ -15,7 +15,9 @@ import pathlib
 import shutil
 import sys
 
-REF = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_golden.py <path of the Typhon checkout>")
+REF = pathlib.Path(sys.argv[1])
 HERE = pathlib.Path(__file__).resolve().parent
 
 MESHES = ["quad20x20.tym", "quad20x10.tym", "quad10x10.tym", "tri5x10.tym", "mxlay2x20quad-h50.tym",

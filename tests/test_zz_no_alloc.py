@@ -100,3 +100,26 @@ def test_static_timestep_errors_and_recovery(env):
     rc = _capi.lib().ty_timestep_static(big, cons.data_ptr(), big, vol.data_ptr(), sums.data_ptr(), 1.4, 0.8,
                                         None, C.byref(dtv))
     assert rc == -1 and "static scratch limit" in _capi.lib().ty_last_error().decode()
+
+
+def test_static_timestep_allocates_nothing(env):
+    """After a first call has loaded the library's module in this context, further calls
+    leave the GPU's free memory and PyTorch's allocator statistics unchanged."""
+    torch, ty, _capi, md, prim = env
+    nci = md.ncell_int
+    cons = torch.tensor(ty.prim_to_cons(prim[:, :nci]), dtype=torch.float64, device="cuda").contiguous()
+    vol = torch.tensor(md.cell_volume[:nci], dtype=torch.float64, device="cuda")
+    sums = torch.tensor(sum_surface_colour_order(md), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    rc, dt0 = static_dt(torch, _capi, cons, vol, sums, nci, 0.8, stream)      # warm-up call
+    assert rc == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    alloc0, reserved0 = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
+    for _ in range(3):
+        rc, dt = static_dt(torch, _capi, cons, vol, sums, nci, 0.8, stream)
+        assert rc == 0 and dt == dt0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert torch.cuda.memory_allocated() == alloc0 and torch.cuda.memory_reserved() == reserved0

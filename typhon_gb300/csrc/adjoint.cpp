@@ -2,8 +2,8 @@
 //
 // Both act on the handle's resident state U (ty_state_upload_device): ty_residual_device
 // writes R = dt/V sum(+-F S) (ty_residual's value) to a caller device buffer, and
-// ty_adjoint_vjp writes lambda_U = (dR/dU)^T lambda_R for the first-order residual
-// (HIGHRES = NONE, inviscid).  New: Typhon has no adjoint; the unsteady gradient of a
+// ty_adjoint_vjp writes lambda_U = (dR/dU)^T lambda_R for the inviscid residual, first order
+// (HIGHRES = NONE) or second order (MUSCL with no limiter or van Albada, periodic meshes).  New: Typhon has no adjoint; the unsteady gradient of a
 // functional (RK stages, checkpointing, torch.autograd) is composed from these two calls in
 // typhon_gb300/adjoint.py.
 #include <vector>

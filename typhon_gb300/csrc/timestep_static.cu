@@ -17,13 +17,18 @@
 // overlap on the GPU (different streams, or different host threads on the same device)
 // race on the array and give undefined results: serialise them.
 //
+// Module loading.  With CUDA's lazy loading (the default), the first call in a CUDA context
+// makes the driver load this library's module, and that load allocates device memory for the
+// code and for the array.  Later calls in the same context allocate nothing.  A caller that
+// must not allocate during its run makes one call at set-up (it also has to come before any
+// stream capture).
+//
 // The per-cell formula is calc_ns_timestep's (SOURCE/EQNS/calc_ns_timestep.f90:52-103):
 // dt_c = CFL*2*V_c / sum_f S_f / (|u| + a), each operation rounded separately (this file is
 // compiled with -fmad=false), then the minimum over cells (calc_zonetimestep.f90:95).
 #include <cuda_runtime.h>
 
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "../../include/typhon_gpu.h"
@@ -37,10 +42,6 @@ constexpr int kMaxBlocks = 16384;  // cells per call at most kBlock * kMaxBlocks
 constexpr int kResult = kMaxBlocks;      // slot of the result
 constexpr int kErr = kMaxBlocks + 1;     // slot of the error word: int code, int cell
 static __device__ __align__(256) unsigned long long g_scratch[kMaxBlocks + 2];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-unsigned long long* g_scratch_ptr[kMaxDevices] = {};  // device address of g_scratch per device
 
 __global__ void __launch_bounds__(kBlock) k_dt_blockmin(int n, const double* __restrict__ cons, int ld,
                                                         const double* __restrict__ vol,
@@ -112,30 +113,21 @@ __global__ void __launch_bounds__(kBlock) k_dt_final(int nblocks, const unsigned
   }
 }
 
-// Device address of the scratch array on the current device, looked up once per device
-// (the name g_scratch is only a host-side stand-in in host code).
-int scratch_for_current_device(unsigned long long** scratch) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
+// Device address of the scratch array in the CUDA context that is current on this thread.
+// In host code the name g_scratch is only a host-side stand-in, never a device address.  The
+// address belongs to the context that loaded the library's module, not to the device number:
+// after cudaDeviceReset, or when the caller makes another context current on the same
+// device, an address kept from an earlier call would point into freed or foreign memory.  So
+// it is looked up on every call; cudaGetSymbolAddress allocates nothing once the module is
+// loaded in the context.
+int scratch_in_current_context(unsigned long long** scratch) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
   if (e != cudaSuccess) {
-    tyi::set_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    tyi::set_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     return TY_ERR_CUDA;
   }
-  if (dev < 0 || dev >= kMaxDevices) {
-    tyi::set_error("device ordinal out of range");
-    return TY_ERR_ARG;
-  }
-  std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess) {
-      tyi::set_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      return TY_ERR_CUDA;
-    }
-    g_scratch_ptr[dev] = static_cast<unsigned long long*>(p);
-  }
-  *scratch = g_scratch_ptr[dev];
+  *scratch = static_cast<unsigned long long*>(p);
   return TY_OK;
 }
 
@@ -155,7 +147,7 @@ extern "C" int ty_timestep_static(int32_t ncell, const double* cons, int32_t ld,
     return TY_ERR_ARG;
   }
   unsigned long long* scratch = nullptr;
-  int rc = scratch_for_current_device(&scratch);
+  int rc = scratch_in_current_context(&scratch);
   if (rc != TY_OK) return rc;
   unsigned long long* blockmin = scratch;
   int* err = reinterpret_cast<int*>(scratch + kErr);
