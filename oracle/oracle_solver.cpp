@@ -720,6 +720,21 @@ static void roe_flux(double g, const State& L, const State& R, V3 n, double delt
   F[2] = fm.x; F[3] = fm.y; F[4] = fm.z;
 }
 
+// Test access to the Roe flux on arrays of face states (the property tests of the flux:
+// consistency, rotational invariance, contacts).  L, R: [n][5] primitive (rho, p, u, v, w);
+// nrm: [n][3] unit normals; F: [n][5] flux per unit area (mass, energy, momentum).
+extern "C" int ory_roe_flux(double g, double delta_frac, int n, const double* L, const double* R, const double* nrm,
+                            double* F) {
+  for (int i = 0; i < n; ++i) {
+    const double* l = L + 5 * (size_t)i;
+    const double* r = R + 5 * (size_t)i;
+    State sl{l[0], l[1], v3(l[2], l[3], l[4])}, sr{r[0], r[1], v3(r[2], r[3], r[4])};
+    roe_flux(g, sl, sr, v3(nrm[3 * (size_t)i], nrm[3 * (size_t)i + 1], nrm[3 * (size_t)i + 2]), delta_frac,
+             F + 5 * (size_t)i);
+  }
+  return 0;
+}
+
 // calc_jacflux (SOURCE/EQNS/calc_jacflux.f90:49-77): Jacobian of the physical flux along n
 // with respect to (rho, rhoE, rhou, rhov, rhow), for one state; row-major 5x5
 static void jacflux(double g, const double* st /* rho, p, u, v, w */, V3 fn, double vn, double* J) {

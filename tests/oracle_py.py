@@ -77,12 +77,25 @@ def load():
         lib.ory_kdif_typhon_steady.argtypes = [vp, vp, vp, C.c_int, vp, vp, vp, vp]
         lib.ory_kdif_typhon_steady.restype = C.c_int
         lib.ory_run_nrg.argtypes = [C.c_int, vp, C.c_int, C.c_double, C.c_int, C.c_double, vp]
+        lib.ory_roe_flux.argtypes = [C.c_double, C.c_double, C.c_int, vp, vp, vp, vp]
         _lib = lib
     return _lib
 
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def roe_flux(L, R, nrm, gamma=1.4, entropy_fix=0.1):
+    """The oracle's Roe flux per unit area on arrays of face states: L, R [n][5] primitive
+    (rho, p, u, v, w), nrm [n][3] unit normals -> [n][5] (mass, energy, momentum)."""
+    lib = load()
+    L = np.ascontiguousarray(L, np.float64)
+    R = np.ascontiguousarray(R, np.float64)
+    nrm = np.ascontiguousarray(nrm, np.float64)
+    F = np.zeros_like(L)
+    lib.ory_roe_flux(float(gamma), float(entropy_fix), L.shape[0], _p(L), _p(R), _p(nrm), _p(F))
+    return F
 
 
 class Mesh:

@@ -147,10 +147,23 @@ def test_device_timestep_loop_matches_host_loop(ty):
 
 
 def test_fast_mode_vortex_full_size(ty):
-    """The 2D vortex configuration at its full size (8192 triangles): 20 RK4 steps."""
+    """The 2D vortex configuration as benchmarked (8192 triangles, HLLC + MUSCL + van Albada,
+    RK4 at CFL 0.8): all 200 steps in fast mode against the oracle."""
     md, om, prim = make_case(ty, "vortex", 64)
     g, s = pair(ty, md, om, prim, "HLLC", "MUSCL", "ALBADA", mode="fast")
-    g.run_steps("RK4", 0.8, 20)
+    g.run_steps("RK4", 0.8, 200)
+    s.run_steps(200)
+    rel = relerr(g.get_cons(), s.get("cons")[:, :md.ncell_int])
+    assert np.all(rel <= FAST_RTOL), rel
+
+
+def test_fast_mode_tgv_benchmark_size(ty):
+    """The benchmarked configuration at its full size: TGV 64^3 x 5 = 1,310,720 tetrahedra,
+    Roe + MUSCL-UNS + Barth, SSP-RK3 at CFL 0.8, time step on the device; 20 steps in fast
+    mode (the bench's mode) against the oracle, 1e-12 relative L2 per conserved variable."""
+    md, om, prim = make_case(ty, "tgv", 64)
+    g, s = pair(ty, md, om, prim, "ROE", "MUSCL-UNS", "NONE", "BARTH", mode="fast", rk="RK3-SSP")
+    g.run_steps("RK3-SSP", 0.8, 20)
     s.run_steps(20)
     rel = relerr(g.get_cons(), s.get("cons")[:, :md.ncell_int])
     assert np.all(rel <= FAST_RTOL), rel

@@ -1,0 +1,131 @@
+"""Property pins of the GPU Roe flux, through the C ABI (exact and fast modes).
+
+Typhon has no Roe flux (SOURCE/EQNS/calc_flux_inviscid.f90:48-79), so the kernels are pinned
+by properties any correct Roe flux has (tests/flux_props.py): consistency on a uniform state,
+rotational invariance of the whole residual on a rotated mesh, discrete conservation on a
+periodic mesh, and second-order convergence on the isentropic vortex.  The same properties
+are checked on the CPU oracle in tests/test_roe_properties.py.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+import flux_props as fp
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ty():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from typhon_gb300 import build
+    build.build()
+    import typhon_gb300
+    return typhon_gb300
+
+
+def tgv_mesh(ty, n, Q=None):
+    L = 2 * np.pi
+    raw = ty.gen_tet_box(n, L, jitter=0.05, seed=1234)
+    tr = [np.array([L, 0, 0.]), np.array([0, L, 0.]), np.array([0, 0, L])]
+    if Q is not None:
+        raw = dataclasses.replace(raw, vtex=raw.vtex @ Q.T)
+        tr = [Q @ t for t in tr]
+    bcs = [(a, ty.BC_PERIODIC, b, tuple(t)) for (a, b), t in zip((("IMIN", "IMAX"), ("JMIN", "JMAX"),
+                                                                   ("KMIN", "KMAX")), tr)]
+    return ty.preprocess(raw, 3, bcs)
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+@pytest.mark.parametrize("highres,limiter,postlim", [("NONE", "NONE", "NONE"), ("MUSCL-UNS", "NONE", "BARTH")])
+def test_consistency_uniform_state(ty, mode, highres, limiter, postlim):
+    """A uniform state on the periodic tetrahedral mesh: every face flux is F_phys(U).n S, for
+    subsonic and supersonic states, and the residual vanishes (free-stream preservation)."""
+    md = tgv_mesh(ty, 4)
+    rng = np.random.default_rng(7)
+    g = ty.Grid(md)
+    g.set_spat("ROE", highres, limiter, postlim, gradmeth="NONE" if highres == "NONE" else "LSQ", mode=mode)
+    nrm, S = md.face_normal, md.face_surface
+    for speed in (0.3, 3.0):
+        q = fp.random_states(rng, 1, speed=speed)[0]
+        g.set_prim(np.repeat(q[:, None], md.ncell, axis=1))
+        R = g.integration_grid(1e-3)
+        F = g.debug("flux").T / S[:, None]
+        ref = fp.physical_flux(np.repeat(q[None], md.nface, axis=0), nrm)
+        assert (np.abs(F - ref) / np.abs(ref).max()).max() < 1e-14
+        scale = 1e-3 * np.abs(ref).max() * S.max() / md.cell_volume[:md.ncell_int].min()
+        assert np.abs(R).max() < 1e-13 * scale
+    g.close()
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+@pytest.mark.parametrize("highres,limiter", [("NONE", "NONE"), ("MUSCL-UNS", "NONE"), ("MUSCL", "ALBADA")])
+def test_rotational_invariance_of_the_residual(ty, mode, highres, limiter):
+    """The TGV state on a rigidly rotated copy of the mesh (periodic translations rotated too):
+    the residual's density and energy rows are unchanged and its momentum rows are rotated,
+    to rounding.  (Barth's post-limiter limits vector components one by one and is not
+    rotation invariant, so it is left out.)"""
+    from typhon_gb300 import cases
+    rng = np.random.default_rng(11)
+    Q = fp.random_rotation(rng)
+    md0, md1 = tgv_mesh(ty, 6), tgv_mesh(ty, 6, Q)
+    assert np.array_equal(md0.fc1, md1.fc1) and np.array_equal(md0.fc2, md1.fc2)
+    prim0 = cases.taylor_green(md0.cell_centre)
+    prim1 = fp.rotate_prim(prim0.T, Q).T
+    out = []
+    for md, prim in ((md0, prim0), (md1, prim1)):
+        g = ty.Grid(md)
+        g.set_spat("ROE", highres, limiter, "NONE", gradmeth="NONE" if highres == "NONE" else "LSQ", mode=mode)
+        g.set_prim(prim)
+        out.append(g.integration_grid(1e-3))
+        g.close()
+    R0, R1 = out
+    R0r = fp.rotate_flux(R0.T, Q).T
+    scale = np.abs(R0).max(axis=1)
+    scale[2:5] = np.abs(R0[2:5]).max()
+    err = (np.abs(R1 - R0r).max(axis=1)) / scale
+    assert np.all(err < 1e-11), err
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+def test_discrete_conservation(ty, mode):
+    """Benchmark scheme (Roe + MUSCL-UNS + Barth) on the periodic TGV mesh: the sum over cells
+    of R V / dt vanishes to rounding."""
+    from typhon_gb300 import cases
+    md = tgv_mesh(ty, 8)
+    g = ty.Grid(md)
+    g.set_spat("ROE", "MUSCL-UNS", "NONE", "BARTH", mode=mode)
+    g.set_prim(cases.taylor_green(md.cell_centre))
+    dt = g.calc_zonetimestep(0.8)
+    nci = md.ncell_int
+    RV = g.integration_grid(dt) * md.cell_volume[:nci] / dt
+    total = np.abs(RV).sum(axis=1)
+    assert np.all(np.abs(RV.sum(axis=1)) <= 1e-13 * total), RV.sum(axis=1) / total
+    g.close()
+
+
+def test_isentropic_vortex_second_order(ty):
+    """The vortex2d case with the Roe flux (MUSCL, van Albada, RK4, fast mode) at t = 2 on 32,
+    64 and 128 triangles per side: the L1 density error against the translated exact vortex
+    falls at second order."""
+    from typhon_gb300 import cases
+    T = 2.0
+    errs = []
+    for n in (32, 64, 128):
+        raw = ty.gen_grid2d(n, n, 10.0, 10.0, "tri", jitter=0.1, seed=1234)
+        md = ty.preprocess(raw, 2, ty.periodic_box_bcs((10.0, 10.0)))
+        g = ty.Grid(md)
+        g.set_spat("ROE", "MUSCL", "ALBADA", mode="fast")
+        g.set_prim(cases.isentropic_vortex(md.cell_centre))
+        ns = int(np.ceil(T / g.calc_zonetimestep(0.8)))
+        for _ in range(ns):
+            g.treelevel_rungekutta("RK4", T / ns)
+        nci = md.ncell_int
+        ex = fp.vortex_exact(cases, md.cell_centre[:nci], T)
+        errs.append(fp.l1_density_error(g.get_prim()[0], ex[0], md.cell_volume[:nci]))
+        g.close()
+    orders = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
+    assert np.all(orders > 1.8), (errs, orders)
