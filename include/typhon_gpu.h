@@ -207,6 +207,12 @@ int ty_steady_iteration(ty_mesh* mesh, int32_t rk_method, double cfl, int32_t lo
  * which = 0 prim [5][ncell], 1 grad [15][ncell], 2 face flux*S [5][nface],
  *         3 limiter ratios [3][ncell] (Barth post-limiter). */
 int ty_debug_get(ty_mesh* mesh, int32_t which, double* out);
+/* The fast mode's reciprocal, reciprocal square root and square root (Newton-Raphson
+ * iterations from the hardware seeds) on n host values x, results in host y, on the current
+ * device; which = 0 1/x, 1 1/sqrt(x), 2 sqrt(x) (fast mode); 3, 4, 5 the same by CUDA's IEEE
+ * division and square root; 6, 7 the seeds alone (rcp.approx / rsqrt.approx).  For measuring
+ * the fast mode's rounding; no counterpart in the reference. */
+int ty_debug_fastmath(int32_t which, int32_t n, const double* x, double* y);
 
 /* Inlet / outlet parameters per face: host [nface][6] (see ty_bc; rows of other faces are
  * ignored).  Required before a Navier-Stokes operation on a mesh with inlets or outlets. */

@@ -157,16 +157,66 @@ def test_fast_mode_vortex_full_size(ty):
     assert np.all(rel <= FAST_RTOL), rel
 
 
-def test_fast_mode_tgv_benchmark_size(ty):
-    """The benchmarked configuration at its full size: TGV 64^3 x 5 = 1,310,720 tetrahedra,
-    Roe + MUSCL-UNS + Barth, SSP-RK3 at CFL 0.8, time step on the device; 20 steps in fast
-    mode (the bench's mode) against the oracle, 1e-12 relative L2 per conserved variable."""
-    md, om, prim = make_case(ty, "tgv", 64)
+@pytest.fixture(scope="module")
+def tgv64(ty):
+    """The benchmarked mesh: TGV 64^3 x 5 = 1,310,720 tetrahedra (built once per module)."""
+    return make_case(ty, "tgv", 64)
+
+
+def test_exact_mode_tgv_benchmark_size_bitwise(ty, tgv64):
+    """The benchmarked configuration at its full size (TGV 64^3 x 5, Roe + MUSCL-UNS + Barth,
+    SSP-RK3 at CFL 0.8, time step on the device): 20 steps in exact mode are bit-identical to
+    the oracle's, time steps included."""
+    md, om, prim = tgv64
+    g, s = pair(ty, md, om, prim, "ROE", "MUSCL-UNS", "NONE", "BARTH", mode="exact", rk="RK3-SSP")
+    dt_last = g.run_steps("RK3-SSP", 0.8, 20)
+    dts = s.run_steps(20)
+    assert dt_last == dts[-1]
+    assert np.array_equal(g.get_cons(), s.get("cons")[:, :md.ncell_int])
+    g.close()
+
+
+def test_fast_mode_tgv_benchmark_size(ty, tgv64):
+    """Fast mode (the bench's mode) at the benchmarked size.
+
+    This configuration amplifies rounding differences: Typhon's Barth ratio divides neighbour
+    differences of the pressure (about 71.4 at M = 0.1, varying by 1e-3 relative) by face
+    increments, so a last-bit change of the state moves ratios by up to 1e-7 relative, and a
+    difference of one unit in the last place grows about 2.4x per step.  The oracle shows it
+    against itself: its own state with the density raised by one ulp in every cell differs
+    from it by about 1e-7 (momentum) after 20 steps.  So the fast mode is held to
+    * 1e-12 relative L2 per conserved variable after 5 steps from the initial state;
+    * 1e-12 for one step started from the oracle's state, at steps 0, 10 and 19;
+    * after 20 steps, at most 30 times the oracle's own one-ulp divergence (its twin run).
+    The exact mode is bit-identical over the 20 steps (test above)."""
+    md, om, prim = tgv64
+    nci = md.ncell_int
     g, s = pair(ty, md, om, prim, "ROE", "MUSCL-UNS", "NONE", "BARTH", mode="fast", rk="RK3-SSP")
-    g.run_steps("RK3-SSP", 0.8, 20)
-    s.run_steps(20)
-    rel = relerr(g.get_cons(), s.get("cons")[:, :md.ncell_int])
-    assert np.all(rel <= FAST_RTOL), rel
+    # twin: the oracle from the same state with the density raised by one ulp in every cell
+    twin = op.Solver(om, OSCH["ROE"], OHRES["MUSCL-UNS"], OLIM["NONE"], OPOST["BARTH"], op.GRAD_LSQ,
+                     rk="RK3-SSP", cfl=0.8)
+    c0 = s.get("cons").copy()
+    c0[0, :nci] = np.nextafter(c0[0, :nci], np.inf)
+    twin.set_cons(c0)
+    g.run_steps("RK3-SSP", 0.8, 5)
+    states, dts = [s.get("cons").copy()], []
+    for k in range(20):
+        dts.append(s.timestep())
+        s.rk_step(dts[-1])
+        twin.rk_step(dts[-1])
+        states.append(s.get("cons").copy())
+    rel5 = relerr(g.get_cons(), states[5][:, :nci])
+    assert np.all(rel5 <= FAST_RTOL), rel5
+    g.run_steps("RK3-SSP", 0.8, 15)
+    rel20 = relerr(g.get_cons(), states[20][:, :nci])
+    rel_twin = relerr(twin.get("cons")[:, :nci], states[20][:, :nci])
+    assert rel20.max() <= 30 * rel_twin.max(), (rel20, rel_twin)
+    for k in (0, 10, 19):
+        g.set_cons(states[k][:, :nci])
+        g.treelevel_rungekutta("RK3-SSP", dts[k])
+        rel1 = relerr(g.get_cons(), states[k + 1][:, :nci])
+        assert np.all(rel1 <= FAST_RTOL), (k, rel1)
+    g.close()
 
 
 def test_fast_mode_tgv_small(ty):

@@ -62,12 +62,13 @@ def test_consistency_uniform_state(ty, mode, highres, limiter, postlim):
 
 
 @pytest.mark.parametrize("mode", ["exact", "fast"])
-@pytest.mark.parametrize("highres,limiter", [("NONE", "NONE"), ("MUSCL-UNS", "NONE"), ("MUSCL", "ALBADA")])
+@pytest.mark.parametrize("highres,limiter", [("NONE", "NONE"), ("MUSCL-UNS", "NONE"), ("MUSCL", "NONE")])
 def test_rotational_invariance_of_the_residual(ty, mode, highres, limiter):
     """The TGV state on a rigidly rotated copy of the mesh (periodic translations rotated too):
     the residual's density and energy rows are unchanged and its momentum rows are rotated,
-    to rounding.  (Barth's post-limiter limits vector components one by one and is not
-    rotation invariant, so it is left out.)"""
+    to rounding.  (Typhon's limiters and its Barth post-limiter act on the velocity one
+    Cartesian component at a time, LIMITER.f90 scalar forms and postlim_barth.f90, so they
+    are not rotation invariant and are left out.)"""
     from typhon_gb300 import cases
     rng = np.random.default_rng(11)
     Q = fp.random_rotation(rng)

@@ -607,6 +607,8 @@ int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
   h->o.scheme = p->scheme; h->o.highres = p->highres; h->o.limiter = p->limiter; h->o.postlim = p->postlim;
   h->o.gradmeth = p->gradmeth; h->o.mode = p->mode; h->o.gamma = p->gamma; h->o.entropy_fix = p->entropy_fix;
   h->o.inv_entropy_fix = p->entropy_fix > 0.0 ? 1.0 / p->entropy_fix : 0.0;
+  h->o.ig1 = 1.0 / (p->gamma - 1.0);
+  h->o.gig1 = p->gamma * h->o.ig1;
   h->o.viscous = p->viscous; h->o.visc_law = p->visc_law; h->o.visc_kin = p->visc_kin;
   h->o.rgas = p->rgas; h->o.prandtl = p->prandtl;
   for (int v = 0; v < 5; ++v) h->o.farfield[v] = p->farfield[v];

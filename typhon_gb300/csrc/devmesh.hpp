@@ -77,6 +77,7 @@ struct SpatOpts {
   int scheme, highres, limiter, postlim, gradmeth, mode;
   double gamma, entropy_fix;
   double inv_entropy_fix;  // 1 / entropy_fix (fast-mode Roe flux)
+  double ig1, gig1;        // 1 / (gamma - 1), gamma / (gamma - 1) (fast-mode fluxes)
   int viscous, visc_law;
   double visc_kin, rgas, prandtl;
   double farfield[5];  // free stream of far-field faces (rho, p, u, v, w)

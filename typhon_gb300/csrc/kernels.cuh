@@ -24,6 +24,7 @@
 
 #include "../../include/typhon_gpu.h"
 #include "devmesh.hpp"
+#include "fastmath.cuh"
 
 #ifndef TY_KNS
 #error "define TY_KNS and TY_FAST before including kernels.cuh"
@@ -114,7 +115,7 @@ __device__ __forceinline__ void cons_to_prim(double gamma, const double c[5], do
   double rho = c[0];
   double vx, vy, vz;
   if constexpr (kFast) {
-    const double ir = 1.0 / rho;
+    const double ir = rcp_nr(rho);
     vx = c[2] * ir; vy = c[3] * ir; vz = c[4] * ir;
   } else {
     vx = c[2] / rho; vy = c[3] / rho; vz = c[4] / rho;
@@ -624,32 +625,37 @@ __device__ void flux_roe(double g, double eps, const double* L, const double* R,
 // so reciprocals, reconstruction weights and geometric factors are precomputed once
 // (HBM-resident) and the per-stage work avoids divisions.
 
-// Roe flux with shared reciprocals: 1 division + 3 reciprocal square roots per face.
-__device__ void flux_roe_fast(double g, double eps, double ieps, const double* L, const double* R, double nx,
-                              double ny, double nz, double S, double* F) {
-  const double ig1 = 1.0 / (g - 1.0), gig1 = g * ig1;
-  const double rL = rsqrt(L[0]), rR = rsqrt(R[0]);
+// Roe flux with shared reciprocals: no division, 1 reciprocal and 3 reciprocal square roots
+// by Newton-Raphson steps (fastmath.cuh) per face.  The same flux as flux_roe, regrouped so
+// that the central and dissipative parts share their products:
+//   2 F_mass = m_L + m_R - d_mass                       (m = rho u.n)
+//   2 F_ener = m_L H_L + m_R H_R - d_ener               (rho u.n (rho E + p) = m H)
+//   2 F_mom  = A u_L + B u_R + c_n n, with the Roe velocity u~ = k_L u_L + k_R u_R and the
+//              shear jump written through u_R - u_L:
+//              A = m_L + ws - d_mass k_L, B = m_R - ws - d_mass k_R,
+//              c_n = p_L + p_R - (w5 - w1) a + ws (u_R - u_L).n
+__device__ void flux_roe_fast(const SpatOpts& o, const double* L, const double* R, double nx, double ny, double nz,
+                              double S, double* F) {
+  const double g1 = o.gamma - 1.0, eps = o.entropy_fix, ieps = o.inv_entropy_fix, gig1 = o.gig1;
+  const double rL = rsqrt_nr(L[0]), rR = rsqrt_nr(R[0]);
   const double sL = L[0] * rL, sR = R[0] * rR;   // sqrt(rho)
   const double iL = rL * rL, iR = rR * rR;       // 1/rho
-  const double inv = 1.0 / (sL + sR);
+  const double inv = rcp_nr(sL + sR);
   const double kl = sL * inv, kr = sR * inv;
   const double rroe = sL * sR;
   const double ux = kl * L[2] + kr * R[2], uy = kl * L[3] + kr * R[3], uz = kl * L[4] + kr * R[4];
   const double sqL = L[2] * L[2] + L[3] * L[3] + L[4] * L[4];
   const double sqR = R[2] * R[2] + R[3] * R[3] + R[4] * R[4];
-  const double hl = gig1 * L[1] * iL + 0.5 * sqL, hr = gig1 * R[1] * iR + 0.5 * sqR;
+  const double hl = (gig1 * L[1]) * iL + 0.5 * sqL, hr = (gig1 * R[1]) * iR + 0.5 * sqR;
   const double hroe = kl * hl + kr * hr;
   const double q2 = ux * ux + uy * uy + uz * uz;
-  const double a2 = (g - 1.0) * (hroe - 0.5 * q2);
-  const double ra = rsqrt(a2), a = a2 * ra, ia2 = ra * ra;
+  const double a2 = g1 * (hroe - 0.5 * q2);
+  const double ra = rsqrt_nr(a2), a = a2 * ra, ia2 = ra * ra;
   const double vn = ux * nx + uy * ny + uz * nz;
   const double vnl = L[2] * nx + L[3] * ny + L[4] * nz, vnr = R[2] * nx + R[3] * ny + R[4] * nz;
-  const double rel = ig1 * L[1] + 0.5 * L[0] * sqL, rer = ig1 * R[1] + 0.5 * R[0] * sqR;
   const double drho = R[0] - L[0], dp = R[1] - L[1], dvn = vnr - vnl;
-  const double dux = R[2] - L[2], duy = R[3] - L[3], duz = R[4] - L[4];
   const double h = 0.5 * ia2, rad = rroe * a * dvn;
   const double al1 = (dp - rad) * h, al5 = (dp + rad) * h, al2 = drho - dp * ia2;
-  const double dutx = dux - dvn * nx, duty = duy - dvn * ny, dutz = duz - dvn * nz;
   double l1 = fabs(vn - a), l5 = fabs(vn + a);
   const double l2 = fabs(vn);
   const double delta = eps * a;
@@ -662,38 +668,40 @@ __device__ void flux_roe_fast(double g, double eps, double ieps, const double* L
   const double w1 = l1 * al1, w2 = l2 * al2, w5 = l5 * al5, ws = l2 * rroe;
   const double d_mass = w1 + w2 + w5;
   const double wa = (w5 - w1) * a;
-  const double dmx = d_mass * ux + wa * nx + ws * dutx;
-  const double dmy = d_mass * uy + wa * ny + ws * duty;
-  const double dmz = d_mass * uz + wa * nz + ws * dutz;
-  const double d_ener = (w1 + w5) * hroe + wa * vn + w2 * (0.5 * q2) + ws * ((ux * dux + uy * duy + uz * duz) - vn * dvn);
   const double ml = vnl * L[0], mr = vnr * R[0];
-  const double pp = L[1] + R[1];
   const double hs = 0.5 * S;  // flux times surface: the 1/2 of the Roe average folded in
+  // momentum
+  const double A = ml + ws - d_mass * kl, B = mr - ws - d_mass * kr;
+  const double cn = (L[1] + R[1]) - wa + ws * dvn;
+  F[2] = hs * (A * L[2] + B * R[2] + cn * nx);
+  F[3] = hs * (A * L[3] + B * R[3] + cn * ny);
+  F[4] = hs * (A * L[4] + B * R[4] + cn * nz);
+  // energy
+  const double udu = ux * (R[2] - L[2]) + uy * (R[3] - L[3]) + uz * (R[4] - L[4]);
+  const double d_ener = (w1 + w5) * hroe + wa * vn + w2 * (0.5 * q2) + ws * (udu - vn * dvn);
+  F[1] = hs * (ml * hl + mr * hr - d_ener);
   F[0] = hs * (ml + mr - d_mass);
-  F[1] = hs * (vnl * (rel + L[1]) + vnr * (rer + R[1]) - d_ener);
-  F[2] = hs * (ml * L[2] + mr * R[2] + pp * nx - dmx);
-  F[3] = hs * (ml * L[3] + mr * R[3] + pp * ny - dmy);
-  F[4] = hs * (ml * L[4] + mr * R[4] + pp * nz - dmz);
 }
 
-// HLLC (calc_flux_hllc.f90 with beta = 1) with shared reciprocals: 3 divisions,
-// 3 square roots and 2 reciprocal square roots per face.
-__device__ void flux_hllc_fast(double g, const double* L, const double* R, double nx, double ny, double nz,
+// HLLC (calc_flux_hllc.f90 with beta = 1) with shared reciprocals: no division; 3
+// reciprocals, 3 square roots and 2 reciprocal square roots by Newton-Raphson iterations
+// (fastmath.cuh) per face.
+__device__ void flux_hllc_fast(const SpatOpts& o, const double* L, const double* R, double nx, double ny, double nz,
                                double* F) {
-  const double ig1 = 1.0 / (g - 1.0), gig1 = g * ig1;
-  const double rL = rsqrt(L[0]), rR = rsqrt(R[0]);
+  const double g = o.gamma, ig1 = o.ig1, gig1 = o.gig1;
+  const double rL = rsqrt_nr(L[0]), rR = rsqrt_nr(R[0]);
   const double sL = L[0] * rL, sR = R[0] * rR;
   const double iL = rL * rL, iR = rR * rR;
-  const double inv = 1.0 / (sL + sR);
+  const double inv = rcp_nr(sL + sR);
   const double kl = sL * inv, kr = sR * inv;
   const double rux = kl * L[2] + kr * R[2], ruy = kl * L[3] + kr * R[3], ruz = kl * L[4] + kr * R[4];
   const double sqL = L[2] * L[2] + L[3] * L[3] + L[4] * L[4];
   const double sqR = R[2] * R[2] + R[3] * R[3] + R[4] * R[4];
   const double hroe = kl * (gig1 * L[1] * iL + 0.5 * sqL) + kr * (gig1 * R[1] * iR + 0.5 * sqR);
   const double vnl = L[2] * nx + L[3] * ny + L[4] * nz, vnr = R[2] * nx + R[3] * ny + R[4] * nz;
-  const double al = sqrt(g * L[1] * iL), ar = sqrt(g * R[1] * iR);
+  const double al = sqrt_nr(g * L[1] * iL), ar = sqrt_nr(g * R[1] * iR);
   const double vm = rux * nx + ruy * ny + ruz * nz;
-  const double am = sqrt((g - 1.0) * (hroe - 0.5 * (rux * rux + ruy * ruy + ruz * ruz)));
+  const double am = sqrt_nr((g - 1.0) * (hroe - 0.5 * (rux * rux + ruy * ruy + ruz * ruz)));
   const double rel = ig1 * L[1] + 0.5 * L[0] * sqL, rer = ig1 * R[1] + 0.5 * R[0] * sqR;
   const double sl = fmin(vnl - al, vm - am), sr = fmax(vnr + ar, vm + am);
   if (sl >= 0.0) {
@@ -706,11 +714,11 @@ __device__ void flux_hllc_fast(double g, const double* L, const double* R, doubl
     F[2] = m0 * R[2] + R[1] * nx; F[3] = m0 * R[3] + R[1] * ny; F[4] = m0 * R[4] + R[1] * nz;
   } else {
     const double rqL = L[0] * (sl - vnl), rqR = R[0] * (sr - vnr);
-    const double Sst = (rqR * vnr - rqL * vnl - R[1] + L[1]) / (rqR - rqL);
+    const double Sst = (rqR * vnr - rqL * vnl - R[1] + L[1]) * rcp_nr(rqR - rqL);
     const bool left = Sst >= 0.0;
     const double* Q = left ? L : R;
     const double rq = left ? rqL : rqR, s = left ? sl : sr, vnq = left ? vnl : vnr, re = left ? rel : rer;
-    const double iks = 1.0 / (s - Sst);
+    const double iks = rcp_nr(s - Sst);
     const double pst = Q[1] - rq * (vnq - Sst);
     const double dp = pst - Q[1];
     const double m0 = Sst * iks;
@@ -815,10 +823,10 @@ __device__ __forceinline__ void face_flux_fast(const DevMesh& m, const DevState&
   double F[5];
   const double S = m.fs[f];
   if (o.scheme == TY_SCH_ROE && o.viscous == TY_VISC_NONE) {
-    flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, S, F);
+    flux_roe_fast(o, QL, QR, nx, ny, nz, S, F);
   } else {
-    if (o.scheme == TY_SCH_ROE) flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, 1.0, F);
-    else if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
+    if (o.scheme == TY_SCH_ROE) flux_roe_fast(o, QL, QR, nx, ny, nz, 1.0, F);
+    else if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_HLLE) flux_hlle(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_AUSMM) flux_ausmm(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
@@ -836,11 +844,11 @@ __device__ __forceinline__ void face_flux(const DevMesh& m, const DevState& s, c
   const double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
   double F[5];
   if constexpr (kFast) {
-    if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o.gamma, QL, QR, nx, ny, nz, F);
+    if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_HLLE) flux_hlle(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_AUSMM) flux_ausmm(o.gamma, QL, QR, nx, ny, nz, F);
-    else flux_roe_fast(o.gamma, o.entropy_fix, o.inv_entropy_fix, QL, QR, nx, ny, nz, 1.0, F);  // unit surface
+    else flux_roe_fast(o, QL, QR, nx, ny, nz, 1.0, F);  // unit surface
   } else {
     if (o.scheme == TY_SCH_HLLC) flux_hllc(o.gamma, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
@@ -1005,16 +1013,21 @@ __device__ __forceinline__ void delta_fast(const DevMesh& m, const SpatOpts& o, 
 // Fused per-cell kernel: least-squares gradient (A^-1 d weights), face increments on every
 // face of the cell, Barth-type ratio without per-face divisions, and the limited face
 // states written once per face side (cl for the fc1 side, cr for the fc2 side).
+// The neighbour differences dq of the gradient pass and the increments are staged in shared
+// memory ([slot*5+var][thread], conflict-free), so each is computed once and the kernel keeps
+// few registers live (four blocks of 128 threads per SM).
 // The ratio min_f max(klim (q_nb - q_c)/increment, 0) is tracked as a fraction n/d; the
 // comparisons run on the integer pipe (positive finite doubles order like their bit
-// patterns), leaving the FP64 pipe to the arithmetic.  One division per variable group.
-// The increments are staged in shared memory ([slot*5+var][thread], conflict-free) so the
-// kernel keeps few registers live and runs two or more blocks per SM.
+// patterns), leaving the FP64 pipe to the arithmetic, and the one division per variable
+// group is a Newton-Raphson reciprocal.  The increment is the reconstruction's value (the
+// exact mode, like Typhon, rounds it through the face value first); an increment of exactly
+// zero imposes no constraint in both modes.
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
 
 template <int NS, int BLK>
-__global__ void __launch_bounds__(BLK, 2) k_cell_fast(DevMesh m, DevState s, SpatOpts o, double klim) {
+__global__ void __launch_bounds__(BLK, 512 / BLK) k_cell_fast(DevMesh m, DevState s, SpatOpts o, double klim) {
   __shared__ double sD[NS * 5][BLK];
+  __shared__ double sQ[NS * 5][BLK];
   const int c = blockIdx.x * BLK + threadIdx.x;
   if (c >= m.nci) return;
   const int t = threadIdx.x;
@@ -1032,12 +1045,15 @@ __global__ void __launch_bounds__(BLK, 2) k_cell_fast(DevMesh m, DevState s, Spa
     if (e < 0) break;
     ns = sl + 1;
     const int f = e >> 1, side = e & 1, nb = m.cfn[sl * ni + c];
-    const double wx = m.lsqw[(3 * side) * lf + f], wy = m.lsqw[(3 * side + 1) * lf + f];
-    const double wz = m.lsqw[(3 * side + 2) * lf + f];
+    // q(fc2) - q(fc1) = +-dq: the weight's sign flipped on the integer pipe for side 1
+    const long long sb = (long long)side << 63;
+    const double wx = __longlong_as_double(__double_as_longlong(m.lsqw[(3 * side) * lf + f]) ^ sb);
+    const double wy = __longlong_as_double(__double_as_longlong(m.lsqw[(3 * side + 1) * lf + f]) ^ sb);
+    const double wz = __longlong_as_double(__double_as_longlong(m.lsqw[(3 * side + 2) * lf + f]) ^ sb);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      double dq = prim[v * ld + nb] - qc[v];
-      dq = side ? -dq : dq;  // q(fc2) - q(fc1)
+      const double dq = prim[v * ld + nb] - qc[v];
+      sQ[sl * 5 + v][t] = dq;
       gr[3 * v] = fma(dq, wx, gr[3 * v]);
       gr[3 * v + 1] = fma(dq, wy, gr[3 * v + 1]);
       gr[3 * v + 2] = fma(dq, wz, gr[3 * v + 2]);
@@ -1049,15 +1065,14 @@ __global__ void __launch_bounds__(BLK, 2) k_cell_fast(DevMesh m, DevState s, Spa
   double bn[3] = {1.0, 1.0, 1.0}, bd[3] = {klim, klim, klim};
   bool zero[3] = {false, false, false};
   for (int sl = 0; sl < ns; ++sl) {
-    const int e = m.cf[sl * ni + c], f = e >> 1, side = e & 1, nb = m.cfn[sl * ni + c];
+    const int e = m.cf[sl * ni + c], f = e >> 1, side = e & 1;
     double dq[5], D[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) dq[v] = prim[v * ld + nb] - qc[v];
+    for (int v = 0; v < 5; ++v) dq[v] = sQ[sl * 5 + v][t];
     delta_fast(m, o, f, side, gr, dq, D);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      // increment as the rounded face value minus the cell value, as Typhon forms it
-      const double den = (qc[v] + D[v]) - qc[v];
+      const double den = D[v];
       sD[sl * 5 + v][t] = den;
       if (barth) {
         const int k = v < 2 ? v : 2;
@@ -1076,7 +1091,7 @@ __global__ void __launch_bounds__(BLK, 2) k_cell_fast(DevMesh m, DevState s, Spa
   double r[3] = {1.0, 1.0, 1.0};
   if (barth) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) r[k] = zero[k] ? 0.0 : fmin(1.0, klim * bn[k] / bd[k]);
+    for (int k = 0; k < 3; ++k) r[k] = zero[k] ? 0.0 : fmin(1.0, klim * bn[k] * rcp_nr(bd[k]));
 #pragma unroll
     for (int k = 0; k < 3; ++k) s.ratio[k * ld + c] = r[k];
   }
@@ -1159,6 +1174,14 @@ __device__ __forceinline__ bool cell_dt(const DevMesh& m, double gamma, double c
   double d;
   if constexpr (kFast) d = cfl * m.geo2[c];
   else d = cfl * 2.0 * m.cvol[c] / m.sumS[c];
+  if constexpr (kFast) {
+    const double irho = rcp_nr(u[0]);
+    const double rv2 = u[2] * u[2] + u[3] * u[3] + u[4] * u[4];
+    const double a2 = (u[1] - 0.5 * rv2 * irho) * gg1 * irho;
+    if (!(a2 > 0.0)) return false;
+    dt = d * rcp_nr(sqrt_nr(rv2) * irho + sqrt_nr(a2));
+    return true;
+  }
   double irho = 1.0 / u[0];
   double rv2 = u[2] * u[2] + u[3] * u[3] + u[4] * u[4];
   double a2 = (u[1] - 0.5 * rv2 * irho) * gg1 * irho;
@@ -1227,11 +1250,16 @@ __global__ void __launch_bounds__(kBlock) k_rk_update(DevMesh m, DevState s, RkS
     double R[5];
     gather_residual(m, s, c, R);
     const double dtv = plan.dtloc ? plan.dtloc[c] : load_dt(dt, dtbits);
-    double coef;
-    if constexpr (kFast) coef = dtv * m.invV[c];
-    else coef = dtv / m.cvol[c];
+    // exact: R = (dt/V) R first, as flux_to_res does; fast: dt/V folded into each stage
+    // coefficient (one product per coefficient instead of one per variable)
+    double coef, rs = 1.0;
+    if constexpr (kFast) {
+      rs = dtv * m.invV[c];
+    } else {
+      coef = dtv / m.cvol[c];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) R[v] = coef * R[v];
+      for (int v = 0; v < 5; ++v) R[v] = coef * R[v];
+    }
     double u0[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) u0[v] = s.u0[v * ld + c];
@@ -1240,19 +1268,21 @@ __global__ void __launch_bounds__(kBlock) k_rk_update(DevMesh m, DevState s, RkS
     for (int k = 0; k < plan.nops; ++k) {
       const RkOp op = plan.ops[k];
       double* part = s.pk[op.target];
+      const double oc = kFast ? op.c * rs : op.c;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         double base = op.from_u0 ? u0[v] : part[v * ld + c];
-        double val = base + op.c * R[v];
+        double val = base + oc * R[v];
         if (op.is_next) next[v] = val;
         else part[v * ld + c] = val;
       }
       if (op.is_next) have_next = true;
     }
     if (plan.has_acc) {
+      const double ca = kFast ? plan.c_acc * rs : plan.c_acc;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        double a = plan.acc_init ? plan.c_acc * R[v] : s.acc[v * ld + c] + plan.c_acc * R[v];
+        double a = plan.acc_init ? ca * R[v] : s.acc[v * ld + c] + ca * R[v];
         if (plan.final_stage) next[v] = u0[v] + a;
         if (!plan.final_stage || plan.store_acc) s.acc[v * ld + c] = a;
       }
@@ -1299,11 +1329,11 @@ cudaError_t residual_faces(const DevMesh& m, const DevState& s, const SpatOpts& 
     const double klim = o.postlim == TY_POSTLIM_SUPERBARTH ? 1.0 : 0.5;
     if (m.nslot <= 4)
       pr->launch(K_CELL_FAST, st, [&] {
-        k_cell_fast<4, 256><<<(unsigned)((m.nci + 255) / 256), 256, 0, st>>>(m, s, o, klim);
+        k_cell_fast<4, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim);
       });
     else
       pr->launch(K_CELL_FAST, st, [&] {
-        k_cell_fast<8, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim);
+        k_cell_fast<8, 64><<<(unsigned)((m.nci + 63) / 64), 64, 0, st>>>(m, s, o, klim);
       });
     if (o.viscous != TY_VISC_NONE && m.ng > 0)
       pr->launch(K_GHOST_GRAD, st, [&] { k_ghost_grad<<<nblk(m.ng), kBlock, 0, st>>>(m, s.grad); });
