@@ -252,9 +252,14 @@ typedef enum {
 } ty_krylov;
 typedef enum {
   TY_PREC_FP64 = 0,      /* everything in FP64 */
-  TY_PREC_MIXED = 1      /* TY_KRYLOV_FGMRES only: FP32 blocks, mat-vec, preconditioner and
+  TY_PREC_MIXED = 1,     /* TY_KRYLOV_FGMRES only: FP32 blocks, mat-vec, preconditioner and
                             Krylov basis (swept in FP32, FP64 block sums); FP64 residual of the
                             step and of each restart, Hessenberg algebra and update */
+  TY_PREC_MIXED_FP64ORTHO = 2  /* TY_KRYLOV_FGMRES only: FP32 blocks, FP32 Jacobian-vector
+                            products and FP32 block-Jacobi preconditioner (FP32 preconditioned
+                            vectors); the Krylov basis, its orthogonalisation (two sweeps,
+                            measured Gram matrix), the residuals, the Hessenberg algebra and the
+                            update in FP64 */
 } ty_precision;
 typedef struct ty_imp_params {
   int32_t krylov;        /* ty_krylov (INVERSION = GMRES is TY_KRYLOV_GMRES) */
@@ -324,8 +329,16 @@ int ty_kdif_get_temperature(ty_mesh* mesh, double* T);         /* host [ncell_in
 /* residual dt/V sum(+-F S) of U = Cp T (host [ncell_int], may be NULL) */
 int ty_kdif_residual(ty_mesh* mesh, double dt, double* R);
 typedef enum {
-  TY_KSOLVE_CG = 0,          /* conjugate gradients + Jacobi, FP64 (new: Typhon has CGS/BiCG/GMRES) */
-  TY_KSOLVE_CG32_REFINE = 1  /* FP32 conjugate gradients inside FP64 iterative refinement */
+  TY_KSOLVE_CG = 0,          /* conjugate gradients + Jacobi, FP64 (new: Typhon has CGS/BiCG/GMRES):
+                                Chronopoulos-Gear single-reduction form, two launches per
+                                iteration, no host round trip between checks */
+  TY_KSOLVE_CG32_REFINE = 1, /* FP32 conjugate gradients inside FP64 iterative refinement */
+  TY_KSOLVE_CG_MIXED = 2     /* TY_KSOLVE_CG on the face conductances stored in FP32 (FP64
+                                vectors and arithmetic; the difference form keeps the matrix
+                                spectrally within 1e-7 of the FP64 one) until the relative
+                                residual is below 1e-6, then the FP64 residual replaces the
+                                recurrence's and the iteration continues on the FP64 matrix
+                                (stats.refinements = 1 when it switched) */
 } ty_kdif_solver;
 typedef struct ty_kdif_solve {
   int32_t solver;        /* ty_kdif_solver */

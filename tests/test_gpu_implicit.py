@@ -205,6 +205,7 @@ def _dense(s, nc):
 @pytest.mark.parametrize("inversion,precision,mode,tol", [("FGMRES", "fp64", "exact", 1e-9),
                                                           ("FGMRES", "fp64", "fast", 1e-9),
                                                           ("FGMRES", "mixed", "fast", 1e-5),
+                                                          ("FGMRES", "mixed-fp64ortho", "fast", 1e-5),
                                                           ("GMRES", "fp64", "fast", 1e-9)])
 def test_krylov_solution_against_dense_solve(ty, golden_dir, inversion, precision, mode, tol):
     """The update of one implicit step against a dense solve of the oracle's BDLU system."""
@@ -224,7 +225,8 @@ def test_krylov_solution_against_dense_solve(ty, golden_dir, inversion, precisio
 
 @pytest.mark.parametrize("inversion,precision,scheme,highres,steps",
                          [("GMRES", "fp64", "RUSANOV", "NONE", 20), ("FGMRES", "fp64", "RUSANOV", "NONE", 20),
-                          ("FGMRES", "mixed", "RUSANOV", "NONE", 25), ("JFNK", "fp64", "RUSANOV", "NONE", 20),
+                          ("FGMRES", "mixed", "RUSANOV", "NONE", 25), ("FGMRES", "mixed-fp64ortho", "RUSANOV", "NONE", 25),
+                          ("JFNK", "fp64", "RUSANOV", "NONE", 20),
                           ("JFNK", "fp64", "HLLC", "MUSCL", 30)])
 def test_steady_convergence(ty, golden_dir, inversion, precision, scheme, highres, steps):
     """Implicit steps with a growing CFL drive a perturbed free stream through far-field
@@ -260,4 +262,8 @@ def test_implicit_errors(ty, golden_dir):
     with pytest.raises(ty.TyphonError):            # nothing assembled in FP64 yet
         g.implicit_matvec(np.zeros((md.ncell_int, 5)))
     st = g.implicit_step(1.0, "FGMRES", nkrylov=30, precision="mixed")
+    assert st["lin_res"] <= 1e-4
+    with pytest.raises(ty.TyphonError):            # the FP64-basis mixed form is FGMRES only too
+        g.implicit_step(1.0, "JFNK", precision="mixed-fp64ortho")
+    st = g.implicit_step(1.0, "FGMRES", nkrylov=30, precision="mixed-fp64ortho")
     assert st["lin_res"] <= 1e-4

@@ -81,21 +81,28 @@ def test_exact_kdif_bitwise(ty, scheme):
     assert np.linalg.norm(dT - dTo) / np.linalg.norm(dTo) < 1e-11
 
 
-def test_fp32_cg_with_refinement_reaches_fp64(ty):
+@pytest.mark.parametrize("solver", ["CG32", "CG-MIXED"])
+def test_mixed_precision_solvers_reach_fp64(ty, solver):
+    """FP32 CG inside FP64 refinement, and CG on FP32 face conductances switched to the FP64
+    matrix at 1e-6 (residual replacement): both reach the FP64 CG solution, to 1e-12 on the
+    FP64 system."""
     md, om, kind, val, kc, T0 = box_case(ty, n=8)
+    kc = kc * np.exp(np.random.default_rng(3).standard_normal(kc.shape))   # heterogeneous k
     sols = {}
-    for solver in ("CG", "CG32"):
+    for sv in ("CG", solver):
         g = ty.Grid(md)
         g.set_spat("HLLC", mode="fast")
         g.kdif_setup(kc, kind, val, flux="FULL", heat_capacity=1.0)
         g.kdif_set_temperature(T0)
         for _ in range(3):
-            st = g.kdif_implicit_step(1e-2, solver, tol=1e-12)
+            st = g.kdif_implicit_step(1e-2, sv, tol=1e-12)
             assert st["rel_res"] < 1e-12, st
-        sols[solver] = g.kdif_temperature()
-        if solver == "CG32":
-            assert st["refinements"] >= 2
-    assert np.linalg.norm(sols["CG32"] - sols["CG"]) / np.linalg.norm(sols["CG"]) < 1e-11
+            if sv == "CG32":
+                assert st["refinements"] >= 2
+            if sv == "CG-MIXED":
+                assert st["refinements"] == 1     # switched from FP32 to FP64 conductances
+        sols[sv] = g.kdif_temperature()
+    assert np.linalg.norm(sols[solver] - sols["CG"]) / np.linalg.norm(sols["CG"]) < 1e-11
 
 
 def test_fast_kdif_close(ty):

@@ -12,10 +12,11 @@
 //   TY_KRYLOV_GMRES   Typhon's bdlu_gmres (SOURCE/MATH/bdlu_gmres.f90:50-217): restarted
 //                     GMRES(NKRYLOV), modified Gram-Schmidt, Givens rotations, x0 = b/diag,
 //                     its stopping test and restart limit, no preconditioner, FP64.
-//   TY_KRYLOV_FGMRES  flexible GMRES(m) with classical Gram-Schmidt applied twice (CGS2) and
-//                     right block-Jacobi preconditioning on the assembled BDLU matrix; FP64, or
-//                     mixed: FP32 blocks, FP32 mat-vec and preconditioner, FP64 basis,
-//                     orthogonalisation and update (new).
+//   TY_KRYLOV_FGMRES  flexible GMRES(m) with right block-Jacobi preconditioning on the
+//                     assembled BDLU matrix (new), its basis orthogonalised through a measured
+//                     Gram matrix; FP64, or mixed: FP32 blocks, FP32 mat-vec and preconditioner,
+//                     with the basis in FP64 (TY_PREC_MIXED_FP64ORTHO) or in FP32
+//                     (TY_PREC_MIXED); residuals, Hessenberg algebra and update in FP64.
 //   TY_KRYLOV_JFNK    the same flexible GMRES with Jacobian-free products
 //                     J z = z - (R(U + eps z) - R(U)) / eps of the full FP64 residual,
 //                     block-Jacobi preconditioned with the assembled diagonal blocks (new;
@@ -105,8 +106,9 @@ int ensure_buffers(ty_mesh* h, const ty_imp_params* p) {
   const DevMesh& m = h->m;
   int rc;
   if (!im.lists && (rc = build_lists(h))) return rc;
-  const bool need64 = !(p->krylov == TY_KRYLOV_FGMRES && p->precision == TY_PREC_MIXED);
-  const bool need32 = p->krylov == TY_KRYLOV_FGMRES && p->precision == TY_PREC_MIXED;
+  const bool need32 = p->krylov == TY_KRYLOV_FGMRES && p->precision != TY_PREC_FP64;  // FP32 blocks
+  const bool need64 = !need32;
+  const bool basis32 = p->krylov == TY_KRYLOV_FGMRES && p->precision == TY_PREC_MIXED;  // FP32 basis
   if (need64 && !im.fp64_blocks) {
     if ((rc = h->alloc(im.upper, (size_t)std::max(m.nfi, 1) * kBlk)) ||
         (rc = h->alloc(im.lower, (size_t)std::max(m.nfi, 1) * kBlk)) ||
@@ -124,15 +126,14 @@ int ensure_buffers(ty_mesh* h, const ty_imp_params* p) {
   const size_t n = 5 * (size_t)m.nci;
   const int nk = p->krylov == TY_KRYLOV_BICGSTAB ? std::max(p->nkrylov, 5) : p->nkrylov;
   const bool gm = p->krylov == TY_KRYLOV_GMRES || p->krylov == TY_KRYLOV_BICGSTAB;  // no preconditioned basis
-  if (im.nk < nk || (need32 && !im.Z32) || (!need32 && !gm && !im.Z)) {
+  // Krylov storage: V (FP64 basis, always), V32 (FP32 basis), Z / Z32 (preconditioned vectors
+  // of the flexible GMRES in FP64 / FP32); buffers that exist are regrown with the capacity
+  if (im.nk < nk || (need32 && !im.Z32) || (basis32 && !im.V32) || (!need32 && !gm && !im.Z)) {
     const int cap = std::max(nk, im.nk);
     if ((rc = grow(h, im.V, (size_t)(cap + 1) * n))) return rc;
-    if (!gm || im.Z || im.Z32) {
-      if (need32 || im.Z32) {
-        if ((rc = grow(h, im.Z32, (size_t)cap * n)) || (rc = grow(h, im.V32, (size_t)(cap + 1) * n))) return rc;
-      }
-      if (!need32 || im.Z) { if ((rc = grow(h, im.Z, (size_t)cap * n))) return rc; }
-    }
+    if ((need32 || im.Z32) && (rc = grow(h, im.Z32, (size_t)cap * n))) return rc;
+    if ((basis32 || im.V32) && (rc = grow(h, im.V32, (size_t)(cap + 1) * n))) return rc;
+    if (((!need32 && !gm) || im.Z) && (rc = grow(h, im.Z, (size_t)cap * n))) return rc;
     im.nk = cap;
   }
   if (p->krylov == TY_KRYLOV_JFNK && !im.jfnk) {
@@ -285,7 +286,7 @@ int gmres_typhon(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
 // ---- flexible GMRES(m), CGS2, right block-Jacobi preconditioning ----
 struct Operator {
   ty_mesh* h;
-  int kind;  // 0 assembled FP64, 1 assembled FP32, 2 Jacobian-free
+  int kind;  // 0 assembled FP64, 1 assembled FP32 (FP32 basis), 2 Jacobian-free, 3 assembled FP32 (FP64 basis)
   double unorm = 0.0;
   ImpArgs a{};
   int apply(const double* z, const float* z32, double* w, int* matvecs);
@@ -301,7 +302,7 @@ int Operator::apply(const double* z, const float* z32, double* w, int* matvecs) 
     IMP_CU(IMP_CALL(h, imp_matvec, m, im, z, nullptr, w, s, &h->prof));
     return TY_OK;
   }
-  if (kind == 1) {
+  if (kind == 1 || kind == 3) {
     IMP_CU(IMP_CALL(h, imp_matvec32, m, im, z32, w, s, &h->prof));
     return TY_OK;
   }
@@ -343,15 +344,16 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
   const DevMesh& m = h->m;
   const size_t n = 5 * (size_t)m.nci;
   const int mk = p->nkrylov;
-  const bool f32 = op.kind == 1;
+  const bool f32 = op.kind == 1;                    // FP32 basis, swept in FP32 arithmetic
+  const bool z32 = op.kind == 1 || op.kind == 3;    // FP32 preconditioned vectors and mat-vec
   cudaStream_t s = h->stream;
   double* P = im.pinned;
   double* V64 = f32 ? nullptr : im.V;
   float* V32 = f32 ? im.V32 : nullptr;
   auto Vd = [&](int i) { return V64 ? V64 + (size_t)i * n : nullptr; };
   auto Vf = [&](int i) { return V32 ? V32 + (size_t)i * n : nullptr; };
-  auto Z = [&](int i) { return f32 ? nullptr : im.Z + (size_t)i * n; };
-  auto Z32 = [&](int i) { return f32 ? im.Z32 + (size_t)i * n : nullptr; };
+  auto Z = [&](int i) { return z32 ? nullptr : im.Z + (size_t)i * n; };
+  auto Z32 = [&](int i) { return z32 ? im.Z32 + (size_t)i * n : nullptr; };
   const int ld = mk + 1;
   std::vector<double> R((size_t)ld * ld, 0.0), Hc((size_t)ld * mk, 0.0), T((size_t)ld * mk, 0.0);
   std::vector<double> cs(mk), sn(mk), a(mk + 1), gr(mk), y(mk), u(mk + 1), c(mk + 1), t(mk + 2);
@@ -396,7 +398,7 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
       if (cycles == 0) {
         beta = beta0;
       } else {  // r = b - A x
-        if (f32) IMP_CU(IMP_CALL(h, imp_to_f32, im.x, Z32(0), n, s));
+        if (z32) IMP_CU(IMP_CALL(h, imp_to_f32, im.x, Z32(0), n, s));
         if (int rc = op.apply(im.x, Z32(0), im.w, &matvecs)) return rc;
         IMP_CU(IMP_CALL(h, imp_fd_combine, im.b, nullptr, im.w, nullptr, 1.0, im.r, n, s));
         IMP_CU(IMP_CALL(h, imp_dot, im.r, im.r, n, im.part, im.scal + kScalMisc, s));
@@ -465,7 +467,7 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
       }
       if (nused > 0) {
         if (int rc = put(h, kScalY, y.data(), nused)) return rc;
-        IMP_CU(IMP_CALL(h, imp_axpy_multi, im.x, f32 ? nullptr : im.Z, f32 ? im.Z32 : nullptr, n, nused,
+        IMP_CU(IMP_CALL(h, imp_axpy_multi, im.x, z32 ? nullptr : im.Z, z32 ? im.Z32 : nullptr, n, nused,
                         im.scal + kScalY, 0, n, s));
       }
       rel = std::fabs(a[nused]) / beta0;
@@ -487,7 +489,7 @@ int ty_implicit_step(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
   if (!p || !st) return TY_ERR_ARG;
   if (int rc = ready(h)) return rc;
   if (p->krylov < TY_KRYLOV_GMRES || p->krylov > TY_KRYLOV_BICGSTAB || p->precision < TY_PREC_FP64 ||
-      p->precision > TY_PREC_MIXED || p->nkrylov < 1 || p->max_it < 0 || !(p->inv_res > 0.0) || !(p->cfl > 0.0) ||
+      p->precision > TY_PREC_MIXED_FP64ORTHO || p->nkrylov < 1 || p->max_it < 0 || !(p->inv_res > 0.0) || !(p->cfl > 0.0) ||
       ((p->krylov == TY_KRYLOV_GMRES || p->krylov == TY_KRYLOV_BICGSTAB) && p->nkrylov > kMaxKrylov) ||
       ((p->krylov == TY_KRYLOV_FGMRES || p->krylov == TY_KRYLOV_JFNK) && p->nkrylov > kMaxCgs) ||
       (p->krylov != TY_KRYLOV_FGMRES && p->precision != TY_PREC_FP64)) {
@@ -517,7 +519,7 @@ int ty_implicit_step(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
   a.local_dt = p->local_dt ? 1 : 0;
   a.dtg = S.dtbits;
   a.src = (h->o.mode == TY_MODE_FAST && h->o.highres != TY_HRES_NONE) ? 2 : (h->o.postlim != TY_POSTLIM_NONE ? 1 : 0);
-  const bool mixed = p->krylov == TY_KRYLOV_FGMRES && p->precision == TY_PREC_MIXED;
+  const bool mixed = p->krylov == TY_KRYLOV_FGMRES && p->precision != TY_PREC_FP64;
   a.want64 = mixed ? 0 : 1;
   a.want32 = mixed ? 1 : 0;
   IMP_CU(IMP_CALL(h, imp_assemble, m, S, h->o, im, a, s, &h->prof));
@@ -538,7 +540,7 @@ int ty_implicit_step(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
   } else if (p->krylov == TY_KRYLOV_BICGSTAB) {
     rc = bicgstab_typhon(h, p, st);
   } else {
-    Operator op{h, mixed ? 1 : (p->krylov == TY_KRYLOV_JFNK ? 2 : 0)};
+    Operator op{h, mixed ? (p->precision == TY_PREC_MIXED ? 1 : 3) : (p->krylov == TY_KRYLOV_JFNK ? 2 : 0)};
     op.a = a;
     if (op.kind == 2) {
       IMP_CU(cudaMemcpyAsync(im.r0, im.b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));

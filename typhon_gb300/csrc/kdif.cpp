@@ -4,8 +4,10 @@
 // (d.n), |d|^2) is computed once on the host in the oracle's operation order.  The implicit
 // step assembles the symmetrised system diag(V/dt) A (symmetric positive definite: A is
 // Typhon's DLU matrix I + dt/V J with the compact Jacobian J_R = -k (d.n) / (Cp |d|^2),
-// J_L = -J_R) and solves it by Jacobi-preconditioned conjugate gradients in FP64, or by FP32
-// conjugate gradients inside FP64 iterative refinement.
+// J_L = -J_R) and solves it by Jacobi-preconditioned conjugate gradients in FP64 (one fused
+// pair of launches per iteration, kdif.cuh), by the same iteration on FP32 conductances until
+// 1e-6 and then on FP64 ones (mixed), or by FP32 conjugate gradients inside FP64 iterative
+// refinement.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -122,8 +124,12 @@ int ty_kdif_setup(ty_mesh* h, const ty_kdif_params* p, const double* conductivit
         (rc = h->alloc(k.p32, (size_t)nci)) || (rc = h->alloc(k.q32, (size_t)nci)) ||
         (rc = h->alloc(k.x32, (size_t)nci)) || (rc = h->alloc(k.diag32, (size_t)nci)) ||
         (rc = h->alloc(k.jac32, (size_t)nf)) || (rc = h->alloc(k.part, 4 * (size_t)kRedBlocks)) ||
-        (rc = h->alloc(k.scal, (size_t)16)) || (rc = h->alloc(k.cfo, cfo.size())) || (rc = h->alloc(k.cfon, cfon.size())))
+        (rc = h->alloc(k.scal, (size_t)16)) || (rc = h->alloc(k.cfo, cfo.size())) || (rc = h->alloc(k.cfon, cfon.size())) ||
+        (rc = h->alloc(k.ell_m, (size_t)nci)) || (rc = h->alloc(k.ell_a, (size_t)ns * nci)) ||
+        (rc = h->alloc(k.ell_a32, (size_t)ns * nci)) || (rc = h->alloc(k.ell_nb, (size_t)ns * nci)) ||
+        (rc = h->alloc(k.dinv, (size_t)nci)) || (rc = h->alloc(k.s, (size_t)nci)) || (rc = h->alloc(k.count, 2)))
       return rc;
+    TY_CU(cudaMemset(k.count, 0, 2 * sizeof(unsigned)));
     TY_CU(cudaMemcpy(k.cfo, cfo.data(), cfo.size() * sizeof(int), cudaMemcpyHostToDevice));
     TY_CU(cudaMemcpy(k.cfon, cfon.data(), cfon.size() * sizeof(int), cudaMemcpyHostToDevice));
     TY_CU(cudaMemset(k.T, 0, m.ldc * sizeof(double)));
@@ -173,7 +179,7 @@ int ty_kdif_residual(ty_mesh* h, double dt, double* R) {
 int ty_kdif_implicit_step(ty_mesh* h, double dt, const ty_kdif_solve* s, ty_kdif_stats* st) {
   if (int rc = kd_ready(h)) return rc;
   if (!s || !st || !(dt > 0.0) || !(s->tol > 0.0) || s->max_it < 1 ||
-      (s->solver != TY_KSOLVE_CG && s->solver != TY_KSOLVE_CG32_REFINE)) {
+      (s->solver != TY_KSOLVE_CG && s->solver != TY_KSOLVE_CG32_REFINE && s->solver != TY_KSOLVE_CG_MIXED)) {
     tyi::set_error("ty_kdif_implicit_step: bad dt or solver parameters");
     return TY_ERR_ARG;
   }
@@ -187,19 +193,34 @@ int ty_kdif_implicit_step(ty_mesh* h, double dt, const ty_kdif_solve* s, ty_kdif
   double* P = k.pinned;
   const int check = 10;  // iterations between host reads of the residual norm
   if (!f32) {
-    TY_CU(KD_CALL(h, kdif_cg_start, m, k, 0, q));
+    // fused single-reduction CG; the mixed form runs on the FP32 conductances until the
+    // residual is below kSwitch, then replaces the residual by the FP64 system's and continues
+    // on the FP64 conductances with the Krylov directions kept
+    constexpr double kSwitch = 1e-6;
+    bool a32 = s->solver == TY_KSOLVE_CG_MIXED && s->tol < kSwitch;
+    TY_CU(KD_CALL(h, kdif_ell_build, m, k, dt, q));
+    TY_CU(KD_CALL(h, kdif_fcg_a, m, k, 1, q));
+    TY_CU(KD_CALL(h, kdif_fcg_b, m, k, 1, a32 ? 1 : 0, q));
     if (int rc = fetch(h, 3, 1)) return rc;
     const double b2 = P[3];
     double rel = 0.0;
     int it = 0;
     if (b2 > 0.0) {
+      rel = 1.0;
       while (it < s->max_it) {
-        TY_CU(KD_CALL(h, kdif_cg_iter, m, k, 0, q));
+        TY_CU(KD_CALL(h, kdif_fcg_a, m, k, 0, q));
+        TY_CU(KD_CALL(h, kdif_fcg_b, m, k, 0, a32 ? 1 : 0, q));
         ++it;
         if (it % check == 0 || it == s->max_it) {
-          if (int rc = fetch(h, 4, 1)) return rc;
-          rel = std::sqrt(P[4] / b2);
-          if (rel < s->tol) break;
+          if (int rc = fetch(h, 11, 1)) return rc;
+          rel = std::sqrt(P[11] / b2);
+          if (a32 && rel < kSwitch) {
+            TY_CU(KD_CALL(h, kdif_fcg_replace, m, k, q));
+            a32 = false;
+            st->refinements = 1;
+            continue;
+          }
+          if (!a32 && rel < s->tol) break;
         }
       }
     }

@@ -264,7 +264,153 @@ __global__ void k_kdif_update_T(DevMesh m, KdifState k) {
   k.T[c] = k.T[c] + k.x[c] / k.cp;
 }
 
+// ---- fused conjugate gradients (single reduction per iteration) ----
+// Chronopoulos and Gear's arrangement of Jacobi-preconditioned CG: with u = D^-1 r, w = S u,
+// and p and s = S p carried by recurrences, both inner products of an iteration,
+// gamma = r.u and delta = w.u, come from the same iterate, so an iteration is two launches
+// and no host round trip:
+//   A: x += alpha p, r -= alpha s, u = r / diag; gamma, r.r;   beta = gamma / gamma_old
+//   B: w = S u, p = u + beta p, s = w + beta s; delta;         alpha = gamma / (delta - beta gamma / alpha_old)
+// Each launch reduces in a fixed grid (block sums, then the last block to finish sums the
+// block partials in block order): deterministic.  Scalars: scal[8] gamma, [9] alpha,
+// [10] beta, [11] r.r, [12] delta.
+constexpr int kFcgGamma = 8, kFcgAlpha = 9, kFcgBeta = 10, kFcgRR = 11, kFcgDelta = 12;
+
+// the symmetrised matrix in difference form (kdif.hpp) and the Jacobi inverse
+__global__ void __launch_bounds__(kBlock) k_kdif_ell(DevMesh m, KdifState k, double dt) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t n = m.nci;
+  double mc = m.cvol[c] / dt, d = mc;
+  for (int sl = 0; sl < m.nslot; ++sl) {
+    const int e = k.cfo[sl * n + c];
+    double a = 0.0;
+    int nb = c;
+    if (e >= 0) {
+      const int f = e >> 1;
+      if (f >= m.nfi) mc = mc - k.jac[f];
+      else { a = -k.jac[f]; nb = k.cfon[sl * n + c]; }
+      d = d - k.jac[f];
+    }
+    k.ell_a[sl * n + c] = a;
+    k.ell_a32[sl * n + c] = (float)a;
+    k.ell_nb[sl * n + c] = nb;
+  }
+  k.ell_m[c] = mc;
+  k.dinv[c] = 1.0 / d;
+}
+
+// last block of a launch: true in every thread of the block that finished last
+__device__ __forceinline__ bool kd_last_block(unsigned* count) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(count, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+// sum of the block partials part[0..nb) in block order (every thread; valid in thread 0)
+__device__ __forceinline__ double kd_sum_partials(const double* part, int nb) {
+  double a = 0.0;
+  for (int i = threadIdx.x; i < nb; i += kRedThreads) a += __ldcg(part + i);
+  return block_sum(a);
+}
+
+// A (first: x = 0, r = b)
+__global__ void __launch_bounds__(kRedThreads) k_kdif_fcg_a(int n, KdifState k, int first) {
+  const double alpha = first ? 0.0 : k.scal[kFcgAlpha];
+  double g = 0.0, rr = 0.0;
+  for (int i = blockIdx.x * kRedThreads + threadIdx.x; i < n; i += gridDim.x * kRedThreads) {
+    double xi, ri;
+    if (first) { xi = 0.0; ri = k.bal[i]; }
+    else { xi = k.x[i] + alpha * k.p[i]; ri = k.r[i] - alpha * k.s[i]; }
+    const double ui = ri * k.dinv[i];
+    k.x[i] = xi; k.r[i] = ri; k.z[i] = ui;
+    g += ri * ui;
+    rr += ri * ri;
+  }
+  g = block_sum(g);
+  if (threadIdx.x == 0) k.part[blockIdx.x] = g;
+  rr = block_sum(rr);
+  if (threadIdx.x == 0) k.part[kRedBlocks + blockIdx.x] = rr;
+  if (!kd_last_block(k.count)) return;
+  const double gt = kd_sum_partials(k.part, gridDim.x);
+  const double rt = kd_sum_partials(k.part + kRedBlocks, gridDim.x);
+  if (threadIdx.x == 0) {
+    k.scal[kFcgBeta] = first ? 0.0 : gt / k.scal[kFcgGamma];
+    k.scal[kFcgGamma] = gt;
+    k.scal[kFcgRR] = rt;
+    if (first) k.scal[3] = rt;   // |b|^2
+    *k.count = 0u;
+  }
+}
+
+// B: w = S u with FP64 (A32 = false) or FP32 (A32 = true) conductances
+template <bool A32>
+__global__ void __launch_bounds__(kRedThreads) k_kdif_fcg_b(int n, int ns, KdifState k, int first) {
+  const double beta = k.scal[kFcgBeta];
+  double dl = 0.0;
+  for (int c = blockIdx.x * kRedThreads + threadIdx.x; c < n; c += gridDim.x * kRedThreads) {
+    const double uc = k.z[c];
+    double w = k.ell_m[c] * uc;
+    for (int sl = 0; sl < ns; ++sl) {
+      const double a = A32 ? (double)k.ell_a32[sl * (size_t)n + c] : k.ell_a[sl * (size_t)n + c];
+      w = fma(a, uc - k.z[k.ell_nb[sl * (size_t)n + c]], w);
+    }
+    if (first) { k.p[c] = uc; k.s[c] = w; }
+    else { k.p[c] = fma(beta, k.p[c], uc); k.s[c] = fma(beta, k.s[c], w); }
+    dl += w * uc;
+  }
+  dl = block_sum(dl);
+  if (threadIdx.x == 0) k.part[blockIdx.x] = dl;
+  if (!kd_last_block(k.count + 1)) return;
+  const double dt = kd_sum_partials(k.part, gridDim.x);
+  if (threadIdx.x == 0) {
+    const double gm = k.scal[kFcgGamma];
+    k.scal[kFcgDelta] = dt;
+    k.scal[kFcgAlpha] = first ? gm / dt : gm / (dt - beta * gm / k.scal[kFcgAlpha]);
+    k.count[1] = 0u;
+  }
+}
+
+// residual replacement when the operator changes from FP32 to FP64 conductances:
+// r = b - S x and s = S p with the FP64 matrix, so that the recurrences continue on the true
+// residual of the FP64 system with the Krylov directions kept
+__global__ void __launch_bounds__(kRedThreads) k_kdif_fcg_replace(int n, int ns, KdifState k) {
+  for (int c = blockIdx.x * kRedThreads + threadIdx.x; c < n; c += gridDim.x * kRedThreads) {
+    const double xc = k.x[c], pc = k.p[c];
+    double sx = k.ell_m[c] * xc, sp = k.ell_m[c] * pc;
+    for (int sl = 0; sl < ns; ++sl) {
+      const double a = k.ell_a[sl * (size_t)n + c];
+      const int nb = k.ell_nb[sl * (size_t)n + c];
+      sx = fma(a, xc - k.x[nb], sx);
+      sp = fma(a, pc - k.p[nb], sp);
+    }
+    k.r[c] = k.bal[c] - sx;
+    k.s[c] = sp;
+  }
+}
+
 // ---- launchers ----
+cudaError_t kdif_ell_build(const DevMesh& m, const KdifState& k, double dt, cudaStream_t st) {
+  k_kdif_ell<<<nblk(m.nci), kBlock, 0, st>>>(m, k, dt);
+  return cudaGetLastError();
+}
+cudaError_t kdif_fcg_a(const DevMesh& m, const KdifState& k, int first, cudaStream_t st) {
+  k_kdif_fcg_a<<<red_grid(m.nci), kRedThreads, 0, st>>>(m.nci, k, first);
+  return cudaGetLastError();
+}
+cudaError_t kdif_fcg_b(const DevMesh& m, const KdifState& k, int first, int f32, cudaStream_t st) {
+  if (f32) k_kdif_fcg_b<true><<<red_grid(m.nci), kRedThreads, 0, st>>>(m.nci, m.nslot, k, first);
+  else k_kdif_fcg_b<false><<<red_grid(m.nci), kRedThreads, 0, st>>>(m.nci, m.nslot, k, first);
+  return cudaGetLastError();
+}
+cudaError_t kdif_fcg_replace(const DevMesh& m, const KdifState& k, cudaStream_t st) {
+  k_kdif_fcg_replace<<<red_grid(m.nci), kRedThreads, 0, st>>>(m.nci, m.nslot, k);
+  return cudaGetLastError();
+}
+
 cudaError_t kdif_residual(const DevMesh& m, const KdifState& k, double dt, cudaStream_t st) {
   if (m.ng > 0) k_kdif_ghost<<<nblk(m.ng), kBlock, 0, st>>>(m, k);
   if (k.scheme != TY_KDIF_COMPACT) k_kdif_grad<<<nblk(m.nci), kBlock, 0, st>>>(m, k);

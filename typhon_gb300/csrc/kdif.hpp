@@ -32,6 +32,17 @@ struct KdifState {
   double* pinned = nullptr;     // host mirror of scal
   int* cfo = nullptr;           // [nslot][nci] faces in ascending order (diagonal, mat-vec)
   int* cfon = nullptr;
+  // fused conjugate gradients: the symmetrised matrix in difference form,
+  //   (S x)_c = m_c x_c + sum_sl a[sl][c] (x_c - x[nb[sl][c]]),
+  // m_c = V_c/dt + the conductances of the cell's boundary faces, a = the conductance
+  // -J_R S of each interior face (0 with nb = c in unused slots)
+  double* ell_m = nullptr;      // [nci]
+  double* ell_a = nullptr;      // [nslot][nci]
+  float* ell_a32 = nullptr;     // [nslot][nci] the same conductances in FP32
+  int* ell_nb = nullptr;        // [nslot][nci]
+  double* dinv = nullptr;       // [nci] 1 / diagonal (Jacobi)
+  double* s = nullptr;          // [nci] S p (the single-reduction recurrence)
+  unsigned* count = nullptr;    // [2] finished blocks of the two fused kernels (last block reduces)
 };
 
 #define TY_DECLARE_KDIF(NS)                                                                          \
@@ -41,6 +52,10 @@ struct KdifState {
   cudaError_t kdif_matvec(const DevMesh& m, const KdifState& k, const double* x, double* y,           \
                           cudaStream_t st);                                                           \
   cudaError_t kdif_cg_start(const DevMesh& m, const KdifState& k, int f32, cudaStream_t st);          \
+  cudaError_t kdif_ell_build(const DevMesh& m, const KdifState& k, double dt, cudaStream_t st);         \
+  cudaError_t kdif_fcg_a(const DevMesh& m, const KdifState& k, int first, cudaStream_t st);              \
+  cudaError_t kdif_fcg_b(const DevMesh& m, const KdifState& k, int first, int f32, cudaStream_t st);     \
+  cudaError_t kdif_fcg_replace(const DevMesh& m, const KdifState& k, cudaStream_t st);                  \
   cudaError_t kdif_cg_iter(const DevMesh& m, const KdifState& k, int f32, cudaStream_t st);           \
   cudaError_t kdif_residual64(const DevMesh& m, const KdifState& k, cudaStream_t st);                 \
   cudaError_t kdif_refine(const DevMesh& m, const KdifState& k, cudaStream_t st);                     \

@@ -32,7 +32,7 @@ MODE = {"exact": 0, "fast": 1}
 DISSIPATIVE_FLUX = {"NONE": 0, "CELL-AVERAGE": 1, "FULL": 2}
 VISC_LAW = {"KINEMATIC-CONSTANT": 0, "SUTHERLAND": 1}
 KRYLOV = {"GMRES": 0, "FGMRES": 1, "JFNK": 2, "BICGSTAB": 3}
-PRECISION = {"fp64": 0, "mixed": 1}
+PRECISION = {"fp64": 0, "mixed": 1, "mixed-fp64ortho": 2}
 KDIF_FLUX = {"COMPACT": 0, "CELL-AVERAGE": 1, "FULL": 2}
 KBC_ISOTHERMAL, KBC_FLUX, KBC_EXTRAPOLATE = 1, 2, 3
 
@@ -201,7 +201,8 @@ class Grid:
     def implicit_step(self, cfl, inversion="GMRES", nkrylov=50, max_it=50, inv_res=1e-4, local_dt=False,
                       precision="fp64"):
         """One backward-Euler step on the resident state.  inversion: GMRES (Typhon's
-        bdlu_gmres), FGMRES (block Jacobi, measured Gram matrix) or JFNK; precision fp64 | mixed (FGMRES).
+        bdlu_gmres), FGMRES (block Jacobi, measured Gram matrix) or JFNK; precision fp64 | mixed-fp64ortho
+        (FGMRES: FP32 matrix, mat-vec and block Jacobi, FP64 basis) | mixed (FGMRES: FP32 basis too).
         Returns the ty_imp_stats fields as a dict."""
         p = _capi.ImpParams(KRYLOV[inversion], PRECISION[precision], int(nkrylov), int(max_it), int(local_dt), 0,
                             float(inv_res), float(cfl))
@@ -351,9 +352,10 @@ class Grid:
         return R
 
     def kdif_implicit_step(self, dt, solver="CG", tol=1e-12, max_it=20000, inner_tol=1e-5):
-        """One backward-Euler step; solver CG (FP64, Jacobi) or CG32 (FP32 CG inside FP64
-        iterative refinement).  Returns iterations, refinements, final relative residual."""
-        s = _capi.KdifSolve({"CG": 0, "CG32": 1}[solver], int(max_it), float(tol), float(inner_tol))
+        """One backward-Euler step; solver CG (FP64, Jacobi), CG-MIXED (the same on FP32 face
+        conductances to 1e-6, then FP64) or CG32 (FP32 CG inside FP64 iterative refinement).
+        Returns iterations, refinements, final relative residual."""
+        s = _capi.KdifSolve({"CG": 0, "CG32": 1, "CG-MIXED": 2}[solver], int(max_it), float(tol), float(inner_tol))
         st = _capi.KdifStats()
         _capi.check(self.lib.ty_kdif_implicit_step(self.h, float(dt), C.byref(s), C.byref(st)),
                     "ty_kdif_implicit_step")
