@@ -58,6 +58,7 @@ def parse():
                          "instead of the runs to 1e-10 (a short sequence of launches for ncu)")
     ap.add_argument("--kdif-inner-tol", type=float, default=1e-3, help="kdif3d: FP32 inner CG tolerance")
     ap.add_argument("--kdif-inner-max", type=int, default=300, help="kdif3d: FP32 inner CG iterations at most")
+    ap.add_argument("--kdif-refine", action="store_true", help="kdif3d: also run FP32 CG inside FP64 refinement")
     return ap.parse_args()
 
 
@@ -295,12 +296,7 @@ def run_ours(args, rank, world, local):
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload} {'64^3x5 tets' if args.workload == 'tgv3d' else '64x64x2 tris'}"
-                   if n == w["n"] else f"{args.workload} n={n}", "cells": nci, "faces": md.nface,
-                   "scheme": w["scheme"], "highres": w["highres"], "limiter": w["limiter"],
-                   "postlim": w["postlim"], "rk": w["rk"], "cfl": w["cfl"], "mode": args.mode,
-                   "parallelism": f"replicas{world}",
-                   "l2": "working set larger than L2 (no flush needed)"},
+        "config": workload_config(args, nci, md.nface, world),
         "e2e": e2e, "roofline": roofline, "kernels": per,
         "gpu_launches": int(kl.sum()), "clocks": clocks, "mesh_build_s": round(t_mesh, 2),
         "fp64_peak_tflops": round(fp64 / 1e12, 3) if fp64 else None,
@@ -309,8 +305,21 @@ def run_ours(args, rank, world, local):
     return out
 
 
-def cpu_sample(args, n_steps):
-    """The CPU restatement (oracle, OpenMP) on the same mesh and setup: n_steps steps."""
+def workload_config(args, cells, faces, world):
+    """The `config` object of both arms' JSON lines (the same workload and setup)."""
+    from typhon_gb300 import cases
+    w = cases.WORKLOADS[args.workload]
+    n = args.n or w["n"]
+    name = {"tgv3d": f"tgv3d {n}^3x5 tets", "vortex2d": f"vortex2d {n}x{n}x2 tris"}[args.workload]
+    return {"workload": name, "cells": int(cells), "faces": int(faces), "scheme": w["scheme"],
+            "highres": w["highres"], "limiter": w["limiter"], "postlim": w["postlim"], "rk": w["rk"],
+            "cfl": w["cfl"], "mode": args.mode, "parallelism": f"replicas{world}",
+            "l2": "working set larger than L2 (no flush needed)"}
+
+
+def cpu_sample(args, n_steps, warmup=1, with_mesh=False):
+    """The CPU restatement (oracle, OpenMP) on the same mesh and setup: warmup untimed steps,
+    then n_steps timed steps."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_py as op
     from typhon_gb300 import cases
@@ -327,14 +336,17 @@ def cpu_sample(args, n_steps):
     s = op.Solver(om, sch, hres, lim, post, op.GRAD_LSQ, rk=w["rk"], cfl=w["cfl"])
     d = om.export()
     s.set_prim(cases.initial_prim(args.workload, d["ccentre"]))
-    s.run_steps(1)  # warm (first-touch, LSQ factors)
+    s.run_steps(max(1, warmup))  # warm (first-touch, LSQ factors)
     t0 = time.perf_counter()
     s.run_steps(n_steps)
     dt = time.perf_counter() - t0
-    cores = os.cpu_count()
-    return {"value": om.ncell_int * n_steps / dt, "unit": "cell-updates/s", "cores": cores, "kind": "port",
-            "sample": f"{n_steps} {w['rk']} step(s) of the full {om.ncell_int}-cell mesh, OpenMP on {cores} "
-                      f"threads ({dt:.1f} s)"}
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
+    out = {"value": om.ncell_int * n_steps / dt, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+           "sample": f"{n_steps} {w['rk']} step(s) of the full {om.ncell_int}-cell mesh, OpenMP on {cores} "
+                     f"threads ({dt:.1f} s)"}
+    if with_mesh:
+        return out, om.ncell_int, om.nface
+    return out
 
 
 def run_implicit(args):
@@ -358,7 +370,7 @@ def run_implicit(args):
     if args.imp_steps:
         # a fixed number of FGMRES steps (FP64, then mixed) at the starting CFL, after one warm-up
         res = {}
-        for prec in ("fp64", "mixed"):
+        for prec in ("fp64", "mixed-fp64ortho", "mixed"):
             g = ty.Grid(md)
             g.set_spat(w["scheme"], w["highres"], w["limiter"], w["postlim"], mode="fast", farfield=ff)
             g.set_prim(prim0)
@@ -378,8 +390,8 @@ def run_implicit(args):
     variants = {}
     states = {}
     with ClockSampler(0) as clk:
-        for name, inv, prec in (("fgmres_fp64", "FGMRES", "fp64"), ("fgmres_mixed", "FGMRES", "mixed"),
-                                ("jfnk_fp64", "JFNK", "fp64")):
+        for name, inv, prec in (("fgmres_fp64", "FGMRES", "fp64"), ("fgmres_mixed", "FGMRES", "mixed-fp64ortho"),
+                                ("fgmres_mixed_f32basis", "FGMRES", "mixed"), ("jfnk_fp64", "JFNK", "fp64")):
             g = ty.Grid(md)
             g.set_spat(w["scheme"], w["highres"], w["limiter"], w["postlim"], mode="fast", farfield=ff)
             g.set_prim(prim0)
@@ -420,12 +432,13 @@ def run_implicit(args):
                               "profiled_step": {"wall_ms": round(wall * 1e3, 3), "kernels": prof}}
             g.close()
     ref = states["fgmres_fp64"]
-    for name in ("fgmres_mixed", "jfnk_fp64"):
+    for name in ("fgmres_mixed", "fgmres_mixed_f32basis", "jfnk_fp64"):
         d = states[name] - ref
         variants[name]["state_vs_fp64"] = [float(np.linalg.norm(d[0]) / np.linalg.norm(ref[0])),
                                            float(np.linalg.norm(d[1]) / np.linalg.norm(ref[1])),
                                            float(np.linalg.norm(d[2:5]) / np.linalg.norm(ref[2:5]))]
-    out = {"metric": "seconds to a 1e-10 relative residual, mixed FP32/FP64 implicit", "unit": "s",
+    out = {"metric": "seconds to a 1e-10 relative residual, mixed implicit (FP32 Jv and block Jacobi, FP64 "
+                     "Krylov basis, orthogonalisation, residual and update)", "unit": "s",
            "value": variants["fgmres_mixed"]["seconds"], "higher_is_better": False, "n_gpus": 1,
            "steps": variants["fgmres_mixed"]["steps"], "warmup": 1, "dtype": "f64+f32", "data": "synthetic",
            "scaling": "weak", "vs_baseline": None,
@@ -439,10 +452,12 @@ def run_implicit(args):
 
 
 def run_kdif(args):
-    """Heat conduction: 50 backward-Euler steps of the KDIF config with FP64 conjugate
-    gradients + Jacobi and with FP32 conjugate gradients inside FP64 iterative refinement,
-    both to a 1e-12 relative residual per step.  Wall-clock time of the steps (synchronised),
-    iterations, and the FP32-refined final temperature against the FP64 one."""
+    """Heat conduction: 50 backward-Euler steps of the KDIF config to a 1e-12 relative
+    residual per step with FP64 conjugate gradients + Jacobi (fused single-reduction
+    iteration) and with the mixed form (the same iteration on FP32 face conductances to 1e-6,
+    then the FP64 matrix); --kdif-refine adds FP32 CG inside FP64 iterative refinement.
+    Wall-clock time of the steps (synchronised), iterations, the mixed final temperature
+    against the FP64 one, and the FP64 iteration's device time against the HBM roofline."""
     import torch
     import typhon_gb300 as ty
     from typhon_gb300 import build, cases
@@ -452,8 +467,9 @@ def run_kdif(args):
     md, kc, kind, val = cases.make_kdif3d(args.n)
     nci = md.ncell_int
     variants, temps = {}, {}
+    runs = [("cg_fp64", "CG"), ("cg_mixed", "CG-MIXED")] + ([("cg32_refined", "CG32")] if args.kdif_refine else [])
     with ClockSampler(0) as clk:
-        for name, solver in (("cg_fp64", "CG"), ("cg32_refined", "CG32")):
+        for name, solver in runs:
             g = ty.Grid(md)
             g.set_spat("HLLC", mode="fast")
             g.kdif_setup(kc, kind, val, flux="FULL", heat_capacity=w["heat_capacity"])
@@ -461,33 +477,65 @@ def run_kdif(args):
             g.kdif_implicit_step(w["dt"], solver, tol=1e-3)          # warm-up (workspace, clocks)
             g.kdif_set_temperature(np.zeros(md.ncell))
             g.synchronize()
-            its, worst = 0, 0.0
+            its, worst, switched = 0, 0.0, 0
             t0 = time.perf_counter()
             for _ in range(w["steps"]):
-                if solver == "CG":
-                    st = g.kdif_implicit_step(w["dt"], solver, tol=w["tol"])
-                else:
+                if solver == "CG32":
                     st = g.kdif_implicit_step(w["dt"], solver, tol=w["tol"], max_it=args.kdif_inner_max,
                                               inner_tol=args.kdif_inner_tol)
+                else:
+                    st = g.kdif_implicit_step(w["dt"], solver, tol=w["tol"])
                 its += st["iterations"]
                 worst = max(worst, st["rel_res"])
+                switched += st["refinements"]
             g.synchronize()
             t = time.perf_counter() - t0
             temps[name] = g.kdif_temperature()
             variants[name] = {"seconds": round(t, 3), "iterations": its, "worst_rel_res": worst,
                               "ms_per_step": round(1e3 * t / w["steps"], 3)}
+            if solver == "CG-MIXED":
+                variants[name]["steps_switched_to_fp64"] = switched
+            if solver in ("CG", "CG-MIXED"):
+                # device time of one conjugate-gradient iteration: a fixed 400 iterations
+                # (tolerance out of reach), CUDA events on the handle's stream
+                stream = torch.cuda.Stream()
+                from typhon_gb300 import _capi
+                _capi.check(g.lib.ty_set_stream(g.h, stream.cuda_stream), "ty_set_stream")
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                with torch.cuda.stream(stream):
+                    e0.record(stream)
+                    st = g.kdif_implicit_step(w["dt"], "CG", tol=1e-300, max_it=400)
+                    e1.record(stream)
+                torch.cuda.synchronize()
+                _capi.check(g.lib.ty_set_stream(g.h, None), "ty_set_stream")
+                ms = e0.elapsed_time(e1) / st["iterations"]
+                ns = g.info()["max_faces_per_cell"]
+                # algorithmic bytes per cell and iteration: A reads p, s, x, r, 1/diag and writes
+                # x, r, u (64 B); B reads u, m, the conductances (8 B) and neighbour indices (4 B)
+                # of every slot, p, s and writes p, s (48 + 12 ns B)
+                bpc = 64 + 48 + 12 * ns
+                if name == "cg_fp64":
+                    peak, kind_ = measured_peaks()
+                    ach = bpc * nci / (ms * 1e-3) / 1e9
+                    variants[name]["iteration"] = {
+                        "ms": round(ms, 5), "bytes_per_cell": bpc, "achieved_gbs": round(ach, 1), "peak_gbs": peak,
+                        "frac": round(ach / peak, 4), "peak_source": kind_,
+                        "note": "400 iterations timed with CUDA events, including the residual-norm read every "
+                                "10 iterations and the step's residual and assembly"}
             g.close()
-    d = temps["cg32_refined"] - temps["cg_fp64"]
-    variants["cg32_refined"]["T_vs_fp64"] = float(np.linalg.norm(d) / np.linalg.norm(temps["cg_fp64"]))
-    out = {"metric": "seconds for 50 implicit KDIF steps to 1e-12, FP32 CG + FP64 refinement", "unit": "s",
-           "value": variants["cg32_refined"]["seconds"], "higher_is_better": False, "n_gpus": 1,
+    d = temps["cg_mixed"] - temps["cg_fp64"]
+    variants["cg_mixed"]["T_vs_fp64"] = float(np.linalg.norm(d) / np.linalg.norm(temps["cg_fp64"]))
+    if "cg32_refined" in temps:
+        d = temps["cg32_refined"] - temps["cg_fp64"]
+        variants["cg32_refined"]["T_vs_fp64"] = float(np.linalg.norm(d) / np.linalg.norm(temps["cg_fp64"]))
+    out = {"metric": "seconds for 50 implicit KDIF steps to 1e-12, mixed CG (FP32 conductances, then FP64)",
+           "unit": "s", "value": variants["cg_mixed"]["seconds"], "higher_is_better": False, "n_gpus": 1,
            "steps": w["steps"], "warmup": 1, "dtype": "f64+f32", "data": "synthetic", "scaling": "weak",
            "vs_baseline": None,
            "config": {"workload": f"kdif3d {args.n or w['n']}^3x6 tets, lognormal k with 8 inclusions x100",
-                      "cells": nci, "dt": w["dt"], "flux": "FULL",
-                      "inner": f"FP32 CG to {args.kdif_inner_tol:g} or {args.kdif_inner_max} iterations"},
+                      "cells": nci, "dt": w["dt"], "flux": "FULL"},
            "variants": variants,
-           "speedup_cg32_vs_fp64": round(variants["cg_fp64"]["seconds"] / variants["cg32_refined"]["seconds"], 3),
+           "speedup_mixed_vs_fp64": round(variants["cg_fp64"]["seconds"] / variants["cg_mixed"]["seconds"], 3),
            "clocks": clk.summary()}
     print(json.dumps(out))
 
@@ -654,13 +702,13 @@ def main():
         if rank != 0:
             return
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
-        steps = max(1, min(args.steps, 3))
-        cb = cpu_sample(args, steps)
+        cb, cells, faces = cpu_sample(args, args.steps, args.warmup, with_mesh=True)
         out = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": cb["unit"], "n_gpus": world,
-               "steps": steps, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "f64", "data": "synthetic",
-               "config": {"workload": args.workload, "note": "CPU restatement of Typhon's solver (oracle), "
-                          "Typhon is Fortran and no Fortran compiler is available"},
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": cells / cb["value"] * 1e3,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": workload_config(args, cells, faces, world),
+               "implementation": "the CPU restatement of Typhon's solver (oracle/, OpenMP on all host cores); Typhon "
+                                 "itself is Fortran and no Fortran compiler exists in the image or on the GPU box",
                "cpu_baseline": cb,
                "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))

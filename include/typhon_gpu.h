@@ -336,9 +336,9 @@ typedef enum {
   TY_KSOLVE_CG_MIXED = 2     /* TY_KSOLVE_CG on the face conductances stored in FP32 (FP64
                                 vectors and arithmetic; the difference form keeps the matrix
                                 spectrally within 1e-7 of the FP64 one) until the relative
-                                residual is below 1e-6, then the FP64 residual replaces the
-                                recurrence's and the iteration continues on the FP64 matrix
-                                (stats.refinements = 1 when it switched) */
+                                residual is below 1e-6, then restarted on the FP64 matrix from
+                                the FP64 system's residual (stats.refinements = 1 when it
+                                switched) */
 } ty_kdif_solver;
 typedef struct ty_kdif_solve {
   int32_t solver;        /* ty_kdif_solver */
@@ -373,7 +373,9 @@ int ty_kdif_matvec(ty_mesh* mesh, const double* x, double* y);
  *   ty_residual_device: R = dt/V sum(+-F S), ty_residual's value.
  *   ty_adjoint_vjp:     lambda_U = (dR/dU)^T lambda_R of the inviscid residual, first order
  *                       (HIGHRES = NONE, any boundary) or second order (least-squares
- *                       gradients, HIGHRES = MUSCL with no limiter or van Albada, periodic
+ *                       gradients, HIGHRES = MUSCL or MUSCL-UNS with no limiter or van
+ *                       Albada, POST-LIMITER = BARTH / SUPERBARTH frozen: its ratios are
+ *                       those of the state and are not differentiated; periodic
  *                       boundaries); TY_ERR_UNSUPPORTED otherwise.  A reversed face loop
  *                       (hand-written reverse-mode flux derivatives, reversed
  *                       reconstruction) and per-cell gathers, no atomics. */

@@ -1,7 +1,9 @@
-"""Complex-step reference of the first-order residual (test infrastructure).
+"""Complex-step reference of the residual (test infrastructure).
 
-A numpy restatement of the first-order residual R = dt/V sum(+-F S) (Rusanov, HLLC and Roe
-fluxes, periodic and symmetry boundaries) written so that it is analytic in the state: the
+A numpy restatement of the residual R = dt/V sum(+-F S) (Rusanov, HLLC and Roe fluxes; first
+order with periodic and symmetry boundaries, or least-squares gradients with MUSCL / MUSCL-UNS,
+van Albada and the frozen Barth post-limiter on periodic meshes) written so that it is analytic
+in the state: the
 absolute value is z sign(Re z), max/min compare real parts, the square root is the complex
 one.  Evaluated at U + i h d it gives dR/dU d to machine precision (complex step), and with
 the Runge-Kutta tables of typhon_gb300.adjoint the derivative of a whole explicit run.
@@ -165,9 +167,10 @@ def gradient(md, P, w):
     return G
 
 
-def muscl(md, P, G, faces, side, limiter):
-    """MUSCL (HIGHRES = MUSCL) state of one side of `faces`: q_c + G_c.CF + sg (u.CF), sg =
-    phi(2g - LR, LR) - g with van Albada's phi (or LR - g without limiter)."""
+def muscl(md, P, G, faces, side, limiter, highres="MUSCL"):
+    """MUSCL state of one side of `faces`: q_c + G_c.CF + sg (u.CF), sg = phi(a, LR) - g with
+    van Albada's phi (or LR - g without limiter), a = 2g - LR for HIGHRES = MUSCL
+    (tvdgradstr) and a = g for MUSCL-UNS (tvdgraduns)."""
     fc1, fc2 = md.fc1[faces], md.fc2[faces]
     c = fc2 if side else fc1
     CL, CR = md.cell_centre[fc1], md.cell_centre[fc2]
@@ -180,7 +183,7 @@ def muscl(md, P, G, faces, side, limiter):
     Gc = G[:, c, :]
     g = np.einsum("vfk,fk->vf", Gc, u)
     if limiter == "ALBADA":
-        a, b = 2.0 * g - LR, LR
+        a, b = (g if highres == "MUSCL-UNS" else 2.0 * g - LR), LR
         pos = (a.real * b.real) > 0.0
         den = np.where(pos, a * a + b * b, 1.0)
         phi = np.where(pos, a * b * (a + b) / den, 0.0)
@@ -190,9 +193,34 @@ def muscl(md, P, G, faces, side, limiter):
     return P[:, c] + np.einsum("vfk,fk->vf", Gc, CF) + sg * uc
 
 
-def residual(md, U, dt, scheme="RUSANOV", g=1.4, highres="NONE", limiter="NONE"):
+def barth_ratios(md, P, QL, QR, klim=0.5):
+    """Typhon's face-ratio post-limiter (postlimit_barth.f90:42-223) from the real parts:
+    r[group, c] = min(1, min over the cell's faces and the group's variables of
+    max(klim (q_nb - q_c) / (q_face - q_c), 0)), groups rho, p and the velocity vector; a face
+    whose increment is exactly zero imposes no constraint.  The ratios are real: a complex
+    step through the limited states differentiates the limiter frozen at them."""
+    nci, nfi = md.ncell_int, md.nface_int
+    Pr, QLr, QRr = P.real, QL.real, QR.real
+    r = np.ones((3, nci))
+    grp = [0, 1, 2, 2, 2]
+    inner = np.arange(nfi)
+    for cells, nb, q, sel in ((md.fc1, md.fc2, QLr, np.arange(md.nface)),
+                              (md.fc2[inner], md.fc1[inner], QRr[:, inner], inner)):
+        c, n = cells, nb
+        for v in range(5):
+            den = q[v] - Pr[v, c]
+            dq = Pr[v, n] - Pr[v, c]
+            ok = den != 0.0
+            t = np.full(den.shape, np.inf)
+            t[ok] = np.maximum(klim * (dq[ok] / den[ok]), 0.0)
+            np.minimum.at(r[grp[v]], c, t)
+    return r
+
+
+def residual(md, U, dt, scheme="RUSANOV", g=1.4, highres="NONE", limiter="NONE", postlim="NONE"):
     """R [5, ncell_int] of the residual at U [5, ncell_int] (real or complex): first order, or
-    least-squares gradients and MUSCL with no limiter or van Albada (periodic boundaries)."""
+    least-squares gradients and MUSCL / MUSCL-UNS with no limiter or van Albada, optionally
+    Typhon's Barth post-limiter with its ratios frozen (periodic boundaries)."""
     nci, nf, nfi = md.ncell_int, md.nface, md.nface_int
     fc1, fc2 = md.fc1, md.fc2
     P = prim(U, g)
@@ -200,12 +228,20 @@ def residual(md, U, dt, scheme="RUSANOV", g=1.4, highres="NONE", limiter="NONE")
         P = P[:, _ghost_source(md)]
         G = gradient(md, P, lsq_weights(md))
         allf = np.arange(nf)
-        QL = muscl(md, P, G, allf, 0, limiter)
+        QL = muscl(md, P, G, allf, 0, limiter, highres)
         QR = np.empty_like(QL)
         inner = np.arange(nfi)
-        QR[:, inner] = muscl(md, P, G, inner, 1, limiter)
+        QR[:, inner] = muscl(md, P, G, inner, 1, limiter, highres)
         b = np.arange(nfi, nf)
-        QR[:, b] = muscl(md, P, G, md.face_partner[b] - 1, 0, limiter)
+        if postlim != "NONE":
+            r = barth_ratios(md, P, QL, QR, 0.5 if postlim == "BARTH" else 1.0)
+            grp = [0, 1, 2, 2, 2]
+            for v in range(5):
+                QL[v] = P[v, fc1] + r[grp[v], fc1] * (QL[v] - P[v, fc1])
+                QR[v, inner] = P[v, fc2[inner]] + r[grp[v], fc2[inner]] * (QR[v, inner] - P[v, fc2[inner]])
+            QR[:, b] = QL[:, md.face_partner[b] - 1]
+        else:
+            QR[:, b] = muscl(md, P, G, md.face_partner[b] - 1, 0, limiter, highres)
         n = md.face_normal.T
         F = {"RUSANOV": rusanov, "HLLC": hllc, "ROE": roe}[scheme](QL, QR, n, g) * md.face_surface
         R = np.zeros((5, nci), dtype=U.dtype)
@@ -232,7 +268,7 @@ def residual(md, U, dt, scheme="RUSANOV", g=1.4, highres="NONE", limiter="NONE")
     return dt / md.cell_volume[:nci] * R
 
 
-def rk_run(md, U0, dts, table, scheme="RUSANOV", highres="NONE", limiter="NONE"):
+def rk_run(md, U0, dts, table, scheme="RUSANOV", highres="NONE", limiter="NONE", postlim="NONE"):
     U = U0
     for dt in dts:
         Rs = []
@@ -241,7 +277,7 @@ def rk_run(md, U0, dts, table, scheme="RUSANOV", highres="NONE", limiter="NONE")
             for s in range(k):
                 if table[k - 1][s] != 0.0:
                     Uk = Uk + table[k - 1][s] * Rs[s]
-            Rs.append(residual(md, Uk, dt, scheme, highres=highres, limiter=limiter))
+            Rs.append(residual(md, Uk, dt, scheme, highres=highres, limiter=limiter, postlim=postlim))
         for s, c in enumerate(table[-1]):
             if c != 0.0:
                 U = U + c * Rs[s]

@@ -119,9 +119,11 @@ def test_complex_step_reference_matches_real_residual(golden_dir):
 
 @pytest.mark.parametrize("scheme,oscheme", [("HLLC", 1), ("ROE", 3), ("RUSANOV", 2)])
 @pytest.mark.parametrize("limiter", ["ALBADA", "NONE"])
-def test_complex_step_reference_matches_muscl_residual(scheme, oscheme, limiter):
-    """The second-order restatement (least-squares gradients, MUSCL, van Albada) against the
-    oracle's residual on a jittered periodic mesh."""
+@pytest.mark.parametrize("highres,postlim", [("MUSCL", "NONE"), ("MUSCL-UNS", "NONE"), ("MUSCL-UNS", "BARTH"),
+                                             ("MUSCL", "SUPERBARTH")])
+def test_complex_step_reference_matches_muscl_residual(scheme, oscheme, limiter, highres, postlim):
+    """The second-order restatement (least-squares gradients, MUSCL or MUSCL-UNS, van Albada,
+    Barth post-limiters) against the oracle's residual on a jittered periodic mesh."""
     import oracle_py as op
     import typhon_gb300 as ty
     raw = ty.gen_grid2d(10, 10, 1.0, 1.0, "tri", jitter=0.1, seed=3)
@@ -131,10 +133,14 @@ def test_complex_step_reference_matches_muscl_residual(scheme, oscheme, limiter)
     prim = np.stack([1 + 0.1 * np.sin(6.28 * x + 0.3) * np.sin(6.28 * y + 1.1), 0.7 + 0.05 * np.cos(6.28 * (x + y)),
                      0.3 + 0.1 * np.sin(6.28 * y), 0.1 * np.cos(6.28 * x), 0 * x])
     olim = op.LIM_ALBADA if limiter == "ALBADA" else op.LIM_NONE
-    s = op.Solver(om, oscheme, op.HRES_MUSCL, olim, op.POSTLIM_NONE, op.GRAD_LSQ, cfl=1.0)
+    ohres = {"MUSCL": op.HRES_MUSCL, "MUSCL-UNS": op.HRES_MUSCLUNS}[highres]
+    opost = {"NONE": op.POSTLIM_NONE, "BARTH": op.POSTLIM_BARTH, "SUPERBARTH": op.POSTLIM_SUPERBARTH}[postlim]
+    s = op.Solver(om, oscheme, ohres, olim, opost, op.GRAD_LSQ, cfl=1.0)
     s.set_prim(prim)
     s.rhs(1e-3)
     U = s.get("cons")[:, :md.ncell_int]
-    R = cs.residual(md, U, 1e-3, scheme, highres="MUSCL", limiter=limiter)
+    R = cs.residual(md, U, 1e-3, scheme, highres=highres, limiter=limiter, postlim=postlim)
+    if postlim != "NONE":   # the limiter is active somewhere on this state
+        assert (s.get("limratio")[:, :md.ncell_int] < 1.0).any()
     Ro = s.get("residu")[:, :md.ncell_int]
     assert np.abs(R - Ro).max() <= 1e-12 * np.abs(Ro).max()

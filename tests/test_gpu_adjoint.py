@@ -3,7 +3,9 @@
 * ty_adjoint_vjp against central finite differences of ty_residual_device (periodic,
   symmetry, far-field, slip and no-slip wall boundaries; HLLC, Rusanov, Roe; exact and fast
   modes); the second-order VJP (least-squares gradients, MUSCL, van Albada) likewise on
-  periodic meshes, and through a whole unsteady run against the complex step.
+  periodic meshes, and through a whole unsteady run against the complex step; with Typhon's
+  Barth post-limiter frozen (MUSCL-UNS and MUSCL), against the complex step of the numpy
+  restatement with the same frozen ratios (finite differences would see the limiter move).
 * The gradient of J = sum over a sub-box of rho^2 V after an RK3-SSP run, through
   typhon_gb300.adjoint (binomial checkpointing or stored stage states, torch.autograd),
   against the complex-step derivative of the numpy restatement in tests/residual_cs.py:
@@ -126,8 +128,8 @@ def test_unsteady_gradient_against_complex_step(env, scheme):
 def test_adjoint_rejects_unsupported_second_order(env, golden_dir):
     torch, ty, adjoint = env
     md = jittered(ty, 4)
-    for highres, limiter, postlim in (("MUSCL-UNS", "ALBADA", "NONE"), ("MUSCL", "MINMOD", "NONE"),
-                                      ("MUSCL", "ALBADA", "BARTH")):
+    for highres, limiter, postlim in (("MUSCL-FAST", "ALBADA", "NONE"), ("MUSCL", "MINMOD", "NONE"),
+                                      ("MUSCL-UNS", "SUPERBEE", "BARTH"), ("NONE", "NONE", "BARTH")):
         g = ty.Grid(md)
         g.set_spat("HLLC", highres, limiter, postlim)
         st = adjoint.Stepper(g, "RK2")
@@ -230,6 +232,68 @@ def test_muscl_tgv3d_gradient_against_complex_step(env):
         d = rng.standard_normal(U0.shape) * np.abs(U0).mean(axis=1, keepdims=True)
         Uc = cs.rk_run(md, U0 + 1j * 1e-30 * d, dts, adjoint.RK_TABLES["RK3-SSP"], "HLLC", highres="MUSCL",
                        limiter="ALBADA")
+        dJ = float(np.sum(box * Uc[0] ** 2).imag / 1e-30)
+        ad = float(np.sum(grad * d))
+        assert abs(ad - dJ) <= 1e-8 * abs(dJ), (ad, dJ)
+    g.close()
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+@pytest.mark.parametrize("scheme,highres,limiter,postlim", [("ROE", "MUSCL-UNS", "NONE", "BARTH"),
+                                                            ("HLLC", "MUSCL-UNS", "ALBADA", "NONE"),
+                                                            ("HLLC", "MUSCL", "ALBADA", "SUPERBARTH")])
+def test_frozen_barth_vjp_against_complex_step(env, scheme, highres, limiter, postlim, mode):
+    """One residual's VJP with the Barth post-limiter frozen at the state's ratios (and
+    MUSCL-UNS): lambda_R . (dR/dU d) against the complex step of the numpy restatement, whose
+    ratios come from the real parts.  The state is rough enough for the limiter to act."""
+    torch, ty, adjoint = env
+    md = jittered(ty)
+    g = ty.Grid(md)
+    g.set_spat(scheme, highres, limiter, postlim, mode=mode)
+    st = adjoint.Stepper(g, "RK3-SSP")
+    rng = np.random.default_rng(2)
+    U0 = smooth_cons(ty, md) * (1.0 + 0.05 * rng.standard_normal((1, md.ncell_int)))
+    U = torch.tensor(U0, device="cuda")
+    lamR = rng.standard_normal(U0.shape)
+    d = rng.standard_normal(U0.shape) * np.abs(U0).mean(axis=1, keepdims=True)
+    dt = 1e-3
+    lamU = st.vjp(U, dt, torch.tensor(lamR, device="cuda")).cpu().numpy()
+    Rc = cs.residual(md, U0 + 1j * 1e-30 * d, dt, scheme, highres=highres, limiter=limiter, postlim=postlim)
+    cs_dir = float(np.sum(lamR * Rc.imag) / 1e-30)
+    ad = float(np.sum(lamU * d))
+    assert abs(ad - cs_dir) <= 1e-9 * abs(cs_dir), (ad, cs_dir)
+    R = st.residual(U, dt).cpu().numpy()
+    assert np.abs(R - Rc.real).max() <= 1e-11 * np.abs(R).max()
+    g.close()
+
+
+def test_config2_scheme_gradient_against_complex_step(env):
+    """The benchmarked explicit scheme (Roe, MUSCL-UNS, Barth post-limiter frozen) through 20
+    SSP-RK3 steps of the Taylor-Green vortex on 6^3 x 5 tetrahedra: the adjoint gradient of
+    J = sum over the centred sub-box of rho^2 V against the complex step of the numpy
+    restatement on 4 seeded directions."""
+    torch, ty, adjoint = env
+    from typhon_gb300 import cases
+    md = cases.make_mesh("tgv3d", 6)
+    nci = md.ncell_int
+    g = ty.Grid(md)
+    g.set_spat("ROE", "MUSCL-UNS", "NONE", "BARTH", mode="exact")
+    prim = cases.taylor_green(md.cell_centre)
+    U0 = ty.prim_to_cons(prim[:, :nci])
+    g.set_prim(prim)
+    dts = [g.calc_zonetimestep(0.8)] * 20
+    cc = md.cell_centre[:nci]
+    L = 2 * np.pi
+    box = np.all(np.abs(cc - L / 2) < L / 4, axis=1).astype(float) * md.cell_volume[:nci]
+    Ut = torch.tensor(U0, device="cuda", requires_grad=True)
+    J = (adjoint.rk_solve(Ut, g, "RK3-SSP", dts)[0] ** 2 * torch.tensor(box, device="cuda")).sum()
+    J.backward()
+    grad = Ut.grad.cpu().numpy()
+    rng = np.random.default_rng(9)
+    for _ in range(4):
+        d = rng.standard_normal(U0.shape) * np.abs(U0).mean(axis=1, keepdims=True)
+        Uc = cs.rk_run(md, U0 + 1j * 1e-30 * d, dts, adjoint.RK_TABLES["RK3-SSP"], "ROE", highres="MUSCL-UNS",
+                       limiter="NONE", postlim="BARTH")
         dJ = float(np.sum(box * Uc[0] ** 2).imag / 1e-30)
         ad = float(np.sum(grad * d))
         assert abs(ad - dJ) <= 1e-8 * abs(dJ), (ad, dJ)

@@ -83,9 +83,8 @@ def test_exact_kdif_bitwise(ty, scheme):
 
 @pytest.mark.parametrize("solver", ["CG32", "CG-MIXED"])
 def test_mixed_precision_solvers_reach_fp64(ty, solver):
-    """FP32 CG inside FP64 refinement, and CG on FP32 face conductances switched to the FP64
-    matrix at 1e-6 (residual replacement): both reach the FP64 CG solution, to 1e-12 on the
-    FP64 system."""
+    """FP32 CG inside FP64 refinement, and CG on FP32 face conductances restarted on the FP64
+    matrix at 1e-6: both reach the FP64 CG solution, to 1e-12 on the FP64 system."""
     md, om, kind, val, kc, T0 = box_case(ty, n=8)
     kc = kc * np.exp(np.random.default_rng(3).standard_normal(kc.shape))   # heterogeneous k
     sols = {}

@@ -3,7 +3,8 @@
 // Both act on the handle's resident state U (ty_state_upload_device): ty_residual_device
 // writes R = dt/V sum(+-F S) (ty_residual's value) to a caller device buffer, and
 // ty_adjoint_vjp writes lambda_U = (dR/dU)^T lambda_R for the inviscid residual, first order
-// (HIGHRES = NONE) or second order (MUSCL with no limiter or van Albada, periodic meshes).  New: Typhon has no adjoint; the unsteady gradient of a
+// (HIGHRES = NONE) or second order (MUSCL or MUSCL-UNS with no limiter or van Albada, the
+// Barth post-limiter frozen at the state's ratios; periodic meshes).  New: Typhon has no adjoint; the unsteady gradient of a
 // functional (RK stages, checkpointing, torch.autograd) is composed from these two calls in
 // typhon_gb300/adjoint.py.
 #include <vector>
@@ -37,10 +38,11 @@ int ty_adjoint_vjp(ty_mesh* h, double dt, const double* lamR, double* lamU) {
   if (!lamR || !lamU) return TY_ERR_ARG;
   const bool second = h->o.highres != TY_HRES_NONE;
   if (h->o.viscous != TY_VISC_NONE ||
-      (second && (h->o.highres != TY_HRES_MUSCL || (h->o.limiter != TY_LIM_NONE && h->o.limiter != TY_LIM_ALBADA) ||
-                  h->o.postlim != TY_POSTLIM_NONE || h->nonperiodic_bc))) {
-    tyi::set_error("ty_adjoint_vjp: inviscid residual, first order or MUSCL with no limiter or van Albada "
-                   "(no post-limiter, periodic boundaries)");
+      (second && ((h->o.highres != TY_HRES_MUSCL && h->o.highres != TY_HRES_MUSCLUNS) ||
+                  (h->o.limiter != TY_LIM_NONE && h->o.limiter != TY_LIM_ALBADA) || h->nonperiodic_bc)) ||
+      (!second && h->o.postlim != TY_POSTLIM_NONE)) {
+    tyi::set_error("ty_adjoint_vjp: inviscid residual, first order, or MUSCL / MUSCL-UNS with no limiter or van "
+                   "Albada and the Barth post-limiter frozen (periodic boundaries)");
     return TY_ERR_UNSUPPORTED;
   }
   if (h->o.scheme == TY_SCH_HLLE || h->o.scheme == TY_SCH_AUSMM || h->inout_bc) {

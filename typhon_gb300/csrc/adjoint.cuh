@@ -1,5 +1,4 @@
-// Adjoint (vector-Jacobian product) of the first-order residual, instantiated per mode after
-// kernels.cuh.  New: Typhon has no adjoint (its inverse mode differentiates by finite
+// Adjoint (vector-Jacobian product) of the residual, instantiated per mode after kernels.cuh.  New: Typhon has no adjoint (its inverse mode differentiates by finite
 // differences, SOURCE/MAIN/inverse_calc_sensi.f90).
 //
 // R_c = dt/V_c sum_f (+-) F_f(U) S_f with face states Q_L = prim(U_fc1), Q_R = prim(U_fc2) or
@@ -122,16 +121,21 @@ __global__ void __launch_bounds__(128) k_adj_face(DevMesh m, SpatOpts o, const d
   }
 }
 
-// ---- second order: least-squares gradients, MUSCL (HIGHRES = MUSCL) with no limiter or the
-// van Albada limiter, on meshes whose boundaries are periodic.  The reconstruction of one face
-// side (recon, owner cell c, cells i1 = fc1, i2 = fc2 of the owner face F) is
-//   q = q_c + G_c . CF + sg (u . CF),  sg = phi(2g - LR, LR) - g (phi = 0: sg = LR - g),
-//   g = G_c . u,  LR = (q_i2 - q_i1) / dLR,
-// with phi(a, b) = a b (a + b) / (a^2 + b^2) where a b > 0, else 0 (smooth van Albada).
+// ---- second order: least-squares gradients, MUSCL or MUSCL-UNS with no limiter or the van
+// Albada limiter, Typhon's Barth post-limiter frozen, on meshes whose boundaries are periodic.
+// The reconstruction of one face side (recon, owner cell c, cells i1 = fc1, i2 = fc2 of the
+// owner face F) is
+//   q = q_c + r_c (G_c . CF + sg (u . CF)),  g = G_c . u,  LR = (q_i2 - q_i1) / dLR,
+//   sg = phi(2g - LR, LR) - g (MUSCL, tvdgradstr) or phi(g, LR) - g (MUSCL-UNS, tvdgraduns),
+//   phi = 0: sg = LR - g,
+// with phi(a, b) = a b (a + b) / (a^2 + b^2) where a b > 0, else 0 (smooth van Albada), and
+// r_c the cell's Barth ratio for the variable's group (postlimit_barth.f90:42-223), held
+// constant (1 without a post-limiter): the adjoint of the frozen limiter scales the
+// increment's adjoint by r_c.
 // reverse of one face side: Qb -> rec[0..4] adjoint of q_c, rec[5..19] of G_c (3 per
 // variable), rec[20..24] of LR over dLR (+ to i2, - to i1)
 __device__ void recon_vjp(const DevMesh& m, const DevState& s, const SpatOpts& o, int F, int side,
-                          const double* Qb, double* rec) {
+                          const double* Qb, const double* ratio, double* rec) {
   const size_t ld = m.ldc, lf = m.ldf;
   const int icl = m.fc1[F], icr = m.fc2[F];
   const int c = side ? icr : icl;
@@ -140,31 +144,37 @@ __device__ void recon_vjp(const DevMesh& m, const DevState& s, const SpatOpts& o
   const double* CF = side ? m.RF : m.LF;
   const double cx = CF[F], cy = CF[lf + F], cz = CF[2 * lf + F];
   const double uc = ux * cx + uy * cy + uz * cz;
+  const bool uns = o.highres == TY_HRES_MUSCLUNS;
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
     const double gx = s.grad[(3 * v) * ld + c], gy = s.grad[(3 * v + 1) * ld + c], gz = s.grad[(3 * v + 2) * ld + c];
     const double LR = (s.prim[v * ld + icr] - s.prim[v * ld + icl]) * idLR;
     const double g = gx * ux + gy * uy + gz * uz;
-    const double qb = Qb[v], sgb = qb * uc;
+    const double qb = Qb[v], db = ratio[v < 2 ? v : 2] * qb, sgb = db * uc;
     double gb, LRb;
     if (o.limiter == TY_LIM_NONE) {
       LRb = sgb;
       gb = -sgb;
     } else {
-      const double a = 2.0 * g - LR, b = LR;
+      const double a = uns ? g : 2.0 * g - LR, b = LR;
       double pa = 0.0, pb = 0.0;
       if (a * b > 0.0) {
         const double D = a * a + b * b, iD2 = 1.0 / (D * D);
         pa = b * b * (b * b + 2.0 * a * b - a * a) * iD2;
         pb = a * a * (a * a + 2.0 * a * b - b * b) * iD2;
       }
-      gb = 2.0 * sgb * pa - sgb;
-      LRb = sgb * pb - sgb * pa;
+      if (uns) {
+        gb = sgb * pa - sgb;
+        LRb = sgb * pb;
+      } else {
+        gb = 2.0 * sgb * pa - sgb;
+        LRb = sgb * pb - sgb * pa;
+      }
     }
     rec[v] = qb;
-    rec[5 + 3 * v] = qb * cx + gb * ux;
-    rec[6 + 3 * v] = qb * cy + gb * uy;
-    rec[7 + 3 * v] = qb * cz + gb * uz;
+    rec[5 + 3 * v] = db * cx + gb * ux;
+    rec[6 + 3 * v] = db * cy + gb * uy;
+    rec[7 + 3 * v] = db * cz + gb * uz;
     rec[20 + v] = LRb * idLR;
   }
 }
@@ -192,16 +202,30 @@ __global__ void __launch_bounds__(128) k_adj_face2(DevMesh m, DevState s, SpatOp
   const int F1 = interior ? f : m.part[f], s1 = interior ? 1 : 0;
   recon(m, s, o, f, 0, QL);
   recon(m, s, o, F1, s1, QR);
+  // frozen post-limiter: each side's increment scaled by its owner cell's ratio
+  double rL[3] = {1.0, 1.0, 1.0}, rR[3] = {1.0, 1.0, 1.0};
+  if (o.postlim != TY_POSTLIM_NONE) {
+    const int cR = s1 ? m.fc2[F1] : m.fc1[F1];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { rL[k] = s.ratio[k * ld + c1]; rR[k] = s.ratio[k * ld + cR]; }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const int k = v < 2 ? v : 2;
+      const double qL = s.prim[v * ld + c1], qR = s.prim[v * ld + cR];
+      QL[v] = qL + rL[k] * (QL[v] - qL);
+      QR[v] = qR + rR[k] * (QR[v] - qR);
+    }
+  }
   double QLb[5] = {0, 0, 0, 0, 0}, QRb[5] = {0, 0, 0, 0, 0};
   const double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
   if constexpr (SCH == TY_SCH_HLLC) hllc_vjp(o.gamma, QL, QR, nx, ny, nz, Fb, QLb, QRb);
   else if constexpr (SCH == TY_SCH_RUSANOV) rusanov_vjp(o.gamma, QL, QR, nx, ny, nz, Fb, QLb, QRb);
   else roe_vjp(o.gamma, o.entropy_fix, QL, QR, nx, ny, nz, Fb, QLb, QRb);
   double r[25];
-  recon_vjp(m, s, o, f, 0, QLb, r);
+  recon_vjp(m, s, o, f, 0, QLb, rL, r);
 #pragma unroll
   for (int k = 0; k < 25; ++k) rec[k * lf + f] = r[k];
-  recon_vjp(m, s, o, F1, s1, QRb, r);
+  recon_vjp(m, s, o, F1, s1, QRb, rR, r);
 #pragma unroll
   for (int k = 0; k < 25; ++k) rec[(25 + k) * lf + f] = r[k];
 }
@@ -319,7 +343,19 @@ cudaError_t adjoint_vjp_muscl(const DevMesh& m, const DevState& s, const SpatOpt
                               const double* lamR, double dt, double* rec, double* qg, double* lamU, cudaStream_t st) {
   k_prim<<<nblk(m.nci), kBlock, 0, st>>>(m, u, s.prim, o.gamma);
   if (m.ng > 0) k_ghost_prim<<<nblk(m.ng), kBlock, 0, st>>>(m, s.prim, o);
-  k_grad<<<nblk(m.nci), kBlock, 0, st>>>(m, s);
+  if (o.postlim != TY_POSTLIM_NONE) {  // gradient and the Barth ratios of the forward residual
+    const double klim = o.postlim == TY_POSTLIM_SUPERBARTH ? 1.0 : 0.5;
+    if (kFast) {
+      if (m.nslot <= 4) k_cell_fast<4, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim);
+      else k_cell_fast<8, 64><<<(unsigned)((m.nci + 63) / 64), 64, 0, st>>>(m, s, o, klim);
+    } else {
+      k_grad<<<nblk(m.nci), kBlock, 0, st>>>(m, s);
+      k_face_states<<<nblk(m.nf), kBlock, 0, st>>>(m, s, o);
+      k_barth<<<nblk(m.nci), kBlock, 0, st>>>(m, s, klim);
+    }
+  } else {
+    k_grad<<<nblk(m.nci), kBlock, 0, st>>>(m, s);
+  }
   const unsigned gf = (unsigned)((m.nf + 127) / 128);
   if (o.scheme == TY_SCH_HLLC) k_adj_face2<TY_SCH_HLLC><<<gf, 128, 0, st>>>(m, s, o, lamR, dt, rec);
   else if (o.scheme == TY_SCH_RUSANOV) k_adj_face2<TY_SCH_RUSANOV><<<gf, 128, 0, st>>>(m, s, o, lamR, dt, rec);

@@ -194,8 +194,8 @@ int ty_kdif_implicit_step(ty_mesh* h, double dt, const ty_kdif_solve* s, ty_kdif
   const int check = 10;  // iterations between host reads of the residual norm
   if (!f32) {
     // fused single-reduction CG; the mixed form runs on the FP32 conductances until the
-    // residual is below kSwitch, then replaces the residual by the FP64 system's and continues
-    // on the FP64 conductances with the Krylov directions kept
+    // residual is below kSwitch, then restarts on the FP64 conductances from the FP64
+    // system's residual
     constexpr double kSwitch = 1e-6;
     bool a32 = s->solver == TY_KSOLVE_CG_MIXED && s->tol < kSwitch;
     TY_CU(KD_CALL(h, kdif_ell_build, m, k, dt, q));
@@ -214,8 +214,10 @@ int ty_kdif_implicit_step(ty_mesh* h, double dt, const ty_kdif_solve* s, ty_kdif
         if (it % check == 0 || it == s->max_it) {
           if (int rc = fetch(h, 11, 1)) return rc;
           rel = std::sqrt(P[11] / b2);
-          if (a32 && rel < kSwitch) {
+          if (a32 && rel < kSwitch) {  // restart on the FP64 matrix from the true residual
             TY_CU(KD_CALL(h, kdif_fcg_replace, m, k, q));
+            TY_CU(KD_CALL(h, kdif_fcg_a, m, k, 2, q));
+            TY_CU(KD_CALL(h, kdif_fcg_b, m, k, 1, 0, q));
             a32 = false;
             st->refinements = 1;
             continue;

@@ -317,13 +317,14 @@ __device__ __forceinline__ double kd_sum_partials(const double* part, int nb) {
   return block_sum(a);
 }
 
-// A (first: x = 0, r = b)
+// A (first = 1: start, x = 0, r = b; first = 2: restart from the current x and r)
 __global__ void __launch_bounds__(kRedThreads) k_kdif_fcg_a(int n, KdifState k, int first) {
   const double alpha = first ? 0.0 : k.scal[kFcgAlpha];
   double g = 0.0, rr = 0.0;
   for (int i = blockIdx.x * kRedThreads + threadIdx.x; i < n; i += gridDim.x * kRedThreads) {
     double xi, ri;
-    if (first) { xi = 0.0; ri = k.bal[i]; }
+    if (first == 1) { xi = 0.0; ri = k.bal[i]; }
+    else if (first == 2) { xi = k.x[i]; ri = k.r[i]; }
     else { xi = k.x[i] + alpha * k.p[i]; ri = k.r[i] - alpha * k.s[i]; }
     const double ui = ri * k.dinv[i];
     k.x[i] = xi; k.r[i] = ri; k.z[i] = ui;
@@ -341,7 +342,7 @@ __global__ void __launch_bounds__(kRedThreads) k_kdif_fcg_a(int n, KdifState k, 
     k.scal[kFcgBeta] = first ? 0.0 : gt / k.scal[kFcgGamma];
     k.scal[kFcgGamma] = gt;
     k.scal[kFcgRR] = rt;
-    if (first) k.scal[3] = rt;   // |b|^2
+    if (first == 1) k.scal[3] = rt;   // |b|^2
     *k.count = 0u;
   }
 }
@@ -374,21 +375,16 @@ __global__ void __launch_bounds__(kRedThreads) k_kdif_fcg_b(int n, int ns, KdifS
   }
 }
 
-// residual replacement when the operator changes from FP32 to FP64 conductances:
-// r = b - S x and s = S p with the FP64 matrix, so that the recurrences continue on the true
-// residual of the FP64 system with the Krylov directions kept
+// the true residual r = b - S x of the FP64 system, from which the iteration restarts when
+// the operator changes from FP32 to FP64 conductances (continuing the old directions on the
+// changed operator loses their conjugacy: on this stiff system the iteration stagnates)
 __global__ void __launch_bounds__(kRedThreads) k_kdif_fcg_replace(int n, int ns, KdifState k) {
   for (int c = blockIdx.x * kRedThreads + threadIdx.x; c < n; c += gridDim.x * kRedThreads) {
-    const double xc = k.x[c], pc = k.p[c];
-    double sx = k.ell_m[c] * xc, sp = k.ell_m[c] * pc;
-    for (int sl = 0; sl < ns; ++sl) {
-      const double a = k.ell_a[sl * (size_t)n + c];
-      const int nb = k.ell_nb[sl * (size_t)n + c];
-      sx = fma(a, xc - k.x[nb], sx);
-      sp = fma(a, pc - k.p[nb], sp);
-    }
+    const double xc = k.x[c];
+    double sx = k.ell_m[c] * xc;
+    for (int sl = 0; sl < ns; ++sl)
+      sx = fma(k.ell_a[sl * (size_t)n + c], xc - k.x[k.ell_nb[sl * (size_t)n + c]], sx);
     k.r[c] = k.bal[c] - sx;
-    k.s[c] = sp;
   }
 }
 

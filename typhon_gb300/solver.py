@@ -353,7 +353,7 @@ class Grid:
 
     def kdif_implicit_step(self, dt, solver="CG", tol=1e-12, max_it=20000, inner_tol=1e-5):
         """One backward-Euler step; solver CG (FP64, Jacobi), CG-MIXED (the same on FP32 face
-        conductances to 1e-6, then FP64) or CG32 (FP32 CG inside FP64 iterative refinement).
+        conductances to 1e-6, then restarted on the FP64 matrix) or CG32 (FP32 CG inside FP64 iterative refinement).
         Returns iterations, refinements, final relative residual."""
         s = _capi.KdifSolve({"CG": 0, "CG32": 1, "CG-MIXED": 2}[solver], int(max_it), float(tol), float(inner_tol))
         st = _capi.KdifStats()
