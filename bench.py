@@ -59,6 +59,13 @@ def parse():
     ap.add_argument("--kdif-inner-tol", type=float, default=1e-3, help="kdif3d: FP32 inner CG tolerance")
     ap.add_argument("--kdif-inner-max", type=int, default=300, help="kdif3d: FP32 inner CG iterations at most")
     ap.add_argument("--kdif-refine", action="store_true", help="kdif3d: also run FP32 CG inside FP64 refinement")
+    ap.add_argument("--adj-cs-n", type=int, default=8, help="adjoint3d: mesh size of the complex-step check")
+    ap.add_argument("--adj-cs-steps", type=int, default=0, help="adjoint3d: steps of the complex-step check "
+                    "(default: the configuration's)")
+    ap.add_argument("--adj-cs-directions", type=int, default=0, help="adjoint3d: directions of the complex-step "
+                    "check (default: the configuration's)")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the short implicit, KDIF and adjoint runs of the default line")
     return ap.parse_args()
 
 
@@ -290,6 +297,24 @@ def run_ours(args, rank, world, local):
         t_e2e = float(t.item())
     e2e = {"value": nci * e2e_steps * world / t_e2e, "unit": "cell-updates/s",
            "h2d_bytes_per_step": 40 * nci, "d2h_bytes_per_step": 40 * nci, "steps": e2e_steps}
+    # the exact mode (bit-identical to the oracle) on the same grid and state, device time
+    exact = None
+    if args.mode == "fast":
+        g.set_spat(w["scheme"], w["highres"], w["limiter"], w["postlim"], mode="exact")
+        g.run_steps(w["rk"], w["cfl"], 2)
+        ke = max(5, min(args.steps, 20))
+        torch.cuda.synchronize(local)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            g.run_steps(w["rk"], w["cfl"], ke)
+            e1.record(stream)
+        torch.cuda.synchronize(local)
+        mse = e0.elapsed_time(e1)
+        exact = {"value": nci * ke / (mse * 1e-3), "unit": "cell-updates/s", "steps": ke,
+                 "ms_per_step": round(mse / ke, 4),
+                 "parity": "bit-identical to the oracle over 20 steps at this size (the fast mode agrees to 1e-12 "
+                           "for 5 steps and stays within the oracle's own one-ulp sensitivity over 20)"}
+        g.set_spat(w["scheme"], w["highres"], w["limiter"], w["postlim"], mode=args.mode)
     clocks = clk.summary()
     fp64 = fp64_peak()
     out = {
@@ -298,7 +323,7 @@ def run_ours(args, rank, world, local):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args, nci, md.nface, world),
         "e2e": e2e, "roofline": roofline, "kernels": per,
-        "gpu_launches": int(kl.sum()), "clocks": clocks, "mesh_build_s": round(t_mesh, 2),
+        "gpu_launches": int(kl.sum()), "clocks": clocks, "mesh_build_s": round(t_mesh, 2), "exact_mode": exact,
         "fp64_peak_tflops": round(fp64 / 1e12, 3) if fp64 else None,
     }
     g.close()
@@ -540,17 +565,27 @@ def run_kdif(args):
     print(json.dumps(out))
 
 
-def complex_step_sample(w, n=8, steps=20, directions=3):
-    """The adjoint configuration on a small sample (TGV n^3 x 5, `steps` steps): GPU adjoint
-    directional derivatives against the complex step of the numpy restatement of the same
-    residual (tests/residual_cs.py, the checker; never the measured path)."""
-    import importlib.util
+def _cs_worker_init(tests_dir):
+    sys.path.insert(0, tests_dir)
+
+
+def _cs_direction(job):
+    import residual_cs as cs
+    md, U0, d, dts, table, box, scheme, highres, limiter = job
+    return cs.box_functional_derivative(md, U0, d, dts, table, box, scheme, highres=highres, limiter=limiter)
+
+
+def complex_step_sample(w, n=8, steps=None, directions=None):
+    """The adjoint configuration on a small sample (TGV n^3 x 5, the configuration's steps and
+    seeded directions): GPU adjoint directional derivatives against the complex step of the
+    numpy restatement of the same residual (tests/residual_cs.py, the checker; never the
+    measured path), one direction per process of a spawned pool."""
+    import multiprocessing as mp
     import torch
     import typhon_gb300 as ty
     from typhon_gb300 import adjoint, cases
-    spec = importlib.util.spec_from_file_location("residual_cs", Path(__file__).parent / "tests" / "residual_cs.py")
-    cs = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(cs)
+    steps = steps or w["steps"]
+    directions = directions or w["directions"]
     md = cases.make_mesh("tgv3d", n)
     nci = md.ncell_int
     g = ty.Grid(md)
@@ -568,15 +603,16 @@ def complex_step_sample(w, n=8, steps=20, directions=3):
     grad = Ut.grad.cpu().numpy()
     g.close()
     rng = np.random.default_rng(w["seed"])
-    errs = []
-    for _ in range(directions):
-        d = rng.standard_normal(U0.shape) * np.abs(U0).mean(axis=1, keepdims=True)
-        Uc = cs.rk_run(md, U0 + 1j * 1e-30 * d, dts, adjoint.RK_TABLES[w["rk"]], w["scheme"], highres=w["highres"],
-                       limiter=w["limiter"])
-        dJ = float(np.sum(box * Uc[0] ** 2).imag / 1e-30)
-        errs.append(abs(float(np.sum(grad * d)) - dJ) / max(abs(dJ), 1e-300))
-    return {"sample": f"TGV {n}^3x5 tets ({nci} cells), {steps} steps", "directions": directions,
-            "max_rel_err": max(errs)}
+    ds = [rng.standard_normal(U0.shape) * np.abs(U0).mean(axis=1, keepdims=True) for _ in range(directions)]
+    jobs = [(md, U0, d, dts, adjoint.RK_TABLES[w["rk"]], box, w["scheme"], w["highres"], w["limiter"]) for d in ds]
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(min(directions, os.cpu_count() or 1), initializer=_cs_worker_init,
+                                       initargs=(str(ROOT / "tests"),)) as pool:
+        ref = pool.map(_cs_direction, jobs)
+    errs = [abs(float(np.sum(grad * d)) - r) / max(abs(r), 1e-300) for d, r in zip(ds, ref)]
+    return {"sample": f"TGV {n}^3x5 tets ({nci} cells), {steps} {w['rk']} steps", "directions": directions,
+            "max_rel_err": max(errs), "median_rel_err": float(np.median(errs)),
+            "checker_s": round(time.perf_counter() - t0, 1)}
 
 
 def run_adjoint(args):
@@ -650,17 +686,18 @@ def run_adjoint(args):
         fd = (Jp - Jm) / (2 * eps)
         ad = float((grad * d).sum())
         errs.append(abs(ad - fd) / max(abs(fd), 1e-300))
-    cs_check = complex_step_sample(w)
-    out = {"metric": "adjoint / primal time, unsteady gradient of int rho^2 (reverse sweep over stored stage "
-                     "states)", "unit": "ratio",
-           "value": round(t_rev / t_primal, 3), "higher_is_better": False, "n_gpus": 1, "steps": w["steps"],
+    cs_check = complex_step_sample(w, n=args.adj_cs_n, steps=args.adj_cs_steps or w["steps"],
+                                   directions=args.adj_cs_directions or w["directions"])
+    out = {"metric": "adjoint gradient / primal time, unsteady gradient of int rho^2 (forward pass storing the "
+                     "stage states plus the reverse sweep)", "unit": "ratio",
+           "value": round((t_fwd_store + t_rev) / t_primal, 3), "higher_is_better": False, "n_gpus": 1, "steps": w["steps"],
            "warmup": 2, "dtype": "f64", "data": "synthetic", "scaling": "weak", "vs_baseline": None,
            "config": {"workload": f"adjoint3d TGV {n}^3x5 tets, {w['scheme']} + {w['highres']} {w['limiter']} "
                                   f"(least-squares gradients), {w['rk']}",
                       "cells": nci, "dt": dt, "storage_policy": policy, "J": J0},
            "primal_s": round(t_primal, 4), "primal_library_rk_s": round(t_lib, 4),
            "primal_storing_stages_s": round(t_fwd_store, 4), "stage_storage_bytes": tape_bytes,
-           "reverse_sweep_s": round(t_rev, 4),
+           "reverse_sweep_s": round(t_rev, 4), "reverse_sweep_vs_primal": round(t_rev / t_primal, 3),
            "gradient_total_vs_primal": round((t_fwd_store + t_rev) / t_primal, 3),
            "binomial": {"snapshots": w["snaps"], "adjoint_s": round(t_adj, 4),
                         "adjoint_vs_primal": round(t_adj / t_primal, 3),
@@ -675,6 +712,47 @@ def run_adjoint(args):
            "complex_step_check": cs_check,
            "clocks": clk.summary()}
     print(json.dumps(out))
+
+
+def secondary_runs():
+    """Short but complete runs of the three other measurements, each in its own process at a
+    reduced size (the full-size runs are the --workload options), summarised for the default
+    line: time to a 1e-10 residual of FP64 vs mixed implicit solves, 50 KDIF steps of FP64 vs
+    mixed conjugate gradients, and the unsteady adjoint's cost against its primal run."""
+    runs = {"implicit": ["--workload", "ffbox3d-implicit", "--n", "24"],
+            "kdif": ["--workload", "kdif3d", "--n", "35"],
+            "adjoint": ["--workload", "adjoint3d", "--n", "20", "--adj-cs-n", "6", "--adj-cs-steps", "20",
+                        "--adj-cs-directions", "4"]}
+    out = {}
+    for name, extra in runs.items():
+        try:
+            r = subprocess.run([sys.executable, str(ROOT / "bench.py"), *extra], capture_output=True, text=True,
+                               timeout=600)
+            line = [ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1]
+            d = json.loads(line)
+        except (subprocess.TimeoutExpired, IndexError, ValueError) as e:
+            out[name] = {"error": f"{type(e).__name__}"}
+            continue
+        v = d["variants"] if "variants" in d else {}
+        if name == "implicit":
+            out[name] = {"workload": d["config"]["workload"], "cells": d["config"]["cells"], "steps": d["steps"],
+                         "seconds_fp64": v["fgmres_fp64"]["seconds"], "seconds_mixed": v["fgmres_mixed"]["seconds"],
+                         "seconds_mixed_f32basis": v["fgmres_mixed_f32basis"]["seconds"],
+                         "speedup_mixed_vs_fp64": d["speedup_mixed_vs_fp64"],
+                         "mixed_state_vs_fp64": max(v["fgmres_mixed"]["state_vs_fp64"]),
+                         "reached_1e-10": all(x["reached"] for x in v.values())}
+        elif name == "kdif":
+            out[name] = {"workload": d["config"]["workload"], "cells": d["config"]["cells"],
+                         "seconds_cg_fp64": v["cg_fp64"]["seconds"], "seconds_cg_mixed": v["cg_mixed"]["seconds"],
+                         "speedup_mixed_vs_fp64": d["speedup_mixed_vs_fp64"],
+                         "cg_iteration_hbm_frac": v["cg_fp64"]["iteration"]["frac"]}
+        else:
+            out[name] = {"workload": d["config"]["workload"], "cells": d["config"]["cells"], "steps": d["steps"],
+                         "gradient_vs_primal": d["value"], "reverse_sweep_vs_primal": d["reverse_sweep_vs_primal"],
+                         "binomial_vs_primal": d["binomial"]["adjoint_vs_primal"],
+                         "complex_step_max_rel_err": d["complex_step_check"]["max_rel_err"],
+                         "complex_step_sample": d["complex_step_check"]["sample"]}
+    return out
 
 
 def main():
@@ -718,6 +796,8 @@ def main():
         if not args.no_cpu_baseline:
             os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
             out["cpu_baseline"] = cpu_sample(args, args.cpu_sample_steps)
+        if world == 1 and not args.no_secondary and args.workload == "tgv3d" and args.n is None:
+            out["secondary"] = secondary_runs()
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

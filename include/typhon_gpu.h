@@ -42,7 +42,18 @@ extern "C" {
 /* ---- option enums (values match the oracle and the Python binding) ---- */
 /* TY_SCH_HLLE: calc_flux_hlle.f90 (beta = 1) with the HLL Jacobian of its wave speeds. */
 /* TY_SCH_AUSMM: calc_flux_ausmm.f90 (explicit only: Typhon has no AUSM-M Jacobian). */
-enum ty_scheme { TY_SCH_HLLC = 1, TY_SCH_RUSANOV = 2, TY_SCH_ROE = 3, TY_SCH_AUSMM = 4, TY_SCH_HLLE = 5 };
+/* The wave-speed variants of Typhon's HLLC and HLLE (SCHEME = HLLCB, HLLCK, HLLCKB, HLLEB,
+ * HLLEK, HLLEKB; def_spat.f90:68-76, calc_flux_hllc.f90:64-124, calc_flux_hlle.f90:64-120):
+ * B takes beta = sqrt((gamma-1)/(2 gamma)) in place of 1 in the outer wave speeds, K the
+ * kinetic (EFM) estimates c (m (1 -+ erf m)/2 -+ exp(-m^2)/(2 sqrt pi)), m = u.n/c -+ beta
+ * sqrt(gamma/2), c = a / sqrt(gamma/2).  The implicit step uses the HLL Jacobian of the same
+ * speeds; the adjoint refuses them.  The K variants call erf and exp, whose device results
+ * may differ from the C library's in the last bit: TY_MODE_EXACT is then within 1e-13 of the
+ * CPU restatement instead of bit-identical. */
+enum ty_scheme {
+  TY_SCH_HLLC = 1, TY_SCH_RUSANOV = 2, TY_SCH_ROE = 3, TY_SCH_AUSMM = 4, TY_SCH_HLLE = 5,
+  TY_SCH_HLLCB = 6, TY_SCH_HLLCK = 7, TY_SCH_HLLCKB = 8, TY_SCH_HLLEB = 9, TY_SCH_HLLEK = 10, TY_SCH_HLLEKB = 11
+};
 enum ty_highres { TY_HRES_NONE = 0, TY_HRES_MUSCL = 1, TY_HRES_MUSCLFAST = 2, TY_HRES_MUSCLUNS = 3 };
 enum ty_limiter {
   TY_LIM_NONE = 0, TY_LIM_MINMOD = 1, TY_LIM_ALBADA = 2, TY_LIM_VLEER = 3,

@@ -130,7 +130,12 @@ bool build_umesh(const RawMesh& raw, int geo_dim, const std::vector<BcDef>& bcs,
 
 // ---------------------------------------------------------------------------
 // Solver
-enum Scheme { SCH_HLLC = 1, SCH_RUSANOV = 2, SCH_ROE = 3, SCH_AUSMM = 4, SCH_HLLE = 5 };
+// HLLC and HLLE with Typhon's wave-speed variants (def_spat.f90:68-76): B = the beta of
+// calc_flux_hllc.f90:70-72 / calc_flux_hlle.f90:68-70, K = the kinetic (EFM) estimates
+enum Scheme { SCH_HLLC = 1, SCH_RUSANOV = 2, SCH_ROE = 3, SCH_AUSMM = 4, SCH_HLLE = 5, SCH_HLLCB = 6, SCH_HLLCK = 7,
+              SCH_HLLCKB = 8, SCH_HLLEB = 9, SCH_HLLEK = 10, SCH_HLLEKB = 11 };
+inline bool is_hllc(int s) { return s == SCH_HLLC || (s >= SCH_HLLCB && s <= SCH_HLLCKB); }
+inline bool is_hlle(int s) { return s == SCH_HLLE || (s >= SCH_HLLEB && s <= SCH_HLLEKB); }
 enum HighRes { HRES_NONE = 0, HRES_MUSCL = 1, HRES_MUSCLFAST = 2, HRES_MUSCLUNS = 3 };
 enum Limiter { LIM_NONE = 0, LIM_MINMOD = 1, LIM_ALBADA = 2, LIM_VLEER = 3, LIM_SBEE = 4,
                LIM_KIM3 = 5, LIM_LIM03 = 6 };

@@ -762,6 +762,34 @@ static void jacflux(double g, const double* st /* rho, p, u, v, w */, V3 fn, dou
   A(5, 5) = A(5, 5) + vn;
 }
 
+// Wave speeds of the HLLC / HLLE family (calc_flux_hllc.f90:64-124, calc_flux_hlle.f90:64-120):
+// beta = 1 or sqrt((g-1)/(2g)) (the B variants); the K variants take the kinetic (EFM)
+// estimates cl (m kinw + kind) with m = vn/cl -+ f1 beta, cl = a/f1, f1 = sqrt(g/2),
+// kinw = (1 -+ erf(m))/2, kind = -+ exp(-m^2) / (2 sqrt(pi)).  Standard HLLE clamps to 0,
+// the kinetic HLLE does not (calc_flux_hlle.f90:110-120).
+static void hll_wave_speeds(int scheme, double g, double vnl, double vnr, double al, double ar, double vm, double am,
+                            double& sl, double& sr) {
+  const bool b = scheme == SCH_HLLCB || scheme == SCH_HLLCKB || scheme == SCH_HLLEB || scheme == SCH_HLLEKB;
+  const bool kin = scheme == SCH_HLLCK || scheme == SCH_HLLCKB || scheme == SCH_HLLEK || scheme == SCH_HLLEKB;
+  const double beta = b ? std::sqrt((g - 1.0) / (2 * g)) : 1.0;
+  if (kin) {
+    const double PIcst = 3.141592653589793238462643;
+    const double f1 = std::sqrt(0.5 * g), f2 = 0.5 / std::sqrt(PIcst);
+    const double cl = al / f1, cr = ar / f1;
+    const double modml = vnl / cl - f1 * beta, modmr = vnr / cr + f1 * beta;
+    const double kinwl = 0.5 * (1.0 - std::erf(modml)), kinwr = 0.5 * (1.0 + std::erf(modmr));
+    const double kindl = -f2 * std::exp(-modml * modml), kindr = +f2 * std::exp(-modmr * modmr);
+    sl = std::min(cl * (modml * kinwl + kindl), vm - am);
+    sr = std::max(cr * (modmr * kinwr + kindr), vm + am);
+  } else if (is_hlle(scheme)) {
+    sl = std::min(std::min(0.0, vnl - beta * al), vm - am);
+    sr = std::max(std::max(0.0, vnr + beta * ar), vm + am);
+  } else {
+    sl = std::min(vnl - beta * al, vm - am);
+    sr = std::max(vnr + beta * ar, vm + am);
+  }
+}
+
 void Solver::face_fluxes() {
   const int nf = m->nface;
   const double g = sp.gamma;
@@ -771,7 +799,7 @@ void Solver::face_fluxes() {
     State L = face_state(cell_l, nf, f), R = face_state(cell_r, nf, f);
     V3 fn = m->fnormal[f];
     double F[5];
-    if (sp.scheme == SCH_HLLC) {  // calc_flux_hllc.f90:86-171, beta = 1
+    if (is_hllc(sp.scheme)) {  // calc_flux_hllc.f90:86-171
       // calc_roe_states.f90:35-53
       const double gig1 = g / (g - 1.0);
       double t1 = std::sqrt(R.rho / L.rho);
@@ -789,9 +817,8 @@ void Solver::face_fluxes() {
       double am = std::sqrt(g * roe_p / roe_rho);
       double rel = ig1 * L.p + 0.5 * L.rho * sqrabs(L.u);
       double rer = ig1 * R.p + 0.5 * R.rho * sqrabs(R.u);
-      const double beta = 1.0;
-      double sl = std::min(vnl - beta * al, vm - am);
-      double sr = std::max(vnr + beta * ar, vm + am);
+      double sl, sr;
+      hll_wave_speeds(sp.scheme, g, vnl, vnr, al, ar, vm, am, sl, sr);
       if (calc_jac) {  // calc_flux_hllc.f90:178-203 -> calc_jac_hll.f90:46-57
         double qL[5] = {L.rho, L.p, L.u.x, L.u.y, L.u.z}, qR[5] = {R.rho, R.p, R.u.x, R.u.y, R.u.z};
         double JL[25], JR[25];
@@ -836,7 +863,7 @@ void Solver::face_fluxes() {
         V3 mo = (Sst * rvst) + (pst * fn);
         F[2] = mo.x; F[3] = mo.y; F[4] = mo.z;
       }
-    } else if (sp.scheme == SCH_HLLE) {  // calc_flux_hlle.f90:83-150, beta = 1
+    } else if (is_hlle(sp.scheme)) {  // calc_flux_hlle.f90:83-150
       const double gig1 = g / (g - 1.0);
       double t1 = std::sqrt(R.rho / L.rho);  // calc_roe_states.f90:35-53
       double roe_rho = L.rho * t1;
@@ -853,8 +880,8 @@ void Solver::face_fluxes() {
       double am = std::sqrt(g * roe_p / roe_rho);
       double rel = ig1 * L.p + .5 * L.rho * sqrabs(L.u);
       double rer = ig1 * R.p + .5 * R.rho * sqrabs(R.u);
-      double sl = std::min(std::min(0.0, vnl - al), vm - am);
-      double sr = std::max(std::max(0.0, vnr + ar), vm + am);
+      double sl, sr;
+      hll_wave_speeds(sp.scheme, g, vnl, vnr, al, ar, vm, am, sl, sr);
       double iks = 1.0 / (sr - sl);
       double kl = sr * iks, kr = -sl * iks, ku = sl * sr * iks;
       F[0] = (kl * vnl - ku) * L.rho + (kr * vnr + ku) * R.rho;

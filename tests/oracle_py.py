@@ -16,6 +16,7 @@ LIB = ROOT / "oracle" / "build" / "liboracle.so"
 BC_PERIODIC, BC_SYMMETRY, BC_WALL, BC_FARFIELD, BC_NOSLIP, BC_HEAT = 1, 2, 3, 4, 5, 6
 BC_INLET_SUB, BC_OUTLET_SUB, BC_INLET_SUP, BC_OUTLET_SUP = 7, 8, 9, 10
 SCH_HLLC, SCH_RUSANOV, SCH_ROE, SCH_AUSMM, SCH_HLLE = 1, 2, 3, 4, 5
+SCH_HLLCB, SCH_HLLCK, SCH_HLLCKB, SCH_HLLEB, SCH_HLLEK, SCH_HLLEKB = 6, 7, 8, 9, 10, 11
 HRES_NONE, HRES_MUSCL, HRES_MUSCLFAST, HRES_MUSCLUNS = 0, 1, 2, 3
 LIM_NONE, LIM_MINMOD, LIM_ALBADA, LIM_VLEER, LIM_SBEE, LIM_KIM3, LIM_LIM03 = range(7)
 POSTLIM_NONE, POSTLIM_BARTH, POSTLIM_SUPERBARTH = 0, 1, 2

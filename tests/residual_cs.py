@@ -282,3 +282,11 @@ def rk_run(md, U0, dts, table, scheme="RUSANOV", highres="NONE", limiter="NONE",
             if c != 0.0:
                 U = U + c * Rs[s]
     return U
+
+
+def box_functional_derivative(md, U0, d, dts, table, box, scheme, highres="NONE", limiter="NONE", postlim="NONE",
+                              h=1e-30):
+    """Complex-step derivative along d of J(U0) = sum(box * rho^2) after an explicit run (the
+    reference of the adjoint's directional derivatives)."""
+    Uc = rk_run(md, U0 + 1j * h * d, dts, table, scheme, highres=highres, limiter=limiter, postlim=postlim)
+    return float(np.sum(box * Uc[0] ** 2).imag / h)

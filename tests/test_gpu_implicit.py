@@ -20,7 +20,8 @@ MXLAY_BCS = [("IMIN", op.BC_PERIODIC, "IMAX", (1.0, 0.0, 0.0)),
              ("JMAX", op.BC_WALL, "", (0.0, 0.0, 0.0), (1.0, 0.0, 0.0))]
 FARFIELD_BOX = [(f, op.BC_FARFIELD, "", (0.0, 0.0, 0.0)) for f in ("IMIN", "IMAX", "JMIN", "JMAX")]
 FREESTREAM = (1.0, 1.0 / 1.4, 0.5, 0.1, 0.0)   # M = 0.5 at a small angle
-OSCH = {"HLLC": op.SCH_HLLC, "RUSANOV": op.SCH_RUSANOV, "ROE": op.SCH_ROE}
+OSCH = {"HLLC": op.SCH_HLLC, "RUSANOV": op.SCH_RUSANOV, "ROE": op.SCH_ROE, "HLLCB": op.SCH_HLLCB,
+        "HLLEB": op.SCH_HLLEB}
 OHRES = {"NONE": op.HRES_NONE, "MUSCL": op.HRES_MUSCL, "MUSCL-FAST": op.HRES_MUSCLFAST, "MUSCL-UNS": op.HRES_MUSCLUNS}
 OLIM = {"NONE": op.LIM_NONE, "ALBADA": op.LIM_ALBADA, "MINMOD": op.LIM_MINMOD}
 OPOST = {"NONE": op.POSTLIM_NONE, "BARTH": op.POSTLIM_BARTH}
@@ -123,6 +124,8 @@ CASES = [
     ("mxlay2x20quad-h50.tym", "mxlay", "RUSANOV", "NONE", "NONE", "NONE", "FULL", False),
     ("quad20x20.tym", "farfield", "HLLC", "MUSCL", "ALBADA", "NONE", "NONE", True),
     ("quad20x20.tym", "farfield", "ROE", "NONE", "NONE", "NONE", "NONE", False),
+    ("quad20x20.tym", "periodic", "HLLCB", "NONE", "NONE", "NONE", "NONE", True),
+    ("quad20x20.tym", "farfield", "HLLEB", "MUSCL", "ALBADA", "NONE", "NONE", False),
 ]
 
 

@@ -45,8 +45,9 @@ int ty_adjoint_vjp(ty_mesh* h, double dt, const double* lamR, double* lamU) {
                    "Albada and the Barth post-limiter frozen (periodic boundaries)");
     return TY_ERR_UNSUPPORTED;
   }
-  if (h->o.scheme == TY_SCH_HLLE || h->o.scheme == TY_SCH_AUSMM || h->inout_bc) {
-    tyi::set_error("ty_adjoint_vjp: HLLE and AUSM-M fluxes and inlet / outlet boundaries have no adjoint");
+  if (h->o.scheme == TY_SCH_HLLE || h->o.scheme == TY_SCH_AUSMM || h->o.scheme > TY_SCH_HLLE || h->inout_bc) {
+    tyi::set_error("ty_adjoint_vjp: the HLLE and AUSM-M fluxes, the HLLC / HLLE wave-speed variants and inlet / "
+                   "outlet boundaries have no adjoint");
     return TY_ERR_UNSUPPORTED;
   }
   DevMesh& m = h->m;

@@ -571,7 +571,7 @@ int ty_set_bc_data(ty_mesh* h, const double* data) {
 
 int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
   if (!h || !p) return TY_ERR_ARG;
-  if (p->scheme < TY_SCH_HLLC || p->scheme > TY_SCH_HLLE || p->highres < 0 || p->highres > TY_HRES_MUSCLUNS ||
+  if (p->scheme < TY_SCH_HLLC || p->scheme > TY_SCH_HLLEKB || p->highres < 0 || p->highres > TY_HRES_MUSCLUNS ||
       p->limiter < 0 || p->limiter > TY_LIM_LIM03 || p->postlim < 0 || p->postlim > TY_POSTLIM_SUPERBARTH ||
       p->gradmeth < 0 || p->gradmeth > TY_GRAD_LSQW || (p->mode != TY_MODE_EXACT && p->mode != TY_MODE_FAST) ||
       !(p->gamma > 1.0)) {
@@ -609,6 +609,16 @@ int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
   h->o.inv_entropy_fix = p->entropy_fix > 0.0 ? 1.0 / p->entropy_fix : 0.0;
   h->o.ig1 = 1.0 / (p->gamma - 1.0);
   h->o.gig1 = p->gamma * h->o.ig1;
+  {  // the HLL family's wave-speed variant (def_spat.f90:68-76, calc_flux_hllc.f90:64-72)
+    const int sc = p->scheme;
+    h->o.hll_family = (sc == TY_SCH_HLLC || (sc >= TY_SCH_HLLCB && sc <= TY_SCH_HLLCKB)) ? 1
+                      : (sc == TY_SCH_HLLE || (sc >= TY_SCH_HLLEB && sc <= TY_SCH_HLLEKB)) ? 2 : 0;
+    const bool b = sc == TY_SCH_HLLCB || sc == TY_SCH_HLLCKB || sc == TY_SCH_HLLEB || sc == TY_SCH_HLLEKB;
+    h->o.hll_kin = (sc == TY_SCH_HLLCK || sc == TY_SCH_HLLCKB || sc == TY_SCH_HLLEK || sc == TY_SCH_HLLEKB) ? 1 : 0;
+    h->o.hll_beta = b ? std::sqrt((p->gamma - 1.0) / (2 * p->gamma)) : 1.0;
+    h->o.hll_f1 = std::sqrt(0.5 * p->gamma);
+    h->o.hll_f2 = 0.5 / std::sqrt(3.141592653589793238462643);
+  }
   h->o.viscous = p->viscous; h->o.visc_law = p->visc_law; h->o.visc_kin = p->visc_kin;
   h->o.rgas = p->rgas; h->o.prandtl = p->prandtl;
   for (int v = 0; v < 5; ++v) h->o.farfield[v] = p->farfield[v];

@@ -78,6 +78,10 @@ struct SpatOpts {
   double gamma, entropy_fix;
   double inv_entropy_fix;  // 1 / entropy_fix (fast-mode Roe flux)
   double ig1, gig1;        // 1 / (gamma - 1), gamma / (gamma - 1) (fast-mode fluxes)
+  // HLL family (TY_SCH_HLLC / HLLE and their B, K, KB variants): 1 HLLC, 2 HLLE, 0 other;
+  // kinetic wave speeds; beta; f1 = sqrt(gamma/2), f2 = 1/(2 sqrt(pi)) of the kinetic estimates
+  int hll_family, hll_kin;
+  double hll_beta, hll_f1, hll_f2;
   int viscous, visc_law;
   double visc_kin, rgas, prandtl;
   double farfield[5];  // free stream of far-field faces (rho, p, u, v, w)

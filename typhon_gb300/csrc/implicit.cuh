@@ -68,7 +68,7 @@ __device__ void face_jacobians(const SpatOpts& o, const double* L, const double*
     return;
   }
   double sl, sr;
-  if (o.scheme == TY_SCH_HLLC || o.scheme == TY_SCH_HLLE) {  // HLLC / HLLE wave speeds (calc_flux_hllc.f90:86-118, calc_flux_hlle.f90:83-110, beta = 1)
+  if (o.hll_family != 0) {  // the HLLC / HLLE family's wave speeds (calc_flux_hllc.f90:86-124, calc_flux_hlle.f90:83-120)
     const double gig1 = g / (g - 1.0);
     double t1 = sqrt(R[0] / L[0]);
     double roe_rho = L[0] * t1;
@@ -83,10 +83,11 @@ __device__ void face_jacobians(const SpatOpts& o, const double* L, const double*
     double roe_p = (h1 - 0.5 * (rux * rux + ruy * ruy + ruz * ruz)) * roe_rho / gig1;
     double vm = rux * nx + ruy * ny + ruz * nz;
     double am = sqrt(g * roe_p / roe_rho);
-    sl = fmin(vnl - 1.0 * al, vm - am);
-    sr = fmax(vnr + 1.0 * ar, vm + am);
-    sl = fmin(sl, 0.0);
-    sr = fmax(sr, 0.0);
+    hll_speeds(o, vnl, vnr, al, ar, vm, am, sl, sr);
+    if (o.hll_family == 1) {  // calc_flux_hllc.f90 passes min(sl, 0), max(sr, 0) to calc_jac_hll
+      sl = fmin(sl, 0.0);
+      sr = fmax(sr, 0.0);
+    }
   } else {  // Roe flux: HLL Jacobian with Einfeldt's speeds from the Roe average (new)
     double t1 = sqrt(R[0] / L[0]);
     double kl = 1.0 / (1.0 + t1), kr = t1 * kl;

@@ -432,8 +432,34 @@ __device__ __forceinline__ void mirror(const DevMesh& m, int f, double q[5]) {
 // ---------------------------------------------------------------------------
 // Riemann fluxes per unit area, F = (mass, energy, momentum x, y, z)
 
+// Outer wave speeds of the HLL family (calc_flux_hllc.f90:64-124, calc_flux_hlle.f90:64-120):
+// beta = 1 (HLLC, HLLE, K) or sqrt((g-1)/(2g)) (B, KB variants); the kinetic variants take the
+// EFM estimates c (m kinw + kind), m = vn/c -+ f1 beta, c = a/f1, kinw = (1 -+ erf m)/2,
+// kind = -+ f2 exp(-m^2).  Standard HLLE speeds are clamped to 0, the kinetic ones are not.
+__device__ __forceinline__ void hll_speeds(const SpatOpts& o, double vnl, double vnr, double al, double ar, double vm,
+                                           double am, double& sl, double& sr) {
+  const double beta = o.hll_beta;
+  if (o.hll_kin) {
+    const double f1 = o.hll_f1, f2 = o.hll_f2;
+    const double cl = al / f1, cr = ar / f1;
+    const double modml = vnl / cl - f1 * beta, modmr = vnr / cr + f1 * beta;
+    const double kinwl = 0.5 * (1.0 - erf(modml)), kinwr = 0.5 * (1.0 + erf(modmr));
+    const double kindl = -f2 * exp(-modml * modml), kindr = +f2 * exp(-modmr * modmr);
+    sl = fmin(cl * (modml * kinwl + kindl), vm - am);
+    sr = fmax(cr * (modmr * kinwr + kindr), vm + am);
+  } else if (o.hll_family == 2) {
+    sl = fmin(fmin(0.0, vnl - beta * al), vm - am);
+    sr = fmax(fmax(0.0, vnr + beta * ar), vm + am);
+  } else {
+    sl = fmin(vnl - beta * al, vm - am);
+    sr = fmax(vnr + beta * ar, vm + am);
+  }
+}
+
 // calc_flux_hlle.f90:83-150 (beta = 1), the Roe average of calc_roe_states.f90:37-53
-__device__ void flux_hlle(double g, const double* L, const double* R, double nx, double ny, double nz, double* F) {
+__device__ void flux_hlle(const SpatOpts& o, const double* L, const double* R, double nx, double ny, double nz,
+                          double* F) {
+  const double g = o.gamma;
   const double ig1 = 1.0 / (g - 1.0);
   const double gig1 = g / (g - 1.0);
   double t1 = sqrt(R[0] / L[0]);
@@ -455,8 +481,8 @@ __device__ void flux_hlle(double g, const double* L, const double* R, double nx,
   double am = sqrt(g * roe_p / roe_rho);
   double rel = ig1 * L[1] + .5 * L[0] * sqL;
   double rer = ig1 * R[1] + .5 * R[0] * sqR;
-  double sl = fmin(fmin(0.0, vnl - al), vm - am);
-  double sr = fmax(fmax(0.0, vnr + ar), vm + am);
+  double sl, sr;
+  hll_speeds(o, vnl, vnr, al, ar, vm, am, sl, sr);
   double iks = 1.0 / (sr - sl);
   double kl = sr * iks, kr = -sl * iks, ku = sl * sr * iks;
   double wl = kl * vnl - ku, wr = kr * vnr + ku;
@@ -492,7 +518,9 @@ __device__ void flux_ausmm(double g, const double* L, const double* R, double nx
   F[3] = ml * L[3] + mr * R[3] + pf * ny;
   F[4] = ml * L[4] + mr * R[4] + pf * nz;
 }
-__device__ void flux_hllc(double g, const double* L, const double* R, double nx, double ny, double nz, double* F) {
+__device__ void flux_hllc(const SpatOpts& o, const double* L, const double* R, double nx, double ny, double nz,
+                          double* F) {
+  const double g = o.gamma;
   const double ig1 = 1.0 / (g - 1.0);
   const double gig1 = g / (g - 1.0);
   // calc_roe_states.f90:37-53
@@ -516,9 +544,8 @@ __device__ void flux_hllc(double g, const double* L, const double* R, double nx,
   double am = sqrt(g * roe_p / roe_rho);
   double rel = ig1 * L[1] + 0.5 * L[0] * sqL;
   double rer = ig1 * R[1] + 0.5 * R[0] * sqR;
-  const double beta = 1.0;
-  double sl = fmin(vnl - beta * al, vm - am);
-  double sr = fmax(vnr + beta * ar, vm + am);
+  double sl, sr;
+  hll_speeds(o, vnl, vnr, al, ar, vm, am, sl, sr);
   if (sl >= 0.0) {
     F[0] = vnl * L[0];
     F[1] = vnl * (rel + L[1]);
@@ -703,7 +730,8 @@ __device__ void flux_hllc_fast(const SpatOpts& o, const double* L, const double*
   const double vm = rux * nx + ruy * ny + ruz * nz;
   const double am = sqrt_nr((g - 1.0) * (hroe - 0.5 * (rux * rux + ruy * ruy + ruz * ruz)));
   const double rel = ig1 * L[1] + 0.5 * L[0] * sqL, rer = ig1 * R[1] + 0.5 * R[0] * sqR;
-  const double sl = fmin(vnl - al, vm - am), sr = fmax(vnr + ar, vm + am);
+  double sl, sr;
+  hll_speeds(o, vnl, vnr, al, ar, vm, am, sl, sr);
   if (sl >= 0.0) {
     const double m0 = vnl * L[0];
     F[0] = m0; F[1] = vnl * (rel + L[1]);
@@ -826,8 +854,8 @@ __device__ __forceinline__ void face_flux_fast(const DevMesh& m, const DevState&
     flux_roe_fast(o, QL, QR, nx, ny, nz, S, F);
   } else {
     if (o.scheme == TY_SCH_ROE) flux_roe_fast(o, QL, QR, nx, ny, nz, 1.0, F);
-    else if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o, QL, QR, nx, ny, nz, F);
-    else if (o.scheme == TY_SCH_HLLE) flux_hlle(o.gamma, QL, QR, nx, ny, nz, F);
+    else if (o.hll_family == 1) flux_hllc_fast(o, QL, QR, nx, ny, nz, F);
+    else if (o.hll_family == 2) flux_hlle(o, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_AUSMM) flux_ausmm(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
     if (o.viscous != TY_VISC_NONE) add_viscous(m, s, o, f, F);
@@ -844,15 +872,15 @@ __device__ __forceinline__ void face_flux(const DevMesh& m, const DevState& s, c
   const double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
   double F[5];
   if constexpr (kFast) {
-    if (o.scheme == TY_SCH_HLLC) flux_hllc_fast(o, QL, QR, nx, ny, nz, F);
+    if (o.hll_family == 1) flux_hllc_fast(o, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
-    else if (o.scheme == TY_SCH_HLLE) flux_hlle(o.gamma, QL, QR, nx, ny, nz, F);
+    else if (o.hll_family == 2) flux_hlle(o, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_AUSMM) flux_ausmm(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_roe_fast(o, QL, QR, nx, ny, nz, 1.0, F);  // unit surface
   } else {
-    if (o.scheme == TY_SCH_HLLC) flux_hllc(o.gamma, QL, QR, nx, ny, nz, F);
+    if (o.hll_family == 1) flux_hllc(o, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_RUSANOV) flux_rusanov(o.gamma, QL, QR, nx, ny, nz, F);
-    else if (o.scheme == TY_SCH_HLLE) flux_hlle(o.gamma, QL, QR, nx, ny, nz, F);
+    else if (o.hll_family == 2) flux_hlle(o, QL, QR, nx, ny, nz, F);
     else if (o.scheme == TY_SCH_AUSMM) flux_ausmm(o.gamma, QL, QR, nx, ny, nz, F);
     else flux_roe(o.gamma, o.entropy_fix, QL, QR, nx, ny, nz, F);
   }

@@ -21,7 +21,8 @@ from .umesh import MeshDesc
 
 # option names as in Typhon's SPAT_PARAM / TIME_PARAM blocks (SOURCE/PARAM/def_spat.f90,
 # def_time.f90) -> C ABI enum values
-SCHEME = {"HLLC": 1, "RUSANOV": 2, "ROE": 3, "AUSMM": 4, "HLLE": 5, "HLL": 5}
+SCHEME = {"HLLC": 1, "RUSANOV": 2, "ROE": 3, "AUSMM": 4, "HLLE": 5, "HLL": 5, "HLLCB": 6, "HLLCK": 7, "HLLCKB": 8,
+          "HLLEB": 9, "HLLEK": 10, "HLLEKB": 11}
 HIGHRES = {"NONE": 0, "MUSCL": 1, "MUSCL-FAST": 2, "MUSCL-UNS": 3}
 LIMITER = {"NONE": 0, "MINMOD": 1, "ALBADA": 2, "VAN_ALBADA": 2, "VAN_LEER": 3, "VANLEER": 3, "SUPERBEE": 4,
            "KIM3": 5, "LIM03": 6}
