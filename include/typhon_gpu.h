@@ -228,6 +228,13 @@ int ty_debug_fastmath(int32_t which, int32_t n, const double* x, double* y);
 /* Inlet / outlet parameters per face: host [nface][6] (see ty_bc; rows of other faces are
  * ignored).  Required before a Navier-Stokes operation on a mesh with inlets or outlets. */
 int ty_set_bc_data(ty_mesh* mesh, const double* data);
+/* Rotational periodicity: the rotation of each face [nface][9] (ty_umesh_face_rotation).  Ghost
+ * states of rotational periodic faces take the partner cell's state with the velocity rotated
+ * (R u), their gradients R g for the scalars and G R^T for the velocity (Typhon's transten_per
+ * multiplies on the right only), and the right face states take the partner face's left
+ * state with the velocity rotated (calcboco_connect_per_match.f90:56-78).  The implicit step
+ * follows; the adjoint and heat conduction refuse such a mesh. */
+int ty_mesh_set_face_rotation(ty_mesh* mesh, const double* rot);
 
 /* Wait for the handle's stream. */
 int ty_synchronize(ty_mesh* mesh);
@@ -436,6 +443,19 @@ int ty_umesh_add_vertex_mark(ty_umesh* um, const char* family, int32_t ntag, con
  * partner family and the translation from this family to the partner. */
 int ty_umesh_add_bc(ty_umesh* um, const char* family, int32_t kind, const char* partner,
                     const double* translation3, const double* wallvel3);
+/* Makes the periodic definition of `family` (added by ty_umesh_add_bc) a rotation: BLOCK:
+ * PERIODICITY TYPE = ROTATION with ROTATION_CENTER, ROTATION_AXIS (normalised here) and
+ * ROTATION_ANGLE in degrees (def_mesh.f90:230-247), from this family to its partner.  The
+ * faces are matched after rotating their centres (transloc_per, MESHPARAMS.f90:125-146) and
+ * each ghost centre is the face centre plus the partner's face-to-cell vector rotated back
+ * (init_connect_grid.f90:210-225). */
+int ty_umesh_set_rotation(ty_umesh* um, const char* family, const double* centre3, const double* axis3,
+                          double angle_deg);
+/* The rotation of each face [nface*9], row-major: the one that brings vectors of the
+ * partner's frame into the face's frame on faces of rotational periodic families (calc_rot of
+ * transvec_per, VEC3D.f90:652-674), the identity elsewhere.  Returns 1 when a family is
+ * rotational, 0 otherwise (then pass nothing to ty_mesh_set_face_rotation). */
+int ty_umesh_face_rotation(const ty_umesh* um, double* out);
 int ty_umesh_build(ty_umesh* um, int32_t dim);
 /* Pointers into the built description (valid until ty_umesh_free). */
 int ty_umesh_desc(const ty_umesh* um, ty_mesh_desc* out);

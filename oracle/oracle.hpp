@@ -97,7 +97,17 @@ struct BcDef {
   // wall: wall velocity
   V3 wall_velocity;
   double data[6] = {0, 0, 0, 0, 0, 0};  // inlet / outlet parameters (BcKind)
+  // periodic by rotation (BLOCK:PERIODICITY TYPE = ROTATION, MESHPARAMS.f90:125-205): centre,
+  // unit axis, angle in radians from this family to the partner (translation then unused)
+  bool rotation = false;
+  V3 rot_centre, rot_axis;
+  double rot_angle = 0.0;
 };
+
+// calc_rot (CFDTOOLS/Math/VEC3D.f90:652-674): row-major rotation about the unit axis
+void calc_rot(V3 axis, double angle, double* M);
+// M v, summed in column order
+V3 rot_apply(const double* M, V3 v);
 
 struct Boco {
   std::string family;
@@ -108,6 +118,10 @@ struct Boco {
   std::vector<int> partner_face;  // periodic: partner face of each face
   V3 wall_velocity;
   double data[6] = {0, 0, 0, 0, 0, 0};
+  // periodic by rotation: the rotation bringing the partner's vectors into this family's
+  // frame (calc_rot of the angle -rlink * angle, transvec_per), row-major
+  bool rotation = false;
+  double rot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
 };
 
 // Preprocessed mesh in Typhon's numbering (st_ustmesh).

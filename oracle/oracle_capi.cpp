@@ -19,6 +19,7 @@ namespace {
 struct MeshHandle {
   RawMesh raw;
   UMesh m;
+  std::vector<BcDef> rotations;  // periodic families by rotation (family, centre, axis, angle)
 };
 void set_err(char* buf, int len, const std::string& s) {
   if (buf && len > 0) {
@@ -89,11 +90,43 @@ int ory_mesh_build(void* h, int geo_dim, int nbc, const char* const* fam, const 
                    char* err, int errlen) {
   auto* mh = (MeshHandle*)h;
   std::string e;
-  if (!build_umesh(mh->raw, geo_dim, make_bcs(nbc, fam, kind, partner, trans, wallvel, bcdata), mh->m, e)) {
+  std::vector<BcDef> bcs = make_bcs(nbc, fam, kind, partner, trans, wallvel, bcdata);
+  for (auto& b : bcs)
+    for (const auto& r : mh->rotations)
+      if (r.family == b.family) {
+        b.rotation = true;
+        b.rot_centre = r.rot_centre;
+        b.rot_axis = r.rot_axis;
+        b.rot_angle = r.rot_angle;
+      }
+  if (!build_umesh(mh->raw, geo_dim, bcs, mh->m, e)) {
     set_err(err, errlen, e);
     return -1;
   }
   return 0;
+}
+// A periodic family connected to its partner by a rotation (BLOCK:PERIODICITY TYPE =
+// ROTATION): centre, axis (normalised here), angle in degrees (def_mesh.f90:242-247), from
+// this family to the partner.  Call before ory_mesh_build.
+void ory_raw_set_rotation(void* h, const char* family, const double* centre, const double* axis, double angle_deg) {
+  BcDef r;
+  r.family = family;
+  r.rot_centre = v3(centre[0], centre[1], centre[2]);
+  V3 a = v3(axis[0], axis[1], axis[2]);
+  r.rot_axis = a / vabs(a);
+  r.rot_angle = angle_deg / 180.0 * 3.141592653589793238462643;
+  ((MeshHandle*)h)->rotations.push_back(r);
+}
+// Rotation of each face [nface][9], row-major: the one bringing the partner's vectors into
+// this face's frame on faces of rotational periodic families, identity elsewhere.
+void ory_mesh_face_rotation(void* h, double* out) {
+  auto& m = ((MeshHandle*)h)->m;
+  for (int f = 0; f < m.nface; ++f)
+    for (int k = 0; k < 9; ++k) out[9 * f + k] = (k % 4 == 0) ? 1.0 : 0.0;
+  for (auto& b : m.bocos)
+    if (b.rotation)
+      for (int f : b.iface)
+        for (int k = 0; k < 9; ++k) out[9 * f + k] = b.rot[k];
 }
 // sizes: ncell_int, ncell, nface_int, nface, ncolors, dim, nboco
 void ory_mesh_sizes(void* h, int* out) {

@@ -22,6 +22,22 @@
 
 namespace ory {
 
+void calc_rot(V3 axis, double angle, double* M) {
+  const double costh = std::cos(angle), sinth = std::sin(angle);
+  const double a[3] = {axis.x, axis.y, axis.z};
+  M[0] = costh; M[4] = costh; M[8] = costh;
+  M[1] = -axis.z * sinth; M[2] = +axis.y * sinth;
+  M[3] = +axis.z * sinth; M[5] = -axis.x * sinth;
+  M[6] = -axis.y * sinth; M[7] = +axis.x * sinth;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) M[3 * i + j] = M[3 * i + j] + (1.0 - costh) * a[i] * a[j];
+}
+
+V3 rot_apply(const double* M, V3 v) {
+  return v3(M[0] * v.x + M[1] * v.y + M[2] * v.z, M[3] * v.x + M[4] * v.y + M[5] * v.z,
+            M[6] * v.x + M[7] * v.y + M[8] * v.z);
+}
+
 int elem_dim(int t) {
   switch (t) {
     case ELEM_BAR2: return 1;
@@ -517,7 +533,15 @@ bool build_umesh(const RawMesh& raw, int geo_dim, const std::vector<BcDef>& bcs,
     const BcDef& d = bcs[b.def];
     const int nf = (int)b.iface.size();
     std::vector<V3> vv1(nf);
-    for (int i = 0; i < nf; ++i) vv1[i] = m.fcentre[b.iface[i]] + b.rlink * d.translation;
+    if (d.rotation) {  // transloc_per: rotate the face centres about the centre by rlink * angle
+      double M[9];
+      calc_rot(d.rot_axis, b.rlink * d.rot_angle, M);
+      for (int i = 0; i < nf; ++i) vv1[i] = rot_apply(M, m.fcentre[b.iface[i]] - d.rot_centre) + d.rot_centre;
+      b.rotation = true;
+      calc_rot(d.rot_axis, -b.rlink * d.rot_angle, b.rot);
+    } else {
+      for (int i = 0; i < nf; ++i) vv1[i] = m.fcentre[b.iface[i]] + b.rlink * d.translation;
+    }
     const Boco* b2 = nullptr;
     for (auto& o : m.bocos)
       if (o.kind == BC_PERIODIC && o.def == b.def && o.rlink * b.rlink < 0) {
@@ -547,6 +571,7 @@ bool build_umesh(const RawMesh& raw, int geo_dim, const std::vector<BcDef>& bcs,
       int f = b.iface[a], fp = b.partner_face[a];
       int g = c2[f] - 1, icper = c1[fp] - 1;
       V3 dfc = m.ccentre[icper] - m.fcentre[fp];  // translation: vector unchanged
+      if (b.rotation) dfc = rot_apply(b.rot, dfc);  // transvec_per(-rlink) (init_connect_grid.f90:218-223)
       m.cvol[g] = m.cvol[icper];
       m.ccentre[g] = m.fcentre[f] + dfc;
     }

@@ -225,6 +225,10 @@ void Solver::boco_cell_state() {
       if (b.kind == BC_PERIODIC) {
         int s = m->fc1[b.partner_face[k]];
         for (int v = 0; v < 5; ++v) prim[v * nc + g] = prim[v * nc + s];
+        if (b.rotation) {  // transvec_per: the velocity rotated into this family's frame
+          V3 u = rot_apply(b.rot, v3(prim[2 * nc + s], prim[3 * nc + s], prim[4 * nc + s]));
+          prim[2 * nc + g] = u.x; prim[3 * nc + g] = u.y; prim[4 * nc + g] = u.z;
+        }
       } else if (b.kind == BC_SYMMETRY) {
         // calcboco_ust_sym: mirror the velocity across the face plane
         int i = m->fc1[f];
@@ -282,6 +286,20 @@ void Solver::boco_cell_grad() {
       int g = m->fc2[b.iface[k]];
       int s = m->fc1[b.partner_face[k]];
       for (int v = 0; v < 15; ++v) grad[v * nc + g] = grad[v * nc + s];
+      if (b.rotation) {
+        // scalar gradients: vectors, R g (transvec_per); the velocity gradient tensor
+        // G(i,j) = du_i/dx_j: G R^T (transten_per -> t3d_rot, TENSOR3.f90:328-340)
+        const double* R = b.rot;
+        for (int q = 0; q < 2; ++q) {
+          V3 gq = rot_apply(R, v3(grad[(3 * q) * nc + s], grad[(3 * q + 1) * nc + s], grad[(3 * q + 2) * nc + s]));
+          grad[(3 * q) * nc + g] = gq.x; grad[(3 * q + 1) * nc + g] = gq.y; grad[(3 * q + 2) * nc + g] = gq.z;
+        }
+        for (int i = 0; i < 3; ++i) {
+          double G[3];
+          for (int j = 0; j < 3; ++j) G[j] = grad[(6 + 3 * i + j) * nc + s];
+          for (int j = 0; j < 3; ++j) grad[(6 + 3 * i + j) * nc + g] = G[0] * R[3 * j] + G[1] * R[3 * j + 1] + G[2] * R[3 * j + 2];
+        }
+      }
     }
   }
 }
@@ -297,6 +315,10 @@ void Solver::boco_face_state() {
       if (b.kind == BC_PERIODIC) {
         int fp = b.partner_face[k];
         for (int v = 0; v < 5; ++v) cell_r[v * nf + f] = cell_l[v * nf + fp];
+        if (b.rotation) {
+          V3 u = rot_apply(b.rot, v3(cell_l[2 * nf + fp], cell_l[3 * nf + fp], cell_l[4 * nf + fp]));
+          cell_r[2 * nf + f] = u.x; cell_r[3 * nf + f] = u.y; cell_r[4 * nf + f] = u.z;
+        }
       } else if (b.kind == BC_WALL || b.kind == BC_NOSLIP) {
         // setboco_ns_flux.f90, face-state mode: cell_r takes cell_l's PRESSURE as its density
         // ("weak BC"), cell_l's pressure, and the velocity reflected about the wall velocity;

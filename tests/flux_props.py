@@ -81,3 +81,68 @@ def vortex_exact(cases, xy, t, length=10.0, mach=0.5, gamma=GAMMA):
 
 def l1_density_error(rho, rho_exact, vol):
     return float(np.sum(np.abs(rho - rho_exact) * vol) / np.sum(vol))
+
+
+def rotation_z(deg):
+    t = np.radians(deg)
+    return np.array([[np.cos(t), -np.sin(t), 0.0], [np.sin(t), np.cos(t), 0.0], [0.0, 0.0, 1.0]])
+
+
+def exact_sector(raw, right="RIGHT", left="LEFT", angle=30.0):
+    """A copy of a 2D sector mesh whose `left` boundary vertices are moved onto the exact
+    rotation of the matching `right` boundary vertices (mesh files store coordinates to
+    single-precision-like accuracy), so that the sector is periodic to rounding."""
+    import dataclasses
+    bar = [(t, ie, c) for t, ie, c in raw.sections if t == 2][0]
+    pos = {e: i for i, e in enumerate(bar[1])}
+
+    def verts(fam):
+        tags = [m[1] for m in raw.marks if m[0] == fam][0]
+        return np.unique(bar[2][[pos[t] for t in tags]].reshape(-1)) - 1
+
+    vr, vl = verts(right), verts(left)
+    vt = raw.vtex.copy()
+    rot = vt[vr] @ rotation_z(angle).T
+    for i in vl:
+        j = np.argmin(np.linalg.norm(rot - vt[i], axis=1))
+        vt[i] = rot[j]
+    return dataclasses.replace(raw, vtex=vt)
+
+
+def tiled_annulus(raw, copies=12, angle=30.0, keep=("RMIN", "RMAX")):
+    """The full ring of `copies` rotated copies of a periodic sector mesh (coincident vertices
+    merged, so the periodic sides become interior faces); the marks in `keep` are gathered
+    over all copies.  Cells of copy 0 come first, in the sector's order."""
+    import dataclasses
+    from scipy.spatial import cKDTree
+    n = raw.vtex.shape[0]
+    allv = np.concatenate([raw.vtex @ rotation_z(angle * k).T for k in range(copies)])
+    tree = cKDTree(allv)
+    ident = np.arange(len(allv))
+    for i, j in sorted(tree.query_pairs(1e-9)):
+        ident[j] = min(ident[j], ident[i])
+    ident = ident[ident]                                  # first occurrence of each position
+    used, newid = np.unique(ident, return_inverse=True)
+    vt = allv[used]
+    sections, marks = [], []
+    nextel = 1
+    for t, ie, c in raw.sections:
+        if t == 2:
+            continue
+        conn = np.concatenate([newid[c - 1 + n * k] + 1 for k in range(copies)]).astype(np.int32)
+        sections.append((t, np.arange(nextel, nextel + len(conn), dtype=np.int32), conn))
+        nextel += len(conn)
+    bar = [(t, ie, c) for t, ie, c in raw.sections if t == 2][0]
+    pos = {e: i for i, e in enumerate(bar[1])}
+    bconn, btag = [], {}
+    for fam in keep:
+        tags = [m[1] for m in raw.marks if m[0] == fam][0]
+        rows = bar[2][[pos[t] for t in tags]]
+        ids = []
+        for k in range(copies):
+            ids.extend(range(nextel + len(bconn), nextel + len(bconn) + len(rows)))
+            bconn.extend((newid[rows - 1 + n * k] + 1).tolist())
+        btag[fam] = np.array(ids, dtype=np.int32)
+    sections.append((2, np.arange(nextel, nextel + len(bconn), dtype=np.int32), np.array(bconn, dtype=np.int32)))
+    marks = [(fam, btag[fam]) for fam in keep]
+    return dataclasses.replace(raw, vtex=vt, sections=sections, marks=marks)

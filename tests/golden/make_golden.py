@@ -21,7 +21,7 @@ REF = pathlib.Path(sys.argv[1])
 HERE = pathlib.Path(__file__).resolve().parent
 
 MESHES = ["quad20x20.tym", "quad20x10.tym", "quad10x10.tym", "tri5x10.tym", "mxlay2x20quad-h50.tym",
-          "tube.cgns", "square-quad10.cgns", "rect4x1.cgns", "expansion-10.cgns"]
+          "tube.cgns", "square-quad10.cgns", "rect4x1.cgns", "expansion-10.cgns", "perrot2d.cgns"]
 CASES = {
     "RK2": "NRG/TIME/RUNGEKUTTA/RK2/RHOERR.tmon",
     "RK2-SSP": "NRG/TIME/RUNGEKUTTA/RK2-SSP/RHOERR.tmon",
@@ -32,6 +32,7 @@ CASES = {
     "RK12BS": "NRG/TIME/RUNGEKUTTA/RK12BS/RHOERR.tmon",
     "RK13BS": "NRG/TIME/RUNGEKUTTA/RK13BS/RHOERR.tmon",
     "PER2D-TRANS": "NRG/MESH/CON/PER2D-TRANS/RHODEV.tmon",
+    "PER2D-ROT": ["NRG/MESH/CON/PER2D-ROT/histovarNS_RMIN", "NRG/MESH/CON/PER2D-ROT/histovarNS_RMAX"],
     "TYM-QUAD": "NRG/MESH/ELEM/TYM-QUAD/PAVG.tmon",
     "VISCOUS-CELLAVG-DELTA": "NRG/NS/NUM/FLUX/VISCOUS/CELLAVG/DELTA.tmon",
     "VISCOUS-CELLAVG-VXERR": "NRG/NS/NUM/FLUX/VISCOUS/CELLAVG/VXERR.tmon",

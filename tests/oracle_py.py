@@ -45,6 +45,8 @@ def load():
         lib.ory_raw_add_mark.argtypes = [vp, C.c_char_p, C.c_int, vp]
         lib.ory_raw_add_vertex_mark.argtypes = [vp, C.c_char_p, C.c_int, vp]
         lib.ory_mesh_build.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, C.c_char_p, C.c_int]
+        lib.ory_raw_set_rotation.argtypes = [vp, C.c_char_p, vp, vp, C.c_double]
+        lib.ory_mesh_face_rotation.argtypes = [vp, vp]
         lib.ory_mesh_sizes.argtypes = [vp, vp]
         lib.ory_mesh_export.argtypes = [vp] + [vp] * 11
         lib.ory_mesh_facevtex.argtypes = [vp, C.c_int, vp]
@@ -135,9 +137,14 @@ class Mesh:
             add(m.h, name.encode(), t.shape[0], _p(t))
         return m
 
-    def build(self, dim, bcs):
+    def build(self, dim, bcs, rotations=None):
         """bcs: list of (family, kind, partner, translation(3)[, wall_velocity(3)[, data(6)]]),
-        data the inlet / outlet parameters of BcKind."""
+        data the inlet / outlet parameters of BcKind; rotations: {family: (centre(3), axis(3),
+        angle in degrees)} for periodic families connected by a rotation."""
+        for fam_, (ctr, ax, ang) in (rotations or {}).items():
+            c3 = np.ascontiguousarray(ctr, np.float64)
+            a3 = np.ascontiguousarray(ax, np.float64)
+            self.lib.ory_raw_set_rotation(self.h, fam_.upper().encode(), _p(c3), _p(a3), float(ang))
         n = len(bcs)
         fam = (C.c_char_p * n)(*[b[0].encode() for b in bcs])
         kind = np.array([b[1] for b in bcs], dtype=np.int32)
@@ -156,6 +163,12 @@ class Mesh:
         (self.ncell_int, self.ncell, self.nface_int, self.nface, self.ncolors, self.dim,
          self.nboco) = map(int, s)
         return self
+
+    def face_rotation(self):
+        """[nface, 3, 3]: the rotation into each face's frame (identity off rotational faces)."""
+        out = np.zeros(9 * self.nface)
+        self.lib.ory_mesh_face_rotation(self.h, _p(out))
+        return out.reshape(self.nface, 3, 3)
 
     def export(self):
         nf, nc = self.nface, self.ncell

@@ -99,6 +99,7 @@ _SIGS = {
     "ty_debug_get": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
     "ty_debug_fastmath": ([C.c_int32, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "ty_set_bc_data": ([C.c_void_p, C.c_void_p], C.c_int),
+    "ty_mesh_set_face_rotation": ([C.c_void_p, C.c_void_p], C.c_int),
     "ty_synchronize": ([C.c_void_p], C.c_int),
     "ty_set_stream": ([C.c_void_p, C.c_void_p], C.c_int),
     "ty_profile_enable": ([C.c_void_p, C.c_int32], C.c_int),
@@ -125,6 +126,8 @@ _SIGS = {
     "ty_umesh_add_mark": ([C.c_void_p, C.c_char_p, C.c_int32, C.c_void_p], C.c_int),
     "ty_umesh_add_vertex_mark": ([C.c_void_p, C.c_char_p, C.c_int32, C.c_void_p], C.c_int),
     "ty_umesh_face_family": ([C.c_void_p, C.c_void_p], C.c_int),
+    "ty_umesh_set_rotation": ([C.c_void_p, C.c_char_p, C.c_void_p, C.c_void_p, C.c_double], C.c_int),
+    "ty_umesh_face_rotation": ([C.c_void_p, C.c_void_p], C.c_int),
     "ty_umesh_add_bc": ([C.c_void_p, C.c_char_p, C.c_int32, C.c_char_p, C.c_void_p, C.c_void_p], C.c_int),
     "ty_umesh_build": ([C.c_void_p, C.c_int32], C.c_int),
     "ty_umesh_desc": ([C.c_void_p, C.POINTER(MeshDesc)], C.c_int),

@@ -45,6 +45,10 @@ int ty_adjoint_vjp(ty_mesh* h, double dt, const double* lamR, double* lamU) {
                    "Albada and the Barth post-limiter frozen (periodic boundaries)");
     return TY_ERR_UNSUPPORTED;
   }
+  if (h->m.frot) {
+    tyi::set_error("ty_adjoint_vjp: no adjoint on meshes with rotational periodicity");
+    return TY_ERR_UNSUPPORTED;
+  }
   if (h->o.scheme == TY_SCH_HLLE || h->o.scheme == TY_SCH_AUSMM || h->o.scheme > TY_SCH_HLLE || h->inout_bc) {
     tyi::set_error("ty_adjoint_vjp: the HLLE and AUSM-M fluxes, the HLLC / HLLE wave-speed variants and inlet / "
                    "outlet boundaries have no adjoint");

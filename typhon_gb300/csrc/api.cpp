@@ -569,6 +569,29 @@ int ty_set_bc_data(ty_mesh* h, const double* data) {
   return TY_OK;
 }
 
+int ty_mesh_set_face_rotation(ty_mesh* h, const double* rot) {
+  if (!h || !rot) return TY_ERR_ARG;
+  TY_CU(cudaSetDevice(h->device));
+  const int nf = h->m.nf;
+  const size_t lf = h->m.ldf;
+  std::vector<double> d(9 * lf, 0.0);
+  bool any = false;
+  for (int f = 0; f < nf; ++f)
+    for (int q = 0; q < 9; ++q) {
+      const double v = rot[9 * (size_t)f + q];
+      d[q * lf + f] = v;
+      any = any || v != ((q % 4 == 0) ? 1.0 : 0.0);
+    }
+  if (!any) return TY_OK;  // translations only: nothing to rotate
+  if (!h->m.frot) {
+    if (int rc = h->upload(h->m.frot, d)) return rc;
+  } else {
+    TY_CU(cudaMemcpy(const_cast<double*>(h->m.frot), d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  h->prim_valid = false;
+  return TY_OK;
+}
+
 int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
   if (!h || !p) return TY_ERR_ARG;
   if (p->scheme < TY_SCH_HLLC || p->scheme > TY_SCH_HLLEKB || p->highres < 0 || p->highres > TY_HRES_MUSCLUNS ||

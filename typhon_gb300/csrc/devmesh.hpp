@@ -54,6 +54,9 @@ struct DevMesh {
   const double* geo2 = nullptr;   // [nci] 2 V / sum S (fast mode time step)
   const double* vgeo = nullptr;   // [5][ldf] viscous flux: HL/(HL+HR), HR/(HL+HR), C_R - C_L (3)
   const double* gdist = nullptr;  // [ng] wall ghosts: |F - C|^2 / |(F - C).n| (setboco_ns_flux.f90)
+  const double* frot = nullptr;   // [9][ldf] periodic faces connected by a rotation: the row-major
+                                  // rotation bringing the partner's vectors into the face's frame
+                                  // (transvec_per); null when no family is rotational
 };
 
 struct DevState {

@@ -155,6 +155,7 @@ __device__ void implicit_face_states(const DevMesh& m, const DevState& s, const 
   const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
   if (kind == TY_BC_PERIODIC) {
     side_state(m.part[f], 0, QR);
+    rot_to_face(m, f, QR);
   } else if (kind == TY_BC_WALL || kind == TY_BC_NOSLIP) {
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {

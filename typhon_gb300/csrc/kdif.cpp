@@ -50,6 +50,10 @@ int ty_kdif_setup(ty_mesh* h, const ty_kdif_params* p, const double* conductivit
     return TY_ERR_ARG;
   }
   TY_CU(cudaSetDevice(h->device));
+  if (h->m.frot) {
+    tyi::set_error("ty_kdif_setup: heat conduction on meshes with rotational periodicity is not built");
+    return TY_ERR_UNSUPPORTED;
+  }
   DevMesh& m = h->m;
   KdifState& k = h->kd;
   const int nci = m.nci, nc = m.nc, nf = m.nf, nfi = m.nfi;

@@ -38,6 +38,20 @@ constexpr int kBlock = 256;
 
 __device__ __forceinline__ double d3(const double* a, int ld, int i, int k) { return a[k * (size_t)ld + i]; }
 
+// Rotational periodicity (calcboco_connect_per_match.f90:56-78, transvec_per): the velocity
+// (q[2..4]) of a state taken from the partner of periodic face f, rotated into f's frame.
+__device__ __forceinline__ void rot_to_face(const DevMesh& m, int f, double* q) {
+  if (!m.frot) return;
+  const size_t lf = m.ldf;
+  double R[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) R[k] = m.frot[k * lf + f];
+  const double x = q[2], y = q[3], z = q[4];
+  q[2] = R[0] * x + R[1] * y + R[2] * z;
+  q[3] = R[3] * x + R[4] * y + R[5] * z;
+  q[4] = R[6] * x + R[7] * y + R[8] * z;
+}
+
 // ---------------------------------------------------------------------------
 // Limiters (LIMITER.f90).  Scalars (rho, p) pass through the array forms, vector
 // components through the scalar forms, as tvdgrad*_scal / tvdgrad*_vect call them.
@@ -251,6 +265,11 @@ __global__ void k_ghost_prim(DevMesh m, double* __restrict__ prim, SpatOpts o) {
   }
   prim[g] = prim[src];
   prim[ld + g] = prim[ld + src];
+  if (kind == TY_BC_PERIODIC && m.frot) {
+    double q[5] = {0.0, 0.0, vx, vy, vz};
+    rot_to_face(m, f, q);
+    vx = q[2]; vy = q[3]; vz = q[4];
+  }
   if (kind == TY_BC_SYMMETRY) {
     double nx = d3(m.fn, m.ldf, f, 0), ny = d3(m.fn, m.ldf, f, 1), nz = d3(m.fn, m.ldf, f, 2);
     double wx = vx - 0.0, wy = vy - 0.0, wz = vz - 0.0;
@@ -334,8 +353,30 @@ __global__ void k_ghost_grad(DevMesh m, double* __restrict__ grad) {
   if (m.fbc[f] != TY_BC_PERIODIC) return;
   const int g = m.nci + k, src = m.gsrc[k];
   const size_t ld = m.ldc;
+  if (!m.frot) {
 #pragma unroll
-  for (int v = 0; v < 15; ++v) grad[v * ld + g] = grad[v * ld + src];
+    for (int v = 0; v < 15; ++v) grad[v * ld + g] = grad[v * ld + src];
+    return;
+  }
+  // rotational periodicity: the scalar gradients are vectors, R g (transvec_per); the velocity
+  // gradient G(i,j) = du_i/dx_j becomes G R^T (transten_per -> t3d_rot, TENSOR3.f90:328-340)
+  const size_t lf = m.ldf;
+  double R[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) R[q] = m.frot[q * lf + f];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const double x = grad[(3 * q) * ld + src], y = grad[(3 * q + 1) * ld + src], z = grad[(3 * q + 2) * ld + src];
+    grad[(3 * q) * ld + g] = R[0] * x + R[1] * y + R[2] * z;
+    grad[(3 * q + 1) * ld + g] = R[3] * x + R[4] * y + R[5] * z;
+    grad[(3 * q + 2) * ld + g] = R[6] * x + R[7] * y + R[8] * z;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const double G0 = grad[(6 + 3 * i) * ld + src], G1 = grad[(7 + 3 * i) * ld + src], G2 = grad[(8 + 3 * i) * ld + src];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) grad[(6 + 3 * i + j) * ld + g] = G0 * R[3 * j] + G1 * R[3 * j + 1] + G2 * R[3 * j + 2];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -899,6 +940,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux(DevMesh m, DevState s, Spa
   const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
   if (kind == TY_BC_PERIODIC) {
     recon(m, s, o, m.part[f], 0, QR);  // cell_r(face) = cell_l(partner face)
+    rot_to_face(m, f, QR);
   } else if (kind == TY_BC_WALL || kind == TY_BC_NOSLIP) {
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {
@@ -979,6 +1021,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_lim(DevMesh m, DevState s,
   const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
   if (kind == TY_BC_PERIODIC) {
     limited(m.part[f], 0, QR);
+    rot_to_face(m, f, QR);
   } else if (kind == TY_BC_WALL || kind == TY_BC_NOSLIP) {
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {
@@ -1144,6 +1187,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux_fast(DevMesh m, DevState s
     const int p = m.part[f];
 #pragma unroll
     for (int v = 0; v < 5; ++v) QR[v] = s.cl[v * lf + p];
+    rot_to_face(m, f, QR);
   } else if (kind == TY_BC_WALL || kind == TY_BC_NOSLIP) {
     wall_state(m, f, QL, QR);
   } else if (kind == TY_BC_FARFIELD) {

@@ -60,7 +60,31 @@ int elem_dim(int t) {
 
 struct Section { int type; std::vector<int> ielem, vtex; };
 struct Mark { std::string family; std::vector<int> tags; bool vertex = false; };
-struct BcIn { std::string family, partner; int kind; V3 trans, wallvel; };
+struct BcIn {
+  std::string family, partner;
+  int kind;
+  V3 trans, wallvel;
+  bool rot = false;     // periodic by rotation: centre, unit axis, angle (radians) to the partner
+  V3 rc{0, 0, 0}, ra{0, 0, 1};
+  double ang = 0.0;
+};
+
+// calc_rot (CFDTOOLS/Math/VEC3D.f90:652-674): row-major rotation about the unit axis a by
+// angle; the same operations and order as the oracle's
+void calc_rot(V3 a, double angle, double* M) {
+  const double costh = std::cos(angle), sinth = std::sin(angle);
+  const double ax[3] = {a.x, a.y, a.z};
+  M[0] = costh; M[4] = costh; M[8] = costh;
+  M[1] = -a.z * sinth; M[2] = +a.y * sinth;
+  M[3] = +a.z * sinth; M[5] = -a.x * sinth;
+  M[6] = -a.y * sinth; M[7] = +a.x * sinth;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) M[3 * i + j] = M[3 * i + j] + (1.0 - costh) * ax[i] * ax[j];
+}
+V3 rot_apply(const double* M, V3 v) {
+  return mk(M[0] * v.x + M[1] * v.y + M[2] * v.z, M[3] * v.x + M[4] * v.y + M[5] * v.z,
+            M[6] * v.x + M[7] * v.y + M[8] * v.z);
+}
 
 std::string upper(std::string s) {
   for (auto& c : s) c = (char)toupper((unsigned char)c);
@@ -100,6 +124,8 @@ struct ty_umesh {
   std::vector<int32_t> facevtex;          // [4*nface], 1-based, 0 padded
   std::vector<double> fnormal, fcentre, fsurf, ccentre, cvol, fwallvel;
   std::vector<int32_t> fcolor, fbc, fpartner, ffamily;
+  std::vector<double> frot;               // [nface][9] rotation into each face's frame
+  bool has_rot = false;
 };
 
 extern "C" {
@@ -389,6 +415,8 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
 
   // ---- ghost cells: physical boundaries first, then periodic connections ----
   std::vector<int> fbc(nface, TY_BC_INTERIOR), fpart(nface, 0), ffam(nface, -1);
+  std::vector<double> frot(9 * (size_t)nface, 0.0);  // rotation into each face's frame (identity)
+  for (int f = 0; f < nface; ++f) frot[9 * (size_t)f] = frot[9 * (size_t)f + 4] = frot[9 * (size_t)f + 8] = 1.0;
   std::vector<double> fwall(3 * (size_t)nface, 0.0);
   int nlim = 0;
   for (auto& b : bocos) {
@@ -450,9 +478,15 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
     std::unordered_map<std::array<long long, 3>, std::vector<int>, AH> grid;
     for (size_t k = 0; k < nf; ++k) grid[cell_of(fc[b2->iface[k]])].push_back((int)k);
     b.partner.resize(nf);
+    double Mloc[9], Mvec[9];  // transloc_per (rlink * angle) and transvec_per (-rlink * angle)
+    if (d.rot) {
+      calc_rot(d.ra, b.rlink * d.ang, Mloc);
+      calc_rot(d.ra, -b.rlink * d.ang, Mvec);
+    }
     for (size_t k = 0; k < nf; ++k) {
       V3 p = fc[b.iface[k]];
-      p = add(p, scl(b.rlink, d.trans));
+      if (d.rot) p = add(rot_apply(Mloc, sub(p, d.rc)), d.rc);
+      else p = add(p, scl(b.rlink, d.trans));
       auto c0 = cell_of(p);
       double best = std::numeric_limits<double>::max();
       int ib = -1;
@@ -466,7 +500,9 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
               if (dist < best || (dist == best && j < ib)) { best = dist; ib = j; }
             }
           }
-      if (ib < 0 || !(best <= 1e-6 * h)) return fail("periodic faces do not match");
+      // matching_index (GRID_CONNECT.f90) takes the nearest face with no tolerance; the guard
+      // allows for meshes written with single-precision-like coordinates (perrot2d.cgns: 3e-8)
+      if (ib < 0 || !(best <= 1e-3 * h)) return fail("periodic faces do not match");
       b.partner[k] = b2->iface[ib];
     }
     for (int f : b.iface) {
@@ -477,6 +513,10 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
       int f = b.iface[k], fp = b.partner[k];
       int g = F2[f] - 1, icper = F1[fp] - 1;
       V3 dfc = sub(cc[icper], fc[fp]);
+      if (d.rot) {  // init_connect_grid.f90:218-223: the face-to-cell vector rotated
+        dfc = rot_apply(Mvec, dfc);
+        for (int q = 0; q < 9; ++q) frot[9 * (size_t)f + q] = Mvec[q];
+      }
       cv[g] = cv[icper];
       cc[g] = add(fc[f], dfc);
       fbc[f] = TY_BC_PERIODIC;
@@ -509,6 +549,9 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
   um->fpartner = fpart;
   um->fwallvel = fwall;
   um->ffamily = ffam;
+  um->frot = frot;
+  um->has_rot = false;
+  for (const auto& b : um->bcs) um->has_rot = um->has_rot || b.rot;
   um->built = true;
   return TY_OK;
 }
@@ -529,6 +572,30 @@ int ty_umesh_desc(const ty_umesh* um, ty_mesh_desc* d) {
   d->face_partner = um->fpartner.data();
   d->face_wallvel = um->fwallvel.data();
   return TY_OK;
+}
+
+int ty_umesh_set_rotation(ty_umesh* um, const char* family, const double* centre3, const double* axis3,
+                          double angle_deg) {
+  if (!um || !family || !centre3 || !axis3) return TY_ERR_ARG;
+  const double an = std::sqrt(axis3[0] * axis3[0] + axis3[1] * axis3[1] + axis3[2] * axis3[2]);
+  if (!(an > 0.0)) { tyi::set_error("ty_umesh_set_rotation: zero axis"); return TY_ERR_ARG; }
+  for (auto& b : um->bcs)
+    if (b.kind == TY_BC_PERIODIC && b.family == upper(family)) {
+      b.rot = true;
+      b.rc = mk(centre3[0], centre3[1], centre3[2]);
+      b.ra = mk(axis3[0] / an, axis3[1] / an, axis3[2] / an);
+      b.ang = angle_deg / 180.0 * 3.141592653589793238462643;  // def_mesh.f90:242-244
+      um->built = false;
+      return TY_OK;
+    }
+  tyi::set_error(std::string("ty_umesh_set_rotation: no periodic definition for family ") + family);
+  return TY_ERR_ARG;
+}
+
+int ty_umesh_face_rotation(const ty_umesh* um, double* out) {
+  if (!um || !out || !um->built) return TY_ERR_STATE;
+  std::memcpy(out, um->frot.data(), um->frot.size() * sizeof(double));
+  return um->has_rot ? 1 : 0;
 }
 
 int ty_umesh_face_family(const ty_umesh* um, int32_t* out) {

@@ -59,6 +59,9 @@ class Grid:
         h = C.c_void_p()
         _capi.check(self.lib.ty_mesh_create(C.byref(self._desc), int(device), C.byref(h)), "ty_mesh_create")
         self.h = h
+        if getattr(mesh, "face_rotation", None) is not None:
+            rot = np.ascontiguousarray(mesh.face_rotation, np.float64)
+            _capi.check(self.lib.ty_mesh_set_face_rotation(h, rot.ctypes.data), "ty_mesh_set_face_rotation")
         self.nci = mesh.ncell_int
         self.gamma = 1.4
         self.time = 0.0

@@ -486,6 +486,8 @@ class MeshDesc:
         # boundary definition index of each face (bcs order given to preprocess), -1 interior
         self.face_family = face_family if face_family is not None else np.full(nf, -1, np.int32)
         self.families = list(families)
+        # [nface, 3, 3] rotation into each face's frame when a periodic family is rotational
+        self.face_rotation = None
 
     def faces_of(self, family):
         """Faces (0-based) of a boundary family, in face order."""
@@ -514,10 +516,12 @@ class MeshDesc:
         return d
 
 
-def preprocess(raw: RawMesh, dim, bcs) -> MeshDesc:
+def preprocess(raw: RawMesh, dim, bcs, rotations=None) -> MeshDesc:
     """Native preprocessing (ty_umesh_*): faces, geometry, colours, ghosts, periodicity.
 
     bcs: [(family, kind, partner, translation(3)[, wall_velocity(3)])]
+    rotations: {family: (centre(3), axis(3), angle in degrees)} for periodic families that
+    are connected to their partner by a rotation (BLOCK:PERIODICITY TYPE = ROTATION)
     """
     L = _capi.lib()
     h = C.c_void_p()
@@ -542,6 +546,11 @@ def preprocess(raw: RawMesh, dim, bcs) -> MeshDesc:
             wv = np.ascontiguousarray(b[4] if len(b) > 4 else (0, 0, 0), np.float64)
             _capi.check(L.ty_umesh_add_bc(h, b[0].encode(), int(b[1]), (b[2] or "").encode(),
                                           tr.ctypes.data, wv.ctypes.data), "ty_umesh_add_bc")
+        for fam, (ctr, ax, ang) in (rotations or {}).items():
+            c3 = np.ascontiguousarray(ctr, np.float64)
+            a3 = np.ascontiguousarray(ax, np.float64)
+            _capi.check(L.ty_umesh_set_rotation(h, fam.encode(), c3.ctypes.data, a3.ctypes.data, float(ang)),
+                        "ty_umesh_set_rotation")
         _capi.check(L.ty_umesh_build(h, int(dim)), "ty_umesh_build")
         d = _capi.MeshDesc()
         _capi.check(L.ty_umesh_desc(h, C.byref(d)), "ty_umesh_desc")
@@ -549,6 +558,12 @@ def preprocess(raw: RawMesh, dim, bcs) -> MeshDesc:
         _capi.check(L.ty_umesh_facevtex(h, fv.ctypes.data), "ty_umesh_facevtex")
         ff = np.zeros(d.nface, np.int32)
         _capi.check(L.ty_umesh_face_family(h, ff.ctypes.data), "ty_umesh_face_family")
-        return MeshDesc(d, fv.reshape(d.nface, 4), ff, [b[0].upper() for b in bcs])
+        md = MeshDesc(d, fv.reshape(d.nface, 4), ff, [b[0].upper() for b in bcs])
+        rot = np.zeros(9 * d.nface)
+        rc = L.ty_umesh_face_rotation(h, rot.ctypes.data)
+        _capi.check(min(rc, 0), "ty_umesh_face_rotation")
+        if rc == 1:
+            md.face_rotation = rot.reshape(d.nface, 3, 3)
+        return md
     finally:
         L.ty_umesh_free(h)
