@@ -298,3 +298,48 @@ def test_config2_scheme_gradient_against_complex_step(env):
         ad = float(np.sum(grad * d))
         assert abs(ad - dJ) <= 1e-8 * abs(dJ), (ad, dJ)
     g.close()
+
+
+FAST_EXACT = [("HLLC", "MUSCL", "ALBADA", "NONE"), ("ROE", "MUSCL", "ALBADA", "NONE"),
+              ("RUSANOV", "MUSCL", "NONE", "NONE"), ("HLLC", "MUSCL-UNS", "ALBADA", "NONE"),
+              ("ROE", "MUSCL-UNS", "NONE", "BARTH"), ("HLLC", "MUSCL", "ALBADA", "SUPERBARTH")]
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("scheme,highres,limiter,postlim", FAST_EXACT)
+def test_fast_second_order_vjp_equals_exact(env, dim, scheme, highres, limiter, postlim):
+    """The fast mode's second-order VJP (array-of-structures records, Newton-Raphson
+    reciprocals, limiter derivatives carried from the forward reconstruction) against the
+    exact mode's on the same state: the same products to rounding, except where a limiter
+    switch (van Albada's a b = 0, Barth's minimum) falls between the two modes' roundings of
+    the same gradient, which moves single entries; hence an L2 bound and a looser max bound."""
+    torch, ty, adjoint = env
+    from typhon_gb300 import cases
+    rng = np.random.default_rng(11)
+    if dim == 2:
+        md = jittered(ty, 12)
+        U0 = smooth_cons(ty, md) * (1.0 + 0.05 * rng.standard_normal((1, md.ncell_int)))
+    else:
+        # the Taylor-Green field plus a uniform stream and per-cell noise: no face where the
+        # normal velocity or a limiter argument is rounding noise (the TGV alone has such
+        # faces at its symmetry points, where |vn| and van Albada's a b = 0 are kinks)
+        md = cases.make_mesh("tgv3d", 4)
+        nci = md.ncell_int
+        prim = cases.taylor_green(md.cell_centre)[:, :nci]
+        prim[2:5] += np.array([[0.3], [0.2], [0.1]]) + 0.05 * rng.standard_normal((3, nci))
+        prim[:2] *= 1.0 + 0.02 * rng.standard_normal((2, nci))
+        U0 = ty.prim_to_cons(prim)
+    U = torch.tensor(U0, device="cuda")
+    lamR = torch.tensor(rng.standard_normal(U0.shape), device="cuda")
+    out = {}
+    for mode in ("exact", "fast"):
+        g = ty.Grid(md)
+        g.set_spat(scheme, highres, limiter, postlim, mode=mode)
+        st = adjoint.Stepper(g, "RK3-SSP")
+        out[mode] = st.vjp(U, 1e-3, lamR).cpu().numpy()
+        out[mode + "2"] = st.vjp(U, 1e-3, lamR).cpu().numpy()   # second call: tables reused
+        g.close()
+    assert np.array_equal(out["fast"], out["fast2"])
+    diff = out["fast"] - out["exact"]
+    assert np.linalg.norm(diff) <= 1e-11 * np.linalg.norm(out["exact"]), np.linalg.norm(diff)
+    assert np.abs(diff).max() <= 1e-8 * np.abs(out["exact"]).max()

@@ -56,6 +56,26 @@ int ty_adjoint_vjp(ty_mesh* h, double dt, const double* lamR, double* lamU) {
   }
   DevMesh& m = h->m;
   int rc;
+  if (second && h->o.mode == TY_MODE_FAST) {
+    // array-of-structures records, lambda read and written in the caller's layout
+    if (!h->adj_cell &&
+        ((rc = h->alloc(h->adj_cell, 32 * (size_t)m.ldc)) || (rc = h->alloc(h->adj_rec, 50 * (size_t)m.ldf)) ||
+         (rc = h->alloc(h->adj_qg, 24 * (size_t)m.ldc)) ||
+         (rc = h->alloc(h->adj_w, (3 + 6 * (size_t)m.nslot) * (size_t)m.nci)) ||
+         (rc = h->alloc(h->adj_nbc, (size_t)m.nslot * (size_t)m.nci))))
+      return rc;
+    if (h->adj_w_gradmeth != h->lsq_gradmeth) {
+      cudaError_t e = kfast::adjoint_weights_fast(m, h->adj_w, h->adj_nbc, h->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "adjoint weights");
+      h->adj_w_gradmeth = h->lsq_gradmeth;
+    }
+    cudaError_t e = kfast::adjoint_vjp_muscl_fast(m, h->s, h->o, h->s.u0, lamR, m.nci, dt, h->adj_cell, h->adj_rec,
+                                                  h->adj_qg, h->adj_qg + 5 * (size_t)m.ldc, h->adj_w, h->adj_nbc,
+                                                  lamU, m.nci, h->stream);
+    h->prim_valid = false;  // s.prim now holds this state's primitive variables and ghosts
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint");
+    return TY_OK;
+  }
   if (!h->adj_face) {
     if ((rc = h->alloc(h->adj_face, 10 * (size_t)m.ldf)) || (rc = h->alloc(h->adj_buf, 10 * (size_t)m.ldc)))
       return rc;
@@ -67,10 +87,10 @@ int ty_adjoint_vjp(ty_mesh* h, double dt, const double* lamR, double* lamU) {
                           cudaMemcpyDeviceToDevice, h->stream));
   cudaError_t e;
   if (second) {
-    if (!h->adj_rec &&
-        ((rc = h->alloc(h->adj_rec, 50 * (size_t)m.ldf)) || (rc = h->alloc(h->adj_qg, 20 * (size_t)m.ldc))))
+    if (!h->adj_rec2 &&
+        ((rc = h->alloc(h->adj_rec2, 50 * (size_t)m.ldf)) || (rc = h->alloc(h->adj_qg2, 20 * (size_t)m.ldc))))
       return rc;
-    e = ADJ_CALL(h, adjoint_vjp_muscl, m, h->s, h->o, h->s.u0, bR, dt, h->adj_rec, h->adj_qg, bU, h->stream);
+    e = ADJ_CALL(h, adjoint_vjp_muscl, m, h->s, h->o, h->s.u0, bR, dt, h->adj_rec2, h->adj_qg2, bU, h->stream);
     h->prim_valid = false;  // s.prim now holds this state's primitive variables and ghosts
   } else {
     e = ADJ_CALL(h, adjoint_vjp, m, h->o, h->s.u0, bR, dt, h->adj_face, bU, h->stream);

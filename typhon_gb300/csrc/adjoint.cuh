@@ -375,5 +375,398 @@ cudaError_t adjoint_vjp(const DevMesh& m, const SpatOpts& o, const double* u, co
   return cudaGetLastError();
 }
 
+
+#if TY_FAST
+// ---- fast-mode second-order adjoint.  Same mathematics as adjoint_vjp_muscl, arranged for
+// the FP64 pipe and for whole-sector gathers: records in array-of-structures layout (a
+// gather over random neighbours reads whole 32-byte sectors, where the structure-of-arrays
+// fields used above read 8 bytes of each), per-slot weight tables read coalesced, Newton-
+// Raphson reciprocals and the precomputed 1/V, 1/dLR and reconstruction weights.
+//
+// cell record, 32 doubles per interior cell: q (5), G (15: grad rho, grad p, du_i/dx_j row i),
+// the frozen Barth ratios (3; 1 without a post-limiter), dt/V lambda_R (5), padding (4)
+constexpr int kAdjCell = 32;
+// face record, 44 doubles per face: the gradient adjoints that go to fc1 (15 + pad) and to
+// the cell whose reconstruction is the face's right state (fc2, or on a periodic face the
+// partner face's inside cell) (15 + pad), then the q adjoints of the two (5 + 5, pad 2)
+constexpr int kAdjFace = 44;
+
+// the cell records; without a post-limiter the least-squares gradient is computed here,
+// grad = Wown q_c + sum over slots (+-A^-1 d) q_nb, from the per-slot weight tables (read
+// coalesced) instead of a separate gradient kernel
+__global__ void __launch_bounds__(kBlock) k_adj_pack(DevMesh m, DevState s, bool post, const double* __restrict__ lamR,
+                                                     int ldR, double dt, const double* __restrict__ wtab,
+                                                     double* __restrict__ crec) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t ld = m.ldc, n = m.nci;
+  double r[kAdjCell];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) r[v] = s.prim[v * ld + c];
+  if (post) {  // gradient and ratios of the forward kernel
+#pragma unroll
+    for (int k = 0; k < 15; ++k) r[5 + k] = s.grad[k * ld + c];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[20 + k] = s.ratio[k * ld + c];
+  } else {
+    // grad = sum (+-w)(q_nb - q_c) = sum (+-w) q_nb + Wown q_c (Wown = -sum (+-w))
+    const double wx = wtab[c], wy = wtab[n + c], wz = wtab[2 * n + c];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) { r[5 + 3 * v] = wx * r[v]; r[6 + 3 * v] = wy * r[v]; r[7 + 3 * v] = wz * r[v]; }
+    const double* ws = wtab + (3 + 3 * (size_t)m.nslot) * n;  // own-side weights per slot
+    for (int sl = 0; sl < m.nslot; ++sl) {
+      const int nb = m.cfn[sl * n + c];
+      if (m.cf[sl * n + c] < 0) break;
+      const double* w = ws + 3 * (size_t)sl * n + c;
+      const double ox = w[0], oy = w[n], oz = w[2 * n];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const double q = s.prim[v * ld + nb];
+        r[5 + 3 * v] = fma(q, ox, r[5 + 3 * v]);
+        r[6 + 3 * v] = fma(q, oy, r[6 + 3 * v]);
+        r[7 + 3 * v] = fma(q, oz, r[7 + 3 * v]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[20 + k] = 1.0;
+  }
+  const double w = dt * m.invV[c];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) r[23 + v] = w * lamR[(size_t)v * ldR + c];
+#pragma unroll
+  for (int k = 28; k < kAdjCell; ++k) r[k] = 0.0;
+  double2* out = reinterpret_cast<double2*>(crec + (size_t)c * kAdjCell);
+#pragma unroll
+  for (int k = 0; k < kAdjCell / 2; ++k) out[k] = make_double2(r[2 * k], r[2 * k + 1]);
+}
+
+// One side of a face: the owner's record O, the other cell's record N, the face F whose
+// geometry the reconstruction uses (the face itself, or the partner face of a periodic face)
+// and the side of F the owner is on (0: fc1, 1: fc2).  LR = (q_fc2(F) - q_fc1(F)) / dLR =
+// (q_N - q_O) / dLR on side 0 and (q_O - q_N) / dLR on side 1.
+struct AdjSide {
+  const double* O;
+  const double* N;
+  int F, side;
+};
+
+// forward reconstruction of one side (MUSCL / MUSCL-UNS, no limiter or van Albada), the frozen
+// ratio r applied to the increment:
+//   q = q_O + r (G . CF + sg (u . CF)),  g = G . u,  LR = (q_N - q_O) idLR (idLR signed by side),
+//   sg = phi(2g - LR, LR) - g (MUSCL) or phi(g, LR) - g (MUSCL-UNS), phi(a, b) = a b (a + b) /
+//   (a^2 + b^2) where a b > 0, else 0 (van Albada);
+// with van Albada it also returns the derivatives the reverse needs, cg = dq/dg and
+// cq = dq/d(q_N - q_O), so that the reverse does not recompute the limiter.  No limiter: the
+// increment is G . w + (q_N - q_O) k with the precomputed weights (recw).
+__device__ void adj_recon_f(const DevMesh& m, const SpatOpts& o, const AdjSide& sd, double q[5], double cg[5],
+                            double cq[5]) {
+  const size_t lf = m.ldf;
+  const int F = sd.F;
+  const double* __restrict__ O = sd.O;
+  const double* __restrict__ N = sd.N;
+  if (o.limiter == TY_LIM_NONE) {
+    const double* w = m.recw + (4 * sd.side) * lf + F;
+    const double wx = w[0], wy = w[lf], wz = w[2 * lf], k = w[3 * lf];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double inc = O[5 + 3 * v] * wx + O[6 + 3 * v] * wy + O[7 + 3 * v] * wz + (N[v] - O[v]) * k;
+      q[v] = O[v] + O[20 + (v < 2 ? v : 2)] * inc;
+    }
+    return;
+  }
+  // G . CF - g (u . CF) = G . w with w = CF - (u . CF) u, the no-limiter weights (recw)
+  const bool uns = o.highres == TY_HRES_MUSCLUNS;
+  const double ux = m.uLR[F], uy = m.uLR[lf + F], uz = m.uLR[2 * lf + F];
+  const double* w = m.recw + (4 * sd.side) * lf + F;
+  const double wx = w[0], wy = w[lf], wz = w[2 * lf];
+  const double* CF = sd.side ? m.RF : m.LF;
+  const double uc = ux * CF[F] + uy * CF[lf + F] + uz * CF[2 * lf + F];
+  const double idLR = sd.side ? -m.invdLR[F] : m.invdLR[F];
+  double ruc[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) ruc[k] = O[20 + k] * uc;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const double gx = O[5 + 3 * v], gy = O[6 + 3 * v], gz = O[7 + 3 * v];
+    const double g = gx * ux + gy * uy + gz * uz;
+    const double LR = (N[v] - O[v]) * idLR;
+    const double a = uns ? g : 2.0 * g - LR, b = LR;
+    const double ab = a * b;
+    const double rc = ruc[v < 2 ? v : 2];
+    // phi = a b (a + b) / D, D = a^2 + b^2; dphi/da = b^2 (b^2 - a^2 + 2ab) / D^2,
+    // dphi/db = a^2 (a^2 - b^2 + 2ab) / D^2
+    double phi = 0.0, cgv = -rc, cqv = 0.0;
+    if (ab > 0.0) {
+      const double a2 = a * a, b2 = b * b, iD = rcp_nr(a2 + b2);
+      phi = ab * (a + b) * iD;
+      const double dl = b2 - a2;
+      const double X = b2 * fma(2.0, ab, dl), Y = a2 * fma(2.0, ab, -dl);  // D^2 dphi/da, D^2 dphi/db
+      const double k1 = rc * (iD * iD);
+      cgv = uns ? fma(X, k1, -rc) : fma(2.0 * X, k1, -rc);
+      cqv = (uns ? Y : Y - X) * k1 * idLR;
+    }
+    const double inc = fma(phi, uc, gx * wx + gy * wy + gz * wz);
+    q[v] = fma(O[20 + (v < 2 ? v : 2)], inc, O[v]);
+    cg[v] = cgv;
+    cq[v] = cqv;
+  }
+}
+
+// reverse of adj_recon_f: Qb -> adjoints of the owner's q (own), of the other cell's q (oth)
+// and of the owner's gradient (G)
+__device__ void adj_recon_b(const DevMesh& m, const SpatOpts& o, const AdjSide& sd, const double Qb[5],
+                            const double cg[5], const double cq[5], double own[5], double oth[5], double G[15]) {
+  const size_t lf = m.ldf;
+  const int F = sd.F;
+  const double* __restrict__ O = sd.O;
+  if (o.limiter == TY_LIM_NONE) {
+    const double* w = m.recw + (4 * sd.side) * lf + F;
+    const double wx = w[0], wy = w[lf], wz = w[2 * lf], k = w[3 * lf];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double d = O[20 + (v < 2 ? v : 2)] * Qb[v];
+      own[v] = Qb[v] - d * k;
+      oth[v] = d * k;
+      G[3 * v] = d * wx; G[3 * v + 1] = d * wy; G[3 * v + 2] = d * wz;
+    }
+    return;
+  }
+  const double ux = m.uLR[F], uy = m.uLR[lf + F], uz = m.uLR[2 * lf + F];
+  const double* CF = sd.side ? m.RF : m.LF;
+  const double cx = CF[F], cy = CF[lf + F], cz = CF[2 * lf + F];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const double db = O[20 + (v < 2 ? v : 2)] * Qb[v], gb = cg[v] * Qb[v], dqb = cq[v] * Qb[v];
+    own[v] = Qb[v] - dqb;
+    oth[v] = dqb;
+    G[3 * v] = db * cx + gb * ux;
+    G[3 * v + 1] = db * cy + gb * uy;
+    G[3 * v + 2] = db * cz + gb * uz;
+  }
+}
+
+__device__ __forceinline__ void adj_store_g(double* rec, const double G[15]) {
+  double2* o = reinterpret_cast<double2*>(rec);
+#pragma unroll
+  for (int k = 0; k < 7; ++k) o[k] = make_double2(G[2 * k], G[2 * k + 1]);
+  o[7] = make_double2(G[14], 0.0);
+}
+
+// per face: lambda_F, the flux products at the reconstructed states, both reconstructions
+// reversed, summed per destination cell into the face record
+template <int SCH>
+__device__ __forceinline__ void adj_face2f(const DevMesh& m, const SpatOpts& o, const double* __restrict__ crec,
+                                           double* __restrict__ frec, int f) {
+  const bool interior = f < m.nfi;
+  const int c1 = m.fc1[f];
+  const int F1 = interior ? f : m.part[f];
+  const int cR = interior ? m.fc2[f] : m.fc1[F1];
+  const double* A = crec + (size_t)c1 * kAdjCell;
+  const double* B = crec + (size_t)cR * kAdjCell;
+  const double S = m.fs[f];
+  double Fb[5], QL[5], QR[5], cg0[5], cq0[5], cg1[5], cq1[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) Fb[v] = interior ? S * (B[23 + v] - A[23 + v]) : -S * A[23 + v];
+  const AdjSide s0{A, B, f, 0}, s1{B, A, F1, interior ? 1 : 0};
+  adj_recon_f(m, o, s0, QL, cg0, cq0);
+  adj_recon_f(m, o, s1, QR, cg1, cq1);
+  double QLb[5] = {0, 0, 0, 0, 0}, QRb[5] = {0, 0, 0, 0, 0};
+  const size_t lf = m.ldf;
+  const double nx = m.fn[f], ny = m.fn[lf + f], nz = m.fn[2 * lf + f];
+  if constexpr (SCH == TY_SCH_HLLC) hllc_vjp(o.gamma, QL, QR, nx, ny, nz, Fb, QLb, QRb);
+  else if constexpr (SCH == TY_SCH_RUSANOV) rusanov_vjp(o.gamma, QL, QR, nx, ny, nz, Fb, QLb, QRb);
+  else roe_vjp(o.gamma, o.entropy_fix, QL, QR, nx, ny, nz, Fb, QLb, QRb);
+  double* rec = frec + (size_t)f * kAdjFace;
+  double own0[5], oth0[5], own1[5], oth1[5], G[15];
+  adj_recon_b(m, o, s0, QLb, cg0, cq0, own0, oth0, G);
+  adj_store_g(rec, G);
+  adj_recon_b(m, o, s1, QRb, cg1, cq1, own1, oth1, G);
+  adj_store_g(rec + 16, G);
+  // to fc1: its own reconstruction's q adjoint and the right side's adjoint of its q as the
+  // other cell; to the right-state cell the converse
+  double d[12];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) { d[v] = own0[v] + oth1[v]; d[5 + v] = own1[v] + oth0[v]; }
+  d[10] = 0.0; d[11] = 0.0;
+  double2* oq = reinterpret_cast<double2*>(rec + 32);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) oq[k] = make_double2(d[2 * k], d[2 * k + 1]);
+}
+
+template <int SCH>
+__global__ void __launch_bounds__(128) k_adj_face2f(DevMesh m, SpatOpts o, const double* __restrict__ crec,
+                                                    double* __restrict__ frec) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f < m.nf) adj_face2f<SCH>(m, o, crec, frec, f);
+}
+// Roe's reverse holds more values: three blocks per SM (a few spilled registers) rather than two
+__global__ void __launch_bounds__(128, 3) k_adj_face2f_roe(DevMesh m, SpatOpts o, const double* __restrict__ crec,
+                                                           double* __restrict__ frec) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f < m.nf) adj_face2f<TY_SCH_ROE>(m, o, crec, frec, f);
+}
+
+// per cell: the face records gathered (side s of a face: gradient block 16 s, q block 32 + 5 s;
+// a periodic face also brings its partner face's right-state block) into qb [5][ldc] and the
+// gradient adjoints gb [ldc][16].  NS >= nslot: the slot loop is unrolled so that every record
+// load is issued before the first is used.
+template <int NS>
+__global__ void __launch_bounds__(kBlock) k_adj_cell2f(DevMesh m, const double* __restrict__ frec,
+                                                       double* __restrict__ qb, double* __restrict__ gb) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t n = m.nci;
+  int rf[2 * NS], rs[2 * NS];
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    const int e = sl < m.nslot ? m.cf[sl * n + c] : -1;
+    const int f = e >> 1, side = e & 1;
+    rf[2 * sl] = e < 0 ? -1 : f;
+    rs[2 * sl] = side;
+    // periodic face owned by this cell: the partner face's right-state block
+    rf[2 * sl + 1] = (e >= 0 && !side && f >= m.nfi) ? m.part[f] : -1;
+    rs[2 * sl + 1] = 1;
+  }
+  double q[5] = {0, 0, 0, 0, 0}, g[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) g[k] = 0.0;
+#pragma unroll
+  for (int i = 0; i < 2 * NS; ++i) {
+    if (rf[i] < 0) continue;
+    const double* r = frec + (size_t)rf[i] * kAdjFace;
+    const double2* rg = reinterpret_cast<const double2*>(r + 16 * rs[i]);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const double2 t = rg[k];
+      g[2 * k] += t.x;
+      g[2 * k + 1] += t.y;
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) q[v] += r[32 + 5 * rs[i] + v];
+  }
+  const size_t ld = m.ldc;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) qb[v * ld + c] = q[v];
+  double2* og = reinterpret_cast<double2*>(gb + (size_t)c * 16);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) og[k] = make_double2(g[2 * k], g[2 * k + 1]);
+}
+
+// per cell: the least-squares gradient reversed through the weight tables
+// (q_c adjoint += Wown . Gb_c + sum over slots W_slot . Gb_nb), then cons -> prim reversed
+template <int NS>
+__global__ void __launch_bounds__(kBlock) k_adj_cell3f(DevMesh m, SpatOpts o, const double* __restrict__ u,
+                                                       const double* __restrict__ qbuf, const double* __restrict__ gb,
+                                                       const double* __restrict__ wtab, const int* __restrict__ nbc,
+                                                       double* __restrict__ lamU, int ldU) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t ld = m.ldc, n = m.nci;
+  int nb[NS + 1];
+  double w[NS + 1][3];
+  nb[0] = c;
+  w[0][0] = wtab[c]; w[0][1] = wtab[n + c]; w[0][2] = wtab[2 * n + c];
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    nb[sl + 1] = sl < m.nslot ? nbc[sl * n + c] : -1;
+    const double* ws = wtab + (3 + 3 * (size_t)sl) * n + c;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) w[sl + 1][j] = nb[sl + 1] >= 0 ? ws[j * n] : 0.0;
+  }
+  double qb[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) qb[v] = qbuf[v * ld + c];
+#pragma unroll
+  for (int i = 0; i < NS + 1; ++i) {
+    if (nb[i] < 0) continue;
+    const double2* g2 = reinterpret_cast<const double2*>(gb + (size_t)nb[i] * 16);
+    double g[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { const double2 t = g2[k]; g[2 * k] = t.x; g[2 * k + 1] = t.y; }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) qb[v] += w[i][0] * g[3 * v] + w[i][1] * g[3 * v + 1] + w[i][2] * g[3 * v + 2];
+  }
+  double U[5], Q[5], Ub[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+  for (int v = 0; v < 5; ++v) U[v] = u[v * ld + c];
+  const double ir = prim_r(o.gamma, U, Q);
+  prim_vjp(o.gamma, U, ir, qb, Ub);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) lamU[(size_t)v * ldU + c] = Ub[v];
+}
+
+// the weight tables of k_adj_pack and k_adj_cell3f (static geometry): Wown [3][nci] = sum over
+// the cell's faces of -+ (A^-1 d) of its side; per slot [3][nci] the weight with which this
+// cell's q enters the neighbour's gradient (the partner's inside cell for a periodic face);
+// per slot [3][nci] the cell's own +-(A^-1 d) (its gradient is the sum of these times q_nb
+// plus Wown q_c); nbc [nslot][nci] the neighbour (-1 past the cell's last face)
+__global__ void __launch_bounds__(kBlock) k_adj_wbuild(DevMesh m, double* __restrict__ wtab, int* __restrict__ nbc) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t n = m.nci, lf = m.ldf;
+  double W[3] = {0, 0, 0};
+  for (int sl = 0; sl < m.nslot; ++sl) {
+    const int e = m.cf[sl * n + c];
+    double* w = wtab + (3 + 3 * (size_t)sl) * n + c;
+    if (e < 0) {
+      nbc[sl * n + c] = -1;
+      double* wo = wtab + (3 + 3 * (size_t)m.nslot + 3 * (size_t)sl) * n + c;
+      w[0] = w[n] = w[2 * n] = 0.0;
+      wo[0] = wo[n] = wo[2 * n] = 0.0;
+      continue;
+    }
+    const int f = e >> 1, side = e & 1;
+    const double sg = side ? 1.0 : -1.0;
+    double* wo = wtab + (3 + 3 * (size_t)m.nslot + 3 * (size_t)sl) * n + c;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      W[j] += sg * m.lsqw[(3 * side + j) * lf + f];
+      wo[j * n] = -sg * m.lsqw[(3 * side + j) * lf + f];
+    }
+    int oc, of, os;
+    double sgo;
+    if (f < m.nfi) { oc = side ? m.fc1[f] : m.fc2[f]; of = f; os = 1 - side; sgo = sg; }
+    else { of = m.part[f]; oc = m.fc1[of]; os = 0; sgo = 1.0; }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) w[j * n] = sgo * m.lsqw[(3 * os + j) * lf + of];
+    nbc[sl * n + c] = oc;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) wtab[j * n + c] = W[j];
+}
+
+cudaError_t adjoint_weights_fast(const DevMesh& m, double* wtab, int* nbc, cudaStream_t st) {
+  k_adj_wbuild<<<nblk(m.nci), kBlock, 0, st>>>(m, wtab, nbc);
+  return cudaGetLastError();
+}
+
+cudaError_t adjoint_vjp_muscl_fast(const DevMesh& m, const DevState& s, const SpatOpts& o, const double* u,
+                                   const double* lamR, int ldR, double dt, double* crec, double* frec, double* qbuf,
+                                   double* gb, const double* wtab, const int* nbc, double* lamU, int ldU,
+                                   cudaStream_t st) {
+  k_prim<<<nblk(m.nci), kBlock, 0, st>>>(m, u, s.prim, o.gamma);
+  if (m.ng > 0) k_ghost_prim<<<nblk(m.ng), kBlock, 0, st>>>(m, s.prim, o);
+  const bool post = o.postlim != TY_POSTLIM_NONE;
+  if (post) {  // gradient and the Barth ratios of the forward residual
+    const double klim = o.postlim == TY_POSTLIM_SUPERBARTH ? 1.0 : 0.5;
+    if (m.nslot <= 4) k_cell_fast<4, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim);
+    else k_cell_fast<8, 64><<<(unsigned)((m.nci + 63) / 64), 64, 0, st>>>(m, s, o, klim);
+  }
+  k_adj_pack<<<nblk(m.nci), kBlock, 0, st>>>(m, s, post, lamR, ldR, dt, wtab, crec);
+  const unsigned gf = (unsigned)((m.nf + 127) / 128);
+  if (o.scheme == TY_SCH_HLLC) k_adj_face2f<TY_SCH_HLLC><<<gf, 128, 0, st>>>(m, o, crec, frec);
+  else if (o.scheme == TY_SCH_RUSANOV) k_adj_face2f<TY_SCH_RUSANOV><<<gf, 128, 0, st>>>(m, o, crec, frec);
+  else k_adj_face2f_roe<<<gf, 128, 0, st>>>(m, o, crec, frec);
+  if (m.nslot <= 4) {
+    k_adj_cell2f<4><<<nblk(m.nci), kBlock, 0, st>>>(m, frec, qbuf, gb);
+    k_adj_cell3f<4><<<nblk(m.nci), kBlock, 0, st>>>(m, o, u, qbuf, gb, wtab, nbc, lamU, ldU);
+  } else {
+    k_adj_cell2f<kMaxSlot><<<nblk(m.nci), kBlock, 0, st>>>(m, frec, qbuf, gb);
+    k_adj_cell3f<kMaxSlot><<<nblk(m.nci), kBlock, 0, st>>>(m, o, u, qbuf, gb, wtab, nbc, lamU, ldU);
+  }
+  return cudaGetLastError();
+}
+#endif  // TY_FAST
+
 }  // namespace TY_KNS
 }  // namespace tyk

@@ -1,4 +1,4 @@
-// Launchers of the adjoint (vector-Jacobian product) kernels of the first-order residual.
+// Launchers of the adjoint (vector-Jacobian product) kernels of the residual.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -17,5 +17,15 @@ namespace tyk {
 
 TY_DECLARE_ADJOINT(kexact)
 TY_DECLARE_ADJOINT(kfast)
+
+// fast mode only: the second-order adjoint on array-of-structures records (lamR and lamU in
+// the caller's [5][ld] layout) and its static weight tables
+namespace kfast {
+cudaError_t adjoint_weights_fast(const DevMesh& m, double* wtab, int* nbc, cudaStream_t st);
+cudaError_t adjoint_vjp_muscl_fast(const DevMesh& m, const DevState& s, const SpatOpts& o, const double* u,
+                                   const double* lamR, int ldR, double dt, double* crec, double* frec, double* qbuf,
+                                   double* gb, const double* wtab, const int* nbc, double* lamU, int ldU,
+                                   cudaStream_t st);
+}
 
 }  // namespace tyk

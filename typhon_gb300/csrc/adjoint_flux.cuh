@@ -10,6 +10,16 @@
 #pragma once
 #include <cmath>
 
+// The fast-mode kernels (TY_FAST) take the Newton-Raphson reciprocal and square root of
+// fastmath.cuh in the reverse forms; the exact mode and the host take IEEE division and
+// square root.
+#if defined(TY_FAST) && TY_FAST && defined(__CUDACC__)
+#include "fastmath.cuh"
+#define TY_AD_NR 1
+#else
+#define TY_AD_NR 0
+#endif
+
 #ifdef __CUDACC__
 #define TY_AD __host__ __device__ __forceinline__
 #else
@@ -210,11 +220,34 @@ TY_AD void flux_roe_t(double g, double eps, const T* L, const T* R, double nx, d
 
 // The reverse forms below recompute the forward quantities they need with reciprocals
 // (1/rho, 1/a, ...) in place of the forward formulas' divisions: derivative values agree
-// with the dual-number forms to rounding, at a fraction of the FP64 divide/square-root work.
+// with the dual-number forms to rounding, at a fraction of the FP64 divide/square-root work.  ad_rcp, ad_div and ad_sqrt are IEEE
+// operations except in the fast-mode kernels (Newton-Raphson, within a few ulp).
+
+TY_AD double ad_rcp(double a) {
+#if TY_AD_NR && defined(__CUDA_ARCH__)
+  return rcp_nr(a);
+#else
+  return 1.0 / a;
+#endif
+}
+TY_AD double ad_div(double a, double b) {
+#if TY_AD_NR && defined(__CUDA_ARCH__)
+  return a * rcp_nr(b);
+#else
+  return a / b;
+#endif
+}
+TY_AD double ad_sqrt(double a) {
+#if TY_AD_NR && defined(__CUDA_ARCH__)
+  return sqrt_nr(a);
+#else
+  return ::sqrt(a);
+#endif
+}
 
 // cons -> prim with the reciprocal of the density; returns 1/rho
 TY_AD double prim_r(double g, const double* c, double* q) {
-  const double ir = 1.0 / c[0];
+  const double ir = ad_rcp(c[0]);
   const double vx = c[2] * ir, vy = c[3] * ir, vz = c[4] * ir;
   q[0] = c[0];
   q[1] = (g - 1.0) * (c[1] - 0.5 * c[0] * (vx * vx + vy * vy + vz * vz));
@@ -242,12 +275,12 @@ TY_AD void prim_vjp(double g, const double* U, double ir, const double* qb, doub
 TY_AD void roe_vjp(double g, double eps, const double* L, const double* R, double nx, double ny, double nz,
                    const double* Fb, double* Lb, double* Rb) {
   const double n[3] = {nx, ny, nz};
-  const double g1 = g - 1.0, ig1 = 1.0 / g1, gig1 = g * ig1;
-  const double iL = 1.0 / L[0], iR = 1.0 / R[0];
+  const double g1 = g - 1.0, ig1 = ad_rcp(g1), gig1 = g * ig1;
+  const double iL = ad_rcp(L[0]), iR = ad_rcp(R[0]);
   // forward
-  const double t1 = ::sqrt(R[0] * iL), it1 = t1 * L[0] * iR;
+  const double t1 = ad_sqrt(R[0] * iL), it1 = t1 * L[0] * iR;
   const double rroe = L[0] * t1;
-  const double kl = 1.0 / (1.0 + t1), kr = t1 * kl;
+  const double kl = ad_rcp(1.0 + t1), kr = t1 * kl;
   double u[3], du[3], dut[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) u[k] = kl * L[2 + k] + kr * R[2 + k];
@@ -257,7 +290,7 @@ TY_AD void roe_vjp(double g, double eps, const double* L, const double* R, doubl
   const double hroe = kl * hl + kr * hr;
   const double q2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
   const double a2 = g1 * (hroe - 0.5 * q2);
-  const double a = ::sqrt(a2), ia = 1.0 / a, ia2 = ia * ia;
+  const double a = ad_sqrt(a2), ia = ad_rcp(a), ia2 = ia * ia;
   const double vn = u[0] * nx + u[1] * ny + u[2] * nz;
   const double vnl = L[2] * nx + L[3] * ny + L[4] * nz, vnr = R[2] * nx + R[3] * ny + R[4] * nz;
   const double rel = ig1 * L[1] + 0.5 * L[0] * sqL, rer = ig1 * R[1] + 0.5 * R[0] * sqR;
@@ -270,7 +303,7 @@ TY_AD void roe_vjp(double g, double eps, const double* L, const double* R, doubl
   const double l1o = ::fabs(vn - a), l5o = ::fabs(vn + a), l2 = ::fabs(vn);
   const double delta = eps * a;
   const bool fix1 = l1o < delta, fix5 = l5o < delta;
-  const double idl = (fix1 || fix5) ? 1.0 / delta : 0.0;
+  const double idl = (fix1 || fix5) ? ad_rcp(delta) : 0.0;
   const double l1 = fix1 ? (l1o * l1o + delta * delta) * (0.5 * idl) : l1o;
   const double l5 = fix5 ? (l5o * l5o + delta * delta) * (0.5 * idl) : l5o;
   const double w1 = l1 * al1, w2 = l2 * al2, w5 = l5 * al5, ws = l2 * rroe;
@@ -380,10 +413,10 @@ TY_AD void roe_vjp(double g, double eps, const double* L, const double* R, doubl
 TY_AD void rusanov_vjp(double g, const double* L, const double* R, double nx, double ny, double nz,
                        const double* Fb, double* Lb, double* Rb) {
   const double n[3] = {nx, ny, nz};
-  const double ig1 = 1.0 / (g - 1.0);
-  const double iL = 1.0 / L[0], iR = 1.0 / R[0];
+  const double ig1 = ad_rcp(g - 1.0);
+  const double iL = ad_rcp(L[0]), iR = ad_rcp(R[0]);
   const double vnl = L[2] * nx + L[3] * ny + L[4] * nz, vnr = R[2] * nx + R[3] * ny + R[4] * nz;
-  const double al = ::sqrt(g * L[1] * iL), ar = ::sqrt(g * R[1] * iR);
+  const double al = ad_sqrt(g * L[1] * iL), ar = ad_sqrt(g * R[1] * iR);
   const double cl = ::fabs(vnl) + al, cr = ::fabs(vnr) + ar;
   const bool right = cr > cl;
   const double ray = right ? cr : cl;
@@ -415,12 +448,12 @@ TY_AD void rusanov_vjp(double g, const double* L, const double* R, double nx, do
   // the wave speed of one side: a = sqrt(g p / rho), da = a/2 (dp/p - drho/rho)
   if (right) {
     vnrb += signbit(vnr) ? -rayb : rayb;
-    const double h = 0.5 * rayb * g * iR / ar;
+    const double h = ad_div(0.5 * rayb * g * iR, ar);
     Rb[1] += h;
     Rb[0] -= h * R[1] * iR;
   } else {
     vnlb += signbit(vnl) ? -rayb : rayb;
-    const double h = 0.5 * rayb * g * iL / al;
+    const double h = ad_div(0.5 * rayb * g * iL, al);
     Lb[1] += h;
     Lb[0] -= h * L[1] * iL;
   }
@@ -439,10 +472,10 @@ TY_AD void rusanov_vjp(double g, const double* L, const double* R, double nx, do
 TY_AD void hllc_vjp(double g, const double* L, const double* R, double nx, double ny, double nz,
                     const double* Fb, double* Lb, double* Rb) {
   const double n[3] = {nx, ny, nz};
-  const double g1 = g - 1.0, ig1 = 1.0 / g1, gig1 = g * ig1;
-  const double iL = 1.0 / L[0], iR = 1.0 / R[0];
-  const double t1 = ::sqrt(R[0] * iL), it1 = t1 * L[0] * iR;
-  const double kl = 1.0 / (1.0 + t1), kr = t1 * kl;
+  const double g1 = g - 1.0, ig1 = ad_rcp(g1), gig1 = g * ig1;
+  const double iL = ad_rcp(L[0]), iR = ad_rcp(R[0]);
+  const double t1 = ad_sqrt(R[0] * iL), it1 = t1 * L[0] * iR;
+  const double kl = ad_rcp(1.0 + t1), kr = t1 * kl;
   double ru[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) ru[k] = kl * L[2 + k] + kr * R[2 + k];
@@ -451,9 +484,9 @@ TY_AD void hllc_vjp(double g, const double* L, const double* R, double nx, doubl
   const double h = kl * hla + kr * hra;
   const double H = h - 0.5 * (ru[0] * ru[0] + ru[1] * ru[1] + ru[2] * ru[2]);
   const double vnl = L[2] * nx + L[3] * ny + L[4] * nz, vnr = R[2] * nx + R[3] * ny + R[4] * nz;
-  const double al = ::sqrt(g * L[1] * iL), ar = ::sqrt(g * R[1] * iR);
+  const double al = ad_sqrt(g * L[1] * iL), ar = ad_sqrt(g * R[1] * iR);
   const double vm = ru[0] * nx + ru[1] * ny + ru[2] * nz;
-  const double am = ::sqrt(g1 * H);  // sqrt(g roe_p / roe_rho), roe_p = roe_rho H / gig1
+  const double am = ad_sqrt(g1 * H);  // sqrt(g roe_p / roe_rho), roe_p = roe_rho H / gig1
   const double rel = ig1 * L[1] + 0.5 * L[0] * sqL, rer = ig1 * R[1] + 0.5 * R[0] * sqR;
   const bool slm = (vm - am) < (vnl - al), srm = (vm + am) > (vnr + ar);
   const double sl = slm ? vm - am : vnl - al, sr = srm ? vm + am : vnr + ar;
@@ -478,13 +511,13 @@ TY_AD void hllc_vjp(double g, const double* L, const double* R, double nx, doubl
     if (lf) { vnlb += vqb; relb += reb; } else { vnrb += vqb; rerb += reb; }
   } else {
     const double rqL = L[0] * (sl - vnl), rqR = R[0] * (sr - vnr);
-    const double num = rqR * vnr - rqL * vnl - R[1] + L[1], iden = 1.0 / (rqR - rqL);
+    const double num = rqR * vnr - rqL * vnl - R[1] + L[1], iden = ad_rcp(rqR - rqL);
     const double Sst = num * iden;
     const bool lf = Sst >= 0.0;
     const double* Q = lf ? L : R;
     double* Qb = lf ? Lb : Rb;
     const double s = lf ? sl : sr, vq = lf ? vnl : vnr, rq = lf ? rqL : rqR, re = lf ? rel : rer;
-    const double iks = 1.0 / (s - Sst);
+    const double iks = ad_rcp(s - Sst);
     const double rst = rq * iks;
     const double pst = Q[1] - rq * (vq - Sst);
     const double dp = pst - Q[1];
@@ -542,11 +575,11 @@ TY_AD void hllc_vjp(double g, const double* L, const double* R, double nx, doubl
   if (slm) { vmb += slb; amb -= slb; } else { vnlb += slb; alb -= slb; }
   if (srm) { vmb += srb; amb += srb; } else { vnrb += srb; arb += srb; }
   // am = sqrt(g1 H): dam = g1 / (2 am) dH (the Roe density cancels)
-  const double Hb = amb * 0.5 * g1 / am;
+  const double Hb = ad_div(amb * 0.5 * g1, am);
   double klb = Hb * hla, krb = Hb * hra;
   const double hlab = Hb * kl, hrab = Hb * kr;
   const double sqLb = 0.5 * hlab + relb * 0.5 * L[0], sqRb = 0.5 * hrab + rerb * 0.5 * R[0];
-  const double alh = alb * 0.5 * g * iL / al, arh = arb * 0.5 * g * iR / ar;
+  const double alh = ad_div(alb * 0.5 * g * iL, al), arh = ad_div(arb * 0.5 * g * iR, ar);
   Lb[1] += hlab * gig1 * iL + relb * ig1 + alh;
   Lb[0] += relb * 0.5 * sqL - (hlab * gig1 * iL + alh) * L[1] * iL;
   Rb[1] += hrab * gig1 * iR + rerb * ig1 + arh;

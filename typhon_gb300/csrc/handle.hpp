@@ -59,8 +59,16 @@ struct ty_mesh {
   tyk::KdifState kd;  // heat-conduction state (ty_kdif_setup)
   double* adj_face = nullptr;  // [10][ldf] adjoint face products (first use)
   double* adj_buf = nullptr;   // [2][5][ldc] adjoint staging
-  double* adj_rec = nullptr;   // [50][ldf] reversed reconstructions (second-order adjoint)
-  double* adj_qg = nullptr;    // [20][ldc] adjoints of q and of the gradients (second order)
+  double* adj_rec2 = nullptr;  // [50][ldf] reversed reconstructions (second-order adjoint, exact mode)
+  double* adj_qg2 = nullptr;   // [20][ldc] adjoints of q and of the gradients (exact mode)
+  // fast-mode second-order adjoint: cell records [nci][32], face records [nf][44], q adjoints
+  // [5][ldc] + gradient adjoints [nci][16], weight tables [3 + 6 nslot][nci] and neighbours
+  double* adj_cell = nullptr;
+  double* adj_rec = nullptr;
+  double* adj_qg = nullptr;
+  double* adj_w = nullptr;
+  int* adj_nbc = nullptr;
+  int adj_w_gradmeth = -1;
   double* steady_red = nullptr;  // [3 kRedBlocks + 3] partial and final residual sums of ty_steady_iteration
   double* steady_dtloc = nullptr;  // [nci] per-cell time step of ty_steady_iteration (local_dt)
   cudaStream_t own_stream = nullptr;
