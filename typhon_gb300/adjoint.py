@@ -87,7 +87,7 @@ class Stepper:
             for s in range(k):
                 c = self.table[k - 1][s]
                 if c != 0.0:
-                    U += c * Rs[s]
+                    U.add_(Rs[s], alpha=c)
             Us.append(U)
             if k < self.n - 1 or last_residual:
                 Rs.append(self.residual(U, dt))
@@ -99,7 +99,7 @@ class Stepper:
         U = U0.clone()
         for s, c in enumerate(self.table[-1]):
             if c != 0.0:
-                U += c * Rs[s]
+                U.add_(Rs[s], alpha=c)
         if tape is not None:
             tape.append(Us)
         return U
@@ -112,13 +112,13 @@ class Stepper:
         lam_stage = [None] * self.n
         out = lam.clone()
         for s in reversed(range(self.n)):
-            lr = self.table[-1][s] * lam
+            lr = lam * self.table[-1][s]
             for k in range(s + 1, self.n):
                 c = self.table[k - 1][s]
                 if c != 0.0:
-                    lr = lr + c * lam_stage[k]
+                    lr.add_(lam_stage[k], alpha=c)
             lam_stage[s] = self.vjp(Us[s], dt, lr)
-            out += lam_stage[s]
+            out.add_(lam_stage[s])
         return out
 
 

@@ -59,20 +59,27 @@ int ty_adjoint_vjp(ty_mesh* h, double dt, const double* lamR, double* lamU) {
   if (second && h->o.mode == TY_MODE_FAST) {
     // array-of-structures records, lambda read and written in the caller's layout
     if (!h->adj_cell &&
-        ((rc = h->alloc(h->adj_cell, 32 * (size_t)m.ldc)) || (rc = h->alloc(h->adj_rec, 50 * (size_t)m.ldf)) ||
-         (rc = h->alloc(h->adj_qg, 24 * (size_t)m.ldc)) ||
-         (rc = h->alloc(h->adj_w, (3 + 6 * (size_t)m.nslot) * (size_t)m.nci)) ||
-         (rc = h->alloc(h->adj_nbc, (size_t)m.nslot * (size_t)m.nci))))
+        ((rc = h->alloc(h->adj_cell, 32 * (size_t)m.ldc)) || (rc = h->alloc(h->adj_rec, 44 * (size_t)m.ldf)) ||
+         (rc = h->alloc(h->adj_qg, 5 * (size_t)m.ldc)) || (rc = h->alloc(h->adj_ctb, 10 * (size_t)m.ldf)) ||
+         (rc = h->alloc(h->adj_w, (3 + 3 * (size_t)m.nslot) * (size_t)m.nci))))
       return rc;
     if (h->adj_w_gradmeth != h->lsq_gradmeth) {
-      cudaError_t e = kfast::adjoint_weights_fast(m, h->adj_w, h->adj_nbc, h->stream);
+      cudaError_t e = kfast::adjoint_weights_fast(m, h->adj_w, h->stream);
       if (e != cudaSuccess) return cuda_fail(e, "adjoint weights");
       h->adj_w_gradmeth = h->lsq_gradmeth;
     }
     cudaError_t e = kfast::adjoint_vjp_muscl_fast(m, h->s, h->o, h->s.u0, lamR, m.nci, dt, h->adj_cell, h->adj_rec,
-                                                  h->adj_qg, h->adj_qg + 5 * (size_t)m.ldc, h->adj_w, h->adj_nbc,
-                                                  lamU, m.nci, h->stream);
+                                                  h->adj_qg, h->adj_ctb, h->adj_w, lamU, m.nci, h->stream);
     h->prim_valid = false;  // s.prim now holds this state's primitive variables and ghosts
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint");
+    return TY_OK;
+  }
+  if (!second && h->o.mode == TY_MODE_FAST) {
+    if (!h->adj_cell1 &&
+        ((rc = h->alloc(h->adj_cell1, 12 * (size_t)m.ldc)) || (rc = h->alloc(h->adj_face1, 10 * (size_t)m.ldf))))
+      return rc;
+    cudaError_t e = kfast::adjoint_vjp_fast(m, h->o, h->s.u0, lamR, m.nci, dt, h->adj_cell1, h->adj_face1, lamU, m.nci,
+                                            h->stream);
     if (e != cudaSuccess) return cuda_fail(e, "adjoint");
     return TY_OK;
   }

@@ -413,11 +413,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_pack(DevMesh m, DevState s, bool
     const double wx = wtab[c], wy = wtab[n + c], wz = wtab[2 * n + c];
 #pragma unroll
     for (int v = 0; v < 5; ++v) { r[5 + 3 * v] = wx * r[v]; r[6 + 3 * v] = wy * r[v]; r[7 + 3 * v] = wz * r[v]; }
-    const double* ws = wtab + (3 + 3 * (size_t)m.nslot) * n;  // own-side weights per slot
     for (int sl = 0; sl < m.nslot; ++sl) {
       const int nb = m.cfn[sl * n + c];
       if (m.cf[sl * n + c] < 0) break;
-      const double* w = ws + 3 * (size_t)sl * n + c;
+      const double* w = wtab + (3 + 3 * (size_t)sl) * n + c;  // own-side weights of the slot
       const double ox = w[0], oy = w[n], oz = w[2 * n];
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
@@ -607,12 +606,16 @@ __global__ void __launch_bounds__(128, 3) k_adj_face2f_roe(DevMesh m, SpatOpts o
 }
 
 // per cell: the face records gathered (side s of a face: gradient block 16 s, q block 32 + 5 s;
-// a periodic face also brings its partner face's right-state block) into qb [5][ldc] and the
-// gradient adjoints gb [ldc][16].  NS >= nslot: the slot loop is unrolled so that every record
-// load is issued before the first is used.
+// a periodic face also brings its partner face's right-state block) into the adjoints of the
+// cell's q and gradient; the gradient's adjoint is then reversed through the least-squares
+// weights: the cell's own term is added to qb [5][ldc], and the term of each neighbour
+// (G_c = Wown q_c + sum over slots wo_slot q_nb) is written to ctb [nf][2][5] at the face and
+// this cell's side, for the neighbour's gather (k_adj_cell3f).  NS >= nslot: the slot loop is
+// unrolled so that every record load is issued before the first is used.
 template <int NS>
 __global__ void __launch_bounds__(kBlock) k_adj_cell2f(DevMesh m, const double* __restrict__ frec,
-                                                       double* __restrict__ qb, double* __restrict__ gb) {
+                                                       const double* __restrict__ wtab, double* __restrict__ qb,
+                                                       double* __restrict__ ctb) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nci) return;
   const size_t n = m.nci;
@@ -644,47 +647,52 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell2f(DevMesh m, const double* 
 #pragma unroll
     for (int v = 0; v < 5; ++v) q[v] += r[32 + 5 * rs[i] + v];
   }
+  {
+    const double wx = wtab[c], wy = wtab[n + c], wz = wtab[2 * n + c];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) q[v] += wx * g[3 * v] + wy * g[3 * v + 1] + wz * g[3 * v + 2];
+  }
   const size_t ld = m.ldc;
 #pragma unroll
   for (int v = 0; v < 5; ++v) qb[v * ld + c] = q[v];
-  double2* og = reinterpret_cast<double2*>(gb + (size_t)c * 16);
 #pragma unroll
-  for (int k = 0; k < 8; ++k) og[k] = make_double2(g[2 * k], g[2 * k + 1]);
+  for (int sl = 0; sl < NS; ++sl) {
+    const int f = rf[2 * sl];
+    if (f < 0) continue;
+    const double* w = wtab + (3 + 3 * (size_t)sl) * n + c;
+    const double wx = w[0], wy = w[n], wz = w[2 * n];
+    double* o = ctb + (size_t)f * 10 + 5 * rs[2 * sl];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) o[v] = wx * g[3 * v] + wy * g[3 * v + 1] + wz * g[3 * v + 2];
+  }
 }
 
-// per cell: the least-squares gradient reversed through the weight tables
-// (q_c adjoint += Wown . Gb_c + sum over slots W_slot . Gb_nb), then cons -> prim reversed
+// per cell: the neighbours' least-squares terms gathered from ctb (an interior face's other
+// side; on a periodic face owned by this cell, the partner face's owner side, whose ghost is
+// this cell), then cons -> prim reversed
 template <int NS>
 __global__ void __launch_bounds__(kBlock) k_adj_cell3f(DevMesh m, SpatOpts o, const double* __restrict__ u,
-                                                       const double* __restrict__ qbuf, const double* __restrict__ gb,
-                                                       const double* __restrict__ wtab, const int* __restrict__ nbc,
+                                                       const double* __restrict__ qbuf, const double* __restrict__ ctb,
                                                        double* __restrict__ lamU, int ldU) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nci) return;
   const size_t ld = m.ldc, n = m.nci;
-  int nb[NS + 1];
-  double w[NS + 1][3];
-  nb[0] = c;
-  w[0][0] = wtab[c]; w[0][1] = wtab[n + c]; w[0][2] = wtab[2 * n + c];
+  int rf[NS];
 #pragma unroll
   for (int sl = 0; sl < NS; ++sl) {
-    nb[sl + 1] = sl < m.nslot ? nbc[sl * n + c] : -1;
-    const double* ws = wtab + (3 + 3 * (size_t)sl) * n + c;
-#pragma unroll
-    for (int j = 0; j < 3; ++j) w[sl + 1][j] = nb[sl + 1] >= 0 ? ws[j * n] : 0.0;
+    const int e = sl < m.nslot ? m.cf[sl * n + c] : -1;
+    const int f = e >> 1, side = e & 1;
+    rf[sl] = e < 0 ? -1 : (f < m.nfi ? 10 * f + 5 * (1 - side) : 10 * m.part[f]);
   }
   double qb[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) qb[v] = qbuf[v * ld + c];
 #pragma unroll
-  for (int i = 0; i < NS + 1; ++i) {
-    if (nb[i] < 0) continue;
-    const double2* g2 = reinterpret_cast<const double2*>(gb + (size_t)nb[i] * 16);
-    double g[16];
+  for (int sl = 0; sl < NS; ++sl) {
+    if (rf[sl] < 0) continue;
+    const double* r = ctb + rf[sl];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) { const double2 t = g2[k]; g[2 * k] = t.x; g[2 * k + 1] = t.y; }
-#pragma unroll
-    for (int v = 0; v < 5; ++v) qb[v] += w[i][0] * g[3 * v] + w[i][1] * g[3 * v + 1] + w[i][2] * g[3 * v + 2];
+    for (int v = 0; v < 5; ++v) qb[v] += r[v];
   }
   double U[5], Q[5], Ub[5] = {0, 0, 0, 0, 0};
 #pragma unroll
@@ -695,55 +703,41 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell3f(DevMesh m, SpatOpts o, co
   for (int v = 0; v < 5; ++v) lamU[(size_t)v * ldU + c] = Ub[v];
 }
 
-// the weight tables of k_adj_pack and k_adj_cell3f (static geometry): Wown [3][nci] = sum over
-// the cell's faces of -+ (A^-1 d) of its side; per slot [3][nci] the weight with which this
-// cell's q enters the neighbour's gradient (the partner's inside cell for a periodic face);
-// per slot [3][nci] the cell's own +-(A^-1 d) (its gradient is the sum of these times q_nb
-// plus Wown q_c); nbc [nslot][nci] the neighbour (-1 past the cell's last face)
-__global__ void __launch_bounds__(kBlock) k_adj_wbuild(DevMesh m, double* __restrict__ wtab, int* __restrict__ nbc) {
+// the weight tables of k_adj_pack and k_adj_cell2f (static geometry): Wown [3][nci] = sum over
+// the cell's faces of -+ (A^-1 d) of its side, and per slot [3][nci] the cell's own +-(A^-1 d)
+// (its gradient is the sum of these times q_nb plus Wown q_c; zero past the last face)
+__global__ void __launch_bounds__(kBlock) k_adj_wbuild(DevMesh m, double* __restrict__ wtab) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nci) return;
   const size_t n = m.nci, lf = m.ldf;
   double W[3] = {0, 0, 0};
   for (int sl = 0; sl < m.nslot; ++sl) {
     const int e = m.cf[sl * n + c];
-    double* w = wtab + (3 + 3 * (size_t)sl) * n + c;
+    double* wo = wtab + (3 + 3 * (size_t)sl) * n + c;
     if (e < 0) {
-      nbc[sl * n + c] = -1;
-      double* wo = wtab + (3 + 3 * (size_t)m.nslot + 3 * (size_t)sl) * n + c;
-      w[0] = w[n] = w[2 * n] = 0.0;
       wo[0] = wo[n] = wo[2 * n] = 0.0;
       continue;
     }
     const int f = e >> 1, side = e & 1;
     const double sg = side ? 1.0 : -1.0;
-    double* wo = wtab + (3 + 3 * (size_t)m.nslot + 3 * (size_t)sl) * n + c;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       W[j] += sg * m.lsqw[(3 * side + j) * lf + f];
       wo[j * n] = -sg * m.lsqw[(3 * side + j) * lf + f];
     }
-    int oc, of, os;
-    double sgo;
-    if (f < m.nfi) { oc = side ? m.fc1[f] : m.fc2[f]; of = f; os = 1 - side; sgo = sg; }
-    else { of = m.part[f]; oc = m.fc1[of]; os = 0; sgo = 1.0; }
-#pragma unroll
-    for (int j = 0; j < 3; ++j) w[j * n] = sgo * m.lsqw[(3 * os + j) * lf + of];
-    nbc[sl * n + c] = oc;
   }
 #pragma unroll
   for (int j = 0; j < 3; ++j) wtab[j * n + c] = W[j];
 }
 
-cudaError_t adjoint_weights_fast(const DevMesh& m, double* wtab, int* nbc, cudaStream_t st) {
-  k_adj_wbuild<<<nblk(m.nci), kBlock, 0, st>>>(m, wtab, nbc);
+cudaError_t adjoint_weights_fast(const DevMesh& m, double* wtab, cudaStream_t st) {
+  k_adj_wbuild<<<nblk(m.nci), kBlock, 0, st>>>(m, wtab);
   return cudaGetLastError();
 }
 
 cudaError_t adjoint_vjp_muscl_fast(const DevMesh& m, const DevState& s, const SpatOpts& o, const double* u,
                                    const double* lamR, int ldR, double dt, double* crec, double* frec, double* qbuf,
-                                   double* gb, const double* wtab, const int* nbc, double* lamU, int ldU,
-                                   cudaStream_t st) {
+                                   double* ctb, const double* wtab, double* lamU, int ldU, cudaStream_t st) {
   k_prim<<<nblk(m.nci), kBlock, 0, st>>>(m, u, s.prim, o.gamma);
   if (m.ng > 0) k_ghost_prim<<<nblk(m.ng), kBlock, 0, st>>>(m, s.prim, o);
   const bool post = o.postlim != TY_POSTLIM_NONE;
@@ -758,12 +752,125 @@ cudaError_t adjoint_vjp_muscl_fast(const DevMesh& m, const DevState& s, const Sp
   else if (o.scheme == TY_SCH_RUSANOV) k_adj_face2f<TY_SCH_RUSANOV><<<gf, 128, 0, st>>>(m, o, crec, frec);
   else k_adj_face2f_roe<<<gf, 128, 0, st>>>(m, o, crec, frec);
   if (m.nslot <= 4) {
-    k_adj_cell2f<4><<<nblk(m.nci), kBlock, 0, st>>>(m, frec, qbuf, gb);
-    k_adj_cell3f<4><<<nblk(m.nci), kBlock, 0, st>>>(m, o, u, qbuf, gb, wtab, nbc, lamU, ldU);
+    k_adj_cell2f<4><<<nblk(m.nci), kBlock, 0, st>>>(m, frec, wtab, qbuf, ctb);
+    k_adj_cell3f<4><<<nblk(m.nci), kBlock, 0, st>>>(m, o, u, qbuf, ctb, lamU, ldU);
   } else {
-    k_adj_cell2f<kMaxSlot><<<nblk(m.nci), kBlock, 0, st>>>(m, frec, qbuf, gb);
-    k_adj_cell3f<kMaxSlot><<<nblk(m.nci), kBlock, 0, st>>>(m, o, u, qbuf, gb, wtab, nbc, lamU, ldU);
+    k_adj_cell2f<kMaxSlot><<<nblk(m.nci), kBlock, 0, st>>>(m, frec, wtab, qbuf, ctb);
+    k_adj_cell3f<kMaxSlot><<<nblk(m.nci), kBlock, 0, st>>>(m, o, u, qbuf, ctb, lamU, ldU);
   }
+  return cudaGetLastError();
+}
+
+// ---- fast-mode first-order adjoint: primitive states and dt/V lambda_R packed per cell (one
+// cons -> prim per cell instead of one per face side), the face kernel writes the adjoints of
+// the two face states, and the cell kernel reverses cons -> prim once per cell.
+constexpr int kAdjCell1 = 12;  // q (5), dt/V lambda_R (5), padding (2)
+
+__global__ void __launch_bounds__(kBlock) k_adj_pack1(DevMesh m, SpatOpts o, const double* __restrict__ u,
+                                                      const double* __restrict__ lamR, int ldR, double dt,
+                                                      double* __restrict__ crec) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t ld = m.ldc;
+  double U[5], r[kAdjCell1];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) U[v] = u[v * ld + c];
+  prim_r(o.gamma, U, r);
+  const double w = dt * m.invV[c];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) r[5 + v] = w * lamR[(size_t)v * ldR + c];
+  r[10] = 0.0; r[11] = 0.0;
+  double2* out = reinterpret_cast<double2*>(crec + (size_t)c * kAdjCell1);
+#pragma unroll
+  for (int k = 0; k < kAdjCell1 / 2; ++k) out[k] = make_double2(r[2 * k], r[2 * k + 1]);
+}
+
+// per face: the adjoints of the left and right face states (10 doubles; the right one is
+// folded into the left through the boundary state on a non-periodic boundary face)
+template <int SCH>
+__global__ void __launch_bounds__(128) k_adj_face1f(DevMesh m, SpatOpts o, const double* __restrict__ crec,
+                                                    double* __restrict__ frec) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int c1 = m.fc1[f];
+  const int kind = f < m.nfi ? TY_BC_INTERIOR : m.fbc[f];
+  const bool two = kind == TY_BC_INTERIOR || kind == TY_BC_PERIODIC;
+  const int cR = kind == TY_BC_INTERIOR ? m.fc2[f] : (kind == TY_BC_PERIODIC ? m.fc1[m.part[f]] : c1);
+  const double* A = crec + (size_t)c1 * kAdjCell1;
+  const double* B = crec + (size_t)cR * kAdjCell1;
+  const double S = m.fs[f];
+  double Fb[5], QL[5], QR[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    Fb[v] = kind == TY_BC_INTERIOR ? S * (B[5 + v] - A[5 + v]) : -S * A[5 + v];
+    QL[v] = A[v];
+    QR[v] = B[v];
+  }
+  if (!two) bc_state(m, o, f, kind, QL, QR);
+  double QLb[5] = {0, 0, 0, 0, 0}, QRb[5] = {0, 0, 0, 0, 0};
+  const size_t lf = m.ldf;
+  const double nx = m.fn[f], ny = m.fn[lf + f], nz = m.fn[2 * lf + f];
+  if constexpr (SCH == TY_SCH_HLLC) hllc_vjp(o.gamma, QL, QR, nx, ny, nz, Fb, QLb, QRb);
+  else if constexpr (SCH == TY_SCH_RUSANOV) rusanov_vjp(o.gamma, QL, QR, nx, ny, nz, Fb, QLb, QRb);
+  else roe_vjp(o.gamma, o.entropy_fix, QL, QR, nx, ny, nz, Fb, QLb, QRb);
+  if (!two) {
+    bc_state_vjp(m, o, f, kind, QRb, QLb);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) QRb[v] = 0.0;
+  }
+  double2* out = reinterpret_cast<double2*>(frec + (size_t)f * 10);
+  out[0] = make_double2(QLb[0], QLb[1]);
+  out[1] = make_double2(QLb[2], QLb[3]);
+  out[2] = make_double2(QLb[4], QRb[0]);
+  out[3] = make_double2(QRb[1], QRb[2]);
+  out[4] = make_double2(QRb[3], QRb[4]);
+}
+
+// per cell: the face-state adjoints of its faces (a periodic face also brings its partner's
+// right state, which is this cell's), then cons -> prim reversed
+template <int NS>
+__global__ void __launch_bounds__(kBlock) k_adj_cell1f(DevMesh m, SpatOpts o, const double* __restrict__ u,
+                                                       const double* __restrict__ frec, double* __restrict__ lamU,
+                                                       int ldU) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t n = m.nci, ld = m.ldc;
+  int rf[2 * NS], rs[2 * NS];
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    const int e = sl < m.nslot ? m.cf[sl * n + c] : -1;
+    const int f = e >> 1, side = e & 1;
+    rf[2 * sl] = e < 0 ? -1 : f;
+    rs[2 * sl] = side;
+    rf[2 * sl + 1] = (e >= 0 && !side && f >= m.nfi && m.fbc[f] == TY_BC_PERIODIC) ? m.part[f] : -1;
+    rs[2 * sl + 1] = 1;
+  }
+  double qb[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+  for (int i = 0; i < 2 * NS; ++i) {
+    if (rf[i] < 0) continue;
+    const double* r = frec + (size_t)rf[i] * 10 + 5 * rs[i];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) qb[v] += r[v];
+  }
+  double U[5], Q[5], Ub[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+  for (int v = 0; v < 5; ++v) U[v] = u[v * ld + c];
+  const double ir = prim_r(o.gamma, U, Q);
+  prim_vjp(o.gamma, U, ir, qb, Ub);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) lamU[(size_t)v * ldU + c] = Ub[v];
+}
+
+cudaError_t adjoint_vjp_fast(const DevMesh& m, const SpatOpts& o, const double* u, const double* lamR, int ldR,
+                             double dt, double* crec, double* frec, double* lamU, int ldU, cudaStream_t st) {
+  k_adj_pack1<<<nblk(m.nci), kBlock, 0, st>>>(m, o, u, lamR, ldR, dt, crec);
+  const unsigned gf = (unsigned)((m.nf + 127) / 128);
+  if (o.scheme == TY_SCH_HLLC) k_adj_face1f<TY_SCH_HLLC><<<gf, 128, 0, st>>>(m, o, crec, frec);
+  else if (o.scheme == TY_SCH_RUSANOV) k_adj_face1f<TY_SCH_RUSANOV><<<gf, 128, 0, st>>>(m, o, crec, frec);
+  else k_adj_face1f<TY_SCH_ROE><<<gf, 128, 0, st>>>(m, o, crec, frec);
+  if (m.nslot <= 4) k_adj_cell1f<4><<<nblk(m.nci), kBlock, 0, st>>>(m, o, u, frec, lamU, ldU);
+  else k_adj_cell1f<kMaxSlot><<<nblk(m.nci), kBlock, 0, st>>>(m, o, u, frec, lamU, ldU);
   return cudaGetLastError();
 }
 #endif  // TY_FAST

@@ -18,14 +18,15 @@ namespace tyk {
 TY_DECLARE_ADJOINT(kexact)
 TY_DECLARE_ADJOINT(kfast)
 
-// fast mode only: the second-order adjoint on array-of-structures records (lamR and lamU in
-// the caller's [5][ld] layout) and its static weight tables
+// fast mode only: the first- and second-order adjoints on array-of-structures records (lamR
+// and lamU in the caller's [5][ld] layout) and the second order's static weight tables
 namespace kfast {
-cudaError_t adjoint_weights_fast(const DevMesh& m, double* wtab, int* nbc, cudaStream_t st);
+cudaError_t adjoint_vjp_fast(const DevMesh& m, const SpatOpts& o, const double* u, const double* lamR, int ldR,
+                             double dt, double* crec, double* frec, double* lamU, int ldU, cudaStream_t st);
+cudaError_t adjoint_weights_fast(const DevMesh& m, double* wtab, cudaStream_t st);
 cudaError_t adjoint_vjp_muscl_fast(const DevMesh& m, const DevState& s, const SpatOpts& o, const double* u,
                                    const double* lamR, int ldR, double dt, double* crec, double* frec, double* qbuf,
-                                   double* gb, const double* wtab, const int* nbc, double* lamU, int ldU,
-                                   cudaStream_t st);
+                                   double* ctb, const double* wtab, double* lamU, int ldU, cudaStream_t st);
 }
 
 }  // namespace tyk

@@ -62,13 +62,16 @@ struct ty_mesh {
   double* adj_rec2 = nullptr;  // [50][ldf] reversed reconstructions (second-order adjoint, exact mode)
   double* adj_qg2 = nullptr;   // [20][ldc] adjoints of q and of the gradients (exact mode)
   // fast-mode second-order adjoint: cell records [nci][32], face records [nf][44], q adjoints
-  // [5][ldc] + gradient adjoints [nci][16], weight tables [3 + 6 nslot][nci] and neighbours
+  // [5][ldc], least-squares terms per face side [nf][2][5], weight tables [3 + 3 nslot][nci]
   double* adj_cell = nullptr;
   double* adj_rec = nullptr;
   double* adj_qg = nullptr;
+  double* adj_ctb = nullptr;
   double* adj_w = nullptr;
-  int* adj_nbc = nullptr;
   int adj_w_gradmeth = -1;
+  // fast-mode first-order adjoint: cell records [nci][12] (prim, dt/V lambda), face records [nf][10]
+  double* adj_cell1 = nullptr;
+  double* adj_face1 = nullptr;
   double* steady_red = nullptr;  // [3 kRedBlocks + 3] partial and final residual sums of ty_steady_iteration
   double* steady_dtloc = nullptr;  // [nci] per-cell time step of ty_steady_iteration (local_dt)
   cudaStream_t own_stream = nullptr;
