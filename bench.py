@@ -64,6 +64,12 @@ def parse():
                     "(default: the configuration's)")
     ap.add_argument("--adj-cs-directions", type=int, default=0, help="adjoint3d: directions of the complex-step "
                     "check (default: the configuration's)")
+    ap.add_argument("--adj-steps", type=int, default=0, help="adjoint3d: RK steps (default: the configuration's)")
+    ap.add_argument("--adj-fd-directions", type=int, default=0,
+                    help="adjoint3d: directions of the central-difference check (default: the configuration's)")
+    ap.add_argument("--adj-no-checks", action="store_true",
+                    help="adjoint3d: skip binomial checkpointing and the derivative checks (a short launch "
+                         "sequence for ncu)")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the short implicit, KDIF and adjoint runs of the default line")
     return ap.parse_args()
@@ -634,13 +640,26 @@ def run_adjoint(args):
     g.set_spat(w["scheme"], w["highres"], w["limiter"], mode="fast")
     g.set_prim(prim)
     dt = g.calc_zonetimestep(w["cfl"])
-    dts = [dt] * w["steps"]
+    nsteps = args.adj_steps or w["steps"]
+    dts = [dt] * nsteps
     U0 = torch.tensor(ty.prim_to_cons(prim[:, :nci]), device="cuda")
     cc = md.cell_centre[:nci]
     L = 2 * np.pi
     box = np.all(np.abs(cc - L / 2) < L / 4, axis=1).astype(float) * md.cell_volume[:nci]
     wbox = torch.tensor(box, device="cuda")
     st = adjoint.Stepper(g, w["rk"])
+
+    def per_call_ms(fn, reps=20):
+        """device time of one call, CUDA events on the library's stream (torch's current)"""
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
 
     def J_of(U):
         return float((U[0] ** 2 * wbox).sum())
@@ -665,6 +684,10 @@ def run_adjoint(args):
         t_lib = time.perf_counter() - t0
         lam = (2.0 * Uf[0] * wbox).unsqueeze(0) * torch.tensor([1.0, 0, 0, 0, 0], device="cuda").unsqueeze(1)
         lam = lam.contiguous()
+        # one residual and one VJP at the final state (state upload included in both)
+        lam_r = torch.randn_like(U0)
+        t_res_ms = per_call_ms(lambda: st.residual(Uf, dt))
+        t_vjp_ms = per_call_ms(lambda: st.vjp(Uf, dt, lam_r))
         # the storage policy of the device: every stage state kept when it fits (it does here)
         policy = adjoint.plan_storage(nci, st.n, len(dts))
         (Uf_s, tape), t_fwd_store = timed(lambda: adjoint.forward_steps_stored(st, U0, dts))
@@ -673,12 +696,16 @@ def run_adjoint(args):
         del tape
         same_primal = bool(torch.equal(Uf_s, Uf))
         # binomial checkpointing with a fixed number of stored states (memory-limited runs)
-        grad_b, t_adj = timed(lambda: adjoint.adjoint_steps(st, U0, dts, lam, w["snaps"]))
-        binomial_diff = float((grad_b - grad).abs().max())
+        if args.adj_no_checks:
+            t_adj, binomial_diff = float("nan"), None
+        else:
+            grad_b, t_adj = timed(lambda: adjoint.adjoint_steps(st, U0, dts, lam, w["snaps"]))
+            binomial_diff = float((grad_b - grad).abs().max())
     rng = np.random.default_rng(w["seed"])
     errs = []
     J0 = J_of(Uf)
-    for _ in range(w["directions"]):
+    fd_dirs = 0 if args.adj_no_checks else (args.adj_fd_directions or w["directions"])
+    for _ in range(fd_dirs):
         d = torch.tensor(rng.standard_normal((5, nci)), device="cuda") * U0.abs().mean(dim=1, keepdim=True)
         eps = 1e-6
         Jp = J_of(adjoint.forward_steps(st, U0 + eps * d, dts))
@@ -686,11 +713,11 @@ def run_adjoint(args):
         fd = (Jp - Jm) / (2 * eps)
         ad = float((grad * d).sum())
         errs.append(abs(ad - fd) / max(abs(fd), 1e-300))
-    cs_check = complex_step_sample(w, n=args.adj_cs_n, steps=args.adj_cs_steps or w["steps"],
-                                   directions=args.adj_cs_directions or w["directions"])
+    cs_check = None if args.adj_no_checks else complex_step_sample(
+        w, n=args.adj_cs_n, steps=args.adj_cs_steps or w["steps"], directions=args.adj_cs_directions or w["directions"])
     out = {"metric": "adjoint gradient / primal time, unsteady gradient of int rho^2 (forward pass storing the "
                      "stage states plus the reverse sweep)", "unit": "ratio",
-           "value": round((t_fwd_store + t_rev) / t_primal, 3), "higher_is_better": False, "n_gpus": 1, "steps": w["steps"],
+           "value": round((t_fwd_store + t_rev) / t_primal, 3), "higher_is_better": False, "n_gpus": 1, "steps": nsteps,
            "warmup": 2, "dtype": "f64", "data": "synthetic", "scaling": "weak", "vs_baseline": None,
            "config": {"workload": f"adjoint3d TGV {n}^3x5 tets, {w['scheme']} + {w['highres']} {w['limiter']} "
                                   f"(least-squares gradients), {w['rk']}",
@@ -699,12 +726,15 @@ def run_adjoint(args):
            "primal_storing_stages_s": round(t_fwd_store, 4), "stage_storage_bytes": tape_bytes,
            "reverse_sweep_s": round(t_rev, 4), "reverse_sweep_vs_primal": round(t_rev / t_primal, 3),
            "gradient_total_vs_primal": round((t_fwd_store + t_rev) / t_primal, 3),
+           "gradient_total_vs_library_primal": round((t_fwd_store + t_rev) / t_lib, 3),
+           "vjp_vs_residual": {"residual_ms": round(t_res_ms, 4), "vjp_ms": round(t_vjp_ms, 4),
+                               "ratio": round(t_vjp_ms / t_res_ms, 3)},
            "binomial": {"snapshots": w["snaps"], "adjoint_s": round(t_adj, 4),
                         "adjoint_vs_primal": round(t_adj / t_primal, 3),
-                        "recomputed_steps": adjoint.checkpoint_cost(w["steps"], w["snaps"]),
+                        "recomputed_steps": adjoint.checkpoint_cost(nsteps, w["snaps"]),
                         "max_abs_diff_vs_stored": binomial_diff},
            "stored_primal_bitwise_equal": same_primal,
-           "fd_check": {"directions": w["directions"], "eps": 1e-6, "max_rel_err": max(errs),
+           "fd_check": None if not errs else {"directions": fd_dirs, "eps": 1e-6, "max_rel_err": max(errs),
                         "median_rel_err": float(np.median(errs)),
                         "note": "van Albada's limiter has a kink where the two slopes change sign (local extrema): "
                                 "central differences of random per-cell perturbations cross kinks over 200 steps, "
@@ -715,14 +745,15 @@ def run_adjoint(args):
 
 
 def secondary_runs():
-    """Short but complete runs of the three other measurements, each in its own process at a
-    reduced size (the full-size runs are the --workload options), summarised for the default
-    line: time to a 1e-10 residual of FP64 vs mixed implicit solves, 50 KDIF steps of FP64 vs
-    mixed conjugate gradients, and the unsteady adjoint's cost against its primal run."""
+    """Short but complete runs of the three other measurements, each in its own process,
+    summarised for the default line: time to a 1e-10 residual of FP64 vs mixed implicit solves
+    and 50 KDIF steps of FP64 vs mixed conjugate gradients at reduced sizes (the full-size runs
+    are the --workload options), and the unsteady adjoint's cost against its primal run at the
+    configuration's size with fewer derivative checks."""
     runs = {"implicit": ["--workload", "ffbox3d-implicit", "--n", "24"],
             "kdif": ["--workload", "kdif3d", "--n", "35"],
-            "adjoint": ["--workload", "adjoint3d", "--n", "20", "--adj-cs-n", "6", "--adj-cs-steps", "20",
-                        "--adj-cs-directions", "4"]}
+            "adjoint": ["--workload", "adjoint3d", "--adj-fd-directions", "2", "--adj-cs-n", "6",
+                        "--adj-cs-steps", "20", "--adj-cs-directions", "4"]}
     out = {}
     for name, extra in runs.items():
         try:
@@ -748,7 +779,10 @@ def secondary_runs():
                          "cg_iteration_hbm_frac": v["cg_fp64"]["iteration"]["frac"]}
         else:
             out[name] = {"workload": d["config"]["workload"], "cells": d["config"]["cells"], "steps": d["steps"],
-                         "gradient_vs_primal": d["value"], "reverse_sweep_vs_primal": d["reverse_sweep_vs_primal"],
+                         "gradient_vs_primal": d["value"],
+                         "gradient_vs_library_primal": d["gradient_total_vs_library_primal"],
+                         "reverse_sweep_vs_primal": d["reverse_sweep_vs_primal"],
+                         "vjp_vs_residual": d["vjp_vs_residual"]["ratio"],
                          "binomial_vs_primal": d["binomial"]["adjoint_vs_primal"],
                          "complex_step_max_rel_err": d["complex_step_check"]["max_rel_err"],
                          "complex_step_sample": d["complex_step_check"]["sample"]}

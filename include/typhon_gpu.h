@@ -184,6 +184,19 @@ int ty_state_upload_device(ty_mesh* mesh, const double* cons_soa);
 int ty_state_download_device(ty_mesh* mesh, double* cons_soa);
 /* Primitive variables of the current state [5][ncell_int] (rho, p, u, v, w), host. */
 int ty_prim_download(ty_mesh* mesh, double* prim_soa);
+/* Typhon's ghost rows in explicit runs (replaces the ghost rows of flux_to_res.f90:90-113 and
+ * update_field.f90:38, where every cell's row, ghosts included, is updated): the residual row
+ * of a ghost cell is the raw flux F S of its face, not scaled by dt/V, and the Runge-Kutta
+ * combination adds it to the ghost's conservative state.  In a first-order run Typhon's ghost
+ * primitive variables come from that state, and its boundary monitors (integ_ustboco.f90,
+ * the histovar files) report them.  ty_ghost_state_set starts the bookkeeping from the ghost
+ * conservative states cons_ghost [5][nghost] (host; ghosts in the mesh's ghost order, cell
+ * ncell_int + k for ghost k); NULL stops it.  Explicit steps (ty_rk_step, ty_rk_steps,
+ * ty_steady_iteration) then keep it; it changes no interior value.  ty_ghost_prim_download
+ * gives the primitive variables [5][nghost] (host) of the ghost states the last stage's
+ * residual was evaluated with. */
+int ty_ghost_state_set(ty_mesh* mesh, const double* cons_ghost);
+int ty_ghost_prim_download(ty_mesh* mesh, double* prim_ghost);
 
 /* Global stability time step (calc_ns_timestep.f90:52-103 + min of
  * calc_zonetimestep.f90:95): dt = min_c 2 CFL V_c / sum_f S_f / (|u|+a). */

@@ -5,9 +5,9 @@ ty_steady_iteration: the residual history equals Typhon's monres.001 at every it
 (1e-10 in log10) and stops at the same iteration, and the state stays bit-identical to the
 oracle's in exact mode (within 1e-12 in fast mode).  From the final state Grid.write_vtk
 writes Typhon's typhonNS.vtk byte for byte and Grid.probe gives the MINP / MAXV / VCOMP
-probes of AUSM-MUSCLUNS as printed; NS/NUM/FLUX/HLLE's outlet flux history comes out as
-printed (its histovar file, of a first-order run, reports ghost conservative states that
-accumulate the raw boundary fluxes, which only the oracle keeps).  The AUSM-M flux has no Jacobian in Typhon: an implicit step with it
+probes of AUSM-MUSCLUNS as printed; NS/NUM/FLUX/HLLE's outlet flux and ghost-state histories
+come out as printed (its histovar file, of a first-order run, reports ghost conservative
+states that accumulate the raw boundary fluxes: ty_ghost_state_set keeps them).  The AUSM-M flux has no Jacobian in Typhon: an implicit step with it
 is refused.
 """
 import numpy as np
@@ -117,12 +117,46 @@ def test_gpu_hlle_histories(ty, golden_dir, mode):
     prim = np.zeros((5, md.ncell))
     prim[0], prim[1], prim[2] = rho, p, u
     g.set_prim(prim)
+    g.set_ghost_prim(prim[:, md.ncell_int:])   # Typhon initialises its ghost cells with the state
     out = g.ns_steady(1.0, 1.0, cycle_res=0.3, global_res=1e-4, method="EXPLICIT", history="RIGHT")
     gf = read_histo(golden_dir / "HLLE-EXPLICIT__histofluxNS_RIGHT")
     gv = read_histo(golden_dir / "HLLE-EXPLICIT__histovarNS_RIGHT")
     assert len(out["cycle_end"]) == 8 and len(gv) == 8
     for c in range(8):
         assert ["%.5E" % v for v in out["flux"][c]] == ["%.5E" % v for v in gf[c]], c
+        # the ghost rows' conservative states, as Typhon's first-order run keeps them
+        assert ["%.5E" % v for v in out["ghost"][c]] == ["%.5E" % v for v in gv[c]], c
+    g.close()
+
+
+def test_gpu_ghost_rows_match_oracle_bitwise(ty, golden_dir):
+    """Exact mode: the ghost conservative bookkeeping reproduces the oracle's ghost primitive
+    states bit for bit after RK3-SSP steps (every row of Typhon's Runge-Kutta combination);
+    a box with symmetry planes and a far field, first-order HLLC (inlets and outlets call pow,
+    whose last bit may differ between CUDA and the C library)."""
+    raw = ty.read_tym(golden_dir / "quad20x10.tym")
+    bcs = [("IMIN", op.BC_FARFIELD, "", (0.0, 0.0, 0.0)), ("IMAX", op.BC_FARFIELD, "", (0.0, 0.0, 0.0)),
+           ("JMIN", op.BC_SYMMETRY, "", (0.0, 0.0, 0.0)), ("JMAX", op.BC_SYMMETRY, "", (0.0, 0.0, 0.0))]
+    md = ty.preprocess(raw, 2, bcs)
+    om = op.Mesh.from_tym(golden_dir / "quad20x10.tym").build(2, bcs)
+    free = (1.0, 1.0 / 1.4, 0.5, 0.1, 0.0)
+    g = ty.Grid(md)
+    g.set_spat("HLLC", mode="exact", farfield=free)
+    c = md.cell_centre
+    n = md.ncell
+    prim = np.stack([1.0 + 0.1 * np.exp(-((c[:, 0] - 1.0) ** 2 + (c[:, 1] - 0.5) ** 2) / 0.02), np.full(n, 1 / 1.4),
+                     np.full(n, 0.5), 0.1 + 0.05 * np.sin(3.0 * c[:, 0]), np.zeros(n)])
+    g.set_prim(prim)
+    g.set_ghost_prim(prim[:, md.ncell_int:])
+    s = op.Solver(om, op.SCH_HLLC, rk="RK3-SSP", farfield=free)
+    s.set_prim(prim)
+    for _ in range(4):
+        dt = s.timestep()
+        g.treelevel_rungekutta("RK3-SSP", dt)
+        s.rk_step(dt)
+    nci = md.ncell_int
+    assert np.array_equal(g.get_cons(), s.get("cons")[:, :nci])
+    assert np.array_equal(g.ghost_prim(), s.get("prim")[:, nci:])
     g.close()
 
 

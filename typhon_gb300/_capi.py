@@ -97,6 +97,8 @@ _SIGS = {
     "ty_steady_iteration": ([C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_double), C.c_void_p],
                             C.c_int),
     "ty_debug_get": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "ty_ghost_state_set": ([C.c_void_p, C.c_void_p], C.c_int),
+    "ty_ghost_prim_download": ([C.c_void_p, C.c_void_p], C.c_int),
     "ty_debug_fastmath": ([C.c_int32, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "ty_set_bc_data": ([C.c_void_p, C.c_void_p], C.c_int),
     "ty_mesh_set_face_rotation": ([C.c_void_p, C.c_void_p], C.c_int),

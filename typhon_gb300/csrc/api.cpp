@@ -356,6 +356,15 @@ int run_step(ty_mesh* h, const RkTab& t, double dt, const unsigned long long* dt
   if (rc) return rc;
   for (int i = 0; i < t.n; ++i) {
     if ((rc = stage_faces(h))) return rc;
+    if (h->ghost_rows) {
+      GhostRk r;
+      r.stage = i;
+      r.nstage = t.n;
+      for (int s = 0; s < i; ++s) r.cs[s] = t.c[i - 1][s];
+      for (int s = 0; s < t.n; ++s) r.cf[s] = t.c[t.n - 1][s];
+      cudaError_t e = MODE_CALL(h, ghost_rows, h->m, h->s, h->o, r, h->gcons, h->gres, h->gprim, h->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "ghost rows");
+    }
     cudaError_t e = MODE_CALL(h, rk_update, h->m, h->s, h->o, plans[i], dt, dtbits_cur,
                               i == t.n - 1 ? dtbits_next : nullptr, cfl, h->stream, &h->prof);
     if (e != cudaSuccess) return cuda_fail(e, "rk update");
@@ -810,6 +819,42 @@ int ty_steady_iteration(ty_mesh* h, int32_t method, double cfl, int32_t local_dt
   }
   TY_CU(cudaStreamSynchronize(h->stream));
   return check_err(h);
+}
+
+int ty_ghost_state_set(ty_mesh* h, const double* cons_ghost) {
+  if (!h) return TY_ERR_ARG;
+  TY_CU(cudaSetDevice(h->device));
+  if (!cons_ghost) {
+    h->ghost_rows = false;
+    return TY_OK;
+  }
+  const size_t ng = (size_t)h->m.ng;
+  if (ng == 0) {
+    tyi::set_error("ty_ghost_state_set: the mesh has no ghost cells");
+    return TY_ERR_ARG;
+  }
+  int rc;
+  if (!h->gcons && ((rc = h->alloc(h->gcons, 5 * ng)) || (rc = h->alloc(h->gres, (size_t)kMaxStage * 5 * ng)) ||
+                    (rc = h->alloc(h->gprim, 5 * ng))))
+    return rc;
+  TY_CU(cudaMemcpyAsync(h->gcons, cons_ghost, 5 * ng * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  TY_CU(cudaMemsetAsync(h->gprim, 0, 5 * ng * sizeof(double), h->stream));
+  TY_CU(cudaStreamSynchronize(h->stream));
+  h->ghost_rows = true;
+  return TY_OK;
+}
+
+int ty_ghost_prim_download(ty_mesh* h, double* prim_ghost) {
+  if (!h || !prim_ghost) return TY_ERR_ARG;
+  if (!h->ghost_rows) {
+    tyi::set_error("ty_ghost_prim_download: no ghost state (ty_ghost_state_set)");
+    return TY_ERR_STATE;
+  }
+  TY_CU(cudaSetDevice(h->device));
+  TY_CU(cudaMemcpyAsync(prim_ghost, h->gprim, 5 * (size_t)h->m.ng * sizeof(double), cudaMemcpyDeviceToHost,
+                        h->stream));
+  TY_CU(cudaStreamSynchronize(h->stream));
+  return TY_OK;
 }
 
 int ty_debug_get(ty_mesh* h, int32_t which, double* out) {

@@ -145,6 +145,18 @@ struct Prof {
   ~Prof() { for (auto e : pool) cudaEventDestroy(e); }
 };
 
+// Typhon's ghost rows in explicit runs (flux_to_res.f90:90-113, update_field.f90:38): the
+// residual row of a ghost cell is the raw flux F S of its face (not scaled by dt/V), and the
+// Runge-Kutta combination adds it to the ghost's conservative state like any cell's row.
+// One stage of that bookkeeping: the stage's ghost state u0 + sum_{s<stage} cs[s] r_s (its
+// primitive variables are kept), the stage's rows r_stage, and after the last stage
+// u0 += cf[0] r_0 + ... + cf[n-1] r_{n-1}.
+struct GhostRk {
+  int stage = 0, nstage = 1;
+  double cs[kMaxStage] = {};
+  double cf[kMaxStage] = {};
+};
+
 // Launch sequences implemented once per arithmetic mode (kernels_exact.cu, kernels_fast.cu).
 #define TY_DECLARE_MODE(NS)                                                                        \
   namespace NS {                                                                                   \
@@ -160,6 +172,8 @@ struct Prof {
   cudaError_t timestep(const DevMesh& m, const DevState& s, const SpatOpts& o, const double* cons, \
                        double cfl, unsigned long long* dtbits, cudaStream_t st, Prof* pr);         \
   cudaError_t unpack_state(const DevMesh& m, const DevState& s, cudaStream_t st);                  \
+  cudaError_t ghost_rows(const DevMesh& m, const DevState& s, const SpatOpts& o, const GhostRk& r,   \
+                         double* gcons, double* gres, double* gprim, cudaStream_t st);             \
   cudaError_t pack_state(const DevMesh& m, const DevState& s, cudaStream_t st);                    \
   }
 

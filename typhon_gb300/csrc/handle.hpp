@@ -72,6 +72,12 @@ struct ty_mesh {
   // fast-mode first-order adjoint: cell records [nci][12] (prim, dt/V lambda), face records [nf][10]
   double* adj_cell1 = nullptr;
   double* adj_face1 = nullptr;
+  // ghost-row bookkeeping of explicit runs (ty_ghost_state_set): conservative states [5][ng],
+  // stage rows [kMaxStage][5][ng], primitive variables of the last stage's state [5][ng]
+  double* gcons = nullptr;
+  double* gres = nullptr;
+  double* gprim = nullptr;
+  bool ghost_rows = false;
   double* steady_red = nullptr;  // [3 kRedBlocks + 3] partial and final residual sums of ty_steady_iteration
   double* steady_dtloc = nullptr;  // [nci] per-cell time step of ty_steady_iteration (local_dt)
   cudaStream_t own_stream = nullptr;

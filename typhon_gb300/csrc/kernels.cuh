@@ -1451,6 +1451,42 @@ cudaError_t timestep(const DevMesh& m, const DevState& s, const SpatOpts& o, con
   return cudaGetLastError();
 }
 
+// One stage of the ghost-row bookkeeping (GhostRk): one thread per ghost cell, [5][ng] arrays
+// (gres [nstage][5][ng]), the operation order of the oracle's Runge-Kutta loop over all cells.
+__global__ void k_ghost_rows(DevMesh m, const double* __restrict__ flux, GhostRk r, double gamma,
+                             double* __restrict__ gcons, double* __restrict__ gres, double* __restrict__ gprim) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= m.ng) return;
+  const size_t ng = m.ng;
+  const int f = m.gface[g];
+  double U[5], Q[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) U[v] = gcons[v * ng + g];
+  for (int s = 0; s < r.stage; ++s)
+#pragma unroll
+    for (int v = 0; v < 5; ++v) U[v] = U[v] + r.cs[s] * gres[(s * 5 + v) * ng + g];
+  cons_to_prim(gamma, U, Q);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    gprim[v * ng + g] = Q[v];
+    gres[(r.stage * 5 + v) * ng + g] = flux[v * (size_t)m.ldf + f];
+  }
+  if (r.stage == r.nstage - 1) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      double a = r.cf[0] * gres[v * ng + g];
+      for (int s = 1; s < r.nstage; ++s) a = a + r.cf[s] * gres[(s * 5 + v) * ng + g];
+      gcons[v * ng + g] = gcons[v * ng + g] + a;
+    }
+  }
+}
+
+cudaError_t ghost_rows(const DevMesh& m, const DevState& s, const SpatOpts& o, const GhostRk& r, double* gcons,
+                       double* gres, double* gprim, cudaStream_t st) {
+  if (m.ng > 0) k_ghost_rows<<<nblk(m.ng), kBlock, 0, st>>>(m, s.flux, r, o.gamma, gcons, gres, gprim);
+  return cudaGetLastError();
+}
+
 // Typhon layout (rho[n], rhoE[n], rhou as (x,y,z)[n]) <-> SoA u0, on the device
 __global__ void k_unpack_state(DevMesh m, const double* __restrict__ stage, double* __restrict__ u0) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;

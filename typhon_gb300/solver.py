@@ -64,6 +64,7 @@ class Grid:
             _capi.check(self.lib.ty_mesh_set_face_rotation(h, rot.ctypes.data), "ty_mesh_set_face_rotation")
         self.nci = mesh.ncell_int
         self.gamma = 1.4
+        self.gradmeth = "NONE"
         self.time = 0.0
 
     def close(self):
@@ -97,6 +98,7 @@ class Grid:
                              (C.c_double * 5)(*map(float, farfield)))
         _capi.check(self.lib.ty_set_params(self.h, C.byref(p)), "ty_set_params")
         self.gamma = gamma
+        self.gradmeth = gradmeth
 
     # -- state -----------------------------------------------------------------------------
     def set_cons(self, cons):
@@ -110,6 +112,25 @@ class Grid:
 
     def set_prim(self, prim):
         self.set_cons(prim_to_cons(np.asarray(prim, np.float64).reshape(5, -1)[:, :self.nci], self.gamma))
+
+    def set_ghost_prim(self, prim_ghost):
+        """Start Typhon's ghost-row bookkeeping of explicit runs (ty_ghost_state_set) from the
+        ghost primitive states [5][nghost] (cells ncell_int.. of the mesh), converted as
+        calc_varcons_ns does; None stops it."""
+        if prim_ghost is None:
+            _capi.check(self.lib.ty_ghost_state_set(self.h, None), "ty_ghost_state_set")
+            return
+        ng = self.mesh.ncell - self.nci
+        cons = np.ascontiguousarray(prim_to_cons(np.asarray(prim_ghost, np.float64).reshape(5, ng), self.gamma))
+        _capi.check(self.lib.ty_ghost_state_set(self.h, cons.ctypes.data), "ty_ghost_state_set")
+        self._ghost_rows = True
+
+    def ghost_prim(self):
+        """Primitive variables [5][nghost] of the ghost states of the last stage (the ghost
+        primitive variables of a first-order Typhon run)."""
+        out = np.zeros((5, self.mesh.ncell - self.nci))
+        _capi.check(self.lib.ty_ghost_prim_download(self.h, out.ctypes.data), "ty_ghost_prim_download")
+        return out
 
     def upload_typhon(self, rho, rhoE, rhou):
         """Upload a conserved state given in Typhon's layout without any conversion:
@@ -245,8 +266,10 @@ class Grid:
         states into its ghost cells (runs with gradients); in a first-order run Typhon's
         ghost cells instead carry conservative states that accumulate the raw boundary
         fluxes F S (flux_to_res.f90 adds them unscaled to the ghost rows, update_field.f90
-        adds those rows), which this library does not keep.  Three scalars per
-        iteration come back to the host.  Returns dict(log_res, cycle_end, flux, ghost)."""
+        adds those rows): with set_ghost_prim called before an explicit first-order run the
+        ghost primitive states come from that bookkeeping (ty_ghost_prim_download), as
+        Typhon's do.  Three scalars per iteration come back to the host.  Returns
+        dict(log_res, cycle_end, flux, ghost)."""
         m, nci = self.mesh, self.nci
         V = m.cell_volume[:nci]
         U = self.get_cons()[:, :nci]
@@ -292,6 +315,9 @@ class Grid:
                 # integ_ustboco.f90: sum of F S over the family's faces, and the S-weighted
                 # average of the ghost primitive states, face by face
                 fl, q = self.debug("flux"), self.debug("prim")
+                if getattr(self, "_ghost_rows", False) and method != "IMPLICIT" and self.gradmeth == "NONE":
+                    q = q.copy()
+                    q[:, nci:] = self.ghost_prim()
                 fs, qa, area = np.zeros(5), np.zeros(5), 0.0
                 for f in hist:
                     fs = fs + fl[:, f]
