@@ -100,8 +100,55 @@ struct FaceKeyHash {
   size_t operator()(const FaceKey& k) const {
     uint64_t h = 1469598103934665603ull;
     for (int x : k.v) { h ^= (uint64_t)(uint32_t)x; h *= 1099511628211ull; }
-    return (size_t)h;
+    return (size_t)(h ^ (h >> 29));
   }
+};
+
+// Face lookup during face creation: open addressing with linear probing in flat arrays (a
+// node-based map spent most of the preprocessing time allocating).  nmax bounds the element
+// faces visited; each interior face is visited twice, so at most about nmax / 2 keys are
+// stored and a power-of-two capacity >= nmax keeps the load near one half or below.
+class FaceTable {
+ public:
+  explicit FaceTable(size_t nmax) {
+    size_t cap = 16;
+    while (cap < nmax) cap <<= 1;
+    mask_ = cap - 1;
+    keys_.resize(cap);
+    vals_.assign(cap, -1);
+  }
+  // the face id of key, or -1 after inserting key with id `fresh`
+  int find_or_insert(const FaceKey& key, int fresh) {
+    size_t i = FaceKeyHash()(key) & mask_;
+    while (true) {
+      if (vals_[i] < 0) {
+        keys_[i] = key;
+        vals_[i] = fresh;
+        return -1;
+      }
+      if (keys_[i] == key) return vals_[i];
+      i = (i + 1) & mask_;
+    }
+  }
+  // the face id of key, or -1
+  int find(const FaceKey& key) const {
+    size_t i = FaceKeyHash()(key) & mask_;
+    while (vals_[i] >= 0) {
+      if (keys_[i] == key) return vals_[i];
+      i = (i + 1) & mask_;
+    }
+    return -1;
+  }
+  // every stored id f replaced by newidx[f]
+  void remap(const std::vector<int>& newidx) {
+    for (int& v : vals_)
+      if (v >= 0) v = newidx[v];
+  }
+
+ private:
+  size_t mask_;
+  std::vector<FaceKey> keys_;
+  std::vector<int> vals_;
 };
 FaceKey key_of(const int* f, int n) {
   FaceKey k;
@@ -196,8 +243,17 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
   std::vector<int> fv;        // 4 per face, creation order
   std::vector<int> fnv;       // vertex count per face
   std::vector<int> c1, c2;    // 1-based cells, 0 = none
-  std::unordered_map<FaceKey, int, FaceKeyHash> lookup;
-  lookup.reserve((size_t)ncell_int * 3);
+  size_t nface_max = 0;  // faces created at most: one per element face
+  for (auto& s : um->sections) {
+    if (elem_dim(s.type) != maxdim) continue;
+    const int per = s.type == 13 ? 3 : s.type == 24 ? 4 : s.type == 101 ? 4 : s.type == 131 ? 5 : 6;
+    nface_max += (size_t)per * s.ielem.size();
+  }
+  FaceTable lookup(nface_max);
+  fv.reserve(4 * nface_max / 2 + 16);
+  fnv.reserve(nface_max / 2 + 4);
+  c1.reserve(nface_max / 2 + 4);
+  c2.reserve(nface_max / 2 + 4);
   static const int tri[3][2] = {{1, 2}, {2, 3}, {3, 1}};
   static const int quad[4][2] = {{1, 2}, {2, 3}, {3, 4}, {4, 1}};
   static const int tet[4][3] = {{1, 3, 2}, {1, 2, 4}, {2, 3, 4}, {3, 1, 4}};
@@ -215,18 +271,16 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
           f[k] = e[loc[k] - 1];
           if (f[k] < 1 || f[k] > nvtex) return false;
         }
-        FaceKey key = key_of(f, n);
-        auto it = lookup.find(key);
-        if (it == lookup.end()) {
-          int id = (int)c1.size();
-          lookup.emplace(key, id);
+        const FaceKey key = key_of(f, n);
+        const int id = lookup.find_or_insert(key, (int)c1.size());
+        if (id < 0) {
           for (int k = 0; k < 4; ++k) fv.push_back(f[k]);
           fnv.push_back(n);
           c1.push_back(icell);
           c2.push_back(0);
         } else {
-          if (c2[it->second] != 0) return false;
-          c2[it->second] = icell;
+          if (c2[id] != 0) return false;
+          c2[id] = icell;
         }
         return true;
       };
@@ -262,7 +316,7 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
     F1[n] = c1[f]; F2[n] = c2[f]; FN[n] = fnv[f];
     for (int k = 0; k < 4; ++k) FV[4 * (size_t)n + k] = fv[4 * (size_t)f + k];
   }
-  for (auto& kv : lookup) kv.second = newidx[kv.second];
+  lookup.remap(newidx);
 
   // ---- boundary marks -> boundary faces (mark order) ----
   struct Boco { std::string family; std::vector<int> iface; int kind = 0; int def = -1; double rlink = 0;
@@ -297,8 +351,8 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
         if (it == face_elem.end()) continue;
         auto& s = um->sections[it->second.first];
         int nv = elem_nv(s.type);
-        auto fk = lookup.find(key_of(&s.vtex[(size_t)it->second.second * nv], nv));
-        if (fk != lookup.end() && fk->second >= nfi) b.iface.push_back(fk->second);
+        const int fk = lookup.find(key_of(&s.vtex[(size_t)it->second.second * nv], nv));
+        if (fk >= nfi) b.iface.push_back(fk);
       }
       if (!b.iface.empty()) bocos.push_back(std::move(b));
     }

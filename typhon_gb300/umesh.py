@@ -276,11 +276,14 @@ def gen_tet_box(n, length, jitter=0.0, seed=1234):
     for t in range(5):
         conn[:, t, :] = np.where(even, v[:, list(tets_even[t])], v[:, list(tets_odd[t])])
     conn = conn.reshape(-1, 4)
-    # boundary triangles: faces seen once
+    # boundary triangles: the element faces whose three nodes lie on one face of the box (the
+    # faces seen once), in element-face order
     fl = np.concatenate([conn[:, [0, 2, 1]], conn[:, [0, 1, 3]], conn[:, [1, 2, 3]], conn[:, [2, 0, 3]]])
-    key = np.sort(fl, axis=1)
-    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
-    bnd = fl[cnt[inv.reshape(-1)] == 1]
+    ijk = np.unravel_index(fl - 1, (n + 1, n + 1, n + 1))
+    on = np.zeros(len(fl), bool)
+    for a in range(3):
+        on |= (ijk[a] == 0).all(axis=1) | (ijk[a] == n).all(axis=1)
+    bnd = fl[on]
     cen = vt[bnd - 1].mean(axis=1)
     tol = 1e-9 * length
     names = [("IMIN", 0, 0.0), ("IMAX", 0, length), ("JMIN", 1, 0.0), ("JMAX", 1, length),
@@ -423,9 +426,13 @@ def gen_kuhn_box(n, length=1.0):
     neg = np.einsum("ij,ij->i", np.cross(b - a, c - a), d - a) < 0
     tets[neg, 1], tets[neg, 2] = tets[neg, 2].copy(), tets[neg, 1].copy()
     fl = np.concatenate([tets[:, [0, 2, 1]], tets[:, [0, 1, 3]], tets[:, [1, 2, 3]], tets[:, [2, 0, 3]]])
-    key = np.sort(fl, axis=1)
-    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
-    bnd = fl[cnt[inv.reshape(-1)] == 1]
+    # boundary triangles: the element faces whose three nodes lie on one face of the box (the
+    # faces seen once), in element-face order
+    ijk = np.unravel_index(fl - 1, (n + 1, n + 1, n + 1))
+    on = np.zeros(len(fl), bool)
+    for a in range(3):
+        on |= (ijk[a] == 0).all(axis=1) | (ijk[a] == n).all(axis=1)
+    bnd = fl[on]
     cen = vt[bnd - 1].mean(axis=1)
     tol = 1e-9 * length
     faces, marks, nextid = [], [], 1
