@@ -83,27 +83,41 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 100 ms while running."""
+    """nvidia-smi clocks and throttle reasons sampled every `interval_ms` while running.  Entering
+    waits (up to 5 s) for the first sample, so that sampling is under way when the measured work
+    starts; mark() / mark(end=True) bracket the timed region, and summary() then covers the
+    samples taken inside it (at least the one nearest to it)."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index):
+    def __init__(self, index, interval_ms=100):
         self.index = index
+        self.interval_ms = interval_ms
         self.lines = []
         self.proc = None
+        self.i0 = self.i1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.interval_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.005)
         except FileNotFoundError:
             self.proc = None
         return self
+
+    def mark(self, end=False):
+        if end:
+            self.i1 = len(self.lines)
+        else:
+            self.i0 = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -120,7 +134,12 @@ class ClockSampler:
     def summary(self):
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if self.i0 is not None:
+            i1 = self.i1 if self.i1 is not None else len(lines)
+            # the samples inside the timed region, and the next one (taken as it ended)
+            lines = lines[max(self.i0 - 1, 0) if i1 <= self.i0 else self.i0:i1 + 1]
+        for ln in lines:
             p = [x.strip() for x in ln.split(",")]
             if len(p) < 8:
                 continue
@@ -215,6 +234,8 @@ def run_ours(args, rank, world, local):
     nci = md.ncell_int
     info = g.info()
     nslot_avg = (2 * md.nface_int + (md.nface - md.nface_int)) / nci
+    # clocks sampled every 20 ms from before the warm-up (the timed region can be ~0.1 s)
+    clk = ClockSampler(local, interval_ms=20).__enter__()
     # warmup
     g.run_steps(w["rk"], w["cfl"], args.warmup)
     torch.cuda.synchronize(local)
@@ -229,12 +250,15 @@ def run_ours(args, rank, world, local):
     _capi.check(g.lib.ty_profile_enable(g.h, 1), "ty_profile_enable")
     barrier()
     torch.cuda.synchronize(local)
-    with ClockSampler(local) as clk:
-        with torch.cuda.stream(stream):
-            e0.record(stream)
-            g.run_steps(w["rk"], w["cfl"], args.steps)
-            e1.record(stream)
-        torch.cuda.synchronize(local)
+    clk.mark()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        g.run_steps(w["rk"], w["cfl"], args.steps)
+        e1.record(stream)
+    torch.cuda.synchronize(local)
+    clk.mark(end=True)
+    time.sleep(0.03)   # the sample taken as the region ended
+    clk.__exit__(None, None, None)
     barrier()
     ms = e0.elapsed_time(e1)
     nk = len(_capi.KERNEL_NAMES)

@@ -346,8 +346,8 @@ cudaError_t adjoint_vjp_muscl(const DevMesh& m, const DevState& s, const SpatOpt
   if (o.postlim != TY_POSTLIM_NONE) {  // gradient and the Barth ratios of the forward residual
     const double klim = o.postlim == TY_POSTLIM_SUPERBARTH ? 1.0 : 0.5;
     if (kFast) {
-      if (m.nslot <= 4) k_cell_fast<4, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim);
-      else k_cell_fast<8, 64><<<(unsigned)((m.nci + 63) / 64), 64, 0, st>>>(m, s, o, klim);
+      if (m.nslot <= 4) k_cell_fast<4, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim, true);
+      else k_cell_fast<8, 64><<<(unsigned)((m.nci + 63) / 64), 64, 0, st>>>(m, s, o, klim, true);
     } else {
       k_grad<<<nblk(m.nci), kBlock, 0, st>>>(m, s);
       k_face_states<<<nblk(m.nf), kBlock, 0, st>>>(m, s, o);
@@ -743,8 +743,8 @@ cudaError_t adjoint_vjp_muscl_fast(const DevMesh& m, const DevState& s, const Sp
   const bool post = o.postlim != TY_POSTLIM_NONE;
   if (post) {  // gradient and the Barth ratios of the forward residual
     const double klim = o.postlim == TY_POSTLIM_SUPERBARTH ? 1.0 : 0.5;
-    if (m.nslot <= 4) k_cell_fast<4, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim);
-    else k_cell_fast<8, 64><<<(unsigned)((m.nci + 63) / 64), 64, 0, st>>>(m, s, o, klim);
+    if (m.nslot <= 4) k_cell_fast<4, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim, true);
+    else k_cell_fast<8, 64><<<(unsigned)((m.nci + 63) / 64), 64, 0, st>>>(m, s, o, klim, true);
   }
   k_adj_pack<<<nblk(m.nci), kBlock, 0, st>>>(m, s, post, lamR, ldR, dt, wtab, crec);
   const unsigned gf = (unsigned)((m.nf + 127) / 128);

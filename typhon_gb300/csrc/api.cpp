@@ -636,6 +636,15 @@ int ty_set_params(ty_mesh* h, const ty_spat_params* p) {
   if ((p->postlim != TY_POSTLIM_NONE || (p->mode == TY_MODE_FAST && p->highres != TY_HRES_NONE)) && !h->s.cl) {
     if ((rc = h->alloc(h->s.cl, 5 * (size_t)h->m.ldf)) || (rc = h->alloc(h->s.cr, 5 * (size_t)h->m.ldf))) return rc;
   }
+  // fast MUSCL / MUSCL-UNS without limiter: the per-cell increment matrices of k_cell_fast
+  h->m.mtab = nullptr;
+  if (p->mode == TY_MODE_FAST && (p->highres == TY_HRES_MUSCL || p->highres == TY_HRES_MUSCLUNS) &&
+      p->limiter == TY_LIM_NONE && p->gradmeth != TY_GRAD_NONE && h->m.nslot > 0) {
+    if (!h->mtab_buf && (rc = h->alloc(h->mtab_buf, (size_t)h->m.nslot * h->m.nslot * (size_t)h->m.nci))) return rc;
+    cudaError_t e = tyk::kfast::build_mtab(h->m, h->mtab_buf, h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "increment matrices");
+    h->m.mtab = h->mtab_buf;
+  }
   h->o.scheme = p->scheme; h->o.highres = p->highres; h->o.limiter = p->limiter; h->o.postlim = p->postlim;
   h->o.gradmeth = p->gradmeth; h->o.mode = p->mode; h->o.gamma = p->gamma; h->o.entropy_fix = p->entropy_fix;
   h->o.inv_entropy_fix = p->entropy_fix > 0.0 ? 1.0 / p->entropy_fix : 0.0;

@@ -49,6 +49,10 @@ struct DevMesh {
   const double* recw = nullptr;   // [8][ldf] fast MUSCL/-UNS without limiter: per side w (3), k (1),
                                   // face increment = grad q . w + (q_nb - q_c) k
   const double* invdLR = nullptr; // [ldf] 1 / dLR (fast mode)
+  const double* mtab = nullptr;   // [nslot][nslot][nci] fast MUSCL/-UNS without limiter: the face
+                                  // increments of a cell are linear in its neighbour differences,
+                                  // D_i = sum_j M_ij dq_j (gradient and reconstruction folded);
+                                  // null when not built
   const int* cfn = nullptr;       // [nslot][nci] neighbour cell across each gather-list face
   const double* invV = nullptr;   // [nci] 1 / V (fast mode)
   const double* geo2 = nullptr;   // [nci] 2 V / sum S (fast mode time step)
@@ -179,5 +183,10 @@ struct GhostRk {
 
 TY_DECLARE_MODE(kexact)
 TY_DECLARE_MODE(kfast)
+
+namespace kfast {
+// the per-cell increment matrices of DevMesh::mtab, from lsqw, recw and the gather lists
+cudaError_t build_mtab(const DevMesh& m, double* mtab, cudaStream_t st);
+}
 
 }  // namespace tyk

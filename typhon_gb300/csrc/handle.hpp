@@ -74,6 +74,7 @@ struct ty_mesh {
   double* adj_face1 = nullptr;
   // ghost-row bookkeeping of explicit runs (ty_ghost_state_set): conservative states [5][ng],
   // stage rows [kMaxStage][5][ng], primitive variables of the last stage's state [5][ng]
+  double* mtab_buf = nullptr;  // [nslot][nslot][nci] increment matrices (DevMesh::mtab)
   double* gcons = nullptr;
   double* gres = nullptr;
   double* gprim = nullptr;

@@ -1095,8 +1095,16 @@ __device__ __forceinline__ void delta_fast(const DevMesh& m, const SpatOpts& o, 
 // zero imposes no constraint in both modes.
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
 
+//
+// With DevMesh::mtab (MUSCL / MUSCL-UNS without limiter) the increments come from the cell's
+// matrix, D_i = sum_j M_ij dq_j: the gradient G = sum_j (+-A^-1 d_j) dq_j and the increment
+// D_i = G . w_i + dq_i k_i folded into one product of nslot^2 multiply-adds per variable (16
+// for a tetrahedron, against 12 for the gradient and 16 for the increments), read coalesced
+// per cell instead of per face; the gradient itself is then computed only when asked
+// (want_grad: a viscous flux or the adjoint reads it).
 template <int NS, int BLK>
-__global__ void __launch_bounds__(BLK, 512 / BLK) k_cell_fast(DevMesh m, DevState s, SpatOpts o, double klim) {
+__global__ void __launch_bounds__(BLK, 512 / BLK) k_cell_fast(DevMesh m, DevState s, SpatOpts o, double klim,
+                                                              bool want_grad) {
   __shared__ double sD[NS * 5][BLK];
   __shared__ double sQ[NS * 5][BLK];
   const int c = blockIdx.x * BLK + threadIdx.x;
@@ -1107,31 +1115,49 @@ __global__ void __launch_bounds__(BLK, 512 / BLK) k_cell_fast(DevMesh m, DevStat
   double qc[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) qc[v] = prim[v * ld + c];
+  const bool mt = m.mtab != nullptr;
+  const bool grad = !mt || want_grad;
   double gr[15];
 #pragma unroll
   for (int k = 0; k < 15; ++k) gr[k] = 0.0;
+  // the gather-list entries and neighbours of every slot first, so that the neighbour loads
+  // below are independent of each other and issue together
+  int es[NS], nbs[NS];
   int ns = 0;
-  for (int sl = 0; sl < m.nslot && sl < NS; ++sl) {
-    const int e = m.cf[sl * ni + c];
-    if (e < 0) break;
-    ns = sl + 1;
-    const int f = e >> 1, side = e & 1, nb = m.cfn[sl * ni + c];
-    // q(fc2) - q(fc1) = +-dq: the weight's sign flipped on the integer pipe for side 1
-    const long long sb = (long long)side << 63;
-    const double wx = __longlong_as_double(__double_as_longlong(m.lsqw[(3 * side) * lf + f]) ^ sb);
-    const double wy = __longlong_as_double(__double_as_longlong(m.lsqw[(3 * side + 1) * lf + f]) ^ sb);
-    const double wz = __longlong_as_double(__double_as_longlong(m.lsqw[(3 * side + 2) * lf + f]) ^ sb);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      const double dq = prim[v * ld + nb] - qc[v];
-      sQ[sl * 5 + v][t] = dq;
-      gr[3 * v] = fma(dq, wx, gr[3 * v]);
-      gr[3 * v + 1] = fma(dq, wy, gr[3 * v + 1]);
-      gr[3 * v + 2] = fma(dq, wz, gr[3 * v + 2]);
-    }
+  for (int sl = 0; sl < NS; ++sl) {
+    es[sl] = sl < m.nslot ? m.cf[sl * ni + c] : -1;
+    nbs[sl] = es[sl] >= 0 ? m.cfn[sl * ni + c] : c;
+    ns += es[sl] >= 0 ? 1 : 0;
   }
 #pragma unroll
-  for (int k = 0; k < 15; ++k) s.grad[k * ld + c] = gr[k];
+  for (int sl = 0; sl < NS; ++sl) {
+    const int e = es[sl];
+    if (e < 0) continue;
+    const int f = e >> 1, side = e & 1, nb = nbs[sl];
+    if (grad) {
+      // q(fc2) - q(fc1) = +-dq: the weight's sign flipped on the integer pipe for side 1
+      const long long sb = (long long)side << 63;
+      const double wx = __longlong_as_double(__double_as_longlong(m.lsqw[(3 * side) * lf + f]) ^ sb);
+      const double wy = __longlong_as_double(__double_as_longlong(m.lsqw[(3 * side + 1) * lf + f]) ^ sb);
+      const double wz = __longlong_as_double(__double_as_longlong(m.lsqw[(3 * side + 2) * lf + f]) ^ sb);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const double dq = prim[v * ld + nb] - qc[v];
+        sQ[sl * 5 + v][t] = dq;
+        gr[3 * v] = fma(dq, wx, gr[3 * v]);
+        gr[3 * v + 1] = fma(dq, wy, gr[3 * v + 1]);
+        gr[3 * v + 2] = fma(dq, wz, gr[3 * v + 2]);
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) sQ[sl * 5 + v][t] = prim[v * ld + nb] - qc[v];
+    }
+  }
+  if (grad) {
+#pragma unroll
+    for (int k = 0; k < 15; ++k) s.grad[k * ld + c] = gr[k];
+  }
   const bool barth = o.postlim != TY_POSTLIM_NONE;
   double bn[3] = {1.0, 1.0, 1.0}, bd[3] = {klim, klim, klim};
   bool zero[3] = {false, false, false};
@@ -1140,7 +1166,24 @@ __global__ void __launch_bounds__(BLK, 512 / BLK) k_cell_fast(DevMesh m, DevStat
     double dq[5], D[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) dq[v] = sQ[sl * 5 + v][t];
-    delta_fast(m, o, f, side, gr, dq, D);
+    if (mt) {
+      // the row's NS coefficients loaded together (one memory latency per row, not per term)
+      const double* M = m.mtab + (size_t)sl * m.nslot * ni + c;
+      double mr[NS];
+#pragma unroll
+      for (int j = 0; j < NS; ++j) mr[j] = j < ns ? __ldg(M + (size_t)j * ni) : 0.0;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) D[v] = 0.0;
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        if (j < ns) {
+#pragma unroll
+          for (int v = 0; v < 5; ++v) D[v] = fma(mr[j], sQ[j * 5 + v][t], D[v]);
+        }
+      }
+    } else {
+      delta_fast(m, o, f, side, gr, dq, D);
+    }
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       const double den = D[v];
@@ -1173,6 +1216,111 @@ __global__ void __launch_bounds__(BLK, 512 / BLK) k_cell_fast(DevMesh m, DevStat
     for (int v = 0; v < 5; ++v) out[v * lf + f] = fma(r[v < 2 ? v : 2], sD[sl * 5 + v][t], qc[v]);
   }
 }
+
+// k_cell_fast for the case of DevMesh::mtab without a gradient output (MUSCL / MUSCL-UNS
+// without limiter, inviscid): the neighbour differences and the increments of the (at most
+// NS) faces stay in registers instead of shared memory, which the FP64 pipe no longer waits
+// for.  Same arithmetic as k_cell_fast.
+template <int NS, int BLK>
+__global__ void __launch_bounds__(BLK, 512 / BLK) k_cell_fast_mt(DevMesh m, DevState s, SpatOpts o, double klim) {
+  const int c = blockIdx.x * BLK + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t ld = m.ldc, lf = m.ldf, ni = m.nci;
+  const double* __restrict__ prim = s.prim;
+  int es[NS], nbs[NS];
+  int ns = 0;
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    es[sl] = sl < m.nslot ? m.cf[sl * ni + c] : -1;
+    nbs[sl] = es[sl] >= 0 ? m.cfn[sl * ni + c] : c;
+    ns += es[sl] >= 0 ? 1 : 0;
+  }
+  double qc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) qc[v] = prim[v * ld + c];
+  double dq[NS][5];
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl)
+#pragma unroll
+    for (int v = 0; v < 5; ++v) dq[sl][v] = prim[v * ld + nbs[sl]] - qc[v];  // 0 on an unused slot
+  const bool barth = o.postlim != TY_POSTLIM_NONE;
+  double bn[3] = {1.0, 1.0, 1.0}, bd[3] = {klim, klim, klim};
+  bool zero[3] = {false, false, false};
+  double D[NS][5];
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    const double* M = m.mtab + (size_t)sl * m.nslot * ni + c;
+    double mr[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) mr[j] = (sl < ns && j < ns) ? __ldg(M + (size_t)j * ni) : 0.0;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      double d = 0.0;
+#pragma unroll
+      for (int j = 0; j < NS; ++j) d = fma(mr[j], dq[j][v], d);
+      D[sl][v] = d;
+      if (barth && sl < ns) {
+        const int k = v < 2 ? v : 2;
+        const long long bden = dbits(d), bdq = dbits(dq[sl][v]);
+        if ((bden << 1) != 0) {                                   // d != 0
+          if ((bdq << 1) == 0 || ((bdq ^ bden) < 0)) {             // dq/d <= 0
+            zero[k] = true;
+          } else {
+            const double x = fabs(dq[sl][v]) * bd[k], y = bn[k] * fabs(d);
+            if (dbits(x) < dbits(y)) { bn[k] = fabs(dq[sl][v]); bd[k] = fabs(d); }
+          }
+        }
+      }
+    }
+  }
+  double r[3] = {1.0, 1.0, 1.0};
+  if (barth) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[k] = zero[k] ? 0.0 : fmin(1.0, klim * bn[k] * rcp_nr(bd[k]));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) s.ratio[k * ld + c] = r[k];
+  }
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    if (sl >= ns) continue;
+    const int e = es[sl], f = e >> 1, side = e & 1;
+    double* out = side ? s.cr : s.cl;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) out[v * lf + f] = fma(r[v < 2 ? v : 2], D[sl][v], qc[v]);
+  }
+}
+
+#if TY_FAST
+// DevMesh::mtab of every interior cell: M_ij = (+-A^-1 d_j) . w_i + k_i [i == j] over the
+// cell's gather-list faces i, j (w, k: the reconstruction weights recw of face i on the cell's
+// side; the least-squares weight's sign flipped for the fc2 side, as k_cell_fast does);
+// zero outside the cell's faces
+__global__ void k_build_mtab(DevMesh m, double* __restrict__ mt) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nci) return;
+  const size_t n = m.nci, lf = m.ldf;
+  const int ns = m.nslot;
+  for (int i = 0; i < ns; ++i) {
+    const int ei = m.cf[i * n + c];
+    for (int j = 0; j < ns; ++j) {
+      const int ej = m.cf[j * n + c];
+      double v = 0.0;
+      if (ei >= 0 && ej >= 0) {
+        const int fi = ei >> 1, si = ei & 1, fj = ej >> 1, sj = ej & 1;
+        const double sg = sj ? -1.0 : 1.0;
+        for (int k = 0; k < 3; ++k) v += sg * m.lsqw[(3 * sj + k) * lf + fj] * m.recw[(4 * si + k) * lf + fi];
+        if (i == j) v += m.recw[(4 * si + 3) * lf + fi];
+      }
+      mt[((size_t)i * ns + j) * n + c] = v;
+    }
+  }
+}
+
+cudaError_t build_mtab(const DevMesh& m, double* mtab, cudaStream_t st) {
+  k_build_mtab<<<(unsigned)((m.nci + kBlock - 1) / kBlock), kBlock, 0, st>>>(m, mtab);
+  return cudaGetLastError();
+}
+#endif
 
 // face fluxes from the limited states of k_cell_fast
 __global__ void __launch_bounds__(kBlock) k_face_flux_fast(DevMesh m, DevState s, SpatOpts o) {
@@ -1399,13 +1547,19 @@ cudaError_t residual_faces(const DevMesh& m, const DevState& s, const SpatOpts& 
     pr->launch(K_GHOST_PRIM, st, [&] { k_ghost_prim<<<nblk(m.ng), kBlock, 0, st>>>(m, s.prim, o); });
   if (kFast && o.highres != TY_HRES_NONE) {
     const double klim = o.postlim == TY_POSTLIM_SUPERBARTH ? 1.0 : 0.5;
-    if (m.nslot <= 4)
+    if (m.nslot <= 4 && m.mtab && o.viscous == TY_VISC_NONE)
       pr->launch(K_CELL_FAST, st, [&] {
-        k_cell_fast<4, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim);
+        k_cell_fast_mt<4, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim);
+      });
+    else if (m.nslot <= 4)
+      pr->launch(K_CELL_FAST, st, [&] {
+        k_cell_fast<4, 128><<<(unsigned)((m.nci + 127) / 128), 128, 0, st>>>(m, s, o, klim,
+                                                                              o.viscous != TY_VISC_NONE);
       });
     else
       pr->launch(K_CELL_FAST, st, [&] {
-        k_cell_fast<8, 64><<<(unsigned)((m.nci + 63) / 64), 64, 0, st>>>(m, s, o, klim);
+        k_cell_fast<8, 64><<<(unsigned)((m.nci + 63) / 64), 64, 0, st>>>(m, s, o, klim,
+                                                                           o.viscous != TY_VISC_NONE);
       });
     if (o.viscous != TY_VISC_NONE && m.ng > 0)
       pr->launch(K_GHOST_GRAD, st, [&] { k_ghost_grad<<<nblk(m.ng), kBlock, 0, st>>>(m, s.grad); });
