@@ -183,7 +183,7 @@ def fp64_peak():
     return None
 
 
-def kernel_bytes(md, nslot_avg):
+def kernel_bytes(md, nslot_avg, mtab=False):
     """Compulsory (algorithmic) DRAM bytes per launch of each kernel: every array element
     the kernel needs is counted once (cells and faces of the whole mesh).  FP64 = 8 B,
     index = 4 B.  nci interior cells, nf faces, ng ghost cells, f = faces per cell."""
@@ -203,8 +203,11 @@ def kernel_bytes(md, nslot_avg):
         "timestep": nci * (8 + 8 + 40),
         "prim": nci * 80,
         # fused fast-mode kernels
-        "cell_fast": 8 * nslot_avg * nci + nf * (48 + 64 + 80) + nc * 40 + nci * (120 + 24),  # lists, A^-1 d,
-        # reconstruction weights, write cl/cr; prim; write grad + ratio
+        # lists, A^-1 d, reconstruction weights, write cl/cr; prim; write grad + ratio; or, with the
+        # per-cell increment matrices (MUSCL/-UNS without limiter), lists, the matrix (nslot^2 per
+        # cell), write cl/cr; prim; write ratio
+        "cell_fast": (8 * nslot_avg * nci + 8 * nslot_avg ** 2 * nci + nf * 80 + nc * 40 + nci * 24) if mtab else
+                     (8 * nslot_avg * nci + nf * (48 + 64 + 80) + nc * 40 + nci * (120 + 24)),
         "face_flux_fast": nf * (80 + 8 + 24 + 8 + 40),     # cl/cr, bc/partner, normal, surface, write flux
     }
 
@@ -274,7 +277,9 @@ def run_ours(args, rank, world, local):
     value = nci * args.steps * world / (ms * 1e-3)
     # per-kernel roofline
     peak, peak_kind = measured_peaks()
-    kb = kernel_bytes(md, nslot_avg)
+    mtab = (args.mode == "fast" and w["highres"] in ("MUSCL", "MUSCL-UNS") and w["limiter"] == "NONE"
+            and info["max_faces_per_cell"] <= 4)
+    kb = kernel_bytes(md, nslot_avg, mtab)
     per = {}
     for i, name in enumerate(_capi.KERNEL_NAMES):
         if kl[i] > 0:
@@ -286,7 +291,8 @@ def run_ours(args, rank, world, local):
     ach = per[dom]["achieved_gbs"]
     # DRAM traffic and FP64 instructions per unit, from one ncu capture of the same kernels on
     # the 40^3x5 mesh (320,000 cells, 649,600 faces), scaled by the units of this mesh
-    per_unit = {"cell_fast": (nci, (96.07e6 + 53.98e6) / 320000, 261),
+    per_unit = {"cell_fast": (nci, (65.42e6 + 11.33e6) / 320000, 198) if mtab else
+                (nci, (96.07e6 + 53.98e6) / 320000, 261),
                 "face_flux_fast": (md.nface, (72.21e6 + 4.60e6) / 649600, 127)}
     traffic = None
     fp64_roof = None
