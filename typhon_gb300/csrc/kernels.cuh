@@ -705,12 +705,14 @@ __device__ void flux_roe(double g, double eps, const double* L, const double* R,
 __device__ void flux_roe_fast(const SpatOpts& o, const double* L, const double* R, double nx, double ny, double nz,
                               double S, double* F) {
   const double g1 = o.gamma - 1.0, eps = o.entropy_fix, ieps = o.inv_entropy_fix, gig1 = o.gig1;
-  const double rL = rsqrt_nr(L[0]), rR = rsqrt_nr(R[0]);
-  const double sL = L[0] * rL, sR = R[0] * rR;   // sqrt(rho)
-  const double iL = rL * rL, iR = rR * rR;       // 1/rho
-  const double inv = rcp_nr(sL + sR);
-  const double kl = sL * inv, kr = sR * inv;
-  const double rroe = sL * sR;
+  // Roe weights from one reciprocal square root: with y = 1/sqrt(rho_L rho_R),
+  // rroe = sqrt(rho_L rho_R) = rho_L rho_R y, kl = sqrt(rho_L) / (sqrt(rho_L) + sqrt(rho_R)) =
+  // rho_L / (rho_L + rroe), kr = rroe / (rho_L + rroe), 1/rho_L = y^2 rho_R, 1/rho_R = y^2 rho_L
+  const double P = L[0] * R[0], y = rsqrt_nr(P), y2 = y * y;
+  const double rroe = P * y;
+  const double inv = rcp_nr(L[0] + rroe);
+  const double kl = L[0] * inv, kr = rroe * inv;
+  const double iL = y2 * R[0], iR = y2 * L[0];
   const double ux = kl * L[2] + kr * R[2], uy = kl * L[3] + kr * R[3], uz = kl * L[4] + kr * R[4];
   const double sqL = L[2] * L[2] + L[3] * L[3] + L[4] * L[4];
   const double sqR = R[2] * R[2] + R[3] * R[3] + R[4] * R[4];
@@ -751,17 +753,18 @@ __device__ void flux_roe_fast(const SpatOpts& o, const double* L, const double* 
   F[0] = hs * (ml + mr - d_mass);
 }
 
-// HLLC (calc_flux_hllc.f90 with beta = 1) with shared reciprocals: no division; 3
-// reciprocals, 3 square roots and 2 reciprocal square roots by Newton-Raphson iterations
-// (fastmath.cuh) per face.
+// HLLC (calc_flux_hllc.f90 with beta = 1) with shared reciprocals: no division; the
+// reciprocals, square roots and reciprocal square roots by Newton-Raphson iterations
+// (fastmath.cuh), the Roe weights and both 1/rho from one reciprocal square root.
 __device__ void flux_hllc_fast(const SpatOpts& o, const double* L, const double* R, double nx, double ny, double nz,
                                double* F) {
   const double g = o.gamma, ig1 = o.ig1, gig1 = o.gig1;
-  const double rL = rsqrt_nr(L[0]), rR = rsqrt_nr(R[0]);
-  const double sL = L[0] * rL, sR = R[0] * rR;
-  const double iL = rL * rL, iR = rR * rR;
-  const double inv = rcp_nr(sL + sR);
-  const double kl = sL * inv, kr = sR * inv;
+  // Roe weights from one reciprocal square root (as flux_roe_fast)
+  const double P = L[0] * R[0], y = rsqrt_nr(P), y2 = y * y;
+  const double rroe = P * y;
+  const double inv = rcp_nr(L[0] + rroe);
+  const double kl = L[0] * inv, kr = rroe * inv;
+  const double iL = y2 * R[0], iR = y2 * L[0];
   const double rux = kl * L[2] + kr * R[2], ruy = kl * L[3] + kr * R[3], ruz = kl * L[4] + kr * R[4];
   const double sqL = L[2] * L[2] + L[3] * L[3] + L[4] * L[4];
   const double sqR = R[2] * R[2] + R[3] * R[3] + R[4] * R[4];
