@@ -47,7 +47,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="tgv3d", choices=["tgv3d", "vortex2d", "ffbox3d-implicit", "kdif3d", "adjoint3d"])
+    ap.add_argument("--workload", default="tgv3d", choices=["tgv3d", "vortex2d", "ffbox3d-implicit", "kdif3d", "adjoint3d",
+                                                             "flatplate-implicit"])
+    ap.add_argument("--fp-nx", type=int, default=None, help="flatplate-implicit: streamwise quads (default 200)")
+    ap.add_argument("--fp-nz", type=int, default=None, help="flatplate-implicit: spanwise quads (default 20)")
+    ap.add_argument("--imp-time-limit", type=float, default=900.0,
+                    help="flatplate-implicit: seconds per solver before the run stops short of the target")
     ap.add_argument("--n", type=int, default=None, help="cells per direction (default: the workload's)")
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
     ap.add_argument("--e2e-steps", type=int, default=None)
@@ -512,6 +517,87 @@ def run_implicit(args):
     print(json.dumps(out))
 
 
+def run_flatplate(args):
+    """Config 3, the laminar flat plate (cases.FLATPLATE): steady implicit solve toward a 1e-10
+    relative residual with FP64 flexible GMRES and the mixed form with an FP64 Krylov basis
+    (FP32 BDLU mat-vec and block Jacobi), each stopped at the target or after
+    --imp-time-limit seconds.  Reports the time each solver takes to reach every residual
+    decade both reach, and the residual each reached."""
+    import torch
+    import typhon_gb300 as ty
+    from typhon_gb300 import build, cases
+    build.build()
+    torch.cuda.set_device(0)
+    w = cases.FLATPLATE
+    t0 = time.time()
+    md = cases.make_flatplate(args.fp_nx, args.fp_nz)
+    t_mesh = time.time() - t0
+    nci = md.ncell_int
+    ff = w["freestream"]
+    scale = np.array([ff[0], ff[1] / 0.4, ff[0] * ff[2], ff[0] * ff[2], ff[0] * ff[2]])
+    variants, states = {}, {}
+    with ClockSampler(0) as clk:
+        for name, prec in (("fgmres_fp64", "fp64"), ("fgmres_mixed", "mixed-fp64ortho")):
+            g = ty.Grid(md)
+            g.set_spat(w["scheme"], "NONE", "NONE", mode="fast", dissipative_flux="CELL-AVERAGE",
+                       viscosity="SUTHERLAND", rgas=w["rgas"], prandtl=w["prandtl"], farfield=ff)
+            prim0 = np.tile(np.array(ff)[:, None], (1, md.ncell))
+            g.set_prim(prim0)
+            kw = dict(nkrylov=w["nkrylov"], max_it=w["max_it"], inv_res=w["inv_res"], local_dt=True, precision=prec)
+            g.implicit_step(1e-3, "FGMRES", **kw)   # allocates the workspace
+            g.set_prim(prim0)
+            g.synchronize()
+            cfl, rmax, steps, matvecs, rel = w["cfl0"], None, 0, 0, 1.0
+            decades = {}
+            t0 = time.perf_counter()
+            while steps < w["max_steps"]:
+                st = g.implicit_step(cfl, "FGMRES", **kw)
+                steps += 1
+                matvecs += st["matvecs"]
+                r = np.asarray(st["res_l2"]) / scale
+                rmax = r if rmax is None else np.maximum(rmax, r)
+                rel = float(np.sqrt(np.sum((r / rmax) ** 2) / 5))
+                if not np.isfinite(rel):
+                    break
+                k = int(np.floor(-np.log10(max(rel, 1e-300))))
+                for dlev in range(1, k + 1):
+                    decades.setdefault(dlev, (round(time.perf_counter() - t0, 3), steps))
+                if rel < w["target"] or time.perf_counter() - t0 > args.imp_time_limit:
+                    break
+                cfl = min(cfl * 1.5, w["cfl_max"])
+            g.synchronize()
+            states[name] = g.get_cons()
+            variants[name] = {"seconds": round(time.perf_counter() - t0, 3), "steps": steps, "matvecs": matvecs,
+                              "final_rel_residual": rel, "reached": bool(rel < w["target"]),
+                              "decades": {f"1e-{k}": v for k, v in sorted(decades.items())}}
+            g.close()
+    d = states["fgmres_mixed"] - states["fgmres_fp64"]
+    ref = states["fgmres_fp64"]
+    common = sorted(set(variants["fgmres_fp64"]["decades"]) & set(variants["fgmres_mixed"]["decades"]),
+                    key=lambda s: int(s.split("-")[1]))
+    deepest = common[-1] if common else None
+    out = {"metric": "seconds to each residual decade, mixed implicit (FP32 Jv and block Jacobi, FP64 Krylov basis, "
+                     "residual and update) vs FP64, laminar flat plate", "unit": "s",
+           "value": variants["fgmres_mixed"]["decades"][deepest][0] if deepest else None,
+           "higher_is_better": False, "n_gpus": 1, "dtype": "f64+f32", "data": "synthetic", "scaling": "weak",
+           "vs_baseline": None,
+           "config": {"workload": f"flat plate {nci} cells (prisms + tets), M 0.3, Re_L 1e4, Rusanov first order, "
+                                  "cell-average viscous flux, Sutherland, adiabatic no-slip wall, far field",
+                      "cells": nci, "cfl": f"{w['cfl0']} -> {w['cfl_max']} (x1.5 per step)",
+                      "krylov": f"row-scaled FGMRES({w['nkrylov']}) x {w['max_it']}, block Jacobi, INV_RES {w['inv_res']}",
+                      "time_limit_s": args.imp_time_limit, "mesh_build_s": round(t_mesh, 2)},
+           "deepest_common_decade": deepest,
+           "speedup_mixed_vs_fp64_at_deepest": (round(variants["fgmres_fp64"]["decades"][deepest][0] /
+                                                      variants["fgmres_mixed"]["decades"][deepest][0], 3)
+                                                if deepest else None),
+           "variants": variants,
+           "state_mixed_vs_fp64": [float(np.linalg.norm(d[0]) / np.linalg.norm(ref[0])),
+                                   float(np.linalg.norm(d[1]) / np.linalg.norm(ref[1])),
+                                   float(np.linalg.norm(d[2:5]) / np.linalg.norm(ref[2:5]))],
+           "clocks": clk.summary()}
+    print(json.dumps(out))
+
+
 def run_kdif(args):
     """Heat conduction: 50 backward-Euler steps of the KDIF config to a 1e-12 relative
     residual per step with FP64 conjugate gradients + Jacobi (fused single-reduction
@@ -846,6 +932,12 @@ def main():
             run_kdif(args)
         elif rank == 0:
             print(json.dumps({"impl": "reference", "unavailable": "the KDIF comparison has no CPU arm"}))
+        return
+    if args.workload == "flatplate-implicit":
+        if rank == 0 and args.impl == "ours":
+            run_flatplate(args)
+        elif rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the implicit comparison has no CPU arm"}))
         return
     if args.workload == "ffbox3d-implicit":
         if rank == 0 and args.impl == "ours":

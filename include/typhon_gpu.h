@@ -292,6 +292,13 @@ typedef enum {
                             measured Gram matrix), the residuals, the Hessenberg algebra and the
                             update in FP64 */
 } ty_precision;
+typedef enum ty_imp_scaling {
+  TY_IMP_SCALE_STATE = 0,  /* equation v divided by the state's RMS magnitude s_v (rho, rhoE,
+                              and sqrt(s_rho s_rhoE) for momentum): the Krylov solve minimises
+                              the residual in units of the state, not the energy equation's
+                              alone (default) */
+  TY_IMP_SCALE_NONE = 1    /* the assembled rows as they are */
+} ty_imp_scaling;
 typedef struct ty_imp_params {
   int32_t krylov;        /* ty_krylov (INVERSION = GMRES is TY_KRYLOV_GMRES) */
   int32_t precision;     /* ty_precision */
@@ -299,9 +306,9 @@ typedef struct ty_imp_params {
   int32_t max_it;        /* IMP_MAX_IT: GMRES stops after 2*max_it+1 cycles (Typhon), the
                             others after max_it cycles */
   int32_t local_dt;      /* DTCALC: 1 = LOCAL_STABILITY_CONDITION, 0 = STABILITY_CONDITION */
-  int32_t reserved;
+  int32_t scaling;       /* ty_imp_scaling of the FGMRES/JFNK system (GMRES: ignored) */
   double inv_res;        /* INV_RES: GMRES uses Typhon's test |r|/|b| < INV_RES |x0|_1; the
-                            others |r|/|b| <= INV_RES */
+                            others |S r|/|S b| <= INV_RES, S their row scale */
   double cfl;            /* stability number of this step (the caller ramps it) */
 } ty_imp_params;
 typedef struct ty_imp_stats {
@@ -312,7 +319,8 @@ typedef struct ty_imp_stats {
   double dt_min;         /* smallest cell time step of the step */
   double res_l2[5];      /* L2 norm over cells of -sum(F S)/V per variable, before the update */
   double du_l1[5];       /* L1 norm of the update per variable (update_field.f90:54-60) */
-  double lin_res;        /* final relative linear residual |b - A x| / |b| */
+  double lin_res;        /* final relative linear residual |S (b - A x)| / |S b| (S = I unless
+                            the FGMRES/JFNK system is scaled) */
   double du_mom;         /* sum over cells of the Euclidean norm of the momentum update (the
                             vector part of Typhon's steady residual, update_field.f90:54-60) */
 } ty_imp_stats;

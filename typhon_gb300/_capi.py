@@ -51,7 +51,7 @@ _lib = None
 class ImpParams(C.Structure):
     """ty_imp_params"""
     _fields_ = [("krylov", C.c_int32), ("precision", C.c_int32), ("nkrylov", C.c_int32), ("max_it", C.c_int32),
-                ("local_dt", C.c_int32), ("reserved", C.c_int32), ("inv_res", C.c_double), ("cfl", C.c_double)]
+                ("local_dt", C.c_int32), ("scaling", C.c_int32), ("inv_res", C.c_double), ("cfl", C.c_double)]
 
 
 class ImpStats(C.Structure):

@@ -66,6 +66,32 @@ FFBOX = dict(dim=3, n=48, length=2 * np.pi, jitter=0.05, seed=1234, scheme="RUSA
              cfl0=10.0, cfl_max=25.0, nkrylov=30, max_it=2, inv_res=1e-2, target=1e-10, max_steps=1500)
 
 
+# config 3: laminar flat plate, M = 0.3, Re_L = 1e4 on the plate's unit length, air at 288 K
+# (Sutherland), adiabatic no-slip wall, far field at the inlet, outlet and top, symmetry
+# upstream of the plate and on the span sides; 2 nx nz 50 prisms + 6 nx nz 25 tetrahedra
+# (nx = 200, nz = 20: 400,000 + 600,000 cells).  First-order Rusanov with its own Jacobian
+# and the cell-average viscous flux (Typhon's scalar viscous Jacobian); backward Euler with
+# local time steps, CFL 10 ramped by 1.5 per step to cfl_max, row-scaled FGMRES(30) x max_it
+# to INV_RES.  Above CFL ~100 the Krylov solve fails with any local preconditioner (block or
+# line Jacobi, incomplete LU) and the scalar viscous Jacobian stalls Newton even with exact
+# solves.
+_T_FP = 288.0
+_A_FP = float(np.sqrt(1.4 * 287.14 * _T_FP))
+_MU_FP = 1.68e-5 * (_T_FP / 273.0) ** 1.5 * (273.0 + 110.5) / (_T_FP + 110.5)
+_RHO_FP = 1e4 * _MU_FP / (0.3 * _A_FP)
+FLATPLATE = dict(nx=200, nz=20, scheme="RUSANOV", rgas=287.14, prandtl=0.72,
+                 freestream=(_RHO_FP, _RHO_FP * 287.14 * _T_FP, 0.3 * _A_FP, 0.0, 0.0),
+                 cfl0=10.0, cfl_max=100.0, nkrylov=30, max_it=5, inv_res=0.05, target=1e-10, max_steps=20000)
+
+
+def make_flatplate(nx=None, nz=None):
+    """Preprocessed flat-plate mesh of FLATPLATE (native preprocessing)."""
+    w = FLATPLATE
+    nx, nz = nx or w["nx"], nz or w["nz"]
+    raw = umesh.gen_flatplate(nx=nx, nz=nz, width=0.01 * nz)
+    return umesh.preprocess(raw, 3, umesh.flatplate_bcs())
+
+
 def make_ffbox(n=None):
     """Preprocessed far-field tetrahedral box of FFBOX (native preprocessing)."""
     w = FFBOX

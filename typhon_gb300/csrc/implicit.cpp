@@ -136,12 +136,21 @@ int ensure_buffers(ty_mesh* h, const ty_imp_params* p) {
     if (((!need32 && !gm) || im.Z) && (rc = grow(h, im.Z, (size_t)cap * n))) return rc;
     im.nk = cap;
   }
+  if ((p->krylov == TY_KRYLOV_FGMRES || p->krylov == TY_KRYLOV_JFNK) && !im.bs && (rc = h->alloc(im.bs, n)))
+    return rc;
   if (p->krylov == TY_KRYLOV_JFNK && !im.jfnk) {
     if ((rc = h->alloc(im.upert, 5 * (size_t)m.ldc)) || (rc = h->alloc(im.r0, n))) return rc;
     IMP_CU(cudaMemset(im.upert, 0, 5 * (size_t)m.ldc * sizeof(double)));
     im.jfnk = true;
   }
   return TY_OK;
+}
+
+constexpr Row5 kOnes{{1.0, 1.0, 1.0, 1.0, 1.0}};
+Row5 row_scale(const ImpState& im) {
+  Row5 r;
+  for (int v = 0; v < 5; ++v) r.v[v] = im.rs[v];
+  return r;
 }
 
 // copy k device scalars from scal[off..] to the pinned buffer and wait
@@ -319,7 +328,7 @@ int Operator::apply(const double* z, const float* z32, double* w, int* matvecs) 
   IMP_CU(MODE_CALL(h, prim_from, h->m, h->s, h->o, im.upert, s, &h->prof));
   if (int rc = stage_faces(h)) return rc;
   IMP_CU(IMP_CALL(h, imp_rhs, m, h->s, im, a, im.r, s));
-  IMP_CU(IMP_CALL(h, imp_fd_combine, z, nullptr, im.r, im.r0, 1.0 / eps, w, n, s));
+  IMP_CU(IMP_CALL(h, imp_fd_combine, z, nullptr, im.r, im.r0, 1.0 / eps, row_scale(im), w, n, s));
   return TY_OK;
 }
 
@@ -383,7 +392,8 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
     a[jc + 1] = -sn[jc] * a[jc];
   };
   IMP_CU(cudaMemsetAsync(im.x, 0, n * sizeof(double), s));
-  IMP_CU(IMP_CALL(h, imp_dot, im.b, im.b, n, im.part, im.scal + kScalMisc, s));
+  IMP_CU(IMP_CALL(h, imp_fd_combine, im.b, nullptr, nullptr, nullptr, 0.0, row_scale(im), im.bs, n, s));
+  IMP_CU(IMP_CALL(h, imp_dot, im.bs, im.bs, n, im.part, im.scal + kScalMisc, s));
   if (int rc = fetch(h, kScalMisc, 1)) return rc;
   const double beta0 = std::sqrt(P[kScalMisc]);
   const char* tv = std::getenv("TY_IMPLICIT_TRACE");  // Arnoldi history on stderr when set to 1
@@ -394,13 +404,13 @@ int fgmres(ty_mesh* h, Operator& op, const ty_imp_params* p, ty_imp_stats* st) {
     const double tol = p->inv_res * beta0;
     for (cycles = 0; cycles < std::max(p->max_it, 1); ++cycles) {
       double beta;
-      const double* src = im.b;
+      const double* src = im.bs;
       if (cycles == 0) {
         beta = beta0;
       } else {  // r = b - A x
         if (z32) IMP_CU(IMP_CALL(h, imp_to_f32, im.x, Z32(0), n, s));
         if (int rc = op.apply(im.x, Z32(0), im.w, &matvecs)) return rc;
-        IMP_CU(IMP_CALL(h, imp_fd_combine, im.b, nullptr, im.w, nullptr, 1.0, im.r, n, s));
+        IMP_CU(IMP_CALL(h, imp_fd_combine, im.bs, nullptr, im.w, nullptr, 1.0, kOnes, im.r, n, s));
         IMP_CU(IMP_CALL(h, imp_dot, im.r, im.r, n, im.part, im.scal + kScalMisc, s));
         if (int rc = fetch(h, kScalMisc, 1)) return rc;
         beta = std::sqrt(P[kScalMisc]);
@@ -492,7 +502,8 @@ int ty_implicit_step(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
       p->precision > TY_PREC_MIXED_FP64ORTHO || p->nkrylov < 1 || p->max_it < 0 || !(p->inv_res > 0.0) || !(p->cfl > 0.0) ||
       ((p->krylov == TY_KRYLOV_GMRES || p->krylov == TY_KRYLOV_BICGSTAB) && p->nkrylov > kMaxKrylov) ||
       ((p->krylov == TY_KRYLOV_FGMRES || p->krylov == TY_KRYLOV_JFNK) && p->nkrylov > kMaxCgs) ||
-      (p->krylov != TY_KRYLOV_FGMRES && p->precision != TY_PREC_FP64)) {
+      (p->krylov != TY_KRYLOV_FGMRES && p->precision != TY_PREC_FP64) ||
+      (p->scaling != TY_IMP_SCALE_STATE && p->scaling != TY_IMP_SCALE_NONE)) {
     tyi::set_error("ty_imp_params: option out of range (GMRES: nkrylov <= 64, FP64; FGMRES/JFNK: nkrylov <= 32)");
     return TY_ERR_ARG;
   }
@@ -534,7 +545,25 @@ int ty_implicit_step(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
   im.last_local = a.local_dt;
   im.last_dt = st->dt_min;
   for (int v = 0; v < 5; ++v) st->res_l2[v] = std::sqrt(im.pinned[kScalMisc + 2 + v]);
-  // 3. solve
+  // 3. solve.  The flexible GMRES scales equation v of its system by 1 / s_v, s from the
+  // state's RMS magnitudes: s_rho, s_rhoE and sqrt(s_rho s_rhoE) for the three momentum
+  // components (a momentum density, the same for all three so that the scale is invariant to
+  // rotations).  Unscaled, the 2-norm of a low-Mach residual is the energy equation's alone.
+  for (int v = 0; v < 5; ++v) im.rs[v] = im.rsi[v] = 1.0;
+  if ((p->krylov == TY_KRYLOV_FGMRES || p->krylov == TY_KRYLOV_JFNK) && p->scaling == TY_IMP_SCALE_STATE) {
+    IMP_CU(IMP_CALL(h, imp_dot, S.u0, S.u0, (size_t)m.nci, im.part, im.scal + kScalMisc, s));
+    IMP_CU(IMP_CALL(h, imp_dot, S.u0 + m.ldc, S.u0 + m.ldc, (size_t)m.nci, im.part, im.scal + kScalMisc + 1, s));
+    if ((rc = fetch(h, kScalMisc, 2))) return rc;
+    const double sr = std::sqrt(im.pinned[kScalMisc] / m.nci), se = std::sqrt(im.pinned[kScalMisc + 1] / m.nci);
+    const double sm = std::sqrt(sr * se);
+    if (sr > 0.0 && se > 0.0 && std::isfinite(sr) && std::isfinite(se)) {
+      const double sv[5] = {sr, se, sm, sm, sm};
+      for (int v = 0; v < 5; ++v) {
+        im.rsi[v] = sv[v];
+        im.rs[v] = 1.0 / sv[v];
+      }
+    }
+  }
   if (p->krylov == TY_KRYLOV_GMRES) {
     rc = gmres_typhon(h, p, st);
   } else if (p->krylov == TY_KRYLOV_BICGSTAB) {
@@ -550,6 +579,7 @@ int ty_implicit_step(ty_mesh* h, const ty_imp_params* p, ty_imp_stats* st) {
     }
     rc = fgmres(h, op, p, st);
   }
+  for (int v = 0; v < 5; ++v) im.rs[v] = im.rsi[v] = 1.0;
   if (rc) return rc;
   // 4. update U += dU
   IMP_CU(IMP_CALL(h, imp_update_state, m, S, im.x, im.part, im.scal + kScalMisc + 10, s));

@@ -511,11 +511,16 @@ __global__ void __launch_bounds__(128) k_imp_matvec(DevMesh m, ImpState im, cons
       for (int v = 0; v < 5; ++v) yv[v] = yv[v] + t[v];
     }
   }
+  if (z) {
 #pragma unroll
-  for (int v = 0; v < 5; ++v) y[5 * (size_t)c + v] = yv[v];
+    for (int v = 0; v < 5; ++v) y[5 * (size_t)c + v] = yv[v];
+  } else {  // S A x (the row scale is all ones outside the flexible GMRES)
+#pragma unroll
+    for (int v = 0; v < 5; ++v) y[5 * (size_t)c + v] = yv[v] * im.rs[v];
+  }
 }
 
-// y = A z with FP32 blocks and FP32 z, FP32 accumulation, FP64 result
+// y = S A z with FP32 blocks and FP32 z, FP32 accumulation, FP64 result
 __global__ void __launch_bounds__(128) k_imp_matvec32(DevMesh m, ImpState im, const float* __restrict__ z,
                                                        double* __restrict__ y) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -549,13 +554,11 @@ __global__ void __launch_bounds__(128) k_imp_matvec32(DevMesh m, ImpState im, co
     }
   }
 #pragma unroll
-  for (int v = 0; v < 5; ++v) y[5 * (size_t)c + v] = (double)yv[v];
+  for (int v = 0; v < 5; ++v) y[5 * (size_t)c + v] = (double)yv[v] * im.rs[v];
 }
 
-// v = w * hinv[0] (when w is given), then the block-Jacobi preconditioned z = D^-1 v
-// (FP64 into z, or FP32 into z32)
-// z = D^-1 v, the block-Jacobi preconditioner of the flexible GMRES: FP64 (v, dinv, z) or
-// FP32 (v32, dinv32, z32)
+// z = D^-1 S^-1 v, the block-Jacobi preconditioner of the flexible GMRES on its row-scaled
+// system (S D)^-1: FP64 (v, dinv, z) or FP32 (v or v32, dinv32, z32)
 __global__ void __launch_bounds__(128) k_imp_precond(DevMesh m, ImpState im, const double* __restrict__ v,
                                                       const float* __restrict__ v32, double* __restrict__ z,
                                                       float* __restrict__ z32) {
@@ -564,7 +567,7 @@ __global__ void __launch_bounds__(128) k_imp_precond(DevMesh m, ImpState im, con
   if (z) {
     double A[25], vv[5], t[5];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) vv[k] = v[5 * (size_t)c + k];
+    for (int k = 0; k < 5; ++k) vv[k] = v[5 * (size_t)c + k] * im.rsi[k];
     load_block(im.dinv + (size_t)c * kBlk, A);
     mv5(A, vv, t);
 #pragma unroll
@@ -573,7 +576,8 @@ __global__ void __launch_bounds__(128) k_imp_precond(DevMesh m, ImpState im, con
     float A[28], vf[5];
     load_block32(im.dinv32 + (size_t)c * kBlk32, A);
 #pragma unroll
-    for (int k = 0; k < 5; ++k) vf[k] = v32 ? v32[5 * (size_t)c + k] : (float)v[5 * (size_t)c + k];
+    for (int k = 0; k < 5; ++k)
+      vf[k] = v32 ? v32[5 * (size_t)c + k] * (float)im.rsi[k] : (float)(v[5 * (size_t)c + k] * im.rsi[k]);
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
       float s = 0.f;
@@ -944,11 +948,13 @@ __global__ void k_imp_perturb(DevMesh m, const double* __restrict__ u0, const do
 #pragma unroll
   for (int v = 0; v < 5; ++v) up[v * (size_t)m.ldc + c] = u0[v * (size_t)m.ldc + c] + eps * z[5 * (size_t)c + v];
 }
+// w = rs (z - (rp - r0) inv_eps) per packed entry (rs of its variable i mod 5); rp null: w = rs z
 __global__ void k_imp_fd(const double* __restrict__ z, const float* __restrict__ z32, const double* __restrict__ rp,
-                         const double* __restrict__ r0, double inv_eps, double* __restrict__ w, size_t n) {
+                         const double* __restrict__ r0, double inv_eps, Row5 rs, double* __restrict__ w, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const double zi = z ? z[i] : (double)z32[i];
-    w[i] = zi - (rp[i] - (r0 ? r0[i] : 0.0)) * inv_eps;
+    const double d = rp ? zi - (rp[i] - (r0 ? r0[i] : 0.0)) * inv_eps : zi;
+    w[i] = d * rs.v[i % 5];
   }
 }
 
@@ -1140,8 +1146,8 @@ cudaError_t imp_perturb(const DevMesh& m, const double* u0, const double* z, dou
 }
 
 cudaError_t imp_fd_combine(const double* z, const float* z32, const double* rp, const double* r0, double inv_eps,
-                           double* w, size_t n, cudaStream_t st) {
-  k_imp_fd<<<std::min<size_t>(grid_of(n, 256), 4 * kRedBlocks), 256, 0, st>>>(z, z32, rp, r0, inv_eps, w, n);
+                           Row5 rs, double* w, size_t n, cudaStream_t st) {
+  k_imp_fd<<<std::min<size_t>(grid_of(n, 256), 4 * kRedBlocks), 256, 0, st>>>(z, z32, rp, r0, inv_eps, rs, w, n);
   return cudaGetLastError();
 }
 

@@ -57,9 +57,20 @@ struct ImpState {
   unsigned* done = nullptr;   // [1] blocks finished in a one-launch reduction (zero between launches)
   double* upert = nullptr;    // [5][ldc] perturbed state (Jacobian-free products)
   double* r0 = nullptr;       // [5 nci] residual at the unperturbed state (Jacobian-free)
+  double* bs = nullptr;       // [5 nci] right-hand side of the flexible GMRES with its rows scaled
+  // Row scale S of the flexible GMRES system (equation v of every cell times rs[v]); the
+  // mat-vec kernels return S A z, the preconditioner applies D^-1 S^-1, so the Krylov solve
+  // minimises |S (b - A x)| over physical updates x.  Ones (exact no-ops) outside that solve.
+  double rs[5] = {1.0, 1.0, 1.0, 1.0, 1.0};
+  double rsi[5] = {1.0, 1.0, 1.0, 1.0, 1.0};  // 1 / rs
   double* pinned = nullptr;   // host mirror of scal (pinned)
   int last_local = 1;         // time step of the last step: per cell, or last_dt everywhere
   double last_dt = 0.0;
+};
+
+// Five per-variable factors passed by value to the flat vector kernels.
+struct Row5 {
+  double v[5];
 };
 
 // Arguments of the assembly kernels.
@@ -106,7 +117,7 @@ struct ImpArgs {
   cudaError_t imp_perturb(const DevMesh& m, const double* u0, const double* z, double eps, double* up,   \
                           cudaStream_t st);                                                             \
   cudaError_t imp_fd_combine(const double* z, const float* z32, const double* rp, const double* r0,      \
-                             double inv_eps, double* w, size_t n, cudaStream_t st);                      \
+                             double inv_eps, Row5 rs, double* w, size_t n, cudaStream_t st);             \
   cudaError_t imp_to_f32(const double* x, float* y, size_t n, cudaStream_t st);                          \
   cudaError_t imp_res_norms(const DevMesh& m, const ImpState& im, const ImpArgs& a, const double* b,     \
                             double* part, double* out, cudaStream_t st);                                 \

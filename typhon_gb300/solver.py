@@ -224,13 +224,14 @@ class Grid:
 
     # -- implicit step (calc_rhs.f90:121-138 with the Jacobians, implicit_solve, update_field) --
     def implicit_step(self, cfl, inversion="GMRES", nkrylov=50, max_it=50, inv_res=1e-4, local_dt=False,
-                      precision="fp64"):
+                      precision="fp64", scaling="state"):
         """One backward-Euler step on the resident state.  inversion: GMRES (Typhon's
         bdlu_gmres), FGMRES (block Jacobi, measured Gram matrix) or JFNK; precision fp64 | mixed-fp64ortho
-        (FGMRES: FP32 matrix, mat-vec and block Jacobi, FP64 basis) | mixed (FGMRES: FP32 basis too).
-        Returns the ty_imp_stats fields as a dict."""
-        p = _capi.ImpParams(KRYLOV[inversion], PRECISION[precision], int(nkrylov), int(max_it), int(local_dt), 0,
-                            float(inv_res), float(cfl))
+        (FGMRES: FP32 matrix, mat-vec and block Jacobi, FP64 basis) | mixed (FGMRES: FP32 basis too);
+        scaling (FGMRES, JFNK): "state" divides equation v by the state's RMS magnitude of
+        variable v, "none" solves the rows as assembled.  Returns the ty_imp_stats fields as a dict."""
+        p = _capi.ImpParams(KRYLOV[inversion], PRECISION[precision], int(nkrylov), int(max_it), int(local_dt),
+                            {"state": 0, "none": 1}[scaling], float(inv_res), float(cfl))
         st = _capi.ImpStats()
         _capi.check(self.lib.ty_implicit_step(self.h, C.byref(p), C.byref(st)), "ty_implicit_step")
         return dict(info=st.info, restarts=st.restarts, matvecs=st.matvecs, dt_min=st.dt_min,
