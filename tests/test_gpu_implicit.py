@@ -311,10 +311,10 @@ def test_row_scaled_krylov_residual(ty, golden_dir, inversion, precision):
 
 def test_flat_plate_row_scaling_converges(ty):
     """Laminar flat plate (M 0.3, Re_L 1e4, 16,000 prisms + 24,000 tetrahedra, Rusanov with its
-    own Jacobian, cell-average viscous flux): with the row-scaled FGMRES, backward Euler at CFL
-    10 -> 100 falls below 1e-6 relative residual (every variable against its largest value) in
-    a few hundred steps; solved as assembled, the 2-norm is the energy equation's alone and the
-    Krylov solve stagnates near 1e-3."""
+    own Jacobian, cell-average viscous flux): with the row-scaled FGMRES(30) x 20, backward
+    Euler at CFL 10 -> 500 falls below 1e-6 relative residual (every variable against its
+    largest value) in a few dozen steps; solved as assembled, the 2-norm is the energy
+    equation's alone and the Krylov solve stagnates near 1e-3 already at CFL 100."""
     from typhon_gb300 import cases
     w = cases.FLATPLATE
     md = cases.make_flatplate(40, 4)
@@ -325,7 +325,7 @@ def test_flat_plate_row_scaling_converges(ty):
                rgas=w["rgas"], prandtl=w["prandtl"], farfield=ff)
     g.set_prim(np.tile(np.array(ff)[:, None], (1, md.ncell)))
     cfl, rmax, rel = w["cfl0"], None, 1.0
-    for step in range(1000):
+    for step in range(200):
         st = g.implicit_step(cfl, "FGMRES", nkrylov=w["nkrylov"], max_it=w["max_it"], inv_res=w["inv_res"],
                              local_dt=True)
         r = np.asarray(st["res_l2"]) / scale
