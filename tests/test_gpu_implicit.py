@@ -311,7 +311,7 @@ def test_row_scaled_krylov_residual(ty, golden_dir, inversion, precision):
 
 def test_flat_plate_row_scaling_converges(ty):
     """Laminar flat plate (M 0.3, Re_L 1e4, 16,000 prisms + 24,000 tetrahedra, Rusanov with its
-    own Jacobian, cell-average viscous flux): with the row-scaled FGMRES(30) x 20, backward
+    own Jacobian, cell-average viscous flux): with the row-scaled FGMRES(15) x 40, backward
     Euler at CFL 10 -> 500 falls below 1e-6 relative residual (every variable against its
     largest value) in a few dozen steps; solved as assembled, the 2-norm is the energy
     equation's alone and the Krylov solve stagnates near 1e-3 already at CFL 100."""
