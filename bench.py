@@ -525,7 +525,7 @@ def run_flatplate(args):
     decade both reach, and the residual each reached."""
     import torch
     import typhon_gb300 as ty
-    from typhon_gb300 import build, cases
+    from typhon_gb300 import _capi, build, cases
     build.build()
     torch.cuda.set_device(0)
     w = cases.FLATPLATE
@@ -548,9 +548,11 @@ def run_flatplate(args):
             g.set_prim(prim0)
             g.synchronize()
             cfl, rmax, steps, matvecs, rel = w["cfl0"], None, 0, 0, 1.0
-            decades = {}
+            decades, mid = {}, None
             t0 = time.perf_counter()
             while steps < w["max_steps"]:
+                if steps == 40:                       # the state profiled below (one host copy)
+                    mid = (g.get_cons(), cfl)
                 st = g.implicit_step(cfl, "FGMRES", **kw)
                 steps += 1
                 matvecs += st["matvecs"]
@@ -566,10 +568,26 @@ def run_flatplate(args):
                     break
                 cfl = min(cfl * 1.5, w["cfl_max"])
             g.synchronize()
+            seconds = time.perf_counter() - t0
             states[name] = g.get_cons()
-            variants[name] = {"seconds": round(time.perf_counter() - t0, 3), "steps": steps, "matvecs": matvecs,
+            variants[name] = {"seconds": round(seconds, 3), "steps": steps, "matvecs": matvecs,
                               "final_rel_residual": rel, "reached": bool(rel < w["target"]),
                               "decades": {f"1e-{k}": v for k, v in sorted(decades.items())}}
+            if mid is not None:                       # per-kernel device time of step 41 (CUDA events)
+                g.set_cons(mid[0])
+                nk = len(_capi.KERNEL_NAMES)
+                kms, kl = np.zeros(nk), np.zeros(nk, np.int32)
+                _capi.check(g.lib.ty_profile_enable(g.h, 1), "ty_profile_enable")
+                t1 = time.perf_counter()
+                st = g.implicit_step(mid[1], "FGMRES", **kw)
+                g.synchronize()
+                wall = time.perf_counter() - t1
+                _capi.check(g.lib.ty_profile_read(g.h, nk, kms.ctypes.data, kl.ctypes.data), "ty_profile_read")
+                _capi.check(g.lib.ty_profile_enable(g.h, 0), "ty_profile_enable")
+                variants[name]["profiled_step"] = {
+                    "step": 41, "cfl": mid[1], "matvecs": st["matvecs"], "wall_ms": round(wall * 1e3, 3),
+                    "kernels": {n: {"launches": int(kl[i]), "ms": round(float(kms[i]), 4)}
+                                for i, n in enumerate(_capi.KERNEL_NAMES) if kl[i] > 0}}
             g.close()
     d = states["fgmres_mixed"] - states["fgmres_fp64"]
     ref = states["fgmres_fp64"]
