@@ -1072,18 +1072,36 @@ unsigned basis_grid(size_t n) {
   return (unsigned)std::max<size_t>(1, std::min<size_t>(g, cap));
 }
 
+template <int J, class T>
+void basis_launch_j(T* V, size_t ldv, int nv, const double* c, const double* src, const double* sp, int extend,
+                    size_t n, double* part, unsigned* done, double* out, cudaStream_t st) {
+  k_basis_pass<J, T><<<basis_grid<J, T>(n), kCgsThreads, 0, st>>>(V, ldv, nv, c, src, sp, extend, n, part, done, out);
+}
+
+// The unrolled loops of a sweep run J slots per entry whatever nv is, so an FP64 sweep (bound
+// by the FP64 pipe) takes the smallest even J >= nv; an FP32 sweep (bound by HBM) takes 8, 16
+// or 32.
 template <class T>
 void basis_launch(T* V, size_t ldv, int nv, const double* c, const double* src, const double* sp, int extend,
                   size_t n, double* part, unsigned* done, double* out, cudaStream_t st) {
-  if (nv <= 8)
-    k_basis_pass<8, T><<<basis_grid<8, T>(n), kCgsThreads, 0, st>>>(V, ldv, nv, c, src, sp, extend, n, part, done,
-                                                                     out);
-  else if (nv <= 16)
-    k_basis_pass<16, T><<<basis_grid<16, T>(n), kCgsThreads, 0, st>>>(V, ldv, nv, c, src, sp, extend, n, part,
-                                                                       done, out);
-  else
-    k_basis_pass<kMaxCgs, T><<<basis_grid<kMaxCgs, T>(n), kCgsThreads, 0, st>>>(V, ldv, nv, c, src, sp, extend, n,
-                                                                                 part, done, out);
+  if constexpr (std::is_same<T, double>::value) {
+    switch ((nv + 1) / 2) {
+      case 0:
+      case 1: basis_launch_j<2>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st); return;
+      case 2: basis_launch_j<4>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st); return;
+      case 3: basis_launch_j<6>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st); return;
+      case 4: basis_launch_j<8>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st); return;
+      case 5: basis_launch_j<10>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st); return;
+      case 6: basis_launch_j<12>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st); return;
+      case 7: basis_launch_j<14>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st); return;
+      case 8: basis_launch_j<16>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st); return;
+      default: basis_launch_j<kMaxCgs>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st); return;
+    }
+  } else {
+    if (nv <= 8) basis_launch_j<8>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st);
+    else if (nv <= 16) basis_launch_j<16>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st);
+    else basis_launch_j<kMaxCgs>(V, ldv, nv, c, src, sp, extend, n, part, done, out, st);
+  }
 }
 
 cudaError_t imp_basis_pass(double* V, float* V32, size_t ldv, int nv, const double* c, const double* src,
