@@ -96,59 +96,53 @@ struct FaceKey {
   std::array<int, 4> v;
   bool operator==(const FaceKey& o) const { return v == o.v; }
 };
-struct FaceKeyHash {
-  size_t operator()(const FaceKey& k) const {
-    uint64_t h = 1469598103934665603ull;
-    for (int x : k.v) { h ^= (uint64_t)(uint32_t)x; h *= 1099511628211ull; }
-    return (size_t)(h ^ (h >> 29));
-  }
-};
 
-// Face lookup during face creation: open addressing with linear probing in flat arrays (a
-// node-based map spent most of the preprocessing time allocating).  nmax bounds the element
-// faces visited; each interior face is visited twice, so at most about nmax / 2 keys are
-// stored and a power-of-two capacity >= nmax keeps the load near one half or below.
-class FaceTable {
+// Face lookup during face creation: the faces are bucketed by their smallest vertex, each
+// bucket a contiguous run of slots sized beforehand from the element faces (each face is
+// visited at most twice, so a bucket never outgrows the count).  Neighbouring cells share
+// vertices, and vertices are numbered with the mesh, so the lookups of a sweep over the cells
+// stay in a few cache lines instead of hashing across the whole table.
+class FaceBuckets {
  public:
-  explicit FaceTable(size_t nmax) {
-    size_t cap = 16;
-    while (cap < nmax) cap <<= 1;
-    mask_ = cap - 1;
-    keys_.resize(cap);
-    vals_.assign(cap, -1);
+  // count[v]: element faces whose smallest vertex is v (vertices 1..nv)
+  explicit FaceBuckets(const std::vector<int>& count) : start_(count.size() + 1, 0), fill_(count.size(), 0) {
+    for (size_t v = 0; v < count.size(); ++v) start_[v + 1] = start_[v] + count[v];
+    slots_.resize(start_.back());
   }
   // the face id of key, or -1 after inserting key with id `fresh`
   int find_or_insert(const FaceKey& key, int fresh) {
-    size_t i = FaceKeyHash()(key) & mask_;
-    while (true) {
-      if (vals_[i] < 0) {
-        keys_[i] = key;
-        vals_[i] = fresh;
-        return -1;
-      }
-      if (keys_[i] == key) return vals_[i];
-      i = (i + 1) & mask_;
-    }
+    const int v = key.v[0];
+    Slot* b = slots_.data() + start_[v];
+    for (int i = 0; i < fill_[v]; ++i)
+      if (b[i].a == key.v[1] && b[i].b == key.v[2] && b[i].c == key.v[3]) return b[i].id;
+    b[fill_[v]++] = Slot{key.v[1], key.v[2], key.v[3], fresh};
+    return -1;
   }
   // the face id of key, or -1
   int find(const FaceKey& key) const {
-    size_t i = FaceKeyHash()(key) & mask_;
-    while (vals_[i] >= 0) {
-      if (keys_[i] == key) return vals_[i];
-      i = (i + 1) & mask_;
-    }
+    const int v = key.v[0];
+    if (v < 0 || v >= (int)fill_.size()) return -1;
+    const Slot* b = slots_.data() + start_[v];
+    for (int i = 0; i < fill_[v]; ++i)
+      if (b[i].a == key.v[1] && b[i].b == key.v[2] && b[i].c == key.v[3]) return b[i].id;
     return -1;
   }
   // every stored id f replaced by newidx[f]
   void remap(const std::vector<int>& newidx) {
-    for (int& v : vals_)
-      if (v >= 0) v = newidx[v];
+    for (size_t v = 0; v < fill_.size(); ++v)
+      for (int i = 0; i < fill_[v]; ++i) {
+        Slot& sl = slots_[start_[v] + i];
+        sl.id = newidx[sl.id];
+      }
   }
 
  private:
-  size_t mask_;
-  std::vector<FaceKey> keys_;
-  std::vector<int> vals_;
+  struct Slot {
+    int a, b, c, id;  // the other three sorted vertices (0 padded) and the face id
+  };
+  std::vector<size_t> start_;
+  std::vector<int> fill_;
+  std::vector<Slot> slots_;
 };
 FaceKey key_of(const int* f, int n) {
   FaceKey k;
@@ -169,7 +163,8 @@ struct ty_umesh {
   int dim = 0, ncell_int = 0, ncell = 0, nface_int = 0, nface = 0;
   std::vector<int32_t> facecell;          // [2*nface], 1-based, column-major
   std::vector<int32_t> facevtex;          // [4*nface], 1-based, 0 padded
-  std::vector<double> fnormal, fcentre, fsurf, ccentre, cvol, fwallvel;
+  std::vector<V3> fnormal, fcentre, ccentre;  // exported as [n][3] doubles (V3 holds three)
+  std::vector<double> fsurf, cvol, fwallvel;
   std::vector<int32_t> fcolor, fbc, fpartner, ffamily;
   std::vector<double> frot;               // [nface][9] rotation into each face's frame
   bool has_rot = false;
@@ -249,16 +244,48 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
     const int per = s.type == 13 ? 3 : s.type == 24 ? 4 : s.type == 101 ? 4 : s.type == 131 ? 5 : 6;
     nface_max += (size_t)per * s.ielem.size();
   }
-  FaceTable lookup(nface_max);
-  fv.reserve(4 * nface_max / 2 + 16);
-  fnv.reserve(nface_max / 2 + 4);
-  c1.reserve(nface_max / 2 + 4);
-  c2.reserve(nface_max / 2 + 4);
   static const int tri[3][2] = {{1, 2}, {2, 3}, {3, 1}};
   static const int quad[4][2] = {{1, 2}, {2, 3}, {3, 4}, {4, 1}};
   static const int tet[4][3] = {{1, 3, 2}, {1, 2, 4}, {2, 3, 4}, {3, 1, 4}};
   static const int hexa[6][4] = {{1, 2, 3, 4}, {1, 2, 6, 5}, {5, 6, 7, 8},
                                  {4, 3, 7, 8}, {1, 4, 8, 5}, {2, 3, 7, 6}};
+  static const int pr_t1[3] = {1, 2, 3}, pr_t2[3] = {4, 5, 6};
+  static const int pr_q1[4] = {1, 3, 6, 4}, pr_q2[4] = {1, 2, 5, 4}, pr_q3[4] = {2, 3, 6, 5};
+  // the faces of one element in creation order (create_facevtex.f90); fn(local vertices, n)
+  // returns false to stop
+  auto for_each_face = [&](int type, auto&& fn) -> int {  // 1 done, 0 stopped, -1 unknown type
+    switch (type) {
+      case 13: for (int k = 0; k < 3; ++k) if (!fn(tri[k], 2)) return 0; return 1;
+      case 24: for (int k = 0; k < 4; ++k) if (!fn(quad[k], 2)) return 0; return 1;
+      case 101: for (int k = 0; k < 4; ++k) if (!fn(tet[k], 3)) return 0; return 1;
+      case 131:
+        return (fn(pr_t1, 3) && fn(pr_t2, 3) && fn(pr_q1, 4) && fn(pr_q2, 4) && fn(pr_q3, 4)) ? 1 : 0;
+      case 141: for (int k = 0; k < 6; ++k) if (!fn(hexa[k], 4)) return 0; return 1;
+      default: return -1;
+    }
+  };
+  // bucket sizes: element faces per smallest vertex (faces with a vertex out of range are
+  // rejected in the creation pass below)
+  std::vector<int> per_vertex((size_t)nvtex + 1, 0);
+  for (auto& s : um->sections) {
+    if (elem_dim(s.type) != maxdim) continue;
+    const int nv = elem_nv(s.type);
+    for (size_t ic = 0; ic < s.ielem.size(); ++ic) {
+      const int* e = &s.vtex[ic * nv];
+      if (for_each_face(s.type, [&](const int* loc, int n) {
+            int m = e[loc[0] - 1];
+            for (int k = 1; k < n; ++k) m = std::min(m, e[loc[k] - 1]);
+            if (m >= 1 && m <= nvtex) ++per_vertex[m];
+            return true;
+          }) < 0)
+        return fail("unsupported element type");
+    }
+  }
+  FaceBuckets lookup(per_vertex);
+  fv.reserve(4 * nface_max / 2 + 16);
+  fnv.reserve(nface_max / 2 + 4);
+  c1.reserve(nface_max / 2 + 4);
+  c2.reserve(nface_max / 2 + 4);
   for (auto& s : um->sections) {
     if (elem_dim(s.type) != maxdim) continue;
     const int nv = elem_nv(s.type);
@@ -284,21 +311,9 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
         }
         return true;
       };
-      bool ok = true;
-      switch (s.type) {
-        case 13: for (int k = 0; k < 3 && ok; ++k) ok = create(tri[k], 2); break;
-        case 24: for (int k = 0; k < 4 && ok; ++k) ok = create(quad[k], 2); break;
-        case 101: for (int k = 0; k < 4 && ok; ++k) ok = create(tet[k], 3); break;
-        case 131: {
-          static const int t1[3] = {1, 2, 3}, t2[3] = {4, 5, 6};
-          static const int q1[4] = {1, 3, 6, 4}, q2[4] = {1, 2, 5, 4}, q3[4] = {2, 3, 6, 5};
-          ok = create(t1, 3) && create(t2, 3) && create(q1, 4) && create(q2, 4) && create(q3, 4);
-          break;
-        }
-        case 141: for (int k = 0; k < 6 && ok; ++k) ok = create(hexa[k], 4); break;
-        default: return fail("unsupported element type");
-      }
-      if (!ok) return fail("bad connectivity (vertex out of range or 3 cells on a face)");
+      const int r = for_each_face(s.type, create);
+      if (r < 0) return fail("unsupported element type");
+      if (r == 0) return fail("bad connectivity (vertex out of range or 3 cells on a face)");
     }
   }
   const int nface = (int)c1.size();
@@ -469,8 +484,12 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
 
   // ---- ghost cells: physical boundaries first, then periodic connections ----
   std::vector<int> fbc(nface, TY_BC_INTERIOR), fpart(nface, 0), ffam(nface, -1);
-  std::vector<double> frot(9 * (size_t)nface, 0.0);  // rotation into each face's frame (identity)
-  for (int f = 0; f < nface; ++f) frot[9 * (size_t)f] = frot[9 * (size_t)f + 4] = frot[9 * (size_t)f + 8] = 1.0;
+  // rotation into each face's frame (identity), stored only when a family is rotational
+  bool any_rot = false;
+  for (const auto& b : um->bcs) any_rot = any_rot || b.rot;
+  std::vector<double> frot(any_rot ? 9 * (size_t)nface : 0, 0.0);
+  if (any_rot)
+    for (int f = 0; f < nface; ++f) frot[9 * (size_t)f] = frot[9 * (size_t)f + 4] = frot[9 * (size_t)f + 8] = 1.0;
   std::vector<double> fwall(3 * (size_t)nface, 0.0);
   int nlim = 0;
   for (auto& b : bocos) {
@@ -588,24 +607,18 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
   um->facevtex.assign(FV.begin(), FV.end());
   for (int f = 0; f < nface; ++f)
     for (int k = FN[f]; k < 4; ++k) um->facevtex[4 * (size_t)f + k] = 0;
-  um->fnormal.resize(3 * (size_t)nface); um->fcentre.resize(3 * (size_t)nface); um->fsurf = fs;
-  for (int f = 0; f < nface; ++f) {
-    um->fnormal[3 * (size_t)f] = fn[f].x; um->fnormal[3 * (size_t)f + 1] = fn[f].y; um->fnormal[3 * (size_t)f + 2] = fn[f].z;
-    um->fcentre[3 * (size_t)f] = fc[f].x; um->fcentre[3 * (size_t)f + 1] = fc[f].y; um->fcentre[3 * (size_t)f + 2] = fc[f].z;
-  }
-  um->ccentre.resize(3 * (size_t)ncell);
-  for (int c = 0; c < ncell; ++c) {
-    um->ccentre[3 * (size_t)c] = cc[c].x; um->ccentre[3 * (size_t)c + 1] = cc[c].y; um->ccentre[3 * (size_t)c + 2] = cc[c].z;
-  }
-  um->cvol = cv;
-  um->fcolor = color;
-  um->fbc = fbc;
-  um->fpartner = fpart;
-  um->fwallvel = fwall;
-  um->ffamily = ffam;
-  um->frot = frot;
-  um->has_rot = false;
-  for (const auto& b : um->bcs) um->has_rot = um->has_rot || b.rot;
+  um->fnormal = std::move(fn);
+  um->fcentre = std::move(fc);
+  um->ccentre = std::move(cc);
+  um->fsurf = std::move(fs);
+  um->cvol = std::move(cv);
+  um->fcolor = std::move(color);
+  um->fbc = std::move(fbc);
+  um->fpartner = std::move(fpart);
+  um->fwallvel = std::move(fwall);
+  um->ffamily = std::move(ffam);
+  um->frot = std::move(frot);
+  um->has_rot = any_rot;
   um->built = true;
   return TY_OK;
 }
@@ -616,10 +629,11 @@ int ty_umesh_desc(const ty_umesh* um, ty_mesh_desc* d) {
   d->ncell_int = um->ncell_int; d->ncell = um->ncell;
   d->nface_int = um->nface_int; d->nface = um->nface;
   d->facecell = um->facecell.data();
-  d->face_normal = um->fnormal.data();
+  static_assert(sizeof(V3) == 3 * sizeof(double), "V3 must be three packed doubles");
+  d->face_normal = reinterpret_cast<const double*>(um->fnormal.data());
   d->face_surface = um->fsurf.data();
-  d->face_centre = um->fcentre.data();
-  d->cell_centre = um->ccentre.data();
+  d->face_centre = reinterpret_cast<const double*>(um->fcentre.data());
+  d->cell_centre = reinterpret_cast<const double*>(um->ccentre.data());
   d->cell_volume = um->cvol.data();
   d->face_color = um->fcolor.data();
   d->face_bc = um->fbc.data();
@@ -648,8 +662,13 @@ int ty_umesh_set_rotation(ty_umesh* um, const char* family, const double* centre
 
 int ty_umesh_face_rotation(const ty_umesh* um, double* out) {
   if (!um || !out || !um->built) return TY_ERR_STATE;
+  if (!um->has_rot) {  // the identity everywhere
+    for (int f = 0; f < um->nface; ++f)
+      for (int q = 0; q < 9; ++q) out[9 * (size_t)f + q] = (q % 4 == 0) ? 1.0 : 0.0;
+    return 0;
+  }
   std::memcpy(out, um->frot.data(), um->frot.size() * sizeof(double));
-  return um->has_rot ? 1 : 0;
+  return 1;
 }
 
 int ty_umesh_face_family(const ty_umesh* um, int32_t* out) {

@@ -566,11 +566,12 @@ def preprocess(raw: RawMesh, dim, bcs, rotations=None) -> MeshDesc:
         ff = np.zeros(d.nface, np.int32)
         _capi.check(L.ty_umesh_face_family(h, ff.ctypes.data), "ty_umesh_face_family")
         md = MeshDesc(d, fv.reshape(d.nface, 4), ff, [b[0].upper() for b in bcs])
-        rot = np.zeros(9 * d.nface)
-        rc = L.ty_umesh_face_rotation(h, rot.ctypes.data)
-        _capi.check(min(rc, 0), "ty_umesh_face_rotation")
-        if rc == 1:
-            md.face_rotation = rot.reshape(d.nface, 3, 3)
+        if rotations:                                 # [nface][3][3] only when a family rotates
+            rot = np.zeros(9 * d.nface)
+            rc = L.ty_umesh_face_rotation(h, rot.ctypes.data)
+            _capi.check(min(rc, 0), "ty_umesh_face_rotation")
+            if rc == 1:
+                md.face_rotation = rot.reshape(d.nface, 3, 3)
         return md
     finally:
         L.ty_umesh_free(h)
