@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -463,7 +464,25 @@ int ty_umesh_build(ty_umesh* um, int32_t dim) {
 
   // ---- greedy colouring: the first colour free at both cells (boundary: one cell) ----
   std::vector<int> color(nface);
-  {
+  bool coloured = false;
+  {  // colours of each cell as a bit mask (the first free colour is the lowest clear bit)
+    std::vector<uint64_t> used(ncell, 0);
+    int ncolor = 0;
+    coloured = true;
+    for (int f = 0; f < nface && coloured; ++f) {
+      const int a = F1[f] - 1;
+      const int b = (F2[f] == 0 || F2[f] > ncell) ? a : F2[f] - 1;
+      const uint64_t u = used[a] | used[b];
+      int chosen = 0;
+      while (chosen < ncolor && ((u >> chosen) & 1u)) ++chosen;
+      if (chosen == ncolor) ++ncolor;
+      if (ncolor > 64) { coloured = false; break; }  // more colours than bits: the general form
+      color[f] = chosen;
+      used[a] |= 1ull << chosen;
+      used[b] |= 1ull << chosen;
+    }
+  }
+  if (!coloured) {
     std::vector<std::vector<int>> vcol(ncell);
     int ncolor = 0;
     for (int f = 0; f < nface; ++f) {
