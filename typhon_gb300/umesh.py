@@ -277,8 +277,11 @@ def gen_tet_box(n, length, jitter=0.0, seed=1234):
         conn[:, t, :] = np.where(even, v[:, list(tets_even[t])], v[:, list(tets_odd[t])])
     conn = conn.reshape(-1, 4)
     # boundary triangles: the element faces whose three nodes lie on one face of the box (the
-    # faces seen once), in element-face order
-    fl = np.concatenate([conn[:, [0, 2, 1]], conn[:, [0, 1, 3]], conn[:, [1, 2, 3]], conn[:, [2, 0, 3]]])
+    # faces seen once), in element-face order; only the tetrahedra of the outer hexahedron
+    # layer can own one
+    layer = ((I == 0) | (I == n - 1) | (J == 0) | (J == n - 1) | (K == 0) | (K == n - 1))
+    outer = conn[np.repeat(layer, 5)]
+    fl = np.concatenate([outer[:, [0, 2, 1]], outer[:, [0, 1, 3]], outer[:, [1, 2, 3]], outer[:, [2, 0, 3]]])
     ijk = np.unravel_index(fl - 1, (n + 1, n + 1, n + 1))
     on = np.zeros(len(fl), bool)
     for a in range(3):
@@ -362,9 +365,12 @@ def gen_flatplate(nx=200, nz=20, n_prism=50, n_tet=25, x0=-0.5, x1=1.0, width=0.
     alltri = np.concatenate([ptri, ttri])
 
     def once(f):
-        key = np.sort(f, axis=1)
-        _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
-        return f[cnt[inv.reshape(-1)] == 1]
+        # on a box the faces seen once are those whose nodes all lie on one of its six planes
+        ijk = np.unravel_index(f - 1, (nx + 1, ny + 1, nz + 1))
+        on = np.zeros(len(f), bool)
+        for a, top_index in enumerate((nx, ny, nz)):
+            on |= (ijk[a] == 0).all(axis=1) | (ijk[a] == top_index).all(axis=1)
+        return f[on]
 
     btri, bquad = once(alltri), once(pquad)
     top = y[-1]
@@ -425,9 +431,12 @@ def gen_kuhn_box(n, length=1.0):
     a, b, c, d = (vt[tets[:, q] - 1] for q in range(4))
     neg = np.einsum("ij,ij->i", np.cross(b - a, c - a), d - a) < 0
     tets[neg, 1], tets[neg, 2] = tets[neg, 2].copy(), tets[neg, 1].copy()
-    fl = np.concatenate([tets[:, [0, 2, 1]], tets[:, [0, 1, 3]], tets[:, [1, 2, 3]], tets[:, [2, 0, 3]]])
     # boundary triangles: the element faces whose three nodes lie on one face of the box (the
-    # faces seen once), in element-face order
+    # faces seen once), in element-face order; only the tetrahedra of the outer hexahedron
+    # layer can own one
+    layer = ((I == 0) | (I == n - 1) | (J == 0) | (J == n - 1) | (K == 0) | (K == n - 1))
+    outer = tets[np.repeat(layer, 6)]
+    fl = np.concatenate([outer[:, [0, 2, 1]], outer[:, [0, 1, 3]], outer[:, [1, 2, 3]], outer[:, [2, 0, 3]]])
     ijk = np.unravel_index(fl - 1, (n + 1, n + 1, n + 1))
     on = np.zeros(len(fl), bool)
     for a in range(3):
