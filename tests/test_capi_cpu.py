@@ -139,3 +139,38 @@ def test_bad_mesh_is_rejected(ty):
     raw = ty.gen_grid2d(4, 4, 1.0, 1.0, "quad")
     with pytest.raises(ty.TyphonError):
         ty.preprocess(raw, 2, [("IMIN", 1, "IMAX", (1.0, 0, 0))])   # JMIN/JMAX undefined
+
+
+def _faces_seen_once(sections):
+    """Reference definition of the boundary: the element faces that belong to one element only."""
+    from collections import Counter
+    from typhon_gb300 import umesh
+    local = {umesh.ELEM_TETRA4: [(0, 2, 1), (0, 1, 3), (1, 2, 3), (2, 0, 3)],
+             umesh.ELEM_PENTA6: [(0, 1, 2), (3, 4, 5), (0, 2, 5, 3), (0, 1, 4, 3), (1, 2, 5, 4)]}
+    cnt = Counter()
+    for typ, _, conn in sections:
+        for loc in local[typ]:
+            for row in conn[:, list(loc)]:
+                cnt[tuple(sorted(row))] += 1
+    return {k for k, v in cnt.items() if v == 1}
+
+
+@pytest.mark.parametrize("kind", ["tet", "kuhn", "plate"])
+def test_generator_boundary_is_faces_seen_once(ty, kind):
+    """The generators find their boundary triangles and quadrilaterals by a plane test on the
+    box's grid indices; every boundary face is an element face seen once, and every element
+    face seen once is marked exactly once."""
+    if kind == "tet":
+        raw = ty.umesh.gen_tet_box(4, 1.0, jitter=0.05, seed=3)
+    elif kind == "kuhn":
+        raw = ty.umesh.gen_kuhn_box(3, 1.0)
+    else:
+        raw = ty.umesh.gen_flatplate(nx=6, nz=2, n_prism=3, n_tet=2)
+    cell_types = (ty.umesh.ELEM_TETRA4, ty.umesh.ELEM_PENTA6)
+    cells = [s for s in raw.sections if s[0] in cell_types]
+    faces = [s for s in raw.sections if s[0] not in cell_types]
+    bnd = [tuple(sorted(r)) for _, _, conn in faces for r in conn]
+    assert len(bnd) == len(set(bnd))
+    assert set(bnd) == _faces_seen_once(cells)
+    marked = np.sort(np.concatenate([m[1] for m in raw.marks]))
+    assert np.array_equal(marked, np.arange(1, len(bnd) + 1))
