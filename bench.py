@@ -95,6 +95,24 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device):
+    """The largest x over the ranks of the process group (the job's time is its slowest
+    rank's); x itself for one rank."""
+    if world == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, world, seconds):
+    """Whole-job rate of N replicas that each process units_per_rank in `seconds` (the
+    max-over-ranks time): every rank's units over the slowest rank's time."""
+    return units_per_rank * world / seconds
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every `interval_ms` while running.  Entering
     waits (up to 5 s) for the first sample, so that sampling is under way when the measured work
@@ -282,12 +300,8 @@ def run_ours(args, rank, world, local):
     kl = np.zeros(nk, np.int32)
     _capi.check(g.lib.ty_profile_read(g.h, nk, kms.ctypes.data, kl.ctypes.data), "ty_profile_read")
     _capi.check(g.lib.ty_profile_enable(g.h, 0), "ty_profile_enable")
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = nci * args.steps * world / (ms * 1e-3)
+    ms = max_over_ranks(ms, world, "cuda")
+    value = job_throughput(nci * args.steps, world, ms * 1e-3)
     # per-kernel roofline
     peak, peak_kind = measured_peaks()
     mtab = (args.mode == "fast" and w["highres"] in ("MUSCL", "MUSCL-UNS") and w["limiter"] == "NONE"
@@ -339,12 +353,8 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize(local)
     t_e2e = time.perf_counter() - t0
     barrier()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e = {"value": nci * e2e_steps * world / t_e2e, "unit": "cell-updates/s",
+    t_e2e = max_over_ranks(t_e2e, world, "cuda")
+    e2e = {"value": job_throughput(nci * e2e_steps, world, t_e2e), "unit": "cell-updates/s",
            "h2d_bytes_per_step": 40 * nci, "d2h_bytes_per_step": 40 * nci, "steps": e2e_steps}
     # the exact mode (bit-identical to the oracle) on the same grid and state, device time
     exact = None
