@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="tgv3d", choices=["tgv3d", "vortex2d", "ffbox3d-implicit", "kdif3d", "adjoint3d",
                                                              "flatplate-implicit"])
+    ap.add_argument("--cell-order", default="given", choices=["given", "shuffled", "shuffled-rcm"],
+                    help="tgv3d / vortex2d: the generator's cell numbering, a random one, or a random one "
+                         "renumbered in reverse Cuthill-McKee order")
     ap.add_argument("--fp-nx", type=int, default=None, help="flatplate-implicit: streamwise quads (default 200)")
     ap.add_argument("--fp-nz", type=int, default=None, help="flatplate-implicit: spanwise quads (default 20)")
     ap.add_argument("--imp-time-limit", type=float, default=900.0,
@@ -257,7 +260,7 @@ def run_ours(args, rank, world, local):
     w = cases.WORKLOADS[args.workload]
     n = args.n or w["n"]
     t0 = time.time()
-    md = cases.make_mesh(args.workload, n)
+    md = cases.make_mesh(args.workload, n, args.cell_order)
     t_mesh = time.time() - t0
     prim = cases.initial_prim(args.workload, md.cell_centre)
     g = ty.Grid(md, device=local)
@@ -395,10 +398,13 @@ def workload_config(args, cells, faces, world):
     w = cases.WORKLOADS[args.workload]
     n = args.n or w["n"]
     name = {"tgv3d": f"tgv3d {n}^3x5 tets", "vortex2d": f"vortex2d {n}x{n}x2 tris"}[args.workload]
-    return {"workload": name, "cells": int(cells), "faces": int(faces), "scheme": w["scheme"],
-            "highres": w["highres"], "limiter": w["limiter"], "postlim": w["postlim"], "rk": w["rk"],
-            "cfl": w["cfl"], "mode": args.mode, "parallelism": f"replicas{world}",
-            "l2": "working set larger than L2 (no flush needed)"}
+    out = {"workload": name, "cells": int(cells), "faces": int(faces), "scheme": w["scheme"],
+           "highres": w["highres"], "limiter": w["limiter"], "postlim": w["postlim"], "rk": w["rk"],
+           "cfl": w["cfl"], "mode": args.mode, "parallelism": f"replicas{world}",
+           "l2": "working set larger than L2 (no flush needed)"}
+    if args.cell_order != "given":
+        out["cell_order"] = args.cell_order
+    return out
 
 
 def cpu_sample(args, n_steps, warmup=1, with_mesh=False):
@@ -409,7 +415,7 @@ def cpu_sample(args, n_steps, warmup=1, with_mesh=False):
     from typhon_gb300 import cases
     w = cases.WORKLOADS[args.workload]
     n = args.n or w["n"]
-    raw = cases.make_raw(args.workload, n)
+    raw = cases.make_raw(args.workload, n, args.cell_order)
     from typhon_gb300 import umesh
     om = op.Mesh.from_raw(raw).build(w["dim"], umesh.periodic_box_bcs((w["length"],) * w["dim"]))
     sch = {"HLLC": op.SCH_HLLC, "RUSANOV": op.SCH_RUSANOV, "ROE": op.SCH_ROE}[w["scheme"]]

@@ -482,6 +482,13 @@ int ty_umesh_build(ty_umesh* um, int32_t dim);
 int ty_umesh_desc(const ty_umesh* um, ty_mesh_desc* out);
 /* Face -> vertex lists of the built mesh: [nface*4] 1-based, 0 padded. */
 int ty_umesh_facevtex(const ty_umesh* um, int32_t* out);
+/* Reverse Cuthill-McKee order of the cells of each cell section (new; the benchmark spec's RCM
+ * numbering for locality, Typhon keeps the file's order): out [ncell_int], for every cell
+ * section in ty_umesh_add_section order, the 0-based positions of its elements in their new
+ * order, computed on the cells the section's interior faces connect.  Rebuilding the mesh
+ * with each section's element rows taken in this order (element numbers kept in place)
+ * numbers neighbouring cells, and so the faces created from them, close together. */
+int ty_umesh_rcm_order(const ty_umesh* um, int32_t* out);
 /* Boundary definition of each face [nface]: the index (0-based, in ty_umesh_add_bc order)
  * of the definition its family matched, -1 for interior faces.  Lets a caller give per-face
  * values (KDIF wall kinds and temperatures, ...) by family. */

@@ -174,3 +174,45 @@ def test_generator_boundary_is_faces_seen_once(ty, kind):
     assert set(bnd) == _faces_seen_once(cells)
     marked = np.sort(np.concatenate([m[1] for m in raw.marks]))
     assert np.array_equal(marked, np.arange(1, len(bnd) + 1))
+
+
+def _neighbour_spread(md):
+    nfi = md.nface_int
+    c1, c2 = md.fc1[:nfi], md.fc2[:nfi]
+    inner = c2 < md.ncell_int
+    return float(np.abs(c1[inner] - c2[inner]).mean())
+
+
+def test_rcm_order_restores_locality_and_keeps_oracle_parity(ty):
+    """A tet box with its cells shuffled, renumbered in reverse Cuthill-McKee order: the mean
+    index distance between face neighbours falls back to that of the generator's numbering,
+    the cells are the same (a permutation of the element rows, element numbers in place), and
+    the native preprocessing of the renumbered mesh is still the oracle's bit for bit."""
+    from typhon_gb300 import cases
+    L = 2 * np.pi
+    raw = ty.gen_tet_box(10, L, jitter=0.05, seed=1234)
+    bcs = ty.periodic_box_bcs((L, L, L))
+    mixed = cases.shuffle_cells(raw, seed=3)
+    rcm = ty.reorder_rcm(mixed, 3, bcs)
+    (t0, ie0, c0), (t1, ie1, c1) = mixed.sections[0], rcm.sections[0]
+    assert t0 == t1 and np.array_equal(ie0, ie1)
+    assert sorted(map(tuple, np.sort(c0, axis=1))) == sorted(map(tuple, np.sort(c1, axis=1)))
+    md_mixed, md_rcm, md_gen = (ty.preprocess(r, 3, bcs) for r in (mixed, rcm, raw))
+    assert _neighbour_spread(md_rcm) < 0.1 * _neighbour_spread(md_mixed)
+    assert _neighbour_spread(md_rcm) < 2.0 * _neighbour_spread(md_gen)
+    assert abs(md_rcm.cell_volume[:md_rcm.ncell_int].sum() - L ** 3) < 1e-9 * L ** 3
+    d = op.Mesh.from_raw(rcm).build(3, bcs).export()
+    assert all(_same(md_rcm, d).values()), _same(md_rcm, d)
+
+
+def test_rcm_order_per_section(ty):
+    """Prisms and tetrahedra are renumbered within their own sections."""
+    raw = ty.umesh.gen_flatplate(nx=8, nz=2, n_prism=3, n_tet=2)
+    bcs = ty.umesh.flatplate_bcs()
+    rcm = ty.reorder_rcm(raw, 3, bcs)
+    for (ta, ia, ca), (tb, ib, cb) in zip(raw.sections, rcm.sections):
+        assert ta == tb and np.array_equal(ia, ib)
+        assert sorted(map(tuple, np.sort(ca, axis=1))) == sorted(map(tuple, np.sort(cb, axis=1)))
+    md = ty.preprocess(rcm, 3, bcs)
+    d = op.Mesh.from_raw(rcm).build(3, bcs).export()
+    assert all(_same(md, d).values()), _same(md, d)

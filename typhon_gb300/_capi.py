@@ -134,6 +134,7 @@ _SIGS = {
     "ty_umesh_build": ([C.c_void_p, C.c_int32], C.c_int),
     "ty_umesh_desc": ([C.c_void_p, C.POINTER(MeshDesc)], C.c_int),
     "ty_umesh_facevtex": ([C.c_void_p, C.c_void_p], C.c_int),
+    "ty_umesh_rcm_order": ([C.c_void_p, C.c_void_p], C.c_int),
 }
 
 

@@ -150,18 +150,39 @@ WORKLOADS = {
 }
 
 
-def make_raw(name, n=None):
+def shuffle_cells(raw, seed=1):
+    """The same mesh with the element rows of each cell section in a random order (seeded):
+    a stand-in for a mesh file whose numbering scatters neighbouring cells."""
+    rng = np.random.default_rng(seed)
+    dmax = max(umesh.DIM[t] for t, _, _ in raw.sections)
+    secs = [(t, ie, conn[rng.permutation(len(ie))] if umesh.DIM[t] == dmax else conn) for t, ie, conn in raw.sections]
+    return umesh.RawMesh(vtex=raw.vtex, sections=secs, marks=list(raw.marks))
+
+
+def make_raw(name, n=None, cell_order="given"):
+    """Element mesh of a workload.  cell_order: "given" (the generator's numbering),
+    "shuffled" (rows of the cell section permuted at random), "shuffled-rcm" (shuffled,
+    then renumbered in reverse Cuthill-McKee order)."""
     w = WORKLOADS[name]
     n = n or w["n"]
     if w["dim"] == 2:
-        return umesh.gen_grid2d(n, n, w["length"], w["length"], "tri", jitter=w["jitter"], seed=w["seed"])
-    return umesh.gen_tet_box(n, w["length"], jitter=w["jitter"], seed=w["seed"])
+        raw = umesh.gen_grid2d(n, n, w["length"], w["length"], "tri", jitter=w["jitter"], seed=w["seed"])
+    else:
+        raw = umesh.gen_tet_box(n, w["length"], jitter=w["jitter"], seed=w["seed"])
+    if cell_order == "given":
+        return raw
+    raw = shuffle_cells(raw)
+    if cell_order == "shuffled":
+        return raw
+    if cell_order == "shuffled-rcm":
+        return umesh.reorder_rcm(raw, w["dim"], umesh.periodic_box_bcs((w["length"],) * w["dim"]))
+    raise ValueError(f"cell_order {cell_order!r}")
 
 
-def make_mesh(name, n=None):
+def make_mesh(name, n=None, cell_order="given"):
     """Preprocessed mesh of a workload (native preprocessing)."""
     w = WORKLOADS[name]
-    raw = make_raw(name, n)
+    raw = make_raw(name, n, cell_order)
     return umesh.preprocess(raw, w["dim"], umesh.periodic_box_bcs((w["length"],) * w["dim"]))
 
 

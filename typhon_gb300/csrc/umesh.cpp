@@ -696,6 +696,99 @@ int ty_umesh_face_family(const ty_umesh* um, int32_t* out) {
   return TY_OK;
 }
 
+int ty_umesh_rcm_order(const ty_umesh* um, int32_t* order) {
+  if (!um || !order || !um->built) return TY_ERR_STATE;
+  int maxdim = 0;
+  for (auto& s : um->sections) maxdim = std::max(maxdim, elem_dim(s.type));
+  const int nci = um->ncell_int, nface = um->nface;
+  // section and position of every cell
+  std::vector<int> sec_of((size_t)nci + 1, -1), pos_of((size_t)nci + 1, -1);
+  for (size_t si = 0; si < um->sections.size(); ++si) {
+    const Section& s = um->sections[si];
+    if (elem_dim(s.type) != maxdim) continue;
+    for (size_t p = 0; p < s.ielem.size(); ++p) {
+      const int id = s.ielem[p];
+      if (id < 1 || id > nci) return TY_ERR_MESH;
+      sec_of[id] = (int)si;
+      pos_of[id] = (int)p;
+    }
+  }
+  size_t off = 0;
+  for (size_t si = 0; si < um->sections.size(); ++si) {
+    const Section& s = um->sections[si];
+    if (elem_dim(s.type) != maxdim) continue;
+    const int m = (int)s.ielem.size();
+    // adjacency of the section's cells through interior faces (CSR over positions)
+    std::vector<int> deg(m, 0);
+    for (int f = 0; f < nface; ++f) {
+      const int a = um->facecell[f], b = um->facecell[nface + f];
+      if (b < 1 || b > nci || a < 1 || a > nci) continue;
+      if (sec_of[a] != (int)si || sec_of[b] != (int)si) continue;
+      ++deg[pos_of[a]];
+      ++deg[pos_of[b]];
+    }
+    std::vector<size_t> xadj((size_t)m + 1, 0);
+    for (int p = 0; p < m; ++p) xadj[p + 1] = xadj[p] + deg[p];
+    std::vector<int> adj(xadj[m]), fill(m, 0);
+    for (int f = 0; f < nface; ++f) {
+      const int a = um->facecell[f], b = um->facecell[nface + f];
+      if (b < 1 || b > nci || a < 1 || a > nci) continue;
+      if (sec_of[a] != (int)si || sec_of[b] != (int)si) continue;
+      const int pa = pos_of[a], pb = pos_of[b];
+      adj[xadj[pa] + fill[pa]++] = pb;
+      adj[xadj[pb] + fill[pb]++] = pa;
+    }
+    // Cuthill-McKee from a pseudo-peripheral cell of each connected component (the
+    // lowest-degree cell of the last level of a breadth-first search from the lowest-degree
+    // unvisited cell), neighbours in increasing degree; then the whole order reversed
+    std::vector<int> by_deg(m);
+    for (int p = 0; p < m; ++p) by_deg[p] = p;
+    std::stable_sort(by_deg.begin(), by_deg.end(), [&](int x, int y) { return deg[x] < deg[y]; });
+    std::vector<char> seen(m, 0);
+    std::vector<int> cm, level, mark(m, -1), nb;
+    cm.reserve(m);
+    size_t next_start = 0;
+    int stamp = 0;
+    while ((int)cm.size() < m) {
+      while (seen[by_deg[next_start]]) ++next_start;
+      int start = by_deg[next_start];
+      // one breadth-first search to move the start to the far side of its component
+      {
+        ++stamp;
+        level.assign(1, start);
+        mark[start] = stamp;
+        std::vector<int> last = level;
+        while (!level.empty()) {
+          last = level;
+          std::vector<int> nxt;
+          for (int u : level)
+            for (size_t k = xadj[u]; k < xadj[u + 1]; ++k) {
+              const int w = adj[k];
+              if (mark[w] != stamp && !seen[w]) { mark[w] = stamp; nxt.push_back(w); }
+            }
+          level.swap(nxt);
+        }
+        for (int u : last)
+          if (deg[u] < deg[start] || (deg[u] == deg[start] && u < start)) start = u;
+      }
+      size_t head = cm.size();
+      cm.push_back(start);
+      seen[start] = 1;
+      while (head < cm.size()) {
+        const int u = cm[head++];
+        nb.clear();
+        for (size_t k = xadj[u]; k < xadj[u + 1]; ++k)
+          if (!seen[adj[k]]) { seen[adj[k]] = 1; nb.push_back(adj[k]); }
+        std::stable_sort(nb.begin(), nb.end(), [&](int x, int y) { return deg[x] < deg[y]; });
+        cm.insert(cm.end(), nb.begin(), nb.end());
+      }
+    }
+    for (int k = 0; k < m; ++k) order[off + k] = cm[m - 1 - k];
+    off += m;
+  }
+  return TY_OK;
+}
+
 int ty_umesh_facevtex(const ty_umesh* um, int32_t* out) {
   if (!um || !out || !um->built) return TY_ERR_STATE;
   std::memcpy(out, um->facevtex.data(), um->facevtex.size() * sizeof(int32_t));

@@ -532,14 +532,8 @@ class MeshDesc:
         return d
 
 
-def preprocess(raw: RawMesh, dim, bcs, rotations=None) -> MeshDesc:
-    """Native preprocessing (ty_umesh_*): faces, geometry, colours, ghosts, periodicity.
-
-    bcs: [(family, kind, partner, translation(3)[, wall_velocity(3)])]
-    rotations: {family: (centre(3), axis(3), angle in degrees)} for periodic families that
-    are connected to their partner by a rotation (BLOCK:PERIODICITY TYPE = ROTATION)
-    """
-    L = _capi.lib()
+def _umesh_built(L, raw: RawMesh, dim, bcs, rotations):
+    """A ty_umesh handle holding raw, bcs and rotations, built (the caller frees it)."""
     h = C.c_void_p()
     _capi.check(L.ty_umesh_new(C.byref(h)), "ty_umesh_new")
     try:
@@ -568,6 +562,22 @@ def preprocess(raw: RawMesh, dim, bcs, rotations=None) -> MeshDesc:
             _capi.check(L.ty_umesh_set_rotation(h, fam.encode(), c3.ctypes.data, a3.ctypes.data, float(ang)),
                         "ty_umesh_set_rotation")
         _capi.check(L.ty_umesh_build(h, int(dim)), "ty_umesh_build")
+    except BaseException:
+        L.ty_umesh_free(h)
+        raise
+    return h
+
+
+def preprocess(raw: RawMesh, dim, bcs, rotations=None) -> MeshDesc:
+    """Native preprocessing (ty_umesh_*): faces, geometry, colours, ghosts, periodicity.
+
+    bcs: [(family, kind, partner, translation(3)[, wall_velocity(3)])]
+    rotations: {family: (centre(3), axis(3), angle in degrees)} for periodic families that
+    are connected to their partner by a rotation (BLOCK:PERIODICITY TYPE = ROTATION)
+    """
+    L = _capi.lib()
+    h = _umesh_built(L, raw, dim, bcs, rotations)
+    try:
         d = _capi.MeshDesc()
         _capi.check(L.ty_umesh_desc(h, C.byref(d)), "ty_umesh_desc")
         fv = np.zeros(4 * d.nface, np.int32)
@@ -584,3 +594,28 @@ def preprocess(raw: RawMesh, dim, bcs, rotations=None) -> MeshDesc:
         return md
     finally:
         L.ty_umesh_free(h)
+
+
+def reorder_rcm(raw: RawMesh, dim, bcs, rotations=None) -> RawMesh:
+    """The same mesh with the element rows of each cell section in reverse Cuthill-McKee
+    order (ty_umesh_rcm_order; element numbers, nodes and boundary marks unchanged), so that
+    preprocessing it numbers neighbouring cells, and the faces made from them, close together.
+    Typhon keeps the file's order; this is the locality renumbering applied before
+    preprocessing, for meshes whose native numbering scatters neighbours."""
+    L = _capi.lib()
+    h = _umesh_built(L, raw, dim, bcs, rotations)
+    try:
+        order = np.zeros(raw.ncell, np.int32)
+        _capi.check(L.ty_umesh_rcm_order(h, order.ctypes.data), "ty_umesh_rcm_order")
+    finally:
+        L.ty_umesh_free(h)
+    dmax = max(DIM[t] for t, _, _ in raw.sections)
+    secs, off = [], 0
+    for typ, ielem, conn in raw.sections:
+        if DIM[typ] == dmax:
+            m = len(ielem)
+            secs.append((typ, np.asarray(ielem, np.int32).copy(), np.ascontiguousarray(conn[order[off:off + m]])))
+            off += m
+        else:
+            secs.append((typ, ielem, conn))
+    return RawMesh(vtex=raw.vtex, sections=secs, marks=list(raw.marks))
