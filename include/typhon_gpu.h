@@ -482,8 +482,8 @@ int ty_umesh_build(ty_umesh* um, int32_t dim);
 int ty_umesh_desc(const ty_umesh* um, ty_mesh_desc* out);
 /* Face -> vertex lists of the built mesh: [nface*4] 1-based, 0 padded. */
 int ty_umesh_facevtex(const ty_umesh* um, int32_t* out);
-/* Reverse Cuthill-McKee order of the cells of each cell section (new; the benchmark spec's RCM
- * numbering for locality, Typhon keeps the file's order): out [ncell_int], for every cell
+/* Reverse Cuthill-McKee order of the cells of each cell section (new: a numbering for
+ * locality; Typhon keeps the file's order): out [ncell_int], for every cell
  * section in ty_umesh_add_section order, the 0-based positions of its elements in their new
  * order, computed on the cells the section's interior faces connect.  Rebuilding the mesh
  * with each section's element rows taken in this order (element numbers kept in place)
