@@ -145,11 +145,15 @@ class FaceBuckets {
   std::vector<int> fill_;
   std::vector<Slot> slots_;
 };
+// the n (2..4) vertices of a face in increasing order, zero padded
 FaceKey key_of(const int* f, int n) {
   FaceKey k;
   k.v = {0, 0, 0, 0};
-  for (int i = 0; i < n; ++i) k.v[i] = f[i];
-  std::sort(k.v.begin(), k.v.begin() + n);
+  for (int i = 0; i < n && i < 4; ++i) {  // insertion sort of at most four entries
+    int x = f[i], j = i;
+    for (; j > 0 && k.v[j - 1] > x; --j) k.v[j] = k.v[j - 1];
+    k.v[j] = x;
+  }
   return k;
 }
 
